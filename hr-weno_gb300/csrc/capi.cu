@@ -1,0 +1,501 @@
+// capi.cu - the C ABI (include/hrweno_gpu.h): handles, validation with the reference's
+// messages, and the host time loops that reproduce the reference's step sequence exactly.
+//
+//   weno_init            src/hrweno_weno.f90:54-127
+//   rktvd_init/integrate src/hrweno_tvdode.f90:69-178
+//   mstvd_init/integrate src/hrweno_tvdode.f90:180-271
+//   is_done              src/hrweno_tvdode.f90:273-284
+//
+// The time t stays on the host in FP64 and is advanced by the same `t = t + dt` sequence as
+// the reference, so the step count of every integrate call is known before the first launch;
+// the kernels themselves do not depend on t (every flux of the problem descriptor is
+// autonomous).
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/hrweno_gpu.h"
+#include "hrw_internal.h"
+
+using namespace hrw;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+
+#define HRW_CUDA(call)                                                                    \
+  do {                                                                                    \
+    cudaError_t e_ = (call);                                                              \
+    if (e_ != cudaSuccess)                                                                \
+      return fail(e_ == cudaErrorMemoryAllocation ? HRW_ENOMEM : HRW_ECUDA,               \
+                  std::string(#call ": ") + cudaGetErrorString(e_));                      \
+  } while (0)
+
+// is_done (src/hrweno_tvdode.f90:282)
+inline bool is_done(double t, double tout, double dt) {
+  return (t - tout) * std::copysign(1.0, dt) > 0.0;
+}
+
+constexpr int64_t kMaxSteps = int64_t(1) << 40;
+
+struct DevLine {
+  double* width = nullptr;  // device copy of the user's widths (STRICT)
+  double* rws = nullptr;    // device fscale/width (FAST)
+};
+
+// Validate the problem descriptor against the same rules the reference's constructors apply,
+// plus the descriptor's own fields.
+int validate_problem(const hrw_problem* p, int neq) {
+  if (!p) return fail(HRW_EINVAL, "Invalid input 'problem': null pointer.");
+  if (neq <= 0) return fail(HRW_EINVAL, "Invalid input 'neq'. Valid range: neq >= 1.");
+  if (p->kind == HRW_PROBLEM_LINEAR_ODE) {
+    if (!p->rates) return fail(HRW_EINVAL, "Invalid input 'rates': null pointer.");
+    return HRW_OK;
+  }
+  if (p->kind != HRW_PROBLEM_FV1D && p->kind != HRW_PROBLEM_FV2D)
+    return fail(HRW_EINVAL, "Invalid input 'kind'.");
+  const int nd = p->kind == HRW_PROBLEM_FV2D ? 2 : 1;
+  int64_t cells = 1;
+  for (int d = 0; d < nd; ++d) {
+    if (p->ncells[d] <= 0) return fail(HRW_EINVAL, "Invalid input 'ncells'. Valid range: ncells > 0.");
+    if (!(p->xmax[d] > p->xmin[d]))
+      return fail(HRW_EINVAL, "Invalid input 'xmin', 'xmax'. Valid range: xmax > xmin.");
+    if (p->fn[d] != HRW_FN_BURGERS && p->fn[d] != HRW_FN_LINEAR)
+      return fail(HRW_EINVAL, "Invalid input 'fn'.");
+    if (p->bc[d] < HRW_BC_COPY || p->bc[d] > HRW_BC_ZERO_INFLOW)
+      return fail(HRW_EINVAL, "Invalid input 'bc'.");
+    cells *= p->ncells[d];
+  }
+  if (p->k < 1 || p->k > 3) return fail(HRW_EINVAL, "Invalid input 'k'. Valid range: 1 <= k <= 3.");
+  if (!(p->eps > 2.220446049250313e-16))
+    return fail(HRW_EINVAL, "Invalid input 'eps'. Valid range: eps > epsilon.");
+  if (p->flux != HRW_FLUX_LAX_FRIEDRICHS && p->flux != HRW_FLUX_GODUNOV)
+    return fail(HRW_EINVAL, "Invalid input 'flux'.");
+  if (p->numerics != HRW_NUMERICS_FAST && p->numerics != HRW_NUMERICS_STRICT)
+    return fail(HRW_EINVAL, "Invalid input 'numerics'.");
+  if (cells != neq) return fail(HRW_EINVAL, "Invalid input 'neq': neq /= product of ncells.");
+  return HRW_OK;
+}
+
+}  // namespace
+
+// -------------------------------------------------------------------------------------------
+// Handles
+// -------------------------------------------------------------------------------------------
+struct hrw_weno {
+  int nc = 0, k = 3;
+  double eps = 1e-6;
+  int numerics = HRW_NUMERICS_FAST;
+  bool uniform = true;
+  double* cnu = nullptr;  // device cnu(0:k-1,-1:k-1,1:nc)
+  double* buf = nullptr;  // device v, vl, vr for host-memory calls (3 nc)
+  cudaStream_t stream = nullptr;
+};
+
+struct hrw_ode {
+  hrw_problem prob{};
+  int neq = 0, order = 3, method = 0, dtype = HRW_F64;
+  int fevals = 0, istate = 0;
+  int64_t nsteps = 0;
+  cudaStream_t own = nullptr, stream = nullptr;
+  DevLine line[2];
+  double* rates = nullptr;
+  double* u = nullptr;   // device state for host-memory calls (rktvd)
+  double* w1 = nullptr;  // stage buffers
+  double* w2 = nullptr;
+  double* ring_u[5] = {};  // mstvd: u^m at slot m % 5
+  double* ring_l[4] = {};  // mstvd: L(u^m) at slot m % 4
+  int64_t level = 0;       // mstvd: m of the current solution
+  StageArgs base{};
+};
+
+extern "C" {
+
+const char* hrw_last_error(void) { return g_err.c_str(); }
+
+void hrw_problem_init(hrw_problem* p) {
+  if (!p) return;
+  std::memset(p, 0, sizeof(*p));
+  p->kind = HRW_PROBLEM_FV1D;
+  p->k = 3;
+  p->eps = 1e-6;
+  p->flux = HRW_FLUX_LAX_FRIEDRICHS;
+  p->fn[0] = p->fn[1] = HRW_FN_BURGERS;
+  p->coef_a[0] = p->coef_a[1] = 1.0;
+  p->alpha[0] = p->alpha[1] = 1.0;
+  p->bc[0] = p->bc[1] = HRW_BC_COPY;
+  p->xmin[0] = p->xmin[1] = 0.0;
+  p->xmax[0] = p->xmax[1] = 1.0;
+  p->numerics = HRW_NUMERICS_FAST;
+}
+
+// ---- weno ------------------------------------------------------------------------------------
+int hrw_weno_create(int ncells, int k, double eps, const double* xedges, hrw_weno** out) {
+  if (!out) return fail(HRW_EINVAL, "Invalid input 'out': null pointer.");
+  *out = nullptr;
+  // weno_init validation (src/hrweno_weno.f90:72-98); k <= 0 / eps <= 0 mean "not present"
+  if (ncells <= 0) return fail(HRW_EINVAL, "Invalid input 'ncells'. Valid range: ncells > 0.");
+  if (k > 0 && k > 3) return fail(HRW_EINVAL, "Invalid input 'k'. Valid range: 1 <= k <= 3.");
+  if (k == 0 || k < 0) k = 3;
+  if (eps <= 0.0 && eps == eps) eps = 1e-6;
+  if (!(eps > 2.220446049250313e-16))
+    return fail(HRW_EINVAL, "Invalid input 'eps'. Valid range: eps > epsilon.");
+  hrw_weno* w = new hrw_weno;
+  w->nc = ncells;
+  w->k = k;
+  w->eps = eps;
+  cudaError_t e = cudaStreamCreateWithFlags(&w->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMalloc(&w->buf, sizeof(double) * 3 * (size_t)ncells);
+  if (e == cudaSuccess && xedges) {
+    w->uniform = false;
+    double* dx = nullptr;
+    e = cudaMalloc(&w->cnu, sizeof(double) * (size_t)k * (k + 1) * ncells);
+    if (e == cudaSuccess) e = cudaMalloc(&dx, sizeof(double) * ((size_t)ncells + 1));
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(dx, xedges, sizeof(double) * ((size_t)ncells + 1), cudaMemcpyHostToDevice, w->stream);
+    if (e == cudaSuccess) e = launch_calc_cnu(dx, w->cnu, ncells, k, w->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(w->stream);
+    if (dx) cudaFree(dx);
+  }
+  if (e != cudaSuccess) {
+    hrw_weno_destroy(w);
+    return fail(e == cudaErrorMemoryAllocation ? HRW_ENOMEM : HRW_ECUDA,
+                std::string("hrw_weno_create: ") + cudaGetErrorString(e));
+  }
+  *out = w;
+  return HRW_OK;
+}
+
+int hrw_weno_set_numerics(hrw_weno* w, int numerics) {
+  if (!w) return fail(HRW_EINVAL, "Invalid input 'w': null handle.");
+  if (numerics != HRW_NUMERICS_FAST && numerics != HRW_NUMERICS_STRICT)
+    return fail(HRW_EINVAL, "Invalid input 'numerics'.");
+  w->numerics = numerics;
+  return HRW_OK;
+}
+
+int hrw_weno_reconstruct(hrw_weno* w, int dtype, int mem, const void* v, void* vl, void* vr) {
+  if (!w) return fail(HRW_EINVAL, "Invalid input 'w': null handle.");
+  if (!v || !vl || !vr) return fail(HRW_EINVAL, "Invalid input: null array.");
+  if (dtype != HRW_F64) return fail(HRW_EINVAL, "Invalid input 'dtype': reconstruct supports HRW_F64.");
+  const size_t bytes = sizeof(double) * (size_t)w->nc;
+  const double* dv = (const double*)v;
+  double* dl = (double*)vl;
+  double* dr = (double*)vr;
+  if (mem == HRW_MEM_HOST) {
+    dv = w->buf;
+    dl = w->buf + w->nc;
+    dr = w->buf + 2 * (size_t)w->nc;
+    HRW_CUDA(cudaMemcpyAsync((void*)dv, v, bytes, cudaMemcpyHostToDevice, w->stream));
+  }
+  const bool strict = w->numerics == HRW_NUMERICS_STRICT;
+  if (w->uniform) {
+    StageArgs a{};
+    a.v = dv;
+    a.out = dl;
+    a.lout = dr;
+    a.eps = w->eps;
+    a.L.nc = w->nc;
+    a.L.rx = 1.0;
+    HRW_CUDA(launch_stage1d(a, w->k, ST_RECON, strict, w->stream));
+  } else {
+    HRW_CUDA(launch_recon_nonuniform(dv, w->cnu, dl, dr, w->nc, w->k, w->eps, strict, w->stream));
+  }
+  if (mem == HRW_MEM_HOST) {
+    HRW_CUDA(cudaMemcpyAsync(vl, dl, bytes, cudaMemcpyDeviceToHost, w->stream));
+    HRW_CUDA(cudaMemcpyAsync(vr, dr, bytes, cudaMemcpyDeviceToHost, w->stream));
+  }
+  HRW_CUDA(cudaStreamSynchronize(w->stream));
+  return HRW_OK;
+}
+
+int hrw_weno_cnu(const hrw_weno* w, double* cnu_host) {
+  if (!w || !cnu_host) return fail(HRW_EINVAL, "Invalid input: null pointer.");
+  if (w->uniform) return fail(HRW_EINVAL, "hrw_weno_cnu: the grid is uniform (no xedges).");
+  HRW_CUDA(cudaMemcpy(cnu_host, w->cnu, sizeof(double) * (size_t)w->k * (w->k + 1) * w->nc,
+                      cudaMemcpyDeviceToHost));
+  return HRW_OK;
+}
+
+int hrw_weno_destroy(hrw_weno* w) {
+  if (!w) return HRW_OK;
+  if (w->cnu) cudaFree(w->cnu);
+  if (w->buf) cudaFree(w->buf);
+  if (w->stream) cudaStreamDestroy(w->stream);
+  delete w;
+  return HRW_OK;
+}
+
+// ---- ode -------------------------------------------------------------------------------------
+static int ode_create(const hrw_problem* p, int neq, int order, int method, int dtype, hrw_ode** out) {
+  if (!out) return fail(HRW_EINVAL, "Invalid input 'out': null pointer.");
+  *out = nullptr;
+  // rktvd_init / mstvd_init validation (src/hrweno_tvdode.f90:80-90,190-194)
+  if (neq <= 0) return fail(HRW_EINVAL, "Invalid input 'neq'. Valid range: neq >= 1.");
+  if (method == 0 && (order < 1 || order > 3))
+    return fail(HRW_EINVAL, "Invalid input 'order' in 'rktvd'. Valid range: 1 <= k <= 3.");
+  if (dtype != HRW_F64 && dtype != HRW_F32) return fail(HRW_EINVAL, "Invalid input 'dtype'.");
+  if (dtype == HRW_F32) return fail(HRW_EINVAL, "Invalid input 'dtype': HRW_F32 integrators are not built yet.");
+  int rc = validate_problem(p, neq);
+  if (rc != HRW_OK) return rc;
+  hrw_ode* o = new hrw_ode;
+  o->prob = *p;
+  o->neq = neq;
+  o->order = method == 1 ? 3 : order;
+  o->method = method;
+  o->dtype = dtype;
+  o->prob.width[0] = o->prob.width[1] = nullptr;  // host pointers are not kept
+  o->prob.rates = nullptr;
+  auto cleanup = [&](cudaError_t e) {
+    hrw_ode_destroy(o);
+    return fail(e == cudaErrorMemoryAllocation ? HRW_ENOMEM : HRW_ECUDA,
+                std::string("hrw_ode_create: ") + cudaGetErrorString(e));
+  };
+  cudaError_t e = cudaStreamCreateWithFlags(&o->own, cudaStreamNonBlocking);
+  if (e != cudaSuccess) return cleanup(e);
+  o->stream = o->own;
+  const size_t bytes = sizeof(double) * (size_t)neq;
+  StageArgs& b = o->base;
+  b.eps = p->eps;
+  const bool strict = p->numerics == HRW_NUMERICS_STRICT;
+  if (p->kind == HRW_PROBLEM_LINEAR_ODE) {
+    if ((e = cudaMalloc(&o->rates, bytes)) != cudaSuccess) return cleanup(e);
+    if ((e = cudaMemcpy(o->rates, p->rates, bytes, cudaMemcpyHostToDevice)) != cudaSuccess) return cleanup(e);
+  } else {
+    const int nd = p->kind == HRW_PROBLEM_FV2D ? 2 : 1;
+    for (int d = 0; d < nd; ++d) {
+      LineArgs& L = d == 0 ? b.L : b.L2;
+      L.nc = p->ncells[d];
+      L.fn = p->fn[d];
+      L.bc = p->bc[d];
+      L.flux = p->flux;
+      L.a = p->coef_a[d];
+      L.b = p->coef_b[d];
+      L.alpha = p->alpha[d];
+      L.xmin = p->xmin[d];
+      L.rx = (p->xmax[d] - p->xmin[d]) / L.nc;  // grid1%linear (src/hrweno_grids.f90:72)
+      const double fs = fast_flux_scale(p->flux, p->fn[d]);
+      L.rws0 = fs / L.rx;
+      if (p->width[d]) {
+        const size_t wb = sizeof(double) * (size_t)L.nc;
+        std::vector<double> rws(L.nc);
+        for (int i = 0; i < L.nc; ++i) {
+          if (!(p->width[d][i] > 0.0)) {
+            hrw_ode_destroy(o);
+            return fail(HRW_EINVAL, "Invalid input 'width': widths must be > 0.");
+          }
+          rws[i] = fs / p->width[d][i];
+        }
+        if ((e = cudaMalloc(&o->line[d].width, wb)) != cudaSuccess) return cleanup(e);
+        if ((e = cudaMalloc(&o->line[d].rws, wb)) != cudaSuccess) return cleanup(e);
+        if ((e = cudaMemcpy(o->line[d].width, p->width[d], wb, cudaMemcpyHostToDevice)) != cudaSuccess)
+          return cleanup(e);
+        if ((e = cudaMemcpy(o->line[d].rws, rws.data(), wb, cudaMemcpyHostToDevice)) != cudaSuccess)
+          return cleanup(e);
+        L.width = o->line[d].width;
+        L.rws = strict ? nullptr : o->line[d].rws;
+        if (strict) L.rws = nullptr;
+      }
+    }
+    b.ld = p->ncells[0];
+  }
+  if ((e = cudaMalloc(&o->u, bytes)) != cudaSuccess) return cleanup(e);
+  if ((e = cudaMalloc(&o->w1, bytes)) != cudaSuccess) return cleanup(e);
+  if ((e = cudaMalloc(&o->w2, bytes)) != cudaSuccess) return cleanup(e);
+  if (method == 1) {
+    for (int q = 0; q < 5; ++q)
+      if ((e = cudaMalloc(&o->ring_u[q], bytes)) != cudaSuccess) return cleanup(e);
+    for (int q = 0; q < 4; ++q)
+      if ((e = cudaMalloc(&o->ring_l[q], bytes)) != cudaSuccess) return cleanup(e);
+  }
+  o->istate = 1;
+  *out = o;
+  return HRW_OK;
+}
+
+int hrw_rktvd_create(const hrw_problem* p, int neq, int order, int dtype, hrw_ode** out) {
+  return ode_create(p, neq, order, 0, dtype, out);
+}
+
+int hrw_mstvd_create(const hrw_problem* p, int neq, int dtype, hrw_ode** out) {
+  return ode_create(p, neq, 3, 1, dtype, out);
+}
+
+int hrw_ode_set_stream(hrw_ode* o, void* stream) {
+  if (!o) return fail(HRW_EINVAL, "Invalid input 'ode': null handle.");
+  o->stream = stream ? (cudaStream_t)stream : o->own;
+  return HRW_OK;
+}
+
+int hrw_ode_info(const hrw_ode* o, int* fevals, int* istate, int64_t* nsteps) {
+  if (!o) return fail(HRW_EINVAL, "Invalid input 'ode': null handle.");
+  if (fevals) *fevals = o->fevals;
+  if (istate) *istate = o->istate;
+  if (nsteps) *nsteps = o->nsteps;
+  return HRW_OK;
+}
+
+int hrw_ode_destroy(hrw_ode* o) {
+  if (!o) return HRW_OK;
+  for (int d = 0; d < 2; ++d) {
+    if (o->line[d].width) cudaFree(o->line[d].width);
+    if (o->line[d].rws) cudaFree(o->line[d].rws);
+  }
+  double* bufs[] = {o->rates, o->u, o->w1, o->w2};
+  for (double* p : bufs)
+    if (p) cudaFree(p);
+  for (double* p : o->ring_u)
+    if (p) cudaFree(p);
+  for (double* p : o->ring_l)
+    if (p) cudaFree(p);
+  if (o->own) cudaStreamDestroy(o->own);
+  delete o;
+  return HRW_OK;
+}
+
+}  // extern "C"
+
+// -------------------------------------------------------------------------------------------
+// Stage dispatch and time loops
+// -------------------------------------------------------------------------------------------
+static cudaError_t run_stage(hrw_ode* o, int stage, const double* v, const double* u, double* out,
+                             double* lout, const double* uo4, const double* lo4, double dt) {
+  StageArgs a = o->base;
+  a.v = v;
+  a.u = u;
+  a.out = out;
+  a.lout = lout;
+  a.uo4 = uo4;
+  a.lo4 = lo4;
+  a.dt = dt;
+  const bool strict = o->prob.numerics == HRW_NUMERICS_STRICT;
+  switch (o->prob.kind) {
+    case HRW_PROBLEM_LINEAR_ODE: return launch_stage_linear(o->rates, a, o->neq, stage, strict, o->stream);
+    case HRW_PROBLEM_FV1D: return launch_stage1d(a, o->prob.k, stage, strict, o->stream);
+    default: return launch_stage2d(a, o->prob.k, stage, strict, o->stream);
+  }
+}
+
+// One rktvd step from u (in place for orders 2 and 3); order 1 writes into `out1`.
+static cudaError_t rk_step(hrw_ode* o, double* u, double* out1, double dt) {
+  cudaError_t e;
+  if (o->order == 1) return run_stage(o, ST_EULER, u, u, out1, nullptr, nullptr, nullptr, dt);
+  if ((e = run_stage(o, ST_EULER, u, u, o->w1, nullptr, nullptr, nullptr, dt)) != cudaSuccess) return e;
+  if (o->order == 2) return run_stage(o, ST_RK2B, o->w1, u, u, nullptr, nullptr, nullptr, dt);
+  if ((e = run_stage(o, ST_RK3B, o->w1, u, o->w2, nullptr, nullptr, nullptr, dt)) != cudaSuccess) return e;
+  return run_stage(o, ST_RK3C, o->w2, u, u, nullptr, nullptr, nullptr, dt);
+}
+
+// rktvd_integrate (src/hrweno_tvdode.f90:97-178) on device array du.
+static int rk_integrate(hrw_ode* o, double* du, double* t, double tout, double dt, int itask) {
+  // replay the reference's time sequence (:137-143) to count the steps
+  double tt = *t;
+  int64_t n = 0;
+  do {
+    tt = tt + dt;
+    if (++n > kMaxSteps) return fail(HRW_EINVAL, "Invalid input 'dt': too many steps to reach tout.");
+  } while (!(is_done(tt, tout, dt) || itask == 2));
+  double* cur = du;
+  double* other = o->w2;
+  for (int64_t s = 0; s < n; ++s) {
+    HRW_CUDA(rk_step(o, cur, other, dt));
+    if (o->order == 1) std::swap(cur, other);
+  }
+  if (cur != du)
+    HRW_CUDA(cudaMemcpyAsync(du, cur, sizeof(double) * (size_t)o->neq, cudaMemcpyDeviceToDevice, o->stream));
+  *t = tt;
+  o->fevals += (int)(o->order * n);
+  o->nsteps += n;
+  if (o->istate == 1) o->istate = 2;  // (:176)
+  return HRW_OK;
+}
+
+// mstvd_integrate (src/hrweno_tvdode.f90:203-271) on device array du.
+static int ms_integrate(hrw_ode* o, double* du, double* t, double tout, double dt) {
+  const size_t bytes = sizeof(double) * (size_t)o->neq;
+  double tt = *t;
+  if (o->istate == 1) {
+    // RK3 start (:236-249): u^m -> slot m % 5, L(u^m) -> slot m % 4, m = 0..3
+    o->level = 0;
+    HRW_CUDA(cudaMemcpyAsync(o->ring_u[0], du, bytes, cudaMemcpyDeviceToDevice, o->stream));
+    for (int m = 0; m < 4; ++m) {
+      double* um = o->ring_u[m % 5];
+      double* un = o->ring_u[(m + 1) % 5];
+      HRW_CUDA(run_stage(o, ST_RHS, um, um, o->ring_l[m % 4], nullptr, nullptr, nullptr, dt));
+      HRW_CUDA(run_stage(o, ST_EULER, um, um, o->w1, nullptr, nullptr, nullptr, dt));
+      HRW_CUDA(run_stage(o, ST_RK3B, o->w1, um, o->w2, nullptr, nullptr, nullptr, dt));
+      HRW_CUDA(run_stage(o, ST_RK3C, o->w2, um, un, nullptr, nullptr, nullptr, dt));
+      tt = tt + dt;  // ode_start%integrate(u, t, t + 2*dt, dt, itask=2): one step
+    }
+    o->level = 4;
+    o->fevals = 12;  // (:246) the start's RK3 evaluations; the 4 extra rhs calls are not counted
+    o->nsteps += 4;
+    o->istate = 2;
+  } else {
+    HRW_CUDA(cudaMemcpyAsync(o->ring_u[o->level % 5], du, bytes, cudaMemcpyDeviceToDevice, o->stream));
+  }
+  int64_t n = 0;
+  for (double t2 = tt; !is_done(t2, tout, dt); t2 = t2 + dt)
+    if (++n > kMaxSteps) return fail(HRW_EINVAL, "Invalid input 'dt': too many steps to reach tout.");
+  for (int64_t s = 0; s < n; ++s) {  // (:252-268)
+    const int64_t m = o->level;
+    double* um = o->ring_u[m % 5];
+    double* un = o->ring_u[(m + 1) % 5];  // holds u^{m-4}, overwritten in place
+    double* lm = o->ring_l[m % 4];        // holds L(u^{m-4}), overwritten in place
+    HRW_CUDA(run_stage(o, ST_MS, um, um, un, lm, un, lm, dt));
+    tt = tt + dt;
+    o->level = m + 1;
+  }
+  HRW_CUDA(cudaMemcpyAsync(du, o->ring_u[o->level % 5], bytes, cudaMemcpyDeviceToDevice, o->stream));
+  *t = tt;
+  o->fevals += (int)n;
+  o->nsteps += n;
+  return HRW_OK;
+}
+
+extern "C" int hrw_integrate(hrw_ode* o, int mem, void* u, double* t, double tout, double dt, int itask) {
+  if (!o) return fail(HRW_EINVAL, "Invalid input 'ode': null handle.");
+  if (!u || !t) return fail(HRW_EINVAL, "Invalid input: null pointer.");
+  if (o->istate < 1) return fail(HRW_ESTATE, "ode is in an error state.");  // (:126,228)
+  if (is_done(*t, tout, dt)) return HRW_OK;                                  // (:127,229)
+  if (!(dt != 0.0) || !std::isfinite(dt) || !std::isfinite(*t) || !std::isfinite(tout))
+    return fail(HRW_EINVAL, "Invalid input 'dt': must be finite and nonzero.");
+  if (itask != 1 && itask != 2) itask = 1;
+  const size_t bytes = sizeof(double) * (size_t)o->neq;
+  double* du = (double*)u;
+  if (mem == HRW_MEM_HOST) {
+    du = o->u;
+    HRW_CUDA(cudaMemcpyAsync(du, u, bytes, cudaMemcpyHostToDevice, o->stream));
+  }
+  int rc = o->method == 0 ? rk_integrate(o, du, t, tout, dt, itask) : ms_integrate(o, du, t, tout, dt);
+  if (rc != HRW_OK) return rc;
+  if (mem == HRW_MEM_HOST) HRW_CUDA(cudaMemcpyAsync(u, du, bytes, cudaMemcpyDeviceToHost, o->stream));
+  HRW_CUDA(cudaStreamSynchronize(o->stream));
+  return HRW_OK;
+}
+
+extern "C" int hrw_rhs(const hrw_problem* p, int dtype, double t, const void* v, void* vdot, void* stream) {
+  (void)t;
+  if (dtype != HRW_F64) return fail(HRW_EINVAL, "Invalid input 'dtype': hrw_rhs supports HRW_F64.");
+  int neq = p && p->kind == HRW_PROBLEM_FV2D ? p->ncells[0] * p->ncells[1] : (p ? p->ncells[0] : 0);
+  if (p && p->kind == HRW_PROBLEM_LINEAR_ODE) neq = p->ncells[0];
+  hrw_ode* o = nullptr;
+  int rc = ode_create(p, neq, 1, 0, HRW_F64, &o);
+  if (rc != HRW_OK) return rc;
+  if (stream) o->stream = (cudaStream_t)stream;
+  cudaError_t e = run_stage(o, ST_RHS, (const double*)v, (const double*)v, (double*)vdot, nullptr,
+                            nullptr, nullptr, 0.0);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(o->stream);
+  hrw_ode_destroy(o);
+  if (e != cudaSuccess) return fail(HRW_ECUDA, std::string("hrw_rhs: ") + cudaGetErrorString(e));
+  return HRW_OK;
+}

@@ -1,0 +1,258 @@
+// hrw_device.cuh - device building blocks of the fused WENO / flux / TVD stage kernels.
+//
+// Two numerics modes share every kernel:
+//  * FAST (default): the FP64 method with the fewest FP64 instructions.  On GB300 the FP64
+//    pipe retires about 2 DFMA per SM-clock, 1/62 of the FP32 rate, so the stage kernels are
+//    bound by the count of FP64 instructions, not by HBM.  The WENO weights are evaluated in
+//    product form (one reciprocal per cell instead of the twelve divisions of the reference),
+//    candidates use integer-scaled stencils, and values shared by neighbouring cells (second
+//    differences, candidate stencils) are computed once.  Results agree with the reference
+//    to rounding level (a few ulp per stage).
+//  * STRICT: the reference's operation order, one IEEE operation at a time with no fused
+//    multiply-add, true divisions (src/hrweno_weno.f90:178-214, src/hrweno_fluxes.f90:43,67-74,
+//    src/hrweno_tvdode.f90:139-167,257).  Bit-identical to a non-fused CPU build.
+#pragma once
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+namespace hrw {
+
+// ------------------------------------------------------------------------------------------
+// Reciprocal: PTX rcp.approx.ftz.f64 seed, then one cubic Newton-Raphson step
+//   e = 1 - x r,  r' = r (1 + e + e^2)
+// (the order-3 member of the Newton iteration family for 1/x; error e^3 of the seed's e).
+// Valid for normal x; callers keep x inside [2^-1000, 2^1000].
+// ------------------------------------------------------------------------------------------
+__device__ __forceinline__ double rcp_fast(double x) {
+  double r;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
+  double e = fma(-x, r, 1.0);
+  return fma(r, fma(e, e, e), r);
+}
+
+// positive doubles order like their high words
+__device__ __forceinline__ int hiword(double x) { return __double2hiint(x); }
+
+// ------------------------------------------------------------------------------------------
+// Reference tables (src/hrweno_weno.f90:11-21), used by the STRICT path and the guard path.
+// c(j, r) at [j + k*(r+1)].
+// ------------------------------------------------------------------------------------------
+template <int K> struct Tab;
+template <> struct Tab<1> {
+  __device__ static double d(int) { return 1.0; }
+  __device__ static double c(int, int) { return 1.0; }
+};
+template <> struct Tab<2> {
+  __device__ static double d(int r) { return r == 0 ? 2.0 / 3 : 1.0 / 3; }
+  __device__ static double c(int j, int r) {
+    const double t[6] = {3.0 / 2, -1.0 / 2, 1.0 / 2, 1.0 / 2, -1.0 / 2, 3.0 / 2};
+    return t[j + 2 * (r + 1)];
+  }
+};
+template <> struct Tab<3> {
+  __device__ static double d(int r) { return r == 0 ? 3.0 / 10 : (r == 1 ? 6.0 / 10 : 1.0 / 10); }
+  __device__ static double c(int j, int r) {
+    const double t[12] = {11.0 / 6, -7.0 / 6, 1.0 / 3,  1.0 / 3,  5.0 / 6,  -1.0 / 6,
+                          -1.0 / 6, 5.0 / 6,  1.0 / 3,  1.0 / 3,  -7.0 / 6, 11.0 / 6};
+    return t[j + 3 * (r + 1)];
+  }
+};
+
+// ------------------------------------------------------------------------------------------
+// STRICT reconstruction of one cell, reference order (src/hrweno_weno.f90:175-214).
+// p points at v(i); p[-(K-1)] .. p[K-1] must be valid (ghosts already substituted).
+// ------------------------------------------------------------------------------------------
+template <int K>
+__device__ __forceinline__ void recon_strict(const double* p, double eps, double& vl, double& vr) {
+  double vrr[K], vlr[K], beta[K];
+#pragma unroll
+  for (int r = 0; r < K; ++r) {
+    double sr = 0.0, sl = 0.0;
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+      sr = __dadd_rn(sr, __dmul_rn(Tab<K>::c(j, r), p[j - r]));
+      sl = __dadd_rn(sl, __dmul_rn(Tab<K>::c(j, r - 1), p[j - r]));
+    }
+    vrr[r] = sr;
+    vlr[r] = sl;
+  }
+  if constexpr (K == 1) {
+    beta[0] = 0.0;
+  } else if constexpr (K == 2) {  // (src/hrweno_weno.f90:189-191)
+    double a = __dsub_rn(p[1], p[0]), b = __dsub_rn(p[0], p[-1]);
+    beta[0] = __dmul_rn(a, a);
+    beta[1] = __dmul_rn(b, b);
+  } else {  // (src/hrweno_weno.f90:194-202)
+    const double c13 = 13.0 / 12, c14 = 1.0 / 4;
+    double a, b;
+    a = __dadd_rn(__dsub_rn(p[0], __dmul_rn(2.0, p[1])), p[2]);
+    b = __dadd_rn(__dsub_rn(__dmul_rn(3.0, p[0]), __dmul_rn(4.0, p[1])), p[2]);
+    beta[0] = __dadd_rn(__dmul_rn(c13, __dmul_rn(a, a)), __dmul_rn(c14, __dmul_rn(b, b)));
+    a = __dadd_rn(__dsub_rn(p[-1], __dmul_rn(2.0, p[0])), p[1]);
+    b = __dsub_rn(p[-1], p[1]);
+    beta[1] = __dadd_rn(__dmul_rn(c13, __dmul_rn(a, a)), __dmul_rn(c14, __dmul_rn(b, b)));
+    a = __dadd_rn(__dsub_rn(p[-2], __dmul_rn(2.0, p[-1])), p[0]);
+    b = __dadd_rn(__dsub_rn(p[-2], __dmul_rn(4.0, p[-1])), __dmul_rn(3.0, p[0]));
+    beta[2] = __dadd_rn(__dmul_rn(c13, __dmul_rn(a, a)), __dmul_rn(c14, __dmul_rn(b, b)));
+  }
+  double alfa[K], alfat[K];  // (src/hrweno_weno.f90:207-210)
+  double sa = 0.0, sat = 0.0;
+#pragma unroll
+  for (int r = 0; r < K; ++r) {
+    double e = __dadd_rn(eps, beta[r]);
+    double e2 = __dmul_rn(e, e);
+    alfa[r] = __ddiv_rn(Tab<K>::d(r), e2);
+    alfat[r] = __ddiv_rn(Tab<K>::d(K - 1 - r), e2);
+  }
+#pragma unroll
+  for (int r = 0; r < K; ++r) { sa = __dadd_rn(sa, alfa[r]); sat = __dadd_rn(sat, alfat[r]); }
+  double ar = 0.0, al = 0.0;  // (src/hrweno_weno.f90:213-214)
+#pragma unroll
+  for (int r = 0; r < K; ++r) {
+    ar = __dadd_rn(ar, __dmul_rn(__ddiv_rn(alfa[r], sa), vrr[r]));
+    al = __dadd_rn(al, __dmul_rn(__ddiv_rn(alfat[r], sat), vlr[r]));
+  }
+  vr = ar;
+  vl = al;
+}
+
+// Out-of-line reference-order path for the rare cells that fail the FAST range guard.
+template <int K>
+__device__ __noinline__ double2 recon_guarded(double vm2, double vm1, double v0, double vp1,
+                                              double vp2, double eps) {
+  const double p[5] = {vm2, vm1, v0, vp1, vp2};
+  double2 out;
+  recon_strict<K>(p + 2, eps, out.x, out.y);  // x = vl, y = vr
+  return out;
+}
+
+// ------------------------------------------------------------------------------------------
+// FAST reconstruction of C consecutive cells held in a register window.
+//   w[q] = v(j0 - K + q), q = 0 .. C+2K-1;  cell c (0..C-1) is centred at w[K + c].
+// Out: vl[c] = v^+_{j-1/2}, vr[c] = v^-_{j+1/2} of cell j0 + c.
+//
+// Algebra (k = 3; k = 2 is analogous):
+//   s_r = (eps + beta_r)^2,  P_0 = s_1 s_2,  P_1 = s_0 s_2,  P_2 = s_0 s_1
+//   alfa_r = d_r / s_r  =>  w_r = d_r P_r / sum_q d_q P_q       (same weights, no division)
+//   vr = sum_r d_r P_r vrr_r / sum_r d_r P_r,   vl likewise with d mirrored
+// with d = (3, 6, 1)/10 scaled to integers and candidates scaled by 6 (integer stencils).
+// Both quotients share one reciprocal of their denominators' product.
+// Guard: the product form squares the range of s; cells whose s would overflow it take the
+// reference-order path (only for |v| of order 1e18 and above).
+// ------------------------------------------------------------------------------------------
+template <int K> struct FastGuard;
+// products reach ~600 s_max^4 (k=3) and ~18 s_max^2 (k=2): keep s_max below 2^240 / 2^480
+template <> struct FastGuard<3> { static constexpr int hi_max = (1023 + 240) << 20; };
+template <> struct FastGuard<2> { static constexpr int hi_max = (1023 + 480) << 20; };
+
+template <int K, int C>
+__device__ __forceinline__ void recon_fast(const double* w, double eps, double* vl, double* vr) {
+  if constexpr (K == 1) {
+#pragma unroll
+    for (int c = 0; c < C; ++c) { vl[c] = w[1 + c]; vr[c] = w[1 + c]; }
+  } else if constexpr (K == 2) {
+    // V0 = 2 vrr0 = v0 + v1, V1 = 2 vrr1 = 3 v0 - v-1, W0 = 2 vlr0 = 3 v0 - v1,
+    // W1 = 2 vlr1 = v-1 + v0 = V0 of the previous cell; beta1 = beta0 of the previous cell.
+    double V0p = w[1] + w[2];  // V0 of cell c = -1 (centre q = 1)
+    double dp = w[2] - w[1];
+    double ep = eps + dp * dp;
+    double s0p = ep * ep;  // s0 of cell -1
+#pragma unroll
+    for (int c = 0; c < C; ++c) {
+      const int q = 2 + c;
+      const double V0 = w[q] + w[q + 1];
+      const double V1 = fma(3.0, w[q], -w[q - 1]);
+      const double W0 = fma(3.0, w[q], -w[q + 1]);
+      const double W1 = V0p;
+      const double d0 = w[q + 1] - w[q];
+      const double e0 = fma(d0, d0, eps);
+      const double s0 = e0 * e0, s1 = s0p;
+      const double s1x2 = s1 + s1, s0x2 = s0 + s0;
+      const double den = s1x2 + s0;    // 2 s1 + s0  (d = (2, 1)/3)
+      const double dent = s1 + s0x2;   // s1 + 2 s0  (d mirrored)
+      const double num = fma(s1x2, V0, s0 * V1);
+      const double numt = fma(s1, W0, s0x2 * W1);
+      if (max(hiword(s0), hiword(s1)) < FastGuard<2>::hi_max) {
+        const double R = rcp_fast((den + den) * dent);
+        vr[c] = num * (dent * R);
+        vl[c] = numt * (den * R);
+      } else {
+        const double2 g = recon_guarded<2>(0.0, w[q - 1], w[q], w[q + 1], 0.0, eps);
+        vl[c] = g.x;
+        vr[c] = g.y;
+      }
+      V0p = V0;
+      s0p = s0;
+    }
+  } else {
+    // hv(m) = v(m)/2, A(m) = 13/12 (v(m-1) - 2 v(m) + v(m+1))^2, both shared by neighbours.
+    double hv[C + 6], A[C + 2];
+#pragma unroll
+    for (int q = 1; q < C + 5; ++q) hv[q] = 0.5 * w[q];
+    const double c13 = 13.0 / 12;
+#pragma unroll
+    for (int m = 0; m < C + 2; ++m) {  // centre q = m + 2 (cells -1 .. C)
+      const int q = m + 2;
+      const double D = fma(-2.0, w[q], w[q - 1] + w[q + 1]);
+      A[m] = (c13 * D) * D;
+    }
+    // candidates x6: V0 = 2v0 + 5v1 - v2, V1 = -v-1 + 5v0 + 2v1, V2 = 2v-2 - 7v-1 + 11v0,
+    // W0 = 11v0 - 7v1 + 2v2, W1 = V0 of previous cell, W2 = V1 of previous cell.
+    double V0p = fma(5.0, w[3], fma(2.0, w[2], -w[4]));  // cell -1: centre q = 2
+    double V1p = fma(5.0, w[2], fma(2.0, w[3], -w[1]));
+#pragma unroll
+    for (int c = 0; c < C; ++c) {
+      const int q = 3 + c;
+      const double V0 = fma(5.0, w[q + 1], fma(2.0, w[q], -w[q + 2]));
+      const double V1 = fma(5.0, w[q], fma(2.0, w[q + 1], -w[q - 1]));
+      const double V2 = fma(11.0, w[q], fma(-7.0, w[q - 1], 2.0 * w[q - 2]));
+      const double W0 = fma(11.0, w[q], fma(-7.0, w[q + 1], 2.0 * w[q + 2]));
+      const double W1 = V0p, W2 = V1p;
+      const double E0 = fma(1.5, w[q], fma(-2.0, w[q + 1], hv[q + 2]));
+      const double E1 = hv[q - 1] - hv[q + 1];
+      const double E2 = fma(1.5, w[q], fma(-2.0, w[q - 1], hv[q - 2]));
+      const double b0 = fma(E0, E0, A[c + 2]);  // A(j+1)
+      const double b1 = fma(E1, E1, A[c + 1]);  // A(j)
+      const double b2 = fma(E2, E2, A[c]);      // A(j-1)
+      const double e0 = eps + b0, e1 = eps + b1, e2 = eps + b2;
+      const double s0 = e0 * e0, s1 = e1 * e1, s2 = e2 * e2;
+      if (max(max(hiword(s0), hiword(s1)), hiword(s2)) < FastGuard<3>::hi_max) {
+        const double P0 = s1 * s2, P1 = s0 * s2, P2 = s0 * s1;
+        const double Q1 = 6.0 * P1, T0 = 3.0 * P0, T2 = 3.0 * P2;
+        const double den = (Q1 + P2) + T0;   // d = (3, 6, 1)/10
+        const double dent = (Q1 + P0) + T2;  // d mirrored = (1, 6, 3)/10
+        const double num = fma(T0, V0, fma(Q1, V1, P2 * V2));
+        const double numt = fma(T2, W2, fma(Q1, W1, P0 * W0));
+        const double R = rcp_fast((6.0 * den) * dent);
+        vr[c] = num * (dent * R);
+        vl[c] = numt * (den * R);
+      } else {
+        const double2 g = recon_guarded<3>(w[q - 2], w[q - 1], w[q], w[q + 1], w[q + 2], eps);
+        vl[c] = g.x;
+        vr[c] = g.y;
+      }
+      V0p = V0;
+      V1p = V1;
+    }
+  }
+}
+
+// single cell, no neighbour sharing (block-edge cells).  Reads p[-(K-1)] .. p[K-1] only; the
+// two outermost window slots, which a single cell does not use, repeat the nearest value.
+template <int K>
+__device__ __forceinline__ void recon_fast_one(const double* p, double eps, double& vl, double& vr) {
+  double w[1 + 2 * K];
+#pragma unroll
+  for (int q = 0; q < 1 + 2 * K; ++q) {
+    int o = q - K;
+    o = o < -(K - 1) ? -(K - 1) : (o > K - 1 ? K - 1 : o);
+    w[q] = p[o];
+  }
+  double l[1], r[1];
+  recon_fast<K, 1>(w, eps, l, r);
+  vl = l[0];
+  vr = r[0];
+}
+
+}  // namespace hrw

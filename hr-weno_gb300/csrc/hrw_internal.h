@@ -1,0 +1,66 @@
+// hrw_internal.h - host-side declarations shared by the C-ABI and the kernel launchers.
+#pragma once
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+namespace hrw {
+
+// Kind of stage a launch performs: what it combines with L(v).
+enum StageKind : int {
+  ST_RHS = 0,    // out = L(v)
+  ST_EULER = 1,  // out = v + dt L(v)                      (rktvd :139,150,163)
+  ST_RK2B = 2,   // out = (u + v + dt L(v)) / 2            (rktvd :152)
+  ST_RK3B = 3,   // out = (3u + v + dt L(v)) / 4           (rktvd :165)
+  ST_RK3C = 4,   // out = (u + 2v + 2dt L(v)) / 3          (rktvd :167)
+  ST_MS = 5,     // out = (25v + 50dt L(v) + 7uo4 + 10dt lo4)/32, lout = L(v)  (mstvd :257)
+  ST_RECON = 6   // out = vl, lout = vr                    (weno%reconstruct)
+};
+
+// One dimension of the problem as the kernels see it.
+struct LineArgs {
+  int nc;
+  int fn;        // HRW_FN_*
+  int bc;        // HRW_BC_*
+  int flux;      // HRW_FLUX_*
+  double a, b;   // LINEAR: g(x) = a + b x
+  double alpha;  // Lax-Friedrichs alpha
+  double xmin, rx;
+  // STRICT: divide by width (width[] or rx); FAST: multiply by rws (rws[] or rws0), which
+  // already carries the flux scaling of the FAST flux form.
+  const double* width;
+  const double* rws;
+  double rws0;
+};
+
+struct StageArgs {
+  const double* v;    // stencil input
+  const double* u;    // u^n for RK2B / RK3B / RK3C
+  double* out;
+  double* lout;       // ST_MS: L(v); ST_RECON: vr
+  const double* uo4;  // ST_MS: u^{n-4}
+  const double* lo4;  // ST_MS: L(u^{n-4})
+  double eps, dt;
+  LineArgs L;
+  // 2D only
+  LineArgs L2;
+  int64_t ld;         // row stride (nc1) of the 2D layout
+};
+
+// FAST flux form: the kernels evaluate F / fscale, fscale folded into rws.
+double fast_flux_scale(int flux, int fn);
+
+// 1D fused stage over nc cells; k in 1..3; strict selects the reference-order numerics.
+cudaError_t launch_stage1d(const StageArgs& a, int k, int stage, bool strict, cudaStream_t s);
+// 2D fused stage (x1 fastest), dimension by dimension.
+cudaError_t launch_stage2d(const StageArgs& a, int k, int stage, bool strict, cudaStream_t s);
+// Linear ODE u' = a u stage (test problem of the reference's integrator tests).
+cudaError_t launch_stage_linear(const double* rates, const StageArgs& a, int64_t n, int stage,
+                                bool strict, cudaStream_t s);
+// Non-uniform WENO: coefficients cnu(0:k-1,-1:k-1,1:nc) from xedges(0:nc), on the device.
+cudaError_t launch_calc_cnu(const double* xedges, double* cnu, int nc, int k, cudaStream_t s);
+// Reconstruction with per-cell coefficients (non-uniform grid).
+cudaError_t launch_recon_nonuniform(const double* v, const double* cnu, double* vl, double* vr,
+                                    int nc, int k, double eps, bool strict, cudaStream_t s);
+
+}  // namespace hrw

@@ -1,0 +1,78 @@
+"""rktvd / mstvd types (src/hrweno_tvdode.f90): TVD Runge-Kutta and multistep integrators.
+
+The reference's `integrate(u, t, tout, dt)` updates u and t in place; Python floats are
+immutable, so integrate() updates u in place and returns the new t.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+from . import _abi as A
+from ._arrays import describe
+from .problems import Problem
+
+_DT = {"f64": A.HRW_F64, "f32": A.HRW_F32}
+
+
+class _tvdode:
+    def __init__(self, h, problem: Problem, neq: int):
+        self._h = h
+        self.problem = problem
+        self.neq = neq
+
+    def integrate(self, u, t: float, tout: float, dt: float, itask: int = 1) -> float:
+        mem, p, _ = describe(u, self.neq, True)
+        tt = C.c_double(t)
+        A.check(A.lib().hrw_integrate(self._h, mem, p, C.byref(tt), float(tout), float(dt),
+                                      int(itask)))
+        return tt.value
+
+    def set_stream(self, stream) -> None:
+        """Run on a CUDA stream (an int handle, e.g. torch.cuda.Stream().cuda_stream)."""
+        A.check(A.lib().hrw_ode_set_stream(self._h, C.c_void_p(int(stream) if stream else 0)))
+
+    def _info(self):
+        fe, st, ns = C.c_int(), C.c_int(), C.c_int64()
+        A.check(A.lib().hrw_ode_info(self._h, C.byref(fe), C.byref(st), C.byref(ns)))
+        return fe.value, st.value, ns.value
+
+    @property
+    def fevals(self) -> int:
+        return self._info()[0]
+
+    @property
+    def istate(self) -> int:
+        return self._info()[1]
+
+    @property
+    def nsteps(self) -> int:
+        return self._info()[2]
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and A._lib is not None:
+            A._lib.hrw_ode_destroy(h)
+            self._h = None
+
+
+class rktvd(_tvdode):  # noqa: N801
+    """rktvd(fu, neq, order) with fu given as a Problem (src/hrweno_tvdode.f90:69-95)."""
+
+    def __init__(self, problem: Problem, neq: int, order: int = 3, dtype: str = "f64"):
+        h = C.c_void_p()
+        self._cp = problem.to_c()
+        A.check(A.lib().hrw_rktvd_create(C.byref(self._cp), int(neq), int(order), _DT[dtype],
+                                         C.byref(h)))
+        super().__init__(h, problem, int(neq))
+        self.order = int(order)
+
+
+class mstvd(_tvdode):  # noqa: N801
+    """mstvd(fu, neq) with fu given as a Problem (src/hrweno_tvdode.f90:180-201)."""
+
+    def __init__(self, problem: Problem, neq: int, dtype: str = "f64"):
+        h = C.c_void_p()
+        self._cp = problem.to_c()
+        A.check(A.lib().hrw_mstvd_create(C.byref(self._cp), int(neq), _DT[dtype], C.byref(h)))
+        super().__init__(h, problem, int(neq))
+        self.order = 3

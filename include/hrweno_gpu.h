@@ -1,0 +1,135 @@
+/*
+ * hrweno_gpu.h - C ABI of the GB300 (sm_103a) implementation of HR-WENO's hot path:
+ * WENO reconstruction, the monotone numerical fluxes and the TVD Runge-Kutta /
+ * multistep stage updates, fused into one CUDA kernel per stage.
+ *
+ * Every entry point is `extern "C"`, takes plain pointers and sizes, and returns a
+ * status code (HRW_OK == 0).  Where the Fortran reference aborts with `error stop`,
+ * this library returns HRW_EINVAL and keeps the reference's message, readable through
+ * hrw_last_error().  Handles are not thread-safe; each handle owns one CUDA stream.
+ *
+ * Reference interfaces replaced (paths inside HugoMVale/HR-WENO):
+ *   weno(ncells,k,eps,xedges)          src/hrweno_weno.f90:48-50,54-127
+ *   weno%reconstruct(v,vl,vr)          src/hrweno_weno.f90:44,129-219
+ *   lax_friedrichs / godunov           src/hrweno_fluxes.f90:22-45,47-76
+ *   rktvd(fu,neq,order)                src/hrweno_tvdode.f90:59-61,69-95
+ *   mstvd(fu,neq)                      src/hrweno_tvdode.f90:63-65,180-201
+ *   ode%integrate(u,t,tout,dt,itask)   src/hrweno_tvdode.f90:97-178,203-271
+ *   the user right-hand side `fu`      example/example1_burgers_1d_fv.f90:72-109,
+ *                                      example/example2_pbe_2d_fv.f90:73-129
+ * The reference stores the right-hand side as a procedure pointer
+ * (src/hrweno_tvdode.f90:16,50-57).  A GPU stage kernel cannot call back into host code,
+ * so the right-hand side is described by an hrw_problem instead.
+ */
+#ifndef HRWENO_GPU_H
+#define HRWENO_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------------------- */
+enum {
+  HRW_OK = 0,
+  HRW_EINVAL = 1,   /* invalid input; message as in the reference's `msg` field */
+  HRW_ECUDA = 2,    /* a CUDA runtime call failed */
+  HRW_ESTATE = 3,   /* handle is in an error state (reference: istate < 1) */
+  HRW_ETIMEOUT = 4, /* a bounded device-side wait ran out; the context stays usable */
+  HRW_ENOMEM = 5    /* device allocation failed */
+};
+
+/* ---- element type and memory space of user arrays -------------------------------- */
+enum { HRW_F64 = 0, HRW_F32 = 1 };
+enum { HRW_MEM_HOST = 0, HRW_MEM_DEVICE = 1 };
+
+/* ---- problem descriptor: the right-hand side L(u) -------------------------------- */
+enum {
+  HRW_PROBLEM_FV1D = 1,       /* example1: WENO + flux + conservative difference on a line */
+  HRW_PROBLEM_FV2D = 2,       /* example2: dimension-by-dimension sweeps, x1 fastest */
+  HRW_PROBLEM_LINEAR_ODE = 3  /* u_i' = a_i u_i (test/test_tvdode.f90:107-111) */
+};
+enum { HRW_FLUX_LAX_FRIEDRICHS = 0, HRW_FLUX_GODUNOV = 1 };
+/* physical flux f(u, x): BURGERS = u^2/2; LINEAR = (a + b*x) * u, x = interface coordinate */
+enum { HRW_FN_BURGERS = 0, HRW_FN_LINEAR = 1 };
+/* domain-boundary fluxes (per dimension):
+ *   COPY        F_{1/2} = F_{3/2}, F_{nc+1/2} = F_{nc-1/2}  (example1...f90:103-104)
+ *   ZERO        F_{1/2} = F_{nc+1/2} = 0                   (example2...f90:117-120)
+ *   ZERO_INFLOW F_{1/2} = 0, F_{nc+1/2} = f(vr(nc)): no inflow, free outflow */
+enum { HRW_BC_COPY = 0, HRW_BC_ZERO = 1, HRW_BC_ZERO_INFLOW = 2 };
+/* FAST: the FP64 method with the fewest FP64 instructions (product-form WENO weights, one
+ * reciprocal per cell, fused multiply-adds); agrees with the reference to rounding level.
+ * STRICT: the reference's operation order with no fused multiply-add and true divisions;
+ * bit-identical to a non-fused CPU build of the reference's formulas. */
+enum { HRW_NUMERICS_FAST = 0, HRW_NUMERICS_STRICT = 1 };
+
+typedef struct hrw_problem {
+  int32_t kind;       /* HRW_PROBLEM_* */
+  int32_t ncells[2];  /* FV1D: ncells[0]; FV2D: [nc1, nc2], u((j-1)*nc1+i) as example2:124 */
+  int32_t k;          /* WENO order 2k-1, 1 <= k <= 3 */
+  double eps;         /* WENO smoothing factor, eps > epsilon */
+  int32_t flux;       /* HRW_FLUX_* (same numerical flux in every dimension) */
+  int32_t fn[2];      /* HRW_FN_* per dimension */
+  double coef_a[2];   /* LINEAR: a per dimension */
+  double coef_b[2];   /* LINEAR: b per dimension */
+  double alpha[2];    /* Lax-Friedrichs alpha = max|f'(u)| per dimension */
+  int32_t bc[2];      /* HRW_BC_* per dimension */
+  double xmin[2];     /* uniform grid as grid1%linear: edges(i) = xmin + (xmax-xmin)/nc*i */
+  double xmax[2];
+  const double* width[2]; /* optional host array(nc) of cell widths; NULL: (xmax-xmin)/nc */
+  const double* rates;    /* LINEAR_ODE: host array(neq) of rates a_i */
+  int32_t numerics;       /* HRW_NUMERICS_* */
+} hrw_problem;
+
+/* Fill *p with the defaults: FV1D, k=3, eps=1e-6, Lax-Friedrichs, Burgers, alpha=1,
+ * COPY boundaries, grid [0,1], FAST numerics.  ncells must still be set. */
+void hrw_problem_init(hrw_problem* p);
+
+/* ---- errors ----------------------------------------------------------------------- */
+/* Message of the last failing call on this host thread ("" if none). */
+const char* hrw_last_error(void);
+
+/* ---- WENO reconstruction (weno type) ---------------------------------------------- */
+typedef struct hrw_weno hrw_weno;
+
+/* weno(ncells, k, eps, xedges): xedges is NULL (uniform grid) or a host array(ncells+1).
+ * k <= 0 selects the default k = 3; eps <= 0 selects the default 1e-6
+ * (the reference's optional arguments, src/hrweno_weno.f90:60-69). */
+int hrw_weno_create(int ncells, int k, double eps, const double* xedges, hrw_weno** out);
+/* Select HRW_NUMERICS_FAST (default) or HRW_NUMERICS_STRICT for later reconstructions. */
+int hrw_weno_set_numerics(hrw_weno* w, int numerics);
+/* w%reconstruct(v, vl, vr): arrays of ncells elements of `dtype` in memory space `mem`. */
+int hrw_weno_reconstruct(hrw_weno* w, int dtype, int mem, const void* v, void* vl, void* vr);
+/* Copy the non-uniform coefficients cnu(0:k-1,-1:k-1,1:nc), Fortran order, to the host. */
+int hrw_weno_cnu(const hrw_weno* w, double* cnu_host);
+int hrw_weno_destroy(hrw_weno* w);
+
+/* ---- TVD ODE integrators (rktvd / mstvd types) ------------------------------------ */
+typedef struct hrw_ode hrw_ode;
+
+/* rktvd(fu, neq, order): order 1..3; dtype HRW_F64 (the method itself) or HRW_F32
+ * (bulk FP32 with a compensated two-sum accumulation of u; time stays FP64). */
+int hrw_rktvd_create(const hrw_problem* p, int neq, int order, int dtype, hrw_ode** out);
+/* mstvd(fu, neq): 5-step, 3rd-order TVD multistep with an RK3 start. */
+int hrw_mstvd_create(const hrw_problem* p, int neq, int dtype, hrw_ode** out);
+/* ode%integrate(u, t, tout, dt[, itask]): u (neq elements of the ode's dtype) is updated
+ * in place, *t advances like the reference (it stops at the first step with t > tout).
+ * itask: 1 normal integration until tout, 2 single step. */
+int hrw_integrate(hrw_ode* ode, int mem, void* u, double* t, double tout, double dt, int itask);
+/* fevals, istate (1 first call, 2 later calls, -1 error) and steps taken so far. */
+int hrw_ode_info(const hrw_ode* ode, int* fevals, int* istate, int64_t* nsteps);
+/* Run this handle's kernels on `stream` (a cudaStream_t); NULL restores its own stream. */
+int hrw_ode_set_stream(hrw_ode* ode, void* stream);
+int hrw_ode_destroy(hrw_ode* ode);
+
+/* ---- right-hand side alone (fu of the reference's driver) -------------------------- */
+/* vdot = L(v) at time t for problem p, both arrays device pointers of `dtype`
+ * (LINEAR_ODE: neq = ncells[0]). */
+int hrw_rhs(const hrw_problem* p, int dtype, double t, const void* v, void* vdot, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HRWENO_GPU_H */

@@ -1,0 +1,126 @@
+"""TEST INFRASTRUCTURE ONLY - ctypes wrapper of the CPU oracle (oracle/hrweno_oracle.cpp).
+
+Only tests/, __graft_entry__.smoke() and the cpu-baseline leg of bench.py import this module;
+the product library never does.  The oracle restates HugoMVale/HR-WENO's Fortran in the
+reference's operation order (see the header of hrweno_oracle.cpp) and is pinned by the
+reference's own known-answer tests (tests/test_oracle_kat.py).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+SRC = HERE / "hrweno_oracle.cpp"
+LIB = HERE / "_build" / "libhrweno_oracle.so"
+
+_lib = None
+
+
+def build(force: bool = False) -> Path:
+    """Compile the oracle with g++ (no fused multiply-add)."""
+    LIB.parent.mkdir(exist_ok=True)
+    hdr = HERE.parent / "include" / "hrweno_gpu.h"
+    if force or not LIB.exists() or LIB.stat().st_mtime < max(SRC.stat().st_mtime, hdr.stat().st_mtime):
+        subprocess.run(["g++", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-std=c++17",
+                        "-o", str(LIB), str(SRC)], check=True)
+    return LIB
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(str(LIB))
+        dp = C.POINTER(C.c_double)
+        L.orc_last_error.restype = C.c_char_p
+        L.orc_weno_reconstruct.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, dp, dp, dp, dp]
+        L.orc_weno_calc_cnu.argtypes = [C.c_int, C.c_int, dp, dp]
+        L.orc_numflux.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
+                                  C.c_double, C.c_double, C.c_double, C.c_double]
+        L.orc_numflux.restype = C.c_double
+        L.orc_rhs.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_double, dp, dp]
+        L.orc_ode_create.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_int]
+        L.orc_ode_create.restype = C.c_void_p
+        L.orc_ode_integrate.argtypes = [C.c_void_p, dp, dp, C.c_double, C.c_double, C.c_int]
+        L.orc_ode_info.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                   C.POINTER(C.c_longlong)]
+        L.orc_ode_destroy.argtypes = [C.c_void_p]
+        _lib = L
+    return _lib
+
+
+def _p(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class OracleError(RuntimeError):
+    pass
+
+
+def reconstruct(v, k: int = 3, eps: float = 1e-6, xedges=None, prec: int = 64):
+    """weno(nc, k, eps, xedges)%reconstruct(v, vl, vr) -> (vl, vr)."""
+    v = np.ascontiguousarray(v, dtype=np.float64)
+    vl, vr = np.empty_like(v), np.empty_like(v)
+    xe = None if xedges is None else np.ascontiguousarray(xedges, dtype=np.float64)
+    rc = lib().orc_weno_reconstruct(prec, v.size, k, eps, None if xe is None else _p(xe),
+                                    _p(v), _p(vl), _p(vr))
+    if rc:
+        raise OracleError(lib().orc_last_error().decode())
+    return vl, vr
+
+
+def calc_cnu(nc: int, k: int, xedges) -> np.ndarray:
+    """cnu(0:k-1, -1:k-1, 1:nc) as an array [nc, k+1, k]."""
+    xe = np.ascontiguousarray(xedges, dtype=np.float64)
+    out = np.empty(k * (k + 1) * nc)
+    lib().orc_weno_calc_cnu(nc, k, _p(xe), _p(out))
+    return out.reshape(nc, k + 1, k)
+
+
+FLUX_TEST_UXT = 100
+
+
+def numflux(kind: int, fn: int, vm: float, vp: float, x: float, t: float, alpha: float = 0.0,
+            a: float = 1.0, b: float = 0.0) -> float:
+    """lax_friedrichs (kind 0) or godunov (kind 1) with flux fn."""
+    return lib().orc_numflux(kind, fn, a, b, vm, vp, x, t, alpha)
+
+
+def rhs(problem, v, t: float = 0.0, prec: int = 64) -> np.ndarray:
+    """vdot = L(v) of a hrweno Problem."""
+    cp = problem.to_c()
+    v = np.ascontiguousarray(v, dtype=np.float64)
+    out = np.empty_like(v)
+    lib().orc_rhs(prec, C.addressof(cp), v.size, t, _p(v), _p(out))
+    return out
+
+
+class ODE:
+    """rktvd (method 0) / mstvd (method 1) of the oracle at precision prec (32, 64, 128)."""
+
+    def __init__(self, problem, neq: int, method: int = 0, order: int = 3, prec: int = 64):
+        self._cp = problem.to_c()
+        self._h = lib().orc_ode_create(prec, C.addressof(self._cp), neq, method, order)
+        if not self._h:
+            raise OracleError(lib().orc_last_error().decode())
+        self.neq = neq
+
+    def integrate(self, u: np.ndarray, t: float, tout: float, dt: float, itask: int = 1) -> float:
+        assert u.dtype == np.float64 and u.flags.c_contiguous and u.size == self.neq
+        tt = C.c_double(t)
+        lib().orc_ode_integrate(self._h, _p(u), C.byref(tt), tout, dt, itask)
+        return tt.value
+
+    def info(self):
+        fe, st, ns = C.c_int(), C.c_int(), C.c_longlong()
+        lib().orc_ode_info(self._h, C.byref(fe), C.byref(st), C.byref(ns))
+        return fe.value, st.value, ns.value
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.orc_ode_destroy(self._h)
+            self._h = None

@@ -1,0 +1,81 @@
+"""Oracle properties the reference's semantics imply (CPU only)."""
+import numpy as np
+import pytest
+
+from hrweno.problems import burgers_1d, linear_ode, pbe_2d
+
+
+def config1_u0(nc=500):
+    x = -5.0 + (10.0 / nc) * (np.arange(nc) + 0.5)
+    return np.exp(-x ** 2)
+
+
+def test_config1_step_count_and_time(orc):
+    """101 output times to t=12 with dt=1e-2: 1201 steps, t ends at 12.009999999999788
+    (is_done overshoot, src/hrweno_tvdode.f90:127,137-143,282)."""
+    nc = 500
+    prob = burgers_1d(nc, k=3, alpha=1.0)
+    ode = orc.ODE(prob, nc, method=0, order=3)
+    u, t = config1_u0(nc), 0.0
+    for ii in range(101):
+        t = ode.integrate(u, t, 12.0 * ii / 100, 1e-2)
+    fe, st, ns = ode.info()
+    assert ns == 1201 and fe == 3 * 1201 and st == 2
+    assert t == 12.009999999999788
+
+
+def test_quad_yardstick_config1(orc):
+    """REAL64 oracle vs the REAL128 yardstick on the 500-cell shock case: the rounding-level
+    sensitivity of the problem, which sets the scale of the 1e-12 parity tolerance."""
+    nc = 500
+    prob = burgers_1d(nc, k=3, alpha=1.0)
+    res = {}
+    for prec in (64, 128):
+        ode = orc.ODE(prob, nc, method=0, order=3, prec=prec)
+        u = config1_u0(nc)
+        ode.integrate(u, 0.0, 3.0, 1e-2)
+        res[prec] = u
+    err = np.max(np.abs(res[64] - res[128])) / np.max(np.abs(res[128]))
+    assert err < 1e-13, err
+
+
+def test_conservation_zero_bc(orc):
+    """With zero boundary fluxes the FV update conserves sum(u * width) to rounding."""
+    nc = 200
+    prob = burgers_1d(nc, k=3, alpha=1.5, bc="zero", flux="godunov")
+    ode = orc.ODE(prob, nc, method=0, order=3)
+    u = 0.5 + config1_u0(nc)
+    m0 = u.sum()
+    ode.integrate(u, 0.0, 1.0, 1e-2)
+    assert abs(u.sum() - m0) <= 1e-12 * m0
+
+
+def test_mstvd_fevals(orc):
+    """mstvd counts the start's 12 RK3 evaluations, not the 4 extra rhs calls (:246)."""
+    ode = orc.ODE(linear_ode(np.ones(3)), 3, method=1)
+    u = np.ones(3)
+    t = ode.integrate(u, 0.0, 0.1, 0.01)
+    fe, st, ns = ode.info()
+    assert st == 2
+    # start: 4 steps to t=0.04; then steps while not is_done: t = 0.05 ... 0.11
+    assert fe == 12 + (ns - 4)
+
+
+def test_pbe2d_rhs_linear_in_n(orc):
+    """The upwind 2D right-hand side is homogeneous of degree 1 in n (WENO weights are
+    scale-invariant only up to eps, so use a scale where eps is negligible)."""
+    n1 = n2 = 24
+    prob = pbe_2d(n1, n2, flux="godunov", bc="zero_inflow")
+    rng = np.random.default_rng(1)
+    v = rng.uniform(1e4, 2e4, n1 * n2)  # beta >> eps
+    a = orc.rhs(prob, v)
+    b = orc.rhs(prob, 2.0 * v)
+    np.testing.assert_allclose(b, 2.0 * a, rtol=1e-8, atol=1e-8 * np.abs(a).max())
+
+
+@pytest.mark.parametrize("k", [1, 2, 3])
+def test_reconstruct_constant_state(orc, k):
+    v = np.full(17, 0.3)
+    vl, vr = orc.reconstruct(v, k=k)
+    assert np.all(vl == 0.3) or np.allclose(vl, 0.3, rtol=1e-15)
+    assert np.allclose(vr, 0.3, rtol=1e-15)
