@@ -1,0 +1,351 @@
+#!/usr/bin/env python
+"""Benchmark of the fused WENO5 / Lax-Friedrichs / RK3 stage path on one GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload: 1D inviscid Burgers on 2^24 uniform cells of [-5, 5], u0 a seeded sum of 8
+Gaussians, WENO5 (k = 3, eps = 1e-6), global Lax-Friedrichs flux with alpha = max|u0|, copy
+boundaries, rktvd order 3, CFL 0.4.  One step is one RK3 time step over the whole line
+(three fused stage kernels); the metric is cell-updates per second, one cell-update being
+one cell advanced one full RK3 step.
+
+`value` times K steps on device-resident data with CUDA events on the library's stream.
+`e2e` times K calls of the reference-facing integrate(u, t, tout, dt, itask=2) with u in
+pinned host memory: each call copies u to the device, takes one step and copies u back.
+`--impl reference` times the CPU restatement of the reference (oracle/, all host threads,
+bit-identical results for any thread count) on the same workload.
+
+Under torchrun (N > 1) every rank integrates its own replica of the line (replicas only:
+the single-line path has no exchange step here); value = all ranks' cell-updates / the
+slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+for p in (ROOT, ROOT / "hr-weno_gb300"):
+    if str(p) not in sys.path:
+        sys.path.insert(0, str(p))
+
+METRIC = "WENO5-RK3 cell-updates/s & HBM-roofline %; batched/FP32/adjoint vs plain FP64"
+UNIT = "cell-updates/s"
+NC = 1 << 24
+# algorithmic HBM bytes of one FP64 RK3 cell-update: stage 1 reads u, writes u1 (16 B);
+# stage 2 reads u, u1, writes u2 (24 B); stage 3 reads u, u2, writes u (24 B)
+BYTES_PER_CELL_UPDATE = 64
+LAUNCHES_PER_STEP = 3
+L2_BYTES = 126 * 1024 * 1024
+
+# DRAM bytes per cell and stage launch of the FP64 stage kernel, measured by ncu
+# (dram__bytes_read.sum + dram__bytes_write.sum over the three RK3 stage launches of one
+# step of the 2^24-cell line, divided by cells x 3); profiles/stage1d_fp64_weno5_rk3.md.
+NCU_DRAM_BYTES_PER_CELL_LAUNCH = 943.8e6 / (3 * (1 << 24))
+# FP64 pipe utilisation of the same capture (sm__inst_executed_pipe_fp64, % of peak active)
+NCU_FP64_PIPE_PCT = 85.7
+
+
+def peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return {"hbm_gbs": float(d["hbm_gbs"]), "src": "measured"}
+    return {"hbm_gbs": 6800.0, "src": "fallback"}
+
+
+# ------------------------------------------------------------------------------------------
+# clocks during the timed region
+# ------------------------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    NAMES = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200", "-i", str(self.device)],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, ValueError):
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        self.out = ""
+        if self.proc is not None:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                self.out, _ = self.proc.communicate()
+
+    def summary(self):
+        rows = []
+        for line in (self.out or "").splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                rows.append((float(f[1]), float(f[2]), f[5:9]))
+            except ValueError:
+                continue
+        if not rows:
+            return None
+        reasons = set()
+        for _, _, flags in rows:
+            for name, flag in zip(self.NAMES, flags):
+                if flag.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(r[0] for r in rows),
+                "sm_max_mhz": max(r[1] for r in rows), "samples": len(rows),
+                "reasons": sorted(reasons)}
+
+
+# ------------------------------------------------------------------------------------------
+# distributed plumbing (replicas)
+# ------------------------------------------------------------------------------------------
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch
+            import torch.distributed as dist
+            backend = "nccl" if torch.cuda.is_available() else "gloo"
+            if backend == "nccl":
+                torch.cuda.set_device(self.local)
+            dist.init_process_group(backend)
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg is not None:
+            self.pg.barrier()
+
+    def max(self, x: float) -> float:
+        if self.pg is None:
+            return x
+        import torch
+        dev = "cuda" if torch.cuda.is_available() else "cpu"
+        t = torch.tensor([x], dtype=torch.float64, device=dev)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg is not None:
+            self.pg.destroy_process_group()
+
+
+# ------------------------------------------------------------------------------------------
+# CPU: the oracle (restatement of the reference), bounded sample
+# ------------------------------------------------------------------------------------------
+def cpu_rate(u0: np.ndarray, prob, dt: float, steps: int, threads: int):
+    """cell-updates/s of the oracle over `steps` RK3 steps of the full line."""
+    from oracle import oracle
+    used = oracle.set_threads(threads)
+    ode = oracle.ODE(prob, u0.size, 0, 3)
+    u = u0.copy()
+    t0 = time.perf_counter()
+    ode.integrate(u, 0.0, (steps - 0.5) * dt, dt)
+    el = time.perf_counter() - t0
+    assert ode.info()[2] == steps
+    return u0.size * steps / el, el, used
+
+
+def run_reference(args) -> None:
+    from hrweno import workloads
+    prob, u0, dt = workloads.large_burgers(NC, k=3)
+    threads = os.cpu_count() or 1
+    # warm-up (page-in, thread pool), then K steps each timed as one bounded sample
+    _, el1, used = cpu_rate(u0, prob, dt, 1, threads)
+    for _ in range(max(args.warmup - 1, 0)):
+        cpu_rate(u0, prob, dt, 1, threads)
+    # keep the run to a few minutes: cells of each step's sample scale down if needed
+    budget_s = 150.0
+    n = NC
+    while n > (1 << 16) and el1 * (n / NC) * args.steps > budget_s:
+        n //= 2
+    if n != NC:
+        prob, u0s, dt = workloads.large_burgers(n, k=3, u0=u0[:: NC // n].copy())
+    else:
+        u0s = u0
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        cpu_rate(u0s, prob, dt, 1, threads)
+    el = time.perf_counter() - t0
+    v = n * args.steps / el
+    sample = (f"{args.steps} RK3 steps, each one step over {n} cells"
+              + (" (a strided sub-line of the 2^24-cell line)" if n != NC else " (the full line)"))
+    line = {
+        "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic: seeded 8-Gaussian u0 (numpy default_rng(1))",
+        "config": config_dict(), "impl": "reference",
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": used, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def config_dict() -> dict:
+    return {"workload": "burgers1d_2^24_weno5_lf_rk3", "cells": NC, "k": 3, "eps": 1e-6,
+            "flux": "lax_friedrichs", "alpha": "max|u0|", "bc": "copy", "cfl": 0.4,
+            "integrator": "rktvd order 3", "numerics": "fast",
+            "l2": "inputs larger than L2: u, u1, u2 are 128 MiB each (384 MiB working set)"}
+
+
+# ------------------------------------------------------------------------------------------
+# GPU arm
+# ------------------------------------------------------------------------------------------
+def run_ours(args, dist: Dist) -> None:
+    import torch
+
+    import hrweno
+    from hrweno import workloads
+
+    dev = dist.local if dist.world > 1 else 0
+    torch.cuda.set_device(dev)
+    prob, u0, dt = workloads.large_burgers(NC, k=3)
+    stream = torch.cuda.Stream()
+
+    # ---- device-resident K steps ---------------------------------------------------------
+    ode = hrweno.rktvd(prob, NC, 3)
+    ode.set_stream(stream.cuda_stream)
+    u = torch.from_numpy(u0).cuda()
+    t = ode.integrate(u, 0.0, (args.warmup - 0.5) * dt, dt)
+    torch.cuda.synchronize()
+    n0 = ode.nsteps
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(dev) as clk:
+        e0.record(stream)
+        t = ode.integrate(u, t, t + (args.steps - 0.5) * dt, dt)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    dist.barrier()
+    steps_done = ode.nsteps - n0
+    assert steps_done == args.steps, (steps_done, args.steps)
+    el = dist.max(e0.elapsed_time(e1) * 1e-3)
+    value = dist.world * NC * args.steps / el
+    assert bool(torch.isfinite(u).all())
+
+    # ---- e2e: reference-facing call on pinned host memory, one step per call -------------
+    ode2 = hrweno.rktvd(prob, NC, 3)
+    ode2.set_stream(stream.cuda_stream)
+    uh = torch.from_numpy(u0.copy()).pin_memory()
+    th = 0.0
+    for _ in range(max(1, min(args.warmup, 3))):
+        th = ode2.integrate(uh, th, th + 0.5 * dt, dt, itask=2)
+    dist.barrier()
+    torch.cuda.synchronize()
+    h0 = time.perf_counter()
+    for _ in range(args.steps):
+        th = ode2.integrate(uh, th, th + 0.5 * dt, dt, itask=2)
+    torch.cuda.synchronize()
+    e2e_el = dist.max(time.perf_counter() - h0)
+    dist.barrier()
+    e2e = {"value": dist.world * NC * args.steps / e2e_el, "unit": UNIT,
+           "h2d_bytes_per_step": 8 * NC, "d2h_bytes_per_step": 8 * NC}
+
+    if dist.rank != 0:
+        return
+
+    pk = peaks()
+    launch_s = el / (args.steps * LAUNCHES_PER_STEP)
+    bytes_per_launch = BYTES_PER_CELL_UPDATE * NC / LAUNCHES_PER_STEP
+    achieved = bytes_per_launch / launch_s / 1e9
+    traffic = (None if NCU_DRAM_BYTES_PER_CELL_LAUNCH is None
+               else NCU_DRAM_BYTES_PER_CELL_LAUNCH * NC)
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                "frac": achieved / pk["hbm_gbs"], "traffic": traffic,
+                "peak_src": f"{pk['src']} (MEASURED_PEAKS.json hbm_gbs)" if pk["src"] == "measured"
+                else "fallback 6.8 TB/s"}
+    # the FP64 pipe bounds this kernel on GB300 (FP64 is 1/64 of the FP32 rate)
+    dfma = ffma = None
+    try:
+        import ctypes as C
+        d, f = C.c_double(), C.c_double()
+        L = hrweno.lib()
+        L.hrw_diag_fma_rates.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        if L.hrw_diag_fma_rates(C.byref(d), C.byref(f)) == 0:
+            dfma, ffma = d.value, f.value
+    except Exception:  # diagnostics only
+        pass
+
+    # ---- CPU baseline: the oracle, 1 core, bounded sample ----------------------------------
+    cpu = None
+    if not args.no_cpu:
+        steps = 3
+        v, el_cpu, used = cpu_rate(u0, prob, dt, steps, 1)
+        cpu = {"value": v, "unit": UNIT, "cores": used, "kind": "port",
+               "sample": f"{steps} RK3 steps of the full 2^24-cell line ({el_cpu:.1f} s), "
+                         f"oracle restatement, -O2, 1 thread; host has {os.cpu_count()} cores"}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic: seeded 8-Gaussian u0 (numpy default_rng(1))",
+        "config": config_dict(),
+        "roofline": roofline,
+        "fp64_pipe": {"bound": "fp64", "ncu_pct_of_peak": NCU_FP64_PIPE_PCT,
+                      "dfma_per_s_measured": dfma, "ffma_per_s_measured": ffma},
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "gpu_launches": steps_done * LAUNCHES_PER_STEP,
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main() -> None:
+    global NC
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--cells", type=int, default=NC,
+                    help="cells of the line (default 2^24, the benchmark workload; smaller "
+                         "lines are for profiler captures)")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    NC = args.cells
+    if args.impl == "reference":
+        # CPU arm: rank 0 alone runs; no process group is needed
+        if int(os.environ.get("RANK", "0")) == 0:
+            run_reference(args)
+        return
+    dist = Dist()
+    try:
+        run_ours(args, dist)
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    main()

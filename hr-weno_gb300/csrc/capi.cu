@@ -307,6 +307,8 @@ static int ode_create(const hrw_problem* p, int neq, int order, int method, int 
       }
     }
     b.ld = p->ncells[0];
+    b.upwind = nd == 2 && p->flux == HRW_FLUX_GODUNOV && positive_velocity(b.L) &&
+               positive_velocity(b.L2);
   }
   if ((e = cudaMalloc(&o->u, bytes)) != cudaSuccess) return cleanup(e);
   if ((e = cudaMalloc(&o->w1, bytes)) != cudaSuccess) return cleanup(e);

@@ -146,11 +146,16 @@ template <int K> struct FastGuard;
 template <> struct FastGuard<3> { static constexpr int hi_max = (1023 + 240) << 20; };
 template <> struct FastGuard<2> { static constexpr int hi_max = (1023 + 480) << 20; };
 
-template <int K, int C>
+// WL = false computes vr only (vl is left untouched): the upwind flux of a positive velocity
+// needs the left state of each interface alone.
+template <int K, int C, bool WL = true>
 __device__ __forceinline__ void recon_fast(const double* w, double eps, double* vl, double* vr) {
   if constexpr (K == 1) {
 #pragma unroll
-    for (int c = 0; c < C; ++c) { vl[c] = w[1 + c]; vr[c] = w[1 + c]; }
+    for (int c = 0; c < C; ++c) {
+      if constexpr (WL) vl[c] = w[1 + c];
+      vr[c] = w[1 + c];
+    }
   } else if constexpr (K == 2) {
     // V0 = 2 vrr0 = v0 + v1, V1 = 2 vrr1 = 3 v0 - v-1, W0 = 2 vlr0 = 3 v0 - v1,
     // W1 = 2 vlr1 = v-1 + v0 = V0 of the previous cell; beta1 = beta0 of the previous cell.
@@ -174,12 +179,16 @@ __device__ __forceinline__ void recon_fast(const double* w, double eps, double* 
       const double num = fma(s1x2, V0, s0 * V1);
       const double numt = fma(s1, W0, s0x2 * W1);
       if (max(hiword(s0), hiword(s1)) < FastGuard<2>::hi_max) {
-        const double R = rcp_fast((den + den) * dent);
-        vr[c] = num * (dent * R);
-        vl[c] = numt * (den * R);
+        if constexpr (WL) {
+          const double R = rcp_fast((den + den) * dent);
+          vr[c] = num * (dent * R);
+          vl[c] = numt * (den * R);
+        } else {
+          vr[c] = num * rcp_fast(den + den);
+        }
       } else {
         const double2 g = recon_guarded<2>(0.0, w[q - 1], w[q], w[q + 1], 0.0, eps);
-        vl[c] = g.x;
+        if constexpr (WL) vl[c] = g.x;
         vr[c] = g.y;
       }
       V0p = V0;
@@ -223,13 +232,17 @@ __device__ __forceinline__ void recon_fast(const double* w, double eps, double* 
         const double den = (Q1 + P2) + T0;   // d = (3, 6, 1)/10
         const double dent = (Q1 + P0) + T2;  // d mirrored = (1, 6, 3)/10
         const double num = fma(T0, V0, fma(Q1, V1, P2 * V2));
-        const double numt = fma(T2, W2, fma(Q1, W1, P0 * W0));
-        const double R = rcp_fast((6.0 * den) * dent);
-        vr[c] = num * (dent * R);
-        vl[c] = numt * (den * R);
+        if constexpr (WL) {
+          const double numt = fma(T2, W2, fma(Q1, W1, P0 * W0));
+          const double R = rcp_fast((6.0 * den) * dent);
+          vr[c] = num * (dent * R);
+          vl[c] = numt * (den * R);
+        } else {
+          vr[c] = num * rcp_fast(6.0 * den);
+        }
       } else {
         const double2 g = recon_guarded<3>(w[q - 2], w[q - 1], w[q], w[q + 1], w[q + 2], eps);
-        vl[c] = g.x;
+        if constexpr (WL) vl[c] = g.x;
         vr[c] = g.y;
       }
       V0p = V0;
@@ -238,21 +251,33 @@ __device__ __forceinline__ void recon_fast(const double* w, double eps, double* 
   }
 }
 
-// single cell, no neighbour sharing (block-edge cells).  Reads p[-(K-1)] .. p[K-1] only; the
-// two outermost window slots, which a single cell does not use, repeat the nearest value.
+// single cell, no neighbour sharing (block-edge cells).  Reads p[o * stride] for
+// o = -(K-1) .. K-1 only; the two outermost window slots, which a single cell does not use,
+// repeat the nearest value.
 template <int K>
-__device__ __forceinline__ void recon_fast_one(const double* p, double eps, double& vl, double& vr) {
+__device__ __forceinline__ void recon_fast_one(const double* p, double eps, double& vl, double& vr,
+                                               int stride = 1) {
   double w[1 + 2 * K];
 #pragma unroll
   for (int q = 0; q < 1 + 2 * K; ++q) {
     int o = q - K;
     o = o < -(K - 1) ? -(K - 1) : (o > K - 1 ? K - 1 : o);
-    w[q] = p[o];
+    w[q] = p[o * stride];
   }
   double l[1], r[1];
   recon_fast<K, 1>(w, eps, l, r);
   vl = l[0];
   vr = r[0];
+}
+
+// STRICT single cell with a stride: gathers p[o * stride] and runs the reference order.
+template <int K>
+__device__ __forceinline__ void recon_strict_strided(const double* p, int stride, double eps,
+                                                     double& vl, double& vr) {
+  double w[2 * K - 1];
+#pragma unroll
+  for (int q = 0; q < 2 * K - 1; ++q) w[q] = p[(q - (K - 1)) * stride];
+  recon_strict<K>(w + (K - 1), eps, vl, vr);
 }
 
 }  // namespace hrw

@@ -45,10 +45,13 @@ struct StageArgs {
   // 2D only
   LineArgs L2;
   int64_t ld;         // row stride (nc1) of the 2D layout
+  int upwind;         // Godunov flux of g(x) u with g > 0 everywhere: F = g vm (2D kernel)
 };
 
 // FAST flux form: the kernels evaluate F / fscale, fscale folded into rws.
 double fast_flux_scale(int flux, int fn);
+// True when the line's flux is g(x) u with g > 0 at every interface (upwind Godunov).
+bool positive_velocity(const LineArgs& L);
 
 // 1D fused stage over nc cells; k in 1..3; strict selects the reference-order numerics.
 cudaError_t launch_stage1d(const StageArgs& a, int k, int stage, bool strict, cudaStream_t s);

@@ -1,0 +1,153 @@
+// hrw_stage.cuh - numerical fluxes and TVD stage combines shared by the 1D and 2D fused
+// stage kernels.
+//
+//   lax_friedrichs / godunov    src/hrweno_fluxes.f90:22-76 (formulas :43, :67-74)
+//   physical fluxes             example/example1_burgers_1d_fv.f90:111-122 (u^2/2),
+//                               example/example2_pbe_2d_fv.f90:131-155 (g(x) u)
+//   rktvd / mstvd stage update  src/hrweno_tvdode.f90:139-167,257
+#pragma once
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+#include "../../include/hrweno_gpu.h"
+#include "hrw_internal.h"
+
+namespace hrw {
+
+// --------------------------------------------------------------------------------------------
+// Numerical fluxes.  e = edge index of the interface (x = xmin + rx*e, grid1%right).
+// --------------------------------------------------------------------------------------------
+__device__ __forceinline__ double g_fast(const LineArgs& L, int64_t e) {
+  return L.b != 0.0 ? fma(L.b, fma(L.rx, (double)e, L.xmin), L.a) : L.a;
+}
+
+// FAST: returns F / fast_flux_scale(flux, fn).
+__device__ __forceinline__ double flux_fast(const LineArgs& L, double vm, double vp, int64_t e) {
+  if (L.fn == HRW_FN_BURGERS) {
+    if (L.flux == HRW_FLUX_LAX_FRIEDRICHS)  // 4F = vm^2 + vp^2 - 2 alpha (vp - vm)
+      return fma(-2.0 * L.alpha, vp - vm, fma(vp, vp, vm * vm));
+    const double fm = vm * vm, fp = vp * vp;  // 2F
+    return vm <= vp ? fmin(fm, fp) : fmax(fm, fp);
+  }
+  const double g = g_fast(L, e);
+  if (L.flux == HRW_FLUX_LAX_FRIEDRICHS)  // 2F = (g + alpha) vm + (g - alpha) vp
+    return fma(g + L.alpha, vm, (g - L.alpha) * vp);
+  const double fm = g * vm, fp = g * vp;  // F
+  return vm <= vp ? fmin(fm, fp) : fmax(fm, fp);
+}
+// FAST physical flux f(v) at edge e, same scaling as flux_fast.
+__device__ __forceinline__ double phys_fast(const LineArgs& L, double v, int64_t e) {
+  const double s = L.flux == HRW_FLUX_LAX_FRIEDRICHS ? 2.0 : 1.0;
+  if (L.fn == HRW_FN_BURGERS) return s * (v * v);
+  return s * (g_fast(L, e) * v);
+}
+
+// STRICT: reference order (src/hrweno_fluxes.f90:43,67-74; example1...f90:111-122).
+__device__ __forceinline__ double g_strict(const LineArgs& L, int64_t e) {
+  const double x = __dadd_rn(L.xmin, __dmul_rn(L.rx, (double)e));
+  return __dadd_rn(L.a, __dmul_rn(L.b, x));
+}
+__device__ __forceinline__ double phys_strict(const LineArgs& L, double v, int64_t e) {
+  if (L.fn == HRW_FN_BURGERS) return __ddiv_rn(__dmul_rn(v, v), 2.0);
+  return __dmul_rn(g_strict(L, e), v);
+}
+__device__ __forceinline__ double flux_strict(const LineArgs& L, double vm, double vp, int64_t e) {
+  const double fm = phys_strict(L, vm, e), fp = phys_strict(L, vp, e);
+  if (L.flux == HRW_FLUX_LAX_FRIEDRICHS)
+    return __ddiv_rn(__dsub_rn(__dadd_rn(fm, fp), __dmul_rn(L.alpha, __dsub_rn(vp, vm))), 2.0);
+  if (vm <= vp) return fm < fp ? fm : fp;
+  return fm > fp ? fm : fp;
+}
+
+template <bool STRICT>
+__device__ __forceinline__ double numflux(const LineArgs& L, double vm, double vp, int64_t e) {
+  if constexpr (STRICT) return flux_strict(L, vm, vp, e);
+  else return flux_fast(L, vm, vp, e);
+}
+template <bool STRICT>
+__device__ __forceinline__ double physflux(const LineArgs& L, double v, int64_t e) {
+  if constexpr (STRICT) return phys_strict(L, v, e);
+  else return phys_fast(L, v, e);
+}
+
+// Godunov flux of f = g(x) u with g > 0 on the whole line is g vm (upwind).  For g > 0 and
+// vm <= vp, rounding is monotone so fl(g vm) <= fl(g vp) and min() picks fl(g vm); for
+// vm > vp max() picks it too: the result is bit-identical to numflux<STRICT>() and needs
+// only the left state.
+template <bool STRICT>
+__device__ __forceinline__ double upwind_flux(const LineArgs& L, double vm, int64_t e) {
+  if constexpr (STRICT) return __dmul_rn(g_strict(L, e), vm);
+  else return g_fast(L, e) * vm;
+}
+
+// Flux difference dF = F_{j+1/2} - F_{j-1/2} of cell j with the domain-boundary fluxes:
+//   COPY        F_{1/2} = F_{3/2}, F_{nc+1/2} = F_{nc-1/2}  (example1...f90:103-104)
+//   ZERO        F_{1/2} = F_{nc+1/2} = 0                    (example2...f90:117-120)
+//   ZERO_INFLOW F_{1/2} = 0, F_{nc+1/2} = f(vr(nc))
+template <bool STRICT>
+__device__ __forceinline__ double flux_diff(const LineArgs& L, int64_t j, double FL, double FR,
+                                            double vr_j) {
+  if (j == 0 || j == L.nc - 1) {
+    if (L.bc == HRW_BC_COPY) {
+      FL = FR = 0.0;
+    } else {
+      if (j == 0) FL = 0.0;
+      if (j == L.nc - 1) FR = L.bc == HRW_BC_ZERO ? 0.0 : physflux<STRICT>(L, vr_j, j + 1);
+    }
+  }
+  if constexpr (STRICT) return __dsub_rn(FR, FL);
+  else return FR - FL;
+}
+
+// --------------------------------------------------------------------------------------------
+// Stage combines of cell j.
+// STRICT: udot is the exact right-hand side value, reference order.
+// FAST:   q = sum over dimensions of rws * dF (= -udot), or for 1D dF and rws separately.
+// --------------------------------------------------------------------------------------------
+template <int ST>
+__device__ __forceinline__ void combine_strict(const StageArgs& a, int64_t j, double v, double udot) {
+  const double dt = a.dt;
+  if constexpr (ST == ST_RHS) {
+    a.out[j] = udot;
+  } else if constexpr (ST == ST_EULER) {  // ui = u + dt*udot  (:139,150,163)
+    a.out[j] = __dadd_rn(v, __dmul_rn(dt, udot));
+  } else if constexpr (ST == ST_RK2B) {  // u = (u + ui + dt*udot)/2  (:152)
+    a.out[j] = __ddiv_rn(__dadd_rn(__dadd_rn(a.u[j], v), __dmul_rn(dt, udot)), 2.0);
+  } else if constexpr (ST == ST_RK3B) {  // ui = (3*u + ui + dt*udot)/4  (:165)
+    a.out[j] = __ddiv_rn(__dadd_rn(__dadd_rn(__dmul_rn(3.0, a.u[j]), v), __dmul_rn(dt, udot)), 4.0);
+  } else if constexpr (ST == ST_RK3C) {  // u = (u + 2*ui + 2*dt*udot)/3  (:167)
+    a.out[j] = __ddiv_rn(
+        __dadd_rn(__dadd_rn(a.u[j], __dmul_rn(2.0, v)), __dmul_rn(__dmul_rn(2.0, dt), udot)), 3.0);
+  } else if constexpr (ST == ST_MS) {  // (25u + 50dt udot + 7 uold4 + 10dt udotold4)/32  (:257)
+    const double t1 = __dadd_rn(__dmul_rn(25.0, v), __dmul_rn(__dmul_rn(50.0, dt), udot));
+    const double t2 = __dadd_rn(t1, __dmul_rn(7.0, a.uo4[j]));
+    a.out[j] = __ddiv_rn(__dadd_rn(t2, __dmul_rn(__dmul_rn(10.0, dt), a.lo4[j])), 32.0);
+    a.lout[j] = udot;
+  }
+}
+
+// out from v and q = rws * dF (rws passed separately so that 1D folds it into dt)
+template <int ST>
+__device__ __forceinline__ void combine_fast(const StageArgs& a, int64_t j, double v, double dF,
+                                             double rws) {
+  if constexpr (ST == ST_RHS) {
+    a.out[j] = -(rws * dF);
+  } else if constexpr (ST == ST_EULER) {
+    a.out[j] = fma(-a.dt * rws, dF, v);
+  } else if constexpr (ST == ST_RK2B) {
+    a.out[j] = fma(0.5, a.u[j], fma(0.5, v, (-0.5 * a.dt * rws) * dF));
+  } else if constexpr (ST == ST_RK3B) {
+    a.out[j] = fma(0.75, a.u[j], fma(0.25, v, (-0.25 * a.dt * rws) * dF));
+  } else if constexpr (ST == ST_RK3C) {
+    a.out[j] = fma(1.0 / 3.0, a.u[j], fma(2.0 / 3.0, v, (-(2.0 / 3.0) * a.dt * rws) * dF));
+  } else if constexpr (ST == ST_MS) {
+    const double udot = -(rws * dF);
+    a.out[j] = fma(25.0 / 32.0, v,
+                   fma((50.0 / 32.0) * a.dt, udot,
+                       fma(7.0 / 32.0, a.uo4[j], ((10.0 / 32.0) * a.dt) * a.lo4[j])));
+    a.lout[j] = udot;
+  }
+}
+
+}  // namespace hrw

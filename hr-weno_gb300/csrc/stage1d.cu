@@ -13,11 +13,14 @@
 // window; the two block-edge cells whose reconstruction the neighbouring tiles own are
 // recomputed by two lanes.  Fluxes at the thread's C+1 interfaces use the neighbours'
 // edge values through shared memory, then each cell's update is written once.
+#include <cmath>
+
 #include <cuda_runtime.h>
 
 #include "../../include/hrweno_gpu.h"
 #include "hrw_device.cuh"
 #include "hrw_internal.h"
+#include "hrw_stage.cuh"
 
 namespace hrw {
 
@@ -26,104 +29,28 @@ double fast_flux_scale(int flux, int fn) {
   return fn == HRW_FN_BURGERS ? 0.5 : 1.0;
 }
 
-// --------------------------------------------------------------------------------------------
-// Numerical fluxes.  e = edge index of the interface (x = xmin + rx*e, grid1%right).
-// --------------------------------------------------------------------------------------------
-// FAST: returns F / fast_flux_scale(flux, fn).
-__device__ __forceinline__ double flux_fast(const LineArgs& L, double vm, double vp, int64_t e) {
-  if (L.fn == HRW_FN_BURGERS) {
-    if (L.flux == HRW_FLUX_LAX_FRIEDRICHS)  // 4F = vm^2 + vp^2 - 2 alpha (vp - vm)
-      return fma(-2.0 * L.alpha, vp - vm, fma(vp, vp, vm * vm));
-    const double fm = vm * vm, fp = vp * vp;  // 2F
-    return vm <= vp ? fmin(fm, fp) : fmax(fm, fp);
+bool positive_velocity(const LineArgs& L) {
+  if (L.fn != HRW_FN_LINEAR) return false;
+  // g(x_e) = a + b*(xmin + rx*e) is monotone in e under any rounding of its three operations,
+  // so its minimum over the interfaces e = 0..nc sits at an end; the margin stays far above
+  // the rounding differences between the host and the device evaluation orders
+  for (int64_t e : {(int64_t)0, (int64_t)L.nc}) {
+    const double x = L.xmin + L.rx * (double)e;
+    const double g = L.a + L.b * x;
+    if (!(g > 1e-12 * (std::fabs(L.a) + std::fabs(L.b * x)))) return false;
   }
-  double g = L.a;
-  if (L.b != 0.0) g = fma(L.b, fma(L.rx, (double)e, L.xmin), L.a);
-  if (L.flux == HRW_FLUX_LAX_FRIEDRICHS)  // 2F = (g + alpha) vm + (g - alpha) vp
-    return fma(g + L.alpha, vm, (g - L.alpha) * vp);
-  const double fm = g * vm, fp = g * vp;  // F
-  return vm <= vp ? fmin(fm, fp) : fmax(fm, fp);
-}
-// FAST physical flux f(v) at edge e, same scaling as flux_fast.
-__device__ __forceinline__ double phys_fast(const LineArgs& L, double v, int64_t e) {
-  const double s = L.flux == HRW_FLUX_LAX_FRIEDRICHS ? 2.0 : 1.0;
-  if (L.fn == HRW_FN_BURGERS) return s * (v * v);
-  double g = L.a;
-  if (L.b != 0.0) g = fma(L.b, fma(L.rx, (double)e, L.xmin), L.a);
-  return s * (g * v);
+  return true;
 }
 
-// STRICT: reference order (src/hrweno_fluxes.f90:43,67-74; example1...f90:111-122).
-__device__ __forceinline__ double phys_strict(const LineArgs& L, double v, int64_t e) {
-  if (L.fn == HRW_FN_BURGERS) return __ddiv_rn(__dmul_rn(v, v), 2.0);
-  const double x = __dadd_rn(L.xmin, __dmul_rn(L.rx, (double)e));
-  return __dmul_rn(__dadd_rn(L.a, __dmul_rn(L.b, x)), v);
-}
-__device__ __forceinline__ double flux_strict(const LineArgs& L, double vm, double vp, int64_t e) {
-  const double fm = phys_strict(L, vm, e), fp = phys_strict(L, vp, e);
-  if (L.flux == HRW_FLUX_LAX_FRIEDRICHS)
-    return __ddiv_rn(__dsub_rn(__dadd_rn(fm, fp), __dmul_rn(L.alpha, __dsub_rn(vp, vm))), 2.0);
-  if (vm <= vp) return fm < fp ? fm : fp;
-  return fm > fp ? fm : fp;
-}
-
-template <bool STRICT>
-__device__ __forceinline__ double numflux(const LineArgs& L, double vm, double vp, int64_t e) {
-  if constexpr (STRICT) return flux_strict(L, vm, vp, e);
-  else return flux_fast(L, vm, vp, e);
-}
-template <bool STRICT>
-__device__ __forceinline__ double physflux(const LineArgs& L, double v, int64_t e) {
-  if constexpr (STRICT) return phys_strict(L, v, e);
-  else return phys_fast(L, v, e);
-}
-
-// --------------------------------------------------------------------------------------------
 // Stage combine for cell j.  dF = F_{j+1/2} - F_{j-1/2} in the flux form of the mode.
-// --------------------------------------------------------------------------------------------
 template <int ST, bool STRICT>
 __device__ __forceinline__ void combine(const StageArgs& a, const LineArgs& L, int64_t j,
                                         double v, double dF) {
   if constexpr (STRICT) {
     const double w = L.width ? L.width[j] : L.rx;
-    const double udot = __ddiv_rn(-dF, w);  // vdot = -(F_i - F_{i-1})/width  (example1:107)
-    const double dt = a.dt;
-    if constexpr (ST == ST_RHS) {
-      a.out[j] = udot;
-    } else if constexpr (ST == ST_EULER) {
-      a.out[j] = __dadd_rn(v, __dmul_rn(dt, udot));
-    } else if constexpr (ST == ST_RK2B) {
-      a.out[j] = __ddiv_rn(__dadd_rn(__dadd_rn(a.u[j], v), __dmul_rn(dt, udot)), 2.0);
-    } else if constexpr (ST == ST_RK3B) {
-      a.out[j] = __ddiv_rn(__dadd_rn(__dadd_rn(__dmul_rn(3.0, a.u[j]), v), __dmul_rn(dt, udot)), 4.0);
-    } else if constexpr (ST == ST_RK3C) {
-      a.out[j] = __ddiv_rn(
-          __dadd_rn(__dadd_rn(a.u[j], __dmul_rn(2.0, v)), __dmul_rn(__dmul_rn(2.0, dt), udot)), 3.0);
-    } else if constexpr (ST == ST_MS) {
-      const double t1 = __dadd_rn(__dmul_rn(25.0, v), __dmul_rn(__dmul_rn(50.0, dt), udot));
-      const double t2 = __dadd_rn(t1, __dmul_rn(7.0, a.uo4[j]));
-      a.out[j] = __ddiv_rn(__dadd_rn(t2, __dmul_rn(__dmul_rn(10.0, dt), a.lo4[j])), 32.0);
-      a.lout[j] = udot;
-    }
+    combine_strict<ST>(a, j, v, __ddiv_rn(-dF, w));  // vdot = -(F_i - F_{i-1})/width (ex1:107)
   } else {
-    const double rws = L.rws ? L.rws[j] : L.rws0;
-    if constexpr (ST == ST_RHS) {
-      a.out[j] = -(rws * dF);
-    } else if constexpr (ST == ST_EULER) {
-      a.out[j] = fma(-a.dt * rws, dF, v);
-    } else if constexpr (ST == ST_RK2B) {
-      a.out[j] = fma(0.5, a.u[j], fma(0.5, v, (-0.5 * a.dt * rws) * dF));
-    } else if constexpr (ST == ST_RK3B) {
-      a.out[j] = fma(0.75, a.u[j], fma(0.25, v, (-0.25 * a.dt * rws) * dF));
-    } else if constexpr (ST == ST_RK3C) {
-      a.out[j] = fma(1.0 / 3.0, a.u[j], fma(2.0 / 3.0, v, (-(2.0 / 3.0) * a.dt * rws) * dF));
-    } else if constexpr (ST == ST_MS) {
-      const double udot = -(rws * dF);
-      a.out[j] = fma(25.0 / 32.0, v,
-                     fma((50.0 / 32.0) * a.dt, udot,
-                         fma(7.0 / 32.0, a.uo4[j], ((10.0 / 32.0) * a.dt) * a.lo4[j])));
-      a.lout[j] = udot;
-    }
+    combine_fast<ST>(a, j, v, dF, L.rws ? L.rws[j] : L.rws0);
   }
 }
 
@@ -196,16 +123,7 @@ __global__ void __launch_bounds__(NT) stage1d_kernel(StageArgs a) {
     for (int c = 0; c < C; ++c) {
       const int64_t j = j0 + c;
       if (j >= nc) break;
-      double FL = F[c], FR = F[c + 1];
-      if (j == 0 || j == nc - 1) {
-        if (L.bc == HRW_BC_COPY) {  // F_0 = F_1, F_nc = F_{nc-1}  (example1:103-104)
-          FL = FR = 0.0;
-        } else {
-          if (j == 0) FL = 0.0;  // ZERO and ZERO_INFLOW (example2:117-120)
-          if (j == nc - 1) FR = L.bc == HRW_BC_ZERO ? 0.0 : physflux<STRICT>(L, vr[c], j + 1);
-        }
-      }
-      const double dF = STRICT ? __dsub_rn(FR, FL) : FR - FL;
+      const double dF = flux_diff<STRICT>(L, j, F[c], F[c + 1], vr[c]);
       combine<ST, STRICT>(a, L, j, sv[H + l0 + c], dF);
     }
   }

@@ -1,8 +1,229 @@
-// stage2d.cu - placeholder until the 2D kernel lands.
+// stage2d.cu - fused 2D stage kernel: dimension-by-dimension WENO reconstruction, numerical
+// fluxes in x1 and x2, the conservative update and the TVD stage combine, one pass per stage.
+//
+// Follows, for one stage of the reference's time loop on the 2D population-balance example:
+//   x1 sweep over contiguous rows       example/example2_pbe_2d_fv.f90:97-103
+//   x2 sweep over strided columns       example/example2_pbe_2d_fv.f90:106-112
+//   boundary fluxes                     example/example2_pbe_2d_fv.f90:117-120
+//   update -(dF1)/dx1 - (dF2)/dx2       example/example2_pbe_2d_fv.f90:123-127
+//   weno_reconstruct                    src/hrweno_weno.f90:129-219
+//   godunov / lax_friedrichs            src/hrweno_fluxes.f90:22-76
+//   mstvd / rktvd stage update          src/hrweno_tvdode.f90:139-167,257
+//
+// Layout: u((j-1)*nc1 + i), x1 fastest (example2...f90:124).  One block owns a 32 x 32 tile
+// of cells; the tile plus a k-cell halo in each direction is staged in shared memory once
+// (ghosts replicate the first/last cell of each row and column, src/hrweno_weno.f90:172-173).
+// Each of the 128 threads reconstructs a segment of 8 cells along x1 from a register window,
+// then a segment of 8 cells along x2; segment-edge states are exchanged through shared
+// memory and the tile-edge states are recomputed by one lane each.  The x1 flux divergence
+// is parked in shared memory; the x2 pass adds its own and writes each cell once.
+//
+// Upwind specialisation (UPW): for the Godunov flux of f = g(x) u with g > 0 on the whole
+// domain in both directions, F = g vm exactly (hrw_stage.cuh: upwind_flux), so only the left
+// state vr of every interface is reconstructed.
 #include <cuda_runtime.h>
 
+#include "../../include/hrweno_gpu.h"
+#include "hrw_device.cuh"
 #include "hrw_internal.h"
+#include "hrw_stage.cuh"
 
 namespace hrw {
-cudaError_t launch_stage2d(const StageArgs&, int, int, bool, cudaStream_t) { return cudaErrorNotSupported; }
+
+namespace {
+
+constexpr int TX = 32, TY = 32, C = 8, NT = 128;
+static_assert(TX * TY == NT * C, "one segment of C cells per thread and direction");
+static_assert(TX == 32 && TY / C == NT / 32 && TX / C == NT / 32, "warp-per-segment mapping");
+
+template <int K, int ST, bool STRICT, bool UPW>
+__global__ void __launch_bounds__(NT) stage2d_kernel(StageArgs a) {
+  constexpr int H = K;
+  constexpr int RW = TX + 2 * H;      // loaded row width
+  constexpr int SW = RW + 1;          // odd row stride: the x1 pass reads 32 rows per warp
+  constexpr int SQ = TX + 1;          // odd stride of the parked x1 divergence
+  constexpr int NSX = TX / C, NSY = TY / C;
+  __shared__ double sv[(TY + 2 * H) * SW];
+  __shared__ double sq[TY * SQ];
+  __shared__ double sLx[TY * (NSX + 1)], sRx[TY * (NSX + 1)];  // [row][segment edge]
+  __shared__ double sLy[(NSY + 1) * TX], sRy[(NSY + 1) * TX];  // [segment edge][column]
+
+  const LineArgs& L1 = a.L;
+  const LineArgs& L2 = a.L2;
+  const int64_t n1 = L1.nc, n2 = L2.nc, ld = a.ld;
+  const int64_t bx = (int64_t)blockIdx.x * TX, by = (int64_t)blockIdx.y * TY;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+
+  // ---- stage the tile and its halo ------------------------------------------------------------
+  for (int q = tid; q < (TY + 2 * H) * RW; q += NT) {
+    const int row = q / RW, col = q - row * RW;
+    int64_t gy = by - H + row, gx = bx - H + col;
+    gy = gy < 0 ? 0 : (gy >= n2 ? n2 - 1 : gy);
+    gx = gx < 0 ? 0 : (gx >= n1 ? n1 - 1 : gx);
+    sv[row * SW + col] = a.v[gy * ld + gx];
+  }
+  __syncthreads();
+
+  // ---- x1 reconstruction: row r = lane, segment sg = warp ------------------------------------
+  const int r = lane, sg = warp;
+  double vl[C], vr[C];
+  {
+    const double* row = &sv[(r + H) * SW + sg * C];  // row[q] = v(bx + sg*C - H + q)
+    if constexpr (STRICT) {
+#pragma unroll
+      for (int c = 0; c < C; ++c) recon_strict<K>(row + H + c, a.eps, vl[c], vr[c]);
+    } else {
+      double w[C + 2 * K];
+#pragma unroll
+      for (int q = 0; q < C + 2 * K; ++q) w[q] = row[q];
+      recon_fast<K, C, !UPW>(w, a.eps, vl, vr);
+    }
+    if constexpr (!UPW) sLx[r * (NSX + 1) + sg] = vl[0];
+    sRx[r * (NSX + 1) + sg + 1] = vr[C - 1];
+  }
+  // tile-edge cells: warp 0 the left column (vr of x1 = bx-1), warp 1 the right column (vl of
+  // x1 = bx+TX); warp 2 the row above (vr of x2 = by-1), warp 3 the row below (vl of by+TY)
+  {
+    double el, er;
+    const double* p;
+    int stride;
+    if (warp < 2) {
+      p = &sv[(lane + H) * SW + (warp == 0 ? H - 1 : H + TX)];
+      stride = 1;
+    } else {
+      p = &sv[(warp == 2 ? H - 1 : H + TY) * SW + H + lane];
+      stride = SW;
+    }
+    const bool need = !UPW || warp == 0 || warp == 2;
+    if (need) {
+      if constexpr (STRICT) recon_strict_strided<K>(p, stride, a.eps, el, er);
+      else recon_fast_one<K>(p, a.eps, el, er, stride);
+      if (warp == 0) sRx[lane * (NSX + 1)] = er;
+      else if (warp == 1) sLx[lane * (NSX + 1) + NSX] = el;
+      else if (warp == 2) sRy[lane] = er;
+      else sLy[NSY * TX + lane] = el;
+    }
+  }
+  __syncthreads();
+
+  // ---- x1 fluxes of the segment; park the x1 divergence --------------------------------------
+  {
+    const int64_t j0 = bx + sg * C;
+    double F[C + 1];
+    if constexpr (UPW) {
+      F[0] = upwind_flux<STRICT>(L1, sRx[r * (NSX + 1) + sg], j0);
+#pragma unroll
+      for (int c = 1; c <= C; ++c) F[c] = upwind_flux<STRICT>(L1, vr[c - 1], j0 + c);
+    } else {
+      F[0] = numflux<STRICT>(L1, sRx[r * (NSX + 1) + sg], vl[0], j0);
+#pragma unroll
+      for (int c = 1; c < C; ++c) F[c] = numflux<STRICT>(L1, vr[c - 1], vl[c], j0 + c);
+      F[C] = numflux<STRICT>(L1, vr[C - 1], sLx[r * (NSX + 1) + sg + 1], j0 + C);
+    }
+#pragma unroll
+    for (int c = 0; c < C; ++c) {
+      const int64_t gx = j0 + c;
+      double t = 0.0;
+      if (gx < n1) {
+        const double dF = flux_diff<STRICT>(L1, gx, F[c], F[c + 1], vr[c]);
+        if constexpr (STRICT) t = __ddiv_rn(dF, L1.width ? L1.width[gx] : L1.rx);
+        else t = (L1.rws ? L1.rws[gx] : L1.rws0) * dF;
+      }
+      sq[r * SQ + sg * C + c] = t;
+    }
+  }
+
+  // ---- x2 reconstruction: column = lane, segment sy = warp -----------------------------------
+  const int col = lane, sy = warp;
+  {
+    const double* cp = &sv[(sy * C) * SW + H + col];  // cp[q*SW] = v(x2 = by + sy*C - H + q)
+    if constexpr (STRICT) {
+#pragma unroll
+      for (int c = 0; c < C; ++c) recon_strict_strided<K>(cp + (H + c) * SW, SW, a.eps, vl[c], vr[c]);
+    } else {
+      double w[C + 2 * K];
+#pragma unroll
+      for (int q = 0; q < C + 2 * K; ++q) w[q] = cp[q * SW];
+      recon_fast<K, C, !UPW>(w, a.eps, vl, vr);
+    }
+    if constexpr (!UPW) sLy[sy * TX + col] = vl[0];
+    sRy[(sy + 1) * TX + col] = vr[C - 1];
+  }
+  __syncthreads();
+
+  // ---- x2 fluxes, the update and the stage combine -------------------------------------------
+  {
+    const int64_t gx = bx + col;
+    const int64_t j0 = by + sy * C;
+    double F[C + 1];
+    if constexpr (UPW) {
+      F[0] = upwind_flux<STRICT>(L2, sRy[sy * TX + col], j0);
+#pragma unroll
+      for (int c = 1; c <= C; ++c) F[c] = upwind_flux<STRICT>(L2, vr[c - 1], j0 + c);
+    } else {
+      F[0] = numflux<STRICT>(L2, sRy[sy * TX + col], vl[0], j0);
+#pragma unroll
+      for (int c = 1; c < C; ++c) F[c] = numflux<STRICT>(L2, vr[c - 1], vl[c], j0 + c);
+      F[C] = numflux<STRICT>(L2, vr[C - 1], sLy[(sy + 1) * TX + col], j0 + C);
+    }
+    if (gx < n1) {
+#pragma unroll
+      for (int c = 0; c < C; ++c) {
+        const int64_t gy = j0 + c;
+        if (gy >= n2) break;
+        const double dF = flux_diff<STRICT>(L2, gy, F[c], F[c + 1], vr[c]);
+        const int ly = sy * C + c;
+        const double v = sv[(ly + H) * SW + H + col];
+        const double t1 = sq[ly * SQ + col];
+        const int64_t j = gy * ld + gx;
+        if constexpr (STRICT) {
+          // vdot = -((f1(i)-f1(i-1))/dx1) - (f2(j)-f2(j-1))/dx2   (example2...f90:123-127)
+          const double t2 = __ddiv_rn(dF, L2.width ? L2.width[gy] : L2.rx);
+          combine_strict<ST>(a, j, v, __dsub_rn(-t1, t2));
+        } else {
+          const double q = fma(L2.rws ? L2.rws[gy] : L2.rws0, dF, t1);
+          combine_fast<ST>(a, j, v, q, 1.0);
+        }
+      }
+    }
+  }
+}
+
+template <int K, int ST, bool STRICT, bool UPW>
+cudaError_t launch_k(const StageArgs& a, cudaStream_t s) {
+  const dim3 grid((unsigned)((a.L.nc + TX - 1) / TX), (unsigned)((a.L2.nc + TY - 1) / TY));
+  stage2d_kernel<K, ST, STRICT, UPW><<<grid, NT, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+template <int K, bool STRICT, bool UPW>
+cudaError_t launch_st(const StageArgs& a, int stage, cudaStream_t s) {
+  switch (stage) {
+    case ST_RHS: return launch_k<K, ST_RHS, STRICT, UPW>(a, s);
+    case ST_EULER: return launch_k<K, ST_EULER, STRICT, UPW>(a, s);
+    case ST_RK2B: return launch_k<K, ST_RK2B, STRICT, UPW>(a, s);
+    case ST_RK3B: return launch_k<K, ST_RK3B, STRICT, UPW>(a, s);
+    case ST_RK3C: return launch_k<K, ST_RK3C, STRICT, UPW>(a, s);
+    case ST_MS: return launch_k<K, ST_MS, STRICT, UPW>(a, s);
+  }
+  return cudaErrorInvalidValue;
+}
+
+template <bool STRICT, bool UPW>
+cudaError_t launch_kk(const StageArgs& a, int k, int stage, cudaStream_t s) {
+  if (k == 1) return launch_st<1, STRICT, UPW>(a, stage, s);
+  if (k == 2) return launch_st<2, STRICT, UPW>(a, stage, s);
+  return launch_st<3, STRICT, UPW>(a, stage, s);
+}
+
+}  // namespace
+
+cudaError_t launch_stage2d(const StageArgs& a, int k, int stage, bool strict, cudaStream_t s) {
+  if (a.L.nc <= 0 || a.L2.nc <= 0) return cudaSuccess;
+  if (a.L2.nc > 65535LL * TY) return cudaErrorInvalidValue;
+  const bool upw = a.upwind;
+  if (strict) return upw ? launch_kk<true, true>(a, k, stage, s) : launch_kk<true, false>(a, k, stage, s);
+  return upw ? launch_kk<false, true>(a, k, stage, s) : launch_kk<false, false>(a, k, stage, s);
+}
+
 }  // namespace hrw

@@ -24,6 +24,16 @@
 
 #include "../include/hrweno_gpu.h"
 
+#ifdef _OPENMP
+#include <omp.h>
+// The reference's cell loop is `do concurrent` (src/hrweno_weno.f90:174) and every stage
+// combine is an elementwise array expression, so splitting these loops over threads leaves
+// each element's arithmetic, and therefore every result bit, unchanged.
+#define ORC_PARFOR _Pragma("omp parallel for schedule(static)")
+#else
+#define ORC_PARFOR
+#endif
+
 #if defined(__x86_64__) || defined(__i386__)
 typedef __float128 qreal;
 #else
@@ -122,6 +132,7 @@ static void weno_reconstruct(int nc, int k, T eps, const T* cnu, const T* v, T* 
   for (int q = 1; q <= nc; ++q) vext[q + k - 1] = v[q - 1];
   for (int q = 1 - (k - 1); q <= 0; ++q) vext[q + k - 1] = v[0];
   for (int q = nc + 1; q <= nc + k - 1; ++q) vext[q + k - 1] = v[nc - 1];
+  ORC_PARFOR
   for (int i = 1; i <= nc; ++i) {  // (:174)
     const T* ci = cnu ? cnu + (size_t)k * (k + 1) * (i - 1) : c;  // (:170,177)
     auto C = [&](int j, int r) { return ci[j + k * (r + 1)]; };
@@ -222,6 +233,7 @@ static void line_fluxes(const hrw_problem& p, int dim, const Line<T>& L, T eps, 
                         const T* v, T* vl, T* vr, T* F) {
   const int nc = L.nc;
   weno_reconstruct<T>(nc, p.k, eps, nullptr, v, vl, vr);
+  ORC_PARFOR
   for (int i = 1; i <= nc - 1; ++i) F[i] = numflux<T>(p, dim, vr[i - 1], vl[i], L.right(i), t);
   switch (p.bc[dim]) {
     case HRW_BC_COPY:  // (example1...f90:103-104)
@@ -277,6 +289,7 @@ struct Problem {
     if (p.kind == HRW_PROBLEM_FV1D) {  // example1...f90:72-109
       const Line<T>& L = line[0];
       line_fluxes<T>(p, 0, L, eps, t, v, vl.data(), vr.data(), F.data());
+      ORC_PARFOR
       for (int i = 1; i <= L.nc; ++i) vdot[i - 1] = -(F[i] - F[i - 1]) / L.w(i);  // (:107)
       return;
     }
@@ -337,20 +350,26 @@ struct ODE {
     const T dtt = (T)dt;
     if (order == 1) {  // (:137-143)
       prob.rhs(t, u, udot.data());
+      ORC_PARFOR
       for (int i = 0; i < n; ++i) u[i] = u[i] + dtt * udot[i];
       fe += 1;
     } else if (order == 2) {  // (:148-155)
       prob.rhs(t, u, udot.data());
+      ORC_PARFOR
       for (int i = 0; i < n; ++i) ui[i] = u[i] + dtt * udot[i];
       prob.rhs(t + dt, ui.data(), udot.data());
+      ORC_PARFOR
       for (int i = 0; i < n; ++i) u[i] = (u[i] + ui[i] + dtt * udot[i]) / 2;
       fe += 2;
     } else {  // (:161-169)
       prob.rhs(t, u, udot.data());
+      ORC_PARFOR
       for (int i = 0; i < n; ++i) ui[i] = u[i] + dtt * udot[i];
       prob.rhs(t + dt, ui.data(), udot.data());
+      ORC_PARFOR
       for (int i = 0; i < n; ++i) ui[i] = (3 * u[i] + ui[i] + dtt * udot[i]) / 4;
       prob.rhs(t + dt / 2, ui.data(), udot.data());
+      ORC_PARFOR
       for (int i = 0; i < n; ++i) u[i] = (u[i] + 2 * ui[i] + 2 * dtt * udot[i]) / 3;
       fe += 3;
     }
@@ -453,6 +472,17 @@ using namespace orc;
 extern "C" {
 
 const char* orc_last_error(void) { return g_msg.c_str(); }
+
+// Threads used by the 1D loops (1 = the serial reference); returns the count in effect.
+int orc_set_threads(int n) {
+#ifdef _OPENMP
+  if (n > 0) omp_set_num_threads(n);
+  return omp_get_max_threads();
+#else
+  (void)n;
+  return 1;
+#endif
+}
 
 // weno%reconstruct at precision prec (32, 64, 128); xedges nullable (non-uniform grid).
 int orc_weno_reconstruct(int prec, int nc, int k, double eps, const double* xedges,

@@ -25,8 +25,8 @@ def build(force: bool = False) -> Path:
     LIB.parent.mkdir(exist_ok=True)
     hdr = HERE.parent / "include" / "hrweno_gpu.h"
     if force or not LIB.exists() or LIB.stat().st_mtime < max(SRC.stat().st_mtime, hdr.stat().st_mtime):
-        subprocess.run(["g++", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-std=c++17",
-                        "-o", str(LIB), str(SRC)], check=True)
+        subprocess.run(["g++", "-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared",
+                        "-std=c++17", "-o", str(LIB), str(SRC)], check=True)
     return LIB
 
 
@@ -49,8 +49,15 @@ def lib() -> C.CDLL:
         L.orc_ode_info.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int),
                                    C.POINTER(C.c_longlong)]
         L.orc_ode_destroy.argtypes = [C.c_void_p]
+        L.orc_set_threads.argtypes = [C.c_int]
+        L.orc_set_threads.restype = C.c_int
         _lib = L
     return _lib
+
+
+def set_threads(n: int) -> int:
+    """Threads of the oracle's 1D cell loops (1: serial, as the reference); returns the count."""
+    return lib().orc_set_threads(int(n))
 
 
 def _p(a: np.ndarray):

@@ -79,3 +79,20 @@ def test_reconstruct_constant_state(orc, k):
     vl, vr = orc.reconstruct(v, k=k)
     assert np.all(vl == 0.3) or np.allclose(vl, 0.3, rtol=1e-15)
     assert np.allclose(vr, 0.3, rtol=1e-15)
+
+
+def test_oracle_reproduces_golden_config1(orc):
+    """The committed 500-cell snapshots (tests/golden/oracle_config1.json) are reproduced bit
+    for bit from the stored u0: the oracle gives the same bits on every machine."""
+    import json
+    from pathlib import Path
+    gold = json.loads((Path(__file__).parent / "golden" / "oracle_config1.json").read_text())
+    nc = gold["nc"]
+    prob = burgers_1d(nc, -5.0, 5.0, k=3, eps=1e-6, flux="lax_friedrichs", alpha=1.0, bc="copy")
+    ode = orc.ODE(prob, nc, method=0, order=3)
+    u = np.array(gold["u0"])
+    t = 0.0
+    for snap in gold["snapshots"]:
+        t = ode.integrate(u, t, snap["tout"], gold["dt"])
+        assert t == snap["t"]
+        assert np.array_equal(u, np.array(snap["u"]))
