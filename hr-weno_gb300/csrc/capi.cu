@@ -153,7 +153,7 @@ int hrw_weno_create(int ncells, int k, double eps, const double* xedges, hrw_wen
   w->nc = ncells;
   w->k = k;
   w->eps = eps;
-  cudaError_t e = cudaStreamCreateWithFlags(&w->stream, cudaStreamNonBlocking);
+  cudaError_t e = cudaStreamCreateWithFlags(&w->stream, cudaStreamDefault);
   if (e == cudaSuccess) e = cudaMalloc(&w->buf, sizeof(double) * 3 * (size_t)ncells);
   if (e == cudaSuccess && xedges) {
     w->uniform = false;
@@ -260,7 +260,7 @@ static int ode_create(const hrw_problem* p, int neq, int order, int method, int 
     return fail(e == cudaErrorMemoryAllocation ? HRW_ENOMEM : HRW_ECUDA,
                 std::string("hrw_ode_create: ") + cudaGetErrorString(e));
   };
-  cudaError_t e = cudaStreamCreateWithFlags(&o->own, cudaStreamNonBlocking);
+  cudaError_t e = cudaStreamCreateWithFlags(&o->own, cudaStreamDefault);
   if (e != cudaSuccess) return cleanup(e);
   o->stream = o->own;
   const size_t bytes = sizeof(double) * (size_t)neq;

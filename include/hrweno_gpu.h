@@ -6,7 +6,9 @@
  * Every entry point is `extern "C"`, takes plain pointers and sizes, and returns a
  * status code (HRW_OK == 0).  Where the Fortran reference aborts with `error stop`,
  * this library returns HRW_EINVAL and keeps the reference's message, readable through
- * hrw_last_error().  Handles are not thread-safe; each handle owns one CUDA stream.
+ * hrw_last_error().  Handles are not thread-safe; each handle owns one CUDA stream, created
+ * blocking, so that its work is ordered after earlier work of the legacy default stream
+ * (device arrays that the caller filled there are complete before a stage kernel reads them).
  *
  * Reference interfaces replaced (paths inside HugoMVale/HR-WENO):
  *   weno(ncells,k,eps,xedges)          src/hrweno_weno.f90:48-50,54-127
