@@ -88,6 +88,11 @@ int validate_problem(const hrw_problem* p, int neq) {
 
 }  // namespace
 
+namespace hrw {
+// Record msg as this host thread's last error (read by hrw_last_error) and return code.
+int set_error(int code, const char* msg) { return fail(code, msg); }
+}  // namespace hrw
+
 // -------------------------------------------------------------------------------------------
 // Handles
 // -------------------------------------------------------------------------------------------

@@ -50,6 +50,8 @@ struct StageArgs {
 
 // FAST flux form: the kernels evaluate F / fscale, fscale folded into rws.
 double fast_flux_scale(int flux, int fn);
+// Record msg as the calling thread's last error (hrw_last_error) and return code.
+int set_error(int code, const char* msg);
 // True when the line's flux is g(x) u with g > 0 at every interface (upwind Godunov).
 bool positive_velocity(const LineArgs& L);
 

@@ -131,6 +131,23 @@ int hrw_ode_destroy(hrw_ode* ode);
  * (LINEAR_ODE: neq = ncells[0]). */
 int hrw_rhs(const hrw_problem* p, int dtype, double t, const void* v, void* vdot, void* stream);
 
+/* ---- RK3 steps that allocate no device memory -------------------------------------- */
+/* No counterpart in the reference.  For callers that cannot allocate device memory: a
+ * framework whose caching allocator already owns the whole device, or a step loop that must
+ * not pay the implicit device synchronisation of cudaMalloc/cudaFree.  Runs nsteps rktvd
+ * order-3 steps of a uniform-grid FV1D problem (width[0] must be NULL) on the device array
+ * u (ncells[0] doubles), in place, on `stream` (a cudaStream_t; NULL is the legacy default
+ * stream), and returns without waiting for the GPU.  The two RK stage arrays live in one
+ * fixed buffer inside the library (2 * HRW_NOALLOC_MAX_CELLS doubles, 16 MiB, held by every
+ * GPU that loads the library until the process exits); larger lines are rejected with
+ * HRW_EINVAL.  The first call on a device looks up that buffer's device address, so make
+ * that first call before any stream capture.  All calls share the buffer: calls whose work
+ * overlaps on the GPU (other streams, other threads) race and give wrong results; calls on
+ * one stream are ordered and safe.  Same kernels and operation order as hrw_integrate, so
+ * the results are bit-identical to an rktvd(order 3) handle's. */
+#define HRW_NOALLOC_MAX_CELLS (1 << 20)
+int hrw_rktvd3_steps_noalloc(const hrw_problem* p, double* u, double dt, int nsteps, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
