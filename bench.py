@@ -44,6 +44,9 @@ NC = 1 << 24
 # stage 2 reads u, u1, writes u2 (24 B); stage 3 reads u, u2, writes u (24 B)
 BYTES_PER_CELL_UPDATE = 64
 LAUNCHES_PER_STEP = 3
+# compensated FP32: stage 1 reads hi, lo and writes d1 (12 B); stage 2 reads hi, lo, d1 and
+# writes d2 (16 B); stage 3 reads hi, lo, d2 and writes hi, lo (20 B)
+F32C_BYTES_PER_CELL_UPDATE = 48
 L2_BYTES = 126 * 1024 * 1024
 
 # DRAM bytes per cell and stage launch of the FP64 stage kernel, measured by ncu
@@ -251,6 +254,33 @@ def run_ours(args, dist: Dist) -> None:
     value = dist.world * NC * args.steps / el
     assert bool(torch.isfinite(u).all())
 
+    # ---- compensated FP32 form on the same line: same steps, error against FP64 ----------
+    forms = {}
+    if not args.no_forms:
+        ode32 = hrweno.rktvd(prob, NC, 3, dtype="f32c")
+        ode32.set_stream(stream.cuda_stream)
+        u32 = torch.from_numpy(u0).cuda()
+        t32 = ode32.integrate(u32, 0.0, (args.warmup - 0.5) * dt, dt)
+        torch.cuda.synchronize()
+        dist.barrier()
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        t32 = ode32.integrate(u32, t32, t32 + (args.steps - 0.5) * dt, dt)
+        f1.record(stream)
+        torch.cuda.synchronize()
+        el32 = dist.max(f0.elapsed_time(f1) * 1e-3)
+        diff = (u32 - u).abs()
+        v32 = dist.world * NC * args.steps / el32
+        forms["f32c"] = {
+            "value": v32, "unit": UNIT, "ms_per_step": 1e3 * el32 / args.steps,
+            "speedup_vs_f64": v32 / value, "bytes_per_cell_update": F32C_BYTES_PER_CELL_UPDATE,
+            "hbm_frac": F32C_BYTES_PER_CELL_UPDATE * v32 / dist.world / 1e9 / peaks()["hbm_gbs"],
+            "rel_l1_vs_f64": float(diff.sum() / u.abs().sum()),
+            "rel_linf_vs_f64": float(diff.max() / u.abs().max()),
+            "steps_compared": args.warmup + args.steps,
+        }
+        del ode32, u32, diff
+
     # ---- e2e: reference-facing call on pinned host memory, one step per call -------------
     ode2 = hrweno.rktvd(prob, NC, 3)
     ode2.set_stream(stream.cuda_stream)
@@ -314,6 +344,7 @@ def run_ours(args, dist: Dist) -> None:
                       "dfma_per_s_measured": dfma, "ffma_per_s_measured": ffma},
         "cpu_baseline": cpu,
         "e2e": e2e,
+        "forms": forms,
         "gpu_launches": steps_done * LAUNCHES_PER_STEP,
         "clocks": clk.summary(),
     }
@@ -328,6 +359,7 @@ def main() -> None:
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-forms", action="store_true", help="skip the FP32 form")
     ap.add_argument("--cells", type=int, default=NC,
                     help="cells of the line (default 2^24, the benchmark workload; smaller "
                          "lines are for profiler captures)")

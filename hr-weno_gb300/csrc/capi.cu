@@ -121,6 +121,17 @@ struct hrw_ode {
   double* ring_l[4] = {};  // mstvd: L(u^m) at slot m % 4
   int64_t level = 0;       // mstvd: m of the current solution
   StageArgs base{};
+  // compensated FP32 form (HRW_F32C): state slots as float pairs; rktvd ping-pongs between
+  // slots 0 and 1, mstvd keeps u^m in slot m % 5 and L(u^m) in fl[m % 4]
+  float* fmem = nullptr;
+  float* fhi[5] = {};
+  float* flo[5] = {};
+  float* fl[4] = {};
+  float* fd1 = nullptr;  // stage increments
+  float* fd2 = nullptr;
+  float* frw = nullptr;  // per-cell 1/width
+  int fslot = 0;
+  F32CArgs fbase{};
 };
 
 extern "C" {
@@ -248,10 +259,19 @@ static int ode_create(const hrw_problem* p, int neq, int order, int method, int 
   if (neq <= 0) return fail(HRW_EINVAL, "Invalid input 'neq'. Valid range: neq >= 1.");
   if (method == 0 && (order < 1 || order > 3))
     return fail(HRW_EINVAL, "Invalid input 'order' in 'rktvd'. Valid range: 1 <= k <= 3.");
-  if (dtype != HRW_F64 && dtype != HRW_F32) return fail(HRW_EINVAL, "Invalid input 'dtype'.");
-  if (dtype == HRW_F32) return fail(HRW_EINVAL, "Invalid input 'dtype': HRW_F32 integrators are not built yet.");
+  if (dtype != HRW_F64 && dtype != HRW_F32C) {
+    if (dtype == HRW_F32)
+      return fail(HRW_EINVAL, "Invalid input 'dtype': HRW_F32 integrators are not built; use HRW_F32C.");
+    return fail(HRW_EINVAL, "Invalid input 'dtype'.");
+  }
   int rc = validate_problem(p, neq);
   if (rc != HRW_OK) return rc;
+  if (dtype == HRW_F32C) {
+    if (p->kind != HRW_PROBLEM_FV1D)
+      return fail(HRW_EINVAL, "Invalid input 'dtype': HRW_F32C supports HRW_PROBLEM_FV1D problems.");
+    if (!(p->eps > 1.1920928955078125e-07))  // epsilon(1.0_real32), src/hrweno_weno.f90:92
+      return fail(HRW_EINVAL, "Invalid input 'eps'. Valid range: eps > epsilon.");
+  }
   hrw_ode* o = new hrw_ode;
   o->prob = *p;
   o->neq = neq;
@@ -316,6 +336,42 @@ static int ode_create(const hrw_problem* p, int neq, int order, int method, int 
                positive_velocity(b.L2);
   }
   if ((e = cudaMalloc(&o->u, bytes)) != cudaSuccess) return cleanup(e);
+  if (dtype == HRW_F32C) {
+    // float buffers: rktvd 2 slots (hi, lo) + 2 increments; mstvd 5 slots + 4 L + 2 increments
+    const int slots = method == 1 ? 5 : 2;
+    const size_t n = (size_t)neq, nf = n * (2 * slots + (method == 1 ? 4 : 0) + 2 + (p->width[0] ? 1 : 0));
+    if ((e = cudaMalloc(&o->fmem, sizeof(float) * nf)) != cudaSuccess) return cleanup(e);
+    float* q = o->fmem;
+    for (int k = 0; k < slots; ++k) { o->fhi[k] = q; q += n; o->flo[k] = q; q += n; }
+    if (method == 1)
+      for (int k = 0; k < 4; ++k) { o->fl[k] = q; q += n; }
+    o->fd1 = q; q += n;
+    o->fd2 = q; q += n;
+    F32CArgs& f = o->fbase;
+    const LineArgs& L = b.L;
+    f.eps = (float)p->eps;
+    f.L.nc = L.nc;
+    f.L.fn = L.fn;
+    f.L.bc = L.bc;
+    f.L.flux = L.flux;
+    f.L.a = (float)L.a;
+    f.L.b = (float)L.b;
+    f.L.alpha = (float)L.alpha;
+    f.L.xmin = (float)L.xmin;
+    f.L.rx = (float)L.rx;
+    f.L.gstep = (float)(L.b * L.rx);
+    if (p->width[0]) {
+      o->frw = q;
+      std::vector<float> rw(n);
+      for (size_t i = 0; i < n; ++i) rw[i] = (float)(1.0 / p->width[0][i]);
+      if ((e = cudaMemcpy(o->frw, rw.data(), sizeof(float) * n, cudaMemcpyHostToDevice)) != cudaSuccess)
+        return cleanup(e);
+      f.L.rw = o->frw;
+    }
+    o->istate = 1;
+    *out = o;
+    return HRW_OK;
+  }
   if ((e = cudaMalloc(&o->w1, bytes)) != cudaSuccess) return cleanup(e);
   if ((e = cudaMalloc(&o->w2, bytes)) != cudaSuccess) return cleanup(e);
   if (method == 1) {
@@ -364,6 +420,7 @@ int hrw_ode_destroy(hrw_ode* o) {
     if (p) cudaFree(p);
   for (double* p : o->ring_l)
     if (p) cudaFree(p);
+  if (o->fmem) cudaFree(o->fmem);
   if (o->own) cudaStreamDestroy(o->own);
   delete o;
   return HRW_OK;
@@ -469,6 +526,101 @@ static int ms_integrate(hrw_ode* o, double* du, double* t, double tout, double d
   return HRW_OK;
 }
 
+// ---- compensated FP32 form ---------------------------------------------------------------------
+static void split_pair(double x, float& hi, float& lo) {
+  hi = (float)x;
+  lo = (float)(x - (double)hi);
+}
+
+static cudaError_t run_f32c(hrw_ode* o, int stage, int slot, const float* dv, float* out, int slot_out,
+                            const float* hi4, const float* lo4, const float* l4, float* lout, double dt) {
+  F32CArgs a = o->fbase;
+  a.hi = o->fhi[slot];
+  a.lo = o->flo[slot];
+  a.dv = dv;
+  a.out = out;
+  a.hi_out = slot_out >= 0 ? o->fhi[slot_out] : nullptr;
+  a.lo_out = slot_out >= 0 ? o->flo[slot_out] : nullptr;
+  a.hi4 = hi4;
+  a.lo4 = lo4;
+  a.l4 = l4;
+  a.lout = lout;
+  const LineArgs& L = o->base.L;
+  const bool widths = o->frw != nullptr;
+  split_pair(widths ? dt : dt / L.rx, a.c_hi, a.c_lo);
+  split_pair(dt, a.dt_hi, a.dt_lo);
+  a.lscale = widths ? 1.0f : (float)(1.0 / L.rx);
+  return launch_stage1d_f32c(a, o->prob.k, stage, o->stream);
+}
+
+// one rktvd step from slot `from` into slot `to`
+static cudaError_t rk_step_f32c(hrw_ode* o, int from, int to, double dt) {
+  cudaError_t e;
+  if (o->order == 1) return run_f32c(o, FC_RK1, from, nullptr, nullptr, to, nullptr, nullptr, nullptr, nullptr, dt);
+  if ((e = run_f32c(o, FC_E1, from, nullptr, o->fd1, -1, nullptr, nullptr, nullptr, nullptr, dt)) != cudaSuccess)
+    return e;
+  if (o->order == 2) return run_f32c(o, FC_RK2B, from, o->fd1, nullptr, to, nullptr, nullptr, nullptr, nullptr, dt);
+  if ((e = run_f32c(o, FC_RK3B, from, o->fd1, o->fd2, -1, nullptr, nullptr, nullptr, nullptr, dt)) != cudaSuccess)
+    return e;
+  return run_f32c(o, FC_RK3C, from, o->fd2, nullptr, to, nullptr, nullptr, nullptr, nullptr, dt);
+}
+
+static int rk_integrate_f32c(hrw_ode* o, double* du, double* t, double tout, double dt, int itask) {
+  double tt = *t;
+  int64_t n = 0;
+  do {
+    tt = tt + dt;
+    if (++n > kMaxSteps) return fail(HRW_EINVAL, "Invalid input 'dt': too many steps to reach tout.");
+  } while (!(is_done(tt, tout, dt) || itask == 2));
+  int slot = 0;
+  HRW_CUDA(launch_split_f64(du, o->fhi[0], o->flo[0], o->neq, o->stream));
+  for (int64_t s = 0; s < n; ++s) {
+    HRW_CUDA(rk_step_f32c(o, slot, 1 - slot, dt));
+    slot = 1 - slot;
+  }
+  HRW_CUDA(launch_merge_f64(o->fhi[slot], o->flo[slot], du, o->neq, o->stream));
+  *t = tt;
+  o->fevals += (int)(o->order * n);
+  o->nsteps += n;
+  if (o->istate == 1) o->istate = 2;
+  return HRW_OK;
+}
+
+static int ms_integrate_f32c(hrw_ode* o, double* du, double* t, double tout, double dt) {
+  double tt = *t;
+  if (o->istate == 1) {  // RK3 start (src/hrweno_tvdode.f90:236-249)
+    o->level = 0;
+    HRW_CUDA(launch_split_f64(du, o->fhi[0], o->flo[0], o->neq, o->stream));
+    for (int m = 0; m < 4; ++m) {
+      HRW_CUDA(run_f32c(o, FC_RHS, m % 5, nullptr, o->fl[m % 4], -1, nullptr, nullptr, nullptr, nullptr, dt));
+      HRW_CUDA(rk_step_f32c(o, m % 5, (m + 1) % 5, dt));
+      tt = tt + dt;
+    }
+    o->level = 4;
+    o->fevals = 12;
+    o->nsteps += 4;
+    o->istate = 2;
+  } else {
+    HRW_CUDA(launch_split_f64(du, o->fhi[o->level % 5], o->flo[o->level % 5], o->neq, o->stream));
+  }
+  int64_t n = 0;
+  for (double t2 = tt; !is_done(t2, tout, dt); t2 = t2 + dt)
+    if (++n > kMaxSteps) return fail(HRW_EINVAL, "Invalid input 'dt': too many steps to reach tout.");
+  for (int64_t s = 0; s < n; ++s) {  // (:252-268)
+    const int64_t m = o->level;
+    const int cur = (int)(m % 5), nxt = (int)((m + 1) % 5);  // nxt holds u^{m-4}
+    float* lm = o->fl[m % 4];                                 // holds L(u^{m-4})
+    HRW_CUDA(run_f32c(o, FC_MS, cur, nullptr, nullptr, nxt, o->fhi[nxt], o->flo[nxt], lm, lm, dt));
+    tt = tt + dt;
+    o->level = m + 1;
+  }
+  HRW_CUDA(launch_merge_f64(o->fhi[o->level % 5], o->flo[o->level % 5], du, o->neq, o->stream));
+  *t = tt;
+  o->fevals += (int)n;
+  o->nsteps += n;
+  return HRW_OK;
+}
+
 extern "C" int hrw_integrate(hrw_ode* o, int mem, void* u, double* t, double tout, double dt, int itask) {
   if (!o) return fail(HRW_EINVAL, "Invalid input 'ode': null handle.");
   if (!u || !t) return fail(HRW_EINVAL, "Invalid input: null pointer.");
@@ -483,7 +635,11 @@ extern "C" int hrw_integrate(hrw_ode* o, int mem, void* u, double* t, double tou
     du = o->u;
     HRW_CUDA(cudaMemcpyAsync(du, u, bytes, cudaMemcpyHostToDevice, o->stream));
   }
-  int rc = o->method == 0 ? rk_integrate(o, du, t, tout, dt, itask) : ms_integrate(o, du, t, tout, dt);
+  int rc;
+  if (o->dtype == HRW_F32C)
+    rc = o->method == 0 ? rk_integrate_f32c(o, du, t, tout, dt, itask) : ms_integrate_f32c(o, du, t, tout, dt);
+  else
+    rc = o->method == 0 ? rk_integrate(o, du, t, tout, dt, itask) : ms_integrate(o, du, t, tout, dt);
   if (rc != HRW_OK) return rc;
   if (mem == HRW_MEM_HOST) HRW_CUDA(cudaMemcpyAsync(u, du, bytes, cudaMemcpyDeviceToHost, o->stream));
   HRW_CUDA(cudaStreamSynchronize(o->stream));
@@ -492,15 +648,24 @@ extern "C" int hrw_integrate(hrw_ode* o, int mem, void* u, double* t, double tou
 
 extern "C" int hrw_rhs(const hrw_problem* p, int dtype, double t, const void* v, void* vdot, void* stream) {
   (void)t;
-  if (dtype != HRW_F64) return fail(HRW_EINVAL, "Invalid input 'dtype': hrw_rhs supports HRW_F64.");
+  if (dtype != HRW_F64 && dtype != HRW_F32C)
+    return fail(HRW_EINVAL, "Invalid input 'dtype': hrw_rhs supports HRW_F64 and HRW_F32C.");
   int neq = p && p->kind == HRW_PROBLEM_FV2D ? p->ncells[0] * p->ncells[1] : (p ? p->ncells[0] : 0);
   if (p && p->kind == HRW_PROBLEM_LINEAR_ODE) neq = p->ncells[0];
   hrw_ode* o = nullptr;
-  int rc = ode_create(p, neq, 1, 0, HRW_F64, &o);
+  int rc = ode_create(p, neq, 1, 0, dtype, &o);
   if (rc != HRW_OK) return rc;
   if (stream) o->stream = (cudaStream_t)stream;
-  cudaError_t e = run_stage(o, ST_RHS, (const double*)v, (const double*)v, (double*)vdot, nullptr,
-                            nullptr, nullptr, 0.0);
+  cudaError_t e;
+  if (dtype == HRW_F32C) {
+    e = launch_split_f64((const double*)v, o->fhi[0], o->flo[0], neq, o->stream);
+    if (e == cudaSuccess)
+      e = run_f32c(o, FC_RHS, 0, nullptr, o->fd1, -1, nullptr, nullptr, nullptr, nullptr, 1.0);
+    if (e == cudaSuccess) e = launch_widen_f32(o->fd1, (double*)vdot, neq, o->stream);
+  } else {
+    e = run_stage(o, ST_RHS, (const double*)v, (const double*)v, (double*)vdot, nullptr, nullptr,
+                  nullptr, 0.0);
+  }
   if (e == cudaSuccess) e = cudaStreamSynchronize(o->stream);
   hrw_ode_destroy(o);
   if (e != cudaSuccess) return fail(HRW_ECUDA, std::string("hrw_rhs: ") + cudaGetErrorString(e));

@@ -1,0 +1,181 @@
+// hrw_f32c.cuh - device building blocks of the compensated FP32 form.
+//
+// The FP32 form keeps the state as a pair of floats u = hi + lo (about 48 significant bits)
+// and evaluates the right-hand side in *difference form*.  Plain FP32 loses the flux
+// difference: F_{j+1/2} - F_{j-1/2} is a difference of O(1) numbers that agree to O(dx), so
+// a rounding of eps|u| in each reconstructed state becomes an error of eps|u|/dx in L(u) --
+// at 2^24 cells that is of the order of L itself.  Here every quantity that enters a
+// cancellation is formed from compensated neighbour differences d_m = u_{m+1} - u_m:
+//
+//  * the WENO candidates and smoothness indicators of src/hrweno_weno.f90:178-204 are linear
+//    and quadratic forms in the differences (rewritten below, same method);
+//  * the reconstructed states are carried as offsets a, b from the cell's own value v;
+//  * the flux difference of cell j is G(right) - G(left) with G = F - f(v_j) computed from the
+//    offsets, so the O(1) part f(v_j) cancels exactly instead of in rounding;
+//  * stage values are stored as small increments relative to u, and the increment of the
+//    final stage is added to (hi, lo) by an error-free two-sum.
+//
+// The rounding errors that remain are relative to the small quantities (differences,
+// increments), which is what keeps the FP32 form within 1e-6 relative L1 of FP64.
+#pragma once
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+#include "../../include/hrweno_gpu.h"
+#include "hrw_internal.h"
+
+namespace hrw {
+
+// error-free transformation: s + e == x + y exactly
+__device__ __forceinline__ void two_sum(float x, float y, float& s, float& e) {
+  s = __fadd_rn(x, y);
+  const float bb = __fsub_rn(s, x);
+  e = __fadd_rn(__fsub_rn(x, __fsub_rn(s, bb)), __fsub_rn(y, bb));
+}
+
+// (hi, lo) += x, renormalised so that |lo| <= ulp(hi)/2
+__device__ __forceinline__ void acc_add(float& hi, float& lo, float x) {
+  float s, e;
+  two_sum(hi, x, s, e);
+  const float t = __fadd_rn(lo, e);
+  hi = __fadd_rn(s, t);
+  lo = __fsub_rn(t, __fsub_rn(hi, s));
+}
+
+// 1/x by the MUFU approximation (about 1 ulp); x normal and positive
+__device__ __forceinline__ float rcpf(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
+// ---------------------------------------------------------------------------------------------
+// WENO offsets of one cell from its differences (k = 1..3).
+//   d[q] = d_{j-K+1+q}, q = 0 .. 2K-3  (k=3: d_{j-2}, d_{j-1}, d_j, d_{j+1}; k=2: d_{j-1}, d_j)
+// Returns rr = vr(j) - v(j) and rl = vl(j) - v(j).
+//
+// In terms of the differences (d_{-2} = v_{j-1} - v_{j-2}, ..., d_1 = v_{j+2} - v_{j+1}), the
+// reference's k = 3 candidates (c3 table, src/hrweno_weno.f90:19-21) minus v_j are
+//   vrr0 (4 d0 - d1)/6      vrr1 (d_{-1} + 2 d0)/6     vrr2 (5 d_{-1} - 2 d_{-2})/6
+//   vlr0 (2 d1 - 5 d0)/6    vlr1 -(2 d_{-1} + d0)/6    vlr2 (d_{-2} - 4 d_{-1})/6
+// and its smoothness indicators (:194-202) are
+//   beta0 = 13/12 (d1 - d0)^2      + 1/4 (d1 - 3 d0)^2
+//   beta1 = 13/12 (d0 - d_{-1})^2  + 1/4 (d_{-1} + d0)^2
+//   beta2 = 13/12 (d_{-1} - d_{-2})^2 + 1/4 (3 d_{-1} - d_{-2})^2.
+// For k = 2 (c2 table, :16-18; :189-191): vrr0 = d0/2, vrr1 = d_{-1}/2, vlr0 = -d0/2,
+// vlr1 = -d_{-1}/2, beta0 = d0^2, beta1 = d_{-1}^2.
+// Weights (:207-210) in product form with two reciprocals; cells whose squared indicators
+// leave the float range of the products take the quotient form.
+// ---------------------------------------------------------------------------------------------
+template <int K>
+__device__ __forceinline__ void recon_diff(const float* d, float eps, float& rl, float& rr) {
+  if constexpr (K == 1) {
+    rl = 0.f;
+    rr = 0.f;
+  } else if constexpr (K == 2) {
+    const float dm = d[0], d0 = d[1];
+    const float e0 = fmaf(d0, d0, eps), e1 = fmaf(dm, dm, eps);
+    const float s0 = e0 * e0, s1 = e1 * e1;
+    // w0 = (2/3)/s0 / (...) = 2 s1 / (2 s1 + s0);  mirrored d: w~0 = s1 / (s1 + 2 s0)
+    if (fmaxf(s0, s1) < 1e30f) {
+      const float den = fmaf(2.f, s1, s0), dent = fmaf(2.f, s0, s1);
+      // rr = (w0 d0 + w1 d_{-1}) / 2, rl = -(w~0 d0 + w~1 d_{-1}) / 2
+      rr = 0.5f * fmaf(2.f * s1, d0, s0 * dm) * rcpf(den);
+      rl = -0.5f * fmaf(s1, d0, 2.f * s0 * dm) * rcpf(dent);
+    } else {
+      const float a0 = (2.f / 3.f) / s0, a1 = (1.f / 3.f) / s1;
+      const float t0 = (1.f / 3.f) / s0, t1 = (2.f / 3.f) / s1;
+      rr = 0.5f * (a0 * d0 + a1 * dm) / (a0 + a1);
+      rl = -0.5f * (t0 * d0 + t1 * dm) / (t0 + t1);
+    }
+  } else {
+    const float dmm = d[0], dm = d[1], d0 = d[2], d1 = d[3];
+    const float c13 = 13.f / 12.f;
+    const float A0 = d1 - d0, A1 = d0 - dm, A2 = dm - dmm;
+    const float B0 = fmaf(-3.f, d0, d1), B1 = dm + d0, B2 = fmaf(3.f, dm, -dmm);
+    const float b0 = fmaf(c13 * A0, A0, 0.25f * B0 * B0);
+    const float b1 = fmaf(c13 * A1, A1, 0.25f * B1 * B1);
+    const float b2 = fmaf(c13 * A2, A2, 0.25f * B2 * B2);
+    const float e0 = eps + b0, e1 = eps + b1, e2 = eps + b2;
+    const float s0 = e0 * e0, s1 = e1 * e1, s2 = e2 * e2;
+    // candidates x6
+    const float R0 = fmaf(4.f, d0, -d1), R1 = fmaf(2.f, d0, dm), R2 = fmaf(5.f, dm, -2.f * dmm);
+    const float L0 = fmaf(2.f, d1, -5.f * d0), L1 = -fmaf(2.f, dm, d0), L2 = fmaf(-4.f, dm, dmm);
+    if (fmaxf(s0, fmaxf(s1, s2)) < 1e18f) {
+      // d = (3, 6, 1)/10: w_r ~ d_r P_r with P_0 = s1 s2, P_1 = s0 s2, P_2 = s0 s1
+      const float P0 = s1 * s2, P1 = s0 * s2, P2 = s0 * s1;
+      const float den = fmaf(3.f, P0, fmaf(6.f, P1, P2));
+      const float dent = fmaf(3.f, P2, fmaf(6.f, P1, P0));  // mirrored d = (1, 6, 3)/10
+      const float num = fmaf(3.f * P0, R0, fmaf(6.f * P1, R1, P2 * R2));
+      const float numt = fmaf(P0, L0, fmaf(6.f * P1, L1, 3.f * P2 * L2));
+      rr = (num * rcpf(den)) * (1.f / 6.f);
+      rl = (numt * rcpf(dent)) * (1.f / 6.f);
+    } else {
+      const float a0 = 0.3f / s0, a1 = 0.6f / s1, a2 = 0.1f / s2;
+      const float t0 = 0.1f / s0, t1 = 0.6f / s1, t2 = 0.3f / s2;
+      rr = (a0 * R0 + a1 * R1 + a2 * R2) / (6.f * (a0 + a1 + a2));
+      rl = (t0 * L0 + t1 * L1 + t2 * L2) / (6.f * (t0 + t1 + t2));
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// G = F(v + a, v + b) - f_base at interface e, for a cell of value v whose left-hand side
+// state at the interface is v + a and right-hand side state v + b.  f_base is f(v) for
+// Burgers and g(x_L) v for the linear flux, where x_L is the cell's left edge: the part of
+// the two interface fluxes that cancels in the cell's flux difference.
+//   Lax-Friedrichs (src/hrweno_fluxes.f90:43), Godunov (:67-74).
+// ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ float flux_g(const LineF& L, float v, float a, float b, float g) {
+  if (L.fn == HRW_FN_BURGERS) {
+    if (L.flux == HRW_FLUX_LAX_FRIEDRICHS)  // 4F - 2v^2 = a(2v + a + 2 alpha) + b(2v + b - 2 alpha)
+      return 0.25f * fmaf(a, 2.f * v + a + 2.f * L.alpha, b * (2.f * v + b - 2.f * L.alpha));
+    // 2F - v^2 = a(2v + a) or b(2v + b); min if vm <= vp (a <= b), else max
+    const float fa = a * (2.f * v + a), fb = b * (2.f * v + b);
+    return 0.5f * (a <= b ? fminf(fa, fb) : fmaxf(fa, fb));
+  }
+  // linear f = g u: F - g v = ((g + alpha) a + (g - alpha) b)/2 (LF) or g a / g b (Godunov)
+  if (L.flux == HRW_FLUX_LAX_FRIEDRICHS) return 0.5f * fmaf(g + L.alpha, a, (g - L.alpha) * b);
+  const float fa = g * a, fb = g * b;
+  return a <= b ? fminf(fa, fb) : fmaxf(fa, fb);
+}
+// physical flux minus the same base, for the free-outflow boundary: f(v + a) - f_base
+__device__ __forceinline__ float phys_g(const LineF& L, float v, float a, float g) {
+  if (L.fn == HRW_FN_BURGERS) return 0.5f * a * (2.f * v + a);
+  return g * a;
+}
+__device__ __forceinline__ float g_at(const LineF& L, int64_t e) {
+  return L.b != 0.f ? fmaf(L.b, fmaf(L.rx, (float)e, L.xmin), L.a) : L.a;
+}
+
+// Flux difference F_{j+1/2} - F_{j-1/2} of cell j (value v) from the offsets:
+//   left interface:  left state  v + (rr_{j-1} - d_{j-1}),  right state v + rl_j
+//   right interface: left state  v + rr_j,                  right state v + (d_j + rl_{j+1})
+// with the boundary fluxes of example1...f90:103-104 / example2...f90:117-120.
+__device__ __forceinline__ float flux_diff_f32c(const LineF& L, int64_t j, float v, float rr_m,
+                                                float d_m, float rl_j, float rr_j, float d_j,
+                                                float rl_p) {
+  const bool lin = L.fn != HRW_FN_BURGERS;
+  const float gL = lin ? g_at(L, j) : 0.f;
+  const float gR = lin ? g_at(L, j + 1) : 0.f;
+  // G_R - G_L, with the base f(v) (Burgers) or g v (linear) of both interfaces removed; the
+  // linear flux adds back (g_R - g_L) v = b rx v
+  float GL = flux_g(L, v, rr_m - d_m, rl_j, gL);
+  float GR = flux_g(L, v, rr_j, d_j + rl_p, gR);
+  float extra = lin ? L.gstep * v : 0.f;
+  if (j == 0 || j == L.nc - 1) {
+    // boundary fluxes in full (no cancellation there): F = fbase + G
+    const float fbL = lin ? gL * v : 0.5f * v * v, fbR = lin ? gR * v : 0.5f * v * v;
+    float FL = fbL + GL, FR = fbR + GR;
+    if (L.bc == HRW_BC_COPY) {
+      return 0.f;  // F_0 = F_1 or F_nc = F_{nc-1}: the boundary cell's difference vanishes
+    }
+    if (j == 0) FL = 0.f;
+    if (j == L.nc - 1) FR = L.bc == HRW_BC_ZERO ? 0.f : fbR + phys_g(L, v, rr_j, gR);
+    return FR - FL;
+  }
+  return (GR - GL) + extra;
+}
+
+}  // namespace hrw

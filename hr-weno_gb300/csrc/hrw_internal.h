@@ -48,6 +48,53 @@ struct StageArgs {
   int upwind;         // Godunov flux of g(x) u with g > 0 everywhere: F = g vm (2D kernel)
 };
 
+// ---- compensated FP32 form (hrw_f32c.cuh, stage1d_f32c.cu) ---------------------------------
+enum F32CStage : int {
+  FC_RHS = 0,   // out = L(u + dv)
+  FC_E1 = 1,    // out = dt L(u)
+  FC_RK1 = 2,   // u' = u + dt L(u)
+  FC_RK2B = 3,  // u' = u + (d1 + dt L(u + d1)) / 2
+  FC_RK3B = 4,  // out = (d1 + dt L(u + d1)) / 4
+  FC_RK3C = 5,  // u' = u + 2/3 (d2 + dt L(u + d2))
+  FC_MS = 6     // u' = u + (7 (u4 - u) + 50 dt L(u) + 10 dt L4) / 32, lout = L(u)
+};
+
+// One dimension of a compensated-FP32 problem as the kernels see it.
+struct LineF {
+  int nc;
+  int fn, bc, flux;
+  float a, b, alpha;  // g(x) = a + b x; LF alpha
+  float xmin, rx;
+  float gstep;        // g(x_{e+1}) - g(x_e) = b * rx
+  const float* rw;    // per-cell 1 / width, or null (uniform grid)
+};
+
+struct F32CArgs {
+  const float* hi;    // state u = hi + lo
+  const float* lo;
+  const float* dv;    // stored stage increment added to the stencil input, or null
+  float* out;         // increment or L(u) output
+  float* hi_out;      // new state (a buffer other than hi/lo)
+  float* lo_out;
+  const float* hi4;   // FC_MS: u^{n-4}
+  const float* lo4;
+  const float* l4;    // FC_MS: L(u^{n-4})
+  float* lout;        // FC_MS: L(u^n)
+  // scalars as float pairs so that no rounding of dt or dx biases every increment alike:
+  //   q_j = -dF_j (uniform grid) or -dF_j / width_j;  L_j = q_j * lscale;
+  //   dt L_j = (c_hi + c_lo) q_j;  dt x = (dt_hi + dt_lo) x
+  float c_hi, c_lo;   // dt / dx (uniform) or dt (per-cell widths)
+  float dt_hi, dt_lo;
+  float lscale;       // 1 / dx (uniform) or 1
+  float eps;
+  LineF L;
+};
+
+cudaError_t launch_stage1d_f32c(const F32CArgs& a, int k, int stage, cudaStream_t s);
+cudaError_t launch_split_f64(const double* u, float* hi, float* lo, int64_t n, cudaStream_t s);
+cudaError_t launch_merge_f64(const float* hi, const float* lo, double* u, int64_t n, cudaStream_t s);
+cudaError_t launch_widen_f32(const float* x, double* y, int64_t n, cudaStream_t s);
+
 // FAST flux form: the kernels evaluate F / fscale, fscale folded into rws.
 double fast_flux_scale(int flux, int fn);
 // Record msg as the calling thread's last error (hrw_last_error) and return code.

@@ -140,7 +140,11 @@ __device__ __forceinline__ void combine_fast(const StageArgs& a, int64_t j, doub
   } else if constexpr (ST == ST_RK3B) {
     a.out[j] = fma(0.75, a.u[j], fma(0.25, v, (-0.25 * a.dt * rws) * dF));
   } else if constexpr (ST == ST_RK3C) {
-    a.out[j] = fma(1.0 / 3.0, a.u[j], fma(2.0 / 3.0, v, (-(2.0 / 3.0) * a.dt * rws) * dF));
+    // (u + 2v + 2 dt L)/3 = u + 2/3 ((v - u) + dt L): the rounded 2/3 touches only the small
+    // increment.  fl(1/3) u + fl(2/3) v would scale u by fl(1/3) + fl(2/3) = 1 - 2^-54 each
+    // step, a coherent loss of mass that moves shocks.
+    const double u = a.u[j];
+    a.out[j] = fma(2.0 / 3.0, fma(-a.dt * rws, dF, v - u), u);
   } else if constexpr (ST == ST_MS) {
     const double udot = -(rws * dF);
     a.out[j] = fma(25.0 / 32.0, v,

@@ -42,8 +42,8 @@ __global__ void stage_linear_kernel(const double* __restrict__ rates, StageArgs 
       else if constexpr (ST == ST_EULER) a.out[i] = fma(dt, udot, v);
       else if constexpr (ST == ST_RK2B) a.out[i] = fma(0.5, a.u[i], fma(0.5, v, (0.5 * dt) * udot));
       else if constexpr (ST == ST_RK3B) a.out[i] = fma(0.75, a.u[i], fma(0.25, v, (0.25 * dt) * udot));
-      else if constexpr (ST == ST_RK3C)
-        a.out[i] = fma(1.0 / 3.0, a.u[i], fma(2.0 / 3.0, v, ((2.0 / 3.0) * dt) * udot));
+      else if constexpr (ST == ST_RK3C)  // u + 2/3 ((v - u) + dt udot): unbiased in u
+        a.out[i] = fma(2.0 / 3.0, fma(dt, udot, v - a.u[i]), a.u[i]);
       else if constexpr (ST == ST_MS) {
         a.out[i] = fma(25.0 / 32.0, v,
                        fma((50.0 / 32.0) * dt, udot,

@@ -12,7 +12,7 @@ LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libhrweno_gb300.so"
 
 # status codes
 HRW_OK, HRW_EINVAL, HRW_ECUDA, HRW_ESTATE, HRW_ETIMEOUT, HRW_ENOMEM = range(6)
-HRW_F64, HRW_F32 = 0, 1
+HRW_F64, HRW_F32, HRW_F32C = 0, 1, 2
 HRW_MEM_HOST, HRW_MEM_DEVICE = 0, 1
 HRW_PROBLEM_FV1D, HRW_PROBLEM_FV2D, HRW_PROBLEM_LINEAR_ODE = 1, 2, 3
 HRW_FLUX_LAX_FRIEDRICHS, HRW_FLUX_GODUNOV = 0, 1

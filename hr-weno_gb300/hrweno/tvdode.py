@@ -11,7 +11,8 @@ from . import _abi as A
 from ._arrays import describe
 from .problems import Problem
 
-_DT = {"f64": A.HRW_F64, "f32": A.HRW_F32}
+# "f64": the FP64 method; "f32c": compensated FP32 bulk precision (user arrays stay float64)
+_DT = {"f64": A.HRW_F64, "f32": A.HRW_F32, "f32c": A.HRW_F32C}
 
 
 class _tvdode:

@@ -44,7 +44,13 @@ enum {
 };
 
 /* ---- element type and memory space of user arrays -------------------------------- */
-enum { HRW_F64 = 0, HRW_F32 = 1 };
+/* HRW_F64:  the FP64 method itself; user arrays are doubles.
+ * HRW_F32:  reserved for the REAL32 build of the reference (src/hrweno_kinds.F90:9-10).
+ * HRW_F32C: compensated FP32 bulk precision (FV1D problems): user arrays stay doubles; inside,
+ *           the state is a float pair hi + lo and the right-hand side is evaluated in FP32 in
+ *           difference form (compensated neighbour differences, flux differences relative
+ *           to each cell's own flux, two-sum accumulation of u); t stays FP64. */
+enum { HRW_F64 = 0, HRW_F32 = 1, HRW_F32C = 2 };
 enum { HRW_MEM_HOST = 0, HRW_MEM_DEVICE = 1 };
 
 /* ---- problem descriptor: the right-hand side L(u) -------------------------------- */
@@ -111,8 +117,8 @@ int hrw_weno_destroy(hrw_weno* w);
 /* ---- TVD ODE integrators (rktvd / mstvd types) ------------------------------------ */
 typedef struct hrw_ode hrw_ode;
 
-/* rktvd(fu, neq, order): order 1..3; dtype HRW_F64 (the method itself) or HRW_F32
- * (bulk FP32 with a compensated two-sum accumulation of u; time stays FP64). */
+/* rktvd(fu, neq, order): order 1..3; dtype HRW_F64 (the method itself) or HRW_F32C
+ * (compensated FP32 bulk precision, FV1D problems; the user array stays FP64). */
 int hrw_rktvd_create(const hrw_problem* p, int neq, int order, int dtype, hrw_ode** out);
 /* mstvd(fu, neq): 5-step, 3rd-order TVD multistep with an RK3 start. */
 int hrw_mstvd_create(const hrw_problem* p, int neq, int dtype, hrw_ode** out);
@@ -127,8 +133,9 @@ int hrw_ode_set_stream(hrw_ode* ode, void* stream);
 int hrw_ode_destroy(hrw_ode* ode);
 
 /* ---- right-hand side alone (fu of the reference's driver) -------------------------- */
-/* vdot = L(v) at time t for problem p, both arrays device pointers of `dtype`
- * (LINEAR_ODE: neq = ncells[0]). */
+/* vdot = L(v) at time t for problem p, both arrays device pointers of doubles
+ * (LINEAR_ODE: neq = ncells[0]); dtype HRW_F64, or HRW_F32C to evaluate L in the
+ * compensated FP32 form (FV1D problems). */
 int hrw_rhs(const hrw_problem* p, int dtype, double t, const void* v, void* vdot, void* stream);
 
 /* ---- RK3 steps that allocate no device memory -------------------------------------- */

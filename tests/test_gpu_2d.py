@@ -155,4 +155,5 @@ def test_pbe_mass_balance(hw):
     m0 = float(ug.sum())
     hw.mstvd(prob, n * n).integrate(ug, 0.0, 200.5 * dt, dt)
     assert abs(float(ug.sum()) - m0) <= 1e-12 * m0
-    assert float(ug.min()) > -1e-6  # WENO keeps the pulse essentially non-negative
+    # WENO is not positivity-preserving: small undershoots at the pulse foot only
+    assert float(ug.min()) > -1e-4 * float(ug.max())

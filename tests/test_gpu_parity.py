@@ -195,12 +195,18 @@ def test_rktvd_orders(hw, orc, order, k):
     x = np.linspace(-1, 1, nc)
     u0 = 0.5 + np.exp(-20 * x ** 2) * np.sign(np.sin(9 * x))
     for numerics in ("strict", "fast"):
-        prob = hw.burgers_1d(nc, -1.0, 1.0, k=k, flux="godunov", bc="zero", numerics=numerics)
+        # outflow boundaries keep the local CFL number below 0.6 (a wall would pile mass into
+        # the last cell until forward Euler blows up)
+        prob = hw.burgers_1d(nc, -1.0, 1.0, k=k, flux="godunov", bc="copy", numerics=numerics)
         g, o = hw.rktvd(prob, nc, order), orc.ODE(prob, nc, 0, order)
         ug, uo = u0.copy(), u0.copy()
-        tg = g.integrate(ug, 0.0, 0.2, 5e-4)
-        to = o.integrate(uo, 0.0, 0.2, 5e-4)
+        # forward Euler is not stable with WENO (its amplification factor exceeds 1 on the
+        # imaginary axis), so order 1 runs 20 steps only; orders 2 and 3 run 400
+        tend = 0.2 if order > 1 else 0.01
+        tg = g.integrate(ug, 0.0, tend, 5e-4)
+        to = o.integrate(uo, 0.0, tend, 5e-4)
         assert tg == to and g.fevals == o.info()[0]
+        assert np.all(np.isfinite(uo)) and np.max(np.abs(uo)) < 2.0
         if numerics == "strict":
             assert np.array_equal(ug, uo)
         else:
@@ -218,9 +224,11 @@ def test_mstvd_1d(hw, orc, numerics):
     g, o = hw.mstvd(prob, nc), orc.ODE(prob, nc, 1)
     ug, uo = u0.copy(), u0.copy()
     tg = to = 0.0
+    # CFL 0.24: at 0.48 the multistep method sits at its stability limit and rounding grows
+    # (the FP64 and binary128 oracles then disagree completely); here they agree to 2e-15
     for tout in (0.0, 0.05, 0.1, 0.25):
-        tg = g.integrate(ug, tg, tout, 4e-4)
-        to = o.integrate(uo, to, tout, 4e-4)
+        tg = g.integrate(ug, tg, tout, 2e-4)
+        to = o.integrate(uo, to, tout, 2e-4)
         assert tg == to
         assert g.fevals == o.info()[0] and g.nsteps == o.info()[2]
         if numerics == "strict":
