@@ -351,6 +351,99 @@ def run_ours(args, dist: Dist) -> None:
     print(json.dumps(line), flush=True)
 
 
+# ------------------------------------------------------------------------------------------
+# 2D population balance (example2): 4096^2, WENO5 dimension by dimension, upwind Godunov,
+# mstvd; one step is one multistep update of the grid (one fused launch)
+# ------------------------------------------------------------------------------------------
+PBE_N = 4096
+# mstvd FP64: read u^n, u^{n-4}, L^{n-4}; write u^{n+1}, L^n
+PBE_BYTES_PER_CELL_UPDATE = 40
+
+
+def pbe_config_dict(n: int) -> dict:
+    return {"workload": f"pbe2d_{n}^2_weno5_godunov_mstvd", "cells": n * n, "k": 3,
+            "eps": 1e-6, "flux": "godunov (upwind, g1 = 1 + 0.5 x1, g2 = 0.5)",
+            "bc": "zero_inflow", "cfl": 0.4, "integrator": "mstvd (5-step, 3rd order)",
+            "numerics": "fast",
+            "l2": f"inputs larger than L2: 5 + 4 ring slots of {n * n * 8 >> 20} MiB"}
+
+
+def run_pbe2d(args, dist: Dist) -> None:
+    import torch
+
+    import hrweno
+    from hrweno import workloads
+
+    dev = dist.local if dist.world > 1 else 0
+    torch.cuda.set_device(dev)
+    n = args.pbe_n
+    cells = n * n
+    prob, n0, dt = workloads.pbe_config(n, n)
+    stream = torch.cuda.Stream()
+    ode = hrweno.mstvd(prob, cells)
+    ode.set_stream(stream.cuda_stream)
+    u = torch.from_numpy(n0).cuda()
+    # the RK3 start (4 steps + 4 right-hand sides) and W multistep steps, untimed
+    t = ode.integrate(u, 0.0, (4 + args.warmup - 0.5) * dt, dt)
+    torch.cuda.synchronize()
+    n0steps = ode.nsteps
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    dist.barrier()
+    with ClockSampler(dev) as clk:
+        e0.record(stream)
+        t = ode.integrate(u, t, t + (args.steps - 0.5) * dt, dt)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    steps_done = ode.nsteps - n0steps
+    assert steps_done == args.steps
+    el = dist.max(e0.elapsed_time(e1) * 1e-3)
+    value = dist.world * cells * args.steps / el
+    # e2e: one multistep step per reference-facing call on pinned host memory
+    ode2 = hrweno.mstvd(prob, cells)
+    ode2.set_stream(stream.cuda_stream)
+    uh = torch.from_numpy(n0.copy()).pin_memory()
+    th = ode2.integrate(uh, 0.0, 4.5 * dt, dt)
+    torch.cuda.synchronize()
+    h0 = time.perf_counter()
+    for _ in range(args.steps):
+        th = ode2.integrate(uh, th, th + 0.5 * dt, dt)
+    torch.cuda.synchronize()
+    e2e_el = dist.max(time.perf_counter() - h0)
+    if dist.rank != 0:
+        return
+    pk = peaks()
+    achieved = PBE_BYTES_PER_CELL_UPDATE * cells * args.steps / el / 1e9
+    cpu = None
+    if not args.no_cpu:
+        from oracle import oracle
+        m = 1024  # bounded sample: the 1024^2 grid, 3 multistep steps after the start
+        p1, v1, dt1 = workloads.pbe_config(m, m)
+        used = oracle.set_threads(1)
+        o = oracle.ODE(p1, m * m, 1)
+        tt = o.integrate(v1, 0.0, 4.5 * dt1, dt1)
+        c0 = time.perf_counter()
+        o.integrate(v1, tt, tt + 2.5 * dt1, dt1)
+        cel = time.perf_counter() - c0
+        cpu = {"value": m * m * 3 / cel, "unit": UNIT, "cores": used, "kind": "port",
+               "sample": f"3 mstvd steps of the 1024^2 grid ({cel:.1f} s), oracle, 1 thread"}
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic: Gaussian pulse at (0.2, 0.2), sigma 0.05",
+        "config": pbe_config_dict(n),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                     "frac": achieved / pk["hbm_gbs"], "traffic": None,
+                     "peak_src": pk["src"]},
+        "cpu_baseline": cpu,
+        "e2e": {"value": dist.world * cells * args.steps / e2e_el, "unit": UNIT,
+                "h2d_bytes_per_step": 8 * cells, "d2h_bytes_per_step": 8 * cells},
+        "gpu_launches": steps_done,
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main() -> None:
     global NC
     ap = argparse.ArgumentParser()
@@ -360,6 +453,9 @@ def main() -> None:
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-forms", action="store_true", help="skip the FP32 form")
+    ap.add_argument("--workload", default="burgers1d", choices=["burgers1d", "pbe2d"],
+                    help="burgers1d (default): the 2^24-cell line; pbe2d: the 2D PBE grid")
+    ap.add_argument("--pbe-n", type=int, default=PBE_N, help="pbe2d grid size per dimension")
     ap.add_argument("--cells", type=int, default=NC,
                     help="cells of the line (default 2^24, the benchmark workload; smaller "
                          "lines are for profiler captures)")
@@ -374,7 +470,10 @@ def main() -> None:
         return
     dist = Dist()
     try:
-        run_ours(args, dist)
+        if args.workload == "pbe2d":
+            run_pbe2d(args, dist)
+        else:
+            run_ours(args, dist)
     finally:
         dist.close()
 

@@ -338,15 +338,17 @@ static int ode_create(const hrw_problem* p, int neq, int order, int method, int 
   if ((e = cudaMalloc(&o->u, bytes)) != cudaSuccess) return cleanup(e);
   if (dtype == HRW_F32C) {
     // float buffers: rktvd 2 slots (hi, lo) + 2 increments; mstvd 5 slots + 4 L + 2 increments
+    // each array starts on a 256-byte boundary: the stage kernel reads and writes float4
     const int slots = method == 1 ? 5 : 2;
-    const size_t n = (size_t)neq, nf = n * (2 * slots + (method == 1 ? 4 : 0) + 2 + (p->width[0] ? 1 : 0));
+    const size_t n = (size_t)neq, sn = (n + 63) / 64 * 64;
+    const size_t nf = sn * (2 * slots + (method == 1 ? 4 : 0) + 2 + (p->width[0] ? 1 : 0));
     if ((e = cudaMalloc(&o->fmem, sizeof(float) * nf)) != cudaSuccess) return cleanup(e);
     float* q = o->fmem;
-    for (int k = 0; k < slots; ++k) { o->fhi[k] = q; q += n; o->flo[k] = q; q += n; }
+    for (int k = 0; k < slots; ++k) { o->fhi[k] = q; q += sn; o->flo[k] = q; q += sn; }
     if (method == 1)
-      for (int k = 0; k < 4; ++k) { o->fl[k] = q; q += n; }
-    o->fd1 = q; q += n;
-    o->fd2 = q; q += n;
+      for (int k = 0; k < 4; ++k) { o->fl[k] = q; q += sn; }
+    o->fd1 = q; q += sn;
+    o->fd2 = q; q += sn;
     F32CArgs& f = o->fbase;
     const LineArgs& L = b.L;
     f.eps = (float)p->eps;
