@@ -444,6 +444,97 @@ def run_pbe2d(args, dist: Dist) -> None:
     print(json.dumps(line), flush=True)
 
 
+# ------------------------------------------------------------------------------------------
+# batched: 4096 independent lines of log-uniform size in [64, 65536], half Burgers, half
+# linear advection, k in {2, 3}, per-problem dt; one step advances every problem one RK3 step
+# ------------------------------------------------------------------------------------------
+BATCH_NPROB = 4096
+
+
+def run_batched(args, dist: Dist) -> None:
+    import tempfile
+
+    import torch
+
+    import hrweno
+    from hrweno import workloads
+
+    dev = dist.local if dist.world > 1 else 0
+    torch.cuda.set_device(dev)
+    probs, lines, dts = workloads.batched_config(BATCH_NPROB, seed=7 + dist.rank)
+    cells = int(sum(v.size for v in lines))
+    stream = torch.cuda.Stream()
+    b = hrweno.batch(probs, order=3)
+    b.set_stream(stream.cuda_stream)
+    packed = b.pack(lines)
+    cache = str(Path(tempfile.gettempdir()) / "hrweno_batch_tune.txt")
+    shapes = b.tune(packed, dts, probe_steps=3, cache_path=cache)
+    u = torch.from_numpy(packed).cuda()
+    t = np.zeros(BATCH_NPROB)
+    b.advance(u, t, dts, args.warmup)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    dist.barrier()
+    with ClockSampler(dev) as clk:
+        e0.record(stream)
+        b.advance(u, t, dts, args.steps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    el = dist.max(e0.elapsed_time(e1) * 1e-3)
+    value = dist.world * cells * args.steps / el
+    assert bool(torch.isfinite(u).all())
+
+    # the plain path: one rktvd handle per problem, integrated one after the other
+    plain_steps = max(1, min(args.steps, 5))
+    odes = [hrweno.rktvd(p, p.ncells[0], 3) for p in probs]
+    for o in odes:
+        o.set_stream(stream.cuda_stream)
+    views = [u[int(b.offsets[i]): int(b.offsets[i]) + int(b.ncells[i])] for i in range(BATCH_NPROB)]
+    for i, o in enumerate(odes):  # warm-up: one step each
+        o.integrate(views[i], 0.0, 0.5 * dts[i], dts[i])
+    torch.cuda.synchronize()
+    p0 = time.perf_counter()
+    for i, o in enumerate(odes):
+        o.integrate(views[i], 0.0, (plain_steps - 0.5) * dts[i], dts[i])
+    torch.cuda.synchronize()
+    plain = cells * plain_steps / (time.perf_counter() - p0)
+    del odes, views
+
+    # e2e: one batched step per call on pinned host memory
+    uh = torch.from_numpy(packed.copy()).pin_memory()
+    th = np.zeros(BATCH_NPROB)
+    b.advance(uh, th, dts, 1)
+    h0 = time.perf_counter()
+    e2e_steps = max(1, min(args.steps, 10))
+    for _ in range(e2e_steps):
+        b.advance(uh, th, dts, 1)
+    e2e_el = dist.max(time.perf_counter() - h0)
+    if dist.rank != 0:
+        return
+    pk = peaks()
+    achieved = BYTES_PER_CELL_UPDATE * cells * args.steps / el / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic: seeded multi-Gaussian u0 in [0, 1] per problem",
+        "config": {"workload": f"batched_{BATCH_NPROB}_uneven_weno_lf_rk3", "problems": BATCH_NPROB,
+                   "cells": cells, "sizes": "log-uniform [64, 65536]", "k": "2 or 3",
+                   "numerics": "fast", "shapes_per_class": shapes,
+                   "l2": f"inputs larger than L2: {cells * 24 >> 20} MiB of u, u1, u2"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                     "frac": achieved / pk["hbm_gbs"], "traffic": None, "peak_src": pk["src"]},
+        "plain_per_problem": {"value": plain, "unit": UNIT, "steps": plain_steps,
+                              "speedup_batched": value / plain},
+        "cpu_baseline": None,
+        "e2e": {"value": dist.world * cells * e2e_steps / e2e_el, "unit": UNIT,
+                "h2d_bytes_per_step": 8 * b.size, "d2h_bytes_per_step": 8 * b.size},
+        "gpu_launches": 3,
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main() -> None:
     global NC
     ap = argparse.ArgumentParser()
@@ -453,7 +544,7 @@ def main() -> None:
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-forms", action="store_true", help="skip the FP32 form")
-    ap.add_argument("--workload", default="burgers1d", choices=["burgers1d", "pbe2d"],
+    ap.add_argument("--workload", default="burgers1d", choices=["burgers1d", "pbe2d", "batched"],
                     help="burgers1d (default): the 2^24-cell line; pbe2d: the 2D PBE grid")
     ap.add_argument("--pbe-n", type=int, default=PBE_N, help="pbe2d grid size per dimension")
     ap.add_argument("--cells", type=int, default=NC,
@@ -472,6 +563,8 @@ def main() -> None:
     try:
         if args.workload == "pbe2d":
             run_pbe2d(args, dist)
+        elif args.workload == "batched":
+            run_batched(args, dist)
         else:
             run_ours(args, dist)
     finally:

@@ -1,0 +1,409 @@
+// capi_batch.cu - the batch handle (hrw_batch_* in include/hrweno_gpu.h): validation, packed
+// layout, per-problem step counts, size classes, the shape autotuner and the launches.
+//
+// Every problem follows the reference's integrate contract on its own: its step count comes
+// from replaying `t = t + dt` until is_done (src/hrweno_tvdode.f90:137-143,273-284) with its
+// own t and dt, so a batched solve takes exactly the steps of a loop of single solves.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/hrweno_gpu.h"
+#include "hrw_batch.h"
+#include "hrw_internal.h"
+
+using namespace hrw;
+
+namespace {
+
+constexpr int kClasses = 3;
+// size classes by cells: [0, 512), [512, 4096), [4096, inf)
+constexpr int64_t kClassHi[kClasses] = {512, 4096, INT64_MAX};
+// shapes used before (or without) tuning: one warp with 4 cells per thread for short lines,
+// one warp with 8 for medium ones, a 256-thread block with 8 for long ones
+constexpr int kDefaultShape[kClasses] = {1, 2, 5};
+
+bool is_done(double t, double tout, double dt) { return (t - tout) * std::copysign(1.0, dt) > 0.0; }
+
+int cls_of(int64_t nc) {
+  for (int c = 0; c < kClasses; ++c)
+    if (nc < kClassHi[c]) return c;
+  return kClasses - 1;
+}
+
+}  // namespace
+
+struct hrw_batch {
+  int nprob = 0, order = 3, dtype = HRW_F64;
+  bool strict = false;
+  std::vector<BatchProblem> probs;
+  std::vector<int64_t> off;  // nprob + 1
+  int64_t total = 0;
+  std::vector<int> members[kClasses];
+  int shape[kClasses] = {kDefaultShape[0], kDefaultShape[1], kDefaultShape[2]};
+  bool tuned = false;
+  BatchProblem* d_probs = nullptr;
+  int* d_order = nullptr;
+  int* d_counter = nullptr;
+  double* u = nullptr;  // device state for host-memory calls
+  double* u1 = nullptr;
+  double* u2 = nullptr;
+  cudaStream_t own = nullptr, main = nullptr;
+  cudaStream_t side[kClasses] = {};
+  cudaEvent_t fork = nullptr, join[kClasses] = {};
+  int sms = 0;
+  std::vector<int64_t> steps_done;  // per problem, all calls
+  std::string dev_name;
+};
+
+namespace {
+
+int batch_fail(int code, const std::string& m) { return set_error(code, m.c_str()); }
+
+#define HRW_BCUDA(call)                                                                  \
+  do {                                                                                   \
+    cudaError_t e_ = (call);                                                             \
+    if (e_ != cudaSuccess)                                                               \
+      return batch_fail(e_ == cudaErrorMemoryAllocation ? HRW_ENOMEM : HRW_ECUDA,        \
+                        std::string(#call ": ") + cudaGetErrorString(e_));               \
+  } while (0)
+
+// Launch every class of the batch for the step counts already in b->probs (uploaded) on the
+// state `u`: the classes run concurrently on their own streams, each one persistent launch.
+int launch_all(hrw_batch* b, double* u, const int* shapes) {
+  std::vector<int> order;
+  std::vector<int> start(kClasses + 1, 0);
+  for (int c = 0; c < kClasses; ++c) {
+    std::vector<int> m = b->members[c];
+    std::stable_sort(m.begin(), m.end(), [&](int x, int y) {
+      return (double)b->probs[x].nc * b->probs[x].nsteps > (double)b->probs[y].nc * b->probs[y].nsteps;
+    });
+    start[c] = (int)order.size();
+    order.insert(order.end(), m.begin(), m.end());
+  }
+  start[kClasses] = (int)order.size();
+  HRW_BCUDA(cudaMemcpyAsync(b->d_probs, b->probs.data(), sizeof(BatchProblem) * b->nprob,
+                            cudaMemcpyHostToDevice, b->main));
+  HRW_BCUDA(cudaMemcpyAsync(b->d_order, order.data(), sizeof(int) * order.size(), cudaMemcpyHostToDevice,
+                            b->main));
+  HRW_BCUDA(cudaMemsetAsync(b->d_counter, 0, sizeof(int) * kClasses, b->main));
+  HRW_BCUDA(cudaEventRecord(b->fork, b->main));
+  for (int c = 0; c < kClasses; ++c) {
+    const int n = start[c + 1] - start[c];
+    HRW_BCUDA(cudaStreamWaitEvent(b->side[c], b->fork, 0));
+    if (n > 0) {
+      BatchArgs A{};
+      A.probs = b->d_probs;
+      A.order_idx = b->d_order + start[c];
+      A.nprob = n;
+      A.counter = b->d_counter + c;
+      A.u = u;
+      A.u1 = b->u1;
+      A.u2 = b->u2;
+      A.order = b->order;
+      const int per_sm = std::max(1, batch_blocks_per_sm(shapes[c], b->strict));
+      const int groups_per_block = 256 / kBatchShapes[shapes[c]].group;
+      int blocks = per_sm * b->sms;
+      blocks = std::min<int64_t>(blocks, (n + groups_per_block - 1) / groups_per_block);
+      HRW_BCUDA(launch_batch(A, shapes[c], b->strict, std::max(blocks, 1), b->side[c]));
+    }
+    HRW_BCUDA(cudaEventRecord(b->join[c], b->side[c]));
+    HRW_BCUDA(cudaStreamWaitEvent(b->main, b->join[c], 0));
+  }
+  return HRW_OK;
+}
+
+std::string tune_key(const hrw_batch* b, int c) {
+  int64_t cells = 0;
+  int mix = 0;
+  for (int p : b->members[c]) {
+    cells += b->probs[p].nc;
+    mix |= 1 << b->probs[p].k;
+  }
+  std::ostringstream s;
+  s << b->dev_name << "|class" << c << "|n" << b->members[c].size() << "|cells" << cells << "|k" << mix
+    << "|order" << b->order << "|" << (b->strict ? "strict" : "fast");
+  std::string k = s.str();
+  std::replace(k.begin(), k.end(), ' ', '_');
+  return k;
+}
+
+}  // namespace
+
+extern "C" {
+
+int hrw_batch_create(const hrw_problem* probs, int nprob, int order, int dtype, hrw_batch** out) {
+  if (!out) return batch_fail(HRW_EINVAL, "Invalid input 'out': null pointer.");
+  *out = nullptr;
+  if (!probs || nprob <= 0) return batch_fail(HRW_EINVAL, "Invalid input 'nprob': must be >= 1.");
+  if (order < 1 || order > 3)
+    return batch_fail(HRW_EINVAL, "Invalid input 'order' in 'rktvd'. Valid range: 1 <= k <= 3.");
+  if (dtype != HRW_F64) return batch_fail(HRW_EINVAL, "Invalid input 'dtype': batches support HRW_F64.");
+  hrw_batch* b = new hrw_batch;
+  b->nprob = nprob;
+  b->order = order;
+  b->dtype = dtype;
+  b->strict = probs[0].numerics == HRW_NUMERICS_STRICT;
+  b->off.resize(nprob + 1);
+  int64_t off = 0;
+  for (int i = 0; i < nprob; ++i) {
+    const hrw_problem& p = probs[i];
+    std::string where = " (problem " + std::to_string(i) + ")";
+    auto bad = [&](const char* m) {
+      delete b;
+      return batch_fail(HRW_EINVAL, std::string(m) + where);
+    };
+    if (p.kind != HRW_PROBLEM_FV1D) return bad("Invalid input 'kind': batches hold FV1D problems.");
+    if (p.ncells[0] <= 0) return bad("Invalid input 'ncells'. Valid range: ncells > 0.");
+    if (p.width[0]) return bad("Invalid input 'width': batches hold uniform grids.");
+    if (p.k < 1 || p.k > 3) return bad("Invalid input 'k'. Valid range: 1 <= k <= 3.");
+    if (!(p.eps > 2.220446049250313e-16)) return bad("Invalid input 'eps'. Valid range: eps > epsilon.");
+    if (p.flux != HRW_FLUX_LAX_FRIEDRICHS && p.flux != HRW_FLUX_GODUNOV) return bad("Invalid input 'flux'.");
+    if (p.fn[0] != HRW_FN_BURGERS && p.fn[0] != HRW_FN_LINEAR) return bad("Invalid input 'fn'.");
+    if (p.bc[0] < HRW_BC_COPY || p.bc[0] > HRW_BC_ZERO_INFLOW) return bad("Invalid input 'bc'.");
+    if (!(p.xmax[0] > p.xmin[0])) return bad("Invalid input 'xmin', 'xmax'. Valid range: xmax > xmin.");
+    if ((p.numerics == HRW_NUMERICS_STRICT) != b->strict)
+      return bad("Invalid input 'numerics': all problems of a batch share one numerics mode.");
+    BatchProblem q{};
+    q.off = off;
+    q.nc = p.ncells[0];
+    q.k = p.k;
+    q.fn = p.fn[0];
+    q.flux = p.flux;
+    q.bc = p.bc[0];
+    q.a = p.coef_a[0];
+    q.b = p.coef_b[0];
+    q.alpha = p.alpha[0];
+    q.xmin = p.xmin[0];
+    q.rx = (p.xmax[0] - p.xmin[0]) / q.nc;  // grid1%linear (src/hrweno_grids.f90:72)
+    q.rws0 = fast_flux_scale(p.flux, p.fn[0]) / q.rx;
+    q.eps = p.eps;
+    b->probs.push_back(q);
+    b->off[i] = off;
+    off += (q.nc + 63) / 64 * 64;
+    b->members[cls_of(q.nc)].push_back(i);
+  }
+  b->off[nprob] = off;
+  b->total = off;
+  b->steps_done.assign(nprob, 0);
+  auto cleanup = [&](cudaError_t e) {
+    hrw_batch_destroy(b);
+    return batch_fail(e == cudaErrorMemoryAllocation ? HRW_ENOMEM : HRW_ECUDA,
+                      std::string("hrw_batch_create: ") + cudaGetErrorString(e));
+  };
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaDeviceProp prop{};
+  if (e == cudaSuccess) e = cudaGetDeviceProperties(&prop, dev);
+  if (e != cudaSuccess) return cleanup(e);
+  b->dev_name = prop.name;
+  const size_t bytes = sizeof(double) * (size_t)off;
+  if ((e = cudaStreamCreateWithFlags(&b->own, cudaStreamDefault)) != cudaSuccess) return cleanup(e);
+  b->main = b->own;
+  for (int c = 0; c < kClasses; ++c) {
+    if ((e = cudaStreamCreateWithFlags(&b->side[c], cudaStreamNonBlocking)) != cudaSuccess) return cleanup(e);
+    if ((e = cudaEventCreateWithFlags(&b->join[c], cudaEventDisableTiming)) != cudaSuccess) return cleanup(e);
+  }
+  if ((e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming)) != cudaSuccess) return cleanup(e);
+  if ((e = cudaMalloc(&b->d_probs, sizeof(BatchProblem) * nprob)) != cudaSuccess) return cleanup(e);
+  if ((e = cudaMalloc(&b->d_order, sizeof(int) * nprob)) != cudaSuccess) return cleanup(e);
+  if ((e = cudaMalloc(&b->d_counter, sizeof(int) * kClasses)) != cudaSuccess) return cleanup(e);
+  if ((e = cudaMalloc(&b->u, bytes)) != cudaSuccess) return cleanup(e);
+  if ((e = cudaMalloc(&b->u1, bytes)) != cudaSuccess) return cleanup(e);
+  if ((e = cudaMalloc(&b->u2, bytes)) != cudaSuccess) return cleanup(e);
+  *out = b;
+  return HRW_OK;
+}
+
+int hrw_batch_layout(const hrw_batch* b, int64_t* offsets) {
+  if (!b || !offsets) return batch_fail(HRW_EINVAL, "Invalid input: null pointer.");
+  std::memcpy(offsets, b->off.data(), sizeof(int64_t) * (b->nprob + 1));
+  return HRW_OK;
+}
+
+int hrw_batch_info(const hrw_batch* b, int* shapes, int64_t* steps_done) {
+  if (!b) return batch_fail(HRW_EINVAL, "Invalid input 'batch': null handle.");
+  if (shapes)
+    for (int c = 0; c < kClasses; ++c) {
+      shapes[2 * c] = kBatchShapes[b->shape[c]].group;
+      shapes[2 * c + 1] = kBatchShapes[b->shape[c]].cells;
+    }
+  if (steps_done) std::memcpy(steps_done, b->steps_done.data(), sizeof(int64_t) * b->nprob);
+  return HRW_OK;
+}
+
+int hrw_batch_set_stream(hrw_batch* b, void* stream) {
+  if (!b) return batch_fail(HRW_EINVAL, "Invalid input 'batch': null handle.");
+  b->main = stream ? (cudaStream_t)stream : b->own;
+  return HRW_OK;
+}
+
+// Advance problem i from t[i] to the first t > tout with its own dt[i] (itask = 1), or by
+// exactly one step when itask = 2; t[] is updated.  u is the packed state (layout from
+// hrw_batch_layout) in memory space `mem`.
+int hrw_batch_integrate(hrw_batch* b, int mem, double* u, double* t, double tout, const double* dt,
+                        int itask) {
+  if (!b) return batch_fail(HRW_EINVAL, "Invalid input 'batch': null handle.");
+  if (!u || !t || !dt) return batch_fail(HRW_EINVAL, "Invalid input: null pointer.");
+  std::vector<double> tnew(b->nprob);
+  for (int i = 0; i < b->nprob; ++i) {
+    const double h = dt[i];
+    if (!(h != 0.0) || !std::isfinite(h) || !std::isfinite(t[i]))
+      return batch_fail(HRW_EINVAL, "Invalid input 'dt': must be finite and nonzero (problem " +
+                                        std::to_string(i) + ").");
+    double tt = t[i];
+    int64_t n = 0;
+    if (!is_done(tt, tout, h)) {
+      do {  // (src/hrweno_tvdode.f90:137-143)
+        tt = tt + h;
+        if (++n > (int64_t(1) << 40))
+          return batch_fail(HRW_EINVAL, "Invalid input 'dt': too many steps to reach tout.");
+      } while (!(is_done(tt, tout, h) || itask == 2));
+    }
+    b->probs[i].dt = h;
+    b->probs[i].nsteps = n;
+    tnew[i] = tt;
+  }
+  double* du = u;
+  const size_t bytes = sizeof(double) * (size_t)b->total;
+  if (mem == HRW_MEM_HOST) {
+    du = b->u;
+    HRW_BCUDA(cudaMemcpyAsync(du, u, bytes, cudaMemcpyHostToDevice, b->main));
+  }
+  int rc = launch_all(b, du, b->shape);
+  if (rc != HRW_OK) return rc;
+  if (mem == HRW_MEM_HOST) HRW_BCUDA(cudaMemcpyAsync(u, du, bytes, cudaMemcpyDeviceToHost, b->main));
+  HRW_BCUDA(cudaStreamSynchronize(b->main));
+  for (int i = 0; i < b->nprob; ++i) {
+    t[i] = tnew[i];
+    b->steps_done[i] += b->probs[i].nsteps;
+  }
+  return HRW_OK;
+}
+
+// nsteps steps of every problem (nsteps calls of integrate(itask = 2) each), one launch per
+// size class; t[] is updated with the reference's t = t + dt sequence.
+int hrw_batch_advance(hrw_batch* b, int mem, double* u, double* t, const double* dt, int64_t nsteps) {
+  if (!b) return batch_fail(HRW_EINVAL, "Invalid input 'batch': null handle.");
+  if (!u || !t || !dt) return batch_fail(HRW_EINVAL, "Invalid input: null pointer.");
+  if (nsteps < 0) return batch_fail(HRW_EINVAL, "Invalid input 'nsteps': must be >= 0.");
+  for (int i = 0; i < b->nprob; ++i) {
+    if (!(dt[i] != 0.0) || !std::isfinite(dt[i]) || !std::isfinite(t[i]))
+      return batch_fail(HRW_EINVAL, "Invalid input 'dt': must be finite and nonzero (problem " +
+                                        std::to_string(i) + ").");
+    b->probs[i].dt = dt[i];
+    b->probs[i].nsteps = nsteps;
+  }
+  double* du = u;
+  const size_t bytes = sizeof(double) * (size_t)b->total;
+  if (mem == HRW_MEM_HOST) {
+    du = b->u;
+    HRW_BCUDA(cudaMemcpyAsync(du, u, bytes, cudaMemcpyHostToDevice, b->main));
+  }
+  int rc = launch_all(b, du, b->shape);
+  if (rc != HRW_OK) return rc;
+  if (mem == HRW_MEM_HOST) HRW_BCUDA(cudaMemcpyAsync(u, du, bytes, cudaMemcpyDeviceToHost, b->main));
+  HRW_BCUDA(cudaStreamSynchronize(b->main));
+  for (int i = 0; i < b->nprob; ++i) {
+    for (int64_t n = 0; n < nsteps; ++n) t[i] = t[i] + dt[i];
+    b->steps_done[i] += nsteps;
+  }
+  return HRW_OK;
+}
+
+// Autotuner: for every size class, time `probe_steps` steps of that class alone with each
+// candidate shape, and keep the fastest.  The probes run on the handle's scratch copy of the
+// state u (memory space `mem`), which they advance; u itself is not changed.  Results are
+// cached in the text file cache_path (one "key shape" line per class; NULL: no cache), keyed
+// by the device name and the class's problem count, total cells, k mix, order and numerics.
+int hrw_batch_tune(hrw_batch* b, int mem, const double* u, const double* dt, int probe_steps,
+                   const char* cache_path) {
+  if (!b || !u || !dt) return batch_fail(HRW_EINVAL, "Invalid input: null pointer.");
+  if (probe_steps < 1) probe_steps = 1;
+  std::vector<std::pair<std::string, int>> cache;
+  if (cache_path) {
+    std::ifstream in(cache_path);
+    std::string k;
+    int s;
+    while (in >> k >> s)
+      if (s >= 0 && s < kNumBatchShapes) cache.emplace_back(k, s);
+  }
+  const size_t bytes = sizeof(double) * (size_t)b->total;
+  HRW_BCUDA(cudaMemcpyAsync(b->u, u, bytes,
+                            mem == HRW_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice,
+                            b->main));
+  cudaEvent_t e0, e1;
+  HRW_BCUDA(cudaEventCreate(&e0));
+  HRW_BCUDA(cudaEventCreate(&e1));
+  bool wrote = false;
+  for (int c = 0; c < kClasses; ++c) {
+    if (b->members[c].empty()) continue;
+    const std::string key = tune_key(b, c);
+    auto hit = std::find_if(cache.begin(), cache.end(), [&](auto& kv) { return kv.first == key; });
+    if (hit != cache.end()) {
+      b->shape[c] = hit->second;
+      continue;
+    }
+    // only this class advances during its probe
+    for (int i = 0; i < b->nprob; ++i) {
+      b->probs[i].dt = dt[i];
+      b->probs[i].nsteps = 0;
+    }
+    for (int p : b->members[c]) b->probs[p].nsteps = probe_steps;
+    float best = 1e30f;
+    int best_s = kDefaultShape[c];
+    for (int s = 0; s < kNumBatchShapes; ++s) {
+      int shapes[kClasses] = {b->shape[0], b->shape[1], b->shape[2]};
+      shapes[c] = s;
+      float ms = 0.f;
+      for (int rep = 0; rep < 2; ++rep) {  // first run warms up
+        HRW_BCUDA(cudaEventRecord(e0, b->main));
+        int rc = launch_all(b, b->u, shapes);
+        if (rc != HRW_OK) return rc;
+        HRW_BCUDA(cudaEventRecord(e1, b->main));
+        HRW_BCUDA(cudaEventSynchronize(e1));
+        HRW_BCUDA(cudaEventElapsedTime(&ms, e0, e1));
+      }
+      if (ms < best) best = ms, best_s = s;
+    }
+    b->shape[c] = best_s;
+    cache.emplace_back(key, best_s);
+    wrote = true;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  b->tuned = true;
+  if (wrote && cache_path) {
+    std::ofstream outf(cache_path);
+    for (auto& kv : cache) outf << kv.first << " " << kv.second << "\n";
+  }
+  return HRW_OK;
+}
+
+int hrw_batch_destroy(hrw_batch* b) {
+  if (!b) return HRW_OK;
+  if (b->d_probs) cudaFree(b->d_probs);
+  if (b->d_order) cudaFree(b->d_order);
+  if (b->d_counter) cudaFree(b->d_counter);
+  if (b->u) cudaFree(b->u);
+  if (b->u1) cudaFree(b->u1);
+  if (b->u2) cudaFree(b->u2);
+  for (int c = 0; c < kClasses; ++c) {
+    if (b->side[c]) cudaStreamDestroy(b->side[c]);
+    if (b->join[c]) cudaEventDestroy(b->join[c]);
+  }
+  if (b->fork) cudaEventDestroy(b->fork);
+  if (b->own) cudaStreamDestroy(b->own);
+  delete b;
+  return HRW_OK;
+}
+
+}  // extern "C"

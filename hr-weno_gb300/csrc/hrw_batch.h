@@ -1,0 +1,41 @@
+// hrw_batch.h - device-side layout of a batch of independent 1D problems (batch.cu).
+#pragma once
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+namespace hrw {
+
+// One problem of the batch: the example1 right-hand side on its own uniform line, with its own
+// time step and number of steps for the current integrate call.
+struct BatchProblem {
+  int64_t off;     // first cell in the packed arrays (a multiple of 64)
+  int nc, k, fn, flux, bc;
+  double a, b, alpha, xmin, rx, rws0, eps;
+  double dt;
+  int64_t nsteps;
+};
+
+struct BatchArgs {
+  const BatchProblem* probs;
+  const int* order_idx;  // problems of this launch, most expensive first
+  int nprob;
+  int* counter;          // next entry of order_idx to claim
+  double* u;             // packed state
+  double* u1;            // packed stage arrays
+  double* u2;
+  int order;             // rktvd order 1..3
+};
+
+struct BatchShape {
+  int group;  // threads that share one problem (whole warps)
+  int cells;  // consecutive cells per thread and pass
+};
+
+constexpr int kNumBatchShapes = 6;
+extern const BatchShape kBatchShapes[kNumBatchShapes];
+
+int batch_blocks_per_sm(int shape, bool strict);
+cudaError_t launch_batch(const BatchArgs& B, int shape, bool strict, int blocks, cudaStream_t s);
+
+}  // namespace hrw

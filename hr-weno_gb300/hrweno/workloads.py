@@ -8,6 +8,9 @@
                              alpha = max|u0|, copy boundaries, dt = CFL dx / max|u0|
     pbe_gaussian_2d(n1, n2)  Gaussian pulse at (0.2, 0.2), sigma 0.05 on [0, 1]^2, x1 fastest
                              (example/example2_pbe_2d_fv.f90:41-52)
+    batched_config(nprob)    independent 1D problems: cell counts log-uniform in [64, 65536],
+                             half Burgers, half linear advection a ~ U(-1, 1), k in {2, 3},
+                             multi-Gaussian u0 in [0, 1], LF flux, per-problem dt at CFL 0.4
 """
 from __future__ import annotations
 
@@ -69,3 +72,37 @@ def pbe_config(n1: int, n2: int, cfl: float = 0.4, k: int = 3, bc: str = "zero_i
                   numerics=numerics)
     dt = cfl / (1.5 * n1 + 0.5 * n2)
     return prob, pbe_gaussian_2d(n1, n2), dt
+
+
+def batched_config(nprob: int = 4096, seed: int = 7, nmin: int = 64, nmax: int = 65536,
+                   cfl: float = 0.4, numerics: str = "fast"):
+    """(problems, initial lines, dt per problem) of the batched workload on [-5, 5]."""
+    from .problems import Problem
+    rng = np.random.default_rng(seed)
+    ncs = np.exp(rng.uniform(np.log(nmin), np.log(nmax), nprob)).astype(np.int64)
+    probs, lines, dts = [], [], []
+    for i in range(nprob):
+        n = int(ncs[i])
+        k = int(rng.integers(2, 4))
+        ng = int(rng.integers(1, 5))
+        x = centres(n, -5.0, 5.0)
+        u = np.zeros(n)
+        for _ in range(ng):
+            u += rng.uniform(0.2, 1.0) * np.exp(-((x - rng.uniform(-4, 4)) / rng.uniform(0.1, 1.0)) ** 2)
+        u *= 1.0 / max(1.0, float(u.max()))  # u0 in [0, 1]
+        if i % 2 == 0:  # Burgers
+            alpha = max(float(np.max(np.abs(u))), 1e-3)
+            p = Problem(kind="fv1d", ncells=(n, 1), k=k, flux="lax_friedrichs",
+                        fn=("burgers", "burgers"), alpha=(alpha, alpha), bc=("copy", "copy"),
+                        xmin=(-5.0, 0.0), xmax=(5.0, 1.0), numerics=numerics)
+        else:  # linear advection f = a u
+            a = float(rng.uniform(-1.0, 1.0))
+            alpha = max(abs(a), 1e-3)
+            p = Problem(kind="fv1d", ncells=(n, 1), k=k, flux="lax_friedrichs",
+                        fn=("linear", "linear"), coef_a=(a, 0.0), coef_b=(0.0, 0.0),
+                        alpha=(alpha, alpha), bc=("copy", "copy"), xmin=(-5.0, 0.0),
+                        xmax=(5.0, 1.0), numerics=numerics)
+        probs.append(p)
+        lines.append(u)
+        dts.append(cfl * (10.0 / n) / alpha)
+    return probs, lines, np.array(dts)

@@ -138,6 +138,37 @@ int hrw_ode_destroy(hrw_ode* ode);
  * compensated FP32 form (FV1D problems). */
 int hrw_rhs(const hrw_problem* p, int dtype, double t, const void* v, void* vdot, void* stream);
 
+/* ---- batches of independent 1D problems ------------------------------------------- */
+/* A batch holds nprob independent FV1D problems on uniform grids (each its own rktvd(fu,
+ * neq, order) of the reference, src/hrweno_tvdode.f90:69-178, with its own ncells, k, flux,
+ * flux function, alpha and boundaries; all share `order`, dtype HRW_F64 and one numerics
+ * mode).  Their states are packed in one array: problem i occupies cells
+ * [offsets[i], offsets[i] + ncells_i) of the layout returned by hrw_batch_layout
+ * (offsets[nprob] is the packed length).  One call advances every problem with one
+ * persistent launch per size class, the classes running concurrently. */
+typedef struct hrw_batch hrw_batch;
+int hrw_batch_create(const hrw_problem* problems, int nprob, int order, int dtype, hrw_batch** out);
+/* offsets[0 .. nprob] of the packed layout */
+int hrw_batch_layout(const hrw_batch* b, int64_t* offsets);
+/* Per problem i: integrate(u_i, t[i], tout, dt[i], itask) with the reference's stopping rule
+ * (itask 1: to the first t > tout; 2: one step); t[] is updated.  u: packed state in `mem`. */
+int hrw_batch_integrate(hrw_batch* b, int mem, double* u, double* t, double tout, const double* dt,
+                        int itask);
+/* Exactly nsteps steps of every problem (nsteps integrate calls with itask = 2 each) in one
+ * persistent launch per size class; t[] is advanced by the reference's t = t + dt. */
+int hrw_batch_advance(hrw_batch* b, int mem, double* u, double* t, const double* dt, int64_t nsteps);
+/* Autotuner: time probe_steps steps of each size class with every candidate (group size,
+ * cells per thread) shape on a scratch copy of u and keep the fastest; cache_path (nullable)
+ * is a text cache keyed by device and class. */
+int hrw_batch_tune(hrw_batch* b, int mem, const double* u, const double* dt, int probe_steps,
+                   const char* cache_path);
+/* shapes[2c], shapes[2c+1]: group threads and cells per thread of size class c (3 classes:
+ * < 512, < 4096, >= 4096 cells); steps_done[i]: steps taken by problem i so far (nullable). */
+int hrw_batch_info(const hrw_batch* b, int* shapes, int64_t* steps_done);
+/* Run on `stream` (a cudaStream_t; NULL restores the handle's own stream). */
+int hrw_batch_set_stream(hrw_batch* b, void* stream);
+int hrw_batch_destroy(hrw_batch* b);
+
 /* ---- RK3 steps that allocate no device memory -------------------------------------- */
 /* No counterpart in the reference.  For callers that cannot allocate device memory: a
  * framework whose caching allocator already owns the whole device, or a step loop that must

@@ -1,0 +1,116 @@
+"""Batched solves (hrw_batch_*) against the oracle and against one-problem-at-a-time solves.
+
+Tolerances: STRICT numerics bit-identical to the oracle; FAST numerics bit-identical to the
+single-problem FAST path (same per-cell arithmetic whatever the launch shape) and within
+1e-12 (normwise relative) of the oracle.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def nrel(a, b):
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+def mixed_problems(hw, numerics, sizes=(1, 2, 3, 5, 8, 31, 64, 200, 511, 512, 600, 1000, 4095,
+                                          4096, 5000, 9000, 20000)):
+    """Every flux, flux function, boundary kind and k across sizes that cross the classes."""
+    rng = np.random.default_rng(5)
+    probs, lines, dts = [], [], []
+    combos = [("lax_friedrichs", "burgers", "copy"), ("godunov", "burgers", "zero"),
+              ("lax_friedrichs", "linear", "zero_inflow"), ("godunov", "linear", "copy")]
+    for i, n in enumerate(sizes):
+        flux, fn, bc = combos[i % 4]
+        k = 1 + i % 3
+        x = np.linspace(-1, 1, n)
+        u = 0.3 + 0.5 * np.exp(-10 * x ** 2) * np.sign(np.sin(7 * x + i)) + 0.01 * rng.standard_normal(n)
+        a = float(rng.uniform(-1, 1))
+        p = hw.Problem(kind="fv1d", ncells=(n, 1), k=k, flux=flux, fn=(fn, fn),
+                       coef_a=(a, 0.0), coef_b=(0.2 if fn == "linear" and i % 3 == 0 else 0.0, 0.0),
+                       alpha=(1.5, 1.5), bc=(bc, bc), xmin=(-1.0, 0.0), xmax=(1.0, 1.0),
+                       numerics=numerics)
+        probs.append(p)
+        lines.append(u)
+        dts.append(0.3 * (2.0 / n) / 1.5)
+    return probs, lines, np.array(dts)
+
+
+@pytest.mark.parametrize("numerics", ["strict", "fast"])
+@pytest.mark.parametrize("order", [1, 2, 3])
+def test_batch_vs_oracle(hw, orc, numerics, order):
+    probs, lines, dts = mixed_problems(hw, numerics)
+    b = hw.batch(probs, order=order)
+    u = b.pack(lines)
+    t = np.zeros(len(probs))
+    steps = 8 if order == 1 else 40
+    tout = 1e9  # itask=2 semantics below: exactly `steps` steps per problem
+    b.integrate(u, t, tout, dts, itask=2)
+    b.advance(u, t, dts, steps - 1)
+    assert np.all(b.steps_done == steps)
+    got = b.unpack(u)
+    for i, (p, v) in enumerate(zip(probs, lines)):
+        o = orc.ODE(p, p.ncells[0], 0, order)
+        uo = v.copy()
+        to = 0.0
+        for _ in range(steps):
+            to = o.integrate(uo, to, tout, dts[i], itask=2)
+        assert t[i] == to
+        if numerics == "strict":
+            assert np.array_equal(got[i], uo), (i, p.ncells[0])
+        else:
+            assert nrel(got[i], uo) <= 1e-12, (i, p.ncells[0], nrel(got[i], uo))
+
+
+def test_batch_fast_equals_single_problem_path(hw):
+    """The batched FAST kernel and the single-problem FAST kernel give the same bits."""
+    import torch
+    from hrweno import workloads
+    probs, lines, dts = workloads.batched_config(96, seed=3, nmax=20000)
+    b = hw.batch(probs, order=3)
+    u = torch.from_numpy(b.pack(lines)).cuda()
+    t = np.zeros(len(probs))
+    b.integrate(u, t, 25.5 * dts.max(), dts)  # itask 1: each problem to its own step count
+    got = b.unpack(u)
+    for i, p in enumerate(probs):
+        ug = torch.from_numpy(lines[i].copy()).cuda()
+        ts = hw.rktvd(p, p.ncells[0], 3).integrate(ug, 0.0, 25.5 * dts.max(), dts[i])
+        assert ts == t[i]
+        assert np.array_equal(got[i], ug.cpu().numpy()), i
+
+
+def test_batch_shapes_agree_and_tuner_caches(hw, tmp_path):
+    """Every candidate shape gives the same bits; the tuner's cache is reused."""
+    import torch
+    from hrweno import workloads
+    probs, lines, dts = workloads.batched_config(64, seed=11, nmax=12000)
+    u0 = workloads  # noqa: F841
+    ref = None
+    cache = str(tmp_path / "tune.txt")
+    b = hw.batch(probs, order=3)
+    packed = b.pack(lines)
+    shapes = b.tune(packed, dts, probe_steps=2, cache_path=cache)
+    assert len(shapes) == 3
+    text = open(cache).read()
+    assert text.count("\n") >= 1
+    b2 = hw.batch(probs, order=3)
+    assert b2.tune(packed, dts, probe_steps=2, cache_path=cache) == shapes
+    for bb in (b, b2):
+        u = torch.from_numpy(packed.copy()).cuda()
+        t = np.zeros(len(probs))
+        bb.integrate(u, t, 10.5 * dts.max(), dts)
+        if ref is None:
+            ref = u.cpu().numpy()
+        assert np.array_equal(u.cpu().numpy(), ref)
+
+
+def test_batch_validation(hw):
+    from hrweno import HrwError
+    ok = hw.burgers_1d(10)
+    with pytest.raises(HrwError, match="uniform grids"):
+        hw.batch([ok, hw.burgers_1d(10, width=np.full(10, 0.1))])
+    with pytest.raises(HrwError, match="one numerics mode"):
+        hw.batch([ok, hw.burgers_1d(10, numerics="strict")])
+    with pytest.raises(HrwError, match="FV1D"):
+        hw.batch([ok, hw.pbe_2d(4, 4)])
