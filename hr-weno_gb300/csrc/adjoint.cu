@@ -1,0 +1,565 @@
+// adjoint.cu - discrete adjoint of WENO reconstruction + global Lax-Friedrichs flux + rktvd(3)
+// for J = 0.5 ||u(T) - u_target||^2, with checkpointed recompute (hrw_adjoint_* in
+// include/hrweno_gpu.h).  No counterpart in the reference, which has no derivatives.
+//
+// Forward map of one step (src/hrweno_tvdode.f90:161-169) with L the example1 right-hand side
+// (example/example1_burgers_1d_fv.f90:72-109) and the fixed-alpha LF flux
+// (src/hrweno_fluxes.f90:43):
+//   u1 = u + dt L(u),  u2 = 3/4 u + 1/4 (u1 + dt L(u1)),  u' = 1/3 u + 2/3 (u2 + dt L(u2)).
+// Its transpose, given lambda' = dJ/du':
+//   A3: l2 = 2/3 (lambda' + dt J(u2)^T lambda'),     acc = 1/3 lambda'
+//   A2: l1 = 1/4 (l2 + dt J(u1)^T l2),               acc += 3/4 l2
+//   A1: lambda = acc + l1 + dt J(u)^T l1
+// where J(v)^T mu is the vector-Jacobian product of L.  It is assembled per cell i from the
+// adjoints of its two reconstructed states, ar_i = dF_{i+1/2}/dvr_i * phi_{i+1/2} and
+// al_i = dF_{i-1/2}/dvl_i * phi_{i-1/2} (phi = the flux adjoint from mu and the boundary
+// rules), pushed back through the WENO map: the candidates are linear, the weights
+// w_r = alpha_r / sum(alpha) with alpha_r = d_r/(eps + beta_r)^2 give
+//   d vr / d beta_s = -2 w_s (q_s - vr) / (eps + beta_s),
+// and the smoothness indicators are quadratic forms.  eps > 0 keeps all of this smooth.
+//
+// Lines are segment-aware: the state holds nseg independent problems of `seg` cells each,
+// every segment with its own boundaries and ghost cells, so one launch serves one long line
+// or a batch of equal-size problems.
+#include <cmath>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/hrweno_gpu.h"
+#include "hrw_device.cuh"
+#include "hrw_internal.h"
+#include "hrw_stage.cuh"
+
+namespace hrw {
+
+namespace {
+
+constexpr unsigned FULL = 0xffffffffu;
+
+struct AdjLine {
+  int64_t n;    // total cells
+  int64_t seg;  // cells per problem (segment)
+  int k, fn, bc;
+  double a, b, alpha, xmin, rx, rdx, eps;
+  double rws0;  // FAST flux scale / dx (stage kernels)
+};
+
+__device__ __forceinline__ LineArgs line_args(const AdjLine& A) {
+  LineArgs L{};
+  L.nc = (int)A.seg;
+  L.fn = A.fn;
+  L.bc = A.bc;
+  L.flux = HRW_FLUX_LAX_FRIEDRICHS;
+  L.a = A.a;
+  L.b = A.b;
+  L.alpha = A.alpha;
+  L.xmin = A.xmin;
+  L.rx = A.rx;
+  L.rws0 = A.rws0;
+  return L;
+}
+
+// --------------------------------------------------------------------------------------------
+// Forward stage (FAST FP64), segment-aware: the warp-pass of the batched kernel with ghosts
+// replicating the first and last cell of each segment.  Requires seg % C == 0 or one segment.
+// --------------------------------------------------------------------------------------------
+template <int K, int ST, int C>
+__global__ void __launch_bounds__(256) adj_fwd_kernel(AdjLine A, StageArgs a) {
+  const LineArgs L = line_args(A);
+  const int lane = threadIdx.x & 31;
+  const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t wv = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; wv * 32 * C < A.n; wv += nwarps) {
+    const int64_t j0 = wv * 32 * C + (int64_t)lane * C;
+    const int64_t jc = j0 < A.n ? j0 : A.n - 1;
+    const int64_t s0 = jc / A.seg * A.seg, s1 = s0 + A.seg - 1;
+    double w[C + 2 * K];
+#pragma unroll
+    for (int q = 0; q < C + 2 * K; ++q) {
+      int64_t g = j0 - K + q;
+      g = g < s0 ? s0 : (g > s1 ? s1 : g);
+      w[q] = a.v[g];
+    }
+    double vl[C], vr[C];
+    recon_fast<K, C>(w, a.eps, vl, vr);
+    double e[2 * K - 1];
+#pragma unroll
+    for (int q = 0; q < 2 * K - 1; ++q) e[q] = lane == 31 ? w[C + 1 + q] : w[q];
+    double el, er;
+    recon_fast_one<K>(&e[K - 1], a.eps, el, er);
+    const double vr_up = __shfl_up_sync(FULL, vr[C - 1], 1);
+    const double vl_dn = __shfl_down_sync(FULL, vl[0], 1);
+    const double vr_m = lane == 0 ? er : vr_up;  // interfaces across segments are never used:
+    const double vl_p = lane == 31 ? el : vl_dn;  // the boundary rules replace them
+    const int64_t l0 = j0 - s0;  // local index of the first cell
+    double F[C + 1];
+    F[0] = flux_fast(L, vr_m, vl[0], l0);
+#pragma unroll
+    for (int c = 1; c < C; ++c) F[c] = flux_fast(L, vr[c - 1], vl[c], l0 + c);
+    F[C] = flux_fast(L, vr[C - 1], vl_p, l0 + C);
+#pragma unroll
+    for (int c = 0; c < C; ++c) {
+      const int64_t j = j0 + c;
+      if (j >= A.n) break;
+      const double dF = flux_diff<false>(L, l0 + c, F[c], F[c + 1], vr[c]);
+      combine_fast<ST>(a, j, w[K + c], dF, L.rws0);
+    }
+  }
+}
+
+// --------------------------------------------------------------------------------------------
+// Reverse WENO of one cell: stencil p[-(K-1) .. K-1], adjoints ar (of vr) and al (of vl);
+// adds d(ar vr + al vl)/dp into out[0 .. 2K-2].  Also returns vr and vl.
+// --------------------------------------------------------------------------------------------
+template <int K>
+__device__ __forceinline__ void weno_vjp_states(const double* p, double eps, double& vl, double& vr) {
+  double l, r;
+  recon_fast_one<K>(p, eps, l, r);
+  vl = l;
+  vr = r;
+}
+
+template <int K>
+__device__ __forceinline__ void weno_vjp(const double* p, double eps, double ar, double al, double* out) {
+  if constexpr (K == 1) {
+    out[0] += ar + al;
+  } else if constexpr (K == 2) {
+    // stencil v_{-1}, v_0, v_1; q0 = (v0 + v1)/2, q1 = (3 v0 - v_{-1})/2; vl: (3 v0 - v1)/2,
+    // (v_{-1} + v0)/2; beta0 = (v1 - v0)^2, beta1 = (v0 - v_{-1})^2; d = (2, 1)/3
+    const double vm = p[-1], v0 = p[0], v1 = p[1];
+    const double D0 = v1 - v0, D1 = v0 - vm;
+    const double ie0 = rcp_fast(eps + D0 * D0), ie1 = rcp_fast(eps + D1 * D1);
+    const double a0 = (2.0 / 3.0) * ie0 * ie0, a1 = (1.0 / 3.0) * ie1 * ie1;
+    const double t0 = (1.0 / 3.0) * ie0 * ie0, t1 = (2.0 / 3.0) * ie1 * ie1;
+    const double iS = rcp_fast(a0 + a1), iT = rcp_fast(t0 + t1);
+    const double w0 = a0 * iS, w1 = a1 * iS, u0 = t0 * iT, u1 = t1 * iT;
+    const double q0 = 0.5 * (v0 + v1), q1 = 0.5 * fma(3.0, v0, -vm);
+    const double r0 = 0.5 * fma(3.0, v0, -v1), r1 = 0.5 * (vm + v0);
+    const double vrr = fma(w0, q0, w1 * q1), vll = fma(u0, r0, u1 * r1);
+    // dbeta_s = -2 [ar w_s (q_s - vr) + al u_s (r_s - vl)] / (eps + beta_s)
+    const double db0 = -2.0 * ie0 * fma(ar * w0, q0 - vrr, al * u0 * (r0 - vll));
+    const double db1 = -2.0 * ie1 * fma(ar * w1, q1 - vrr, al * u1 * (r1 - vll));
+    const double dq0 = ar * w0, dq1 = ar * w1, dr0 = al * u0, dr1 = al * u1;
+    // beta0 = D0^2: d/dv1 = 2 D0, d/dv0 = -2 D0; beta1 = D1^2: d/dv0 = 2 D1, d/dvm = -2 D1
+    const double g0 = 2.0 * D0 * db0, g1 = 2.0 * D1 * db1;
+    out[0] += -0.5 * dq1 + 0.5 * dr1 - g1;
+    out[1] += 0.5 * dq0 + 1.5 * dq1 + 1.5 * dr0 + 0.5 * dr1 - g0 + g1;
+    out[2] += 0.5 * dq0 - 0.5 * dr0 + g0;
+  } else {
+    // stencil v_{-2} .. v_2 (index 0..4); candidates x6 (c3 table, src/hrweno_weno.f90:19-21)
+    const double vmm = p[-2], vm = p[-1], v0 = p[0], v1 = p[1], v2 = p[2];
+    const double A0 = v0 - 2.0 * v1 + v2, B0 = 3.0 * v0 - 4.0 * v1 + v2;
+    const double A1 = vm - 2.0 * v0 + v1, B1 = vm - v1;
+    const double A2 = vmm - 2.0 * vm + v0, B2 = vmm - 4.0 * vm + 3.0 * v0;
+    const double c13 = 13.0 / 12.0;
+    const double b0 = fma(c13 * A0, A0, 0.25 * B0 * B0);
+    const double b1 = fma(c13 * A1, A1, 0.25 * B1 * B1);
+    const double b2 = fma(c13 * A2, A2, 0.25 * B2 * B2);
+    const double ie0 = rcp_fast(eps + b0), ie1 = rcp_fast(eps + b1), ie2 = rcp_fast(eps + b2);
+    const double s0 = ie0 * ie0, s1 = ie1 * ie1, s2 = ie2 * ie2;
+    const double a0 = 0.3 * s0, a1 = 0.6 * s1, a2 = 0.1 * s2;  // d = (3, 6, 1)/10
+    const double t0 = 0.1 * s0, t1 = 0.6 * s1, t2 = 0.3 * s2;  // mirrored
+    const double iS = rcp_fast(a0 + a1 + a2), iT = rcp_fast(t0 + t1 + t2);
+    const double w0 = a0 * iS, w1 = a1 * iS, w2 = a2 * iS;
+    const double u0 = t0 * iT, u1 = t1 * iT, u2 = t2 * iT;
+    const double q0 = (2.0 * v0 + 5.0 * v1 - v2) * (1.0 / 6.0);
+    const double q1 = (-vm + 5.0 * v0 + 2.0 * v1) * (1.0 / 6.0);
+    const double q2 = (2.0 * vmm - 7.0 * vm + 11.0 * v0) * (1.0 / 6.0);
+    const double r0 = (11.0 * v0 - 7.0 * v1 + 2.0 * v2) * (1.0 / 6.0);
+    const double r1 = (2.0 * vm + 5.0 * v0 - v1) * (1.0 / 6.0);
+    const double r2 = (-vmm + 5.0 * vm + 2.0 * v0) * (1.0 / 6.0);
+    const double vrr = w0 * q0 + w1 * q1 + w2 * q2;
+    const double vll = u0 * r0 + u1 * r1 + u2 * r2;
+    const double db0 = -2.0 * ie0 * fma(ar * w0, q0 - vrr, al * u0 * (r0 - vll));
+    const double db1 = -2.0 * ie1 * fma(ar * w1, q1 - vrr, al * u1 * (r1 - vll));
+    const double db2 = -2.0 * ie2 * fma(ar * w2, q2 - vrr, al * u2 * (r2 - vll));
+    const double dq0 = ar * w0 * (1.0 / 6.0), dq1 = ar * w1 * (1.0 / 6.0), dq2 = ar * w2 * (1.0 / 6.0);
+    const double dr0 = al * u0 * (1.0 / 6.0), dr1 = al * u1 * (1.0 / 6.0), dr2 = al * u2 * (1.0 / 6.0);
+    // d beta_s: 13/6 A_s grad(A_s) + 1/2 B_s grad(B_s)
+    const double gA0 = (13.0 / 6.0) * A0 * db0, gB0 = 0.5 * B0 * db0;
+    const double gA1 = (13.0 / 6.0) * A1 * db1, gB1 = 0.5 * B1 * db1;
+    const double gA2 = (13.0 / 6.0) * A2 * db2, gB2 = 0.5 * B2 * db2;
+    // grad A0 = (0,0,1,-2,1), B0 = (0,0,3,-4,1); A1 = (0,1,-2,1,0), B1 = (0,1,0,-1,0);
+    // A2 = (1,-2,1,0,0), B2 = (1,-4,3,0,0); q/r coefficient rows x6 as above
+    out[0] += 2.0 * dq2 - dr2 + gA2 + gB2;
+    out[1] += -dq1 - 7.0 * dq2 + 2.0 * dr1 + 5.0 * dr2 + gA1 + gB1 - 2.0 * gA2 - 4.0 * gB2;
+    out[2] += 2.0 * dq0 + 5.0 * dq1 + 11.0 * dq2 + 11.0 * dr0 + 5.0 * dr1 + 2.0 * dr2 + gA0 +
+              3.0 * gB0 - 2.0 * gA1 + gA2 + 3.0 * gB2;
+    out[3] += 5.0 * dq0 + 2.0 * dq1 - 7.0 * dr0 - dr1 - 2.0 * gA0 - 4.0 * gB0 + gA1 - gB1;
+    out[4] += -dq0 + 2.0 * dr0 + gA0 + gB0;
+  }
+}
+
+// does cell with local index lc use the interface flux on its right / left?
+__device__ __forceinline__ bool uses_fr(int bc, int64_t lc, int64_t seg) {
+  if (bc == HRW_BC_COPY) return lc > 0 && lc < seg - 1;
+  return lc < seg - 1;  // ZERO, ZERO_INFLOW: the last cell's right flux is the boundary's
+}
+__device__ __forceinline__ bool uses_fl(int bc, int64_t lc, int64_t seg) {
+  if (bc == HRW_BC_COPY) return lc > 0 && lc < seg - 1;
+  return lc > 0;
+}
+
+__device__ __forceinline__ double dflux(const AdjLine& A, double v, int64_t e) {
+  // f'(v) at interface e (local index): Burgers u, linear g(x_e)
+  if (A.fn == HRW_FN_BURGERS) return v;
+  return fma(A.b, fma(A.rx, (double)e, A.xmin), A.a);
+}
+
+enum AdjMode : int { ADJ_A3 = 0, ADJ_A2 = 1, ADJ_A1 = 2 };
+
+// --------------------------------------------------------------------------------------------
+// VJP + stage-adjoint combine.  Block: NT cells [s, s+NT); contributors s-(K-1) .. s+NT+K-2.
+//   state: v (the stage input of the forward stage), mu: adjoint of that stage's L output
+//   (scaled as described in the mode), acc: the accumulated adjoint of u.
+// --------------------------------------------------------------------------------------------
+template <int K, int MODE, int NT>
+__global__ void __launch_bounds__(NT) adj_vjp_kernel(AdjLine A, const double* __restrict__ v,
+                                                     const double* __restrict__ mu,
+                                                     double* __restrict__ acc,
+                                                     double* __restrict__ out, double dt) {
+  constexpr int NS = 2 * K - 1;             // stencil width
+  constexpr int NCTR = NT + 2 * (K - 1);    // contributors
+  __shared__ double sc[NCTR * NS];
+  const int64_t s = (int64_t)blockIdx.x * NT;
+  const double idx = A.rdx;
+  for (int t = threadIdx.x; t < NCTR; t += NT) {
+    const int64_t i = s - (K - 1) + t;
+    double o[NS];
+#pragma unroll
+    for (int q = 0; q < NS; ++q) o[q] = 0.0;
+    if (i >= 0 && i < A.n) {
+      const int64_t s0 = i / A.seg * A.seg, s1 = s0 + A.seg - 1, li = i - s0;
+      double p[NS];
+#pragma unroll
+      for (int q = 0; q < NS; ++q) {
+        int64_t g = i - (K - 1) + q;
+        g = g < s0 ? s0 : (g > s1 ? s1 : g);
+        p[q] = v[g];
+      }
+      double vl, vr;
+      weno_vjp_states<K>(&p[K - 1], A.eps, vl, vr);
+      const double mi = mu[i];
+      // flux adjoints of the cell's right and left interfaces
+      double ar = 0.0, al = 0.0;
+      if (li < A.seg - 1) {
+        const double mp = mu[i + 1];
+        const double phi = ((uses_fl(A.bc, li + 1, A.seg) ? mp : 0.0) -
+                            (uses_fr(A.bc, li, A.seg) ? mi : 0.0)) * idx;
+        ar = phi * 0.5 * (dflux(A, vr, li + 1) + A.alpha);
+      } else if (A.bc == HRW_BC_ZERO_INFLOW) {  // F_{nc+1/2} = f(vr(nc))
+        ar = -mi * idx * dflux(A, vr, li + 1);
+      }
+      if (li > 0) {
+        const double mm = mu[i - 1];
+        const double phi = ((uses_fl(A.bc, li, A.seg) ? mi : 0.0) -
+                            (uses_fr(A.bc, li - 1, A.seg) ? mm : 0.0)) * idx;
+        al = phi * 0.5 * (dflux(A, vl, li) - A.alpha);
+      }
+      weno_vjp<K>(&p[K - 1], A.eps, ar, al, o);
+    }
+#pragma unroll
+    for (int q = 0; q < NS; ++q) sc[t * NS + q] = o[q];
+  }
+  __syncthreads();
+  const int64_t m = s + threadIdx.x;
+  if (m >= A.n) return;
+  const int64_t s0 = m / A.seg * A.seg, s1 = s0 + A.seg - 1, lm = m - s0;
+  double w = 0.0;
+#pragma unroll
+  for (int o = -(K - 1); o <= K - 1; ++o) {  // contributor i = m - o sees m at offset o
+    const int64_t i = m - o;
+    if (i >= s0 && i <= s1) w += sc[(i - (s - (K - 1))) * NS + (o + K - 1)];
+  }
+  // ghost positions (outside the segment) clamp onto its end cells
+  if (lm == 0) {
+#pragma unroll
+    for (int ii = 0; ii < K - 1; ++ii) {
+      const int64_t i = s0 + ii;
+#pragma unroll
+      for (int q = 0; q < NS; ++q)
+        if (i <= s1 && i - (K - 1) + q < s0) w += sc[(i - (s - (K - 1))) * NS + q];
+    }
+  }
+  if (lm == A.seg - 1) {
+#pragma unroll
+    for (int ii = 0; ii < K - 1; ++ii) {
+      const int64_t i = s1 - ii;
+#pragma unroll
+      for (int q = 0; q < NS; ++q)
+        if (i >= s0 && i - (K - 1) + q > s1) w += sc[(i - (s - (K - 1))) * NS + q];
+    }
+  }
+  const double mum = mu[m];
+  if constexpr (MODE == ADJ_A3) {
+    out[m] = (2.0 / 3.0) * fma(dt, w, mum);
+    acc[m] = (1.0 / 3.0) * mum;
+  } else if constexpr (MODE == ADJ_A2) {
+    out[m] = 0.25 * fma(dt, w, mum);
+    acc[m] = fma(0.75, mum, acc[m]);
+  } else {
+    out[m] = acc[m] + fma(dt, w, mum);
+  }
+}
+
+// J per segment and lambda_T = u - target
+__global__ void adj_misfit_kernel(AdjLine A, const double* __restrict__ u,
+                                  const double* __restrict__ tgt, double* __restrict__ lam,
+                                  double* __restrict__ J) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < A.n; i += stride) {
+    const double r = u[i] - tgt[i];
+    lam[i] = r;
+    atomicAdd(&J[i / A.seg], 0.5 * r * r);
+  }
+}
+
+template <int K>
+cudaError_t fwd_stage_k(const AdjLine& A, const StageArgs& a, int st, cudaStream_t s) {
+  constexpr int C = 8;
+  const int64_t warps = (A.n + 32 * C - 1) / (32 * C);
+  const int blocks = (int)((warps + 7) / 8 < 152 * 32 ? (warps + 7) / 8 : 152 * 32);
+  if (st == ST_EULER) adj_fwd_kernel<K, ST_EULER, C><<<blocks, 256, 0, s>>>(A, a);
+  else if (st == ST_RK3B) adj_fwd_kernel<K, ST_RK3B, C><<<blocks, 256, 0, s>>>(A, a);
+  else adj_fwd_kernel<K, ST_RK3C, C><<<blocks, 256, 0, s>>>(A, a);
+  return cudaGetLastError();
+}
+
+template <int K>
+cudaError_t vjp_k(const AdjLine& A, int mode, const double* v, const double* mu, double* acc,
+                  double* out, double dt, cudaStream_t s) {
+  constexpr int NT = 256;
+  const unsigned blocks = (unsigned)((A.n + NT - 1) / NT);
+  if (mode == ADJ_A3) adj_vjp_kernel<K, ADJ_A3, NT><<<blocks, NT, 0, s>>>(A, v, mu, acc, out, dt);
+  else if (mode == ADJ_A2) adj_vjp_kernel<K, ADJ_A2, NT><<<blocks, NT, 0, s>>>(A, v, mu, acc, out, dt);
+  else adj_vjp_kernel<K, ADJ_A1, NT><<<blocks, NT, 0, s>>>(A, v, mu, acc, out, dt);
+  return cudaGetLastError();
+}
+
+cudaError_t fwd_stage(const AdjLine& A, const StageArgs& a, int st, cudaStream_t s) {
+  if (A.k == 1) return fwd_stage_k<1>(A, a, st, s);
+  if (A.k == 2) return fwd_stage_k<2>(A, a, st, s);
+  return fwd_stage_k<3>(A, a, st, s);
+}
+
+cudaError_t vjp(const AdjLine& A, int mode, const double* v, const double* mu, double* acc,
+                double* out, double dt, cudaStream_t s) {
+  if (A.k == 1) return vjp_k<1>(A, mode, v, mu, acc, out, dt, s);
+  if (A.k == 2) return vjp_k<2>(A, mode, v, mu, acc, out, dt, s);
+  return vjp_k<3>(A, mode, v, mu, acc, out, dt, s);
+}
+
+}  // namespace
+}  // namespace hrw
+
+using namespace hrw;
+
+struct hrw_adjoint {
+  AdjLine line{};
+  int64_t nseg = 1;
+  int every = 45;
+  cudaStream_t own = nullptr, stream = nullptr;
+  double *u = nullptr, *w1 = nullptr, *w2 = nullptr, *tgt = nullptr;
+  double *lam = nullptr, *la = nullptr, *lb = nullptr, *acc = nullptr, *J = nullptr;
+  std::vector<double*> ckpt;  // checkpoints
+  double* tape = nullptr;     // (every + 1) states + every u1 + every u2
+  int64_t fwd_steps = 0;      // forward steps taken by the last gradient call (incl. recompute)
+};
+
+namespace {
+
+int adj_fail(int code, const std::string& m) { return set_error(code, m.c_str()); }
+
+#define HRW_ACUDA(call)                                                                 \
+  do {                                                                                  \
+    cudaError_t e_ = (call);                                                            \
+    if (e_ != cudaSuccess)                                                              \
+      return adj_fail(e_ == cudaErrorMemoryAllocation ? HRW_ENOMEM : HRW_ECUDA,         \
+                      std::string(#call ": ") + cudaGetErrorString(e_));                \
+  } while (0)
+
+StageArgs base_args(const hrw_adjoint* h, double dt) {
+  StageArgs a{};
+  a.eps = h->line.eps;
+  a.dt = dt;
+  return a;
+}
+
+// one forward RK3 step from `u` to `un` with stage arrays s1, s2 (un may equal u)
+cudaError_t step(hrw_adjoint* h, const double* u, double* s1, double* s2, double* un, double dt) {
+  StageArgs a = base_args(h, dt);
+  a.v = u, a.u = u, a.out = s1;
+  cudaError_t e = fwd_stage(h->line, a, ST_EULER, h->stream);
+  if (e != cudaSuccess) return e;
+  a.v = s1, a.u = u, a.out = s2;
+  if ((e = fwd_stage(h->line, a, ST_RK3B, h->stream)) != cudaSuccess) return e;
+  a.v = s2, a.u = u, a.out = un;
+  return fwd_stage(h->line, a, ST_RK3C, h->stream);
+}
+
+}  // namespace
+
+extern "C" {
+
+int hrw_adjoint_create(const hrw_problem* p, int nseg, int checkpoint_every, hrw_adjoint** out) {
+  if (!out) return adj_fail(HRW_EINVAL, "Invalid input 'out': null pointer.");
+  *out = nullptr;
+  if (!p) return adj_fail(HRW_EINVAL, "Invalid input 'problem': null pointer.");
+  if (p->kind != HRW_PROBLEM_FV1D) return adj_fail(HRW_EINVAL, "hrw_adjoint: FV1D problems only.");
+  if (p->flux != HRW_FLUX_LAX_FRIEDRICHS)
+    return adj_fail(HRW_EINVAL, "hrw_adjoint: the global Lax-Friedrichs flux with fixed alpha only.");
+  if (p->width[0]) return adj_fail(HRW_EINVAL, "hrw_adjoint: uniform grids only.");
+  if (p->ncells[0] <= 0) return adj_fail(HRW_EINVAL, "Invalid input 'ncells'. Valid range: ncells > 0.");
+  if (p->k < 1 || p->k > 3) return adj_fail(HRW_EINVAL, "Invalid input 'k'. Valid range: 1 <= k <= 3.");
+  if (!(p->eps > 2.220446049250313e-16))
+    return adj_fail(HRW_EINVAL, "Invalid input 'eps'. Valid range: eps > epsilon.");
+  if (p->fn[0] != HRW_FN_BURGERS && p->fn[0] != HRW_FN_LINEAR) return adj_fail(HRW_EINVAL, "Invalid input 'fn'.");
+  if (p->bc[0] < HRW_BC_COPY || p->bc[0] > HRW_BC_ZERO_INFLOW) return adj_fail(HRW_EINVAL, "Invalid input 'bc'.");
+  if (nseg < 1) return adj_fail(HRW_EINVAL, "Invalid input 'nseg': must be >= 1.");
+  if (nseg > 1 && p->ncells[0] % 8 != 0)
+    return adj_fail(HRW_EINVAL, "hrw_adjoint: with nseg > 1, ncells must be a multiple of 8.");
+  if (checkpoint_every < 1) return adj_fail(HRW_EINVAL, "Invalid input 'checkpoint_every': must be >= 1.");
+  hrw_adjoint* h = new hrw_adjoint;
+  AdjLine& L = h->line;
+  L.seg = p->ncells[0];
+  L.n = L.seg * nseg;
+  L.k = p->k;
+  L.fn = p->fn[0];
+  L.bc = p->bc[0];
+  L.a = p->coef_a[0];
+  L.b = p->coef_b[0];
+  L.alpha = p->alpha[0];
+  L.xmin = p->xmin[0];
+  L.rx = (p->xmax[0] - p->xmin[0]) / L.seg;
+  L.rdx = 1.0 / L.rx;
+  L.eps = p->eps;
+  L.rws0 = fast_flux_scale(HRW_FLUX_LAX_FRIEDRICHS, L.fn) / L.rx;
+  h->nseg = nseg;
+  h->every = checkpoint_every;
+  const size_t bytes = sizeof(double) * (size_t)L.n;
+  cudaError_t e = cudaStreamCreateWithFlags(&h->own, cudaStreamDefault);
+  h->stream = h->own;
+  double** bufs[] = {&h->u, &h->w1, &h->w2, &h->tgt, &h->lam, &h->la, &h->lb, &h->acc};
+  for (double** b : bufs)
+    if (e == cudaSuccess) e = cudaMalloc(b, bytes);
+  if (e == cudaSuccess) e = cudaMalloc(&h->J, sizeof(double) * nseg);
+  if (e == cudaSuccess) e = cudaMalloc(&h->tape, bytes * (size_t)(3 * checkpoint_every + 1));
+  if (e != cudaSuccess) {
+    hrw_adjoint_destroy(h);
+    return adj_fail(e == cudaErrorMemoryAllocation ? HRW_ENOMEM : HRW_ECUDA,
+                    std::string("hrw_adjoint_create: ") + cudaGetErrorString(e));
+  }
+  *out = h;
+  return HRW_OK;
+}
+
+int hrw_adjoint_gradient(hrw_adjoint* h, int mem, const double* u0, const double* target, double dt,
+                         int64_t nsteps, double* J, double* grad) {
+  if (!h) return adj_fail(HRW_EINVAL, "Invalid input 'adjoint': null handle.");
+  if (!u0 || !target || !grad) return adj_fail(HRW_EINVAL, "Invalid input: null pointer.");
+  if (nsteps < 1) return adj_fail(HRW_EINVAL, "Invalid input 'nsteps': must be >= 1.");
+  if (!(dt != 0.0) || !std::isfinite(dt)) return adj_fail(HRW_EINVAL, "Invalid input 'dt'.");
+  const AdjLine& L = h->line;
+  const size_t bytes = sizeof(double) * (size_t)L.n;
+  const cudaMemcpyKind in = mem == HRW_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
+  const int64_t E = h->every;
+  const int64_t nck = (nsteps + E - 1) / E;  // segments of the time line
+  while ((int64_t)h->ckpt.size() < nck) {
+    double* c = nullptr;
+    HRW_ACUDA(cudaMalloc(&c, bytes));
+    h->ckpt.push_back(c);
+  }
+  double* U = h->tape;  // U[n] = tape + n, U1[n] = tape + E+1+n, U2[n] = tape + 2E+1+n
+  auto Un = [&](int64_t n) { return U + (size_t)n * L.n; };
+  auto U1 = [&](int64_t n) { return U + (size_t)(E + 1 + n) * L.n; };
+  auto U2 = [&](int64_t n) { return U + (size_t)(2 * E + 1 + n) * L.n; };
+  // ---- forward: checkpoints, the last segment recorded on the tape ------------------------
+  HRW_ACUDA(cudaMemcpyAsync(h->u, u0, bytes, in, h->stream));
+  HRW_ACUDA(cudaMemcpyAsync(h->tgt, target, bytes, in, h->stream));
+  int64_t fwd = 0;
+  for (int64_t c = 0; c < nck; ++c) {
+    const int64_t len = std::min(E, nsteps - c * E);
+    HRW_ACUDA(cudaMemcpyAsync(h->ckpt[c], h->u, bytes, cudaMemcpyDeviceToDevice, h->stream));
+    if (c < nck - 1) {
+      for (int64_t n = 0; n < len; ++n) HRW_ACUDA(step(h, h->u, h->w1, h->w2, h->u, dt));
+    } else {
+      HRW_ACUDA(cudaMemcpyAsync(Un(0), h->u, bytes, cudaMemcpyDeviceToDevice, h->stream));
+      for (int64_t n = 0; n < len; ++n) HRW_ACUDA(step(h, Un(n), U1(n), U2(n), Un(n + 1), dt));
+    }
+    fwd += len;
+  }
+  // ---- misfit and lambda(T) -----------------------------------------------------------------
+  const int64_t last_len = nsteps - (nck - 1) * E;
+  HRW_ACUDA(cudaMemsetAsync(h->J, 0, sizeof(double) * h->nseg, h->stream));
+  adj_misfit_kernel<<<152 * 8, 256, 0, h->stream>>>(L, Un(last_len), h->tgt, h->lam, h->J);
+  HRW_ACUDA(cudaGetLastError());
+  // ---- reverse sweep ---------------------------------------------------------------------------
+  for (int64_t c = nck - 1; c >= 0; --c) {
+    const int64_t len = std::min(E, nsteps - c * E);
+    if (c < nck - 1) {  // recompute the segment from its checkpoint, recording every stage
+      HRW_ACUDA(cudaMemcpyAsync(Un(0), h->ckpt[c], bytes, cudaMemcpyDeviceToDevice, h->stream));
+      for (int64_t n = 0; n < len; ++n) HRW_ACUDA(step(h, Un(n), U1(n), U2(n), Un(n + 1), dt));
+      fwd += len;
+    }
+    for (int64_t n = len - 1; n >= 0; --n) {
+      HRW_ACUDA(vjp(L, ADJ_A3, U2(n), h->lam, h->acc, h->la, dt, h->stream));
+      HRW_ACUDA(vjp(L, ADJ_A2, U1(n), h->la, h->acc, h->lb, dt, h->stream));
+      HRW_ACUDA(vjp(L, ADJ_A1, Un(n), h->lb, h->acc, h->lam, dt, h->stream));
+    }
+  }
+  h->fwd_steps = fwd;
+  const cudaMemcpyKind outk = mem == HRW_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+  HRW_ACUDA(cudaMemcpyAsync(grad, h->lam, bytes, outk, h->stream));
+  if (J) HRW_ACUDA(cudaMemcpyAsync(J, h->J, sizeof(double) * h->nseg, cudaMemcpyDeviceToHost, h->stream));
+  HRW_ACUDA(cudaStreamSynchronize(h->stream));
+  return HRW_OK;
+}
+
+// Forward only: u(T) after nsteps steps and J (per segment); the reference point of the
+// adjoint's cost and of finite-difference checks.
+int hrw_adjoint_forward(hrw_adjoint* h, int mem, const double* u0, const double* target, double dt,
+                        int64_t nsteps, double* J, double* uT) {
+  if (!h) return adj_fail(HRW_EINVAL, "Invalid input 'adjoint': null handle.");
+  if (!u0 || !target) return adj_fail(HRW_EINVAL, "Invalid input: null pointer.");
+  const AdjLine& L = h->line;
+  const size_t bytes = sizeof(double) * (size_t)L.n;
+  const cudaMemcpyKind in = mem == HRW_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
+  HRW_ACUDA(cudaMemcpyAsync(h->u, u0, bytes, in, h->stream));
+  HRW_ACUDA(cudaMemcpyAsync(h->tgt, target, bytes, in, h->stream));
+  for (int64_t n = 0; n < nsteps; ++n) HRW_ACUDA(step(h, h->u, h->w1, h->w2, h->u, dt));
+  HRW_ACUDA(cudaMemsetAsync(h->J, 0, sizeof(double) * h->nseg, h->stream));
+  adj_misfit_kernel<<<152 * 8, 256, 0, h->stream>>>(L, h->u, h->tgt, h->lam, h->J);
+  HRW_ACUDA(cudaGetLastError());
+  if (uT)
+    HRW_ACUDA(cudaMemcpyAsync(uT, h->u, bytes, mem == HRW_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice,
+                              h->stream));
+  if (J) HRW_ACUDA(cudaMemcpyAsync(J, h->J, sizeof(double) * h->nseg, cudaMemcpyDeviceToHost, h->stream));
+  HRW_ACUDA(cudaStreamSynchronize(h->stream));
+  return HRW_OK;
+}
+
+int hrw_adjoint_set_stream(hrw_adjoint* h, void* stream) {
+  if (!h) return adj_fail(HRW_EINVAL, "Invalid input 'adjoint': null handle.");
+  h->stream = stream ? (cudaStream_t)stream : h->own;
+  return HRW_OK;
+}
+
+int hrw_adjoint_info(const hrw_adjoint* h, int64_t* forward_steps) {
+  if (!h) return adj_fail(HRW_EINVAL, "Invalid input 'adjoint': null handle.");
+  if (forward_steps) *forward_steps = h->fwd_steps;
+  return HRW_OK;
+}
+
+int hrw_adjoint_destroy(hrw_adjoint* h) {
+  if (!h) return HRW_OK;
+  double* bufs[] = {h->u, h->w1, h->w2, h->tgt, h->lam, h->la, h->lb, h->acc, h->J, h->tape};
+  for (double* b : bufs)
+    if (b) cudaFree(b);
+  for (double* c : h->ckpt) cudaFree(c);
+  if (h->own) cudaStreamDestroy(h->own);
+  delete h;
+  return HRW_OK;
+}
+
+}  // extern "C"

@@ -9,6 +9,7 @@ mirrors the Fortran modules hrweno_weno (weno, %reconstruct) and hrweno_tvdode (
 from ._abi import (HRW_BC_COPY, HRW_BC_ZERO, HRW_BC_ZERO_INFLOW, HRW_F32, HRW_F32C, HRW_F64,  # noqa: F401
                    HRW_FLUX_GODUNOV, HRW_FLUX_LAX_FRIEDRICHS, HRW_FN_BURGERS, HRW_FN_LINEAR,
                    HRW_NUMERICS_FAST, HRW_NUMERICS_STRICT, HrwError, lib)
+from .adjoint import adjoint  # noqa: F401
 from .batch import batch  # noqa: F401
 from .problems import Problem, burgers_1d, linear_ode, pbe_2d  # noqa: F401
 from .tvdode import mstvd, rktvd  # noqa: F401

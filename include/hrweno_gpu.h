@@ -169,6 +169,27 @@ int hrw_batch_info(const hrw_batch* b, int* shapes, int64_t* steps_done);
 int hrw_batch_set_stream(hrw_batch* b, void* stream);
 int hrw_batch_destroy(hrw_batch* b);
 
+/* ---- discrete adjoint --------------------------------------------------------------- */
+/* No counterpart in the reference.  Gradient of J = 0.5 ||u(T) - target||^2 with respect to
+ * the initial state u0, where u(T) is nsteps rktvd(order 3) steps of dt of an FV1D problem
+ * with the global Lax-Friedrichs flux at fixed alpha (eps > 0 keeps the WENO weights smooth).
+ * The state holds nseg independent problems of p->ncells[0] cells each (packed; with
+ * nseg > 1, ncells must be a multiple of 8); J has one entry per problem.  The reverse sweep
+ * recomputes the forward from checkpoints taken every `checkpoint_every` steps (about
+ * sqrt(nsteps) is the usual choice). */
+typedef struct hrw_adjoint hrw_adjoint;
+int hrw_adjoint_create(const hrw_problem* p, int nseg, int checkpoint_every, hrw_adjoint** out);
+/* grad = dJ/du0 (nseg * ncells doubles), J[nseg]; arrays in memory space `mem` (J on the host) */
+int hrw_adjoint_gradient(hrw_adjoint* a, int mem, const double* u0, const double* target, double dt,
+                         int64_t nsteps, double* J, double* grad);
+/* The forward solve alone: J[nseg] and u(T) (nullable) */
+int hrw_adjoint_forward(hrw_adjoint* a, int mem, const double* u0, const double* target, double dt,
+                        int64_t nsteps, double* J, double* uT);
+/* forward steps (initial pass plus recompute) taken by the last gradient call */
+int hrw_adjoint_info(const hrw_adjoint* a, int64_t* forward_steps);
+int hrw_adjoint_set_stream(hrw_adjoint* a, void* stream);
+int hrw_adjoint_destroy(hrw_adjoint* a);
+
 /* ---- RK3 steps that allocate no device memory -------------------------------------- */
 /* No counterpart in the reference.  For callers that cannot allocate device memory: a
  * framework whose caching allocator already owns the whole device, or a step loop that must

@@ -427,6 +427,30 @@ struct ODE {
   }
 };
 
+// ---------------------------------------------------------------------------------------
+// Tangent-linear model: the same templates instantiated on a forward-mode dual number give the
+// exact directional derivative of the discrete forward map, in the reference's operation
+// order.  Comparisons (Godunov's min/max, vm <= vp) act on the value part.
+// ---------------------------------------------------------------------------------------
+struct Dual {
+  double v = 0.0, d = 0.0;
+  Dual() = default;
+  Dual(double x) : v(x), d(0.0) {}  // NOLINT: implicit, like a real literal
+  Dual(double x, double y) : v(x), d(y) {}
+  explicit operator double() const { return v; }
+};
+inline Dual operator+(Dual a, Dual b) { return {a.v + b.v, a.d + b.d}; }
+inline Dual operator-(Dual a, Dual b) { return {a.v - b.v, a.d - b.d}; }
+inline Dual operator-(Dual a) { return {-a.v, -a.d}; }
+inline Dual operator*(Dual a, Dual b) { return {a.v * b.v, a.d * b.v + a.v * b.d}; }
+inline Dual operator/(Dual a, Dual b) { return {a.v / b.v, (a.d * b.v - a.v * b.d) / (b.v * b.v)}; }
+inline Dual operator+(Dual a, int b) { return a + Dual(b); }
+inline Dual operator*(int a, Dual b) { return Dual(a) * b; }
+inline Dual operator/(Dual a, int b) { return a / Dual(b); }
+inline bool operator<(Dual a, Dual b) { return a.v < b.v; }
+inline bool operator>(Dual a, Dual b) { return a.v > b.v; }
+inline bool operator<=(Dual a, Dual b) { return a.v <= b.v; }
+
 struct Handle {
   int prec;
   void* ode;
@@ -564,6 +588,26 @@ int orc_ode_info(void* hh, int* fevals, int* istate, long long* nsteps) {
   if (h->prec == 32) { auto o = (ODE<float>*)h->ode; *fevals = o->fevals; *istate = o->istate; *nsteps = o->nsteps; }
   else if (h->prec == 128) { auto o = (ODE<qreal>*)h->ode; *fevals = o->fevals; *istate = o->istate; *nsteps = o->nsteps; }
   else { auto o = (ODE<double>*)h->ode; *fevals = o->fevals; *istate = o->istate; *nsteps = o->nsteps; }
+  return 0;
+}
+
+// J = 0.5 ||u(T) - target||^2 after nsteps rktvd(order) steps of dt from u0, and its
+// directional derivative dJ = dJ/du0 . du0 by the tangent-linear (dual number) model.
+int orc_tl_misfit(const hrw_problem* p, int neq, int order, const double* u0, const double* du0,
+                  const double* target, double dt, long long nsteps, double* J, double* dJ) {
+  ODE<Dual> ode(*p, neq, order, 0);
+  std::vector<Dual> u(neq);
+  for (int i = 0; i < neq; ++i) u[i] = Dual(u0[i], du0[i]);
+  double t = 0.0;
+  for (long long n = 0; n < nsteps; ++n) ode.rk_step(u.data(), t, dt, ode.fevals);
+  double j = 0.0, dj = 0.0;
+  for (int i = 0; i < neq; ++i) {
+    const double r = u[i].v - target[i];
+    j += 0.5 * r * r;
+    dj += r * u[i].d;
+  }
+  *J = j;
+  *dJ = dj;
   return 0;
 }
 

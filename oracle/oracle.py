@@ -49,6 +49,8 @@ def lib() -> C.CDLL:
         L.orc_ode_info.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int),
                                    C.POINTER(C.c_longlong)]
         L.orc_ode_destroy.argtypes = [C.c_void_p]
+        L.orc_tl_misfit.argtypes = [C.c_void_p, C.c_int, C.c_int, dp, dp, dp, C.c_double,
+                                    C.c_longlong, dp, dp]
         L.orc_set_threads.argtypes = [C.c_int]
         L.orc_set_threads.restype = C.c_int
         _lib = L
@@ -104,6 +106,19 @@ def rhs(problem, v, t: float = 0.0, prec: int = 64) -> np.ndarray:
     out = np.empty_like(v)
     lib().orc_rhs(prec, C.addressof(cp), v.size, t, _p(v), _p(out))
     return out
+
+
+def tl_misfit(problem, u0, du0, target, dt: float, nsteps: int, order: int = 3):
+    """(J, dJ): J = 0.5 ||u(T) - target||^2 after nsteps steps from u0 and its derivative in
+    the direction du0, by the tangent-linear (dual number) model of the oracle."""
+    cp = problem.to_c()
+    u0 = np.ascontiguousarray(u0, dtype=np.float64)
+    du0 = np.ascontiguousarray(du0, dtype=np.float64)
+    target = np.ascontiguousarray(target, dtype=np.float64)
+    J, dJ = C.c_double(), C.c_double()
+    lib().orc_tl_misfit(C.addressof(cp), u0.size, order, _p(u0), _p(du0), _p(target), dt,
+                        nsteps, C.byref(J), C.byref(dJ))
+    return J.value, dJ.value
 
 
 class ODE:

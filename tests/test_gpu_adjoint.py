@@ -1,0 +1,107 @@
+"""The discrete adjoint (hrw_adjoint_*) against the tangent-linear oracle and finite differences.
+
+  grad . d  vs  the oracle's tangent-linear dJ(d) (dual numbers through the reference-order
+            forward map): relative difference <= 1e-10
+  J         vs  the oracle's forward solve: relative difference <= 1e-12
+  central finite differences on the GPU forward map: relative difference <= 1e-6
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def line(n, seed):
+    rng = np.random.default_rng(seed)
+    x = np.linspace(-5, 5, n)
+    u = np.zeros(n)
+    for _ in range(4):
+        u += rng.uniform(0.2, 1.0) * np.exp(-((x - rng.uniform(-4, 4)) / rng.uniform(0.3, 1.0)) ** 2)
+    return u
+
+
+def smooth_direction(n, seed):
+    rng = np.random.default_rng(seed)
+    x = np.linspace(0, 1, n)
+    d = np.zeros(n)
+    for m in range(1, 9):
+        d += rng.standard_normal() * np.sin(np.pi * m * x + rng.uniform(0, 6.28)) / m
+    return d
+
+
+CASES = [
+    dict(k=3, fn="burgers", bc="copy"), dict(k=2, fn="burgers", bc="zero"),
+    dict(k=1, fn="burgers", bc="zero_inflow"), dict(k=3, fn="linear", bc="zero_inflow"),
+    dict(k=3, fn="burgers", bc="zero_inflow"), dict(k=2, fn="linear", bc="copy"),
+]
+
+
+def problem(hw, n, k, fn, bc):
+    a, b = (0.7, 0.1) if fn == "linear" else (1.0, 0.0)
+    return hw.Problem(kind="fv1d", ncells=(n, 1), k=k, eps=1e-6, flux="lax_friedrichs",
+                      fn=(fn, fn), coef_a=(a, 0), coef_b=(b, 0), alpha=(1.5, 1.5), bc=(bc, bc),
+                      xmin=(-5.0, 0.0), xmax=(5.0, 1.0))
+
+
+@pytest.mark.parametrize("case", range(len(CASES)))
+def test_adjoint_vs_tangent_linear(hw, orc, case):
+    n, steps = 400, 60
+    prob = problem(hw, n, **CASES[case])
+    u0 = line(n, case)
+    target = line(n, case + 100) * 0.8
+    dt = 0.4 * (10.0 / n) / 1.5
+    adj = hw.adjoint(prob, checkpoint_every=7)
+    J, g = adj.gradient(u0, target, dt, steps)
+    for s in range(3):
+        d = np.random.default_rng(s).standard_normal(n) if s else smooth_direction(n, s)
+        Jo, dJ = orc.tl_misfit(prob, u0, d, target, dt, steps)
+        assert abs(J[0] - Jo) <= 1e-12 * abs(Jo)
+        assert abs(g @ d - dJ) <= 1e-10 * max(abs(dJ), 1e-30), (case, s, g @ d, dJ)
+    assert adj.forward_steps == steps + (steps - steps % 7 if steps % 7 else steps - 7)
+
+
+def test_adjoint_checkpoint_interval_invariant(hw):
+    n, steps = 300, 50
+    prob = problem(hw, n, 3, "burgers", "copy")
+    u0, target = line(n, 1), line(n, 2) * 0.9
+    dt = 0.4 * (10.0 / n) / 1.5
+    ref = None
+    for every in (1, 6, 50, 1000):
+        J, g = hw.adjoint(prob, checkpoint_every=every).gradient(u0, target, dt, steps)
+        if ref is None:
+            ref = (J, g)
+        assert np.array_equal(g, ref[1]) and abs(J[0] - ref[0][0]) <= 1e-14 * ref[0][0]
+
+
+def test_adjoint_batch_matches_single(hw):
+    n, nseg, steps = 256, 5, 40
+    prob = problem(hw, n, 3, "burgers", "zero_inflow")
+    dt = 0.4 * (10.0 / n) / 1.5
+    u0 = np.concatenate([line(n, s) for s in range(nseg)])
+    tg = np.concatenate([line(n, 50 + s) * 0.9 for s in range(nseg)])
+    Jb, gb = hw.adjoint(prob, nseg=nseg, checkpoint_every=9).gradient(u0, tg, dt, steps)
+    for s in range(nseg):
+        sl = slice(s * n, (s + 1) * n)
+        J1, g1 = hw.adjoint(prob, checkpoint_every=9).gradient(u0[sl], tg[sl], dt, steps)
+        assert np.array_equal(gb[sl], g1)
+        assert abs(Jb[s] - J1[0]) <= 1e-13 * J1[0]
+
+
+def test_adjoint_central_differences(hw):
+    """Central finite differences of the GPU forward map in 6 directions."""
+    import torch
+    n, steps = 1 << 14, 200
+    prob = problem(hw, n, 3, "burgers", "copy")
+    u0 = torch.from_numpy(line(n, 3)).cuda()
+    tg = torch.from_numpy(line(n, 4) * 0.9).cuda()
+    dt = 0.4 * (10.0 / n) / 1.5
+    adj = hw.adjoint(prob, checkpoint_every=15)
+    J, g = adj.gradient(u0, tg, dt, steps)
+    for s in range(6):
+        d = torch.from_numpy(smooth_direction(n, 10 + s)).cuda()
+        h = 1e-5 * float(u0.abs().max()) / float(d.abs().max())
+        Jp, _ = adj.forward(u0 + h * d, tg, dt, steps)
+        Jm, _ = adj.forward(u0 - h * d, tg, dt, steps)
+        fd = (Jp[0] - Jm[0]) / (2 * h)
+        gd = float((g * d).sum())
+        assert abs(fd - gd) <= 1e-6 * abs(gd), (s, fd, gd)
