@@ -535,6 +535,123 @@ def run_batched(args, dist: Dist) -> None:
     print(json.dumps(line), flush=True)
 
 
+# ------------------------------------------------------------------------------------------
+# adjoint: gradient of J = 0.5 ||u(T) - u_target||^2 w.r.t. u0 on the 2^20-cell Burgers line,
+# WENO5, fixed-alpha LF, RK3, 2000 steps, checkpoints every 45 steps; u_target from a forward
+# run of a seeded perturbation of u0; one step here is one gradient evaluation
+# ------------------------------------------------------------------------------------------
+ADJ_N, ADJ_STEPS, ADJ_EVERY = 1 << 20, 2000, 45
+
+
+def run_adjoint(args, dist: Dist) -> None:
+    import torch
+
+    import hrweno
+    from hrweno import workloads
+
+    dev = dist.local if dist.world > 1 else 0
+    torch.cuda.set_device(dev)
+    n, nsteps = ADJ_N, args.adj_steps
+    prob, u0h, dt = workloads.large_burgers(n, k=3)
+    rng = np.random.default_rng(5)
+    pert = 0.05 * workloads.multi_gaussian_1d(n, seed=9)
+    stream = torch.cuda.Stream()
+    adj = hrweno.adjoint(prob, checkpoint_every=ADJ_EVERY)
+    adj.set_stream(stream.cuda_stream)
+    u0 = torch.from_numpy(u0h).cuda()
+    tgt = torch.empty_like(u0)
+    adj.forward(u0 + torch.from_numpy(pert).cuda(), u0, dt, nsteps, uT=tgt)  # u_target
+    J, g = adj.gradient(u0, tgt, dt, nsteps)  # warm-up
+    torch.cuda.synchronize()
+    e = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    with ClockSampler(dev) as clk:
+        e[0].record(stream)
+        for _ in range(args.steps):
+            J, g = adj.gradient(u0, tgt, dt, nsteps, grad=g)
+        e[1].record(stream)
+        e[2].record(stream)
+        for _ in range(args.steps):
+            adj.forward(u0, tgt, dt, nsteps)
+        e[3].record(stream)
+        torch.cuda.synchronize()
+    t_grad = dist.max(e[0].elapsed_time(e[1]) * 1e-3 / args.steps)
+    t_fwd = dist.max(e[2].elapsed_time(e[3]) * 1e-3 / args.steps)
+    # central differences of the forward map in random directions
+    fd = []
+    fd_rough = []
+    xs = np.linspace(0.0, 1.0, n)
+    for s in range(args.fd_directions):  # fourth-order central differences
+        if s % 2 == 0:  # smooth random direction: 16 sine modes with random amplitudes, phases
+            dh = np.zeros(n)
+            for m in range(1, 17):
+                dh += rng.standard_normal() * np.sin(np.pi * m * xs + rng.uniform(0, 2 * np.pi)) / m
+        else:  # rough random direction: i.i.d. normal per cell
+            dh = rng.standard_normal(n)
+        d = torch.from_numpy(dh).cuda()
+        h = 1e-5 * float(u0.abs().max()) / float(d.abs().max())
+        Jv = [adj.forward(u0 + c * h * d, tgt, dt, nsteps)[0][0] for c in (2, 1, -1, -2)]
+        fdv = (8.0 * (Jv[1] - Jv[2]) - (Jv[0] - Jv[3])) / (12.0 * h)
+        gd = float((g * d).sum())
+        (fd if s % 2 == 0 else fd_rough).append(abs(fdv - gd) / abs(gd))
+    # the whole trajectory on the tape (no recompute) when it fits in device memory
+    adj0 = hrweno.adjoint(prob, checkpoint_every=0)
+    adj0.set_stream(stream.cuda_stream)
+    J0, g0 = adj0.gradient(u0, tgt, dt, nsteps)
+    torch.cuda.synchronize()
+    e[0].record(stream)
+    J0, g0 = adj0.gradient(u0, tgt, dt, nsteps, grad=g0)
+    e[1].record(stream)
+    torch.cuda.synchronize()
+    t_tape = e[0].elapsed_time(e[1]) * 1e-3
+    tape_every = adj0.checkpoint_every
+    same = bool(torch.equal(g0, g))
+    del adj0, g0
+    # a batch of 256 problems of 4096 cells, one gradient each, in one set of launches
+    bn, bseg = 4096, 256
+    bprob, _, bdt = workloads.large_burgers(bn, k=3, u0=np.ones(bn))
+    bprob.alpha = (1.0, 1.0)
+    bu0 = torch.from_numpy(np.concatenate(
+        [workloads.multi_gaussian_1d(bn, seed=100 + s) / 2.0 for s in range(bseg)])).cuda()
+    btg = bu0.flip(0).contiguous()
+    badj = hrweno.adjoint(bprob, nseg=bseg, checkpoint_every=ADJ_EVERY)
+    badj.set_stream(stream.cuda_stream)
+    bJ, bg = badj.gradient(bu0, btg, bdt, nsteps)
+    torch.cuda.synchronize()
+    e[0].record(stream)
+    bJ, bg = badj.gradient(bu0, btg, bdt, nsteps, grad=bg)
+    e[1].record(stream)
+    e[2].record(stream)
+    badj.forward(bu0, btg, bdt, nsteps)
+    e[3].record(stream)
+    torch.cuda.synchronize()
+    bt_grad, bt_fwd = e[0].elapsed_time(e[1]) * 1e-3, e[2].elapsed_time(e[3]) * 1e-3
+    if dist.rank != 0:
+        return
+    value = dist.world * n * nsteps / t_grad
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT + " (gradient)", "n_gpus": dist.world,
+        "steps": args.steps, "warmup": 1, "ms_per_step": 1e3 * t_grad,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic: 8-Gaussian u0, target = forward run of u0 + 0.05 x seeded Gaussians",
+        "config": {"workload": f"adjoint_burgers1d_{n}_weno5_lf_rk3", "cells": n,
+                   "time_steps": nsteps, "checkpoint_every": ADJ_EVERY, "alpha": "fixed max|u0|"},
+        "adjoint": {"J": float(J[0]), "gradient_ms": 1e3 * t_grad, "forward_ms": 1e3 * t_fwd,
+                    "cost_vs_forward": t_grad / t_fwd, "forward_steps_in_gradient": adj.forward_steps,
+                    "full_tape": {"gradient_ms": 1e3 * t_tape, "cost_vs_forward": t_tape / t_fwd,
+                                  "checkpoint_every": tape_every, "same_gradient_bits": same},
+                    "fd_directions": args.fd_directions, "fd_order": 4,
+                    "fd_max_rel_err_smooth": max(fd) if fd else None,
+                    "fd_max_rel_err_rough": max(fd_rough) if fd_rough else None,
+                    "fd_median_rel_err_rough": float(np.median(fd_rough)) if fd_rough else None,
+                    "batch": {"problems": bseg, "cells_each": bn, "gradient_ms": 1e3 * bt_grad,
+                              "forward_ms": 1e3 * bt_fwd, "cost_vs_forward": bt_grad / bt_fwd,
+                              "gradient_cell_updates_per_s": bseg * bn * nsteps / bt_grad}},
+        "gpu_launches": None,
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main() -> None:
     global NC
     ap = argparse.ArgumentParser()
@@ -544,9 +661,12 @@ def main() -> None:
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-forms", action="store_true", help="skip the FP32 form")
-    ap.add_argument("--workload", default="burgers1d", choices=["burgers1d", "pbe2d", "batched"],
+    ap.add_argument("--workload", default="burgers1d", choices=["burgers1d", "pbe2d", "batched", "adjoint"],
                     help="burgers1d (default): the 2^24-cell line; pbe2d: the 2D PBE grid")
     ap.add_argument("--pbe-n", type=int, default=PBE_N, help="pbe2d grid size per dimension")
+    ap.add_argument("--adj-steps", type=int, default=ADJ_STEPS, help="adjoint: time steps")
+    ap.add_argument("--fd-directions", type=int, default=8,
+                    help="adjoint: random directions of the central-difference check")
     ap.add_argument("--cells", type=int, default=NC,
                     help="cells of the line (default 2^24, the benchmark workload; smaller "
                          "lines are for profiler captures)")
@@ -565,6 +685,8 @@ def main() -> None:
             run_pbe2d(args, dist)
         elif args.workload == "batched":
             run_batched(args, dist)
+        elif args.workload == "adjoint":
+            run_adjoint(args, dist)
         else:
             run_ours(args, dist)
     finally:

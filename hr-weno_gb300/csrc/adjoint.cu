@@ -21,6 +21,7 @@
 // Lines are segment-aware: the state holds nseg independent problems of `seg` cells each,
 // every segment with its own boundaries and ghost cells, so one launch serves one long line
 // or a batch of equal-size problems.
+#include <algorithm>
 #include <cmath>
 #include <string>
 #include <vector>
@@ -109,87 +110,89 @@ __global__ void __launch_bounds__(256) adj_fwd_kernel(AdjLine A, StageArgs a) {
 }
 
 // --------------------------------------------------------------------------------------------
-// Reverse WENO of one cell: stencil p[-(K-1) .. K-1], adjoints ar (of vr) and al (of vl);
-// adds d(ar vr + al vl)/dp into out[0 .. 2K-2].  Also returns vr and vl.
+// WENO of one cell in division form with everything the reverse pass needs, then the reverse
+// pass: given ar (adjoint of vr) and al (adjoint of vl), add d(ar vr + al vl)/dp into
+// out[0 .. 2K-2] for the stencil p[-(K-1) .. K-1].
 // --------------------------------------------------------------------------------------------
-template <int K>
-__device__ __forceinline__ void weno_vjp_states(const double* p, double eps, double& vl, double& vr) {
-  double l, r;
-  recon_fast_one<K>(p, eps, l, r);
-  vl = l;
-  vr = r;
-}
-
-template <int K>
-__device__ __forceinline__ void weno_vjp(const double* p, double eps, double ar, double al, double* out) {
-  if constexpr (K == 1) {
-    out[0] += ar + al;
-  } else if constexpr (K == 2) {
-    // stencil v_{-1}, v_0, v_1; q0 = (v0 + v1)/2, q1 = (3 v0 - v_{-1})/2; vl: (3 v0 - v1)/2,
-    // (v_{-1} + v0)/2; beta0 = (v1 - v0)^2, beta1 = (v0 - v_{-1})^2; d = (2, 1)/3
+template <int K> struct WenoTape;
+template <> struct WenoTape<1> {
+  double vr, vl;
+  __device__ void fwd(const double* p, double) { vr = vl = p[0]; }
+  __device__ void rev(double ar, double al, double* out) const { out[0] += ar + al; }
+};
+template <> struct WenoTape<2> {
+  // stencil v_{-1}, v_0, v_1; q0 = (v0 + v1)/2, q1 = (3 v0 - v_{-1})/2; vl: r0 = (3 v0 - v1)/2,
+  // r1 = (v_{-1} + v0)/2; beta0 = (v1 - v0)^2, beta1 = (v0 - v_{-1})^2; d = (2, 1)/3
+  double vr, vl, D0, D1, ie0, ie1, w0, w1, u0, u1, q0, q1, r0, r1;
+  __device__ void fwd(const double* p, double eps) {
     const double vm = p[-1], v0 = p[0], v1 = p[1];
-    const double D0 = v1 - v0, D1 = v0 - vm;
-    const double ie0 = rcp_fast(eps + D0 * D0), ie1 = rcp_fast(eps + D1 * D1);
-    const double a0 = (2.0 / 3.0) * ie0 * ie0, a1 = (1.0 / 3.0) * ie1 * ie1;
-    const double t0 = (1.0 / 3.0) * ie0 * ie0, t1 = (2.0 / 3.0) * ie1 * ie1;
-    const double iS = rcp_fast(a0 + a1), iT = rcp_fast(t0 + t1);
-    const double w0 = a0 * iS, w1 = a1 * iS, u0 = t0 * iT, u1 = t1 * iT;
-    const double q0 = 0.5 * (v0 + v1), q1 = 0.5 * fma(3.0, v0, -vm);
-    const double r0 = 0.5 * fma(3.0, v0, -v1), r1 = 0.5 * (vm + v0);
-    const double vrr = fma(w0, q0, w1 * q1), vll = fma(u0, r0, u1 * r1);
+    D0 = v1 - v0, D1 = v0 - vm;
+    ie0 = rcp_fast(fma(D0, D0, eps)), ie1 = rcp_fast(fma(D1, D1, eps));
+    const double s0 = ie0 * ie0, s1 = ie1 * ie1;
+    const double iS = rcp_fast(fma(2.0, s0, s1)), iT = rcp_fast(fma(2.0, s1, s0));
+    w0 = 2.0 * s0 * iS, w1 = s1 * iS, u0 = s0 * iT, u1 = 2.0 * s1 * iT;
+    q0 = 0.5 * (v0 + v1), q1 = 0.5 * fma(3.0, v0, -vm);
+    r0 = 0.5 * fma(3.0, v0, -v1), r1 = 0.5 * (vm + v0);
+    vr = fma(w0, q0, w1 * q1), vl = fma(u0, r0, u1 * r1);
+  }
+  __device__ void rev(double ar, double al, double* out) const {
     // dbeta_s = -2 [ar w_s (q_s - vr) + al u_s (r_s - vl)] / (eps + beta_s)
-    const double db0 = -2.0 * ie0 * fma(ar * w0, q0 - vrr, al * u0 * (r0 - vll));
-    const double db1 = -2.0 * ie1 * fma(ar * w1, q1 - vrr, al * u1 * (r1 - vll));
+    const double db0 = -2.0 * ie0 * fma(ar * w0, q0 - vr, al * u0 * (r0 - vl));
+    const double db1 = -2.0 * ie1 * fma(ar * w1, q1 - vr, al * u1 * (r1 - vl));
     const double dq0 = ar * w0, dq1 = ar * w1, dr0 = al * u0, dr1 = al * u1;
-    // beta0 = D0^2: d/dv1 = 2 D0, d/dv0 = -2 D0; beta1 = D1^2: d/dv0 = 2 D1, d/dvm = -2 D1
     const double g0 = 2.0 * D0 * db0, g1 = 2.0 * D1 * db1;
-    out[0] += -0.5 * dq1 + 0.5 * dr1 - g1;
-    out[1] += 0.5 * dq0 + 1.5 * dq1 + 1.5 * dr0 + 0.5 * dr1 - g0 + g1;
-    out[2] += 0.5 * dq0 - 0.5 * dr0 + g0;
-  } else {
-    // stencil v_{-2} .. v_2 (index 0..4); candidates x6 (c3 table, src/hrweno_weno.f90:19-21)
+    out[0] += fma(-0.5, dq1, fma(0.5, dr1, -g1));
+    out[1] += fma(0.5, dq0 + dr1, fma(1.5, dq1 + dr0, g1 - g0));
+    out[2] += fma(0.5, dq0 - dr0, g0);
+  }
+};
+template <> struct WenoTape<3> {
+  // stencil v_{-2} .. v_2; candidates x6 (c3 table, src/hrweno_weno.f90:19-21); indicators
+  // 13/12 A_s^2 + 1/4 B_s^2 (:194-202); weights d = (3, 6, 1)/10 and mirrored (:207-210)
+  double vr, vl, A0, B0, A1, B1, A2, B2, ie0, ie1, ie2, w0, w1, w2, u0, u1, u2;
+  double q0, q1, q2, r0, r1, r2;  // x6
+  __device__ void fwd(const double* p, double eps) {
     const double vmm = p[-2], vm = p[-1], v0 = p[0], v1 = p[1], v2 = p[2];
-    const double A0 = v0 - 2.0 * v1 + v2, B0 = 3.0 * v0 - 4.0 * v1 + v2;
-    const double A1 = vm - 2.0 * v0 + v1, B1 = vm - v1;
-    const double A2 = vmm - 2.0 * vm + v0, B2 = vmm - 4.0 * vm + 3.0 * v0;
+    A0 = fma(-2.0, v1, v0 + v2), B0 = fma(3.0, v0, fma(-4.0, v1, v2));
+    A1 = fma(-2.0, v0, vm + v1), B1 = vm - v1;
+    A2 = fma(-2.0, vm, vmm + v0), B2 = fma(3.0, v0, fma(-4.0, vm, vmm));
     const double c13 = 13.0 / 12.0;
-    const double b0 = fma(c13 * A0, A0, 0.25 * B0 * B0);
-    const double b1 = fma(c13 * A1, A1, 0.25 * B1 * B1);
-    const double b2 = fma(c13 * A2, A2, 0.25 * B2 * B2);
-    const double ie0 = rcp_fast(eps + b0), ie1 = rcp_fast(eps + b1), ie2 = rcp_fast(eps + b2);
+    ie0 = rcp_fast(eps + fma(c13 * A0, A0, 0.25 * B0 * B0));
+    ie1 = rcp_fast(eps + fma(c13 * A1, A1, 0.25 * B1 * B1));
+    ie2 = rcp_fast(eps + fma(c13 * A2, A2, 0.25 * B2 * B2));
     const double s0 = ie0 * ie0, s1 = ie1 * ie1, s2 = ie2 * ie2;
-    const double a0 = 0.3 * s0, a1 = 0.6 * s1, a2 = 0.1 * s2;  // d = (3, 6, 1)/10
-    const double t0 = 0.1 * s0, t1 = 0.6 * s1, t2 = 0.3 * s2;  // mirrored
-    const double iS = rcp_fast(a0 + a1 + a2), iT = rcp_fast(t0 + t1 + t2);
-    const double w0 = a0 * iS, w1 = a1 * iS, w2 = a2 * iS;
-    const double u0 = t0 * iT, u1 = t1 * iT, u2 = t2 * iT;
-    const double q0 = (2.0 * v0 + 5.0 * v1 - v2) * (1.0 / 6.0);
-    const double q1 = (-vm + 5.0 * v0 + 2.0 * v1) * (1.0 / 6.0);
-    const double q2 = (2.0 * vmm - 7.0 * vm + 11.0 * v0) * (1.0 / 6.0);
-    const double r0 = (11.0 * v0 - 7.0 * v1 + 2.0 * v2) * (1.0 / 6.0);
-    const double r1 = (2.0 * vm + 5.0 * v0 - v1) * (1.0 / 6.0);
-    const double r2 = (-vmm + 5.0 * vm + 2.0 * v0) * (1.0 / 6.0);
-    const double vrr = w0 * q0 + w1 * q1 + w2 * q2;
-    const double vll = u0 * r0 + u1 * r1 + u2 * r2;
-    const double db0 = -2.0 * ie0 * fma(ar * w0, q0 - vrr, al * u0 * (r0 - vll));
-    const double db1 = -2.0 * ie1 * fma(ar * w1, q1 - vrr, al * u1 * (r1 - vll));
-    const double db2 = -2.0 * ie2 * fma(ar * w2, q2 - vrr, al * u2 * (r2 - vll));
-    const double dq0 = ar * w0 * (1.0 / 6.0), dq1 = ar * w1 * (1.0 / 6.0), dq2 = ar * w2 * (1.0 / 6.0);
-    const double dr0 = al * u0 * (1.0 / 6.0), dr1 = al * u1 * (1.0 / 6.0), dr2 = al * u2 * (1.0 / 6.0);
-    // d beta_s: 13/6 A_s grad(A_s) + 1/2 B_s grad(B_s)
+    const double S1 = 6.0 * s1;
+    const double iS = rcp_fast(fma(3.0, s0, S1 + s2)), iT = rcp_fast(fma(3.0, s2, S1 + s0));
+    w0 = 3.0 * s0 * iS, w1 = S1 * iS, w2 = s2 * iS;
+    u0 = s0 * iT, u1 = S1 * iT, u2 = 3.0 * s2 * iT;
+    q0 = fma(5.0, v1, fma(2.0, v0, -v2)), q1 = fma(5.0, v0, fma(2.0, v1, -vm));
+    q2 = fma(11.0, v0, fma(-7.0, vm, 2.0 * vmm));
+    r0 = fma(11.0, v0, fma(-7.0, v1, 2.0 * v2)), r1 = fma(5.0, v0, fma(2.0, vm, -v1));
+    r2 = fma(5.0, vm, fma(2.0, v0, -vmm));
+    vr = fma(w0, q0, fma(w1, q1, w2 * q2)) * (1.0 / 6.0);
+    vl = fma(u0, r0, fma(u1, r1, u2 * r2)) * (1.0 / 6.0);
+  }
+  __device__ void rev(double ar, double al, double* out) const {
+    const double vr6 = 6.0 * vr, vl6 = 6.0 * vl;
+    const double arw = ar * (1.0 / 6.0), alw = al * (1.0 / 6.0);
+    const double db0 = -2.0 * ie0 * fma(arw * w0, q0 - vr6, alw * u0 * (r0 - vl6));
+    const double db1 = -2.0 * ie1 * fma(arw * w1, q1 - vr6, alw * u1 * (r1 - vl6));
+    const double db2 = -2.0 * ie2 * fma(arw * w2, q2 - vr6, alw * u2 * (r2 - vl6));
+    const double dq0 = arw * w0, dq1 = arw * w1, dq2 = arw * w2;
+    const double dr0 = alw * u0, dr1 = alw * u1, dr2 = alw * u2;
+    // d beta_s = 13/6 A_s grad(A_s) + 1/2 B_s grad(B_s); grad A0 = (0,0,1,-2,1),
+    // B0 = (0,0,3,-4,1); A1 = (0,1,-2,1,0), B1 = (0,1,0,-1,0); A2 = (1,-2,1,0,0), B2 = (1,-4,3,0,0)
     const double gA0 = (13.0 / 6.0) * A0 * db0, gB0 = 0.5 * B0 * db0;
     const double gA1 = (13.0 / 6.0) * A1 * db1, gB1 = 0.5 * B1 * db1;
     const double gA2 = (13.0 / 6.0) * A2 * db2, gB2 = 0.5 * B2 * db2;
-    // grad A0 = (0,0,1,-2,1), B0 = (0,0,3,-4,1); A1 = (0,1,-2,1,0), B1 = (0,1,0,-1,0);
-    // A2 = (1,-2,1,0,0), B2 = (1,-4,3,0,0); q/r coefficient rows x6 as above
-    out[0] += 2.0 * dq2 - dr2 + gA2 + gB2;
-    out[1] += -dq1 - 7.0 * dq2 + 2.0 * dr1 + 5.0 * dr2 + gA1 + gB1 - 2.0 * gA2 - 4.0 * gB2;
-    out[2] += 2.0 * dq0 + 5.0 * dq1 + 11.0 * dq2 + 11.0 * dr0 + 5.0 * dr1 + 2.0 * dr2 + gA0 +
-              3.0 * gB0 - 2.0 * gA1 + gA2 + 3.0 * gB2;
-    out[3] += 5.0 * dq0 + 2.0 * dq1 - 7.0 * dr0 - dr1 - 2.0 * gA0 - 4.0 * gB0 + gA1 - gB1;
-    out[4] += -dq0 + 2.0 * dr0 + gA0 + gB0;
+    out[0] += fma(2.0, dq2, gA2 + gB2 - dr2);
+    out[1] += fma(-7.0, dq2, fma(2.0, dr1, fma(5.0, dr2, fma(-2.0, gA2, fma(-4.0, gB2, gA1 + gB1 - dq1)))));
+    out[2] += fma(2.0, dq0, fma(5.0, dq1 + dr1, fma(11.0, dq2 + dr0, fma(2.0, dr2,
+              fma(3.0, gB0 + gB2, fma(-2.0, gA1, gA0 + gA2))))));
+    out[3] += fma(5.0, dq0, fma(2.0, dq1, fma(-7.0, dr0, fma(-2.0, gA0, fma(-4.0, gB0, gA1 - gB1 - dr1)))));
+    out[4] += fma(2.0, dr0, gA0 + gB0 - dq0);
   }
-}
+};
 
 // does cell with local index lc use the interface flux on its right / left?
 __device__ __forceinline__ bool uses_fr(int bc, int64_t lc, int64_t seg) {
@@ -238,8 +241,9 @@ __global__ void __launch_bounds__(NT) adj_vjp_kernel(AdjLine A, const double* __
         g = g < s0 ? s0 : (g > s1 ? s1 : g);
         p[q] = v[g];
       }
-      double vl, vr;
-      weno_vjp_states<K>(&p[K - 1], A.eps, vl, vr);
+      WenoTape<K> W;
+      W.fwd(&p[K - 1], A.eps);
+      const double vl = W.vl, vr = W.vr;
       const double mi = mu[i];
       // flux adjoints of the cell's right and left interfaces
       double ar = 0.0, al = 0.0;
@@ -257,7 +261,7 @@ __global__ void __launch_bounds__(NT) adj_vjp_kernel(AdjLine A, const double* __
                             (uses_fr(A.bc, li - 1, A.seg) ? mm : 0.0)) * idx;
         al = phi * 0.5 * (dflux(A, vl, li) - A.alpha);
       }
-      weno_vjp<K>(&p[K - 1], A.eps, ar, al, o);
+      W.rev(ar, al, o);
     }
 #pragma unroll
     for (int q = 0; q < NS; ++q) sc[t * NS + q] = o[q];
@@ -363,7 +367,9 @@ struct hrw_adjoint {
   double *u = nullptr, *w1 = nullptr, *w2 = nullptr, *tgt = nullptr;
   double *lam = nullptr, *la = nullptr, *lb = nullptr, *acc = nullptr, *J = nullptr;
   std::vector<double*> ckpt;  // checkpoints
-  double* tape = nullptr;     // (every + 1) states + every u1 + every u2
+  double* tape = nullptr;     // (E + 1) states + E u1 + E u2 of the segment being reversed
+  int64_t tape_states = 0;    // capacity of the tape in states
+  int64_t used_every = 0;     // checkpoint interval of the last gradient call
   int64_t fwd_steps = 0;      // forward steps taken by the last gradient call (incl. recompute)
 };
 
@@ -419,7 +425,8 @@ int hrw_adjoint_create(const hrw_problem* p, int nseg, int checkpoint_every, hrw
   if (nseg < 1) return adj_fail(HRW_EINVAL, "Invalid input 'nseg': must be >= 1.");
   if (nseg > 1 && p->ncells[0] % 8 != 0)
     return adj_fail(HRW_EINVAL, "hrw_adjoint: with nseg > 1, ncells must be a multiple of 8.");
-  if (checkpoint_every < 1) return adj_fail(HRW_EINVAL, "Invalid input 'checkpoint_every': must be >= 1.");
+  if (checkpoint_every < 0)
+    return adj_fail(HRW_EINVAL, "Invalid input 'checkpoint_every': must be >= 0 (0: automatic).");
   hrw_adjoint* h = new hrw_adjoint;
   AdjLine& L = h->line;
   L.seg = p->ncells[0];
@@ -444,7 +451,6 @@ int hrw_adjoint_create(const hrw_problem* p, int nseg, int checkpoint_every, hrw
   for (double** b : bufs)
     if (e == cudaSuccess) e = cudaMalloc(b, bytes);
   if (e == cudaSuccess) e = cudaMalloc(&h->J, sizeof(double) * nseg);
-  if (e == cudaSuccess) e = cudaMalloc(&h->tape, bytes * (size_t)(3 * checkpoint_every + 1));
   if (e != cudaSuccess) {
     hrw_adjoint_destroy(h);
     return adj_fail(e == cudaErrorMemoryAllocation ? HRW_ENOMEM : HRW_ECUDA,
@@ -463,7 +469,23 @@ int hrw_adjoint_gradient(hrw_adjoint* h, int mem, const double* u0, const double
   const AdjLine& L = h->line;
   const size_t bytes = sizeof(double) * (size_t)L.n;
   const cudaMemcpyKind in = mem == HRW_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
-  const int64_t E = h->every;
+  // checkpoint interval: as asked, or (0) the whole trajectory on the tape when it fits in
+  // 80% of the free device memory, else sqrt(nsteps)
+  int64_t E = h->every;
+  if (E == 0) {
+    size_t fr = 0, tot = 0;
+    HRW_ACUDA(cudaMemGetInfo(&fr, &tot));
+    const double need = (double)bytes * (3.0 * nsteps + 1.0 - (double)h->tape_states);
+    E = need <= 0.8 * (double)fr ? nsteps : (int64_t)std::ceil(std::sqrt((double)nsteps));
+  }
+  if (h->tape_states < 3 * E + 1) {
+    if (h->tape) cudaFree(h->tape);
+    h->tape = nullptr;
+    h->tape_states = 0;
+    HRW_ACUDA(cudaMalloc(&h->tape, bytes * (size_t)(3 * E + 1)));
+    h->tape_states = 3 * E + 1;
+  }
+  h->used_every = E;
   const int64_t nck = (nsteps + E - 1) / E;  // segments of the time line
   while ((int64_t)h->ckpt.size() < nck) {
     double* c = nullptr;
@@ -545,9 +567,10 @@ int hrw_adjoint_set_stream(hrw_adjoint* h, void* stream) {
   return HRW_OK;
 }
 
-int hrw_adjoint_info(const hrw_adjoint* h, int64_t* forward_steps) {
+int hrw_adjoint_info(const hrw_adjoint* h, int64_t* forward_steps, int64_t* checkpoint_every) {
   if (!h) return adj_fail(HRW_EINVAL, "Invalid input 'adjoint': null handle.");
   if (forward_steps) *forward_steps = h->fwd_steps;
+  if (checkpoint_every) *checkpoint_every = h->used_every;
   return HRW_OK;
 }
 

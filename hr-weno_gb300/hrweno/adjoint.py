@@ -24,7 +24,7 @@ def _setup(L):
     L.hrw_adjoint_create.argtypes = [C.POINTER(A.HrwProblem), i, i, C.POINTER(vp)]
     L.hrw_adjoint_gradient.argtypes = [vp, i, vp, vp, d, C.c_int64, dp, vp]
     L.hrw_adjoint_forward.argtypes = [vp, i, vp, vp, d, C.c_int64, dp, vp]
-    L.hrw_adjoint_info.argtypes = [vp, C.POINTER(C.c_int64)]
+    L.hrw_adjoint_info.argtypes = [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
     L.hrw_adjoint_set_stream.argtypes = [vp, vp]
     L.hrw_adjoint_destroy.argtypes = [vp]
     for n in ("hrw_adjoint_create", "hrw_adjoint_gradient", "hrw_adjoint_forward",
@@ -34,7 +34,8 @@ def _setup(L):
 
 
 class adjoint:  # noqa: N801
-    """adjoint(problem, nseg=1, checkpoint_every=45): nseg packed problems of ncells each."""
+    """adjoint(problem, nseg=1, checkpoint_every=45): nseg packed problems of ncells each;
+    checkpoint_every=0 keeps the whole trajectory in device memory when it fits."""
 
     def __init__(self, problem: Problem, nseg: int = 1, checkpoint_every: int = 45):
         L = A.lib()
@@ -75,8 +76,16 @@ class adjoint:  # noqa: N801
 
     @property
     def forward_steps(self) -> int:
+        """Forward steps (initial pass + recompute) of the last gradient call."""
         n = C.c_int64()
-        A.check(A.lib().hrw_adjoint_info(self._h, C.byref(n)))
+        A.check(A.lib().hrw_adjoint_info(self._h, C.byref(n), None))
+        return n.value
+
+    @property
+    def checkpoint_every(self) -> int:
+        """Checkpoint interval used by the last gradient call."""
+        n = C.c_int64()
+        A.check(A.lib().hrw_adjoint_info(self._h, None, C.byref(n)))
         return n.value
 
     def set_stream(self, stream) -> None:

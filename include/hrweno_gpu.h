@@ -176,7 +176,8 @@ int hrw_batch_destroy(hrw_batch* b);
  * The state holds nseg independent problems of p->ncells[0] cells each (packed; with
  * nseg > 1, ncells must be a multiple of 8); J has one entry per problem.  The reverse sweep
  * recomputes the forward from checkpoints taken every `checkpoint_every` steps (about
- * sqrt(nsteps) is the usual choice). */
+ * sqrt(nsteps) is the usual choice); 0 keeps the whole trajectory on the tape when it fits in
+ * 80% of the free device memory (no recompute), and falls back to sqrt(nsteps). */
 typedef struct hrw_adjoint hrw_adjoint;
 int hrw_adjoint_create(const hrw_problem* p, int nseg, int checkpoint_every, hrw_adjoint** out);
 /* grad = dJ/du0 (nseg * ncells doubles), J[nseg]; arrays in memory space `mem` (J on the host) */
@@ -185,8 +186,9 @@ int hrw_adjoint_gradient(hrw_adjoint* a, int mem, const double* u0, const double
 /* The forward solve alone: J[nseg] and u(T) (nullable) */
 int hrw_adjoint_forward(hrw_adjoint* a, int mem, const double* u0, const double* target, double dt,
                         int64_t nsteps, double* J, double* uT);
-/* forward steps (initial pass plus recompute) taken by the last gradient call */
-int hrw_adjoint_info(const hrw_adjoint* a, int64_t* forward_steps);
+/* forward steps (initial pass plus recompute) and the checkpoint interval of the last
+ * gradient call; either pointer may be NULL */
+int hrw_adjoint_info(const hrw_adjoint* a, int64_t* forward_steps, int64_t* checkpoint_every);
 int hrw_adjoint_set_stream(hrw_adjoint* a, void* stream);
 int hrw_adjoint_destroy(hrw_adjoint* a);
 
