@@ -652,6 +652,73 @@ def run_adjoint(args, dist: Dist) -> None:
     print(json.dumps(line), flush=True)
 
 
+# ------------------------------------------------------------------------------------------
+# config1: the reference's own CPU-runnable case, 500 cells, driven like example1 (101 output
+# times to t = 12, 1201 steps); one step is the whole driver loop
+# ------------------------------------------------------------------------------------------
+def run_config1(args, dist: Dist) -> None:
+    import torch
+
+    import hrweno
+    from hrweno import workloads
+
+    dev = dist.local if dist.world > 1 else 0
+    torch.cuda.set_device(dev)
+    prob, u0 = workloads.burgers_config1()
+    touts = [12.0 * ii / 100 for ii in range(101)]
+
+    def loop(graphs: bool, host: bool):
+        ode = hrweno.rktvd(prob, 500, 3)
+        ode.set_graphs(graphs)
+        u = u0.copy() if host else torch.from_numpy(u0.copy()).cuda()
+        t = 0.0
+        t0 = time.perf_counter()
+        for tout in touts:
+            t = ode.integrate(u, t, tout, 1e-2)
+        torch.cuda.synchronize()
+        return time.perf_counter() - t0, ode.nsteps
+
+    for _ in range(args.warmup):
+        loop(True, False)
+    res = {}
+    for graphs in (True, False):
+        for host in (False, True):
+            els = [loop(graphs, host)[0] for _ in range(args.steps)]
+            res[(graphs, host)] = float(np.median(els))
+    cells_steps = 500 * 1201
+    cpu = None
+    if not args.no_cpu:
+        from oracle import oracle
+        used = oracle.set_threads(1)
+        o = oracle.ODE(prob, 500, 0, 3)
+        u = u0.copy()
+        t, c0 = 0.0, time.perf_counter()
+        for tout in touts:
+            t = o.integrate(u, t, tout, 1e-2)
+        cel = time.perf_counter() - c0
+        cpu = {"value": cells_steps / cel, "unit": UNIT, "cores": used, "kind": "port",
+               "sample": f"the whole 1201-step driver loop ({cel * 1e3:.1f} ms), oracle, 1 thread"}
+    if dist.rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": cells_steps / res[(True, False)], "unit": UNIT,
+        "n_gpus": dist.world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * res[(True, False)], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "u0 = exp(-x^2) (the reference's example1)",
+        "config": {"workload": "config1_burgers500_weno5_lf_rk3", "cells": 500, "time_steps": 1201,
+                   "output_times": 101, "numerics": "fast"},
+        "driver_loop_ms": {"device_graphs": 1e3 * res[(True, False)],
+                           "device_no_graphs": 1e3 * res[(False, False)],
+                           "host_graphs": 1e3 * res[(True, True)],
+                           "host_no_graphs": 1e3 * res[(False, True)]},
+        "cpu_baseline": cpu,
+        "e2e": {"value": cells_steps / res[(True, True)], "unit": UNIT,
+                "h2d_bytes_per_step": 8 * 500 * 101, "d2h_bytes_per_step": 8 * 500 * 101},
+        "gpu_launches": 3 * 1201,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main() -> None:
     global NC
     ap = argparse.ArgumentParser()
@@ -661,7 +728,7 @@ def main() -> None:
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-forms", action="store_true", help="skip the FP32 form")
-    ap.add_argument("--workload", default="burgers1d", choices=["burgers1d", "pbe2d", "batched", "adjoint"],
+    ap.add_argument("--workload", default="burgers1d", choices=["burgers1d", "pbe2d", "batched", "adjoint", "config1"],
                     help="burgers1d (default): the 2^24-cell line; pbe2d: the 2D PBE grid")
     ap.add_argument("--pbe-n", type=int, default=PBE_N, help="pbe2d grid size per dimension")
     ap.add_argument("--adj-steps", type=int, default=ADJ_STEPS, help="adjoint: time steps")
@@ -687,6 +754,8 @@ def main() -> None:
             run_batched(args, dist)
         elif args.workload == "adjoint":
             run_adjoint(args, dist)
+        elif args.workload == "config1":
+            run_config1(args, dist)
         else:
             run_ours(args, dist)
     finally:

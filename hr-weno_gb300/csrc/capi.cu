@@ -132,6 +132,16 @@ struct hrw_ode {
   float* frw = nullptr;  // per-cell 1/width
   int fslot = 0;
   F32CArgs fbase{};
+  // CUDA graphs of kGraphSteps consecutive steps, replayed for long integrate calls
+  struct StepGraph {
+    cudaGraphExec_t exec = nullptr;
+    const void* ptr = nullptr;
+    double dt = 0.0;
+    cudaStream_t stream = nullptr;
+    int64_t phase = -1;
+    int64_t steps = 0;
+  } graph;
+  bool use_graphs = true;
 };
 
 extern "C" {
@@ -401,6 +411,12 @@ int hrw_ode_set_stream(hrw_ode* o, void* stream) {
   return HRW_OK;
 }
 
+int hrw_ode_set_graphs(hrw_ode* o, int enable) {
+  if (!o) return fail(HRW_EINVAL, "Invalid input 'ode': null handle.");
+  o->use_graphs = enable != 0;
+  return HRW_OK;
+}
+
 int hrw_ode_info(const hrw_ode* o, int* fevals, int* istate, int64_t* nsteps) {
   if (!o) return fail(HRW_EINVAL, "Invalid input 'ode': null handle.");
   if (fevals) *fevals = o->fevals;
@@ -423,6 +439,7 @@ int hrw_ode_destroy(hrw_ode* o) {
   for (double* p : o->ring_l)
     if (p) cudaFree(p);
   if (o->fmem) cudaFree(o->fmem);
+  if (o->graph.exec) cudaGraphExecDestroy(o->graph.exec);
   if (o->own) cudaStreamDestroy(o->own);
   delete o;
   return HRW_OK;
@@ -461,6 +478,59 @@ static cudaError_t rk_step(hrw_ode* o, double* u, double* out1, double dt) {
   return run_stage(o, ST_RK3C, o->w2, u, u, nullptr, nullptr, nullptr, dt);
 }
 
+// Captured graphs hold up to kGraphMax consecutive steps (rktvd; an even count for order 1,
+// which ping-pongs between two arrays) or a multiple of kMsPeriod steps (mstvd rotates a
+// 5-slot and a 4-slot ring, so its launch pattern repeats every 20 steps).  A driver loop that
+// integrates the same number of steps per call (the reference's output-time loops) captures
+// one graph and replays it on every later call.
+constexpr int64_t kGraphMax = 64;
+constexpr int64_t kMsPeriod = 20;
+
+// Replay `reps` times a graph of `steps` steps recorded by `record` (which launches them on
+// o->stream).  The graph is captured once and reused while the device array, dt, stream, ring
+// phase and step count stay the same.  Returns false (nothing launched) when capture is not
+// possible on this stream; the caller then launches the steps one by one.
+template <class Record>
+static bool run_graph(hrw_ode* o, const void* ptr, double dt, int64_t phase, int64_t steps,
+                      int64_t reps, Record record) {
+  auto& g = o->graph;
+  if (!g.exec || g.ptr != ptr || g.dt != dt || g.stream != o->stream || g.phase != phase ||
+      g.steps != steps) {
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+    g.exec = nullptr;
+    cudaStreamCaptureStatus st;
+    if (cudaStreamIsCapturing(o->stream, &st) != cudaSuccess || st != cudaStreamCaptureStatusNone)
+      return false;
+    if (cudaStreamBeginCapture(o->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+    const cudaError_t rec = record();
+    cudaGraph_t graph = nullptr;
+    const cudaError_t end = cudaStreamEndCapture(o->stream, &graph);
+    if (rec != cudaSuccess || end != cudaSuccess || !graph ||
+        cudaGraphInstantiate(&g.exec, graph, 0) != cudaSuccess) {
+      if (graph) cudaGraphDestroy(graph);
+      g.exec = nullptr;
+      cudaGetLastError();
+      return false;
+    }
+    cudaGraphDestroy(graph);
+    g.ptr = ptr, g.dt = dt, g.stream = o->stream, g.phase = phase, g.steps = steps;
+  }
+  for (int64_t r = 0; r < reps; ++r)
+    if (cudaGraphLaunch(g.exec, o->stream) != cudaSuccess) return false;
+  return true;
+}
+
+// steps per graph of an rktvd integration of n steps (0: no graph)
+static int64_t rk_graph_steps(const hrw_ode* o, int64_t n) {
+  if (!o->use_graphs || n < 4) return 0;
+  int64_t G = n < kGraphMax ? n : kGraphMax;
+  if (o->order == 1) G &= ~int64_t(1);
+  return G;
+}
+
 // rktvd_integrate (src/hrweno_tvdode.f90:97-178) on device array du.
 static int rk_integrate(hrw_ode* o, double* du, double* t, double tout, double dt, int itask) {
   // replay the reference's time sequence (:137-143) to count the steps
@@ -472,7 +542,21 @@ static int rk_integrate(hrw_ode* o, double* du, double* t, double tout, double d
   } while (!(is_done(tt, tout, dt) || itask == 2));
   double* cur = du;
   double* other = o->w2;
-  for (int64_t s = 0; s < n; ++s) {
+  int64_t s0 = 0;
+  if (const int64_t G = rk_graph_steps(o, n)) {
+    const bool ok = run_graph(o, du, dt, 0, G, n / G, [&]() {
+      double* c = du;
+      double* w = o->w2;
+      for (int64_t s = 0; s < G; ++s) {
+        const cudaError_t e = rk_step(o, c, w, dt);
+        if (e != cudaSuccess) return e;
+        if (o->order == 1) std::swap(c, w);
+      }
+      return cudaSuccess;
+    });
+    if (ok) s0 = n / G * G;
+  }
+  for (int64_t s = s0; s < n; ++s) {
     HRW_CUDA(rk_step(o, cur, other, dt));
     if (o->order == 1) std::swap(cur, other);
   }
@@ -512,14 +596,33 @@ static int ms_integrate(hrw_ode* o, double* du, double* t, double tout, double d
   int64_t n = 0;
   for (double t2 = tt; !is_done(t2, tout, dt); t2 = t2 + dt)
     if (++n > kMaxSteps) return fail(HRW_EINVAL, "Invalid input 'dt': too many steps to reach tout.");
-  for (int64_t s = 0; s < n; ++s) {  // (:252-268)
-    const int64_t m = o->level;
+  auto ms_step = [&](int64_t m) {  // (:252-268)
     double* um = o->ring_u[m % 5];
     double* un = o->ring_u[(m + 1) % 5];  // holds u^{m-4}, overwritten in place
     double* lm = o->ring_l[m % 4];        // holds L(u^{m-4}), overwritten in place
-    HRW_CUDA(run_stage(o, ST_MS, um, um, un, lm, un, lm, dt));
+    return run_stage(o, ST_MS, um, um, un, lm, un, lm, dt);
+  };
+  int64_t s0 = 0;
+  if (o->use_graphs && n >= kMsPeriod) {
+    const int64_t m0 = o->level;
+    const int64_t G = n < 3 * kMsPeriod ? kMsPeriod : 3 * kMsPeriod;
+    const bool ok = run_graph(o, o->ring_u[0], dt, m0 % kMsPeriod, G, n / G, [&]() {
+      for (int64_t s = 0; s < G; ++s) {
+        const cudaError_t e = ms_step(m0 + s);
+        if (e != cudaSuccess) return e;
+      }
+      return cudaSuccess;
+    });
+    if (ok) {
+      s0 = n / G * G;
+      for (int64_t s = 0; s < s0; ++s) tt = tt + dt;
+      o->level = m0 + s0;
+    }
+  }
+  for (int64_t s = s0; s < n; ++s) {
+    HRW_CUDA(ms_step(o->level));
     tt = tt + dt;
-    o->level = m + 1;
+    o->level = o->level + 1;
   }
   HRW_CUDA(cudaMemcpyAsync(du, o->ring_u[o->level % 5], bytes, cudaMemcpyDeviceToDevice, o->stream));
   *t = tt;
@@ -576,7 +679,20 @@ static int rk_integrate_f32c(hrw_ode* o, double* du, double* t, double tout, dou
   } while (!(is_done(tt, tout, dt) || itask == 2));
   int slot = 0;
   HRW_CUDA(launch_split_f64(du, o->fhi[0], o->flo[0], o->neq, o->stream));
-  for (int64_t s = 0; s < n; ++s) {
+  int64_t s0 = 0;
+  int64_t G = rk_graph_steps(o, n);
+  G &= ~int64_t(1);  // the compensated form always ping-pongs its (hi, lo) slots
+  if (G) {
+    const bool ok = run_graph(o, o->fhi[0], dt, 0, G, n / G, [&]() {
+      for (int64_t s = 0; s < G; ++s) {
+        const cudaError_t e = rk_step_f32c(o, (int)(s & 1), (int)(1 - (s & 1)), dt);
+        if (e != cudaSuccess) return e;
+      }
+      return cudaSuccess;
+    });
+    if (ok) s0 = n / G * G;
+  }
+  for (int64_t s = s0; s < n; ++s) {
     HRW_CUDA(rk_step_f32c(o, slot, 1 - slot, dt));
     slot = 1 - slot;
   }

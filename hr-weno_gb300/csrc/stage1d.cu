@@ -129,12 +129,22 @@ __global__ void __launch_bounds__(NT) stage1d_kernel(StageArgs a) {
   }
 }
 
-template <int K, int ST, bool STRICT>
-static cudaError_t launch_k(const StageArgs& a, cudaStream_t s) {
-  constexpr int NT = 128, C = 8;
+template <int K, int ST, bool STRICT, int NT, int C>
+static cudaError_t launch_shape(const StageArgs& a, cudaStream_t s) {
   const int64_t nblk = ((int64_t)a.L.nc + NT * C - 1) / (NT * C);
   stage1d_kernel<K, ST, STRICT, NT, C><<<(unsigned)nblk, NT, 0, s>>>(a);
   return cudaGetLastError();
+}
+
+// Tile shape by line length: 1024-cell tiles (128 threads x 8 cells) once there are at least
+// two tiles per SM; shorter lines use 256- or 64-cell tiles so that their few cells still
+// spread over many SMs (each SM retires only about 2 FP64 instructions per clock).
+template <int K, int ST, bool STRICT>
+static cudaError_t launch_k(const StageArgs& a, cudaStream_t s) {
+  const int64_t nc = a.L.nc;
+  if (nc >= 2 * 152 * 1024) return launch_shape<K, ST, STRICT, 128, 8>(a, s);
+  if (nc >= 2 * 152 * 256) return launch_shape<K, ST, STRICT, 64, 4>(a, s);
+  return launch_shape<K, ST, STRICT, 32, 2>(a, s);
 }
 
 template <int K, bool STRICT>

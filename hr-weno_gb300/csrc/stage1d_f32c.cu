@@ -169,12 +169,19 @@ __global__ void __launch_bounds__(NT) stage1d_f32c_kernel(F32CArgs a) {
   }
 }
 
-template <int K, int ST>
-static cudaError_t launch_k(const F32CArgs& a, cudaStream_t s) {
-  constexpr int NT = 256, C = 8;
+template <int K, int ST, int NT, int C>
+static cudaError_t launch_shape(const F32CArgs& a, cudaStream_t s) {
   const int64_t nblk = ((int64_t)a.L.nc + NT * C - 1) / (NT * C);
   stage1d_f32c_kernel<K, ST, NT, C><<<(unsigned)nblk, NT, 0, s>>>(a);
   return cudaGetLastError();
+}
+
+// 2048-cell blocks (8 warps x 256 cells) for long lines, one-warp blocks of 128 cells for
+// short ones so that they still spread over the SMs
+template <int K, int ST>
+static cudaError_t launch_k(const F32CArgs& a, cudaStream_t s) {
+  if (a.L.nc >= 2 * 152 * 2048) return launch_shape<K, ST, 256, 8>(a, s);
+  return launch_shape<K, ST, 32, 4>(a, s);
 }
 
 template <int K>

@@ -32,6 +32,10 @@ class _tvdode:
         """Run on a CUDA stream (an int handle, e.g. torch.cuda.Stream().cuda_stream)."""
         A.check(A.lib().hrw_ode_set_stream(self._h, C.c_void_p(int(stream) if stream else 0)))
 
+    def set_graphs(self, enable: bool) -> None:
+        """Replay captured CUDA graphs for long integrations (default) or launch each stage."""
+        A.check(A.lib().hrw_ode_set_graphs(self._h, int(bool(enable))))
+
     def _info(self):
         fe, st, ns = C.c_int(), C.c_int(), C.c_int64()
         A.check(A.lib().hrw_ode_info(self._h, C.byref(fe), C.byref(st), C.byref(ns)))

@@ -128,6 +128,12 @@ int hrw_mstvd_create(const hrw_problem* p, int neq, int dtype, hrw_ode** out);
 int hrw_integrate(hrw_ode* ode, int mem, void* u, double* t, double tout, double dt, int itask);
 /* fevals, istate (1 first call, 2 later calls, -1 error) and steps taken so far. */
 int hrw_ode_info(const hrw_ode* ode, int* fevals, int* istate, int64_t* nsteps);
+/* integrate calls of 4 or more steps replay a CUDA graph of captured steps (the stage
+ * launches of up to 64 consecutive rktvd steps, or 20/60 mstvd steps), recorded once per
+ * device array, dt, stream and step count, so a driver loop over output times captures once
+ * and replays on every later call; enable = 0 launches every stage directly.  Both give the
+ * same results bit for bit.  Default: enabled. */
+int hrw_ode_set_graphs(hrw_ode* ode, int enable);
 /* Run this handle's kernels on `stream` (a cudaStream_t); NULL restores its own stream. */
 int hrw_ode_set_stream(hrw_ode* ode, void* stream);
 int hrw_ode_destroy(hrw_ode* ode);
