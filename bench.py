@@ -398,6 +398,40 @@ def run_pbe2d(args, dist: Dist) -> None:
     assert steps_done == args.steps
     el = dist.max(e0.elapsed_time(e1) * 1e-3)
     value = dist.world * cells * args.steps / el
+    # compensated FP32 on the same grid and steps, error against the FP64 result
+    forms = {}
+    if not args.no_forms:
+        ode32 = hrweno.mstvd(prob, cells, dtype="f32c")
+        ode32.set_stream(stream.cuda_stream)
+        u32 = torch.from_numpy(n0).cuda()
+        t32 = ode32.integrate(u32, 0.0, (4 + args.warmup - 0.5) * dt, dt)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        t32 = ode32.integrate(u32, t32, t32 + (args.steps - 0.5) * dt, dt)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        el32 = dist.max(e0.elapsed_time(e1) * 1e-3)
+        diff = (u32 - u).abs()
+        v32 = dist.world * cells * args.steps / el32
+        forms["f32c"] = {"value": v32, "unit": UNIT, "ms_per_step": 1e3 * el32 / args.steps,
+                         "speedup_vs_f64": v32 / value, "bytes_per_cell_update": 32,
+                         "hbm_frac": 32 * v32 / dist.world / 1e9 / peaks()["hbm_gbs"],
+                         "rel_l1_vs_f64": float(diff.sum() / u.abs().sum()),
+                         "rel_linf_vs_f64": float(diff.max() / u.abs().max())}
+        del ode32, u32, diff
+        # accuracy at a stable step: 500 steps at CFL 0.3 on 1024^2 (at 0.4 the multistep
+        # scheme is unstable here and any two implementations drift apart)
+        m = 1024
+        pa, na, dta = workloads.pbe_config(m, m, cfl=0.3)
+        ua = torch.from_numpy(na.copy()).cuda()
+        ub = torch.from_numpy(na.copy()).cuda()
+        hrweno.mstvd(pa, m * m).integrate(ua, 0.0, 499.5 * dta, dta)
+        hrweno.mstvd(pa, m * m, dtype="f32c").integrate(ub, 0.0, 499.5 * dta, dta)
+        dd = (ua - ub).abs()
+        forms["f32c"]["accuracy_1024_cfl0.3_500steps"] = {
+            "rel_l1_vs_f64": float(dd.sum() / ua.abs().sum()),
+            "rel_linf_vs_f64": float(dd.max() / ua.abs().max())}
+        del ua, ub, dd
     # e2e: one multistep step per reference-facing call on pinned host memory
     ode2 = hrweno.mstvd(prob, cells)
     ode2.set_stream(stream.cuda_stream)
@@ -438,6 +472,7 @@ def run_pbe2d(args, dist: Dist) -> None:
         "cpu_baseline": cpu,
         "e2e": {"value": dist.world * cells * args.steps / e2e_el, "unit": UNIT,
                 "h2d_bytes_per_step": 8 * cells, "d2h_bytes_per_step": 8 * cells},
+        "forms": forms,
         "gpu_launches": steps_done,
         "clocks": clk.summary(),
     }

@@ -277,8 +277,8 @@ static int ode_create(const hrw_problem* p, int neq, int order, int method, int 
   int rc = validate_problem(p, neq);
   if (rc != HRW_OK) return rc;
   if (dtype == HRW_F32C) {
-    if (p->kind != HRW_PROBLEM_FV1D)
-      return fail(HRW_EINVAL, "Invalid input 'dtype': HRW_F32C supports HRW_PROBLEM_FV1D problems.");
+    if (p->kind != HRW_PROBLEM_FV1D && p->kind != HRW_PROBLEM_FV2D)
+      return fail(HRW_EINVAL, "Invalid input 'dtype': HRW_F32C supports FV1D and FV2D problems.");
     if (!(p->eps > 1.1920928955078125e-07))  // epsilon(1.0_real32), src/hrweno_weno.f90:92
       return fail(HRW_EINVAL, "Invalid input 'eps'. Valid range: eps > epsilon.");
   }
@@ -351,7 +351,11 @@ static int ode_create(const hrw_problem* p, int neq, int order, int method, int 
     // each array starts on a 256-byte boundary: the stage kernel reads and writes float4
     const int slots = method == 1 ? 5 : 2;
     const size_t n = (size_t)neq, sn = (n + 63) / 64 * 64;
-    const size_t nf = sn * (2 * slots + (method == 1 ? 4 : 0) + 2 + (p->width[0] ? 1 : 0));
+    const int nd = p->kind == HRW_PROBLEM_FV2D ? 2 : 1;
+    size_t nw = 0;  // per-cell 1/width entries of the lines that have widths
+    for (int d = 0; d < nd; ++d)
+      if (p->width[d]) nw += (size_t)(p->ncells[d] + 63) / 64 * 64;
+    const size_t nf = sn * (2 * slots + (method == 1 ? 4 : 0) + 2) + nw;
     if ((e = cudaMalloc(&o->fmem, sizeof(float) * nf)) != cudaSuccess) return cleanup(e);
     float* q = o->fmem;
     for (int k = 0; k < slots; ++k) { o->fhi[k] = q; q += sn; o->flo[k] = q; q += sn; }
@@ -360,25 +364,30 @@ static int ode_create(const hrw_problem* p, int neq, int order, int method, int 
     o->fd1 = q; q += sn;
     o->fd2 = q; q += sn;
     F32CArgs& f = o->fbase;
-    const LineArgs& L = b.L;
     f.eps = (float)p->eps;
-    f.L.nc = L.nc;
-    f.L.fn = L.fn;
-    f.L.bc = L.bc;
-    f.L.flux = L.flux;
-    f.L.a = (float)L.a;
-    f.L.b = (float)L.b;
-    f.L.alpha = (float)L.alpha;
-    f.L.xmin = (float)L.xmin;
-    f.L.rx = (float)L.rx;
-    f.L.gstep = (float)(L.b * L.rx);
-    if (p->width[0]) {
-      o->frw = q;
-      std::vector<float> rw(n);
-      for (size_t i = 0; i < n; ++i) rw[i] = (float)(1.0 / p->width[0][i]);
-      if ((e = cudaMemcpy(o->frw, rw.data(), sizeof(float) * n, cudaMemcpyHostToDevice)) != cudaSuccess)
-        return cleanup(e);
-      f.L.rw = o->frw;
+    f.ld = p->ncells[0];
+    for (int d = 0; d < nd; ++d) {
+      const LineArgs& L = d == 0 ? b.L : b.L2;
+      LineF& F = d == 0 ? f.L : f.L2;
+      F.nc = L.nc;
+      F.fn = L.fn;
+      F.bc = L.bc;
+      F.flux = L.flux;
+      F.a = (float)L.a;
+      F.b = (float)L.b;
+      F.alpha = (float)L.alpha;
+      F.xmin = (float)L.xmin;
+      F.rx = (float)L.rx;
+      F.gstep = (float)(L.b * L.rx);
+      if (p->width[d]) {
+        std::vector<float> rw(L.nc);
+        for (int i = 0; i < L.nc; ++i) rw[i] = (float)(1.0 / p->width[d][i]);
+        if ((e = cudaMemcpy(q, rw.data(), sizeof(float) * L.nc, cudaMemcpyHostToDevice)) != cudaSuccess)
+          return cleanup(e);
+        F.rw = q;
+        if (d == 0) o->frw = q;
+        q += (size_t)(L.nc + 63) / 64 * 64;
+      }
     }
     o->istate = 1;
     *out = o;
@@ -651,10 +660,17 @@ static cudaError_t run_f32c(hrw_ode* o, int stage, int slot, const float* dv, fl
   a.l4 = l4;
   a.lout = lout;
   const LineArgs& L = o->base.L;
-  const bool widths = o->frw != nullptr;
+  const bool widths = a.L.rw != nullptr;
   split_pair(widths ? dt : dt / L.rx, a.c_hi, a.c_lo);
   split_pair(dt, a.dt_hi, a.dt_lo);
   a.lscale = widths ? 1.0f : (float)(1.0 / L.rx);
+  if (o->prob.kind == HRW_PROBLEM_FV2D) {
+    const LineArgs& L2 = o->base.L2;
+    const bool w2 = a.L2.rw != nullptr;
+    split_pair(w2 ? dt : dt / L2.rx, a.c2_hi, a.c2_lo);
+    a.lscale2 = w2 ? 1.0f : (float)(1.0 / L2.rx);
+    return launch_stage2d_f32c(a, o->prob.k, stage, o->stream);
+  }
   return launch_stage1d_f32c(a, o->prob.k, stage, o->stream);
 }
 

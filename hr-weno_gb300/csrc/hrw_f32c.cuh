@@ -178,4 +178,37 @@ __device__ __forceinline__ float flux_diff_f32c(const LineF& L, int64_t j, float
   return (GR - GL) + extra;
 }
 
+// Stage update of one cell in increment form.  h, l: the state u = h + l; dv: the stored
+// stage increment (d1 or d2, zero for the first stage); dtL = dt L(v); Lv = L(v).
+// Writes the stage output, or the new state pair, as stage kind ST requires.
+template <int ST>
+__device__ __forceinline__ void f32c_update(const F32CArgs& a, int64_t j, float h, float l,
+                                            float dv, float dtL, float Lv) {
+  if constexpr (ST == FC_RHS) {
+    a.out[j] = Lv;
+  } else if constexpr (ST == FC_E1) {
+    a.out[j] = dtL;
+  } else if constexpr (ST == FC_RK3B) {
+    a.out[j] = 0.25f * (dv + dtL);
+  } else {
+    float inc;
+    if constexpr (ST == FC_RK1) {
+      inc = dtL;
+    } else if constexpr (ST == FC_RK2B) {
+      inc = 0.5f * (dv + dtL);
+    } else if constexpr (ST == FC_RK3C) {
+      inc = (2.f / 3.f) * (dv + dtL);
+    } else {  // FC_MS: u' = u + (7 (u4 - u) + 50 dt L + 10 dt L4) / 32
+      const float du4 = (a.hi4[j] - h) + (a.lo4[j] - l);
+      const float l4 = a.l4[j];
+      const float dtl4 = fmaf(a.dt_hi, l4, a.dt_lo * l4);
+      inc = fmaf(7.f / 32.f, du4, fmaf(50.f / 32.f, dtL, (10.f / 32.f) * dtl4));
+      a.lout[j] = Lv;
+    }
+    acc_add(h, l, inc);
+    a.hi_out[j] = h;
+    a.lo_out[j] = l;
+  }
+}
+
 }  // namespace hrw

@@ -88,9 +88,15 @@ struct F32CArgs {
   float lscale;       // 1 / dx (uniform) or 1
   float eps;
   LineF L;
+  // 2D (x1 fastest, row stride ld): the x2 line and its dt/dx2 pair and 1/dx2
+  LineF L2;
+  float c2_hi, c2_lo;
+  float lscale2;
+  int64_t ld;
 };
 
 cudaError_t launch_stage1d_f32c(const F32CArgs& a, int k, int stage, cudaStream_t s);
+cudaError_t launch_stage2d_f32c(const F32CArgs& a, int k, int stage, cudaStream_t s);
 cudaError_t launch_split_f64(const double* u, float* hi, float* lo, int64_t n, cudaStream_t s);
 cudaError_t launch_merge_f64(const float* hi, const float* lo, double* u, int64_t n, cudaStream_t s);
 cudaError_t launch_widen_f32(const float* x, double* y, int64_t n, cudaStream_t s);

@@ -46,7 +46,7 @@ enum {
 /* ---- element type and memory space of user arrays -------------------------------- */
 /* HRW_F64:  the FP64 method itself; user arrays are doubles.
  * HRW_F32:  reserved for the REAL32 build of the reference (src/hrweno_kinds.F90:9-10).
- * HRW_F32C: compensated FP32 bulk precision (FV1D problems): user arrays stay doubles; inside,
+ * HRW_F32C: compensated FP32 bulk precision (FV1D and FV2D): user arrays stay doubles; inside,
  *           the state is a float pair hi + lo and the right-hand side is evaluated in FP32 in
  *           difference form (compensated neighbour differences, flux differences relative
  *           to each cell's own flux, two-sum accumulation of u); t stays FP64. */
@@ -118,7 +118,7 @@ int hrw_weno_destroy(hrw_weno* w);
 typedef struct hrw_ode hrw_ode;
 
 /* rktvd(fu, neq, order): order 1..3; dtype HRW_F64 (the method itself) or HRW_F32C
- * (compensated FP32 bulk precision, FV1D problems; the user array stays FP64). */
+ * (compensated FP32 bulk precision, FV1D and FV2D problems; the user array stays FP64). */
 int hrw_rktvd_create(const hrw_problem* p, int neq, int order, int dtype, hrw_ode** out);
 /* mstvd(fu, neq): 5-step, 3rd-order TVD multistep with an RK3 start. */
 int hrw_mstvd_create(const hrw_problem* p, int neq, int dtype, hrw_ode** out);
@@ -141,7 +141,7 @@ int hrw_ode_destroy(hrw_ode* ode);
 /* ---- right-hand side alone (fu of the reference's driver) -------------------------- */
 /* vdot = L(v) at time t for problem p, both arrays device pointers of doubles
  * (LINEAR_ODE: neq = ncells[0]); dtype HRW_F64, or HRW_F32C to evaluate L in the
- * compensated FP32 form (FV1D problems). */
+ * compensated FP32 form (FV1D and FV2D problems). */
 int hrw_rhs(const hrw_problem* p, int dtype, double t, const void* v, void* vdot, void* stream);
 
 /* ---- batches of independent 1D problems ------------------------------------------- */

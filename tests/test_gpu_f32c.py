@@ -119,3 +119,49 @@ def test_f32c_full_size_vs_fp64_gpu(hw):
     assert l1 <= 1e-6, l1
     # the same integration conserves sum(u) to the FP32 increment rounding: copy boundaries
     # with zero flux difference at both boundary cells
+
+
+@pytest.mark.parametrize("shape", [(1, 1), (5, 7), (31, 33), (64, 40), (100, 37)])
+@pytest.mark.parametrize("k", [1, 2, 3])
+@pytest.mark.parametrize("bc", ["zero_inflow", "zero", "copy"])
+def test_rhs_f32c_2d(hw, orc, shape, k, bc):
+    n1, n2 = shape
+    rng = np.random.default_rng(n1 + 7 * n2 + k)
+    from hrweno import workloads
+    v = workloads.pbe_gaussian_2d(n1, n2, sigma=0.2, centre=(0.4, 0.5)) + 0.01 * rng.random(n1 * n2)
+    for flux in ("godunov", "lax_friedrichs"):
+        prob = hw.pbe_2d(n1, n2, k=k, flux=flux, bc=bc)
+        ref = orc.rhs(prob, v)
+        got = rhs_f32c(prob, v)
+        scale = max(np.max(np.abs(ref)), 1e-30)
+        assert np.max(np.abs(got - ref)) <= 2e-6 * scale, (shape, k, bc, flux)
+
+
+def test_f32c_mstvd_2d_vs_oracle(hw, orc):
+    from hrweno import workloads
+    n1, n2 = 96, 80
+    prob, n0, dt = workloads.pbe_config(n1, n2)
+    g, o = hw.mstvd(prob, n1 * n2, dtype="f32c"), orc.ODE(prob, n1 * n2, 1)
+    u32, u64 = n0.copy(), n0.copy()
+    t32 = t64 = 0.0
+    for tout in (0.0, 20 * dt, 61.5 * dt):
+        t32 = g.integrate(u32, t32, tout, dt)
+        t64 = o.integrate(u64, t64, tout, dt)
+        assert t32 == t64 and g.nsteps == o.info()[2]
+    assert rel_l1(u32, u64) <= 1e-6, rel_l1(u32, u64)
+
+
+def test_f32c_pbe1024_vs_fp64_gpu(hw):
+    """1024^2 PBE, mstvd, 500 steps: compensated FP32 against the FP64 GPU path.  CFL 0.3:
+    at 0.4 the multistep method is unstable on this problem and rounding differences of any
+    two implementations (FP64 and binary128 oracles included) grow without bound."""
+    import torch
+    from hrweno import workloads
+    n = 1024
+    prob, n0, dt = workloads.pbe_config(n, n, cfl=0.3)
+    a = torch.from_numpy(n0.copy()).cuda()
+    b = torch.from_numpy(n0.copy()).cuda()
+    hw.mstvd(prob, n * n).integrate(a, 0.0, 499.5 * dt, dt)
+    hw.mstvd(prob, n * n, dtype="f32c").integrate(b, 0.0, 499.5 * dt, dt)
+    l1 = float((a - b).abs().sum() / a.abs().sum())
+    assert l1 <= 1e-6, l1

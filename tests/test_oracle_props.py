@@ -96,3 +96,23 @@ def test_oracle_reproduces_golden_config1(orc):
         t = ode.integrate(u, t, snap["tout"], gold["dt"])
         assert t == snap["t"]
         assert np.array_equal(u, np.array(snap["u"]))
+
+
+def test_pbe_mstvd_stability_limit(orc):
+    """The 2D multistep scheme is rounding-stable at CFL 0.3 (FP64 and binary128 oracles
+    agree to 1e-14 after 300 steps) and unstable at the configuration's CFL 0.4 (they drift
+    apart by orders of magnitude): accuracy checks of the 2D forms use CFL 0.3."""
+    from hrweno import workloads
+    n = 96
+    drift = {}
+    for cfl in (0.3, 0.4):
+        p, n0, dt = workloads.pbe_config(n, n, cfl=cfl)
+        out = []
+        for prec in (64, 128):
+            o = orc.ODE(p, n * n, 1, prec=prec)
+            u = n0.copy()
+            o.integrate(u, 0.0, 299.5 * dt, dt)
+            out.append(u)
+        drift[cfl] = np.abs(out[0] - out[1]).sum() / np.abs(out[1]).sum()
+    assert drift[0.3] < 1e-14
+    assert drift[0.4] > 1e3 * drift[0.3]
