@@ -519,6 +519,26 @@ def run_batched(args, dist: Dist) -> None:
     value = dist.world * cells * args.steps / el
     assert bool(torch.isfinite(u).all())
 
+    # the same batch in compensated FP32
+    b32 = hrweno.batch(probs, order=3, dtype="f32c")
+    b32.set_stream(stream.cuda_stream)
+    shapes32 = b32.tune(packed, dts, probe_steps=3, cache_path=cache)
+    u32 = torch.from_numpy(packed.copy()).cuda()
+    t32 = np.zeros(BATCH_NPROB)
+    b32.advance(u32, t32, dts, args.warmup)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    b32.advance(u32, t32, dts, args.steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    el32 = dist.max(e0.elapsed_time(e1) * 1e-3)
+    d32 = (u32 - u).abs()
+    f32c_form = {"value": dist.world * cells * args.steps / el32, "unit": UNIT,
+                 "ms_per_step": 1e3 * el32 / args.steps, "shapes_per_class": shapes32,
+                 "speedup_vs_f64_batched": el / el32,
+                 "rel_l1_vs_f64": float(d32.sum() / u.abs().sum())}
+    del b32, u32, d32
+
     # the plain path: one rktvd handle per problem, integrated one after the other
     plain_steps = max(1, min(args.steps, 5))
     odes = [hrweno.rktvd(p, p.ncells[0], 3) for p in probs]
@@ -561,6 +581,7 @@ def run_batched(args, dist: Dist) -> None:
                      "frac": achieved / pk["hbm_gbs"], "traffic": None, "peak_src": pk["src"]},
         "plain_per_problem": {"value": plain, "unit": UNIT, "steps": plain_steps,
                               "speedup_batched": value / plain},
+        "forms": {"f32c": f32c_form},
         "cpu_baseline": None,
         "e2e": {"value": dist.world * cells * e2e_steps / e2e_el, "unit": UNIT,
                 "h2d_bytes_per_step": 8 * b.size, "d2h_bytes_per_step": 8 * b.size},

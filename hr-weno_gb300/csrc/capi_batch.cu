@@ -55,6 +55,7 @@ struct hrw_batch {
   double* u = nullptr;  // device state for host-memory calls
   double* u1 = nullptr;
   double* u2 = nullptr;
+  float* fmem = nullptr;  // HRW_F32C: hi/lo slots x 2, d1, d2 (packed like u)
   cudaStream_t own = nullptr, main = nullptr;
   cudaStream_t side[kClasses] = {};
   cudaEvent_t fork = nullptr, join[kClasses] = {};
@@ -108,16 +109,44 @@ int launch_all(hrw_batch* b, double* u, const int* shapes) {
       A.u1 = b->u1;
       A.u2 = b->u2;
       A.order = b->order;
-      const int per_sm = std::max(1, batch_blocks_per_sm(shapes[c], b->strict));
-      const int groups_per_block = 256 / kBatchShapes[shapes[c]].group;
+      const bool f32 = b->dtype == HRW_F32C;
+      if (f32) {
+        float* q = b->fmem;
+        for (int k = 0; k < 2; ++k) {
+          A.fhi[k] = q, q += b->total;
+          A.flo[k] = q, q += b->total;
+        }
+        A.fd1 = q, q += b->total;
+        A.fd2 = q;
+      }
+      const int per_sm = std::max(1, f32 ? batch_f32_blocks_per_sm(shapes[c])
+                                         : batch_blocks_per_sm(shapes[c], b->strict));
+      const int group = f32 ? kBatchShapesF32[shapes[c]].group : kBatchShapes[shapes[c]].group;
+      const int groups_per_block = 256 / group;
       int blocks = per_sm * b->sms;
       blocks = std::min<int64_t>(blocks, (n + groups_per_block - 1) / groups_per_block);
-      HRW_BCUDA(launch_batch(A, shapes[c], b->strict, std::max(blocks, 1), b->side[c]));
+      if (f32) HRW_BCUDA(launch_batch_f32c(A, shapes[c], std::max(blocks, 1), b->side[c]));
+      else HRW_BCUDA(launch_batch(A, shapes[c], b->strict, std::max(blocks, 1), b->side[c]));
     }
     HRW_BCUDA(cudaEventRecord(b->join[c], b->side[c]));
     HRW_BCUDA(cudaStreamWaitEvent(b->main, b->join[c], 0));
   }
   return HRW_OK;
+}
+
+// launch_all on the packed FP64 state du; compensated FP32 batches split it into their
+// (hi, lo) slot 0 first and merge the result back
+int run_all(hrw_batch* b, double* du) {
+  if (b->dtype == HRW_F32C) {
+    float* hi = b->fmem;
+    float* lo = b->fmem + b->total;
+    HRW_BCUDA(launch_split_f64(du, hi, lo, b->total, b->main));
+    int rc = launch_all(b, du, b->shape);
+    if (rc != HRW_OK) return rc;
+    HRW_BCUDA(launch_merge_f64(hi, lo, du, b->total, b->main));
+    return HRW_OK;
+  }
+  return launch_all(b, du, b->shape);
 }
 
 std::string tune_key(const hrw_batch* b, int c) {
@@ -129,7 +158,8 @@ std::string tune_key(const hrw_batch* b, int c) {
   }
   std::ostringstream s;
   s << b->dev_name << "|class" << c << "|n" << b->members[c].size() << "|cells" << cells << "|k" << mix
-    << "|order" << b->order << "|" << (b->strict ? "strict" : "fast");
+    << "|order" << b->order << "|" << (b->strict ? "strict" : "fast")
+    << (b->dtype == HRW_F32C ? "|f32c" : "|f64");
   std::string k = s.str();
   std::replace(k.begin(), k.end(), ' ', '_');
   return k;
@@ -145,7 +175,8 @@ int hrw_batch_create(const hrw_problem* probs, int nprob, int order, int dtype, 
   if (!probs || nprob <= 0) return batch_fail(HRW_EINVAL, "Invalid input 'nprob': must be >= 1.");
   if (order < 1 || order > 3)
     return batch_fail(HRW_EINVAL, "Invalid input 'order' in 'rktvd'. Valid range: 1 <= k <= 3.");
-  if (dtype != HRW_F64) return batch_fail(HRW_EINVAL, "Invalid input 'dtype': batches support HRW_F64.");
+  if (dtype != HRW_F64 && dtype != HRW_F32C)
+    return batch_fail(HRW_EINVAL, "Invalid input 'dtype': batches support HRW_F64 and HRW_F32C.");
   hrw_batch* b = new hrw_batch;
   b->nprob = nprob;
   b->order = order;
@@ -217,8 +248,12 @@ int hrw_batch_create(const hrw_problem* probs, int nprob, int order, int dtype, 
   if ((e = cudaMalloc(&b->d_order, sizeof(int) * nprob)) != cudaSuccess) return cleanup(e);
   if ((e = cudaMalloc(&b->d_counter, sizeof(int) * kClasses)) != cudaSuccess) return cleanup(e);
   if ((e = cudaMalloc(&b->u, bytes)) != cudaSuccess) return cleanup(e);
-  if ((e = cudaMalloc(&b->u1, bytes)) != cudaSuccess) return cleanup(e);
-  if ((e = cudaMalloc(&b->u2, bytes)) != cudaSuccess) return cleanup(e);
+  if (dtype == HRW_F32C) {
+    if ((e = cudaMalloc(&b->fmem, sizeof(float) * (size_t)off * 6)) != cudaSuccess) return cleanup(e);
+  } else {
+    if ((e = cudaMalloc(&b->u1, bytes)) != cudaSuccess) return cleanup(e);
+    if ((e = cudaMalloc(&b->u2, bytes)) != cudaSuccess) return cleanup(e);
+  }
   *out = b;
   return HRW_OK;
 }
@@ -233,8 +268,9 @@ int hrw_batch_info(const hrw_batch* b, int* shapes, int64_t* steps_done) {
   if (!b) return batch_fail(HRW_EINVAL, "Invalid input 'batch': null handle.");
   if (shapes)
     for (int c = 0; c < kClasses; ++c) {
-      shapes[2 * c] = kBatchShapes[b->shape[c]].group;
-      shapes[2 * c + 1] = kBatchShapes[b->shape[c]].cells;
+      const BatchShape& sh = b->dtype == HRW_F32C ? kBatchShapesF32[b->shape[c]] : kBatchShapes[b->shape[c]];
+      shapes[2 * c] = sh.group;
+      shapes[2 * c + 1] = sh.cells;
     }
   if (steps_done) std::memcpy(steps_done, b->steps_done.data(), sizeof(int64_t) * b->nprob);
   return HRW_OK;
@@ -278,7 +314,7 @@ int hrw_batch_integrate(hrw_batch* b, int mem, double* u, double* t, double tout
     du = b->u;
     HRW_BCUDA(cudaMemcpyAsync(du, u, bytes, cudaMemcpyHostToDevice, b->main));
   }
-  int rc = launch_all(b, du, b->shape);
+  int rc = run_all(b, du);
   if (rc != HRW_OK) return rc;
   if (mem == HRW_MEM_HOST) HRW_BCUDA(cudaMemcpyAsync(u, du, bytes, cudaMemcpyDeviceToHost, b->main));
   HRW_BCUDA(cudaStreamSynchronize(b->main));
@@ -308,7 +344,7 @@ int hrw_batch_advance(hrw_batch* b, int mem, double* u, double* t, const double*
     du = b->u;
     HRW_BCUDA(cudaMemcpyAsync(du, u, bytes, cudaMemcpyHostToDevice, b->main));
   }
-  int rc = launch_all(b, du, b->shape);
+  int rc = run_all(b, du);
   if (rc != HRW_OK) return rc;
   if (mem == HRW_MEM_HOST) HRW_BCUDA(cudaMemcpyAsync(u, du, bytes, cudaMemcpyDeviceToHost, b->main));
   HRW_BCUDA(cudaStreamSynchronize(b->main));
@@ -340,6 +376,8 @@ int hrw_batch_tune(hrw_batch* b, int mem, const double* u, const double* dt, int
   HRW_BCUDA(cudaMemcpyAsync(b->u, u, bytes,
                             mem == HRW_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice,
                             b->main));
+  if (b->dtype == HRW_F32C)
+    HRW_BCUDA(launch_split_f64(b->u, b->fmem, b->fmem + b->total, b->total, b->main));
   cudaEvent_t e0, e1;
   HRW_BCUDA(cudaEventCreate(&e0));
   HRW_BCUDA(cudaEventCreate(&e1));
@@ -396,6 +434,7 @@ int hrw_batch_destroy(hrw_batch* b) {
   if (b->u) cudaFree(b->u);
   if (b->u1) cudaFree(b->u1);
   if (b->u2) cudaFree(b->u2);
+  if (b->fmem) cudaFree(b->fmem);
   for (int c = 0; c < kClasses; ++c) {
     if (b->side[c]) cudaStreamDestroy(b->side[c]);
     if (b->join[c]) cudaEventDestroy(b->join[c]);

@@ -25,6 +25,11 @@ struct BatchArgs {
   double* u1;            // packed stage arrays
   double* u2;
   int order;             // rktvd order 1..3
+  // compensated FP32 batches: state slots (hi, lo) x 2 and the stage increments, packed
+  float* fhi[2];
+  float* flo[2];
+  float* fd1;
+  float* fd2;
 };
 
 struct BatchShape {
@@ -37,5 +42,10 @@ extern const BatchShape kBatchShapes[kNumBatchShapes];
 
 int batch_blocks_per_sm(int shape, bool strict);
 cudaError_t launch_batch(const BatchArgs& B, int shape, bool strict, int blocks, cudaStream_t s);
+
+// compensated FP32 batches: their own shapes (cells per thread a multiple of 4)
+extern const BatchShape kBatchShapesF32[kNumBatchShapes];
+int batch_f32_blocks_per_sm(int shape);
+cudaError_t launch_batch_f32c(const BatchArgs& B, int shape, int blocks, cudaStream_t s);
 
 }  // namespace hrw

@@ -14,7 +14,7 @@ from . import _abi as A
 from ._arrays import describe
 from .problems import Problem
 
-_DT = {"f64": A.HRW_F64}
+_DT = {"f64": A.HRW_F64, "f32c": A.HRW_F32C}
 
 
 def _setup(L):

@@ -147,8 +147,8 @@ int hrw_rhs(const hrw_problem* p, int dtype, double t, const void* v, void* vdot
 /* ---- batches of independent 1D problems ------------------------------------------- */
 /* A batch holds nprob independent FV1D problems on uniform grids (each its own rktvd(fu,
  * neq, order) of the reference, src/hrweno_tvdode.f90:69-178, with its own ncells, k, flux,
- * flux function, alpha and boundaries; all share `order`, dtype HRW_F64 and one numerics
- * mode).  Their states are packed in one array: problem i occupies cells
+ * flux function, alpha and boundaries; all share `order`, the dtype (HRW_F64, or HRW_F32C:
+ * the compensated FP32 form, states still packed as FP64) and one numerics mode).  Their states are packed in one array: problem i occupies cells
  * [offsets[i], offsets[i] + ncells_i) of the layout returned by hrw_batch_layout
  * (offsets[nprob] is the packed length).  One call advances every problem with one
  * persistent launch per size class, the classes running concurrently. */

@@ -114,3 +114,44 @@ def test_batch_validation(hw):
         hw.batch([ok, hw.burgers_1d(10, numerics="strict")])
     with pytest.raises(HrwError, match="FV1D"):
         hw.batch([ok, hw.pbe_2d(4, 4)])
+
+
+def test_batch_f32c_vs_fp64(hw):
+    """Compensated-FP32 batches against FP64 batches: relative L1 <= 1e-6 over the batch and
+    <= 1e-5 per problem.  (A coarse line whose profile changes by O(1) per step carries an
+    FP32 error of about eps * sqrt(steps) of its values: the compensation helps where the
+    increments are small against the state.)"""
+    import torch
+    from hrweno import workloads
+    probs, lines, dts = workloads.batched_config(128, seed=21, nmax=30000)
+    res = {}
+    for dtype in ("f64", "f32c"):
+        b = hw.batch(probs, order=3, dtype=dtype)
+        u = torch.from_numpy(b.pack(lines)).cuda()
+        t = np.zeros(len(probs))
+        b.advance(u, t, dts, 60)
+        res[dtype] = b.unpack(u)
+        assert np.all(b.steps_done == 60)
+    num = den = 0.0
+    for a, c in zip(res["f64"], res["f32c"]):
+        assert np.sum(np.abs(a - c)) <= 1e-5 * np.sum(np.abs(a))
+        num += np.sum(np.abs(a - c))
+        den += np.sum(np.abs(a))
+    assert num <= 1e-6 * den
+
+
+@pytest.mark.parametrize("order", [1, 2, 3])
+def test_batch_f32c_vs_single_f32c(hw, order):
+    """A compensated-FP32 batch and single compensated-FP32 solves agree to the FP32 form's
+    own accuracy (the shapes differ, the arithmetic per cell does not)."""
+    probs, lines, dts = mixed_problems(hw, "fast", sizes=(8, 64, 300, 600, 5000, 9000))
+    b = hw.batch(probs, order=order, dtype="f32c")
+    u = b.pack(lines)
+    t = np.zeros(len(probs))
+    steps = 6 if order == 1 else 30
+    b.advance(u, t, dts, steps)
+    got = b.unpack(u)
+    for i, p in enumerate(probs):
+        v = lines[i].copy()
+        hw.rktvd(p, p.ncells[0], order, dtype="f32c").integrate(v, 0.0, (steps - 0.5) * dts[i], dts[i])
+        assert np.array_equal(got[i], v), i
