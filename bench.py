@@ -221,7 +221,7 @@ def config_dict() -> dict:
 # ------------------------------------------------------------------------------------------
 # GPU arm
 # ------------------------------------------------------------------------------------------
-def run_ours(args, dist: Dist) -> None:
+def run_ours(args, dist: Dist) -> dict | None:
     import torch
 
     import hrweno
@@ -300,7 +300,7 @@ def run_ours(args, dist: Dist) -> None:
            "h2d_bytes_per_step": 8 * NC, "d2h_bytes_per_step": 8 * NC}
 
     if dist.rank != 0:
-        return
+        return None
 
     pk = peaks()
     launch_s = el / (args.steps * LAUNCHES_PER_STEP)
@@ -348,7 +348,7 @@ def run_ours(args, dist: Dist) -> None:
         "gpu_launches": steps_done * LAUNCHES_PER_STEP,
         "clocks": clk.summary(),
     }
-    print(json.dumps(line), flush=True)
+    return line
 
 
 # ------------------------------------------------------------------------------------------
@@ -368,7 +368,7 @@ def pbe_config_dict(n: int) -> dict:
             "l2": f"inputs larger than L2: 5 + 4 ring slots of {n * n * 8 >> 20} MiB"}
 
 
-def run_pbe2d(args, dist: Dist) -> None:
+def run_pbe2d(args, dist: Dist) -> dict | None:
     import torch
 
     import hrweno
@@ -444,7 +444,7 @@ def run_pbe2d(args, dist: Dist) -> None:
     torch.cuda.synchronize()
     e2e_el = dist.max(time.perf_counter() - h0)
     if dist.rank != 0:
-        return
+        return None
     pk = peaks()
     achieved = PBE_BYTES_PER_CELL_UPDATE * cells * args.steps / el / 1e9
     cpu = None
@@ -476,7 +476,7 @@ def run_pbe2d(args, dist: Dist) -> None:
         "gpu_launches": steps_done,
         "clocks": clk.summary(),
     }
-    print(json.dumps(line), flush=True)
+    return line
 
 
 # ------------------------------------------------------------------------------------------
@@ -486,7 +486,7 @@ def run_pbe2d(args, dist: Dist) -> None:
 BATCH_NPROB = 4096
 
 
-def run_batched(args, dist: Dist) -> None:
+def run_batched(args, dist: Dist) -> dict | None:
     import tempfile
 
     import torch
@@ -565,7 +565,7 @@ def run_batched(args, dist: Dist) -> None:
         b.advance(uh, th, dts, 1)
     e2e_el = dist.max(time.perf_counter() - h0)
     if dist.rank != 0:
-        return
+        return None
     pk = peaks()
     achieved = BYTES_PER_CELL_UPDATE * cells * args.steps / el / 1e9
     line = {
@@ -588,7 +588,7 @@ def run_batched(args, dist: Dist) -> None:
         "gpu_launches": 3,
         "clocks": clk.summary(),
     }
-    print(json.dumps(line), flush=True)
+    return line
 
 
 # ------------------------------------------------------------------------------------------
@@ -599,7 +599,7 @@ def run_batched(args, dist: Dist) -> None:
 ADJ_N, ADJ_STEPS, ADJ_EVERY = 1 << 20, 2000, 45
 
 
-def run_adjoint(args, dist: Dist) -> None:
+def run_adjoint(args, dist: Dist) -> dict | None:
     import torch
 
     import hrweno
@@ -682,7 +682,7 @@ def run_adjoint(args, dist: Dist) -> None:
     torch.cuda.synchronize()
     bt_grad, bt_fwd = e[0].elapsed_time(e[1]) * 1e-3, e[2].elapsed_time(e[3]) * 1e-3
     if dist.rank != 0:
-        return
+        return None
     value = dist.world * n * nsteps / t_grad
     line = {
         "metric": METRIC, "value": value, "unit": UNIT + " (gradient)", "n_gpus": dist.world,
@@ -705,14 +705,14 @@ def run_adjoint(args, dist: Dist) -> None:
         "gpu_launches": None,
         "clocks": clk.summary(),
     }
-    print(json.dumps(line), flush=True)
+    return line
 
 
 # ------------------------------------------------------------------------------------------
 # config1: the reference's own CPU-runnable case, 500 cells, driven like example1 (101 output
 # times to t = 12, 1201 steps); one step is the whole driver loop
 # ------------------------------------------------------------------------------------------
-def run_config1(args, dist: Dist) -> None:
+def run_config1(args, dist: Dist) -> dict | None:
     import torch
 
     import hrweno
@@ -755,7 +755,7 @@ def run_config1(args, dist: Dist) -> None:
         cpu = {"value": cells_steps / cel, "unit": UNIT, "cores": used, "kind": "port",
                "sample": f"the whole 1201-step driver loop ({cel * 1e3:.1f} ms), oracle, 1 thread"}
     if dist.rank != 0:
-        return
+        return None
     line = {
         "metric": METRIC, "value": cells_steps / res[(True, False)], "unit": UNIT,
         "n_gpus": dist.world, "steps": args.steps, "warmup": args.warmup,
@@ -772,7 +772,7 @@ def run_config1(args, dist: Dist) -> None:
                 "h2d_bytes_per_step": 8 * 500 * 101, "d2h_bytes_per_step": 8 * 500 * 101},
         "gpu_launches": 3 * 1201,
     }
-    print(json.dumps(line), flush=True)
+    return line
 
 
 def main() -> None:
@@ -804,16 +804,37 @@ def main() -> None:
         return
     dist = Dist()
     try:
-        if args.workload == "pbe2d":
-            run_pbe2d(args, dist)
-        elif args.workload == "batched":
-            run_batched(args, dist)
-        elif args.workload == "adjoint":
-            run_adjoint(args, dist)
-        elif args.workload == "config1":
-            run_config1(args, dist)
+        runs = {"pbe2d": run_pbe2d, "batched": run_batched, "adjoint": run_adjoint,
+                "config1": run_config1}
+        if args.workload != "burgers1d":
+            line = runs[args.workload](args, dist)
         else:
-            run_ours(args, dist)
+            line = run_ours(args, dist)
+            if not args.no_forms:
+                # the other forms of the metric, each on its own workload, summarised
+                sub = argparse.Namespace(**vars(args))
+                sub.steps, sub.no_cpu = min(args.steps, 100), True
+                forms = {}
+                pb = run_pbe2d(sub, dist)
+                if pb is not None:
+                    forms["pbe2d_4096"] = {k: pb[k] for k in ("value", "ms_per_step", "roofline", "forms")}
+                sub.steps = min(args.steps, 20)
+                bt = run_batched(sub, dist)
+                if bt is not None:
+                    forms["batched_4096_lines"] = {k: bt[k] for k in ("value", "ms_per_step", "config",
+                                                                     "plain_per_problem", "forms")}
+                sub.steps, sub.fd_directions = 1, 2
+                ad = run_adjoint(sub, dist)
+                if ad is not None:
+                    forms["adjoint_2^20"] = ad["adjoint"]
+                sub.steps = 3
+                c1 = run_config1(sub, dist)
+                if c1 is not None:
+                    forms["config1_500"] = {k: c1[k] for k in ("value", "driver_loop_ms")}
+                if line is not None:
+                    line["forms"].update(forms)
+        if line is not None and dist.rank == 0:
+            print(json.dumps(line), flush=True)
     finally:
         dist.close()
 

@@ -460,10 +460,12 @@ int hrw_adjoint_create(const hrw_problem* p, int nseg, int checkpoint_every, hrw
   return HRW_OK;
 }
 
-int hrw_adjoint_gradient(hrw_adjoint* h, int mem, const double* u0, const double* target, double dt,
-                         int64_t nsteps, double* J, double* grad) {
+// The reverse sweep shared by hrw_adjoint_gradient (lambda(T) = u(T) - target, J computed) and
+// hrw_adjoint_vjp (lambda(T) given).
+static int adjoint_sweep(hrw_adjoint* h, int mem, const double* u0, const double* target,
+                         const double* lambda_T, double dt, int64_t nsteps, double* J, double* grad) {
   if (!h) return adj_fail(HRW_EINVAL, "Invalid input 'adjoint': null handle.");
-  if (!u0 || !target || !grad) return adj_fail(HRW_EINVAL, "Invalid input: null pointer.");
+  if (!u0 || !(target || lambda_T) || !grad) return adj_fail(HRW_EINVAL, "Invalid input: null pointer.");
   if (nsteps < 1) return adj_fail(HRW_EINVAL, "Invalid input 'nsteps': must be >= 1.");
   if (!(dt != 0.0) || !std::isfinite(dt)) return adj_fail(HRW_EINVAL, "Invalid input 'dt'.");
   const AdjLine& L = h->line;
@@ -498,7 +500,7 @@ int hrw_adjoint_gradient(hrw_adjoint* h, int mem, const double* u0, const double
   auto U2 = [&](int64_t n) { return U + (size_t)(2 * E + 1 + n) * L.n; };
   // ---- forward: checkpoints, the last segment recorded on the tape ------------------------
   HRW_ACUDA(cudaMemcpyAsync(h->u, u0, bytes, in, h->stream));
-  HRW_ACUDA(cudaMemcpyAsync(h->tgt, target, bytes, in, h->stream));
+  HRW_ACUDA(cudaMemcpyAsync(h->tgt, target ? target : lambda_T, bytes, in, h->stream));
   int64_t fwd = 0;
   for (int64_t c = 0; c < nck; ++c) {
     const int64_t len = std::min(E, nsteps - c * E);
@@ -513,9 +515,13 @@ int hrw_adjoint_gradient(hrw_adjoint* h, int mem, const double* u0, const double
   }
   // ---- misfit and lambda(T) -----------------------------------------------------------------
   const int64_t last_len = nsteps - (nck - 1) * E;
-  HRW_ACUDA(cudaMemsetAsync(h->J, 0, sizeof(double) * h->nseg, h->stream));
-  adj_misfit_kernel<<<152 * 8, 256, 0, h->stream>>>(L, Un(last_len), h->tgt, h->lam, h->J);
-  HRW_ACUDA(cudaGetLastError());
+  if (target) {
+    HRW_ACUDA(cudaMemsetAsync(h->J, 0, sizeof(double) * h->nseg, h->stream));
+    adj_misfit_kernel<<<152 * 8, 256, 0, h->stream>>>(L, Un(last_len), h->tgt, h->lam, h->J);
+    HRW_ACUDA(cudaGetLastError());
+  } else {
+    HRW_ACUDA(cudaMemcpyAsync(h->lam, h->tgt, bytes, cudaMemcpyDeviceToDevice, h->stream));
+  }
   // ---- reverse sweep ---------------------------------------------------------------------------
   for (int64_t c = nck - 1; c >= 0; --c) {
     const int64_t len = std::min(E, nsteps - c * E);
@@ -533,9 +539,22 @@ int hrw_adjoint_gradient(hrw_adjoint* h, int mem, const double* u0, const double
   h->fwd_steps = fwd;
   const cudaMemcpyKind outk = mem == HRW_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
   HRW_ACUDA(cudaMemcpyAsync(grad, h->lam, bytes, outk, h->stream));
-  if (J) HRW_ACUDA(cudaMemcpyAsync(J, h->J, sizeof(double) * h->nseg, cudaMemcpyDeviceToHost, h->stream));
+  if (J && target)
+    HRW_ACUDA(cudaMemcpyAsync(J, h->J, sizeof(double) * h->nseg, cudaMemcpyDeviceToHost, h->stream));
   HRW_ACUDA(cudaStreamSynchronize(h->stream));
   return HRW_OK;
+}
+
+int hrw_adjoint_gradient(hrw_adjoint* h, int mem, const double* u0, const double* target, double dt,
+                         int64_t nsteps, double* J, double* grad) {
+  if (!target) return adj_fail(HRW_EINVAL, "Invalid input 'target': null pointer.");
+  return adjoint_sweep(h, mem, u0, target, nullptr, dt, nsteps, J, grad);
+}
+
+int hrw_adjoint_vjp(hrw_adjoint* h, int mem, const double* u0, const double* lambda_T, double dt,
+                    int64_t nsteps, double* grad) {
+  if (!lambda_T) return adj_fail(HRW_EINVAL, "Invalid input 'lambda_T': null pointer.");
+  return adjoint_sweep(h, mem, u0, nullptr, lambda_T, dt, nsteps, nullptr, grad);
 }
 
 // Forward only: u(T) after nsteps steps and J (per segment); the reference point of the
@@ -543,20 +562,23 @@ int hrw_adjoint_gradient(hrw_adjoint* h, int mem, const double* u0, const double
 int hrw_adjoint_forward(hrw_adjoint* h, int mem, const double* u0, const double* target, double dt,
                         int64_t nsteps, double* J, double* uT) {
   if (!h) return adj_fail(HRW_EINVAL, "Invalid input 'adjoint': null handle.");
-  if (!u0 || !target) return adj_fail(HRW_EINVAL, "Invalid input: null pointer.");
+  if (!u0) return adj_fail(HRW_EINVAL, "Invalid input: null pointer.");
   const AdjLine& L = h->line;
   const size_t bytes = sizeof(double) * (size_t)L.n;
   const cudaMemcpyKind in = mem == HRW_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
   HRW_ACUDA(cudaMemcpyAsync(h->u, u0, bytes, in, h->stream));
-  HRW_ACUDA(cudaMemcpyAsync(h->tgt, target, bytes, in, h->stream));
   for (int64_t n = 0; n < nsteps; ++n) HRW_ACUDA(step(h, h->u, h->w1, h->w2, h->u, dt));
-  HRW_ACUDA(cudaMemsetAsync(h->J, 0, sizeof(double) * h->nseg, h->stream));
-  adj_misfit_kernel<<<152 * 8, 256, 0, h->stream>>>(L, h->u, h->tgt, h->lam, h->J);
-  HRW_ACUDA(cudaGetLastError());
+  if (target) {
+    HRW_ACUDA(cudaMemcpyAsync(h->tgt, target, bytes, in, h->stream));
+    HRW_ACUDA(cudaMemsetAsync(h->J, 0, sizeof(double) * h->nseg, h->stream));
+    adj_misfit_kernel<<<152 * 8, 256, 0, h->stream>>>(L, h->u, h->tgt, h->lam, h->J);
+    HRW_ACUDA(cudaGetLastError());
+  }
   if (uT)
     HRW_ACUDA(cudaMemcpyAsync(uT, h->u, bytes, mem == HRW_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice,
                               h->stream));
-  if (J) HRW_ACUDA(cudaMemcpyAsync(J, h->J, sizeof(double) * h->nseg, cudaMemcpyDeviceToHost, h->stream));
+  if (J && target)
+    HRW_ACUDA(cudaMemcpyAsync(J, h->J, sizeof(double) * h->nseg, cudaMemcpyDeviceToHost, h->stream));
   HRW_ACUDA(cudaStreamSynchronize(h->stream));
   return HRW_OK;
 }

@@ -145,8 +145,10 @@ __device__ __forceinline__ float phys_g(const LineF& L, float v, float a, float 
   if (L.fn == HRW_FN_BURGERS) return 0.5f * a * (2.f * v + a);
   return g * a;
 }
+// g at interface e (e <= nc < 2^31): the 32-bit conversion stays on the FP32 side; an int64
+// to float conversion would run on the narrow FP64 unit
 __device__ __forceinline__ float g_at(const LineF& L, int64_t e) {
-  return L.b != 0.f ? fmaf(L.b, fmaf(L.rx, (float)e, L.xmin), L.a) : L.a;
+  return L.b != 0.f ? fmaf(L.b, fmaf(L.rx, __int2float_rn((int)e), L.xmin), L.a) : L.a;
 }
 
 // Flux difference F_{j+1/2} - F_{j-1/2} of cell j (value v) from the offsets:

@@ -14,3 +14,9 @@ from .batch import batch  # noqa: F401
 from .problems import Problem, burgers_1d, linear_ode, pbe_2d  # noqa: F401
 from .tvdode import mstvd, rktvd  # noqa: F401
 from .weno import weno  # noqa: F401
+
+
+def weno_solve(*args, **kwargs):
+    """Differentiable u(T) = weno_solve(u0, problem, dt, nsteps) for PyTorch (torch_op)."""
+    from .torch_op import weno_solve as _ws
+    return _ws(*args, **kwargs)

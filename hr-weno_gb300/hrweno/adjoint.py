@@ -24,10 +24,11 @@ def _setup(L):
     L.hrw_adjoint_create.argtypes = [C.POINTER(A.HrwProblem), i, i, C.POINTER(vp)]
     L.hrw_adjoint_gradient.argtypes = [vp, i, vp, vp, d, C.c_int64, dp, vp]
     L.hrw_adjoint_forward.argtypes = [vp, i, vp, vp, d, C.c_int64, dp, vp]
+    L.hrw_adjoint_vjp.argtypes = [vp, i, vp, vp, d, C.c_int64, vp]
     L.hrw_adjoint_info.argtypes = [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
     L.hrw_adjoint_set_stream.argtypes = [vp, vp]
     L.hrw_adjoint_destroy.argtypes = [vp]
-    for n in ("hrw_adjoint_create", "hrw_adjoint_gradient", "hrw_adjoint_forward",
+    for n in ("hrw_adjoint_create", "hrw_adjoint_gradient", "hrw_adjoint_forward", "hrw_adjoint_vjp",
               "hrw_adjoint_info", "hrw_adjoint_set_stream", "hrw_adjoint_destroy"):
         getattr(L, n).restype = C.c_int
     L._adj_ready = True
@@ -63,16 +64,28 @@ class adjoint:  # noqa: N801
         return J, grad
 
     def forward(self, u0, target, dt: float, nsteps: int, uT=None):
-        """(J, uT) of the forward solve alone."""
+        """(J, uT) of the forward solve alone (J is None when target is None)."""
         m0, p0, _ = describe(u0, self.size, False)
-        m1, p1, _ = describe(target, self.size, False)
+        p1 = None
+        if target is not None:
+            _, p1, _ = describe(target, self.size, False)
         pT = None
         if uT is not None:
             _, pT, _ = describe(uT, self.size, True)
         J = np.empty(self.nseg)
         A.check(A.lib().hrw_adjoint_forward(self._h, m0, p0, p1, float(dt), int(nsteps),
                                             J.ctypes.data_as(C.POINTER(C.c_double)), pT))
-        return J, uT
+        return (J if target is not None else None), uT
+
+    def vjp(self, u0, lambda_T, dt: float, nsteps: int, grad=None):
+        """d <lambda_T, u(T)> / du0."""
+        m0, p0, _ = describe(u0, self.size, False)
+        _, p1, _ = describe(lambda_T, self.size, False)
+        if grad is None:
+            grad = u0.new_empty(u0.shape) if hasattr(u0, "new_empty") else np.empty_like(u0)
+        _, p2, _ = describe(grad, self.size, True)
+        A.check(A.lib().hrw_adjoint_vjp(self._h, m0, p0, p1, float(dt), int(nsteps), p2))
+        return grad
 
     @property
     def forward_steps(self) -> int:

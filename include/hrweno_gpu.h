@@ -189,7 +189,11 @@ int hrw_adjoint_create(const hrw_problem* p, int nseg, int checkpoint_every, hrw
 /* grad = dJ/du0 (nseg * ncells doubles), J[nseg]; arrays in memory space `mem` (J on the host) */
 int hrw_adjoint_gradient(hrw_adjoint* a, int mem, const double* u0, const double* target, double dt,
                          int64_t nsteps, double* J, double* grad);
-/* The forward solve alone: J[nseg] and u(T) (nullable) */
+/* grad = d <lambda_T, u(T)> / du0 for any lambda_T: the vector-Jacobian product of the whole
+ * forward map (what an automatic-differentiation framework calls backward) */
+int hrw_adjoint_vjp(hrw_adjoint* a, int mem, const double* u0, const double* lambda_T, double dt,
+                    int64_t nsteps, double* grad);
+/* The forward solve alone: u(T) (nullable) and, when target is not NULL, J[nseg] */
 int hrw_adjoint_forward(hrw_adjoint* a, int mem, const double* u0, const double* target, double dt,
                         int64_t nsteps, double* J, double* uT);
 /* forward steps (initial pass plus recompute) and the checkpoint interval of the last

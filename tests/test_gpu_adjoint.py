@@ -105,3 +105,26 @@ def test_adjoint_central_differences(hw):
         fd = (Jp[0] - Jm[0]) / (2 * h)
         gd = float((g * d).sum())
         assert abs(fd - gd) <= 1e-6 * abs(gd), (s, fd, gd)
+
+
+def test_torch_autograd_op(hw):
+    """loss = 0.5 ||weno_solve(u0) - target||^2; loss.backward() gives the adjoint gradient,
+    and a general upstream gradient matches the tangent-linear oracle."""
+    import torch
+    n, steps = 512, 80
+    prob = problem(hw, n, 3, "burgers", "copy")
+    dt = 0.4 * (10.0 / n) / 1.5
+    u0 = torch.from_numpy(line(n, 5)).cuda().requires_grad_(True)
+    tg = torch.from_numpy(line(n, 6) * 0.9).cuda()
+    uT = hw.weno_solve(u0, prob, dt, steps)
+    loss = 0.5 * ((uT - tg) ** 2).sum()
+    loss.backward()
+    J, g = hw.adjoint(prob, checkpoint_every=0).gradient(u0.detach(), tg, dt, steps)
+    assert abs(float(loss) - J[0]) <= 1e-13 * J[0]
+    assert torch.equal(u0.grad, g)
+    # batched lines with a weighted loss
+    u0b = torch.from_numpy(np.stack([line(n, 7), line(n, 8)])).cuda().requires_grad_(True)
+    w = torch.linspace(0.5, 2.0, n, dtype=torch.float64, device="cuda")
+    (hw.weno_solve(u0b, prob, dt, steps) * w).sum().backward()
+    g1 = hw.adjoint(prob).vjp(u0b.detach()[1].contiguous(), w.contiguous(), dt, steps)
+    assert torch.equal(u0b.grad[1], g1)
