@@ -415,7 +415,7 @@ int hrw_adjoint_create(const hrw_problem* p, int nseg, int checkpoint_every, hrw
   if (p->kind != HRW_PROBLEM_FV1D) return adj_fail(HRW_EINVAL, "hrw_adjoint: FV1D problems only.");
   if (p->flux != HRW_FLUX_LAX_FRIEDRICHS)
     return adj_fail(HRW_EINVAL, "hrw_adjoint: the global Lax-Friedrichs flux with fixed alpha only.");
-  if (p->width[0]) return adj_fail(HRW_EINVAL, "hrw_adjoint: uniform grids only.");
+  if (p->width[0] || p->xedges[0]) return adj_fail(HRW_EINVAL, "hrw_adjoint: uniform grids only.");
   if (p->ncells[0] <= 0) return adj_fail(HRW_EINVAL, "Invalid input 'ncells'. Valid range: ncells > 0.");
   if (p->k < 1 || p->k > 3) return adj_fail(HRW_EINVAL, "Invalid input 'k'. Valid range: 1 <= k <= 3.");
   if (!(p->eps > 2.220446049250313e-16))

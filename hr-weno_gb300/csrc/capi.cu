@@ -50,6 +50,8 @@ constexpr int64_t kMaxSteps = int64_t(1) << 40;
 struct DevLine {
   double* width = nullptr;  // device copy of the user's widths (STRICT)
   double* rws = nullptr;    // device fscale/width (FAST)
+  double* xe = nullptr;     // non-uniform line: edges(0:nc)
+  double* cnu = nullptr;    // non-uniform line: weno coefficients
 };
 
 // Validate the problem descriptor against the same rules the reference's constructors apply,
@@ -73,6 +75,14 @@ int validate_problem(const hrw_problem* p, int neq) {
       return fail(HRW_EINVAL, "Invalid input 'fn'.");
     if (p->bc[d] < HRW_BC_COPY || p->bc[d] > HRW_BC_ZERO_INFLOW)
       return fail(HRW_EINVAL, "Invalid input 'bc'.");
+    if (p->xedges[d]) {
+      if (p->kind != HRW_PROBLEM_FV1D)
+        return fail(HRW_EINVAL, "Invalid input 'xedges': non-uniform lines are supported for FV1D.");
+      if (p->width[d]) return fail(HRW_EINVAL, "Invalid input: give either 'xedges' or 'width'.");
+      for (int i = 0; i < p->ncells[d]; ++i)
+        if (!(p->xedges[d][i + 1] > p->xedges[d][i]))
+          return fail(HRW_EINVAL, "Invalid input 'xedges': edges must increase.");
+    }
     cells *= p->ncells[d];
   }
   if (p->k < 1 || p->k > 3) return fail(HRW_EINVAL, "Invalid input 'k'. Valid range: 1 <= k <= 3.");
@@ -277,6 +287,8 @@ static int ode_create(const hrw_problem* p, int neq, int order, int method, int 
   int rc = validate_problem(p, neq);
   if (rc != HRW_OK) return rc;
   if (dtype == HRW_F32C) {
+    if (p->xedges[0] || p->xedges[1])
+      return fail(HRW_EINVAL, "Invalid input 'xedges': non-uniform lines are supported for HRW_F64.");
     if (p->kind != HRW_PROBLEM_FV1D && p->kind != HRW_PROBLEM_FV2D)
       return fail(HRW_EINVAL, "Invalid input 'dtype': HRW_F32C supports FV1D and FV2D problems.");
     if (!(p->eps > 1.1920928955078125e-07))  // epsilon(1.0_real32), src/hrweno_weno.f90:92
@@ -289,6 +301,7 @@ static int ode_create(const hrw_problem* p, int neq, int order, int method, int 
   o->method = method;
   o->dtype = dtype;
   o->prob.width[0] = o->prob.width[1] = nullptr;  // host pointers are not kept
+  o->prob.xedges[0] = o->prob.xedges[1] = nullptr;
   o->prob.rates = nullptr;
   auto cleanup = [&](cudaError_t e) {
     hrw_ode_destroy(o);
@@ -339,6 +352,29 @@ static int ode_create(const hrw_problem* p, int neq, int order, int method, int 
         L.width = o->line[d].width;
         L.rws = strict ? nullptr : o->line[d].rws;
         if (strict) L.rws = nullptr;
+      }
+      if (p->xedges[d]) {  // weno(ncells, k, eps, xedges): cnu on the device, widths, edges
+        const size_t nb = sizeof(double) * (size_t)L.nc;
+        std::vector<double> w(L.nc), rws(L.nc);
+        for (int i = 0; i < L.nc; ++i) {
+          w[i] = p->xedges[d][i + 1] - p->xedges[d][i];
+          rws[i] = fs / w[i];
+        }
+        DevLine& D = o->line[d];
+        if ((e = cudaMalloc(&D.width, nb)) != cudaSuccess) return cleanup(e);
+        if ((e = cudaMalloc(&D.rws, nb)) != cudaSuccess) return cleanup(e);
+        if ((e = cudaMalloc(&D.xe, nb + sizeof(double))) != cudaSuccess) return cleanup(e);
+        if ((e = cudaMalloc(&D.cnu, nb * (size_t)p->k * (p->k + 1))) != cudaSuccess) return cleanup(e);
+        if ((e = cudaMemcpy(D.width, w.data(), nb, cudaMemcpyHostToDevice)) != cudaSuccess) return cleanup(e);
+        if ((e = cudaMemcpy(D.rws, rws.data(), nb, cudaMemcpyHostToDevice)) != cudaSuccess) return cleanup(e);
+        if ((e = cudaMemcpy(D.xe, p->xedges[d], nb + sizeof(double), cudaMemcpyHostToDevice)) != cudaSuccess)
+          return cleanup(e);
+        if ((e = launch_calc_cnu(D.xe, D.cnu, L.nc, p->k, o->own)) != cudaSuccess) return cleanup(e);
+        if ((e = cudaStreamSynchronize(o->own)) != cudaSuccess) return cleanup(e);
+        L.width = D.width;
+        L.rws = D.rws;
+        L.xe = D.xe;
+        b.cnu = D.cnu;
       }
     }
     b.ld = p->ncells[0];
@@ -439,6 +475,8 @@ int hrw_ode_destroy(hrw_ode* o) {
   for (int d = 0; d < 2; ++d) {
     if (o->line[d].width) cudaFree(o->line[d].width);
     if (o->line[d].rws) cudaFree(o->line[d].rws);
+    if (o->line[d].xe) cudaFree(o->line[d].xe);
+    if (o->line[d].cnu) cudaFree(o->line[d].cnu);
   }
   double* bufs[] = {o->rates, o->u, o->w1, o->w2};
   for (double* p : bufs)
@@ -472,7 +510,9 @@ static cudaError_t run_stage(hrw_ode* o, int stage, const double* v, const doubl
   const bool strict = o->prob.numerics == HRW_NUMERICS_STRICT;
   switch (o->prob.kind) {
     case HRW_PROBLEM_LINEAR_ODE: return launch_stage_linear(o->rates, a, o->neq, stage, strict, o->stream);
-    case HRW_PROBLEM_FV1D: return launch_stage1d(a, o->prob.k, stage, strict, o->stream);
+    case HRW_PROBLEM_FV1D:
+      if (a.cnu) return launch_stage1d_nu(a, o->prob.k, stage, strict, o->stream);
+      return launch_stage1d(a, o->prob.k, stage, strict, o->stream);
     default: return launch_stage2d(a, o->prob.k, stage, strict, o->stream);
   }
 }

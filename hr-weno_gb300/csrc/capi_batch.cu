@@ -193,7 +193,7 @@ int hrw_batch_create(const hrw_problem* probs, int nprob, int order, int dtype, 
     };
     if (p.kind != HRW_PROBLEM_FV1D) return bad("Invalid input 'kind': batches hold FV1D problems.");
     if (p.ncells[0] <= 0) return bad("Invalid input 'ncells'. Valid range: ncells > 0.");
-    if (p.width[0]) return bad("Invalid input 'width': batches hold uniform grids.");
+    if (p.width[0] || p.xedges[0]) return bad("Invalid input 'width': batches hold uniform grids.");
     if (p.k < 1 || p.k > 3) return bad("Invalid input 'k'. Valid range: 1 <= k <= 3.");
     if (!(p.eps > 2.220446049250313e-16)) return bad("Invalid input 'eps'. Valid range: eps > epsilon.");
     if (p.flux != HRW_FLUX_LAX_FRIEDRICHS && p.flux != HRW_FLUX_GODUNOV) return bad("Invalid input 'flux'.");

@@ -31,6 +31,7 @@ struct LineArgs {
   const double* width;
   const double* rws;
   double rws0;
+  const double* xe;  // non-uniform line: edges(0:nc) (x of interface e = xe[e]); null: uniform
 };
 
 struct StageArgs {
@@ -46,6 +47,7 @@ struct StageArgs {
   LineArgs L2;
   int64_t ld;         // row stride (nc1) of the 2D layout
   int upwind;         // Godunov flux of g(x) u with g > 0 everywhere: F = g vm (2D kernel)
+  const double* cnu;  // non-uniform 1D line: weno coefficients cnu(0:k-1,-1:k-1,1:nc)
 };
 
 // ---- compensated FP32 form (hrw_f32c.cuh, stage1d_f32c.cu) ---------------------------------
@@ -112,6 +114,8 @@ bool positive_velocity(const LineArgs& L);
 cudaError_t launch_stage1d(const StageArgs& a, int k, int stage, bool strict, cudaStream_t s);
 // 2D fused stage (x1 fastest), dimension by dimension.
 cudaError_t launch_stage2d(const StageArgs& a, int k, int stage, bool strict, cudaStream_t s);
+// 1D fused stage on a non-uniform line (a.cnu, a.L.xe, a.L.width / a.L.rws set).
+cudaError_t launch_stage1d_nu(const StageArgs& a, int k, int stage, bool strict, cudaStream_t s);
 // Linear ODE u' = a u stage (test problem of the reference's integrator tests).
 cudaError_t launch_stage_linear(const double* rates, const StageArgs& a, int64_t n, int stage,
                                 bool strict, cudaStream_t s);

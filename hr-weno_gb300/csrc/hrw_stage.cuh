@@ -19,7 +19,8 @@ namespace hrw {
 // Numerical fluxes.  e = edge index of the interface (x = xmin + rx*e, grid1%right).
 // --------------------------------------------------------------------------------------------
 __device__ __forceinline__ double g_fast(const LineArgs& L, int64_t e) {
-  return L.b != 0.0 ? fma(L.b, fma(L.rx, (double)e, L.xmin), L.a) : L.a;
+  if (L.b == 0.0) return L.a;
+  return fma(L.b, L.xe ? L.xe[e] : fma(L.rx, (double)e, L.xmin), L.a);
 }
 
 // FAST: returns F / fast_flux_scale(flux, fn).
@@ -45,7 +46,7 @@ __device__ __forceinline__ double phys_fast(const LineArgs& L, double v, int64_t
 
 // STRICT: reference order (src/hrweno_fluxes.f90:43,67-74; example1...f90:111-122).
 __device__ __forceinline__ double g_strict(const LineArgs& L, int64_t e) {
-  const double x = __dadd_rn(L.xmin, __dmul_rn(L.rx, (double)e));
+  const double x = L.xe ? L.xe[e] : __dadd_rn(L.xmin, __dmul_rn(L.rx, (double)e));
   return __dadd_rn(L.a, __dmul_rn(L.b, x));
 }
 __device__ __forceinline__ double phys_strict(const LineArgs& L, double v, int64_t e) {

@@ -153,135 +153,10 @@ __global__ void recon_nonuniform_kernel(const double* __restrict__ v, const doub
     p[q] = v[g];
   }
   const double* ci = cnu + (int64_t)K * (K + 1) * i;  // ci(j, r) at [j + K*(r+1)]
-  const double* c0 = p + (K - 1);                      // v(i)
-  double vrr[K], vlr[K], beta[K];
-#pragma unroll
-  for (int r = 0; r < K; ++r) {
-    double sr = 0.0, sl = 0.0;
-#pragma unroll
-    for (int j = 0; j < K; ++j) {
-      if constexpr (STRICT) {
-        sr = __dadd_rn(sr, __dmul_rn(ci[j + K * (r + 1)], c0[j - r]));
-        sl = __dadd_rn(sl, __dmul_rn(ci[j + K * r], c0[j - r]));
-      } else {
-        sr = fma(ci[j + K * (r + 1)], c0[j - r], sr);
-        sl = fma(ci[j + K * r], c0[j - r], sl);
-      }
-    }
-    vrr[r] = sr;
-    vlr[r] = sl;
-  }
-  if constexpr (STRICT) {
-    // reuse the uniform strict path for beta and weights by re-deriving from the same p
-    // (beta does not depend on the grid, src/hrweno_weno.f90:183-204)
-    if constexpr (K == 1) {
-      beta[0] = 0.0;
-    } else if constexpr (K == 2) {
-      double a = __dsub_rn(c0[1], c0[0]), b = __dsub_rn(c0[0], c0[-1]);
-      beta[0] = __dmul_rn(a, a);
-      beta[1] = __dmul_rn(b, b);
-    } else {
-      const double c13 = 13.0 / 12, c14 = 1.0 / 4;
-      double a, b;
-      a = __dadd_rn(__dsub_rn(c0[0], __dmul_rn(2.0, c0[1])), c0[2]);
-      b = __dadd_rn(__dsub_rn(__dmul_rn(3.0, c0[0]), __dmul_rn(4.0, c0[1])), c0[2]);
-      beta[0] = __dadd_rn(__dmul_rn(c13, __dmul_rn(a, a)), __dmul_rn(c14, __dmul_rn(b, b)));
-      a = __dadd_rn(__dsub_rn(c0[-1], __dmul_rn(2.0, c0[0])), c0[1]);
-      b = __dsub_rn(c0[-1], c0[1]);
-      beta[1] = __dadd_rn(__dmul_rn(c13, __dmul_rn(a, a)), __dmul_rn(c14, __dmul_rn(b, b)));
-      a = __dadd_rn(__dsub_rn(c0[-2], __dmul_rn(2.0, c0[-1])), c0[0]);
-      b = __dadd_rn(__dsub_rn(c0[-2], __dmul_rn(4.0, c0[-1])), __dmul_rn(3.0, c0[0]));
-      beta[2] = __dadd_rn(__dmul_rn(c13, __dmul_rn(a, a)), __dmul_rn(c14, __dmul_rn(b, b)));
-    }
-    double alfa[K], alfat[K], sa = 0.0, sat = 0.0;
-#pragma unroll
-    for (int r = 0; r < K; ++r) {
-      const double e = __dadd_rn(eps, beta[r]);
-      const double e2 = __dmul_rn(e, e);
-      alfa[r] = __ddiv_rn(Tab<K>::d(r), e2);
-      alfat[r] = __ddiv_rn(Tab<K>::d(K - 1 - r), e2);
-    }
-#pragma unroll
-    for (int r = 0; r < K; ++r) { sa = __dadd_rn(sa, alfa[r]); sat = __dadd_rn(sat, alfat[r]); }
-    double ar = 0.0, al = 0.0;
-#pragma unroll
-    for (int r = 0; r < K; ++r) {
-      ar = __dadd_rn(ar, __dmul_rn(__ddiv_rn(alfa[r], sa), vrr[r]));
-      al = __dadd_rn(al, __dmul_rn(__ddiv_rn(alfat[r], sat), vlr[r]));
-    }
-    vr[i] = ar;
-    vl[i] = al;
-  } else {
-    if constexpr (K == 1) {
-      vr[i] = vrr[0];
-      vl[i] = vlr[0];
-    } else {
-      if constexpr (K == 2) {
-        const double a = c0[1] - c0[0], b = c0[0] - c0[-1];
-        beta[0] = a * a;
-        beta[1] = b * b;
-      } else {
-        const double c13 = 13.0 / 12;
-        double a, b;
-        a = fma(-2.0, c0[1], c0[0] + c0[2]);
-        b = fma(3.0, c0[0], fma(-4.0, c0[1], c0[2]));
-        beta[0] = fma(c13 * a, a, 0.25 * (b * b));
-        a = fma(-2.0, c0[0], c0[-1] + c0[1]);
-        b = c0[-1] - c0[1];
-        beta[1] = fma(c13 * a, a, 0.25 * (b * b));
-        a = fma(-2.0, c0[-1], c0[-2] + c0[0]);
-        b = fma(3.0, c0[0], fma(-4.0, c0[-1], c0[-2]));
-        beta[2] = fma(c13 * a, a, 0.25 * (b * b));
-      }
-      // product-form weights: w_r = d_r P_r / sum d_q P_q, P_r = prod_{q != r} s_q
-      double sq[K], P[K];
-      int hmax = 0;
-#pragma unroll
-      for (int r = 0; r < K; ++r) {
-        const double e = eps + beta[r];
-        sq[r] = e * e;
-        hmax = max(hmax, hiword(sq[r]));
-      }
-      if (hmax < FastGuard<K>::hi_max) {
-#pragma unroll
-        for (int r = 0; r < K; ++r) {
-          double pr = 1.0;
-#pragma unroll
-          for (int q = 0; q < K; ++q)
-            if (q != r) pr *= sq[q];
-          P[r] = pr;
-        }
-        double den = 0.0, dent = 0.0, num = 0.0, numt = 0.0;
-#pragma unroll
-        for (int r = 0; r < K; ++r) {
-          const double qr = Tab<K>::d(r) * P[r], qt = Tab<K>::d(K - 1 - r) * P[r];
-          den += qr;
-          dent += qt;
-          num = fma(qr, vrr[r], num);
-          numt = fma(qt, vlr[r], numt);
-        }
-        const double R = rcp_fast(den * dent);
-        vr[i] = num * (dent * R);
-        vl[i] = numt * (den * R);
-      } else {
-        double alfa[K], alfat[K], sa = 0.0, sat = 0.0, ar = 0.0, al = 0.0;
-#pragma unroll
-        for (int r = 0; r < K; ++r) {
-          alfa[r] = Tab<K>::d(r) / sq[r];
-          alfat[r] = Tab<K>::d(K - 1 - r) / sq[r];
-          sa += alfa[r];
-          sat += alfat[r];
-        }
-#pragma unroll
-        for (int r = 0; r < K; ++r) {
-          ar += alfa[r] / sa * vrr[r];
-          al += alfat[r] / sat * vlr[r];
-        }
-        vr[i] = ar;
-        vl[i] = al;
-      }
-    }
-  }
+  double l, r;
+  recon_nu<K, STRICT>(p + (K - 1), ci, eps, l, r);
+  vl[i] = l;
+  vr[i] = r;
 }
 
 template <bool STRICT>

@@ -53,7 +53,7 @@ extern "C" int hrw_rktvd3_steps_noalloc(const hrw_problem* p, double* u, double 
   if (!p || !u) return set_error(HRW_EINVAL, "Invalid input: null pointer.");
   if (p->kind != HRW_PROBLEM_FV1D)
     return set_error(HRW_EINVAL, "hrw_rktvd3_steps_noalloc: only HRW_PROBLEM_FV1D problems.");
-  if (p->width[0])
+  if (p->width[0] || p->xedges[0])
     return set_error(HRW_EINVAL, "hrw_rktvd3_steps_noalloc: only uniform grids (width[0] = NULL).");
   const int64_t nc = p->ncells[0];
   if (nc <= 0) return set_error(HRW_EINVAL, "Invalid input 'ncells'. Valid range: ncells > 0.");

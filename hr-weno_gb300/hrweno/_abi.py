@@ -40,6 +40,7 @@ class HrwProblem(C.Structure):
         ("width", C.POINTER(C.c_double) * 2),
         ("rates", C.POINTER(C.c_double)),
         ("numerics", C.c_int32),
+        ("xedges", C.POINTER(C.c_double) * 2),
     ]
 
 

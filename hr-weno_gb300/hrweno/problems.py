@@ -39,6 +39,7 @@ class Problem:
     width: tuple = (None, None)
     rates: object = None
     numerics: str = "fast"
+    xedges: tuple = (None, None)
     _keep: list = field(default_factory=list, repr=False)
 
     @property
@@ -75,6 +76,11 @@ class Problem:
                 w = np.ascontiguousarray(w, dtype=np.float64)
                 self._keep.append(w)
                 p.width[d] = w.ctypes.data_as(C.POINTER(C.c_double))
+            xe = self.xedges[d] if self.xedges is not None else None
+            if xe is not None:
+                xe = np.ascontiguousarray(xe, dtype=np.float64)
+                self._keep.append(xe)
+                p.xedges[d] = xe.ctypes.data_as(C.POINTER(C.c_double))
         if self.rates is not None:
             r = np.ascontiguousarray(self.rates, dtype=np.float64)
             self._keep.append(r)

@@ -222,7 +222,9 @@ struct Line {  // one dimension of the grid: grid1%linear (src/hrweno_grids.f90:
   int nc = 0;
   T xmin = 0, rx = 0;
   std::vector<T> width;  // per-cell width; empty: uniform rx
-  T right(int i) const { return xmin + rx * (T)i; }  // edges(i) = xmin + rx*i
+  std::vector<T> edges;  // non-uniform line: edges(0:nc); empty: uniform
+  std::vector<T> cnu;    // weno coefficients of the non-uniform line (weno_calc_cnu)
+  T right(int i) const { return edges.empty() ? xmin + rx * (T)i : edges[i]; }  // edges(i)
   T w(int i) const { return width.empty() ? rx : width[i - 1]; }
 };
 
@@ -232,7 +234,7 @@ template <class T>
 static void line_fluxes(const hrw_problem& p, int dim, const Line<T>& L, T eps, T t,
                         const T* v, T* vl, T* vr, T* F) {
   const int nc = L.nc;
-  weno_reconstruct<T>(nc, p.k, eps, nullptr, v, vl, vr);
+  weno_reconstruct<T>(nc, p.k, eps, L.cnu.empty() ? nullptr : L.cnu.data(), v, vl, vr);
   ORC_PARFOR
   for (int i = 1; i <= nc - 1; ++i) F[i] = numflux<T>(p, dim, vr[i - 1], vl[i], L.right(i), t);
   switch (p.bc[dim]) {
@@ -259,6 +261,7 @@ struct Problem {
 
   explicit Problem(const hrw_problem& pp, int n) : p(pp), neq(n) {
     p.width[0] = p.width[1] = nullptr;
+    p.xedges[0] = p.xedges[1] = nullptr;
     p.rates = nullptr;
     int nd = pp.kind == HRW_PROBLEM_FV2D ? 2 : (pp.kind == HRW_PROBLEM_FV1D ? 1 : 0);
     for (int d = 0; d < nd; ++d) {
@@ -269,6 +272,14 @@ struct Problem {
       if (pp.width[d]) {
         L.width.resize(L.nc);
         for (int i = 0; i < L.nc; ++i) L.width[i] = (T)pp.width[d][i];
+      }
+      if (pp.xedges[d]) {  // weno(ncells, k, eps, xedges) and width(i) = edges(i) - edges(i-1)
+        L.edges.resize(L.nc + 1);
+        for (int i = 0; i <= L.nc; ++i) L.edges[i] = (T)pp.xedges[d][i];
+        L.width.resize(L.nc);
+        for (int i = 0; i < L.nc; ++i) L.width[i] = L.edges[i + 1] - L.edges[i];
+        L.cnu.resize((size_t)pp.k * (pp.k + 1) * L.nc);
+        weno_calc_cnu<T>(L.nc, pp.k, L.edges.data(), L.cnu.data());
       }
     }
     if (pp.kind == HRW_PROBLEM_LINEAR_ODE && pp.rates) {

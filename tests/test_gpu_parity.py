@@ -298,3 +298,58 @@ def test_integrate_already_done_is_noop(hw):
     u = u0.copy()
     t = g.integrate(u, 1.0, 0.5, 1e-2)  # (t - tout) * sign(dt) > 0: return at once (:127)
     assert t == 1.0 and np.array_equal(u, u0) and g.fevals == 0 and g.istate == 1
+
+
+def stretched_edges(nc, kind, seed=0):
+    if kind == "cubic":  # test/test_hrweno.f90:123-128 stretches edges as (i/nc)^3
+        return -1.0 + 2.0 * (np.arange(nc + 1) / nc) ** 3
+    rng = np.random.default_rng(seed)
+    return np.concatenate([[-1.0], -1.0 + np.cumsum(rng.uniform(0.5, 1.5, nc)) * (2.0 / nc)])
+
+
+@pytest.mark.parametrize("k", [1, 2, 3])
+@pytest.mark.parametrize("nc", [1, 2, 7, 300, 1000])
+@pytest.mark.parametrize("kind", ["cubic", "random"])
+def test_rhs_1d_nonuniform(hw, orc, k, nc, kind):
+    """weno(ncells, k, eps, xedges) inside the fused stage: cnu coefficients, true widths and
+    interface coordinates (src/hrweno_weno.f90:100-104,177; example1...f90:107)."""
+    xe = stretched_edges(nc, kind, nc)
+    v = rand_line(nc, 9, "smooth") + 1.0
+    cases = [dict(flux="lax_friedrichs", fn="burgers", bc="copy", b=0.0),
+             dict(flux="godunov", fn="burgers", bc="zero", b=0.0),
+             dict(flux="godunov", fn="linear", bc="zero_inflow", b=0.4),
+             dict(flux="lax_friedrichs", fn="linear", bc="copy", b=-0.3)]
+    for c in cases:
+        for numerics in ("strict", "fast"):
+            prob = hw.Problem(kind="fv1d", ncells=(nc, 1), k=k, flux=c["flux"],
+                              fn=(c["fn"], c["fn"]), coef_a=(0.8, 0), coef_b=(c["b"], 0),
+                              alpha=(2.5, 2.5), bc=(c["bc"], c["bc"]), xedges=(xe, None),
+                              numerics=numerics)
+            ref = orc.rhs(prob, v)
+            got = device_rhs(hw, prob, v)
+            if numerics == "strict":
+                assert np.array_equal(got, ref), (c, k, nc, kind)
+            else:
+                assert nrel(got, ref) <= 10 * TOL_ONE, (c, k, nc, kind)
+
+
+@pytest.mark.parametrize("numerics", ["strict", "fast"])
+@pytest.mark.parametrize("order", [2, 3])
+def test_rktvd_nonuniform(hw, orc, numerics, order):
+    nc = 700
+    xe = stretched_edges(nc, "random", 3)
+    xc = 0.5 * (xe[1:] + xe[:-1])
+    u0 = 0.5 + np.exp(-30 * xc ** 2)
+    prob = hw.Problem(kind="fv1d", ncells=(nc, 1), k=3, flux="lax_friedrichs",
+                      fn=("burgers", "burgers"), alpha=(1.5, 1.5), bc=("copy", "copy"),
+                      xedges=(xe, None), numerics=numerics)
+    dt = 0.3 * np.min(np.diff(xe)) / 1.5
+    g, o = hw.rktvd(prob, nc, order), orc.ODE(prob, nc, 0, order)
+    ug, uo = u0.copy(), u0.copy()
+    tg = g.integrate(ug, 0.0, 150.5 * dt, dt)
+    to = o.integrate(uo, 0.0, 150.5 * dt, dt)
+    assert tg == to
+    if numerics == "strict":
+        assert np.array_equal(ug, uo)
+    else:
+        assert nrel(ug, uo) <= TOL_INT

@@ -98,3 +98,17 @@ def test_tables_match_reference_literals():
     c3 = np.array(GOLDEN["c_tables"]["3"])
     assert np.allclose(c3[0], [11 / 6, -7 / 6, 1 / 3]) and np.allclose(c3[3], [1 / 3, -7 / 6, 11 / 6])
     assert GOLDEN["d_tables"]["3"] == [0.3, 0.6, 0.1]
+
+
+def test_fv_nonuniform_uniform_edges_match_uniform_line(orc):
+    """A non-uniform line whose edges are uniform reproduces the uniform line to rounding:
+    cnu equals the c tables (test/test_hrweno.f90:69-112) and the widths equal dx."""
+    from hrweno.problems import burgers_1d
+    nc = 64
+    x = np.linspace(-1, 1, nc)
+    v = 0.5 + np.exp(-10 * x ** 2)
+    p_u = burgers_1d(nc, -1.0, 1.0, k=3, alpha=1.5)
+    p_n = burgers_1d(nc, -1.0, 1.0, k=3, alpha=1.5)
+    p_n.xedges = (-1.0 + 2.0 * np.arange(nc + 1) / nc, None)
+    a, b = orc.rhs(p_u, v), orc.rhs(p_n, v)
+    assert np.max(np.abs(a - b)) <= 1e-11 * np.max(np.abs(a))
