@@ -120,6 +120,35 @@ __device__ __forceinline__ void recon_diff(const float* d, float eps, float& rl,
   }
 }
 
+// K = 3 reconstruction of one cell with the 13/12 (second difference)^2 terms of its three
+// indicators precomputed (neighbouring cells share them): t0, t1, t2 for beta0, beta1, beta2.
+// Same weights and candidates as recon_diff<3>.
+__device__ __forceinline__ void recon_diff3_shared(const float* d, float t0, float t1, float t2,
+                                                   float eps, float& rl, float& rr) {
+  const float dmm = d[0], dm = d[1], d0 = d[2], d1 = d[3];
+  const float B0 = fmaf(-3.f, d0, d1), B1 = dm + d0, B2 = fmaf(3.f, dm, -dmm);
+  const float e0 = eps + fmaf(0.25f * B0, B0, t0);
+  const float e1 = eps + fmaf(0.25f * B1, B1, t1);
+  const float e2 = eps + fmaf(0.25f * B2, B2, t2);
+  const float s0 = e0 * e0, s1 = e1 * e1, s2 = e2 * e2;
+  const float R0 = fmaf(4.f, d0, -d1), R1 = fmaf(2.f, d0, dm), R2 = fmaf(5.f, dm, -2.f * dmm);
+  const float L0 = fmaf(2.f, d1, -5.f * d0), L1 = -fmaf(2.f, dm, d0), L2 = fmaf(-4.f, dm, dmm);
+  if (fmaxf(s0, fmaxf(s1, s2)) < 1e18f) {
+    const float P0 = s1 * s2, P1 = s0 * s2, P2 = s0 * s1;
+    const float den = fmaf(3.f, P0, fmaf(6.f, P1, P2));
+    const float dent = fmaf(3.f, P2, fmaf(6.f, P1, P0));
+    const float num = fmaf(3.f * P0, R0, fmaf(6.f * P1, R1, P2 * R2));
+    const float numt = fmaf(P0, L0, fmaf(6.f * P1, L1, 3.f * P2 * L2));
+    rr = (num * rcpf(den)) * (1.f / 6.f);
+    rl = (numt * rcpf(dent)) * (1.f / 6.f);
+  } else {
+    const float a0 = 0.3f / s0, a1 = 0.6f / s1, a2 = 0.1f / s2;
+    const float u0 = 0.1f / s0, u1 = 0.6f / s1, u2 = 0.3f / s2;
+    rr = (a0 * R0 + a1 * R1 + a2 * R2) / (6.f * (a0 + a1 + a2));
+    rl = (u0 * L0 + u1 * L1 + u2 * L2) / (6.f * (u0 + u1 + u2));
+  }
+}
+
 // ---------------------------------------------------------------------------------------------
 // G = F(v + a, v + b) - f_base at interface e, for a cell of value v whose left-hand side
 // state at the interface is v + a and right-hand side state v + b.  f_base is f(v) for
@@ -127,18 +156,31 @@ __device__ __forceinline__ void recon_diff(const float* d, float eps, float& rl,
 // the two interface fluxes that cancels in the cell's flux difference.
 //   Lax-Friedrichs (src/hrweno_fluxes.f90:43), Godunov (:67-74).
 // ---------------------------------------------------------------------------------------------
-__device__ __forceinline__ float flux_g(const LineF& L, float v, float a, float b, float g) {
-  if (L.fn == HRW_FN_BURGERS) {
-    if (L.flux == HRW_FLUX_LAX_FRIEDRICHS)  // 4F - 2v^2 = a(2v + a + 2 alpha) + b(2v + b - 2 alpha)
-      return 0.25f * fmaf(a, 2.f * v + a + 2.f * L.alpha, b * (2.f * v + b - 2.f * L.alpha));
-    // 2F - v^2 = a(2v + a) or b(2v + b); min if vm <= vp (a <= b), else max
+// Flux kind as a compile-time constant: FK = 2 * (fn == LINEAR) + (flux == GODUNOV).
+template <int FK>
+__device__ __forceinline__ float flux_g_t(const LineF& L, float v, float a, float b, float g) {
+  if constexpr (FK == 0) {  // Burgers, LF: 4F - 2v^2 = a(2v + a + 2 alpha) + b(2v + b - 2 alpha)
+    return 0.25f * fmaf(a, 2.f * v + a + 2.f * L.alpha, b * (2.f * v + b - 2.f * L.alpha));
+  } else if constexpr (FK == 1) {  // Burgers, Godunov: 2F - v^2 = a(2v + a) or b(2v + b)
     const float fa = a * (2.f * v + a), fb = b * (2.f * v + b);
-    return 0.5f * (a <= b ? fminf(fa, fb) : fmaxf(fa, fb));
+    return 0.5f * (a <= b ? fminf(fa, fb) : fmaxf(fa, fb));  // min if vm <= vp (a <= b)
+  } else if constexpr (FK == 2) {  // linear f = g u, LF: F - g v = ((g + alpha) a + (g - alpha) b)/2
+    return 0.5f * fmaf(g + L.alpha, a, (g - L.alpha) * b);
+  } else {  // linear, Godunov: g a or g b
+    const float fa = g * a, fb = g * b;
+    return a <= b ? fminf(fa, fb) : fmaxf(fa, fb);
   }
-  // linear f = g u: F - g v = ((g + alpha) a + (g - alpha) b)/2 (LF) or g a / g b (Godunov)
-  if (L.flux == HRW_FLUX_LAX_FRIEDRICHS) return 0.5f * fmaf(g + L.alpha, a, (g - L.alpha) * b);
-  const float fa = g * a, fb = g * b;
-  return a <= b ? fminf(fa, fb) : fmaxf(fa, fb);
+}
+__device__ __forceinline__ int flux_kind(const LineF& L) {
+  return 2 * (L.fn != HRW_FN_BURGERS) + (L.flux != HRW_FLUX_LAX_FRIEDRICHS);
+}
+__device__ __forceinline__ float flux_g(const LineF& L, float v, float a, float b, float g) {
+  switch (flux_kind(L)) {
+    case 0: return flux_g_t<0>(L, v, a, b, g);
+    case 1: return flux_g_t<1>(L, v, a, b, g);
+    case 2: return flux_g_t<2>(L, v, a, b, g);
+    default: return flux_g_t<3>(L, v, a, b, g);
+  }
 }
 // physical flux minus the same base, for the free-outflow boundary: f(v + a) - f_base
 __device__ __forceinline__ float phys_g(const LineF& L, float v, float a, float g) {
@@ -177,7 +219,22 @@ __device__ __forceinline__ float flux_diff_f32c(const LineF& L, int64_t j, float
     if (j == L.nc - 1) FR = L.bc == HRW_BC_ZERO ? 0.f : fbR + phys_g(L, v, rr_j, gR);
     return FR - FL;
   }
-  return (GR - GL) + extra;
+  return __fadd_rn(GR - GL, extra);  // never contracted with gstep * v: one rounding order
+}
+
+// flux_diff_f32c of a cell that touches no boundary, flux kind known at compile time (the same
+// operations as flux_diff_f32c's interior branch, so both give the same bits)
+template <int FK>
+__device__ __forceinline__ float flux_diff_interior(const LineF& L, int j, float v, float rr_m,
+                                                    float d_m, float rl_j, float rr_j, float d_j,
+                                                    float rl_p) {
+  constexpr bool lin = FK >= 2;
+  const float gL = lin ? g_at(L, j) : 0.f;
+  const float gR = lin ? g_at(L, j + 1) : 0.f;
+  const float GL = flux_g_t<FK>(L, v, rr_m - d_m, rl_j, gL);
+  const float GR = flux_g_t<FK>(L, v, rr_j, d_j + rl_p, gR);
+  const float extra = lin ? L.gstep * v : 0.f;
+  return __fadd_rn(GR - GL, extra);
 }
 
 // Stage update of one cell in increment form.  h, l: the state u = h + l; dv: the stored
@@ -219,8 +276,7 @@ __device__ __forceinline__ void f32c_update(const F32CArgs& a, int64_t j, float 
 // Own cells are read with float4 loads and written with float4 stores when the thread's
 // cells are inside the line (the float buffers are padded to 16-byte aligned slices).
 template <int C>
-__device__ __forceinline__ void load_cells(const float* __restrict__ p, int64_t j0, int64_t nc,
-                                           float* out) {
+__device__ __forceinline__ void load_cells(const float* __restrict__ p, int j0, int nc, float* out) {
   if (j0 + C <= nc) {
 #pragma unroll
     for (int c = 0; c < C; c += 4) {
@@ -234,8 +290,7 @@ __device__ __forceinline__ void load_cells(const float* __restrict__ p, int64_t 
 }
 
 template <int C>
-__device__ __forceinline__ void store_cells(float* __restrict__ p, int64_t j0, int64_t nc,
-                                            const float* v) {
+__device__ __forceinline__ void store_cells(float* __restrict__ p, int j0, int nc, const float* v) {
   if (j0 + C <= nc) {
 #pragma unroll
     for (int c = 0; c < C; c += 4)
@@ -248,12 +303,14 @@ __device__ __forceinline__ void store_cells(float* __restrict__ p, int64_t j0, i
 }
 
 // One warp-pass: lane `lane` handles cells j0 .. j0 + C - 1 of the line a.L (all 32 lanes of
-// the warp call it with consecutive j0 = base + lane * C).
-template <int K, int ST, int C>
-__device__ __forceinline__ void f32c_pass(const F32CArgs& a, int64_t j0, int lane) {
+// the warp call it with consecutive j0 = base + lane * C).  FK: the flux kind when known at
+// compile time, or -1.  Cell indices are 32-bit (lines of < 2^31 cells).
+template <int K, int ST, int C, int FK = -1>
+__device__ __forceinline__ void f32c_pass(const F32CArgs& a, int64_t j0l, int lane) {
   static_assert(C % 4 == 0 && C >= K, "float4 cells and a K-cell shuffle halo");
   const LineF& L = a.L;
-  const int64_t nc = L.nc;
+  const int nc = L.nc;
+  const int j0 = (int)j0l;
   constexpr unsigned FULL = 0xffffffffu;
 
   // ---- state window: w = cells j0 - K .. j0 + C + K - 1 -----------------------------------------
@@ -281,7 +338,7 @@ __device__ __forceinline__ void f32c_pass(const F32CArgs& a, int64_t j0, int lan
   if (lane == 0 || lane == 31) {  // the warp's halo, ghosts replicating v(1) and v(nc)
 #pragma unroll
     for (int q = 0; q < K; ++q) {
-      int64_t g = lane == 0 ? j0 - K + q : j0 + C + q;
+      int g = lane == 0 ? j0 - K + q : j0 + C + q;
       g = g < 0 ? 0 : (g >= nc ? nc - 1 : g);
       const float m = a.dv ? a.lo[g] + a.dv[g] : a.lo[g];
       if (lane == 0) wh[q] = a.hi[g], wm[q] = m;
@@ -294,31 +351,60 @@ __device__ __forceinline__ void f32c_pass(const F32CArgs& a, int64_t j0, int lan
 #pragma unroll
   for (int q = 0; q < C + 2 * K - 1; ++q) d[q] = (wh[q + 1] - wh[q]) + (wm[q + 1] - wm[q]);
   float rl[C], rr[C];
+  if constexpr (K == 3) {
+    // 13/12 (d_m - d_{m-1})^2 once per window position.  Cell c reads d[c+1 .. c+4]
+    // (d_{j-2} .. d_{j+1}): its beta0, beta1, beta2 take t[c+4], t[c+3], t[c+2]
+    float t[C + 4];
 #pragma unroll
-  for (int c = 0; c < C; ++c) recon_diff<K>(&d[c + 1], a.eps, rl[c], rr[c]);
+    for (int m = 2; m < C + 4; ++m) {
+      const float D = d[m] - d[m - 1];
+      t[m] = (13.f / 12.f) * D * D;
+    }
+#pragma unroll
+    for (int c = 0; c < C; ++c)
+      recon_diff3_shared(&d[c + 1], t[c + 4], t[c + 3], t[c + 2], a.eps, rl[c], rr[c]);
+  } else {
+#pragma unroll
+    for (int c = 0; c < C; ++c) recon_diff<K>(&d[c + 1], a.eps, rl[c], rr[c]);
+  }
   // the cells next to the thread's ends: from the neighbouring lanes, or (lanes 0 / 31)
   // reconstructed here: cell j0-1 uses d[0 .. 2K-3], cell j0+C uses d[C+1 .. C+2K-2]
   float ed[2 * K];
 #pragma unroll
   for (int q = 0; q < 2 * K - 2; ++q) ed[q] = lane == 31 ? d[C + 1 + q] : d[q];
   float el, er;
-  recon_diff<K>(ed, a.eps, el, er);
+  if constexpr (K == 3) {
+    float te[3];
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      const float D = ed[q + 1] - ed[q];
+      te[q] = (13.f / 12.f) * D * D;
+    }
+    recon_diff3_shared(ed, te[2], te[1], te[0], a.eps, el, er);
+  } else {
+    recon_diff<K>(ed, a.eps, el, er);
+  }
   const float rr_left = __shfl_up_sync(FULL, rr[C - 1], 1);
   const float rl_right = __shfl_down_sync(FULL, rl[0], 1);
   const float rr_m0 = lane == 0 ? er : rr_left;
   const float rl_pC = lane == 31 ? el : rl_right;
 
   // ---- flux differences and the stage update -------------------------------------------------------
+  const bool interior = j0 > 0 && j0 + C < nc;  // no boundary cell among the thread's cells
+  const float* rw = L.rw;
   float o1[C], o2[C], lq[C];  // outputs; lq = L(v) for the multistep history
 #pragma unroll
   for (int c = 0; c < C; ++c) {
-    const int64_t j = j0 + c;
+    const int j = j0 + c;
     const float v = wh[K + c] + wm[K + c];
     const float rr_m = c == 0 ? rr_m0 : rr[c - 1];
     const float rl_p = c == C - 1 ? rl_pC : rl[c + 1];
-    const float dF = j < nc ? flux_diff_f32c(L, j, v, rr_m, d[c + K - 1], rl[c], rr[c], d[c + K], rl_p)
-                            : 0.f;
-    const float qj = L.rw ? -dF * L.rw[j < nc ? j : nc - 1] : -dF;
+    float dF;
+    if (FK >= 0 && interior)
+      dF = flux_diff_interior<(FK >= 0 ? FK : 0)>(L, j, v, rr_m, d[c + K - 1], rl[c], rr[c], d[c + K], rl_p);
+    else
+      dF = j < nc ? flux_diff_f32c(L, j, v, rr_m, d[c + K - 1], rl[c], rr[c], d[c + K], rl_p) : 0.f;
+    const float qj = rw ? -dF * rw[j < nc ? j : nc - 1] : -dF;
     const float dtL = fmaf(a.c_hi, qj, a.c_lo * qj);  // dt L(v)_j
     lq[c] = qj * a.lscale;
     if constexpr (ST == FC_RHS) {

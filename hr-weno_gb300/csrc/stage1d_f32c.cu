@@ -21,18 +21,24 @@
 
 namespace hrw {
 
-template <int K, int ST, int NT, int C>
+template <int K, int ST, int NT, int C, int FK>
 __global__ void __launch_bounds__(NT) stage1d_f32c_kernel(F32CArgs a) {
   const int lane = threadIdx.x & 31;
   const int64_t gt = (int64_t)blockIdx.x * NT + threadIdx.x;
   if ((gt - lane) * C >= a.L.nc) return;  // whole warp past the line (uniform across the warp)
-  f32c_pass<K, ST, C>(a, gt * C, lane);
+  f32c_pass<K, ST, C, FK>(a, gt * C, lane);
 }
 
 template <int K, int ST, int NT, int C>
 static cudaError_t launch_shape(const F32CArgs& a, cudaStream_t s) {
   const int64_t nblk = ((int64_t)a.L.nc + NT * C - 1) / (NT * C);
-  stage1d_f32c_kernel<K, ST, NT, C><<<(unsigned)nblk, NT, 0, s>>>(a);
+  const int fk = 2 * (a.L.fn != HRW_FN_BURGERS) + (a.L.flux != HRW_FLUX_LAX_FRIEDRICHS);
+  switch (fk) {  // the flux kind as a compile-time constant
+    case 0: stage1d_f32c_kernel<K, ST, NT, C, 0><<<(unsigned)nblk, NT, 0, s>>>(a); break;
+    case 1: stage1d_f32c_kernel<K, ST, NT, C, 1><<<(unsigned)nblk, NT, 0, s>>>(a); break;
+    case 2: stage1d_f32c_kernel<K, ST, NT, C, 2><<<(unsigned)nblk, NT, 0, s>>>(a); break;
+    default: stage1d_f32c_kernel<K, ST, NT, C, 3><<<(unsigned)nblk, NT, 0, s>>>(a); break;
+  }
   return cudaGetLastError();
 }
 
