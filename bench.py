@@ -632,9 +632,11 @@ def run_adjoint(args, dist: Dist) -> dict | None:
         torch.cuda.synchronize()
     t_grad = dist.max(e[0].elapsed_time(e[1]) * 1e-3 / args.steps)
     t_fwd = dist.max(e[2].elapsed_time(e[3]) * 1e-3 / args.steps)
+    tape_bytes = adj.tape_bytes
     # central differences of the forward map in random directions
     fd = []
     fd_rough = []
+    fd_norm = []  # |fd - g.d| / (|g| |d|): the error against the scale of the directional derivative
     xs = np.linspace(0.0, 1.0, n)
     for s in range(args.fd_directions):  # fourth-order central differences
         if s % 2 == 0:  # smooth random direction: 16 sine modes with random amplitudes, phases
@@ -649,6 +651,7 @@ def run_adjoint(args, dist: Dist) -> dict | None:
         fdv = (8.0 * (Jv[1] - Jv[2]) - (Jv[0] - Jv[3])) / (12.0 * h)
         gd = float((g * d).sum())
         (fd if s % 2 == 0 else fd_rough).append(abs(fdv - gd) / abs(gd))
+        fd_norm.append(abs(fdv - gd) / (float(g.norm()) * float(d.norm())))
     # the whole trajectory on the tape (no recompute) when it fits in device memory
     adj0 = hrweno.adjoint(prob, checkpoint_every=0)
     adj0.set_stream(stream.cuda_stream)
@@ -660,7 +663,9 @@ def run_adjoint(args, dist: Dist) -> dict | None:
     torch.cuda.synchronize()
     t_tape = e[0].elapsed_time(e[1]) * 1e-3
     tape_every = adj0.checkpoint_every
+    tape_bytes0 = adj0.tape_bytes
     same = bool(torch.equal(g0, g))
+    gdiff = float((g0 - g).abs().max() / g.abs().max())
     del adj0, g0
     # a batch of 256 problems of 4096 cells, one gradient each, in one set of launches
     bn, bseg = 4096, 256
@@ -693,12 +698,18 @@ def run_adjoint(args, dist: Dist) -> dict | None:
                    "time_steps": nsteps, "checkpoint_every": ADJ_EVERY, "alpha": "fixed max|u0|"},
         "adjoint": {"J": float(J[0]), "gradient_ms": 1e3 * t_grad, "forward_ms": 1e3 * t_fwd,
                     "cost_vs_forward": t_grad / t_fwd, "forward_steps_in_gradient": adj.forward_steps,
-                    "full_tape": {"gradient_ms": 1e3 * t_tape, "cost_vs_forward": t_tape / t_fwd,
-                                  "checkpoint_every": tape_every, "same_gradient_bits": same},
+                    "segment_state_bytes": tape_bytes[0], "weno_tape_bytes": tape_bytes[1],
+                    "auto_checkpointing": {"gradient_ms": 1e3 * t_tape, "cost_vs_forward": t_tape / t_fwd,
+                                           "checkpoint_every": tape_every,
+                                           "segment_state_bytes": tape_bytes0[0],
+                                           "weno_tape_bytes": tape_bytes0[1],
+                                           "same_gradient_bits": same,
+                                           "max_rel_diff_vs_checkpointed": gdiff},
                     "fd_directions": args.fd_directions, "fd_order": 4,
                     "fd_max_rel_err_smooth": max(fd) if fd else None,
                     "fd_max_rel_err_rough": max(fd_rough) if fd_rough else None,
                     "fd_median_rel_err_rough": float(np.median(fd_rough)) if fd_rough else None,
+                    "fd_max_err_over_norms": max(fd_norm) if fd_norm else None,
                     "batch": {"problems": bseg, "cells_each": bn, "gradient_ms": 1e3 * bt_grad,
                               "forward_ms": 1e3 * bt_fwd, "cost_vs_forward": bt_grad / bt_fwd,
                               "gradient_cell_updates_per_s": bseg * bn * nsteps / bt_grad}},
@@ -779,7 +790,9 @@ def main() -> None:
     global NC
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps (default: 200 burgers1d, 100 pbe2d, 20 batched, 2 adjoint "
+                         "gradients, 3 config1 runs)")
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
@@ -788,12 +801,16 @@ def main() -> None:
                     help="burgers1d (default): the 2^24-cell line; pbe2d: the 2D PBE grid")
     ap.add_argument("--pbe-n", type=int, default=PBE_N, help="pbe2d grid size per dimension")
     ap.add_argument("--adj-steps", type=int, default=ADJ_STEPS, help="adjoint: time steps")
-    ap.add_argument("--fd-directions", type=int, default=8,
-                    help="adjoint: random directions of the central-difference check")
+    ap.add_argument("--fd-directions", type=int, default=64,
+                    help="adjoint: random directions of the central-difference check (64 as the "
+                         "adjoint configuration states; the default burgers1d run checks 2)")
     ap.add_argument("--cells", type=int, default=NC,
                     help="cells of the line (default 2^24, the benchmark workload; smaller "
                          "lines are for profiler captures)")
     args = ap.parse_args()
+    if args.steps is None:
+        args.steps = {"burgers1d": 200, "pbe2d": 100, "batched": 20, "adjoint": 2,
+                      "config1": 3}[args.workload]
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
     NC = args.cells

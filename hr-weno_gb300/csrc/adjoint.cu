@@ -63,53 +63,6 @@ __device__ __forceinline__ LineArgs line_args(const AdjLine& A) {
 }
 
 // --------------------------------------------------------------------------------------------
-// Forward stage (FAST FP64), segment-aware: the warp-pass of the batched kernel with ghosts
-// replicating the first and last cell of each segment.  Requires seg % C == 0 or one segment.
-// --------------------------------------------------------------------------------------------
-template <int K, int ST, int C>
-__global__ void __launch_bounds__(256) adj_fwd_kernel(AdjLine A, StageArgs a) {
-  const LineArgs L = line_args(A);
-  const int lane = threadIdx.x & 31;
-  const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
-  for (int64_t wv = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; wv * 32 * C < A.n; wv += nwarps) {
-    const int64_t j0 = wv * 32 * C + (int64_t)lane * C;
-    const int64_t jc = j0 < A.n ? j0 : A.n - 1;
-    const int64_t s0 = jc / A.seg * A.seg, s1 = s0 + A.seg - 1;
-    double w[C + 2 * K];
-#pragma unroll
-    for (int q = 0; q < C + 2 * K; ++q) {
-      int64_t g = j0 - K + q;
-      g = g < s0 ? s0 : (g > s1 ? s1 : g);
-      w[q] = a.v[g];
-    }
-    double vl[C], vr[C];
-    recon_fast<K, C>(w, a.eps, vl, vr);
-    double e[2 * K - 1];
-#pragma unroll
-    for (int q = 0; q < 2 * K - 1; ++q) e[q] = lane == 31 ? w[C + 1 + q] : w[q];
-    double el, er;
-    recon_fast_one<K>(&e[K - 1], a.eps, el, er);
-    const double vr_up = __shfl_up_sync(FULL, vr[C - 1], 1);
-    const double vl_dn = __shfl_down_sync(FULL, vl[0], 1);
-    const double vr_m = lane == 0 ? er : vr_up;  // interfaces across segments are never used:
-    const double vl_p = lane == 31 ? el : vl_dn;  // the boundary rules replace them
-    const int64_t l0 = j0 - s0;  // local index of the first cell
-    double F[C + 1];
-    F[0] = flux_fast(L, vr_m, vl[0], l0);
-#pragma unroll
-    for (int c = 1; c < C; ++c) F[c] = flux_fast(L, vr[c - 1], vl[c], l0 + c);
-    F[C] = flux_fast(L, vr[C - 1], vl_p, l0 + C);
-#pragma unroll
-    for (int c = 0; c < C; ++c) {
-      const int64_t j = j0 + c;
-      if (j >= A.n) break;
-      const double dF = flux_diff<false>(L, l0 + c, F[c], F[c + 1], vr[c]);
-      combine_fast<ST>(a, j, w[K + c], dF, L.rws0);
-    }
-  }
-}
-
-// --------------------------------------------------------------------------------------------
 // WENO of one cell in division form with everything the reverse pass needs, then the reverse
 // pass: given ar (adjoint of vr) and al (adjoint of vl), add d(ar vr + al vl)/dp into
 // out[0 .. 2K-2] for the stencil p[-(K-1) .. K-1].
@@ -194,6 +147,210 @@ template <> struct WenoTape<3> {
   }
 };
 
+// --------------------------------------------------------------------------------------------
+// WENO tape: per cell and forward stage, what the reverse pass needs of the cell's WENO map,
+// so that the reverse does not recompute it.  With ar, al the adjoints of vr, vl:
+//   d beta_r = ar X_r + al Y_r,   X_r = -2 w_r (q_r - vr) / (eps + beta_r),
+//                                 Y_r = -2 w~_r (r_r - vl) / (eps + beta_r)
+// (q, r the candidates, w, w~ the weights), then the candidates' and indicators' gradients.
+// Entries, each a plane of n doubles (structure of arrays):
+//   k = 3: vr, vl, X0..2, Y0..2, w0..2/6, w~0..2/6, 13/6 A0..2, B0..2/2        (20)
+//   k = 2: vr, vl, X0..1, Y0..1, w0..1, w~0..1, 2 D0..1                        (12)
+// with the A, B, D of WenoTape.  FAST cells take them from the product-form weights of the
+// forward pass (one extra reciprocal per cell); guarded cells from WenoTape's division form.
+// --------------------------------------------------------------------------------------------
+template <int K> struct TapeN { static constexpr int n = 0; };
+template <> struct TapeN<2> { static constexpr int n = 12; };
+template <> struct TapeN<3> { static constexpr int n = 20; };
+
+template <int K>
+__device__ __noinline__ void tape_guarded(double vm2, double vm1, double v0, double vp1, double vp2,
+                                          double eps, double vl, double vr, double* wt, int64_t ts,
+                                          int64_t j) {
+  const double p[5] = {vm2, vm1, v0, vp1, vp2};
+  WenoTape<K> W;
+  W.fwd(p + 2, eps);
+  wt[j] = vr;
+  wt[ts + j] = vl;
+  if constexpr (K == 3) {
+    const double q[3] = {W.q0, W.q1, W.q2}, r[3] = {W.r0, W.r1, W.r2};
+    const double w[3] = {W.w0, W.w1, W.w2}, u[3] = {W.u0, W.u1, W.u2};
+    const double ie[3] = {W.ie0, W.ie1, W.ie2}, A[3] = {W.A0, W.A1, W.A2}, B[3] = {W.B0, W.B1, W.B2};
+#pragma unroll
+    for (int s = 0; s < 3; ++s) {
+      wt[(2 + s) * ts + j] = -2.0 * ie[s] * (w[s] * (1.0 / 6.0)) * (q[s] - 6.0 * W.vr);
+      wt[(5 + s) * ts + j] = -2.0 * ie[s] * (u[s] * (1.0 / 6.0)) * (r[s] - 6.0 * W.vl);
+      wt[(8 + s) * ts + j] = w[s] * (1.0 / 6.0);
+      wt[(11 + s) * ts + j] = u[s] * (1.0 / 6.0);
+      wt[(14 + s) * ts + j] = (13.0 / 6.0) * A[s];
+      wt[(17 + s) * ts + j] = 0.5 * B[s];
+    }
+  } else if constexpr (K == 2) {
+    const double q[2] = {W.q0, W.q1}, r[2] = {W.r0, W.r1}, w[2] = {W.w0, W.w1};
+    const double u[2] = {W.u0, W.u1}, ie[2] = {W.ie0, W.ie1}, D[2] = {W.D0, W.D1};
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+      wt[(2 + s) * ts + j] = -2.0 * ie[s] * w[s] * (q[s] - W.vr);
+      wt[(4 + s) * ts + j] = -2.0 * ie[s] * u[s] * (r[s] - W.vl);
+      wt[(6 + s) * ts + j] = w[s];
+      wt[(8 + s) * ts + j] = u[s];
+      wt[(10 + s) * ts + j] = 2.0 * D[s];
+    }
+  }
+}
+
+// The tap of recon_fast that writes the tape of cells j0 + c < n (nothing when wt is null).
+template <int K>
+struct AdjTap {
+  double* wt;
+  int64_t ts, j0, n;
+  double eps;
+  __device__ __forceinline__ void cell(int c, const FastCell3& f) const {
+    const int64_t j = j0 + c;
+    if (!wt || j >= n) return;
+    // 1/e_r from one reciprocal of e0 e1 e2
+    const double t12 = f.e1 * f.e2, t02 = f.e0 * f.e2, t01 = f.e0 * f.e1;
+    const double iE = rcp_fast(f.e0 * t12);
+    const double m0 = -2.0 * (t12 * iE), m1 = -2.0 * (t02 * iE), m2 = -2.0 * (t01 * iE);
+    const double w0 = f.T0 * f.ir, w1 = f.Q1 * f.ir, w2 = f.P2 * f.ir;  // w_r / 6
+    const double u0 = f.P0 * f.il, u1 = f.Q1 * f.il, u2 = f.T2 * f.il;  // w~_r / 6
+    const double vr6 = 6.0 * f.vr, vl6 = 6.0 * f.vl;
+    double* o = wt + j;
+    o[0] = f.vr;
+    o[ts] = f.vl;
+    o[2 * ts] = (m0 * w0) * (f.V0 - vr6);
+    o[3 * ts] = (m1 * w1) * (f.V1 - vr6);
+    o[4 * ts] = (m2 * w2) * (f.V2 - vr6);
+    o[5 * ts] = (m0 * u0) * (f.W0 - vl6);
+    o[6 * ts] = (m1 * u1) * (f.W1 - vl6);
+    o[7 * ts] = (m2 * u2) * (f.W2 - vl6);
+    o[8 * ts] = w0;
+    o[9 * ts] = w1;
+    o[10 * ts] = w2;
+    o[11 * ts] = u0;
+    o[12 * ts] = u1;
+    o[13 * ts] = u2;
+    o[14 * ts] = (13.0 / 6.0) * f.D0;
+    o[15 * ts] = (13.0 / 6.0) * f.D1;
+    o[16 * ts] = (13.0 / 6.0) * f.D2;
+    o[17 * ts] = f.E0;
+    o[18 * ts] = f.E1;
+    o[19 * ts] = f.E2;
+  }
+  __device__ __forceinline__ void cell(int c, const FastCell2& f) const {
+    const int64_t j = j0 + c;
+    if (!wt || j >= n) return;
+    const double iE = rcp_fast(f.e0 * f.e1);
+    const double m0 = -2.0 * (f.e1 * iE), m1 = -2.0 * (f.e0 * iE);  // -2/e_r
+    const double w0 = 4.0 * f.s1 * f.ir, w1 = 2.0 * f.s0 * f.ir;
+    const double u0 = 2.0 * f.s1 * f.il, u1 = 4.0 * f.s0 * f.il;
+    double* o = wt + j;
+    o[0] = f.vr;
+    o[ts] = f.vl;
+    o[2 * ts] = (m0 * w0) * fma(0.5, f.V0, -f.vr);
+    o[3 * ts] = (m1 * w1) * fma(0.5, f.V1, -f.vr);
+    o[4 * ts] = (m0 * u0) * fma(0.5, f.W0, -f.vl);
+    o[5 * ts] = (m1 * u1) * fma(0.5, f.W1, -f.vl);
+    o[6 * ts] = w0;
+    o[7 * ts] = w1;
+    o[8 * ts] = u0;
+    o[9 * ts] = u1;
+    o[10 * ts] = 2.0 * f.d0;
+    o[11 * ts] = 2.0 * f.d1;
+  }
+  __device__ __forceinline__ void guarded(int c, double vm2, double vm1, double v0, double vp1,
+                                          double vp2, double vl, double vr) const {
+    const int64_t j = j0 + c;
+    if (!wt || j >= n) return;
+    tape_guarded<K>(vm2, vm1, v0, vp1, vp2, eps, vl, vr, wt, ts, j);
+  }
+};
+
+// Reverse of the WENO map from the tape: out[0 .. 2K-2] += d(ar vr + al vl)/dp, as
+// WenoTape<K>::rev.
+template <int K>
+__device__ __forceinline__ void rev_tape(const double* __restrict__ wt, int64_t ts, int64_t i,
+                                         double ar, double al, double* out) {
+  const double* t = wt + i;
+  if constexpr (K == 3) {
+    const double db0 = fma(ar, t[2 * ts], al * t[5 * ts]);
+    const double db1 = fma(ar, t[3 * ts], al * t[6 * ts]);
+    const double db2 = fma(ar, t[4 * ts], al * t[7 * ts]);
+    const double dq0 = ar * t[8 * ts], dq1 = ar * t[9 * ts], dq2 = ar * t[10 * ts];
+    const double dr0 = al * t[11 * ts], dr1 = al * t[12 * ts], dr2 = al * t[13 * ts];
+    const double gA0 = t[14 * ts] * db0, gA1 = t[15 * ts] * db1, gA2 = t[16 * ts] * db2;
+    const double gB0 = t[17 * ts] * db0, gB1 = t[18 * ts] * db1, gB2 = t[19 * ts] * db2;
+    out[0] += fma(2.0, dq2, gA2 + gB2 - dr2);
+    out[1] += fma(-7.0, dq2, fma(2.0, dr1, fma(5.0, dr2, fma(-2.0, gA2, fma(-4.0, gB2, gA1 + gB1 - dq1)))));
+    out[2] += fma(2.0, dq0, fma(5.0, dq1 + dr1, fma(11.0, dq2 + dr0, fma(2.0, dr2,
+              fma(3.0, gB0 + gB2, fma(-2.0, gA1, gA0 + gA2))))));
+    out[3] += fma(5.0, dq0, fma(2.0, dq1, fma(-7.0, dr0, fma(-2.0, gA0, fma(-4.0, gB0, gA1 - gB1 - dr1)))));
+    out[4] += fma(2.0, dr0, gA0 + gB0 - dq0);
+  } else if constexpr (K == 2) {
+    const double db0 = fma(ar, t[2 * ts], al * t[4 * ts]);
+    const double db1 = fma(ar, t[3 * ts], al * t[5 * ts]);
+    const double dq0 = ar * t[6 * ts], dq1 = ar * t[7 * ts];
+    const double dr0 = al * t[8 * ts], dr1 = al * t[9 * ts];
+    const double g0 = t[10 * ts] * db0, g1 = t[11 * ts] * db1;
+    out[0] += fma(-0.5, dq1, fma(0.5, dr1, -g1));
+    out[1] += fma(0.5, dq0 + dr1, fma(1.5, dq1 + dr0, g1 - g0));
+    out[2] += fma(0.5, dq0 - dr0, g0);
+  } else {
+    out[0] += ar + al;
+  }
+}
+
+// --------------------------------------------------------------------------------------------
+// Forward stage (FAST FP64), segment-aware: the warp-pass of the batched kernel with ghosts
+// replicating the first and last cell of each segment.  Requires seg % C == 0 or one segment.
+// TAPE: also write this stage's slice wt of the WENO tape for every cell.  The state
+// arithmetic is the same in both instantiations (and in C = 4 and 8 cells per thread), so
+// taped and untaped passes give the same states.
+// --------------------------------------------------------------------------------------------
+template <int K, int ST, int C, bool TAPE>
+__global__ void __launch_bounds__(256) adj_fwd_kernel(AdjLine A, StageArgs a, double* wt) {
+  const LineArgs L = line_args(A);
+  const int lane = threadIdx.x & 31;
+  const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t wv = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; wv * 32 * C < A.n; wv += nwarps) {
+    const int64_t j0 = wv * 32 * C + (int64_t)lane * C;
+    const int64_t jc = j0 < A.n ? j0 : A.n - 1;
+    const int64_t s0 = jc / A.seg * A.seg, s1 = s0 + A.seg - 1;
+    double w[C + 2 * K];
+#pragma unroll
+    for (int q = 0; q < C + 2 * K; ++q) {
+      int64_t g = j0 - K + q;
+      g = g < s0 ? s0 : (g > s1 ? s1 : g);
+      w[q] = a.v[g];
+    }
+    double vl[C], vr[C];
+    if constexpr (TAPE) recon_fast<K, C, true, AdjTap<K>>(w, a.eps, vl, vr, AdjTap<K>{wt, A.n, j0, A.n, a.eps});
+    else recon_fast<K, C>(w, a.eps, vl, vr);
+    double e[2 * K - 1];
+#pragma unroll
+    for (int q = 0; q < 2 * K - 1; ++q) e[q] = lane == 31 ? w[C + 1 + q] : w[q];
+    double el, er;
+    recon_fast_one<K>(&e[K - 1], a.eps, el, er);
+    const double vr_up = __shfl_up_sync(FULL, vr[C - 1], 1);
+    const double vl_dn = __shfl_down_sync(FULL, vl[0], 1);
+    const double vr_m = lane == 0 ? er : vr_up;  // interfaces across segments are never used:
+    const double vl_p = lane == 31 ? el : vl_dn;  // the boundary rules replace them
+    const int64_t l0 = j0 - s0;  // local index of the first cell
+    double F[C + 1];
+    F[0] = flux_fast(L, vr_m, vl[0], l0);
+#pragma unroll
+    for (int c = 1; c < C; ++c) F[c] = flux_fast(L, vr[c - 1], vl[c], l0 + c);
+    F[C] = flux_fast(L, vr[C - 1], vl_p, l0 + C);
+#pragma unroll
+    for (int c = 0; c < C; ++c) {
+      const int64_t j = j0 + c;
+      if (j >= A.n) break;
+      const double dF = flux_diff<false>(L, l0 + c, F[c], F[c + 1], vr[c]);
+      combine_fast<ST>(a, j, w[K + c], dF, L.rws0);
+    }
+  }
+}
+
 // does cell with local index lc use the interface flux on its right / left?
 __device__ __forceinline__ bool uses_fr(int bc, int64_t lc, int64_t seg) {
   if (bc == HRW_BC_COPY) return lc > 0 && lc < seg - 1;
@@ -217,8 +374,9 @@ enum AdjMode : int { ADJ_A3 = 0, ADJ_A2 = 1, ADJ_A1 = 2 };
 //   state: v (the stage input of the forward stage), mu: adjoint of that stage's L output
 //   (scaled as described in the mode), acc: the accumulated adjoint of u.
 // --------------------------------------------------------------------------------------------
-template <int K, int MODE, int NT>
+template <int K, int MODE, int NT, bool TAPE>
 __global__ void __launch_bounds__(NT) adj_vjp_kernel(AdjLine A, const double* __restrict__ v,
+                                                     const double* __restrict__ wt,
                                                      const double* __restrict__ mu,
                                                      double* __restrict__ acc,
                                                      double* __restrict__ out, double dt) {
@@ -235,15 +393,21 @@ __global__ void __launch_bounds__(NT) adj_vjp_kernel(AdjLine A, const double* __
     if (i >= 0 && i < A.n) {
       const int64_t s0 = i / A.seg * A.seg, s1 = s0 + A.seg - 1, li = i - s0;
       double p[NS];
-#pragma unroll
-      for (int q = 0; q < NS; ++q) {
-        int64_t g = i - (K - 1) + q;
-        g = g < s0 ? s0 : (g > s1 ? s1 : g);
-        p[q] = v[g];
-      }
       WenoTape<K> W;
-      W.fwd(&p[K - 1], A.eps);
-      const double vl = W.vl, vr = W.vr;
+      double vl, vr;
+      if constexpr (TAPE) {  // the forward pass recorded the cell's WENO map
+        vr = wt[i];
+        vl = wt[A.n + i];
+      } else {
+#pragma unroll
+        for (int q = 0; q < NS; ++q) {
+          int64_t g = i - (K - 1) + q;
+          g = g < s0 ? s0 : (g > s1 ? s1 : g);
+          p[q] = v[g];
+        }
+        W.fwd(&p[K - 1], A.eps);
+        vl = W.vl, vr = W.vr;
+      }
       const double mi = mu[i];
       // flux adjoints of the cell's right and left interfaces
       double ar = 0.0, al = 0.0;
@@ -261,7 +425,8 @@ __global__ void __launch_bounds__(NT) adj_vjp_kernel(AdjLine A, const double* __
                             (uses_fr(A.bc, li - 1, A.seg) ? mm : 0.0)) * idx;
         al = phi * 0.5 * (dflux(A, vl, li) - A.alpha);
       }
-      W.rev(ar, al, o);
+      if constexpr (TAPE) rev_tape<K>(wt, A.n, i, ar, al, o);
+      else W.rev(ar, al, o);
     }
 #pragma unroll
     for (int q = 0; q < NS; ++q) sc[t * NS + q] = o[q];
@@ -307,52 +472,105 @@ __global__ void __launch_bounds__(NT) adj_vjp_kernel(AdjLine A, const double* __
   }
 }
 
-// J per segment and lambda_T = u - target
-__global__ void adj_misfit_kernel(AdjLine A, const double* __restrict__ u,
-                                  const double* __restrict__ tgt, double* __restrict__ lam,
-                                  double* __restrict__ J) {
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < A.n; i += stride) {
+// J per segment and lambda_T = u - target, summed in a fixed order (the same J, bit for bit,
+// on every call, so that finite differences of J see no summation noise): block b of segment
+// sg sums its chunk of kMisfitChunk cells with compensated (Neumaier) sums per thread and a
+// pairwise tree across the block into part[sg * P + b]; adj_misfit_final adds the P partials.
+constexpr int kMisfitThreads = 256;
+constexpr int64_t kMisfitChunk = 1 << 16;
+
+__device__ __forceinline__ void neumaier(double& s, double& c, double x) {
+  const double t = s + x;
+  c += fabs(s) >= fabs(x) ? (s - t) + x : (x - t) + s;
+  s = t;
+}
+
+__global__ void __launch_bounds__(kMisfitThreads) adj_misfit_kernel(
+    AdjLine A, const double* __restrict__ u, const double* __restrict__ tgt,
+    double* __restrict__ lam, double* __restrict__ part, int P) {
+  __shared__ double red[kMisfitThreads];
+  const int sg = blockIdx.x / P, b = blockIdx.x - sg * P;
+  const int64_t lo = sg * A.seg + b * kMisfitChunk;
+  const int64_t hi = min(lo + kMisfitChunk, (sg + 1) * A.seg);
+  double s = 0.0, c = 0.0;
+  for (int64_t i = lo + threadIdx.x; i < hi; i += kMisfitThreads) {
     const double r = u[i] - tgt[i];
     lam[i] = r;
-    atomicAdd(&J[i / A.seg], 0.5 * r * r);
+    neumaier(s, c, 0.5 * r * r);
   }
+  red[threadIdx.x] = s + c;
+  __syncthreads();
+  for (int w = kMisfitThreads / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = red[0];
 }
 
-template <int K>
-cudaError_t fwd_stage_k(const AdjLine& A, const StageArgs& a, int st, cudaStream_t s) {
-  constexpr int C = 8;
+__global__ void adj_misfit_final(const double* __restrict__ part, int nseg, int P,
+                                 double* __restrict__ J) {
+  const int sg = blockIdx.x * blockDim.x + threadIdx.x;
+  if (sg >= nseg) return;
+  double s = 0.0, c = 0.0;
+  for (int b = 0; b < P; ++b) neumaier(s, c, part[(int64_t)sg * P + b]);
+  J[sg] = s + c;
+}
+
+int misfit_blocks_per_seg(const AdjLine& A) { return (int)((A.seg + kMisfitChunk - 1) / kMisfitChunk); }
+
+template <int K, int C, bool TAPE>
+cudaError_t fwd_stage_kt(const AdjLine& A, const StageArgs& a, int st, double* wt, cudaStream_t s) {
   const int64_t warps = (A.n + 32 * C - 1) / (32 * C);
   const int blocks = (int)((warps + 7) / 8 < 152 * 32 ? (warps + 7) / 8 : 152 * 32);
-  if (st == ST_EULER) adj_fwd_kernel<K, ST_EULER, C><<<blocks, 256, 0, s>>>(A, a);
-  else if (st == ST_RK3B) adj_fwd_kernel<K, ST_RK3B, C><<<blocks, 256, 0, s>>>(A, a);
-  else adj_fwd_kernel<K, ST_RK3C, C><<<blocks, 256, 0, s>>>(A, a);
+  if (st == ST_EULER) adj_fwd_kernel<K, ST_EULER, C, TAPE><<<blocks, 256, 0, s>>>(A, a, wt);
+  else if (st == ST_RK3B) adj_fwd_kernel<K, ST_RK3B, C, TAPE><<<blocks, 256, 0, s>>>(A, a, wt);
+  else adj_fwd_kernel<K, ST_RK3C, C, TAPE><<<blocks, 256, 0, s>>>(A, a, wt);
+  return cudaGetLastError();
+}
+
+// taped passes run 4 cells per thread (the tape's intermediates need the registers)
+template <int K>
+cudaError_t fwd_stage_k(const AdjLine& A, const StageArgs& a, int st, double* wt, cudaStream_t s) {
+  if (TapeN<K>::n > 0 && wt) return fwd_stage_kt<K, 4, true>(A, a, st, wt, s);
+  return fwd_stage_kt<K, 8, false>(A, a, st, nullptr, s);
+}
+
+template <int K, bool TAPE>
+cudaError_t vjp_kt(const AdjLine& A, int mode, const double* v, const double* wt, const double* mu,
+                   double* acc, double* out, double dt, cudaStream_t s) {
+  constexpr int NT = 256;
+  const unsigned blocks = (unsigned)((A.n + NT - 1) / NT);
+  if (mode == ADJ_A3)
+    adj_vjp_kernel<K, ADJ_A3, NT, TAPE><<<blocks, NT, 0, s>>>(A, v, wt, mu, acc, out, dt);
+  else if (mode == ADJ_A2)
+    adj_vjp_kernel<K, ADJ_A2, NT, TAPE><<<blocks, NT, 0, s>>>(A, v, wt, mu, acc, out, dt);
+  else
+    adj_vjp_kernel<K, ADJ_A1, NT, TAPE><<<blocks, NT, 0, s>>>(A, v, wt, mu, acc, out, dt);
   return cudaGetLastError();
 }
 
 template <int K>
-cudaError_t vjp_k(const AdjLine& A, int mode, const double* v, const double* mu, double* acc,
-                  double* out, double dt, cudaStream_t s) {
-  constexpr int NT = 256;
-  const unsigned blocks = (unsigned)((A.n + NT - 1) / NT);
-  if (mode == ADJ_A3) adj_vjp_kernel<K, ADJ_A3, NT><<<blocks, NT, 0, s>>>(A, v, mu, acc, out, dt);
-  else if (mode == ADJ_A2) adj_vjp_kernel<K, ADJ_A2, NT><<<blocks, NT, 0, s>>>(A, v, mu, acc, out, dt);
-  else adj_vjp_kernel<K, ADJ_A1, NT><<<blocks, NT, 0, s>>>(A, v, mu, acc, out, dt);
-  return cudaGetLastError();
+cudaError_t vjp_k(const AdjLine& A, int mode, const double* v, const double* wt, const double* mu,
+                  double* acc, double* out, double dt, cudaStream_t s) {
+  if (TapeN<K>::n > 0 && wt) return vjp_kt<K, true>(A, mode, v, wt, mu, acc, out, dt, s);
+  return vjp_kt<K, false>(A, mode, v, nullptr, mu, acc, out, dt, s);
 }
 
-cudaError_t fwd_stage(const AdjLine& A, const StageArgs& a, int st, cudaStream_t s) {
-  if (A.k == 1) return fwd_stage_k<1>(A, a, st, s);
-  if (A.k == 2) return fwd_stage_k<2>(A, a, st, s);
-  return fwd_stage_k<3>(A, a, st, s);
+cudaError_t fwd_stage(const AdjLine& A, const StageArgs& a, int st, double* wt, cudaStream_t s) {
+  if (A.k == 1) return fwd_stage_k<1>(A, a, st, nullptr, s);
+  if (A.k == 2) return fwd_stage_k<2>(A, a, st, wt, s);
+  return fwd_stage_k<3>(A, a, st, wt, s);
 }
 
-cudaError_t vjp(const AdjLine& A, int mode, const double* v, const double* mu, double* acc,
-                double* out, double dt, cudaStream_t s) {
-  if (A.k == 1) return vjp_k<1>(A, mode, v, mu, acc, out, dt, s);
-  if (A.k == 2) return vjp_k<2>(A, mode, v, mu, acc, out, dt, s);
-  return vjp_k<3>(A, mode, v, mu, acc, out, dt, s);
+// v: the stage's input state; wt: the stage's WENO tape (null: recompute from v)
+cudaError_t vjp(const AdjLine& A, int mode, const double* v, const double* wt, const double* mu,
+                double* acc, double* out, double dt, cudaStream_t s) {
+  if (A.k == 1) return vjp_k<1>(A, mode, v, nullptr, mu, acc, out, dt, s);
+  if (A.k == 2) return vjp_k<2>(A, mode, v, wt, mu, acc, out, dt, s);
+  return vjp_k<3>(A, mode, v, wt, mu, acc, out, dt, s);
 }
+
+int tape_entries(int k) { return k == 3 ? TapeN<3>::n : (k == 2 ? TapeN<2>::n : 0); }
 
 }  // namespace
 }  // namespace hrw
@@ -366,9 +584,13 @@ struct hrw_adjoint {
   cudaStream_t own = nullptr, stream = nullptr;
   double *u = nullptr, *w1 = nullptr, *w2 = nullptr, *tgt = nullptr;
   double *lam = nullptr, *la = nullptr, *lb = nullptr, *acc = nullptr, *J = nullptr;
+  double* part = nullptr;     // partial sums of J (nseg x misfit blocks per segment)
   std::vector<double*> ckpt;  // checkpoints
   double* tape = nullptr;     // (E + 1) states + E u1 + E u2 of the segment being reversed
   int64_t tape_states = 0;    // capacity of the tape in states
+  double* wtape = nullptr;    // WENO tape of the 3E stages of the segment being reversed
+  int64_t wtape_stages = 0;   // its capacity in stages
+  int64_t wtape_used = 0;     // bytes of it the last gradient call used (0: not used)
   int64_t used_every = 0;     // checkpoint interval of the last gradient call
   int64_t fwd_steps = 0;      // forward steps taken by the last gradient call (incl. recompute)
 };
@@ -392,16 +614,30 @@ StageArgs base_args(const hrw_adjoint* h, double dt) {
   return a;
 }
 
-// one forward RK3 step from `u` to `un` with stage arrays s1, s2 (un may equal u)
-cudaError_t step(hrw_adjoint* h, const double* u, double* s1, double* s2, double* un, double dt) {
+// J[nseg] and lambda = u - target
+cudaError_t misfit(hrw_adjoint* h, const double* u) {
+  const int P = misfit_blocks_per_seg(h->line);
+  adj_misfit_kernel<<<(unsigned)(h->nseg * P), kMisfitThreads, 0, h->stream>>>(h->line, u, h->tgt,
+                                                                               h->lam, h->part, P);
+  adj_misfit_final<<<(unsigned)((h->nseg + 127) / 128), 128, 0, h->stream>>>(h->part, (int)h->nseg,
+                                                                             P, h->J);
+  return cudaGetLastError();
+}
+
+// one forward RK3 step from `u` to `un` with stage arrays s1, s2 (un may equal u); wt
+// (nullable): the WENO tape of the step's three stages, one after the other
+cudaError_t step(hrw_adjoint* h, const double* u, double* s1, double* s2, double* un, double dt,
+                 double* wt = nullptr) {
+  const size_t plane = (size_t)tape_entries(h->line.k) * (size_t)h->line.n;
   StageArgs a = base_args(h, dt);
   a.v = u, a.u = u, a.out = s1;
-  cudaError_t e = fwd_stage(h->line, a, ST_EULER, h->stream);
+  cudaError_t e = fwd_stage(h->line, a, ST_EULER, wt, h->stream);
   if (e != cudaSuccess) return e;
   a.v = s1, a.u = u, a.out = s2;
-  if ((e = fwd_stage(h->line, a, ST_RK3B, h->stream)) != cudaSuccess) return e;
+  if ((e = fwd_stage(h->line, a, ST_RK3B, wt ? wt + plane : nullptr, h->stream)) != cudaSuccess)
+    return e;
   a.v = s2, a.u = u, a.out = un;
-  return fwd_stage(h->line, a, ST_RK3C, h->stream);
+  return fwd_stage(h->line, a, ST_RK3C, wt ? wt + 2 * plane : nullptr, h->stream);
 }
 
 }  // namespace
@@ -451,6 +687,7 @@ int hrw_adjoint_create(const hrw_problem* p, int nseg, int checkpoint_every, hrw
   for (double** b : bufs)
     if (e == cudaSuccess) e = cudaMalloc(b, bytes);
   if (e == cudaSuccess) e = cudaMalloc(&h->J, sizeof(double) * nseg);
+  if (e == cudaSuccess) e = cudaMalloc(&h->part, sizeof(double) * nseg * misfit_blocks_per_seg(L));
   if (e != cudaSuccess) {
     hrw_adjoint_destroy(h);
     return adj_fail(e == cudaErrorMemoryAllocation ? HRW_ENOMEM : HRW_ECUDA,
@@ -471,15 +708,26 @@ static int adjoint_sweep(hrw_adjoint* h, int mem, const double* u0, const double
   const AdjLine& L = h->line;
   const size_t bytes = sizeof(double) * (size_t)L.n;
   const cudaMemcpyKind in = mem == HRW_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
-  // checkpoint interval: as asked, or (0) the whole trajectory on the tape when it fits in
-  // 80% of the free device memory, else sqrt(nsteps)
+  // Memory budget: 80% of the free device memory plus the tapes this handle already holds.
+  // A segment of E steps needs 3E + 1 states and, for the WENO tape, 3E stage planes of
+  // tape_entries(k) doubles per cell.
+  const int nq = tape_entries(L.k);
+  size_t fr = 0, tot = 0;
+  HRW_ACUDA(cudaMemGetInfo(&fr, &tot));
+  const double budget = 0.8 * ((double)fr + (double)bytes * (double)h->tape_states +
+                               (double)bytes * nq * (double)h->wtape_stages);
+  auto state_need = [&](int64_t e) { return (double)bytes * (3.0 * e + 1.0); };
+  auto weno_need = [&](int64_t e) { return (double)bytes * nq * 3.0 * e; };
+  // checkpoint interval: as asked, or (0) the whole trajectory with the WENO tape, else the
+  // whole trajectory's states, else sqrt(nsteps) -- the first that fits the budget
   int64_t E = h->every;
   if (E == 0) {
-    size_t fr = 0, tot = 0;
-    HRW_ACUDA(cudaMemGetInfo(&fr, &tot));
-    const double need = (double)bytes * (3.0 * nsteps + 1.0 - (double)h->tape_states);
-    E = need <= 0.8 * (double)fr ? nsteps : (int64_t)std::ceil(std::sqrt((double)nsteps));
+    const int64_t sq = (int64_t)std::ceil(std::sqrt((double)nsteps));
+    if (nq > 0 && state_need(nsteps) + weno_need(nsteps) <= budget) E = nsteps;
+    else if (state_need(nsteps) <= budget) E = nsteps;
+    else E = sq;
   }
+  const bool use_wt = nq > 0 && state_need(E) + weno_need(E) <= budget;
   if (h->tape_states < 3 * E + 1) {
     if (h->tape) cudaFree(h->tape);
     h->tape = nullptr;
@@ -487,6 +735,19 @@ static int adjoint_sweep(hrw_adjoint* h, int mem, const double* u0, const double
     HRW_ACUDA(cudaMalloc(&h->tape, bytes * (size_t)(3 * E + 1)));
     h->tape_states = 3 * E + 1;
   }
+  if (use_wt && h->wtape_stages < 3 * E) {
+    if (h->wtape) cudaFree(h->wtape);
+    h->wtape = nullptr;
+    h->wtape_stages = 0;
+    HRW_ACUDA(cudaMalloc(&h->wtape, bytes * nq * (size_t)(3 * E)));
+    h->wtape_stages = 3 * E;
+  }
+  h->wtape_used = use_wt ? (int64_t)(bytes * nq * (size_t)(3 * E)) : 0;
+  const size_t step_planes = 3 * (size_t)nq * (size_t)L.n;  // WENO tape doubles per step
+  auto WT = [&](int64_t n) { return use_wt ? h->wtape + (size_t)n * step_planes : nullptr; };
+  auto WS = [&](int64_t n, int st) {  // stage st (0..2) of step n
+    return use_wt ? h->wtape + (size_t)n * step_planes + (size_t)st * nq * L.n : nullptr;
+  };
   h->used_every = E;
   const int64_t nck = (nsteps + E - 1) / E;  // segments of the time line
   while ((int64_t)h->ckpt.size() < nck) {
@@ -509,16 +770,14 @@ static int adjoint_sweep(hrw_adjoint* h, int mem, const double* u0, const double
       for (int64_t n = 0; n < len; ++n) HRW_ACUDA(step(h, h->u, h->w1, h->w2, h->u, dt));
     } else {
       HRW_ACUDA(cudaMemcpyAsync(Un(0), h->u, bytes, cudaMemcpyDeviceToDevice, h->stream));
-      for (int64_t n = 0; n < len; ++n) HRW_ACUDA(step(h, Un(n), U1(n), U2(n), Un(n + 1), dt));
+      for (int64_t n = 0; n < len; ++n) HRW_ACUDA(step(h, Un(n), U1(n), U2(n), Un(n + 1), dt, WT(n)));
     }
     fwd += len;
   }
   // ---- misfit and lambda(T) -----------------------------------------------------------------
   const int64_t last_len = nsteps - (nck - 1) * E;
   if (target) {
-    HRW_ACUDA(cudaMemsetAsync(h->J, 0, sizeof(double) * h->nseg, h->stream));
-    adj_misfit_kernel<<<152 * 8, 256, 0, h->stream>>>(L, Un(last_len), h->tgt, h->lam, h->J);
-    HRW_ACUDA(cudaGetLastError());
+    HRW_ACUDA(misfit(h, Un(last_len)));
   } else {
     HRW_ACUDA(cudaMemcpyAsync(h->lam, h->tgt, bytes, cudaMemcpyDeviceToDevice, h->stream));
   }
@@ -527,13 +786,13 @@ static int adjoint_sweep(hrw_adjoint* h, int mem, const double* u0, const double
     const int64_t len = std::min(E, nsteps - c * E);
     if (c < nck - 1) {  // recompute the segment from its checkpoint, recording every stage
       HRW_ACUDA(cudaMemcpyAsync(Un(0), h->ckpt[c], bytes, cudaMemcpyDeviceToDevice, h->stream));
-      for (int64_t n = 0; n < len; ++n) HRW_ACUDA(step(h, Un(n), U1(n), U2(n), Un(n + 1), dt));
+      for (int64_t n = 0; n < len; ++n) HRW_ACUDA(step(h, Un(n), U1(n), U2(n), Un(n + 1), dt, WT(n)));
       fwd += len;
     }
     for (int64_t n = len - 1; n >= 0; --n) {
-      HRW_ACUDA(vjp(L, ADJ_A3, U2(n), h->lam, h->acc, h->la, dt, h->stream));
-      HRW_ACUDA(vjp(L, ADJ_A2, U1(n), h->la, h->acc, h->lb, dt, h->stream));
-      HRW_ACUDA(vjp(L, ADJ_A1, Un(n), h->lb, h->acc, h->lam, dt, h->stream));
+      HRW_ACUDA(vjp(L, ADJ_A3, U2(n), WS(n, 2), h->lam, h->acc, h->la, dt, h->stream));
+      HRW_ACUDA(vjp(L, ADJ_A2, U1(n), WS(n, 1), h->la, h->acc, h->lb, dt, h->stream));
+      HRW_ACUDA(vjp(L, ADJ_A1, Un(n), WS(n, 0), h->lb, h->acc, h->lam, dt, h->stream));
     }
   }
   h->fwd_steps = fwd;
@@ -570,9 +829,7 @@ int hrw_adjoint_forward(hrw_adjoint* h, int mem, const double* u0, const double*
   for (int64_t n = 0; n < nsteps; ++n) HRW_ACUDA(step(h, h->u, h->w1, h->w2, h->u, dt));
   if (target) {
     HRW_ACUDA(cudaMemcpyAsync(h->tgt, target, bytes, in, h->stream));
-    HRW_ACUDA(cudaMemsetAsync(h->J, 0, sizeof(double) * h->nseg, h->stream));
-    adj_misfit_kernel<<<152 * 8, 256, 0, h->stream>>>(L, h->u, h->tgt, h->lam, h->J);
-    HRW_ACUDA(cudaGetLastError());
+    HRW_ACUDA(misfit(h, h->u));
   }
   if (uT)
     HRW_ACUDA(cudaMemcpyAsync(uT, h->u, bytes, mem == HRW_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice,
@@ -596,9 +853,18 @@ int hrw_adjoint_info(const hrw_adjoint* h, int64_t* forward_steps, int64_t* chec
   return HRW_OK;
 }
 
+int hrw_adjoint_tape_info(const hrw_adjoint* h, int64_t* state_bytes, int64_t* weno_tape_bytes) {
+  if (!h) return adj_fail(HRW_EINVAL, "Invalid input 'adjoint': null handle.");
+  const int64_t bytes = (int64_t)sizeof(double) * h->line.n;
+  if (state_bytes) *state_bytes = h->used_every > 0 ? bytes * (3 * h->used_every + 1) : 0;
+  if (weno_tape_bytes) *weno_tape_bytes = h->wtape_used;
+  return HRW_OK;
+}
+
 int hrw_adjoint_destroy(hrw_adjoint* h) {
   if (!h) return HRW_OK;
-  double* bufs[] = {h->u, h->w1, h->w2, h->tgt, h->lam, h->la, h->lb, h->acc, h->J, h->tape};
+  double* bufs[] = {h->u, h->w1, h->w2, h->tgt, h->lam, h->la, h->lb, h->acc, h->J, h->tape,
+                    h->wtape, h->part};
   for (double* b : bufs)
     if (b) cudaFree(b);
   for (double* c : h->ckpt) cudaFree(c);

@@ -13,6 +13,7 @@
 //    src/hrweno_tvdode.f90:139-167,257).  Bit-identical to a non-fused CPU build.
 #pragma once
 #include <cstdint>
+#include <type_traits>
 
 #include <cuda_runtime.h>
 
@@ -146,10 +147,28 @@ template <int K> struct FastGuard;
 template <> struct FastGuard<3> { static constexpr int hi_max = (1023 + 240) << 20; };
 template <> struct FastGuard<2> { static constexpr int hi_max = (1023 + 480) << 20; };
 
+// Intermediates of one FAST cell, handed to a tap (the discrete adjoint records what its
+// reverse pass needs from them).  k = 3: e_r = eps + beta_r, the weight numerators
+// (T0, Q1, P2) of vr and (P0, Q1, T2) of vl, ir = 1/(6 den), il = 1/(6 dent), the x6
+// candidates V (vr) and W (vl), the second differences D at centres j+1, j, j-1 and the
+// half-B terms E of beta_0..2.  k = 2: e0 = eps + (v1 - v0)^2, e1 = eps + (v0 - v-1)^2,
+// s = e^2, ir = 1/(2 den), il = 1/(2 dent), x2 candidates, d0 = v1 - v0, d1 = v0 - v-1.
+struct NoTap {};
+struct FastCell3 {
+  double vr, vl, e0, e1, e2, T0, Q1, P2, P0, T2, ir, il, V0, V1, V2, W0, W1, W2, D0, D1, D2, E0, E1, E2;
+};
+struct FastCell2 {
+  double vr, vl, e0, e1, s0, s1, ir, il, V0, V1, W0, W1, d0, d1;
+};
+
 // WL = false computes vr only (vl is left untouched): the upwind flux of a positive velocity
-// needs the left state of each interface alone.
-template <int K, int C, bool WL = true>
-__device__ __forceinline__ void recon_fast(const double* w, double eps, double* vl, double* vr) {
+// needs the left state of each interface alone.  A tap other than NoTap (WL = true only) is
+// called once per cell: tap.cell(c, FastCell{K}) for FAST cells, tap.guarded(c, v-2, v-1, v0,
+// v1, v2, vl, vr) for the cells that took the reference-order path (k = 2: v-2 = v2 = 0).
+template <int K, int C, bool WL = true, class Tap = NoTap>
+__device__ __forceinline__ void recon_fast(const double* w, double eps, double* vl, double* vr,
+                                           const Tap& tap = Tap{}) {
+  constexpr bool TAP = !std::is_same<Tap, NoTap>::value;
   if constexpr (K == 1) {
 #pragma unroll
     for (int c = 0; c < C; ++c) {
@@ -163,6 +182,7 @@ __device__ __forceinline__ void recon_fast(const double* w, double eps, double* 
     double dp = w[2] - w[1];
     double ep = eps + dp * dp;
     double s0p = ep * ep;  // s0 of cell -1
+    double e0p = ep;       // (taps) e0 and d0 of the previous cell
 #pragma unroll
     for (int c = 0; c < C; ++c) {
       const int q = 2 + c;
@@ -183,6 +203,9 @@ __device__ __forceinline__ void recon_fast(const double* w, double eps, double* 
           const double R = rcp_fast((den + den) * dent);
           vr[c] = num * (dent * R);
           vl[c] = numt * (den * R);
+          if constexpr (TAP)
+            tap.cell(c, FastCell2{vr[c], vl[c], e0, e0p, s0, s1, dent * R, den * R, V0, V1, W0, W1,
+                                  d0, dp});
         } else {
           vr[c] = num * rcp_fast(den + den);
         }
@@ -190,13 +213,18 @@ __device__ __forceinline__ void recon_fast(const double* w, double eps, double* 
         const double2 g = recon_guarded<2>(0.0, w[q - 1], w[q], w[q + 1], 0.0, eps);
         if constexpr (WL) vl[c] = g.x;
         vr[c] = g.y;
+        if constexpr (TAP) tap.guarded(c, 0.0, w[q - 1], w[q], w[q + 1], 0.0, g.x, g.y);
       }
       V0p = V0;
       s0p = s0;
+      if constexpr (TAP) {
+        e0p = e0;
+        dp = d0;
+      }
     }
   } else {
     // hv(m) = v(m)/2, A(m) = 13/12 (v(m-1) - 2 v(m) + v(m+1))^2, both shared by neighbours.
-    double hv[C + 6], A[C + 2];
+    double hv[C + 6], A[C + 2], Dm[C + 2];
 #pragma unroll
     for (int q = 1; q < C + 5; ++q) hv[q] = 0.5 * w[q];
     const double c13 = 13.0 / 12;
@@ -204,6 +232,7 @@ __device__ __forceinline__ void recon_fast(const double* w, double eps, double* 
     for (int m = 0; m < C + 2; ++m) {  // centre q = m + 2 (cells -1 .. C)
       const int q = m + 2;
       const double D = fma(-2.0, w[q], w[q - 1] + w[q + 1]);
+      Dm[m] = D;
       A[m] = (c13 * D) * D;
     }
     // candidates x6: V0 = 2v0 + 5v1 - v2, V1 = -v-1 + 5v0 + 2v1, V2 = 2v-2 - 7v-1 + 11v0,
@@ -237,6 +266,9 @@ __device__ __forceinline__ void recon_fast(const double* w, double eps, double* 
           const double R = rcp_fast((6.0 * den) * dent);
           vr[c] = num * (dent * R);
           vl[c] = numt * (den * R);
+          if constexpr (TAP)
+            tap.cell(c, FastCell3{vr[c], vl[c], e0, e1, e2, T0, Q1, P2, P0, T2, dent * R, den * R,
+                                  V0, V1, V2, W0, W1, W2, Dm[c + 2], Dm[c + 1], Dm[c], E0, E1, E2});
         } else {
           vr[c] = num * rcp_fast(6.0 * den);
         }
@@ -244,6 +276,7 @@ __device__ __forceinline__ void recon_fast(const double* w, double eps, double* 
         const double2 g = recon_guarded<3>(w[q - 2], w[q - 1], w[q], w[q + 1], w[q + 2], eps);
         if constexpr (WL) vl[c] = g.x;
         vr[c] = g.y;
+        if constexpr (TAP) tap.guarded(c, w[q - 2], w[q - 1], w[q], w[q + 1], w[q + 2], g.x, g.y);
       }
       V0p = V0;
       V1p = V1;

@@ -3,7 +3,9 @@
 No counterpart in the reference.  The forward map is nsteps rktvd(order 3) steps
 (src/hrweno_tvdode.f90:161-169) of an FV1D problem with the global Lax-Friedrichs flux at fixed
 alpha; the reverse sweep is the hand-written discrete adjoint of the fused stage kernels, with
-forward recompute from checkpoints.
+forward recompute from checkpoints.  The pass that records a segment also records each cell's
+WENO-map derivatives (the WENO tape) when memory allows, so the reverse pass reads them instead
+of recomputing them.
 """
 from __future__ import annotations
 
@@ -26,10 +28,12 @@ def _setup(L):
     L.hrw_adjoint_forward.argtypes = [vp, i, vp, vp, d, C.c_int64, dp, vp]
     L.hrw_adjoint_vjp.argtypes = [vp, i, vp, vp, d, C.c_int64, vp]
     L.hrw_adjoint_info.argtypes = [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
+    L.hrw_adjoint_tape_info.argtypes = [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
     L.hrw_adjoint_set_stream.argtypes = [vp, vp]
     L.hrw_adjoint_destroy.argtypes = [vp]
     for n in ("hrw_adjoint_create", "hrw_adjoint_gradient", "hrw_adjoint_forward", "hrw_adjoint_vjp",
-              "hrw_adjoint_info", "hrw_adjoint_set_stream", "hrw_adjoint_destroy"):
+              "hrw_adjoint_info", "hrw_adjoint_tape_info", "hrw_adjoint_set_stream",
+              "hrw_adjoint_destroy"):
         getattr(L, n).restype = C.c_int
     L._adj_ready = True
 
@@ -100,6 +104,14 @@ class adjoint:  # noqa: N801
         n = C.c_int64()
         A.check(A.lib().hrw_adjoint_info(self._h, None, C.byref(n)))
         return n.value
+
+    @property
+    def tape_bytes(self) -> tuple[int, int]:
+        """(state bytes, WENO-tape bytes) the last gradient call kept on the device; a WENO
+        tape of 0 bytes means the reverse pass recomputed the WENO maps from the states."""
+        s, w = C.c_int64(), C.c_int64()
+        A.check(A.lib().hrw_adjoint_tape_info(self._h, C.byref(s), C.byref(w)))
+        return s.value, w.value
 
     def set_stream(self, stream) -> None:
         A.check(A.lib().hrw_adjoint_set_stream(self._h, C.c_void_p(int(stream) if stream else 0)))

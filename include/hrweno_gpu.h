@@ -188,7 +188,10 @@ int hrw_batch_destroy(hrw_batch* b);
  * nseg > 1, ncells must be a multiple of 8); J has one entry per problem.  The reverse sweep
  * recomputes the forward from checkpoints taken every `checkpoint_every` steps (about
  * sqrt(nsteps) is the usual choice); 0 keeps the whole trajectory on the tape when it fits in
- * 80% of the free device memory (no recompute), and falls back to sqrt(nsteps). */
+ * 80% of the free device memory (no recompute), and falls back to sqrt(nsteps).  The pass
+ * that records a segment also records each cell's WENO map derivatives (a WENO tape of 20
+ * doubles per cell and stage for k = 3, 12 for k = 2) when they fit the same budget, so the
+ * reverse pass does not recompute them. */
 typedef struct hrw_adjoint hrw_adjoint;
 int hrw_adjoint_create(const hrw_problem* p, int nseg, int checkpoint_every, hrw_adjoint** out);
 /* grad = dJ/du0 (nseg * ncells doubles), J[nseg]; arrays in memory space `mem` (J on the host) */
@@ -204,6 +207,10 @@ int hrw_adjoint_forward(hrw_adjoint* a, int mem, const double* u0, const double*
 /* forward steps (initial pass plus recompute) and the checkpoint interval of the last
  * gradient call; either pointer may be NULL */
 int hrw_adjoint_info(const hrw_adjoint* a, int64_t* forward_steps, int64_t* checkpoint_every);
+/* Device memory the last gradient call kept for its segment: the states (3E + 1 of them) and
+ * the WENO tape (0 when it did not fit: the reverse pass then recomputes each cell's WENO map
+ * from the states); either pointer may be NULL */
+int hrw_adjoint_tape_info(const hrw_adjoint* a, int64_t* state_bytes, int64_t* weno_tape_bytes);
 int hrw_adjoint_set_stream(hrw_adjoint* a, void* stream);
 int hrw_adjoint_destroy(hrw_adjoint* a);
 

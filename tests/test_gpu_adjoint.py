@@ -73,6 +73,24 @@ def test_adjoint_checkpoint_interval_invariant(hw):
         assert np.array_equal(g, ref[1]) and abs(J[0] - ref[0][0]) <= 1e-14 * ref[0][0]
 
 
+def test_adjoint_weno_tape_used(hw, orc):
+    """The pass that records a segment keeps the WENO tape (20 doubles per cell and stage for
+    k = 3, 12 for k = 2, none for k = 1); the gradient through it agrees with the tangent-linear
+    oracle as the recompute path does."""
+    n, steps = 256, 20
+    for k, nq in ((3, 20), (2, 12), (1, 0)):
+        prob = problem(hw, n, k, "burgers", "copy")
+        u0, target = line(n, 7), line(n, 8) * 0.9
+        dt = 0.4 * (10.0 / n) / 1.5
+        adj = hw.adjoint(prob, checkpoint_every=5)
+        J, g = adj.gradient(u0, target, dt, steps)
+        sb, wb = adj.tape_bytes
+        assert sb == 8 * n * (3 * 5 + 1) and wb == 8 * n * nq * 3 * 5
+        d = smooth_direction(n, 3)
+        _, dJ = orc.tl_misfit(prob, u0, d, target, dt, steps)
+        assert abs(g @ d - dJ) <= 1e-10 * abs(dJ)
+
+
 def test_adjoint_batch_matches_single(hw):
     n, nseg, steps = 256, 5, 40
     prob = problem(hw, n, 3, "burgers", "zero_inflow")
