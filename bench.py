@@ -54,7 +54,7 @@ L2_BYTES = 126 * 1024 * 1024
 # step of the 2^24-cell line, divided by cells x 3); profiles/stage1d_fp64_weno5_rk3.md.
 NCU_DRAM_BYTES_PER_CELL_LAUNCH = 943.8e6 / (3 * (1 << 24))
 # FP64 pipe utilisation of the same capture (sm__inst_executed_pipe_fp64, % of peak active)
-NCU_FP64_PIPE_PCT = 85.7
+NCU_FP64_PIPE_PCT = 86.0
 
 
 def peaks() -> dict:
@@ -256,7 +256,7 @@ def run_ours(args, dist: Dist) -> dict | None:
 
     # ---- compensated FP32 form on the same line: same steps, error against FP64 ----------
     forms = {}
-    if not args.no_forms:
+    if "f32c" in args.forms:
         ode32 = hrweno.rktvd(prob, NC, 3, dtype="f32c")
         ode32.set_stream(stream.cuda_stream)
         u32 = torch.from_numpy(u0).cuda()
@@ -400,7 +400,7 @@ def run_pbe2d(args, dist: Dist) -> dict | None:
     value = dist.world * cells * args.steps / el
     # compensated FP32 on the same grid and steps, error against the FP64 result
     forms = {}
-    if not args.no_forms:
+    if "f32c" in args.forms:
         ode32 = hrweno.mstvd(prob, cells, dtype="f32c")
         ode32.set_stream(stream.cuda_stream)
         u32 = torch.from_numpy(n0).cuda()
@@ -652,7 +652,7 @@ def run_adjoint(args, dist: Dist) -> dict | None:
         gd = float((g * d).sum())
         (fd if s % 2 == 0 else fd_rough).append(abs(fdv - gd) / abs(gd))
         fd_norm.append(abs(fdv - gd) / (float(g.norm()) * float(d.norm())))
-    # the whole trajectory on the tape (no recompute) when it fits in device memory
+    # automatic segment length (checkpoint_every = 0)
     adj0 = hrweno.adjoint(prob, checkpoint_every=0)
     adj0.set_stream(stream.cuda_stream)
     J0, g0 = adj0.gradient(u0, tgt, dt, nsteps)
@@ -796,7 +796,11 @@ def main() -> None:
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
-    ap.add_argument("--no-forms", action="store_true", help="skip the FP32 form")
+    ap.add_argument("--forms", default="f32c,pbe2d,batched,adjoint,config1",
+                    help="comma-separated forms reported beside the workload's own line "
+                         "(f32c: the compensated FP32 form of the same workload; the others: "
+                         "their workloads, run after the default burgers1d line)")
+    ap.add_argument("--no-forms", action="store_true", help="same as --forms ''")
     ap.add_argument("--workload", default="burgers1d", choices=["burgers1d", "pbe2d", "batched", "adjoint", "config1"],
                     help="burgers1d (default): the 2^24-cell line; pbe2d: the 2D PBE grid")
     ap.add_argument("--pbe-n", type=int, default=PBE_N, help="pbe2d grid size per dimension")
@@ -808,6 +812,7 @@ def main() -> None:
                     help="cells of the line (default 2^24, the benchmark workload; smaller "
                          "lines are for profiler captures)")
     args = ap.parse_args()
+    args.forms = set() if args.no_forms else {f for f in args.forms.split(",") if f}
     if args.steps is None:
         args.steps = {"burgers1d": 200, "pbe2d": 100, "batched": 20, "adjoint": 2,
                       "config1": 3}[args.workload]
@@ -827,29 +832,32 @@ def main() -> None:
             line = runs[args.workload](args, dist)
         else:
             line = run_ours(args, dist)
-            if not args.no_forms:
-                # the other forms of the metric, each on its own workload, summarised
-                sub = argparse.Namespace(**vars(args))
-                sub.steps, sub.no_cpu = min(args.steps, 100), True
-                forms = {}
+            # the other forms of the metric, each on its own workload, summarised
+            sub = argparse.Namespace(**vars(args))
+            sub.steps, sub.no_cpu = min(args.steps, 100), True
+            forms = {}
+            if "pbe2d" in args.forms:
                 pb = run_pbe2d(sub, dist)
                 if pb is not None:
                     forms["pbe2d_4096"] = {k: pb[k] for k in ("value", "ms_per_step", "roofline", "forms")}
+            if "batched" in args.forms:
                 sub.steps = min(args.steps, 20)
                 bt = run_batched(sub, dist)
                 if bt is not None:
                     forms["batched_4096_lines"] = {k: bt[k] for k in ("value", "ms_per_step", "config",
                                                                      "plain_per_problem", "forms")}
+            if "adjoint" in args.forms:
                 sub.steps, sub.fd_directions = 1, 2
                 ad = run_adjoint(sub, dist)
                 if ad is not None:
                     forms["adjoint_2^20"] = ad["adjoint"]
+            if "config1" in args.forms:
                 sub.steps = 3
                 c1 = run_config1(sub, dist)
                 if c1 is not None:
                     forms["config1_500"] = {k: c1[k] for k in ("value", "driver_loop_ms")}
-                if line is not None:
-                    line["forms"].update(forms)
+            if line is not None:
+                line["forms"].update(forms)
         if line is not None and dist.rank == 0:
             print(json.dumps(line), flush=True)
     finally:

@@ -33,6 +33,25 @@
 #include "hrw_internal.h"
 #include "hrw_stage.cuh"
 
+// Launch shapes (compile-time; measured on the 2^20-cell line): cells per thread of the
+// forward stage without and with the WENO tape, their minimum resident blocks per SM, and the
+// cells per block of the reverse stage.
+#ifndef HRW_ADJ_FWD_C
+#define HRW_ADJ_FWD_C 8
+#endif
+#ifndef HRW_ADJ_FWD_MINB
+#define HRW_ADJ_FWD_MINB 1
+#endif
+#ifndef HRW_ADJ_TAPE_C
+#define HRW_ADJ_TAPE_C 4
+#endif
+#ifndef HRW_ADJ_TAPE_MINB
+#define HRW_ADJ_TAPE_MINB 1
+#endif
+#ifndef HRW_ADJ_VJP_NT
+#define HRW_ADJ_VJP_NT 256
+#endif
+
 namespace hrw {
 
 namespace {
@@ -210,8 +229,8 @@ struct AdjTap {
     if (!wt || j >= n) return;
     // 1/e_r from one reciprocal of e0 e1 e2
     const double t12 = f.e1 * f.e2, t02 = f.e0 * f.e2, t01 = f.e0 * f.e1;
-    const double iE = rcp_fast(f.e0 * t12);
-    const double m0 = -2.0 * (t12 * iE), m1 = -2.0 * (t02 * iE), m2 = -2.0 * (t01 * iE);
+    const double iE = -2.0 * rcp_fast(f.e0 * t12);
+    const double m0 = t12 * iE, m1 = t02 * iE, m2 = t01 * iE;  // -2/e_r
     const double w0 = f.T0 * f.ir, w1 = f.Q1 * f.ir, w2 = f.P2 * f.ir;  // w_r / 6
     const double u0 = f.P0 * f.il, u1 = f.Q1 * f.il, u2 = f.T2 * f.il;  // w~_r / 6
     const double vr6 = 6.0 * f.vr, vl6 = 6.0 * f.vl;
@@ -240,8 +259,8 @@ struct AdjTap {
   __device__ __forceinline__ void cell(int c, const FastCell2& f) const {
     const int64_t j = j0 + c;
     if (!wt || j >= n) return;
-    const double iE = rcp_fast(f.e0 * f.e1);
-    const double m0 = -2.0 * (f.e1 * iE), m1 = -2.0 * (f.e0 * iE);  // -2/e_r
+    const double iE = -2.0 * rcp_fast(f.e0 * f.e1);
+    const double m0 = f.e1 * iE, m1 = f.e0 * iE;  // -2/e_r
     const double w0 = 4.0 * f.s1 * f.ir, w1 = 2.0 * f.s0 * f.ir;
     const double u0 = 2.0 * f.s1 * f.il, u1 = 4.0 * f.s0 * f.il;
     double* o = wt + j;
@@ -266,8 +285,8 @@ struct AdjTap {
   }
 };
 
-// Reverse of the WENO map from the tape: out[0 .. 2K-2] += d(ar vr + al vl)/dp, as
-// WenoTape<K>::rev.
+// Reverse of the WENO map from the tape: out[0 .. 2K-2] = d(ar vr + al vl)/dp, as
+// WenoTape<K>::rev (which adds to out).
 template <int K>
 __device__ __forceinline__ void rev_tape(const double* __restrict__ wt, int64_t ts, int64_t i,
                                          double ar, double al, double* out) {
@@ -280,23 +299,23 @@ __device__ __forceinline__ void rev_tape(const double* __restrict__ wt, int64_t 
     const double dr0 = al * t[11 * ts], dr1 = al * t[12 * ts], dr2 = al * t[13 * ts];
     const double gA0 = t[14 * ts] * db0, gA1 = t[15 * ts] * db1, gA2 = t[16 * ts] * db2;
     const double gB0 = t[17 * ts] * db0, gB1 = t[18 * ts] * db1, gB2 = t[19 * ts] * db2;
-    out[0] += fma(2.0, dq2, gA2 + gB2 - dr2);
-    out[1] += fma(-7.0, dq2, fma(2.0, dr1, fma(5.0, dr2, fma(-2.0, gA2, fma(-4.0, gB2, gA1 + gB1 - dq1)))));
-    out[2] += fma(2.0, dq0, fma(5.0, dq1 + dr1, fma(11.0, dq2 + dr0, fma(2.0, dr2,
+    out[0] = fma(2.0, dq2, gA2 + gB2 - dr2);
+    out[1] = fma(-7.0, dq2, fma(2.0, dr1, fma(5.0, dr2, fma(-2.0, gA2, fma(-4.0, gB2, gA1 + gB1 - dq1)))));
+    out[2] = fma(2.0, dq0, fma(5.0, dq1 + dr1, fma(11.0, dq2 + dr0, fma(2.0, dr2,
               fma(3.0, gB0 + gB2, fma(-2.0, gA1, gA0 + gA2))))));
-    out[3] += fma(5.0, dq0, fma(2.0, dq1, fma(-7.0, dr0, fma(-2.0, gA0, fma(-4.0, gB0, gA1 - gB1 - dr1)))));
-    out[4] += fma(2.0, dr0, gA0 + gB0 - dq0);
+    out[3] = fma(5.0, dq0, fma(2.0, dq1, fma(-7.0, dr0, fma(-2.0, gA0, fma(-4.0, gB0, gA1 - gB1 - dr1)))));
+    out[4] = fma(2.0, dr0, gA0 + gB0 - dq0);
   } else if constexpr (K == 2) {
     const double db0 = fma(ar, t[2 * ts], al * t[4 * ts]);
     const double db1 = fma(ar, t[3 * ts], al * t[5 * ts]);
     const double dq0 = ar * t[6 * ts], dq1 = ar * t[7 * ts];
     const double dr0 = al * t[8 * ts], dr1 = al * t[9 * ts];
     const double g0 = t[10 * ts] * db0, g1 = t[11 * ts] * db1;
-    out[0] += fma(-0.5, dq1, fma(0.5, dr1, -g1));
-    out[1] += fma(0.5, dq0 + dr1, fma(1.5, dq1 + dr0, g1 - g0));
-    out[2] += fma(0.5, dq0 - dr0, g0);
+    out[0] = fma(-0.5, dq1, fma(0.5, dr1, -g1));
+    out[1] = fma(0.5, dq0 + dr1, fma(1.5, dq1 + dr0, g1 - g0));
+    out[2] = fma(0.5, dq0 - dr0, g0);
   } else {
-    out[0] += ar + al;
+    out[0] = ar + al;
   }
 }
 
@@ -308,7 +327,8 @@ __device__ __forceinline__ void rev_tape(const double* __restrict__ wt, int64_t 
 // taped and untaped passes give the same states.
 // --------------------------------------------------------------------------------------------
 template <int K, int ST, int C, bool TAPE>
-__global__ void __launch_bounds__(256) adj_fwd_kernel(AdjLine A, StageArgs a, double* wt) {
+__global__ void __launch_bounds__(256, TAPE ? HRW_ADJ_TAPE_MINB : HRW_ADJ_FWD_MINB)
+    adj_fwd_kernel(AdjLine A, StageArgs a, double* wt) {
   const LineArgs L = line_args(A);
   const int lane = threadIdx.x & 31;
   const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
@@ -384,12 +404,12 @@ __global__ void __launch_bounds__(NT) adj_vjp_kernel(AdjLine A, const double* __
   constexpr int NCTR = NT + 2 * (K - 1);    // contributors
   __shared__ double sc[NCTR * NS];
   const int64_t s = (int64_t)blockIdx.x * NT;
-  const double idx = A.rdx;
+  const double idx = A.rdx, hidx = 0.5 * A.rdx;
   for (int t = threadIdx.x; t < NCTR; t += NT) {
     const int64_t i = s - (K - 1) + t;
     double o[NS];
 #pragma unroll
-    for (int q = 0; q < NS; ++q) o[q] = 0.0;
+    for (int q = 0; q < NS; ++q) o[q] = 0.0;  // (the taped path assigns them)
     if (i >= 0 && i < A.n) {
       const int64_t s0 = i / A.seg * A.seg, s1 = s0 + A.seg - 1, li = i - s0;
       double p[NS];
@@ -414,16 +434,16 @@ __global__ void __launch_bounds__(NT) adj_vjp_kernel(AdjLine A, const double* __
       if (li < A.seg - 1) {
         const double mp = mu[i + 1];
         const double phi = ((uses_fl(A.bc, li + 1, A.seg) ? mp : 0.0) -
-                            (uses_fr(A.bc, li, A.seg) ? mi : 0.0)) * idx;
-        ar = phi * 0.5 * (dflux(A, vr, li + 1) + A.alpha);
+                            (uses_fr(A.bc, li, A.seg) ? mi : 0.0)) * hidx;  // phi / 2
+        ar = phi * (dflux(A, vr, li + 1) + A.alpha);
       } else if (A.bc == HRW_BC_ZERO_INFLOW) {  // F_{nc+1/2} = f(vr(nc))
         ar = -mi * idx * dflux(A, vr, li + 1);
       }
       if (li > 0) {
         const double mm = mu[i - 1];
         const double phi = ((uses_fl(A.bc, li, A.seg) ? mi : 0.0) -
-                            (uses_fr(A.bc, li - 1, A.seg) ? mm : 0.0)) * idx;
-        al = phi * 0.5 * (dflux(A, vl, li) - A.alpha);
+                            (uses_fr(A.bc, li - 1, A.seg) ? mm : 0.0)) * hidx;
+        al = phi * (dflux(A, vl, li) - A.alpha);
       }
       if constexpr (TAPE) rev_tape<K>(wt, A.n, i, ar, al, o);
       else W.rev(ar, al, o);
@@ -435,11 +455,20 @@ __global__ void __launch_bounds__(NT) adj_vjp_kernel(AdjLine A, const double* __
   const int64_t m = s + threadIdx.x;
   if (m >= A.n) return;
   const int64_t s0 = m / A.seg * A.seg, s1 = s0 + A.seg - 1, lm = m - s0;
-  double w = 0.0;
+  double w;
+  const double* sm = sc + (m - s + (K - 1)) * NS;  // contributor m's entries
+  if (lm >= K - 1 && lm <= A.seg - K) {  // every contributor inside the segment
+    // contributor i = m - o sees m at offset o: sc[(i - first) * NS + o + K - 1]
+    w = sm[(K - 1) * NS];
 #pragma unroll
-  for (int o = -(K - 1); o <= K - 1; ++o) {  // contributor i = m - o sees m at offset o
-    const int64_t i = m - o;
-    if (i >= s0 && i <= s1) w += sc[(i - (s - (K - 1))) * NS + (o + K - 1)];
+    for (int o = -(K - 2); o <= K - 1; ++o) w += sm[-o * NS + (o + K - 1)];
+  } else {
+    w = 0.0;
+#pragma unroll
+    for (int o = -(K - 1); o <= K - 1; ++o) {
+      const int64_t i = m - o;
+      if (i >= s0 && i <= s1) w += sc[(i - (s - (K - 1))) * NS + (o + K - 1)];
+    }
   }
   // ghost positions (outside the segment) clamp onto its end cells
   if (lm == 0) {
@@ -477,7 +506,7 @@ __global__ void __launch_bounds__(NT) adj_vjp_kernel(AdjLine A, const double* __
 // sg sums its chunk of kMisfitChunk cells with compensated (Neumaier) sums per thread and a
 // pairwise tree across the block into part[sg * P + b]; adj_misfit_final adds the P partials.
 constexpr int kMisfitThreads = 256;
-constexpr int64_t kMisfitChunk = 1 << 16;
+constexpr int64_t kMisfitChunk = 1 << 13;
 
 __device__ __forceinline__ void neumaier(double& s, double& c, double x) {
   const double t = s + x;
@@ -528,17 +557,17 @@ cudaError_t fwd_stage_kt(const AdjLine& A, const StageArgs& a, int st, double* w
   return cudaGetLastError();
 }
 
-// taped passes run 4 cells per thread (the tape's intermediates need the registers)
+// taped passes run fewer cells per thread (the tape's intermediates need the registers)
 template <int K>
 cudaError_t fwd_stage_k(const AdjLine& A, const StageArgs& a, int st, double* wt, cudaStream_t s) {
-  if (TapeN<K>::n > 0 && wt) return fwd_stage_kt<K, 4, true>(A, a, st, wt, s);
-  return fwd_stage_kt<K, 8, false>(A, a, st, nullptr, s);
+  if (TapeN<K>::n > 0 && wt) return fwd_stage_kt<K, HRW_ADJ_TAPE_C, true>(A, a, st, wt, s);
+  return fwd_stage_kt<K, HRW_ADJ_FWD_C, false>(A, a, st, nullptr, s);
 }
 
 template <int K, bool TAPE>
 cudaError_t vjp_kt(const AdjLine& A, int mode, const double* v, const double* wt, const double* mu,
                    double* acc, double* out, double dt, cudaStream_t s) {
-  constexpr int NT = 256;
+  constexpr int NT = HRW_ADJ_VJP_NT;
   const unsigned blocks = (unsigned)((A.n + NT - 1) / NT);
   if (mode == ADJ_A3)
     adj_vjp_kernel<K, ADJ_A3, NT, TAPE><<<blocks, NT, 0, s>>>(A, v, wt, mu, acc, out, dt);
@@ -718,12 +747,17 @@ static int adjoint_sweep(hrw_adjoint* h, int mem, const double* u0, const double
                                (double)bytes * nq * (double)h->wtape_stages);
   auto state_need = [&](int64_t e) { return (double)bytes * (3.0 * e + 1.0); };
   auto weno_need = [&](int64_t e) { return (double)bytes * nq * 3.0 * e; };
-  // checkpoint interval: as asked, or (0) the whole trajectory with the WENO tape, else the
-  // whole trajectory's states, else sqrt(nsteps) -- the first that fits the budget
+  // checkpoint interval: as asked, or (0) the first that fits the budget of
+  //   the whole trajectory with the WENO tape (no recompute; the cheapest),
+  //   sqrt(nsteps) segments with the WENO tape (one recompute; the reverse reads the tape),
+  //   the whole trajectory's states without it (no recompute; the reverse recomputes the WENO
+  //   maps -- about as fast as the previous choice, with more memory),
+  //   sqrt(nsteps) segments without it.
   int64_t E = h->every;
   if (E == 0) {
     const int64_t sq = (int64_t)std::ceil(std::sqrt((double)nsteps));
     if (nq > 0 && state_need(nsteps) + weno_need(nsteps) <= budget) E = nsteps;
+    else if (nq > 0 && state_need(sq) + weno_need(sq) <= budget) E = sq;
     else if (state_need(nsteps) <= budget) E = nsteps;
     else E = sq;
   }

@@ -223,17 +223,19 @@ __device__ __forceinline__ void recon_fast(const double* w, double eps, double* 
       }
     }
   } else {
-    // hv(m) = v(m)/2, A(m) = 13/12 (v(m-1) - 2 v(m) + v(m+1))^2, both shared by neighbours.
-    double hv[C + 6], A[C + 2], Dm[C + 2];
-#pragma unroll
-    for (int q = 1; q < C + 5; ++q) hv[q] = 0.5 * w[q];
+    // Per centre q, shared by the three cells whose indicators use it:
+    //   D(q) = v(q-1) - 2 v(q) + v(q+1),  Ae(q) = eps + 13/12 D(q)^2,  H(q) = (v(q-1) - v(q+1))/2.
+    // The indicators' B/2 terms follow from them: E1(j) = H(j), E0(j) = D(j+1) + H(j+1) and
+    // E2(j) = D(j-1) - H(j-1), so that eps + beta_r = E_r^2 + Ae(centre of r).
+    double A[C + 2], Dm[C + 2], Hm[C + 2];
     const double c13 = 13.0 / 12;
 #pragma unroll
     for (int m = 0; m < C + 2; ++m) {  // centre q = m + 2 (cells -1 .. C)
       const int q = m + 2;
       const double D = fma(-2.0, w[q], w[q - 1] + w[q + 1]);
       Dm[m] = D;
-      A[m] = (c13 * D) * D;
+      A[m] = fma(c13 * D, D, eps);
+      Hm[m] = 0.5 * (w[q - 1] - w[q + 1]);
     }
     // candidates x6: V0 = 2v0 + 5v1 - v2, V1 = -v-1 + 5v0 + 2v1, V2 = 2v-2 - 7v-1 + 11v0,
     // W0 = 11v0 - 7v1 + 2v2, W1 = V0 of previous cell, W2 = V1 of previous cell.
@@ -247,13 +249,12 @@ __device__ __forceinline__ void recon_fast(const double* w, double eps, double* 
       const double V2 = fma(11.0, w[q], fma(-7.0, w[q - 1], 2.0 * w[q - 2]));
       const double W0 = fma(11.0, w[q], fma(-7.0, w[q + 1], 2.0 * w[q + 2]));
       const double W1 = V0p, W2 = V1p;
-      const double E0 = fma(1.5, w[q], fma(-2.0, w[q + 1], hv[q + 2]));
-      const double E1 = hv[q - 1] - hv[q + 1];
-      const double E2 = fma(1.5, w[q], fma(-2.0, w[q - 1], hv[q - 2]));
-      const double b0 = fma(E0, E0, A[c + 2]);  // A(j+1)
-      const double b1 = fma(E1, E1, A[c + 1]);  // A(j)
-      const double b2 = fma(E2, E2, A[c]);      // A(j-1)
-      const double e0 = eps + b0, e1 = eps + b1, e2 = eps + b2;
+      const double E0 = Dm[c + 2] + Hm[c + 2];  // centre j+1
+      const double E1 = Hm[c + 1];               // centre j
+      const double E2 = Dm[c] - Hm[c];           // centre j-1
+      const double e0 = fma(E0, E0, A[c + 2]);   // eps + beta0
+      const double e1 = fma(E1, E1, A[c + 1]);
+      const double e2 = fma(E2, E2, A[c]);
       const double s0 = e0 * e0, s1 = e1 * e1, s2 = e2 * e2;
       if (max(max(hiword(s0), hiword(s1)), hiword(s2)) < FastGuard<3>::hi_max) {
         const double P0 = s1 * s2, P1 = s0 * s2, P2 = s0 * s1;

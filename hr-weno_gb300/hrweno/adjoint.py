@@ -40,7 +40,8 @@ def _setup(L):
 
 class adjoint:  # noqa: N801
     """adjoint(problem, nseg=1, checkpoint_every=45): nseg packed problems of ncells each;
-    checkpoint_every=0 keeps the whole trajectory in device memory when it fits."""
+    checkpoint_every=0 picks the segment length from the free device memory (the whole
+    trajectory with the WENO tape when it fits, else sqrt(nsteps) segments)."""
 
     def __init__(self, problem: Problem, nseg: int = 1, checkpoint_every: int = 45):
         L = A.lib()

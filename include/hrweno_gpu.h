@@ -187,11 +187,12 @@ int hrw_batch_destroy(hrw_batch* b);
  * The state holds nseg independent problems of p->ncells[0] cells each (packed; with
  * nseg > 1, ncells must be a multiple of 8); J has one entry per problem.  The reverse sweep
  * recomputes the forward from checkpoints taken every `checkpoint_every` steps (about
- * sqrt(nsteps) is the usual choice); 0 keeps the whole trajectory on the tape when it fits in
- * 80% of the free device memory (no recompute), and falls back to sqrt(nsteps).  The pass
- * that records a segment also records each cell's WENO map derivatives (a WENO tape of 20
- * doubles per cell and stage for k = 3, 12 for k = 2) when they fit the same budget, so the
- * reverse pass does not recompute them. */
+ * sqrt(nsteps) is the usual choice).  The pass that records a segment also records each
+ * cell's WENO-map derivatives (a WENO tape of 20 doubles per cell and stage for k = 3, 12 for
+ * k = 2) when they fit in 80% of the free device memory, so the reverse pass does not
+ * recompute them.  checkpoint_every = 0 picks the first that fits that budget: the whole
+ * trajectory with the WENO tape, sqrt(nsteps) segments with it, the whole trajectory's
+ * states without it, sqrt(nsteps) segments without it. */
 typedef struct hrw_adjoint hrw_adjoint;
 int hrw_adjoint_create(const hrw_problem* p, int nseg, int checkpoint_every, hrw_adjoint** out);
 /* grad = dJ/du0 (nseg * ncells doubles), J[nseg]; arrays in memory space `mem` (J on the host) */
