@@ -240,9 +240,11 @@ __device__ __forceinline__ float flux_diff_interior(const LineF& L, int j, float
 // Stage update of one cell in increment form.  h, l: the state u = h + l; dv: the stored
 // stage increment (d1 or d2, zero for the first stage); dtL = dt L(v); Lv = L(v).
 // Writes the stage output, or the new state pair, as stage kind ST requires.
+// h4, l4v, L4v: the multistep history u^{n-4} = h4 + l4v and L(u^{n-4}) (FC_MS only).
 template <int ST>
-__device__ __forceinline__ void f32c_update(const F32CArgs& a, int64_t j, float h, float l,
-                                            float dv, float dtL, float Lv) {
+__device__ __forceinline__ void f32c_update_h(const F32CArgs& a, int64_t j, float h, float l,
+                                              float dv, float dtL, float Lv, float h4, float l4v,
+                                              float L4v) {
   if constexpr (ST == FC_RHS) {
     a.out[j] = Lv;
   } else if constexpr (ST == FC_E1) {
@@ -258,9 +260,8 @@ __device__ __forceinline__ void f32c_update(const F32CArgs& a, int64_t j, float 
     } else if constexpr (ST == FC_RK3C) {
       inc = (2.f / 3.f) * (dv + dtL);
     } else {  // FC_MS: u' = u + (7 (u4 - u) + 50 dt L + 10 dt L4) / 32
-      const float du4 = (a.hi4[j] - h) + (a.lo4[j] - l);
-      const float l4 = a.l4[j];
-      const float dtl4 = fmaf(a.dt_hi, l4, a.dt_lo * l4);
+      const float du4 = (h4 - h) + (l4v - l);
+      const float dtl4 = fmaf(a.dt_hi, L4v, a.dt_lo * L4v);
       inc = fmaf(7.f / 32.f, du4, fmaf(50.f / 32.f, dtL, (10.f / 32.f) * dtl4));
       a.lout[j] = Lv;
     }
@@ -268,6 +269,13 @@ __device__ __forceinline__ void f32c_update(const F32CArgs& a, int64_t j, float 
     a.hi_out[j] = h;
     a.lo_out[j] = l;
   }
+}
+
+template <int ST>
+__device__ __forceinline__ void f32c_update(const F32CArgs& a, int64_t j, float h, float l,
+                                            float dv, float dtL, float Lv) {
+  if constexpr (ST == FC_MS) f32c_update_h<ST>(a, j, h, l, dv, dtL, Lv, a.hi4[j], a.lo4[j], a.l4[j]);
+  else f32c_update_h<ST>(a, j, h, l, dv, dtL, Lv, 0.f, 0.f, 0.f);
 }
 
 // Warp-synchronous layout (no shared memory): each thread owns C consecutive cells and keeps

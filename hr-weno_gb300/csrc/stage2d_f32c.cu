@@ -10,7 +10,21 @@
 //   dt L = (dt/dx1) (-dF1) + (dt/dx2) (-dF2)
 // carries no cancellation of O(1) fluxes.  Stage kinds and the two-sum state update as the 1D
 // compensated kernel (f32c_update).
+//
+// Loading.  When a row holds a multiple of 4 floats (16-byte row pitch), one thread issues TMA
+// tensor copies (cp.async.bulk.tensor.2d) of the tile plus halo of hi, lo and the stage
+// increment -- a 40 x 38 box at (bx - 4, by - 3), the x origin on a 16-byte boundary -- and,
+// for the multistep stage, of the 32 x 32 history tiles, all completing on one mbarrier; the
+// block then builds its padded compensated tile from shared memory, replicating edge cells
+// into the ghosts (the box reads zeros outside the grid).  Otherwise every thread gathers the
+// tile from global memory.  Both loaders feed the same arithmetic, so both give the same bits.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
+
+#include <cstdint>
+#include <mutex>
+#include <vector>
 
 #include "../../include/hrweno_gpu.h"
 #include "hrw_f32c.cuh"
@@ -21,31 +35,117 @@ namespace hrw {
 namespace {
 
 constexpr int TX = 32, TY = 32, C = 8, NT = 128;
+constexpr int BX = 40, BY = 38;  // TMA box of the tile plus halo: x from bx - 4, y from by - 3
+constexpr int BS = (BY * BX + 31) / 32 * 32;  // its shared-memory stride: 128-byte aligned boxes
 
-template <int K, int ST>
-__global__ void __launch_bounds__(NT) stage2d_f32c_kernel(F32CArgs a) {
+// TMA descriptors of one launch: the tile plus halo of hi, lo and the stage increment, and the
+// 32 x 32 history tiles of the multistep stage
+struct TileMaps {
+  CUtensorMap hi, lo, dv;
+  CUtensorMap h4, l4, L4;
+};
+
+__device__ unsigned int g_tma_timeout;  // set when a block's bounded mbarrier wait ran out
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y,
+                                            uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// Wait for phase 0 of the block's mbarrier, at most `limit` polls; true when it completed.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, int limit) {
+  const uint32_t a = smem_u32(bar);
+  for (int it = 0; it < limit; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0; "
+        "selp.u32 %0, 1, 0, p; }"
+        : "=r"(done)
+        : "r"(a)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+template <int K, int ST, bool TMA, bool HAS_DV>
+__global__ void __launch_bounds__(NT) stage2d_f32c_kernel(const __grid_constant__ TileMaps M,
+                                                          F32CArgs a) {
   constexpr int H = K;
   constexpr int RW = TX + 2 * H, SW = RW + 1, SQ = TX + 1;
   constexpr int NSX = TX / C, NSY = TY / C;
+  constexpr bool MS = ST == FC_MS;
+  constexpr int NB = HAS_DV ? 3 : 2;  // TMA tiles: hi, lo (, increment)
   __shared__ float sh[(TY + 2 * H) * SW];
   __shared__ float sm[(TY + 2 * H) * SW];
   __shared__ float sq[TY * SQ];                                 // x1 part of dt L
   __shared__ float sLx[TY * (NSX + 1)], sRx[TY * (NSX + 1)];  // rl / rr at segment edges
   __shared__ float sLy[(NSY + 1) * TX], sRy[(NSY + 1) * TX];
+  __shared__ alignas(128) float tb[TMA ? NB : 1][TMA ? BS : 1];
+  __shared__ alignas(128) float hb[TMA && MS ? 3 : 1][TMA && MS ? TX * TY : 1];
+  __shared__ alignas(8) uint64_t bar;
   const LineF& L1 = a.L;
   const LineF& L2 = a.L2;
-  const int64_t n1 = L1.nc, n2 = L2.nc, ld = a.ld;
-  const int64_t bx = (int64_t)blockIdx.x * TX, by = (int64_t)blockIdx.y * TY;
+  const int n1 = L1.nc, n2 = L2.nc;
+  const int64_t ld = a.ld;
+  const int bx = blockIdx.x * TX, by = blockIdx.y * TY;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
-  for (int q = tid; q < (TY + 2 * H) * RW; q += NT) {
-    const int row = q / RW, col = q - row * RW;
-    int64_t gy = by - H + row, gx = bx - H + col;
-    gy = gy < 0 ? 0 : (gy >= n2 ? n2 - 1 : gy);
-    gx = gx < 0 ? 0 : (gx >= n1 ? n1 - 1 : gx);
-    const int64_t g = gy * ld + gx;
-    sh[row * SW + col] = a.hi[g];
-    sm[row * SW + col] = a.dv ? a.lo[g] + a.dv[g] : a.lo[g];
+  if constexpr (TMA) {
+    if (tid == 0) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bar)) : "memory");
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (tid == 0) {
+      constexpr uint32_t bytes = NB * BY * BX * 4 + (MS ? 3 * TX * TY * 4 : 0);
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(&bar)),
+                   "r"(bytes)
+                   : "memory");
+      tma_load_2d(tb[0], &M.hi, bx - 4, by - 3, &bar);
+      tma_load_2d(tb[1], &M.lo, bx - 4, by - 3, &bar);
+      if constexpr (HAS_DV) tma_load_2d(tb[NB - 1], &M.dv, bx - 4, by - 3, &bar);
+      if constexpr (MS) {
+        tma_load_2d(hb[0], &M.h4, bx, by, &bar);
+        tma_load_2d(hb[1], &M.l4, bx, by, &bar);
+        tma_load_2d(hb[2], &M.L4, bx, by, &bar);
+      }
+    }
+    // bounded wait; on a timeout every thread of the block learns of it, the block waits
+    // (bounded again) for its copies to land and leaves, and the host sees the flag
+    const bool ok = mbar_wait(&bar, 1 << 20);
+    if (__syncthreads_or(!ok)) {
+      if (tid == 0) atomicExch(&g_tma_timeout, 1u);
+      mbar_wait(&bar, 1 << 20);
+      return;
+    }
+    for (int q = tid; q < (TY + 2 * H) * RW; q += NT) {
+      const int row = q / RW, col = q - row * RW;
+      int gy = by - H + row, gx = bx - H + col;
+      gy = gy < 0 ? 0 : (gy >= n2 ? n2 - 1 : gy);
+      gx = gx < 0 ? 0 : (gx >= n1 ? n1 - 1 : gx);
+      const int src = (gy - (by - 3)) * BX + (gx - (bx - 4));
+      sh[row * SW + col] = tb[0][src];
+      sm[row * SW + col] = HAS_DV ? tb[1][src] + tb[NB - 1][src] : tb[1][src];
+    }
+  } else {
+    for (int q = tid; q < (TY + 2 * H) * RW; q += NT) {
+      const int row = q / RW, col = q - row * RW;
+      int gy = by - H + row, gx = bx - H + col;
+      gy = gy < 0 ? 0 : (gy >= n2 ? n2 - 1 : gy);
+      gx = gx < 0 ? 0 : (gx >= n1 ? n1 - 1 : gx);
+      const int64_t g = gy * ld + gx;
+      sh[row * SW + col] = a.hi[g];
+      sm[row * SW + col] = HAS_DV ? a.lo[g] + a.dv[g] : a.lo[g];
+    }
   }
   __syncthreads();
 
@@ -90,10 +190,10 @@ __global__ void __launch_bounds__(NT) stage2d_f32c_kernel(F32CArgs a) {
 
   // ---- x1 flux differences -> dt/dx1 (-dF1) in shared memory -----------------------------------
   {
-    const int64_t j0 = bx + sg * C;
+    const int j0 = bx + sg * C;
 #pragma unroll
     for (int c = 0; c < C; ++c) {
-      const int64_t gx = j0 + c;
+      const int gx = j0 + c;
       float t = 0.f;
       if (gx < n1) {
         const int lj = (r + H) * SW + H + sg * C + c;
@@ -124,12 +224,12 @@ __global__ void __launch_bounds__(NT) stage2d_f32c_kernel(F32CArgs a) {
   __syncthreads();
 
   // ---- x2 flux differences, dt L and the stage update ------------------------------------------
-  const int64_t gx = bx + col;
+  const int gx = bx + col;
   if (gx >= n1) return;
-  const int64_t j0 = by + sy * C;
+  const int j0 = by + sy * C;
 #pragma unroll
   for (int c = 0; c < C; ++c) {
-    const int64_t gy = j0 + c;
+    const int gy = j0 + c;
     if (gy >= n2) break;
     const int ly = sy * C + c;
     const int lj = (ly + H) * SW + H + col;
@@ -143,17 +243,101 @@ __global__ void __launch_bounds__(NT) stage2d_f32c_kernel(F32CArgs a) {
     const float dtL = fmaf(a.c_hi, q1, fmaf(a.c_lo, q1, fmaf(a.c2_hi, q2, a.c2_lo * q2)));
     const float Lv = fmaf(q1, a.lscale, q2 * a.lscale2);
     const int64_t j = gy * ld + gx;
-    const float h = a.hi[j], l = a.lo[j];
-    const float dv = a.dv ? a.dv[j] : 0.f;
-    f32c_update<ST>(a, j, h, l, dv, dtL, Lv);
+    if constexpr (TMA) {
+      const int src = (ly + 3) * BX + col + 4;  // the cell in the halo box
+      const float h = tb[0][src], l = tb[1][src];
+      const float dv = HAS_DV ? tb[NB - 1][src] : 0.f;
+      if constexpr (MS)
+        f32c_update_h<ST>(a, j, h, l, dv, dtL, Lv, hb[0][ly * TX + col], hb[1][ly * TX + col],
+                          hb[2][ly * TX + col]);
+      else
+        f32c_update_h<ST>(a, j, h, l, dv, dtL, Lv, 0.f, 0.f, 0.f);
+    } else {
+      const float h = a.hi[j], l = a.lo[j];
+      const float dv = HAS_DV ? a.dv[j] : 0.f;
+      f32c_update<ST>(a, j, h, l, dv, dtL, Lv);
+    }
   }
+}
+
+// ---- TMA descriptors: encoded through the driver entry point, cached by array -----------------
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      p = nullptr;
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }();
+  return fn;
+}
+
+struct MapEntry {
+  const void* p;
+  int n1, n2, box_x, box_y;
+  CUtensorMap map;
+};
+
+// A float array of n2 rows of n1 values (row pitch n1 floats) as a 2D tensor with a
+// box_x x box_y box; false when it cannot be described (pitch or address not 16-byte aligned).
+bool tile_map(const float* p, int n1, int n2, int box_x, int box_y, CUtensorMap* out) {
+  static std::mutex mu;
+  static std::vector<MapEntry> cache;
+  if (n1 % 4 != 0 || (reinterpret_cast<uintptr_t>(p) & 15) != 0) return false;
+  std::lock_guard<std::mutex> lock(mu);
+  for (const MapEntry& e : cache)
+    if (e.p == p && e.n1 == n1 && e.n2 == n2 && e.box_x == box_x && e.box_y == box_y) {
+      *out = e.map;
+      return true;
+    }
+  const auto fn = encode_fn();
+  if (!fn) return false;
+  MapEntry e{p, n1, n2, box_x, box_y, {}};
+  const cuuint64_t dim[2] = {(cuuint64_t)n1, (cuuint64_t)n2};
+  const cuuint64_t stride[1] = {(cuuint64_t)n1 * sizeof(float)};
+  const cuuint32_t box[2] = {(cuuint32_t)box_x, (cuuint32_t)box_y};
+  const cuuint32_t estride[2] = {1, 1};
+  if (fn(&e.map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(p), dim, stride, box, estride,
+         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+    return false;
+  if (cache.size() >= 256) cache.erase(cache.begin());
+  cache.push_back(e);
+  *out = e.map;
+  return true;
+}
+
+template <int K, int ST, bool TMA, bool HAS_DV>
+cudaError_t launch_kt(const TileMaps& M, const F32CArgs& a, cudaStream_t s) {
+  const dim3 grid((unsigned)((a.L.nc + TX - 1) / TX), (unsigned)((a.L2.nc + TY - 1) / TY));
+  stage2d_f32c_kernel<K, ST, TMA, HAS_DV><<<grid, NT, 0, s>>>(M, a);
+  return cudaGetLastError();
 }
 
 template <int K, int ST>
 cudaError_t launch_k(const F32CArgs& a, cudaStream_t s) {
-  const dim3 grid((unsigned)((a.L.nc + TX - 1) / TX), (unsigned)((a.L2.nc + TY - 1) / TY));
-  stage2d_f32c_kernel<K, ST><<<grid, NT, 0, s>>>(a);
-  return cudaGetLastError();
+  constexpr bool MS = ST == FC_MS;
+  TileMaps M{};
+  const int n1 = a.L.nc, n2 = a.L2.nc;
+  const bool tma = n1 == a.ld && tile_map(a.hi, n1, n2, BX, BY, &M.hi) &&
+                   tile_map(a.lo, n1, n2, BX, BY, &M.lo) &&
+                   (!a.dv || tile_map(a.dv, n1, n2, BX, BY, &M.dv)) &&
+                   (!MS || (tile_map(a.hi4, n1, n2, TX, TY, &M.h4) &&
+                            tile_map(a.lo4, n1, n2, TX, TY, &M.l4) &&
+                            tile_map(a.l4, n1, n2, TX, TY, &M.L4)));
+  if constexpr (MS) {  // the multistep stage has no stage increment
+    if (a.dv) return cudaErrorInvalidValue;
+    return tma ? launch_kt<K, ST, true, false>(M, a, s) : launch_kt<K, ST, false, false>(M, a, s);
+  } else {
+    if (tma) {
+      if (a.dv) return launch_kt<K, ST, true, true>(M, a, s);
+      return launch_kt<K, ST, true, false>(M, a, s);
+    }
+    if (a.dv) return launch_kt<K, ST, false, true>(M, a, s);
+    return launch_kt<K, ST, false, false>(M, a, s);
+  }
 }
 
 template <int K>
@@ -178,6 +362,16 @@ cudaError_t launch_stage2d_f32c(const F32CArgs& a, int k, int stage, cudaStream_
   if (k == 1) return launch_st<1>(a, stage, s);
   if (k == 2) return launch_st<2>(a, stage, s);
   return launch_st<3>(a, stage, s);
+}
+
+// Whether a block of a 2D compensated stage gave up waiting for its tile copies since the
+// last call (and clear the flag).  Synchronises with the device.
+cudaError_t stage2d_f32c_timed_out(bool* timed_out) {
+  unsigned int v = 0, zero = 0;
+  cudaError_t e = cudaMemcpyFromSymbol(&v, g_tma_timeout, sizeof(v));
+  if (e == cudaSuccess && v) e = cudaMemcpyToSymbol(g_tma_timeout, &zero, sizeof(zero));
+  *timed_out = v != 0;
+  return e;
 }
 
 }  // namespace hrw

@@ -121,7 +121,9 @@ def test_f32c_full_size_vs_fp64_gpu(hw):
     # with zero flux difference at both boundary cells
 
 
-@pytest.mark.parametrize("shape", [(1, 1), (5, 7), (31, 33), (64, 40), (100, 37)])
+# rows of a multiple of 4 floats take the TMA tile loader, the others the gathering loader
+@pytest.mark.parametrize("shape", [(1, 1), (5, 7), (31, 33), (64, 40), (100, 37), (4, 9), (36, 70),
+                                   (128, 3)])
 @pytest.mark.parametrize("k", [1, 2, 3])
 @pytest.mark.parametrize("bc", ["zero_inflow", "zero", "copy"])
 def test_rhs_f32c_2d(hw, orc, shape, k, bc):
@@ -137,9 +139,10 @@ def test_rhs_f32c_2d(hw, orc, shape, k, bc):
         assert np.max(np.abs(got - ref)) <= 2e-6 * scale, (shape, k, bc, flux)
 
 
-def test_f32c_mstvd_2d_vs_oracle(hw, orc):
+@pytest.mark.parametrize("shape", [(96, 80), (90, 70)])
+def test_f32c_mstvd_2d_vs_oracle(hw, orc, shape):
     from hrweno import workloads
-    n1, n2 = 96, 80
+    n1, n2 = shape
     prob, n0, dt = workloads.pbe_config(n1, n2)
     g, o = hw.mstvd(prob, n1 * n2, dtype="f32c"), orc.ODE(prob, n1 * n2, 1)
     u32, u64 = n0.copy(), n0.copy()
