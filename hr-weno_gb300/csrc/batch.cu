@@ -22,7 +22,7 @@
 #include "../../include/hrweno_gpu.h"
 #include "hrw_batch.h"
 #include "hrw_device.cuh"
-#include "hrw_f32c.cuh"
+#include "hrw_batch_dev.cuh"
 #include "hrw_internal.h"
 #include "hrw_stage.cuh"
 
@@ -31,19 +31,8 @@ namespace hrw {
 namespace {
 
 constexpr unsigned FULL = 0xffffffffu;
-constexpr int NT = 256;  // threads per block; a block holds NT / G groups
+constexpr int NT = kBatchThreads;
 
-template <int G>
-__device__ __forceinline__ void group_sync(int gid) {
-  if constexpr (G == 32) {
-    __syncwarp();
-  } else if constexpr (G == NT) {
-    __syncthreads();
-  } else {
-    // named barrier gid + 1 (barrier 0 is __syncthreads), G threads of whole warps
-    asm volatile("bar.sync %0, %1;" ::"r"(gid + 1), "r"(G) : "memory");
-  }
-}
 
 // One warp-pass of stage ST over cells j0 .. j0 + C - 1 of this lane (all 32 lanes call it).
 template <int K, int ST, bool STRICT, int C>
@@ -178,134 +167,8 @@ int occupancy() {
   return n;
 }
 
-// ---- compensated FP32 batches ----------------------------------------------------------------
-__device__ __forceinline__ void split_scalar(double x, float& hi, float& lo) {
-  hi = __double2float_rn(x);
-  lo = __double2float_rn(x - (double)hi);
-}
-
-template <int K, int ST, int G, int C>
-__device__ __forceinline__ void f32c_sweep(const F32CArgs& a, int lt, int gid) {
-  const int lane = lt & 31;
-  const int warp_in_group = lt >> 5;
-  for (int64_t base = 0; base < a.L.nc; base += (int64_t)G * C) {
-    const int64_t wbase = base + (int64_t)warp_in_group * 32 * C;
-    if (wbase < a.L.nc) f32c_pass<K, ST, C>(a, wbase + (int64_t)lane * C, lane);
-  }
-  group_sync<G>(gid);
-}
-
-// all steps of one problem in the increment form of the compensated kernels (stage1d_f32c.cu):
-// the state ping-pongs between slots 0 and 1 and ends in slot 0
-template <int K, int G, int C>
-__device__ void run_problem_f32c(const BatchArgs& B, const BatchProblem& P, int lt, int gid) {
-  F32CArgs a{};
-  a.eps = (float)P.eps;
-  a.L.nc = P.nc;
-  a.L.fn = P.fn;
-  a.L.bc = P.bc;
-  a.L.flux = P.flux;
-  a.L.a = (float)P.a;
-  a.L.b = (float)P.b;
-  a.L.alpha = (float)P.alpha;
-  a.L.xmin = (float)P.xmin;
-  a.L.rx = (float)P.rx;
-  a.L.gstep = (float)(P.b * P.rx);
-  a.L.rw = nullptr;
-  split_scalar(P.dt / P.rx, a.c_hi, a.c_lo);
-  split_scalar(P.dt, a.dt_hi, a.dt_lo);
-  a.lscale = (float)(1.0 / P.rx);
-  float* const h0 = B.fhi[0] + P.off;
-  float* const h1 = B.fhi[1] + P.off;
-  float* const l0 = B.flo[0] + P.off;
-  float* const l1 = B.flo[1] + P.off;
-  float* d1 = B.fd1 + P.off;
-  float* d2 = B.fd2 + P.off;
-  int slot = 0;
-  for (int64_t n = 0; n < P.nsteps; ++n) {
-    a.hi = slot ? h1 : h0, a.lo = slot ? l1 : l0;
-    a.hi_out = slot ? h0 : h1, a.lo_out = slot ? l0 : l1;
-    if (B.order == 1) {
-      a.dv = nullptr;
-      f32c_sweep<K, FC_RK1, G, C>(a, lt, gid);
-    } else {
-      a.dv = nullptr, a.out = d1;
-      f32c_sweep<K, FC_E1, G, C>(a, lt, gid);
-      if (B.order == 2) {
-        a.dv = d1;
-        f32c_sweep<K, FC_RK2B, G, C>(a, lt, gid);
-      } else {
-        a.dv = d1, a.out = d2;
-        f32c_sweep<K, FC_RK3B, G, C>(a, lt, gid);
-        a.dv = d2;
-        f32c_sweep<K, FC_RK3C, G, C>(a, lt, gid);
-      }
-    }
-    slot = 1 - slot;
-  }
-  if (slot == 1) {
-    for (int64_t j = lt; j < P.nc; j += G) h0[j] = h1[j], l0[j] = l1[j];
-    group_sync<G>(gid);
-  }
-}
-
-template <int G, int C>
-__global__ void __launch_bounds__(NT, 1) batch_f32c_kernel(BatchArgs B) {
-  static_assert(NT % G == 0 && G % 32 == 0 && NT / G <= 15, "groups of whole warps");
-  constexpr int GPB = NT / G;
-  __shared__ int s_pid[GPB];
-  const int gid = threadIdx.x / G, lt = threadIdx.x % G;
-  for (;;) {
-    if (lt == 0) s_pid[gid] = atomicAdd(B.counter, 1);
-    group_sync<G>(gid);
-    const int pid = s_pid[gid];
-    group_sync<G>(gid);
-    if (pid >= B.nprob) break;
-    const BatchProblem P = B.probs[B.order_idx[pid]];
-    if (P.nsteps <= 0) continue;
-    if (P.k == 3) run_problem_f32c<3, G, C>(B, P, lt, gid);
-    else if (P.k == 2) run_problem_f32c<2, G, C>(B, P, lt, gid);
-    else run_problem_f32c<1, G, C>(B, P, lt, gid);
-  }
-}
-
-template <int G, int C>
-int occupancy_f32() {
-  int n = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_f32c_kernel<G, C>, NT, 0);
-  return n;
-}
-
 }  // namespace
 
-const BatchShape kBatchShapesF32[kNumBatchShapes] = {{32, 4}, {32, 8}, {64, 8}, {128, 4}, {128, 8}, {256, 8}};
-
-int batch_f32_blocks_per_sm(int shape) {
-  switch (shape) {
-    case 0: return occupancy_f32<32, 4>();
-    case 1: return occupancy_f32<32, 8>();
-    case 2: return occupancy_f32<64, 8>();
-    case 3: return occupancy_f32<128, 4>();
-    case 4: return occupancy_f32<128, 8>();
-    default: return occupancy_f32<256, 8>();
-  }
-}
-
-cudaError_t launch_batch_f32c(const BatchArgs& B, int shape, int blocks, cudaStream_t s) {
-  if (B.nprob <= 0) return cudaSuccess;
-  switch (shape) {
-    case 0: batch_f32c_kernel<32, 4><<<blocks, NT, 0, s>>>(B); break;
-    case 1: batch_f32c_kernel<32, 8><<<blocks, NT, 0, s>>>(B); break;
-    case 2: batch_f32c_kernel<64, 8><<<blocks, NT, 0, s>>>(B); break;
-    case 3: batch_f32c_kernel<128, 4><<<blocks, NT, 0, s>>>(B); break;
-    case 4: batch_f32c_kernel<128, 8><<<blocks, NT, 0, s>>>(B); break;
-    case 5: batch_f32c_kernel<256, 8><<<blocks, NT, 0, s>>>(B); break;
-    default: return cudaErrorInvalidValue;
-  }
-  return cudaGetLastError();
-}
-
-// Shapes the autotuner chooses from: {group threads, cells per thread}.
 const BatchShape kBatchShapes[kNumBatchShapes] = {{32, 2}, {32, 4}, {32, 8}, {128, 4}, {128, 8}, {256, 8}};
 
 int batch_blocks_per_sm(int shape, bool strict) {

@@ -1,0 +1,159 @@
+// batch_f32c.cu - the batched solver (batch.cu) in the compensated FP32 form (hrw_f32c.cuh):
+// the same persistent grid of groups and the same queue of problems, each group advancing its
+// problem through every step with the warp pass of the single-line compensated kernel.
+//
+// A step's stages run one copy of the pass with the stage kind as a run-time value, and the
+// numerical flux is resolved once per problem (a template argument; Burgers or linear is a
+// warp-uniform branch): per-stage and per-flux-kind copies of the pass inside one persistent
+// kernel overflow the instruction cache, and its groups run different problems at once.  The
+// arithmetic of every stage is that of the single-line kernel, so batched and single-line
+// solves give the same bits.
+#include <cuda_runtime.h>
+
+#include "../../include/hrweno_gpu.h"
+#include "hrw_batch.h"
+#include "hrw_batch_dev.cuh"
+#include "hrw_f32c.cuh"
+#include "hrw_internal.h"
+
+namespace hrw {
+
+namespace {
+
+constexpr int NT = kBatchThreads;
+
+// ---- compensated FP32 batches ----------------------------------------------------------------
+__device__ __forceinline__ void split_scalar(double x, float& hi, float& lo) {
+  hi = __double2float_rn(x);
+  lo = __double2float_rn(x - (double)hi);
+}
+
+template <int K, int G, int C, int FK>
+__device__ __forceinline__ void f32c_sweep(const F32CArgs& a, int lt, int gid, int stage) {
+  const int lane = lt & 31;
+  const int warp_in_group = lt >> 5;
+  for (int64_t base = 0; base < a.L.nc; base += (int64_t)G * C) {
+    const int64_t wbase = base + (int64_t)warp_in_group * 32 * C;
+    if (wbase < a.L.nc) f32c_pass<K, -1, C, FK>(a, wbase + (int64_t)lane * C, lane, stage);
+  }
+  group_sync<G>(gid);
+}
+
+// all steps of one problem in the increment form of the compensated kernels (stage1d_f32c.cu):
+// the state ping-pongs between slots 0 and 1 and ends in slot 0
+// FK: the problem's flux kind as flux_g_t takes it (4 or 5 here: the numerical flux fixed, the
+// flux function chosen at run time), or -1 (resolved per call)
+template <int K, int G, int C, int FK>
+__device__ void run_problem_f32c(const BatchArgs& B, const BatchProblem& P, int lt, int gid,
+                                 F32CArgs& a) {
+  // a: this group's arguments in shared memory (registers stay free for the warp pass);
+  // thread 0 of the group writes them between sweeps, each sweep ends with a group barrier
+  float* const h0 = B.fhi[0] + P.off;
+  float* const h1 = B.fhi[1] + P.off;
+  float* const l0 = B.flo[0] + P.off;
+  float* const l1 = B.flo[1] + P.off;
+  float* const d1 = B.fd1 + P.off;
+  float* const d2 = B.fd2 + P.off;
+  if (lt == 0) {
+    a = F32CArgs{};
+    a.eps = (float)P.eps;
+    a.L.nc = P.nc;
+    a.L.fn = P.fn;
+    a.L.bc = P.bc;
+    a.L.flux = P.flux;
+    a.L.a = (float)P.a;
+    a.L.b = (float)P.b;
+    a.L.alpha = (float)P.alpha;
+    a.L.xmin = (float)P.xmin;
+    a.L.rx = (float)P.rx;
+    a.L.gstep = (float)(P.b * P.rx);
+    a.L.rw = nullptr;
+    split_scalar(P.dt / P.rx, a.c_hi, a.c_lo);
+    split_scalar(P.dt, a.dt_hi, a.dt_lo);
+    a.lscale = (float)(1.0 / P.rx);
+  }
+  // the step's stages in order, each one sweep through the single call site below (one copy of
+  // the pass serves them all): order 1: RK1; 2: E1, RK2B; 3: E1, RK3B, RK3C
+  const int nst = B.order < 1 ? 1 : (B.order > 3 ? 3 : B.order);
+  int slot = 0;
+  for (int64_t n = 0; n < P.nsteps; ++n) {
+    for (int k = 0; k < nst; ++k) {
+      const int st = nst == 1 ? FC_RK1 : (k == 0 ? FC_E1 : (nst == 2 ? FC_RK2B : (k == 1 ? FC_RK3B : FC_RK3C)));
+      if (lt == 0) {
+        a.hi = slot ? h1 : h0, a.lo = slot ? l1 : l0;
+        a.hi_out = slot ? h0 : h1, a.lo_out = slot ? l0 : l1;
+        a.dv = k == 0 ? nullptr : (k == 1 ? d1 : d2);
+        a.out = k == 0 ? d1 : d2;  // (the last stage writes the state pair instead)
+      }
+      group_sync<G>(gid);
+      f32c_sweep<K, G, C, FK>(a, lt, gid, st);
+    }
+    slot = 1 - slot;
+  }
+  if (slot == 1) {
+    for (int64_t j = lt; j < P.nc; j += G) h0[j] = h1[j], l0[j] = l1[j];
+    group_sync<G>(gid);
+  }
+}
+
+template <int G, int C>
+__global__ void __launch_bounds__(NT, C == 4 ? 3 : 2) batch_f32c_kernel(BatchArgs B) {
+  static_assert(NT % G == 0 && G % 32 == 0 && NT / G <= 15, "groups of whole warps");
+  constexpr int GPB = NT / G;
+  __shared__ int s_pid[GPB];
+  __shared__ F32CArgs s_args[GPB];
+  const int gid = threadIdx.x / G, lt = threadIdx.x % G;
+  for (;;) {
+    if (lt == 0) s_pid[gid] = atomicAdd(B.counter, 1);
+    group_sync<G>(gid);
+    const int pid = s_pid[gid];
+    group_sync<G>(gid);
+    if (pid >= B.nprob) break;
+    const BatchProblem P = B.probs[B.order_idx[pid]];
+    if (P.nsteps <= 0) continue;
+    // one copy of the pass per (k, numerical flux); Burgers or linear is a uniform branch
+    const bool god = P.flux != HRW_FLUX_LAX_FRIEDRICHS;
+    F32CArgs& a = s_args[gid];
+    if (P.k == 3) {
+      if (!god) run_problem_f32c<3, G, C, 4>(B, P, lt, gid, a);
+      else run_problem_f32c<3, G, C, 5>(B, P, lt, gid, a);
+    } else if (P.k == 2) {
+      if (!god) run_problem_f32c<2, G, C, 4>(B, P, lt, gid, a);
+      else run_problem_f32c<2, G, C, 5>(B, P, lt, gid, a);
+    } else {
+      run_problem_f32c<1, G, C, -1>(B, P, lt, gid, a);
+    }
+  }
+}
+
+template <int G, int C>
+int occupancy_f32() {
+  int n = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_f32c_kernel<G, C>, NT, 0);
+  return n;
+}
+
+}  // namespace
+
+const BatchShape kBatchShapesF32[kNumBatchShapesF32] = {{64, 4}, {128, 4}, {256, 4}};
+
+int batch_f32_blocks_per_sm(int shape) {
+  switch (shape) {
+    case 0: return occupancy_f32<64, 4>();
+    case 1: return occupancy_f32<128, 4>();
+    default: return occupancy_f32<256, 4>();
+  }
+}
+
+cudaError_t launch_batch_f32c(const BatchArgs& B, int shape, int blocks, cudaStream_t s) {
+  if (B.nprob <= 0) return cudaSuccess;
+  switch (shape) {
+    case 0: batch_f32c_kernel<64, 4><<<blocks, NT, 0, s>>>(B); break;
+    case 1: batch_f32c_kernel<128, 4><<<blocks, NT, 0, s>>>(B); break;
+    case 2: batch_f32c_kernel<256, 4><<<blocks, NT, 0, s>>>(B); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace hrw

@@ -29,6 +29,8 @@ constexpr int64_t kClassHi[kClasses] = {512, 4096, INT64_MAX};
 // shapes used before (or without) tuning: one warp with 4 cells per thread for short lines,
 // one warp with 8 for medium ones, a 256-thread block with 8 for long ones
 constexpr int kDefaultShape[kClasses] = {1, 2, 5};
+// compensated FP32 (kBatchShapesF32): 128 threads x 4 cells for short lines, 256 x 4 otherwise
+constexpr int kDefaultShapeF32[kClasses] = {1, 2, 2};
 
 bool is_done(double t, double tout, double dt) { return (t - tout) * std::copysign(1.0, dt) > 0.0; }
 
@@ -181,6 +183,8 @@ int hrw_batch_create(const hrw_problem* probs, int nprob, int order, int dtype, 
   b->nprob = nprob;
   b->order = order;
   b->dtype = dtype;
+  if (dtype == HRW_F32C)
+    for (int c = 0; c < kClasses; ++c) b->shape[c] = kDefaultShapeF32[c];
   b->strict = probs[0].numerics == HRW_NUMERICS_STRICT;
   b->off.resize(nprob + 1);
   int64_t off = 0;
@@ -370,7 +374,7 @@ int hrw_batch_tune(hrw_batch* b, int mem, const double* u, const double* dt, int
     std::string k;
     int s;
     while (in >> k >> s)
-      if (s >= 0 && s < kNumBatchShapes) cache.emplace_back(k, s);
+      if (s >= 0 && s < (b->dtype == HRW_F32C ? kNumBatchShapesF32 : kNumBatchShapes)) cache.emplace_back(k, s);
   }
   const size_t bytes = sizeof(double) * (size_t)b->total;
   HRW_BCUDA(cudaMemcpyAsync(b->u, u, bytes,
@@ -397,8 +401,9 @@ int hrw_batch_tune(hrw_batch* b, int mem, const double* u, const double* dt, int
     }
     for (int p : b->members[c]) b->probs[p].nsteps = probe_steps;
     float best = 1e30f;
-    int best_s = kDefaultShape[c];
-    for (int s = 0; s < kNumBatchShapes; ++s) {
+    const bool f32 = b->dtype == HRW_F32C;
+    int best_s = f32 ? kDefaultShapeF32[c] : kDefaultShape[c];
+    for (int s = 0; s < (f32 ? kNumBatchShapesF32 : kNumBatchShapes); ++s) {
       int shapes[kClasses] = {b->shape[0], b->shape[1], b->shape[2]};
       shapes[c] = s;
       float ms = 0.f;

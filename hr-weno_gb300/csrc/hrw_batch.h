@@ -44,7 +44,8 @@ int batch_blocks_per_sm(int shape, bool strict);
 cudaError_t launch_batch(const BatchArgs& B, int shape, bool strict, int blocks, cudaStream_t s);
 
 // compensated FP32 batches: their own shapes (cells per thread a multiple of 4)
-extern const BatchShape kBatchShapesF32[kNumBatchShapes];
+constexpr int kNumBatchShapesF32 = 3;
+extern const BatchShape kBatchShapesF32[kNumBatchShapesF32];
 int batch_f32_blocks_per_sm(int shape);
 cudaError_t launch_batch_f32c(const BatchArgs& B, int shape, int blocks, cudaStream_t s);
 

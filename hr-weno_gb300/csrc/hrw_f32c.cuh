@@ -156,10 +156,13 @@ __device__ __forceinline__ void recon_diff3_shared(const float* d, float t0, flo
 // the two interface fluxes that cancels in the cell's flux difference.
 //   Lax-Friedrichs (src/hrweno_fluxes.f90:43), Godunov (:67-74).
 // ---------------------------------------------------------------------------------------------
-// Flux kind as a compile-time constant: FK = 2 * (fn == LINEAR) + (flux == GODUNOV).
+// Flux kind as a compile-time constant: FK = 2 * (fn == LINEAR) + (flux == GODUNOV), or
+// FK = 4 + (flux == GODUNOV) with the flux function (Burgers or linear) chosen at run time.
 template <int FK>
 __device__ __forceinline__ float flux_g_t(const LineF& L, float v, float a, float b, float g) {
-  if constexpr (FK == 0) {  // Burgers, LF: 4F - 2v^2 = a(2v + a + 2 alpha) + b(2v + b - 2 alpha)
+  if constexpr (FK >= 4) {
+    return L.fn == HRW_FN_BURGERS ? flux_g_t<FK - 4>(L, v, a, b, g) : flux_g_t<FK - 2>(L, v, a, b, g);
+  } else if constexpr (FK == 0) {  // Burgers, LF: 4F - 2v^2 = a(2v + a + 2 alpha) + b(2v + b - 2 alpha)
     return 0.25f * fmaf(a, 2.f * v + a + 2.f * L.alpha, b * (2.f * v + b - 2.f * L.alpha));
   } else if constexpr (FK == 1) {  // Burgers, Godunov: 2F - v^2 = a(2v + a) or b(2v + b)
     const float fa = a * (2.f * v + a), fb = b * (2.f * v + b);
@@ -222,13 +225,22 @@ __device__ __forceinline__ float flux_diff_f32c(const LineF& L, int64_t j, float
   return __fadd_rn(GR - GL, extra);  // never contracted with gstep * v: one rounding order
 }
 
+// flux_diff_f32c out of line: the warp pass's path for the few threads whose cells touch a
+// line end (inlining it into every cell of every specialised pass costs instruction cache
+// and compile time for nothing)
+static __device__ __noinline__ float flux_diff_f32c_call(const LineF& L, int j, float v, float rr_m,
+                                                  float d_m, float rl_j, float rr_j, float d_j,
+                                                  float rl_p) {
+  return flux_diff_f32c(L, j, v, rr_m, d_m, rl_j, rr_j, d_j, rl_p);
+}
+
 // flux_diff_f32c of a cell that touches no boundary, flux kind known at compile time (the same
 // operations as flux_diff_f32c's interior branch, so both give the same bits)
 template <int FK>
 __device__ __forceinline__ float flux_diff_interior(const LineF& L, int j, float v, float rr_m,
                                                     float d_m, float rl_j, float rr_j, float d_j,
                                                     float rl_p) {
-  constexpr bool lin = FK >= 2;
+  const bool lin = FK >= 4 ? L.fn != HRW_FN_BURGERS : FK >= 2;
   const float gL = lin ? g_at(L, j) : 0.f;
   const float gR = lin ? g_at(L, j + 1) : 0.f;
   const float GL = flux_g_t<FK>(L, v, rr_m - d_m, rl_j, gL);
@@ -313,8 +325,16 @@ __device__ __forceinline__ void store_cells(float* __restrict__ p, int j0, int n
 // One warp-pass: lane `lane` handles cells j0 .. j0 + C - 1 of the line a.L (all 32 lanes of
 // the warp call it with consecutive j0 = base + lane * C).  FK: the flux kind when known at
 // compile time, or -1.  Cell indices are 32-bit (lines of < 2^31 cells).
+// ST = -1: the stage kind is the run-time (warp-uniform) `st`, one of the rktvd stages
+// FC_RK1 .. FC_RK3C; one copy of the pass then serves every stage of a step (the batched
+// kernel runs all stages of a problem in one launch, and per-stage copies would not fit the
+// instruction cache).  The per-stage arithmetic is the same as with ST fixed.
 template <int K, int ST, int C, int FK = -1>
-__device__ __forceinline__ void f32c_pass(const F32CArgs& a, int64_t j0l, int lane) {
+__device__ __forceinline__ void f32c_pass(const F32CArgs& a, int64_t j0l, int lane, int st_rt = ST) {
+  static_assert(ST != FC_MS || ST >= 0, "");
+  const int st = ST >= 0 ? ST : st_rt;
+  // the stage writes a.out (the first stages) or the state pair (the last stage)
+  const bool to_out = st == FC_RHS || st == FC_E1 || st == FC_RK3B;
   static_assert(C % 4 == 0 && C >= K, "float4 cells and a K-cell shuffle halo");
   const LineF& L = a.L;
   const int nc = L.nc;
@@ -408,29 +428,48 @@ __device__ __forceinline__ void f32c_pass(const F32CArgs& a, int64_t j0l, int la
     const float rr_m = c == 0 ? rr_m0 : rr[c - 1];
     const float rl_p = c == C - 1 ? rl_pC : rl[c + 1];
     float dF;
-    if (FK >= 0 && interior)
-      dF = flux_diff_interior<(FK >= 0 ? FK : 0)>(L, j, v, rr_m, d[c + K - 1], rl[c], rr[c], d[c + K], rl_p);
-    else
+    if constexpr (FK >= 0) {
+      if (interior)
+        dF = flux_diff_interior<(FK >= 0 ? FK : 0)>(L, j, v, rr_m, d[c + K - 1], rl[c], rr[c], d[c + K], rl_p);
+      else
+        dF = j < nc ? flux_diff_f32c_call(L, j, v, rr_m, d[c + K - 1], rl[c], rr[c], d[c + K], rl_p) : 0.f;
+    } else {
       dF = j < nc ? flux_diff_f32c(L, j, v, rr_m, d[c + K - 1], rl[c], rr[c], d[c + K], rl_p) : 0.f;
+    }
     const float qj = rw ? -dF * rw[j < nc ? j : nc - 1] : -dF;
     const float dtL = fmaf(a.c_hi, qj, a.c_lo * qj);  // dt L(v)_j
     lq[c] = qj * a.lscale;
-    if constexpr (ST == FC_RHS) {
-      o1[c] = lq[c];
-    } else if constexpr (ST == FC_E1) {
-      o1[c] = dtL;
-    } else if constexpr (ST == FC_RK3B) {
-      o1[c] = 0.25f * (dv[c] + dtL);
+    if constexpr (ST >= 0) {
+      if constexpr (ST == FC_RHS) {
+        o1[c] = lq[c];
+      } else if constexpr (ST == FC_E1) {
+        o1[c] = dtL;
+      } else if constexpr (ST == FC_RK3B) {
+        o1[c] = 0.25f * (dv[c] + dtL);
+      } else {
+        o1[c] = hi[c];
+        o2[c] = lo[c];
+        if constexpr (ST == FC_RK1) dv[c] = dtL;
+        else if constexpr (ST == FC_RK2B) dv[c] = 0.5f * (dv[c] + dtL);
+        else if constexpr (ST == FC_RK3C) dv[c] = (2.f / 3.f) * (dv[c] + dtL);
+        else dv[c] = dtL;  // FC_MS: completed with the history below
+      }
     } else {
-      o1[c] = hi[c];
-      o2[c] = lo[c];
-      if constexpr (ST == FC_RK1) dv[c] = dtL;
-      else if constexpr (ST == FC_RK2B) dv[c] = 0.5f * (dv[c] + dtL);
-      else if constexpr (ST == FC_RK3C) dv[c] = (2.f / 3.f) * (dv[c] + dtL);
-      else dv[c] = dtL;  // FC_MS: completed with the history below
+      float r;  // the same expressions as the fixed-stage branches above
+      if (st == FC_E1 || st == FC_RK1) r = dtL;
+      else if (st == FC_RK3B) r = 0.25f * (dv[c] + dtL);
+      else if (st == FC_RK2B) r = 0.5f * (dv[c] + dtL);
+      else r = (2.f / 3.f) * (dv[c] + dtL);  // FC_RK3C
+      if (to_out) {
+        o1[c] = r;
+      } else {
+        o1[c] = hi[c];
+        o2[c] = lo[c];
+        dv[c] = r;
+      }
     }
   }
-  if constexpr (ST == FC_RHS || ST == FC_E1 || ST == FC_RK3B) {
+  if (to_out) {
     store_cells<C>(a.out, j0, nc, o1);
   } else {
     if constexpr (ST == FC_MS) {  // u' = u + (7 (u4 - u) + 50 dt L + 10 dt L4) / 32
