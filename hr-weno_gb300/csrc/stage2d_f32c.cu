@@ -76,7 +76,56 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, int limit) {
   return false;
 }
 
-template <int K, int ST, bool TMA, bool HAS_DV>
+// WENO offsets of the C cells of a segment from its differences d[0 .. C+2K-2]; for k = 3 the
+// 13/12 (second difference)^2 terms are computed once per window position (as the 1D pass)
+template <int K>
+__device__ __forceinline__ void segment_recon(const float* d, float eps, float* rl, float* rr) {
+  if constexpr (K == 3) {
+    float t[C + 4];
+#pragma unroll
+    for (int m = 2; m < C + 4; ++m) {
+      const float D = d[m] - d[m - 1];
+      t[m] = (13.f / 12.f) * D * D;
+    }
+#pragma unroll
+    for (int c = 0; c < C; ++c) recon_diff3_shared(&d[c + 1], t[c + 4], t[c + 3], t[c + 2], eps, rl[c], rr[c]);
+  } else {
+#pragma unroll
+    for (int c = 0; c < C; ++c) recon_diff<K>(&d[c + 1], eps, rl[c], rr[c]);
+  }
+}
+
+// one cell's offsets from its 2K-2 differences (tile-edge cells), the same arithmetic
+template <int K>
+__device__ __forceinline__ void cell_recon(const float* de, float eps, float& el, float& er) {
+  if constexpr (K == 3) {
+    float te[3];
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      const float D = de[q + 1] - de[q];
+      te[q] = (13.f / 12.f) * D * D;
+    }
+    recon_diff3_shared(de, te[2], te[1], te[0], eps, el, er);
+  } else {
+    recon_diff<K>(de, eps, el, er);
+  }
+}
+
+// flux difference of cell j of a segment: `interior` (no cell of the segment on the line's
+// ends) takes the path without the boundary rules when the numerical flux is known (FKI = 4
+// Lax-Friedrichs, 5 Godunov; the flux function is a uniform branch), with the same arithmetic
+template <int FKI>
+__device__ __forceinline__ float seg_flux(const LineF& L, bool interior, int j, float v, float rr_m,
+                                          float d_m, float rl_j, float rr_j, float d_j, float rl_p) {
+  if constexpr (FKI >= 0) {
+    if (interior) return flux_diff_interior<FKI>(L, j, v, rr_m, d_m, rl_j, rr_j, d_j, rl_p);
+    return flux_diff_f32c_call(L, j, v, rr_m, d_m, rl_j, rr_j, d_j, rl_p);
+  } else {
+    return flux_diff_f32c(L, j, v, rr_m, d_m, rl_j, rr_j, d_j, rl_p);
+  }
+}
+
+template <int K, int ST, bool TMA, bool HAS_DV, int FKI>
 __global__ void __launch_bounds__(NT) stage2d_f32c_kernel(const __grid_constant__ TileMaps M,
                                                           F32CArgs a) {
   constexpr int H = K;
@@ -157,8 +206,7 @@ __global__ void __launch_bounds__(NT) stage2d_f32c_kernel(const __grid_constant_
 #pragma unroll
     for (int q = 0; q < C + 2 * K - 1; ++q)
       d[q] = (sh[base + q + 1] - sh[base + q]) + (sm[base + q + 1] - sm[base + q]);
-#pragma unroll
-    for (int c = 0; c < C; ++c) recon_diff<K>(&d[c + 1], a.eps, rl[c], rr[c]);
+    segment_recon<K>(d, a.eps, rl, rr);
     sLx[r * (NSX + 1) + sg] = rl[0];
     sRx[r * (NSX + 1) + sg + 1] = rr[C - 1];
   }
@@ -180,7 +228,7 @@ __global__ void __launch_bounds__(NT) stage2d_f32c_kernel(const __grid_constant_
       de[q] = (sh[m1] - sh[m0]) + (sm[m1] - sm[m0]);
     }
     float el, er;
-    recon_diff<K>(de, a.eps, el, er);
+    cell_recon<K>(de, a.eps, el, er);
     if (warp == 0) sRx[lane * (NSX + 1)] = er;
     else if (warp == 1) sLx[lane * (NSX + 1) + NSX] = el;
     else if (warp == 2) sRy[lane] = er;
@@ -191,6 +239,7 @@ __global__ void __launch_bounds__(NT) stage2d_f32c_kernel(const __grid_constant_
   // ---- x1 flux differences -> dt/dx1 (-dF1) in shared memory -----------------------------------
   {
     const int j0 = bx + sg * C;
+    const bool interior = j0 > 0 && j0 + C < n1;
 #pragma unroll
     for (int c = 0; c < C; ++c) {
       const int gx = j0 + c;
@@ -200,7 +249,8 @@ __global__ void __launch_bounds__(NT) stage2d_f32c_kernel(const __grid_constant_
         const float v = sh[lj] + sm[lj];
         const float rr_m = c == 0 ? sRx[r * (NSX + 1) + sg] : rr[c - 1];
         const float rl_p = c == C - 1 ? sLx[r * (NSX + 1) + sg + 1] : rl[c + 1];
-        const float dF = flux_diff_f32c(L1, gx, v, rr_m, d[c + K - 1], rl[c], rr[c], d[c + K], rl_p);
+        const float dF =
+            seg_flux<FKI>(L1, interior, gx, v, rr_m, d[c + K - 1], rl[c], rr[c], d[c + K], rl_p);
         t = -dF;
       }
       sq[r * SQ + sg * C + c] = t;
@@ -216,8 +266,7 @@ __global__ void __launch_bounds__(NT) stage2d_f32c_kernel(const __grid_constant_
       const int m0 = base + q * SW, m1 = m0 + SW;
       d[q] = (sh[m1] - sh[m0]) + (sm[m1] - sm[m0]);
     }
-#pragma unroll
-    for (int c = 0; c < C; ++c) recon_diff<K>(&d[c + 1], a.eps, rl[c], rr[c]);
+    segment_recon<K>(d, a.eps, rl, rr);
     sLy[sy * TX + col] = rl[0];
     sRy[(sy + 1) * TX + col] = rr[C - 1];
   }
@@ -227,6 +276,7 @@ __global__ void __launch_bounds__(NT) stage2d_f32c_kernel(const __grid_constant_
   const int gx = bx + col;
   if (gx >= n1) return;
   const int j0 = by + sy * C;
+  const bool interior = j0 > 0 && j0 + C < n2;
 #pragma unroll
   for (int c = 0; c < C; ++c) {
     const int gy = j0 + c;
@@ -236,7 +286,8 @@ __global__ void __launch_bounds__(NT) stage2d_f32c_kernel(const __grid_constant_
     const float v = sh[lj] + sm[lj];
     const float rr_m = c == 0 ? sRy[sy * TX + col] : rr[c - 1];
     const float rl_p = c == C - 1 ? sLy[(sy + 1) * TX + col] : rl[c + 1];
-    const float dF2 = flux_diff_f32c(L2, gy, v, rr_m, d[c + K - 1], rl[c], rr[c], d[c + K], rl_p);
+    const float dF2 =
+        seg_flux<FKI>(L2, interior, gy, v, rr_m, d[c + K - 1], rl[c], rr[c], d[c + K], rl_p);
     const float q1 = L1.rw ? sq[ly * SQ + col] * L1.rw[gx] : sq[ly * SQ + col];
     const float q2 = L2.rw ? -dF2 * L2.rw[gy] : -dF2;
     // dt L = c1 q1 + c2 q2 with the dt/dx float pairs; L = q1/dx1 + q2/dx2
@@ -309,10 +360,19 @@ bool tile_map(const float* p, int n1, int n2, int box_x, int box_y, CUtensorMap*
   return true;
 }
 
+// the numerical flux is specialised (interior cells without the boundary rules) for k = 3 on
+// the TMA path, the workloads' case; the rest take the generic flux difference
 template <int K, int ST, bool TMA, bool HAS_DV>
 cudaError_t launch_kt(const TileMaps& M, const F32CArgs& a, cudaStream_t s) {
   const dim3 grid((unsigned)((a.L.nc + TX - 1) / TX), (unsigned)((a.L2.nc + TY - 1) / TY));
-  stage2d_f32c_kernel<K, ST, TMA, HAS_DV><<<grid, NT, 0, s>>>(M, a);
+  if constexpr (K == 3 && TMA) {
+    if (a.L.flux == HRW_FLUX_LAX_FRIEDRICHS)
+      stage2d_f32c_kernel<K, ST, TMA, HAS_DV, 4><<<grid, NT, 0, s>>>(M, a);
+    else
+      stage2d_f32c_kernel<K, ST, TMA, HAS_DV, 5><<<grid, NT, 0, s>>>(M, a);
+  } else {
+    stage2d_f32c_kernel<K, ST, TMA, HAS_DV, -1><<<grid, NT, 0, s>>>(M, a);
+  }
   return cudaGetLastError();
 }
 
