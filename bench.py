@@ -221,6 +221,42 @@ def config_dict() -> dict:
 # ------------------------------------------------------------------------------------------
 # GPU arm
 # ------------------------------------------------------------------------------------------
+def run_k2(args, dist: Dist) -> dict | None:
+    """The same 2^24-cell line with WENO3 (k = 2): FP64 and compensated FP32, and the FP32
+    form's error against FP64 after the same steps."""
+    import torch
+
+    import hrweno
+    from hrweno import workloads
+
+    dev = dist.local if dist.world > 1 else 0
+    torch.cuda.set_device(dev)
+    prob, u0, dt = workloads.large_burgers(NC, k=2)
+    stream = torch.cuda.Stream()
+    res = {}
+    for dtype in ("f64", "f32c"):
+        ode = hrweno.rktvd(prob, NC, 3, dtype=dtype)
+        ode.set_stream(stream.cuda_stream)
+        u = torch.from_numpy(u0).cuda()
+        t = ode.integrate(u, 0.0, (args.warmup - 0.5) * dt, dt)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        dist.barrier()
+        e0.record(stream)
+        t = ode.integrate(u, t, t + (args.steps - 0.5) * dt, dt)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        el = dist.max(e0.elapsed_time(e1) * 1e-3)
+        res[dtype] = (dist.world * NC * args.steps / el, 1e3 * el / args.steps, u)
+    a, b = res["f64"][2], res["f32c"][2]
+    return {"k": 2, "value": res["f64"][0], "unit": UNIT, "ms_per_step": res["f64"][1],
+            "f32c": {"value": res["f32c"][0], "ms_per_step": res["f32c"][1],
+                     "speedup_vs_f64": res["f32c"][0] / res["f64"][0],
+                     "rel_l1_vs_f64": float((a - b).abs().sum() / a.abs().sum()),
+                     "rel_linf_vs_f64": float((a - b).abs().max() / a.abs().max()),
+                     "steps_compared": args.warmup + args.steps}}
+
+
 def run_ours(args, dist: Dist) -> dict | None:
     import torch
 
@@ -365,7 +401,10 @@ def pbe_config_dict(n: int) -> dict:
             "eps": 1e-6, "flux": "godunov (upwind, g1 = 1 + 0.5 x1, g2 = 0.5)",
             "bc": "zero_inflow", "cfl": 0.4, "integrator": "mstvd (5-step, 3rd order)",
             "numerics": "fast",
-            "l2": f"inputs larger than L2: 5 + 4 ring slots of {n * n * 8 >> 20} MiB"}
+            "l2": (f"inputs larger than L2: 5 + 4 ring slots of {n * n * 8 >> 20} MiB"
+                   if 9 * n * n * 8 > 126 << 20 else
+                   f"L2-resident: 5 + 4 ring slots of {n * n * 8 >> 20} MiB fit the 126 MiB L2 "
+                   "(a secondary line; the 4096^2 grid is the L2-exceeding one)")}
 
 
 def run_pbe2d(args, dist: Dist) -> dict | None:
@@ -796,10 +835,11 @@ def main() -> None:
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
-    ap.add_argument("--forms", default="f32c,pbe2d,batched,adjoint,config1",
+    ap.add_argument("--forms", default="f32c,k2,pbe2d,batched,adjoint,config1",
                     help="comma-separated forms reported beside the workload's own line "
-                         "(f32c: the compensated FP32 form of the same workload; the others: "
-                         "their workloads, run after the default burgers1d line)")
+                         "(f32c: the compensated FP32 form of the same workload; k2: the line "
+                         "with WENO3; pbe2d: the 4096^2 and 1024^2 grids; the others: their "
+                         "workloads, run after the default burgers1d line)")
     ap.add_argument("--no-forms", action="store_true", help="same as --forms ''")
     ap.add_argument("--workload", default="burgers1d", choices=["burgers1d", "pbe2d", "batched", "adjoint", "config1"],
                     help="burgers1d (default): the 2^24-cell line; pbe2d: the 2D PBE grid")
@@ -836,10 +876,20 @@ def main() -> None:
             sub = argparse.Namespace(**vars(args))
             sub.steps, sub.no_cpu = min(args.steps, 100), True
             forms = {}
+            if "k2" in args.forms:
+                k2 = run_k2(sub, dist)
+                if k2 is not None:
+                    forms["weno3_k2"] = k2
             if "pbe2d" in args.forms:
                 pb = run_pbe2d(sub, dist)
                 if pb is not None:
                     forms["pbe2d_4096"] = {k: pb[k] for k in ("value", "ms_per_step", "roofline", "forms")}
+                sub1024 = argparse.Namespace(**vars(sub))
+                sub1024.pbe_n = 1024
+                p1 = run_pbe2d(sub1024, dist)
+                if p1 is not None:
+                    forms["pbe2d_1024"] = {k: p1[k] for k in ("value", "ms_per_step", "forms")}
+                    forms["pbe2d_1024"]["l2"] = p1["config"]["l2"]
             if "batched" in args.forms:
                 sub.steps = min(args.steps, 20)
                 bt = run_batched(sub, dist)

@@ -428,11 +428,16 @@ __device__ __forceinline__ void f32c_pass(const F32CArgs& a, int64_t j0l, int la
     const float rr_m = c == 0 ? rr_m0 : rr[c - 1];
     const float rl_p = c == C - 1 ? rl_pC : rl[c + 1];
     float dF;
-    if constexpr (FK >= 0) {
+    if constexpr (FK >= 4) {  // the batched kernel: the boundary path out of line
+      if (interior)
+        dF = flux_diff_interior<FK>(L, j, v, rr_m, d[c + K - 1], rl[c], rr[c], d[c + K], rl_p);
+      else
+        dF = j < nc ? flux_diff_f32c_call(L, j, v, rr_m, d[c + K - 1], rl[c], rr[c], d[c + K], rl_p) : 0.f;
+    } else if constexpr (FK >= 0) {  // the single-line kernel: inline (a call costs registers)
       if (interior)
         dF = flux_diff_interior<(FK >= 0 ? FK : 0)>(L, j, v, rr_m, d[c + K - 1], rl[c], rr[c], d[c + K], rl_p);
       else
-        dF = j < nc ? flux_diff_f32c_call(L, j, v, rr_m, d[c + K - 1], rl[c], rr[c], d[c + K], rl_p) : 0.f;
+        dF = j < nc ? flux_diff_f32c(L, j, v, rr_m, d[c + K - 1], rl[c], rr[c], d[c + K], rl_p) : 0.f;
     } else {
       dF = j < nc ? flux_diff_f32c(L, j, v, rr_m, d[c + K - 1], rl[c], rr[c], d[c + K], rl_p) : 0.f;
     }
