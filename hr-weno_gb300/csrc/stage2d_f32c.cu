@@ -60,20 +60,26 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, i
       : "memory");
 }
 
-// Wait for phase 0 of the block's mbarrier, at most `limit` polls; true when it completed.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, int limit) {
+// Wait for phase `parity` of the block's mbarrier, at most `limit` polls; true when it
+// completed.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int limit) {
   const uint32_t a = smem_u32(bar);
   for (int it = 0; it < limit; ++it) {
     uint32_t done;
     asm volatile(
-        "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0; "
+        "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; "
         "selp.u32 %0, 1, 0, p; }"
         : "=r"(done)
-        : "r"(a)
+        : "r"(a), "r"(parity)
         : "memory");
     if (done) return true;
   }
   return false;
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
 }
 
 // WENO offsets of the C cells of a segment from its differences d[0 .. C+2K-2]; for k = 3 the
@@ -138,8 +144,11 @@ __global__ void __launch_bounds__(NT) stage2d_f32c_kernel(const __grid_constant_
   __shared__ float sq[TY * SQ];                                 // x1 part of dt L
   __shared__ float sLx[TY * (NSX + 1)], sRx[TY * (NSX + 1)];  // rl / rr at segment edges
   __shared__ float sLy[(NSY + 1) * TX], sRy[(NSY + 1) * TX];
+  // TMA boxes; in the multistep stage the same space then takes the three 32 x 32 history
+  // tiles (the padded tile holds each cell's hi and lo exactly, as there is no increment)
+  static_assert(!MS || HAS_DV || 2 * BS >= 3 * TX * TY, "history tiles fit the box space");
   __shared__ alignas(128) float tb[TMA ? NB : 1][TMA ? BS : 1];
-  __shared__ alignas(128) float hb[TMA && MS ? 3 : 1][TMA && MS ? TX * TY : 1];
+  float* const hb = &tb[0][0];
   __shared__ alignas(8) uint64_t bar;
   const LineF& L1 = a.L;
   const LineF& L2 = a.L2;
@@ -155,25 +164,17 @@ __global__ void __launch_bounds__(NT) stage2d_f32c_kernel(const __grid_constant_
     }
     __syncthreads();
     if (tid == 0) {
-      constexpr uint32_t bytes = NB * BY * BX * 4 + (MS ? 3 * TX * TY * 4 : 0);
-      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(&bar)),
-                   "r"(bytes)
-                   : "memory");
+      mbar_expect_tx(&bar, NB * BY * BX * 4);
       tma_load_2d(tb[0], &M.hi, bx - 4, by - 3, &bar);
       tma_load_2d(tb[1], &M.lo, bx - 4, by - 3, &bar);
       if constexpr (HAS_DV) tma_load_2d(tb[NB - 1], &M.dv, bx - 4, by - 3, &bar);
-      if constexpr (MS) {
-        tma_load_2d(hb[0], &M.h4, bx, by, &bar);
-        tma_load_2d(hb[1], &M.l4, bx, by, &bar);
-        tma_load_2d(hb[2], &M.L4, bx, by, &bar);
-      }
     }
     // bounded wait; on a timeout every thread of the block learns of it, the block waits
     // (bounded again) for its copies to land and leaves, and the host sees the flag
-    const bool ok = mbar_wait(&bar, 1 << 20);
+    const bool ok = mbar_wait(&bar, 0, 1 << 20);
     if (__syncthreads_or(!ok)) {
       if (tid == 0) atomicExch(&g_tma_timeout, 1u);
-      mbar_wait(&bar, 1 << 20);
+      mbar_wait(&bar, 0, 1 << 20);
       return;
     }
     for (int q = tid; q < (TY + 2 * H) * RW; q += NT) {
@@ -196,7 +197,20 @@ __global__ void __launch_bounds__(NT) stage2d_f32c_kernel(const __grid_constant_
       sm[row * SW + col] = HAS_DV ? a.lo[g] + a.dv[g] : a.lo[g];
     }
   }
+  if constexpr (TMA && MS) {
+    // the boxes have been read (generic proxy) before the history copies (async proxy)
+    // overwrite them: fence, then the block barrier below, then the copies
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
   __syncthreads();
+  if constexpr (TMA && MS) {
+    if (tid == 0) {
+      mbar_expect_tx(&bar, 3 * TX * TY * 4);
+      tma_load_2d(hb, &M.h4, bx, by, &bar);
+      tma_load_2d(hb + TX * TY, &M.l4, bx, by, &bar);
+      tma_load_2d(hb + 2 * TX * TY, &M.L4, bx, by, &bar);
+    }
+  }
 
   // ---- x1: differences and offsets of the row segment ------------------------------------------
   const int r = lane, sg = warp;
@@ -273,6 +287,14 @@ __global__ void __launch_bounds__(NT) stage2d_f32c_kernel(const __grid_constant_
   __syncthreads();
 
   // ---- x2 flux differences, dt L and the stage update ------------------------------------------
+  if constexpr (TMA && MS) {  // the history tiles (bounded wait, as for the boxes)
+    const bool ok = mbar_wait(&bar, 1, 1 << 20);
+    if (__syncthreads_or(!ok)) {
+      if (tid == 0) atomicExch(&g_tma_timeout, 1u);
+      mbar_wait(&bar, 1, 1 << 20);
+      return;
+    }
+  }
   const int gx = bx + col;
   if (gx >= n1) return;
   const int j0 = by + sy * C;
@@ -294,15 +316,14 @@ __global__ void __launch_bounds__(NT) stage2d_f32c_kernel(const __grid_constant_
     const float dtL = fmaf(a.c_hi, q1, fmaf(a.c_lo, q1, fmaf(a.c2_hi, q2, a.c2_lo * q2)));
     const float Lv = fmaf(q1, a.lscale, q2 * a.lscale2);
     const int64_t j = gy * ld + gx;
-    if constexpr (TMA) {
+    if constexpr (TMA && MS) {  // hi, lo from the padded tile; history from the tiles
+      const int q = ly * TX + col;
+      f32c_update_h<ST>(a, j, sh[lj], sm[lj], 0.f, dtL, Lv, hb[q], hb[TX * TY + q], hb[2 * TX * TY + q]);
+    } else if constexpr (TMA) {
       const int src = (ly + 3) * BX + col + 4;  // the cell in the halo box
       const float h = tb[0][src], l = tb[1][src];
       const float dv = HAS_DV ? tb[NB - 1][src] : 0.f;
-      if constexpr (MS)
-        f32c_update_h<ST>(a, j, h, l, dv, dtL, Lv, hb[0][ly * TX + col], hb[1][ly * TX + col],
-                          hb[2][ly * TX + col]);
-      else
-        f32c_update_h<ST>(a, j, h, l, dv, dtL, Lv, 0.f, 0.f, 0.f);
+      f32c_update_h<ST>(a, j, h, l, dv, dtL, Lv, 0.f, 0.f, 0.f);
     } else {
       const float h = a.hi[j], l = a.lo[j];
       const float dv = HAS_DV ? a.dv[j] : 0.f;
