@@ -817,9 +817,9 @@ extern "C" int hrw_integrate(hrw_ode* o, int mem, void* u, double* t, double tou
   if (rc != HRW_OK) return rc;
   if (mem == HRW_MEM_HOST) HRW_CUDA(cudaMemcpyAsync(u, du, bytes, cudaMemcpyDeviceToHost, o->stream));
   HRW_CUDA(cudaStreamSynchronize(o->stream));
-  if (o->dtype == HRW_F32C && o->prob.kind == HRW_PROBLEM_FV2D) {
+  if (o->prob.kind == HRW_PROBLEM_FV2D) {
     bool timed_out = false;
-    HRW_CUDA(stage2d_f32c_timed_out(&timed_out));
+    HRW_CUDA(o->dtype == HRW_F32C ? stage2d_f32c_timed_out(&timed_out) : stage2d_timed_out(&timed_out));
     if (timed_out) {
       o->istate = -1;
       return fail(HRW_ETIMEOUT, "hrw_integrate: a 2D stage block's bounded wait for its tile copies ran out.");
@@ -850,8 +850,8 @@ extern "C" int hrw_rhs(const hrw_problem* p, int dtype, double t, const void* v,
   }
   if (e == cudaSuccess) e = cudaStreamSynchronize(o->stream);
   bool timed_out = false;
-  if (e == cudaSuccess && dtype == HRW_F32C && p->kind == HRW_PROBLEM_FV2D)
-    e = stage2d_f32c_timed_out(&timed_out);
+  if (e == cudaSuccess && p->kind == HRW_PROBLEM_FV2D)
+    e = dtype == HRW_F32C ? stage2d_f32c_timed_out(&timed_out) : stage2d_timed_out(&timed_out);
   hrw_ode_destroy(o);
   if (e != cudaSuccess) return fail(HRW_ECUDA, std::string("hrw_rhs: ") + cudaGetErrorString(e));
   if (timed_out) return fail(HRW_ETIMEOUT, "hrw_rhs: a 2D stage block's bounded wait for its tile copies ran out.");

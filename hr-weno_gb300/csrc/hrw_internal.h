@@ -102,6 +102,8 @@ cudaError_t launch_stage2d_f32c(const F32CArgs& a, int k, int stage, cudaStream_
 // whether a 2D compensated stage block gave up waiting for its TMA tile copies since the last
 // call (the flag is cleared); synchronises with the device
 cudaError_t stage2d_f32c_timed_out(bool* timed_out);
+// the same for the FP64 2D stage
+cudaError_t stage2d_timed_out(bool* timed_out);
 cudaError_t launch_split_f64(const double* u, float* hi, float* lo, int64_t n, cudaStream_t s);
 cudaError_t launch_merge_f64(const float* hi, const float* lo, double* u, int64_t n, cudaStream_t s);
 cudaError_t launch_widen_f32(const float* x, double* y, int64_t n, cudaStream_t s);

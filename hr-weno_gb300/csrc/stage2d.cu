@@ -27,6 +27,7 @@
 #include "hrw_device.cuh"
 #include "hrw_internal.h"
 #include "hrw_stage.cuh"
+#include "hrw_tma.cuh"
 
 namespace hrw {
 
@@ -36,8 +37,16 @@ constexpr int TX = 32, TY = 32, C = 8, NT = 128;
 static_assert(TX * TY == NT * C, "one segment of C cells per thread and direction");
 static_assert(TX == 32 && TY / C == NT / 32 && TX / C == NT / 32, "warp-per-segment mapping");
 
-template <int K, int ST, bool STRICT, bool UPW>
-__global__ void __launch_bounds__(NT) stage2d_kernel(StageArgs a) {
+__device__ unsigned int g_tma_timeout;  // set when a block's bounded mbarrier wait ran out
+constexpr int BX = 40, BY = 38;         // TMA box of the tile plus halo: x from bx - 4, y from by - 3
+
+// TMA: the tile plus halo of the stage input comes in as one 40 x 38 box of doubles at
+// (bx - 4, by - 3) (x on a 16-byte boundary), completing on a block mbarrier; the block then
+// builds its padded tile from shared memory, replicating edge cells into the ghosts (the box
+// reads zeros outside the grid).  Otherwise every thread gathers the tile from global memory.
+// Both give the same tile, so the same bits.
+template <int K, int ST, bool STRICT, bool UPW, bool TMA>
+__global__ void __launch_bounds__(NT) stage2d_kernel(const __grid_constant__ CUtensorMap Mv, StageArgs a) {
   constexpr int H = K;
   constexpr int RW = TX + 2 * H;      // loaded row width
   constexpr int SW = RW + 1;          // odd row stride: the x1 pass reads 32 rows per warp
@@ -47,6 +56,8 @@ __global__ void __launch_bounds__(NT) stage2d_kernel(StageArgs a) {
   __shared__ double sq[TY * SQ];
   __shared__ double sLx[TY * (NSX + 1)], sRx[TY * (NSX + 1)];  // [row][segment edge]
   __shared__ double sLy[(NSY + 1) * TX], sRy[(NSY + 1) * TX];  // [segment edge][column]
+  __shared__ alignas(128) double tbox[TMA ? BY * BX : 1];
+  __shared__ alignas(8) uint64_t bar;
 
   const LineArgs& L1 = a.L;
   const LineArgs& L2 = a.L2;
@@ -55,12 +66,35 @@ __global__ void __launch_bounds__(NT) stage2d_kernel(StageArgs a) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
   // ---- stage the tile and its halo ------------------------------------------------------------
-  for (int q = tid; q < (TY + 2 * H) * RW; q += NT) {
-    const int row = q / RW, col = q - row * RW;
-    int64_t gy = by - H + row, gx = bx - H + col;
-    gy = gy < 0 ? 0 : (gy >= n2 ? n2 - 1 : gy);
-    gx = gx < 0 ? 0 : (gx >= n1 ? n1 - 1 : gx);
-    sv[row * SW + col] = a.v[gy * ld + gx];
+  if constexpr (TMA) {
+    if (tid == 0) mbar_init(&bar);
+    __syncthreads();
+    if (tid == 0) {
+      mbar_expect_tx(&bar, BY * BX * 8);
+      tma_load_2d(tbox, &Mv, (int)bx - 4, (int)by - 3, &bar);
+    }
+    const bool ok = mbar_wait(&bar, 0, 1 << 20);  // bounded, as stage2d_f32c.cu
+    if (__syncthreads_or(!ok)) {
+      if (tid == 0) atomicExch(&g_tma_timeout, 1u);
+      mbar_wait(&bar, 0, 1 << 20);
+      return;
+    }
+    const int ibx = (int)bx, iby = (int)by, in1 = (int)n1, in2 = (int)n2;
+    for (int q = tid; q < (TY + 2 * H) * RW; q += NT) {
+      const int row = q / RW, col = q - row * RW;
+      int gy = iby - H + row, gx = ibx - H + col;
+      gy = gy < 0 ? 0 : (gy >= in2 ? in2 - 1 : gy);
+      gx = gx < 0 ? 0 : (gx >= in1 ? in1 - 1 : gx);
+      sv[row * SW + col] = tbox[(gy - (iby - 3)) * BX + (gx - (ibx - 4))];
+    }
+  } else {
+    for (int q = tid; q < (TY + 2 * H) * RW; q += NT) {
+      const int row = q / RW, col = q - row * RW;
+      int64_t gy = by - H + row, gx = bx - H + col;
+      gy = gy < 0 ? 0 : (gy >= n2 ? n2 - 1 : gy);
+      gx = gx < 0 ? 0 : (gx >= n1 ? n1 - 1 : gx);
+      sv[row * SW + col] = a.v[gy * ld + gx];
+    }
   }
   __syncthreads();
 
@@ -192,7 +226,11 @@ __global__ void __launch_bounds__(NT) stage2d_kernel(StageArgs a) {
 template <int K, int ST, bool STRICT, bool UPW>
 cudaError_t launch_k(const StageArgs& a, cudaStream_t s) {
   const dim3 grid((unsigned)((a.L.nc + TX - 1) / TX), (unsigned)((a.L2.nc + TY - 1) / TY));
-  stage2d_kernel<K, ST, STRICT, UPW><<<grid, NT, 0, s>>>(a);
+  CUtensorMap mv{};
+  if (a.ld == a.L.nc && tile_map_2d(a.v, 8, (int)a.L.nc, (int)a.L2.nc, BX, BY, &mv))
+    stage2d_kernel<K, ST, STRICT, UPW, true><<<grid, NT, 0, s>>>(mv, a);
+  else
+    stage2d_kernel<K, ST, STRICT, UPW, false><<<grid, NT, 0, s>>>(mv, a);
   return cudaGetLastError();
 }
 
@@ -217,6 +255,14 @@ cudaError_t launch_kk(const StageArgs& a, int k, int stage, cudaStream_t s) {
 }
 
 }  // namespace
+
+cudaError_t stage2d_timed_out(bool* timed_out) {
+  unsigned int v = 0, zero = 0;
+  cudaError_t e = cudaMemcpyFromSymbol(&v, g_tma_timeout, sizeof(v));
+  if (e == cudaSuccess && v) e = cudaMemcpyToSymbol(g_tma_timeout, &zero, sizeof(zero));
+  *timed_out = v != 0;
+  return e;
+}
 
 cudaError_t launch_stage2d(const StageArgs& a, int k, int stage, bool strict, cudaStream_t s) {
   if (a.L.nc <= 0 || a.L2.nc <= 0) return cudaSuccess;

@@ -29,6 +29,7 @@
 #include "../../include/hrweno_gpu.h"
 #include "hrw_f32c.cuh"
 #include "hrw_internal.h"
+#include "hrw_tma.cuh"
 
 namespace hrw {
 
@@ -46,41 +47,6 @@ struct TileMaps {
 };
 
 __device__ unsigned int g_tma_timeout;  // set when a block's bounded mbarrier wait ran out
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-
-__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y,
-                                            uint64_t* bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
-      " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(dst)),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
-      : "memory");
-}
-
-// Wait for phase `parity` of the block's mbarrier, at most `limit` polls; true when it
-// completed.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int limit) {
-  const uint32_t a = smem_u32(bar);
-  for (int it = 0; it < limit; ++it) {
-    uint32_t done;
-    asm volatile(
-        "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; "
-        "selp.u32 %0, 1, 0, p; }"
-        : "=r"(done)
-        : "r"(a), "r"(parity)
-        : "memory");
-    if (done) return true;
-  }
-  return false;
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
-               : "memory");
-}
 
 // WENO offsets of the C cells of a segment from its differences d[0 .. C+2K-2]; for k = 3 the
 // 13/12 (second difference)^2 terms are computed once per window position (as the 1D pass)
@@ -158,10 +124,7 @@ __global__ void __launch_bounds__(NT) stage2d_f32c_kernel(const __grid_constant_
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
   if constexpr (TMA) {
-    if (tid == 0) {
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bar)) : "memory");
-      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
+    if (tid == 0) mbar_init(&bar);
     __syncthreads();
     if (tid == 0) {
       mbar_expect_tx(&bar, NB * BY * BX * 4);
@@ -332,57 +295,6 @@ __global__ void __launch_bounds__(NT) stage2d_f32c_kernel(const __grid_constant_
   }
 }
 
-// ---- TMA descriptors: encoded through the driver entry point, cached by array -----------------
-PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
-  static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
-    void* p = nullptr;
-    cudaDriverEntryPointQueryResult q{};
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
-            cudaSuccess ||
-        q != cudaDriverEntryPointSuccess)
-      p = nullptr;
-    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
-  }();
-  return fn;
-}
-
-struct MapEntry {
-  const void* p;
-  int n1, n2, box_x, box_y;
-  CUtensorMap map;
-};
-
-// A float array of n2 rows of n1 values (row pitch n1 floats) as a 2D tensor with a
-// box_x x box_y box; false when it cannot be described (pitch or address not 16-byte aligned).
-bool tile_map(const float* p, int n1, int n2, int box_x, int box_y, CUtensorMap* out) {
-  static std::mutex mu;
-  static std::vector<MapEntry> cache;
-  if (n1 % 4 != 0 || (reinterpret_cast<uintptr_t>(p) & 15) != 0) return false;
-  std::lock_guard<std::mutex> lock(mu);
-  for (const MapEntry& e : cache)
-    if (e.p == p && e.n1 == n1 && e.n2 == n2 && e.box_x == box_x && e.box_y == box_y) {
-      *out = e.map;
-      return true;
-    }
-  const auto fn = encode_fn();
-  if (!fn) return false;
-  MapEntry e{p, n1, n2, box_x, box_y, {}};
-  const cuuint64_t dim[2] = {(cuuint64_t)n1, (cuuint64_t)n2};
-  const cuuint64_t stride[1] = {(cuuint64_t)n1 * sizeof(float)};
-  const cuuint32_t box[2] = {(cuuint32_t)box_x, (cuuint32_t)box_y};
-  const cuuint32_t estride[2] = {1, 1};
-  if (fn(&e.map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(p), dim, stride, box, estride,
-         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
-    return false;
-  if (cache.size() >= 256) cache.erase(cache.begin());
-  cache.push_back(e);
-  *out = e.map;
-  return true;
-}
-
-// the numerical flux is specialised (interior cells without the boundary rules) for k = 3 on
-// the TMA path, the workloads' case; the rest take the generic flux difference
 template <int K, int ST, bool TMA, bool HAS_DV>
 cudaError_t launch_kt(const TileMaps& M, const F32CArgs& a, cudaStream_t s) {
   const dim3 grid((unsigned)((a.L.nc + TX - 1) / TX), (unsigned)((a.L2.nc + TY - 1) / TY));
@@ -402,12 +314,12 @@ cudaError_t launch_k(const F32CArgs& a, cudaStream_t s) {
   constexpr bool MS = ST == FC_MS;
   TileMaps M{};
   const int n1 = a.L.nc, n2 = a.L2.nc;
-  const bool tma = n1 == a.ld && tile_map(a.hi, n1, n2, BX, BY, &M.hi) &&
-                   tile_map(a.lo, n1, n2, BX, BY, &M.lo) &&
-                   (!a.dv || tile_map(a.dv, n1, n2, BX, BY, &M.dv)) &&
-                   (!MS || (tile_map(a.hi4, n1, n2, TX, TY, &M.h4) &&
-                            tile_map(a.lo4, n1, n2, TX, TY, &M.l4) &&
-                            tile_map(a.l4, n1, n2, TX, TY, &M.L4)));
+  const bool tma = n1 == a.ld && tile_map_2d(a.hi, 4, n1, n2, BX, BY, &M.hi) &&
+                   tile_map_2d(a.lo, 4, n1, n2, BX, BY, &M.lo) &&
+                   (!a.dv || tile_map_2d(a.dv, 4, n1, n2, BX, BY, &M.dv)) &&
+                   (!MS || (tile_map_2d(a.hi4, 4, n1, n2, TX, TY, &M.h4) &&
+                            tile_map_2d(a.lo4, 4, n1, n2, TX, TY, &M.l4) &&
+                            tile_map_2d(a.l4, 4, n1, n2, TX, TY, &M.L4)));
   if constexpr (MS) {  // the multistep stage has no stage increment
     if (a.dv) return cudaErrorInvalidValue;
     return tma ? launch_kt<K, ST, true, false>(M, a, s) : launch_kt<K, ST, false, false>(M, a, s);
@@ -436,6 +348,59 @@ cudaError_t launch_st(const F32CArgs& a, int stage, cudaStream_t s) {
 }
 
 }  // namespace
+
+// ---- TMA descriptors: encoded through the driver entry point, cached by array ----------------
+namespace {
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      p = nullptr;
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }();
+  return fn;
+}
+
+struct MapEntry {
+  const void* p;
+  int elem, n1, n2, box_x, box_y;
+  CUtensorMap map;
+};
+
+}  // namespace
+
+bool tile_map_2d(const void* p, int elem_bytes, int n1, int n2, int box_x, int box_y, CUtensorMap* out) {
+  static std::mutex mu;
+  static std::vector<MapEntry> cache;
+  if ((int64_t)n1 * elem_bytes % 16 != 0 || (reinterpret_cast<uintptr_t>(p) & 15) != 0) return false;
+  std::lock_guard<std::mutex> lock(mu);
+  for (const MapEntry& e : cache)
+    if (e.p == p && e.elem == elem_bytes && e.n1 == n1 && e.n2 == n2 && e.box_x == box_x &&
+        e.box_y == box_y) {
+      *out = e.map;
+      return true;
+    }
+  const auto fn = encode_fn();
+  if (!fn) return false;
+  MapEntry e{p, elem_bytes, n1, n2, box_x, box_y, {}};
+  const cuuint64_t dim[2] = {(cuuint64_t)n1, (cuuint64_t)n2};
+  const cuuint64_t stride[1] = {(cuuint64_t)n1 * (cuuint64_t)elem_bytes};
+  const cuuint32_t box[2] = {(cuuint32_t)box_x, (cuuint32_t)box_y};
+  const cuuint32_t estride[2] = {1, 1};
+  const CUtensorMapDataType dt = elem_bytes == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+  if (fn(&e.map, dt, 2, const_cast<void*>(p), dim, stride, box, estride, CU_TENSOR_MAP_INTERLEAVE_NONE,
+         CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+    return false;
+  if (cache.size() >= 256) cache.erase(cache.begin());
+  cache.push_back(e);
+  *out = e.map;
+  return true;
+}
 
 cudaError_t launch_stage2d_f32c(const F32CArgs& a, int k, int stage, cudaStream_t s) {
   if (a.L.nc <= 0 || a.L2.nc <= 0) return cudaSuccess;
