@@ -61,7 +61,10 @@ template <int K, int ST, bool STRICT, int NT, int C>
 __global__ void __launch_bounds__(NT) stage1d_kernel(StageArgs a) {
   constexpr int T = NT * C;
   constexpr int H = K;  // halo: cell j needs v(j-K .. j+K) through its two interfaces
-  __shared__ double sv[T + 2 * H];
+  // the tile with one padding double after every 8: thread t's window starts at cell 8t, and
+  // unpadded those windows (64 bytes apart) would fall on two bank groups (16-way conflicts)
+  constexpr int TP = T + 2 * H;
+  __shared__ double sv[TP + TP / 8 + 1];
   __shared__ double sL[NT + 1];  // sL[t] = vl of thread t's first cell; sL[NT] = vl(s+T)
   __shared__ double sR[NT + 1];  // sR[t+1] = vr of thread t's last cell; sR[0] = vr(s-1)
   const LineArgs& L = a.L;
@@ -72,20 +75,20 @@ __global__ void __launch_bounds__(NT) stage1d_kernel(StageArgs a) {
   for (int q = tid; q < T + 2 * H; q += NT) {
     int64_t g = s - H + q;
     g = g < 0 ? 0 : (g >= nc ? nc - 1 : g);
-    sv[q] = a.v[g];
+    sv[q + (q >> 3)] = a.v[g];
   }
   __syncthreads();
 
   // ---- reconstruction of the thread's C cells --------------------------------------------
-  const int l0 = tid * C;  // first local cell; its centre is sv[H + l0]
+  const int l0 = tid * C;  // first local cell; its centre is tile cell H + l0
   double vl[C], vr[C];
+  double w[C + 2 * K];
+#pragma unroll
+  for (int q = 0; q < C + 2 * K; ++q) w[q] = sv[l0 + q + ((l0 + q) >> 3)];  // v(j0 - K + q)
   if constexpr (STRICT) {
 #pragma unroll
-    for (int c = 0; c < C; ++c) recon_strict<K>(&sv[H + l0 + c], a.eps, vl[c], vr[c]);
+    for (int c = 0; c < C; ++c) recon_strict<K>(&w[K + c], a.eps, vl[c], vr[c]);
   } else {
-    double w[C + 2 * K];
-#pragma unroll
-    for (int q = 0; q < C + 2 * K; ++q) w[q] = sv[l0 + q];  // v(j0 - K + q)
     recon_fast<K, C>(w, a.eps, vl, vr);
   }
   sL[tid] = vl[0];
@@ -94,9 +97,15 @@ __global__ void __launch_bounds__(NT) stage1d_kernel(StageArgs a) {
   if (tid >= NT - 2) {
     const int which = tid - (NT - 2);  // 0: cell s-1, 1: cell s+T
     const int lc = which == 0 ? H - 1 : H + T;
+    double p[2 * K - 1];  // the cell's stencil, lc - (K-1) .. lc + K-1
+#pragma unroll
+    for (int q = 0; q < 2 * K - 1; ++q) {
+      const int i = lc - (K - 1) + q;
+      p[q] = sv[i + (i >> 3)];
+    }
     double el, er;
-    if constexpr (STRICT) recon_strict<K>(&sv[lc], a.eps, el, er);
-    else recon_fast_one<K>(&sv[lc], a.eps, el, er);
+    if constexpr (STRICT) recon_strict<K>(&p[K - 1], a.eps, el, er);
+    else recon_fast_one<K>(&p[K - 1], a.eps, el, er);
     if (which == 0) sR[0] = er;
     else sL[NT] = el;
   }
@@ -124,7 +133,7 @@ __global__ void __launch_bounds__(NT) stage1d_kernel(StageArgs a) {
       const int64_t j = j0 + c;
       if (j >= nc) break;
       const double dF = flux_diff<STRICT>(L, j, F[c], F[c + 1], vr[c]);
-      combine<ST, STRICT>(a, L, j, sv[H + l0 + c], dF);
+      combine<ST, STRICT>(a, L, j, w[K + c], dF);
     }
   }
 }
