@@ -152,6 +152,10 @@ struct hrw_ode {
     int64_t steps = 0;
   } graph;
   bool use_graphs = true;
+  // host lines with the copies overlapped (rk3_integrate_host): two compute streams and a copy
+  // stream beside `stream`, and their events
+  cudaStream_t pipe[2] = {}, copy = nullptr;
+  cudaEvent_t ev_start = nullptr, ev_in[8] = {}, ev_s3[8] = {}, ev_join[3] = {};
 };
 
 extern "C" {
@@ -487,6 +491,15 @@ int hrw_ode_destroy(hrw_ode* o) {
     if (p) cudaFree(p);
   if (o->fmem) cudaFree(o->fmem);
   if (o->graph.exec) cudaGraphExecDestroy(o->graph.exec);
+  for (cudaStream_t st : {o->pipe[0], o->pipe[1], o->copy})
+    if (st) cudaStreamDestroy(st);
+  for (cudaEvent_t ev : o->ev_in)
+    if (ev) cudaEventDestroy(ev);
+  for (cudaEvent_t ev : o->ev_s3)
+    if (ev) cudaEventDestroy(ev);
+  for (cudaEvent_t ev : o->ev_join)
+    if (ev) cudaEventDestroy(ev);
+  if (o->ev_start) cudaEventDestroy(o->ev_start);
   if (o->own) cudaStreamDestroy(o->own);
   delete o;
   return HRW_OK;
@@ -515,6 +528,19 @@ static cudaError_t run_stage(hrw_ode* o, int stage, const double* v, const doubl
       return launch_stage1d(a, o->prob.k, stage, strict, o->stream);
     default: return launch_stage2d(a, o->prob.k, stage, strict, o->stream);
   }
+}
+
+// A stage of a uniform 1D line over cells cell0 .. cell0 + ncell - 1 on stream `st`.
+static cudaError_t run_stage_range(hrw_ode* o, int stage, const double* v, const double* u, double* out,
+                                   int64_t cell0, int64_t ncell, double dt, cudaStream_t st) {
+  StageArgs a = o->base;
+  a.v = v;
+  a.u = u;
+  a.out = out;
+  a.dt = dt;
+  a.cell0 = cell0;
+  a.ncell = ncell;
+  return launch_stage1d(a, o->prob.k, stage, o->prob.numerics == HRW_NUMERICS_STRICT, st);
 }
 
 // One rktvd step from u (in place for orders 2 and 3); order 1 writes into `out1`.
@@ -795,6 +821,92 @@ static int ms_integrate_f32c(hrw_ode* o, double* du, double* t, double tout, dou
   return HRW_OK;
 }
 
+// rktvd(3) of a uniform FP64 line on a page-locked host array, with the copies overlapped:
+// the line is copied in by chunks of whole 1024-cell tiles, and stage 1 of the first step runs
+// on each chunk as soon as it and its right neighbour (the halo) have landed; stage 3 of the
+// last step runs by chunks, each chunk's copy back following it.  Chunks alternate between two
+// streams, so the tail of one overlaps the next.  The arithmetic is that of rk_integrate.
+constexpr int kPipeChunks = 4;
+constexpr int64_t kPipeTile = 1024;
+
+static bool host_pipeline_ok(const hrw_ode* o, const void* u) {
+  if (o->dtype != HRW_F64 || o->prob.kind != HRW_PROBLEM_FV1D || o->method != 0 || o->order != 3 ||
+      o->line[0].xe || (int64_t)o->neq < 2 * 152 * kPipeTile)
+    return false;
+  cudaPointerAttributes at{};
+  if (cudaPointerGetAttributes(&at, u) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return at.type == cudaMemoryTypeHost;  // page-locked: asynchronous copies
+}
+
+static int rk3_integrate_host(hrw_ode* o, double* uh, double* t, double tout, double dt, int itask) {
+  double tt = *t;
+  int64_t n = 0;
+  do {  // the reference's time sequence (src/hrweno_tvdode.f90:137-143)
+    tt = tt + dt;
+    if (++n > kMaxSteps) return fail(HRW_EINVAL, "Invalid input 'dt': too many steps to reach tout.");
+  } while (!(is_done(tt, tout, dt) || itask == 2));
+  if (!o->copy) {
+    for (cudaStream_t* st : {&o->pipe[0], &o->pipe[1], &o->copy})
+      HRW_CUDA(cudaStreamCreateWithFlags(st, cudaStreamNonBlocking));
+    HRW_CUDA(cudaEventCreateWithFlags(&o->ev_start, cudaEventDisableTiming));
+    for (int i = 0; i < kPipeChunks; ++i) {
+      HRW_CUDA(cudaEventCreateWithFlags(&o->ev_in[i], cudaEventDisableTiming));
+      HRW_CUDA(cudaEventCreateWithFlags(&o->ev_s3[i], cudaEventDisableTiming));
+    }
+    for (cudaEvent_t& ev : o->ev_join) HRW_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  }
+  const int64_t nc = o->neq;
+  const int64_t chunk = ((nc + kPipeChunks - 1) / kPipeChunks + kPipeTile - 1) / kPipeTile * kPipeTile;
+  const int nch = (int)((nc + chunk - 1) / chunk);
+  double* du = o->u;
+  cudaStream_t ms = o->stream;
+  // every side stream starts after the work already queued on the handle's stream
+  HRW_CUDA(cudaEventRecord(o->ev_start, ms));
+  for (cudaStream_t st : {o->pipe[0], o->pipe[1], o->copy}) HRW_CUDA(cudaStreamWaitEvent(st, o->ev_start, 0));
+  for (int i = 0; i < nch; ++i) {
+    const int64_t off = i * chunk, len = std::min(chunk, nc - off);
+    HRW_CUDA(cudaMemcpyAsync(du + off, uh + off, sizeof(double) * (size_t)len, cudaMemcpyHostToDevice, o->copy));
+    HRW_CUDA(cudaEventRecord(o->ev_in[i], o->copy));
+  }
+  // stage 1 of the first step, per chunk: its cells and the right neighbour's halo have arrived
+  for (int i = 0; i < nch; ++i) {
+    const int64_t off = i * chunk, len = std::min(chunk, nc - off);
+    cudaStream_t st = o->pipe[i & 1];
+    HRW_CUDA(cudaStreamWaitEvent(st, o->ev_in[std::min(i + 1, nch - 1)], 0));
+    HRW_CUDA(run_stage_range(o, ST_EULER, du, du, o->w1, off, len, dt, st));
+  }
+  for (int p = 0; p < 2; ++p) {
+    HRW_CUDA(cudaEventRecord(o->ev_join[p], o->pipe[p]));
+    HRW_CUDA(cudaStreamWaitEvent(ms, o->ev_join[p], 0));
+  }
+  for (int64_t s = 0; s < n; ++s) {
+    if (s > 0) HRW_CUDA(run_stage(o, ST_EULER, du, du, o->w1, nullptr, nullptr, nullptr, dt));
+    HRW_CUDA(run_stage(o, ST_RK3B, o->w1, du, o->w2, nullptr, nullptr, nullptr, dt));
+    if (s < n - 1) HRW_CUDA(run_stage(o, ST_RK3C, o->w2, du, du, nullptr, nullptr, nullptr, dt));
+  }
+  // stage 3 of the last step, per chunk, each chunk copied back behind it
+  HRW_CUDA(cudaEventRecord(o->ev_join[2], ms));
+  for (int p = 0; p < 2; ++p) HRW_CUDA(cudaStreamWaitEvent(o->pipe[p], o->ev_join[2], 0));
+  for (int i = 0; i < nch; ++i) {
+    const int64_t off = i * chunk, len = std::min(chunk, nc - off);
+    cudaStream_t st = o->pipe[i & 1];
+    HRW_CUDA(run_stage_range(o, ST_RK3C, o->w2, du, du, off, len, dt, st));
+    HRW_CUDA(cudaEventRecord(o->ev_s3[i], st));
+    HRW_CUDA(cudaStreamWaitEvent(o->copy, o->ev_s3[i], 0));
+    HRW_CUDA(cudaMemcpyAsync(uh + off, du + off, sizeof(double) * (size_t)len, cudaMemcpyDeviceToHost, o->copy));
+  }
+  HRW_CUDA(cudaEventRecord(o->ev_join[0], o->copy));
+  HRW_CUDA(cudaStreamWaitEvent(ms, o->ev_join[0], 0));  // later work on the handle's stream
+  *t = tt;
+  o->fevals += (int)(3 * n);
+  o->nsteps += n;
+  if (o->istate == 1) o->istate = 2;
+  return HRW_OK;
+}
+
 extern "C" int hrw_integrate(hrw_ode* o, int mem, void* u, double* t, double tout, double dt, int itask) {
   if (!o) return fail(HRW_EINVAL, "Invalid input 'ode': null handle.");
   if (!u || !t) return fail(HRW_EINVAL, "Invalid input: null pointer.");
@@ -805,6 +917,12 @@ extern "C" int hrw_integrate(hrw_ode* o, int mem, void* u, double* t, double tou
   if (itask != 1 && itask != 2) itask = 1;
   const size_t bytes = sizeof(double) * (size_t)o->neq;
   double* du = (double*)u;
+  if (mem == HRW_MEM_HOST && host_pipeline_ok(o, u)) {
+    const int rc = rk3_integrate_host(o, (double*)u, t, tout, dt, itask);
+    if (rc != HRW_OK) return rc;
+    HRW_CUDA(cudaStreamSynchronize(o->stream));
+    return HRW_OK;
+  }
   if (mem == HRW_MEM_HOST) {
     du = o->u;
     HRW_CUDA(cudaMemcpyAsync(du, u, bytes, cudaMemcpyHostToDevice, o->stream));

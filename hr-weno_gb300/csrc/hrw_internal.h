@@ -48,6 +48,10 @@ struct StageArgs {
   int64_t ld;         // row stride (nc1) of the 2D layout
   int upwind;         // Godunov flux of g(x) u with g > 0 everywhere: F = g vm (2D kernel)
   const double* cnu;  // non-uniform 1D line: weno coefficients cnu(0:k-1,-1:k-1,1:nc)
+  // uniform 1D line (stage1d_kernel): update only cells cell0 .. cell0 + ncell - 1 (ncell = 0:
+  // the whole line); cell0 and ncell are multiples of the launch's tile (1024 cells for lines
+  // of at least 2 x 152 x 1024 cells), so that ranges launched side by side write disjoint cells
+  int64_t cell0, ncell;
 };
 
 // ---- compensated FP32 form (hrw_f32c.cuh, stage1d_f32c.cu) ---------------------------------

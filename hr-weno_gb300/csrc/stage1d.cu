@@ -69,7 +69,7 @@ __global__ void __launch_bounds__(NT) stage1d_kernel(StageArgs a) {
   __shared__ double sR[NT + 1];  // sR[t+1] = vr of thread t's last cell; sR[0] = vr(s-1)
   const LineArgs& L = a.L;
   const int64_t nc = L.nc;
-  const int64_t s = (int64_t)blockIdx.x * T;
+  const int64_t s = a.cell0 + (int64_t)blockIdx.x * T;
   const int tid = threadIdx.x;
 
   for (int q = tid; q < T + 2 * H; q += NT) {
@@ -140,7 +140,9 @@ __global__ void __launch_bounds__(NT) stage1d_kernel(StageArgs a) {
 
 template <int K, int ST, bool STRICT, int NT, int C>
 static cudaError_t launch_shape(const StageArgs& a, cudaStream_t s) {
-  const int64_t nblk = ((int64_t)a.L.nc + NT * C - 1) / (NT * C);
+  const int64_t span = a.ncell > 0 ? a.ncell : (int64_t)a.L.nc - a.cell0;
+  const int64_t nblk = (span + NT * C - 1) / (NT * C);
+  if (nblk <= 0) return cudaSuccess;
   stage1d_kernel<K, ST, STRICT, NT, C><<<(unsigned)nblk, NT, 0, s>>>(a);
   return cudaGetLastError();
 }

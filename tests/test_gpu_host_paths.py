@@ -1,6 +1,6 @@
-"""integrate on host arrays: pageable arrays are copied in and out; page-locked arrays on a host
-whose memory the GPU reads through its page tables (NVLink-C2C) are updated in place by the
-stage kernels.  Every path gives the bits of the device-array path."""
+"""integrate on host arrays: pageable arrays are copied in and out; page-locked lines of at least
+2 x 152 x 1024 cells (rktvd order 3, FP64) overlap the copies with the first and last stages
+by chunks.  Every path gives the bits of the device-array path."""
 import numpy as np
 import pytest
 
@@ -8,7 +8,7 @@ pytestmark = pytest.mark.gpu
 
 
 @pytest.mark.parametrize("numerics", ["fast", "strict"])
-@pytest.mark.parametrize("n", [5000, 1 << 16])
+@pytest.mark.parametrize("n", [5000, 1 << 16, 1 << 19, (1 << 19) + 777])
 @pytest.mark.parametrize("itask", [1, 2])
 def test_host_arrays_match_device(hw, numerics, n, itask):
     import torch
