@@ -155,7 +155,7 @@ struct hrw_ode {
   // host lines with the copies overlapped (rk3_integrate_host): two compute streams and a copy
   // stream beside `stream`, and their events
   cudaStream_t pipe[2] = {}, copy = nullptr;
-  cudaEvent_t ev_start = nullptr, ev_in[8] = {}, ev_s3[8] = {}, ev_join[3] = {};
+  cudaEvent_t ev_start = nullptr, ev_in[16] = {}, ev_s3[16] = {}, ev_join[3] = {};
 };
 
 extern "C" {
@@ -822,12 +822,14 @@ static int ms_integrate_f32c(hrw_ode* o, double* du, double* t, double tout, dou
 }
 
 // rktvd(3) of a uniform FP64 line on a page-locked host array, with the copies overlapped:
-// the line is copied in by chunks of whole 1024-cell tiles, and stage 1 of the first step runs
+// the line is copied in by 16 chunks of whole 1024-cell tiles (measured: 4 and 8 chunks leave
+// more of the first and last copies exposed), and stage 1 of the first step runs
 // on each chunk as soon as it and its right neighbour (the halo) have landed; stage 3 of the
 // last step runs by chunks, each chunk's copy back following it.  Chunks alternate between two
 // streams, so the tail of one overlaps the next.  The arithmetic is that of rk_integrate.
-constexpr int kPipeChunks = 4;
+constexpr int kPipeChunks = 16;
 constexpr int64_t kPipeTile = 1024;
+static_assert(kPipeChunks <= (int)(sizeof(hrw_ode::ev_in) / sizeof(cudaEvent_t)), "one event per chunk");
 
 static bool host_pipeline_ok(const hrw_ode* o, const void* u) {
   if (o->dtype != HRW_F64 || o->prob.kind != HRW_PROBLEM_FV1D || o->method != 0 || o->order != 3 ||
