@@ -71,6 +71,14 @@ __global__ void __launch_bounds__(NT) stage1d_kernel(StageArgs a) {
   const int64_t nc = L.nc;
   const int64_t s = a.cell0 + (int64_t)blockIdx.x * T;
   const int tid = threadIdx.x;
+  // launched as a programmatic dependent of the previous kernel on the stream: wait here, before
+  // any memory access, until that kernel has completed and its writes are visible (its launch
+  // and this grid's scheduling overlap its tail)
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  // a grid of at most one wave (every block resident from the start) lets the next stage's
+  // grid launch at once, its blocks queueing behind this one's; larger grids trigger it as
+  // their blocks exit, so that waiting blocks take no slots from their later waves
+  if (gridDim.x <= 152 * 4) asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 
   for (int q = tid; q < T + 2 * H; q += NT) {
     int64_t g = s - H + q;
@@ -143,7 +151,17 @@ static cudaError_t launch_shape(const StageArgs& a, cudaStream_t s) {
   const int64_t span = a.ncell > 0 ? a.ncell : (int64_t)a.L.nc - a.cell0;
   const int64_t nblk = (span + NT * C - 1) / (NT * C);
   if (nblk <= 0) return cudaSuccess;
-  stage1d_kernel<K, ST, STRICT, NT, C><<<(unsigned)nblk, NT, 0, s>>>(a);
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = dim3((unsigned)nblk);
+  cfg.blockDim = dim3(NT);
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  const cudaError_t e = cudaLaunchKernelEx(&cfg, stage1d_kernel<K, ST, STRICT, NT, C>, a);
+  if (e != cudaSuccess) return e;
   return cudaGetLastError();
 }
 
