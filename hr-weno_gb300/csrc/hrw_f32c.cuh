@@ -187,8 +187,8 @@ __device__ __forceinline__ float flux_g(const LineF& L, float v, float a, float 
 }
 // physical flux minus the same base, for the free-outflow boundary: f(v + a) - f_base
 __device__ __forceinline__ float phys_g(const LineF& L, float v, float a, float g) {
-  if (L.fn == HRW_FN_BURGERS) return 0.5f * a * (2.f * v + a);
-  return g * a;
+  if (L.fn == HRW_FN_BURGERS) return __fmul_rn(__fmul_rn(0.5f, a), __fadd_rn(__fmul_rn(2.f, v), a));
+  return __fmul_rn(g, a);
 }
 // g at interface e (e <= nc < 2^31): the 32-bit conversion stays on the FP32 side; an int64
 // to float conversion would run on the narrow FP64 unit
@@ -212,15 +212,17 @@ __device__ __forceinline__ float flux_diff_f32c(const LineF& L, int64_t j, float
   float GR = flux_g(L, v, rr_j, d_j + rl_p, gR);
   float extra = lin ? L.gstep * v : 0.f;
   if (j == 0 || j == L.nc - 1) {
-    // boundary fluxes in full (no cancellation there): F = fbase + G
-    const float fbL = lin ? gL * v : 0.5f * v * v, fbR = lin ? gR * v : 0.5f * v * v;
-    float FL = fbL + GL, FR = fbR + GR;
+    // boundary fluxes in full (no cancellation there): F = fbase + G, each operation rounded
+    // as written (no contraction), so that inlined and out-of-line copies give the same bits
+    const float hv = __fmul_rn(__fmul_rn(0.5f, v), v);
+    const float fbL = lin ? __fmul_rn(gL, v) : hv, fbR = lin ? __fmul_rn(gR, v) : hv;
+    float FL = __fadd_rn(fbL, GL), FR = __fadd_rn(fbR, GR);
     if (L.bc == HRW_BC_COPY) {
       return 0.f;  // F_0 = F_1 or F_nc = F_{nc-1}: the boundary cell's difference vanishes
     }
     if (j == 0) FL = 0.f;
-    if (j == L.nc - 1) FR = L.bc == HRW_BC_ZERO ? 0.f : fbR + phys_g(L, v, rr_j, gR);
-    return FR - FL;
+    if (j == L.nc - 1) FR = L.bc == HRW_BC_ZERO ? 0.f : __fadd_rn(fbR, phys_g(L, v, rr_j, gR));
+    return __fsub_rn(FR, FL);
   }
   return __fadd_rn(GR - GL, extra);  // never contracted with gstep * v: one rounding order
 }
