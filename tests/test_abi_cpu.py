@@ -1,5 +1,6 @@
 """The C-ABI library loads and exports every entry point the header declares; validation
 mirrors the reference's constructors.  No compute call runs here (CPU only)."""
+import ctypes as C
 import re
 from pathlib import Path
 
@@ -50,3 +51,55 @@ def test_ode_validation_messages(hw):
     bad = burgers_1d(10, k=5)
     with pytest.raises(HrwError, match=r"Invalid input 'k'"):
         rktvd(bad, 10, 3)
+
+
+def _header_problem_fields():
+    """(name, count) of struct hrw_problem in include/hrweno_gpu.h, in order."""
+    import re
+    text = (ROOT / "include" / "hrweno_gpu.h").read_text()
+    body = text[text.index("typedef struct hrw_problem {"):text.index("} hrw_problem;")]
+    body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
+    fields = []
+    for m in re.finditer(r"([A-Za-z_][\w ]*?[\s*]+)(\w+)(?:\[(\d+)\])?;", body.split("{", 1)[1]):
+        fields.append((m.group(2), int(m.group(3) or 1)))
+    return fields
+
+
+def test_problem_layouts_agree():
+    """struct hrw_problem, its ctypes mirror and the Fortran bind(c) type in INTEGRATION.md list
+    the same fields in the same order (a missing field shifts every later one)."""
+    import re
+    import ctypes as C
+    from hrweno import _abi
+    hdr = _header_problem_fields()
+    cty = [(name, getattr(t, "_length_", 1)) for name, t in _abi.HrwProblem._fields_]
+    assert hdr == cty, (hdr, cty)
+    text = (ROOT / "INTEGRATION.md").read_text()
+    block = text[text.index("type, bind(c) :: hrw_problem"):]
+    block = block[:block.index("end type")]
+    fort = []
+    for line in block.splitlines()[1:]:
+        decl = line.split("::", 1)[1] if "::" in line else ""
+        for item in re.finditer(r"(\w+)(?:\((\d+)\))?", decl):
+            fort.append((item.group(1), int(item.group(2) or 1)))
+    assert fort == hdr, (fort, hdr)
+
+
+def test_problem_offsets_match_c_compiler(tmp_path):
+    """Offsets and size of struct hrw_problem as the C compiler lays it out, against ctypes."""
+    import shutil
+    import subprocess
+    from hrweno import _abi
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    names = [n for n, _ in _abi.HrwProblem._fields_]
+    src = tmp_path / "layout.c"
+    src.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "hrweno_gpu.h"\nint main(void) {\n'
+                   + "".join(f'  printf("%zu\\n", offsetof(hrw_problem, {n}));\n' for n in names)
+                   + '  printf("%zu\\n", sizeof(hrw_problem));\n  return 0;\n}\n')
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-I", str(ROOT / "include"), str(src), "-o", str(exe)], check=True)
+    got = [int(x) for x in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()]
+    want = [getattr(_abi.HrwProblem, n).offset for n in names] + [C.sizeof(_abi.HrwProblem)]
+    assert got == want, (got, want)
