@@ -349,7 +349,7 @@ cudaError_t launch_st(const F32CArgs& a, int stage, cudaStream_t s) {
 
 }  // namespace
 
-// ---- TMA descriptors: encoded through the driver entry point, cached by array ----------------
+// ---- TMA descriptors: cuTensorMapEncodeTiled (CUDA driver API), cached by array ---------------
 namespace {
 
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
