@@ -384,6 +384,7 @@ __device__ __forceinline__ bool uses_fl(int bc, int64_t lc, int64_t seg) {
 __device__ __forceinline__ double dflux(const AdjLine& A, double v, int64_t e) {
   // f'(v) at interface e (local index): Burgers u, linear g(x_e)
   if (A.fn == HRW_FN_BURGERS) return v;
+  if (A.fn == HRW_FN_BURGERS_LINEAR) return v + fma(A.b, fma(A.rx, (double)e, A.xmin), A.a);
   return fma(A.b, fma(A.rx, (double)e, A.xmin), A.a);
 }
 
@@ -685,7 +686,7 @@ int hrw_adjoint_create(const hrw_problem* p, int nseg, int checkpoint_every, hrw
   if (p->k < 1 || p->k > 3) return adj_fail(HRW_EINVAL, "Invalid input 'k'. Valid range: 1 <= k <= 3.");
   if (!(p->eps > 2.220446049250313e-16))
     return adj_fail(HRW_EINVAL, "Invalid input 'eps'. Valid range: eps > epsilon.");
-  if (p->fn[0] != HRW_FN_BURGERS && p->fn[0] != HRW_FN_LINEAR) return adj_fail(HRW_EINVAL, "Invalid input 'fn'.");
+  if (p->fn[0] < HRW_FN_BURGERS || p->fn[0] > HRW_FN_BURGERS_LINEAR) return adj_fail(HRW_EINVAL, "Invalid input 'fn'.");
   if (p->bc[0] < HRW_BC_COPY || p->bc[0] > HRW_BC_ZERO_INFLOW) return adj_fail(HRW_EINVAL, "Invalid input 'bc'.");
   if (nseg < 1) return adj_fail(HRW_EINVAL, "Invalid input 'nseg': must be >= 1.");
   if (nseg > 1 && p->ncells[0] % 8 != 0)

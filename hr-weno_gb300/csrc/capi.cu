@@ -71,7 +71,7 @@ int validate_problem(const hrw_problem* p, int neq) {
     if (p->ncells[d] <= 0) return fail(HRW_EINVAL, "Invalid input 'ncells'. Valid range: ncells > 0.");
     if (!(p->xmax[d] > p->xmin[d]))
       return fail(HRW_EINVAL, "Invalid input 'xmin', 'xmax'. Valid range: xmax > xmin.");
-    if (p->fn[d] != HRW_FN_BURGERS && p->fn[d] != HRW_FN_LINEAR)
+    if (p->fn[d] < HRW_FN_BURGERS || p->fn[d] > HRW_FN_BURGERS_LINEAR)
       return fail(HRW_EINVAL, "Invalid input 'fn'.");
     if (p->bc[d] < HRW_BC_COPY || p->bc[d] > HRW_BC_ZERO_INFLOW)
       return fail(HRW_EINVAL, "Invalid input 'bc'.");
@@ -297,6 +297,9 @@ static int ode_create(const hrw_problem* p, int neq, int order, int method, int 
       return fail(HRW_EINVAL, "Invalid input 'dtype': HRW_F32C supports FV1D and FV2D problems.");
     if (!(p->eps > 1.1920928955078125e-07))  // epsilon(1.0_real32), src/hrweno_weno.f90:92
       return fail(HRW_EINVAL, "Invalid input 'eps'. Valid range: eps > epsilon.");
+    for (int d = 0; d < (p->kind == HRW_PROBLEM_FV2D ? 2 : 1); ++d)
+      if (p->fn[d] == HRW_FN_BURGERS_LINEAR)  // its difference-form algebra is not written
+        return fail(HRW_EINVAL, "Invalid input 'fn': HRW_F32C supports BURGERS and LINEAR.");
   }
   hrw_ode* o = new hrw_ode;
   o->prob = *p;

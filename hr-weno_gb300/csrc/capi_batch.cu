@@ -201,7 +201,9 @@ int hrw_batch_create(const hrw_problem* probs, int nprob, int order, int dtype, 
     if (p.k < 1 || p.k > 3) return bad("Invalid input 'k'. Valid range: 1 <= k <= 3.");
     if (!(p.eps > 2.220446049250313e-16)) return bad("Invalid input 'eps'. Valid range: eps > epsilon.");
     if (p.flux != HRW_FLUX_LAX_FRIEDRICHS && p.flux != HRW_FLUX_GODUNOV) return bad("Invalid input 'flux'.");
-    if (p.fn[0] != HRW_FN_BURGERS && p.fn[0] != HRW_FN_LINEAR) return bad("Invalid input 'fn'.");
+    if (p.fn[0] < HRW_FN_BURGERS || p.fn[0] > HRW_FN_BURGERS_LINEAR) return bad("Invalid input 'fn'.");
+    if (p.fn[0] == HRW_FN_BURGERS_LINEAR && b->dtype == HRW_F32C)
+      return bad("Invalid input 'fn': HRW_F32C supports BURGERS and LINEAR.");
     if (p.bc[0] < HRW_BC_COPY || p.bc[0] > HRW_BC_ZERO_INFLOW) return bad("Invalid input 'bc'.");
     if (!(p.xmax[0] > p.xmin[0])) return bad("Invalid input 'xmin', 'xmax'. Valid range: xmax > xmin.");
     if ((p.numerics == HRW_NUMERICS_STRICT) != b->strict)

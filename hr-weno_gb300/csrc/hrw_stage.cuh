@@ -31,6 +31,13 @@ __device__ __forceinline__ double flux_fast(const LineArgs& L, double vm, double
     const double fm = vm * vm, fp = vp * vp;  // 2F
     return vm <= vp ? fmin(fm, fp) : fmax(fm, fp);
   }
+  if (L.fn == HRW_FN_BURGERS_LINEAR) {  // 2f(v) = v (v + 2g)
+    const double g2 = 2.0 * g_fast(L, e);
+    const double fm = vm * (vm + g2), fp = vp * (vp + g2);
+    if (L.flux == HRW_FLUX_LAX_FRIEDRICHS)  // 4F = 2f(vm) + 2f(vp) - 2 alpha (vp - vm)
+      return fma(-2.0 * L.alpha, vp - vm, fm + fp);
+    return vm <= vp ? fmin(fm, fp) : fmax(fm, fp);  // 2F
+  }
   const double g = g_fast(L, e);
   if (L.flux == HRW_FLUX_LAX_FRIEDRICHS)  // 2F = (g + alpha) vm + (g - alpha) vp
     return fma(g + L.alpha, vm, (g - L.alpha) * vp);
@@ -41,6 +48,7 @@ __device__ __forceinline__ double flux_fast(const LineArgs& L, double vm, double
 __device__ __forceinline__ double phys_fast(const LineArgs& L, double v, int64_t e) {
   const double s = L.flux == HRW_FLUX_LAX_FRIEDRICHS ? 2.0 : 1.0;
   if (L.fn == HRW_FN_BURGERS) return s * (v * v);
+  if (L.fn == HRW_FN_BURGERS_LINEAR) return s * (v * (v + 2.0 * g_fast(L, e)));
   return s * (g_fast(L, e) * v);
 }
 
@@ -51,6 +59,8 @@ __device__ __forceinline__ double g_strict(const LineArgs& L, int64_t e) {
 }
 __device__ __forceinline__ double phys_strict(const LineArgs& L, double v, int64_t e) {
   if (L.fn == HRW_FN_BURGERS) return __ddiv_rn(__dmul_rn(v, v), 2.0);
+  if (L.fn == HRW_FN_BURGERS_LINEAR)  // (u*u)/2 + (a + b*x)*u
+    return __dadd_rn(__ddiv_rn(__dmul_rn(v, v), 2.0), __dmul_rn(g_strict(L, e), v));
   return __dmul_rn(g_strict(L, e), v);
 }
 __device__ __forceinline__ double flux_strict(const LineArgs& L, double vm, double vp, int64_t e) {

@@ -65,7 +65,7 @@ extern "C" int hrw_rktvd3_steps_noalloc(const hrw_problem* p, double* u, double 
     return set_error(HRW_EINVAL, "Invalid input 'eps'. Valid range: eps > epsilon.");
   if (p->flux != HRW_FLUX_LAX_FRIEDRICHS && p->flux != HRW_FLUX_GODUNOV)
     return set_error(HRW_EINVAL, "Invalid input 'flux'.");
-  if (p->fn[0] != HRW_FN_BURGERS && p->fn[0] != HRW_FN_LINEAR)
+  if (p->fn[0] < HRW_FN_BURGERS || p->fn[0] > HRW_FN_BURGERS_LINEAR)
     return set_error(HRW_EINVAL, "Invalid input 'fn'.");
   if (p->bc[0] < HRW_BC_COPY || p->bc[0] > HRW_BC_ZERO_INFLOW)
     return set_error(HRW_EINVAL, "Invalid input 'bc'.");

@@ -25,8 +25,8 @@
 namespace hrw {
 
 double fast_flux_scale(int flux, int fn) {
-  if (flux == HRW_FLUX_LAX_FRIEDRICHS) return fn == HRW_FN_BURGERS ? 0.25 : 0.5;
-  return fn == HRW_FN_BURGERS ? 0.5 : 1.0;
+  if (flux == HRW_FLUX_LAX_FRIEDRICHS) return fn == HRW_FN_LINEAR ? 0.5 : 0.25;
+  return fn == HRW_FN_LINEAR ? 1.0 : 0.5;
 }
 
 bool positive_velocity(const LineArgs& L) {

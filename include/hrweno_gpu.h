@@ -60,8 +60,10 @@ enum {
   HRW_PROBLEM_LINEAR_ODE = 3  /* u_i' = a_i u_i (test/test_tvdode.f90:107-111) */
 };
 enum { HRW_FLUX_LAX_FRIEDRICHS = 0, HRW_FLUX_GODUNOV = 1 };
-/* physical flux f(u, x): BURGERS = u^2/2; LINEAR = (a + b*x) * u, x = interface coordinate */
-enum { HRW_FN_BURGERS = 0, HRW_FN_LINEAR = 1 };
+/* physical flux f(u, x): BURGERS = u^2/2; LINEAR = (a + b*x) * u, x = interface coordinate;
+ * BURGERS_LINEAR = u^2/2 + (a + b*x) * u (convex: Burgers carried by a velocity field; the FP64
+ * paths, not HRW_F32C) */
+enum { HRW_FN_BURGERS = 0, HRW_FN_LINEAR = 1, HRW_FN_BURGERS_LINEAR = 2 };
 /* domain-boundary fluxes (per dimension):
  *   COPY        F_{1/2} = F_{3/2}, F_{nc+1/2} = F_{nc-1/2}  (example1...f90:103-104)
  *   ZERO        F_{1/2} = F_{nc+1/2} = 0                   (example2...f90:117-120)

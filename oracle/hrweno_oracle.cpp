@@ -189,6 +189,7 @@ template <class T>
 static T phys_flux(int fn, T a, T b, T u, T x, T t) {
   if (fn == HRW_FN_BURGERS) return (u * u) / 2;  // example1...f90:111-122
   if (fn == FN_TEST_UXT) return u * x * t;
+  if (fn == HRW_FN_BURGERS_LINEAR) return (u * u) / 2 + (a + b * x) * u;  // Burgers + g(x) u
   return (a + b * x) * u;  // f = g(x) u, example2...f90:131-155 with g = a + b x
 }
 

@@ -103,3 +103,11 @@ def test_problem_offsets_match_c_compiler(tmp_path):
     got = [int(x) for x in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()]
     want = [getattr(_abi.HrwProblem, n).offset for n in names] + [C.sizeof(_abi.HrwProblem)]
     assert got == want, (got, want)
+
+
+def test_f32c_rejects_burgers_linear(hw):
+    from hrweno import HrwError
+    prob = hw.Problem(kind="fv1d", ncells=(100, 1), fn=("burgers_linear", "burgers_linear"),
+                      coef_a=(0.5, 0.0), xmin=(-1.0, 0.0), xmax=(1.0, 1.0))
+    with pytest.raises(HrwError, match=r"HRW_F32C supports BURGERS and LINEAR"):
+        hw.rktvd(prob, 100, 3, dtype="f32c")

@@ -116,3 +116,19 @@ def test_pbe_mstvd_stability_limit(orc):
         drift[cfl] = np.abs(out[0] - out[1]).sum() / np.abs(out[1]).sum()
     assert drift[0.3] < 1e-14
     assert drift[0.4] > 1e3 * drift[0.3]
+
+
+def test_flux_burgers_linear_consistency_and_upwinding(orc):
+    """f(u, x) = u^2/2 + (a + b x) u in the reference's flux checks (test/test_fluxes.f90:27-71):
+    h(v, v) = f(v) for both fluxes; Godunov takes the upwind state where f' keeps one sign."""
+    from hrweno import _abi as A
+    a, b, x = 0.5, 0.25, 2.0
+    f = lambda u: u * u / 2 + (a + b * x) * u  # noqa: E731
+    for v in (-3.0, 0.2, 1.7):
+        for kind in (A.HRW_FLUX_LAX_FRIEDRICHS, A.HRW_FLUX_GODUNOV):
+            h = orc.numflux(kind, A.HRW_FN_BURGERS_LINEAR, v, v, x, 0.0, alpha=5.0, a=a, b=b)
+            assert abs(h - f(v)) <= 1e-15 * max(1.0, abs(f(v)))
+    # f'(u) = u + 1 > 0 for u > -1: the flux from the left state
+    vm, vp = 0.4, 0.9
+    assert orc.numflux(A.HRW_FLUX_GODUNOV, A.HRW_FN_BURGERS_LINEAR, vm, vp, x, 0.0, a=a, b=b) == f(vm)
+    assert orc.numflux(A.HRW_FLUX_GODUNOV, A.HRW_FN_BURGERS_LINEAR, vp, vm, x, 0.0, a=a, b=b) == f(vp)
