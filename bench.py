@@ -212,10 +212,14 @@ def run_reference(args) -> None:
 
 
 def config_dict() -> dict:
-    return {"workload": "burgers1d_2^24_weno5_lf_rk3", "cells": NC, "k": 3, "eps": 1e-6,
+    mib = NC * 8 >> 20
+    name = "2^24" if NC == 1 << 24 else str(NC)
+    return {"workload": f"burgers1d_{name}_weno5_lf_rk3", "cells": NC, "k": 3, "eps": 1e-6,
             "flux": "lax_friedrichs", "alpha": "max|u0|", "bc": "copy", "cfl": 0.4,
             "integrator": "rktvd order 3", "numerics": "fast",
-            "l2": "inputs larger than L2: u, u1, u2 are 128 MiB each (384 MiB working set)"}
+            "l2": (f"inputs larger than L2: u, u1, u2 are {mib} MiB each ({3 * mib} MiB working set)"
+                   if 3 * NC * 8 > 126 << 20 else
+                   f"L2-resident: u, u1, u2 are {NC * 8 >> 10} KiB each (a reduced line, not the benchmark workload)")}
 
 
 # ------------------------------------------------------------------------------------------
