@@ -1,6 +1,6 @@
 """A second, independent restatement of the reference's formulas -- vectorised numpy, written
-from src/hrweno_weno.f90 and example/example1_burgers_1d_fv.f90 -- against the C++ oracle on
-random inputs (CPU only).  The oracle is pinned to the reference's known-answer tests; this
+from src/hrweno_weno.f90, src/hrweno_fluxes.f90, src/hrweno_tvdode.f90 and the two example
+drivers -- against the C++ oracle on random inputs (CPU only).  The oracle is pinned to the reference's known-answer tests; this
 checks it everywhere else, to rounding level (numpy sums in its own order)."""
 import numpy as np
 import pytest
@@ -93,3 +93,96 @@ def test_burgers_rhs_matches_numpy(hw, orc, k, flux, bc, nc):
         got = rhs_burgers_np(v, -5.0, 5.0, k, 1e-6, flux, 1.3, bc)
         scale = max(np.max(np.abs(ref)), 1e-300)
         assert np.max(np.abs(got - ref)) <= 1e-12 * scale, (k, flux, bc, nc)
+
+
+def numflux_np(flux, f, vm, vp, alpha):
+    """lax_friedrichs / godunov (src/hrweno_fluxes.f90:43,67-74), elementwise."""
+    if flux == "lax_friedrichs":
+        return (f(vm) + f(vp) - alpha * (vp - vm)) / 2
+    fm, fp = f(vm), f(vp)
+    return np.where(vm <= vp, np.minimum(fm, fp), np.maximum(fm, fp))
+
+
+def sweep_np(lines_, k, eps, flux, alpha, bc, g_at, dx):
+    """One direction of example2's right-hand side (example/example2_pbe_2d_fv.f90:96-120) for a
+    stack of lines [m, n]: -dF/dx of f = g(x) u with g at the interfaces (g_at(e), e = 0..n)."""
+    m, n = lines_.shape
+    out = np.empty_like(lines_)
+    ge = g_at(np.arange(n + 1))
+    for r in range(m):
+        vl, vr = reconstruct_np(lines_[r], k, eps)
+        F = np.zeros(n + 1)
+        g = ge[1:n]
+        F[1:n] = numflux_np(flux, lambda u: g * u, vr[:-1], vl[1:], alpha)  # noqa: B023
+        if bc == "copy" and n > 1:
+            F[0], F[n] = F[1], F[n - 1]
+        elif bc == "zero_inflow":
+            F[n] = ge[n] * vr[-1]
+        out[r] = -(F[1:] - F[:-1]) / dx
+    return out
+
+
+@pytest.mark.parametrize("flux", ["lax_friedrichs", "godunov"])
+@pytest.mark.parametrize("bc", ["zero", "zero_inflow", "copy"])
+@pytest.mark.parametrize("shape", [(1, 1), (5, 7), (40, 24)])
+def test_pbe_rhs_matches_numpy(hw, orc, flux, bc, shape):
+    """example2's dimension-by-dimension right-hand side, u((j-1) n1 + i): x1 rows, then x2
+    columns, vdot = -dF1/dx1 - dF2/dx2 (:123-127)."""
+    n1, n2 = shape
+    g1, g2 = (1.0, 0.5), (0.5, -0.2)
+    prob = hw.pbe_2d(n1, n2, g1=g1, g2=g2, k=3, flux=flux, bc=bc, numerics="strict")
+    rng = np.random.default_rng(n1 + n2)
+    v = np.abs(rng.standard_normal(n1 * n2)) + 0.1
+    ref = orc.rhs(prob, v)
+    u = v.reshape(n2, n1)
+    dx1, dx2 = 1.0 / n1, 1.0 / n2
+    a1 = sweep_np(u, 3, 1e-6, flux, abs(g1[0]) + abs(g1[1]), bc,
+                  lambda e: g1[0] + g1[1] * (e * dx1), dx1)
+    a2 = sweep_np(u.T.copy(), 3, 1e-6, flux, abs(g2[0]) + abs(g2[1]), bc,
+                  lambda e: g2[0] + g2[1] * (e * dx2), dx2).T
+    got = (a1 + a2).reshape(-1)
+    scale = max(np.max(np.abs(ref)), 1e-300)
+    assert np.max(np.abs(got - ref)) <= 1e-12 * scale
+
+
+def rk3_step(u, dt, L):
+    """src/hrweno_tvdode.f90:160-171 (the stage formulas as written)."""
+    u1 = u + dt * L(u)
+    u2 = (3 * u + u1 + dt * L(u1)) / 4
+    return (u + 2 * u2 + 2 * dt * L(u2)) / 3
+
+
+def test_rktvd3_and_mstvd_match_numpy(hw, orc):
+    """rktvd(3) steps and mstvd (its RK3 start and equation 4.26 with the history shift,
+    src/hrweno_tvdode.f90:236-265) restated in numpy on example1's right-hand side."""
+    nc, dt = 200, 5e-3
+    prob = hw.burgers_1d(nc, -5.0, 5.0, k=3, eps=1e-6, flux="lax_friedrichs", alpha=1.0, bc="copy",
+                         numerics="strict")
+    x = -5.0 + 10.0 / nc * (np.arange(nc) + 0.5)
+    u0 = np.exp(-x * x)
+    L = lambda u: rhs_burgers_np(u, -5.0, 5.0, 3, 1e-6, "lax_friedrichs", 1.0, "copy")  # noqa: E731
+    # rktvd(3), 12 steps
+    u = u0.copy()
+    for _ in range(12):
+        u = rk3_step(u, dt, L)
+    o = orc.ODE(prob, nc, 0, 3)
+    uo = u0.copy()
+    o.integrate(uo, 0.0, 11.5 * dt, dt)
+    assert np.max(np.abs(uo - u)) <= 1e-12 * np.max(np.abs(u))
+    # mstvd: 4 RK3 start steps recording u and L(u) (oldest first), then 10 multistep steps
+    u = u0.copy()
+    hu, hl = [], []
+    for _ in range(4):
+        hu.append(u.copy())
+        hl.append(L(u))
+        u = rk3_step(u, dt, L)
+    for _ in range(10):
+        ud = L(u)
+        ui = (25 * u + 50 * dt * ud + 7 * hu[0] + 10 * dt * hl[0]) / 32
+        hu = hu[1:] + [u.copy()]
+        hl = hl[1:] + [ud]
+        u = ui
+    o = orc.ODE(prob, nc, 1)
+    uo = u0.copy()
+    o.integrate(uo, 0.0, 13.5 * dt, dt)
+    assert np.max(np.abs(uo - u)) <= 1e-12 * np.max(np.abs(u))
