@@ -3,7 +3,7 @@
 Tolerances:
   STRICT numerics  bit-identical to the oracle (same IEEE operations in the same order).
   FAST numerics    normwise relative error max|gpu - oracle| / max|oracle| <= 1e-12 for
-                   integrations (spec bound), <= 1e-13 for one reconstruction / rhs.
+                   integrations (the 1e-12 relative parity bound), <= 1e-13 for one reconstruction / rhs.
 """
 import json
 from pathlib import Path
