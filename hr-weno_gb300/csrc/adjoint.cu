@@ -733,6 +733,7 @@ static int adjoint_sweep(hrw_adjoint* h, int mem, const double* u0, const double
                          const double* lambda_T, double dt, int64_t nsteps, double* J, double* grad) {
   if (!h) return adj_fail(HRW_EINVAL, "Invalid input 'adjoint': null handle.");
   if (!u0 || !(target || lambda_T) || !grad) return adj_fail(HRW_EINVAL, "Invalid input: null pointer.");
+  if (mem != HRW_MEM_HOST && mem != HRW_MEM_DEVICE) return adj_fail(HRW_EINVAL, "Invalid input 'mem'.");
   if (nsteps < 1) return adj_fail(HRW_EINVAL, "Invalid input 'nsteps': must be >= 1.");
   if (!(dt != 0.0) || !std::isfinite(dt)) return adj_fail(HRW_EINVAL, "Invalid input 'dt'.");
   const AdjLine& L = h->line;
@@ -857,6 +858,7 @@ int hrw_adjoint_forward(hrw_adjoint* h, int mem, const double* u0, const double*
                         int64_t nsteps, double* J, double* uT) {
   if (!h) return adj_fail(HRW_EINVAL, "Invalid input 'adjoint': null handle.");
   if (!u0) return adj_fail(HRW_EINVAL, "Invalid input: null pointer.");
+  if (mem != HRW_MEM_HOST && mem != HRW_MEM_DEVICE) return adj_fail(HRW_EINVAL, "Invalid input 'mem'.");
   const AdjLine& L = h->line;
   const size_t bytes = sizeof(double) * (size_t)L.n;
   const cudaMemcpyKind in = mem == HRW_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;

@@ -227,6 +227,7 @@ int hrw_weno_reconstruct(hrw_weno* w, int dtype, int mem, const void* v, void* v
   if (!w) return fail(HRW_EINVAL, "Invalid input 'w': null handle.");
   if (!v || !vl || !vr) return fail(HRW_EINVAL, "Invalid input: null array.");
   if (dtype != HRW_F64) return fail(HRW_EINVAL, "Invalid input 'dtype': reconstruct supports HRW_F64.");
+  if (mem != HRW_MEM_HOST && mem != HRW_MEM_DEVICE) return fail(HRW_EINVAL, "Invalid input 'mem'.");
   const size_t bytes = sizeof(double) * (size_t)w->nc;
   const double* dv = (const double*)v;
   double* dl = (double*)vl;
@@ -566,22 +567,27 @@ constexpr int64_t kMsPeriod = 20;
 
 // Replay `reps` times a graph of `steps` steps recorded by `record` (which launches them on
 // o->stream).  The graph is captured once and reused while the device array, dt, stream, ring
-// phase and step count stay the same.  Returns false (nothing launched) when capture is not
-// possible on this stream; the caller then launches the steps one by one.
+// phase and step count stay the same.  *replayed = false (nothing launched, cudaSuccess) when
+// capture is not possible on this stream; the caller then launches the steps one by one.  A
+// replay that fails returns its error: the replays before it have run, so the steps cannot be
+// launched again from the start.
 template <class Record>
-static bool run_graph(hrw_ode* o, const void* ptr, double dt, int64_t phase, int64_t steps,
-                      int64_t reps, Record record) {
+static cudaError_t run_graph(hrw_ode* o, const void* ptr, double dt, int64_t phase, int64_t steps,
+                             int64_t reps, bool* replayed, Record record) {
+  *replayed = false;
   auto& g = o->graph;
   if (!g.exec || g.ptr != ptr || g.dt != dt || g.stream != o->stream || g.phase != phase ||
       g.steps != steps) {
     if (g.exec) cudaGraphExecDestroy(g.exec);
     g.exec = nullptr;
     cudaStreamCaptureStatus st;
-    if (cudaStreamIsCapturing(o->stream, &st) != cudaSuccess || st != cudaStreamCaptureStatusNone)
-      return false;
+    if (cudaStreamIsCapturing(o->stream, &st) != cudaSuccess || st != cudaStreamCaptureStatusNone) {
+      cudaGetLastError();
+      return cudaSuccess;
+    }
     if (cudaStreamBeginCapture(o->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
       cudaGetLastError();
-      return false;
+      return cudaSuccess;
     }
     const cudaError_t rec = record();
     cudaGraph_t graph = nullptr;
@@ -591,14 +597,17 @@ static bool run_graph(hrw_ode* o, const void* ptr, double dt, int64_t phase, int
       if (graph) cudaGraphDestroy(graph);
       g.exec = nullptr;
       cudaGetLastError();
-      return false;
+      return cudaSuccess;
     }
     cudaGraphDestroy(graph);
     g.ptr = ptr, g.dt = dt, g.stream = o->stream, g.phase = phase, g.steps = steps;
   }
-  for (int64_t r = 0; r < reps; ++r)
-    if (cudaGraphLaunch(g.exec, o->stream) != cudaSuccess) return false;
-  return true;
+  for (int64_t r = 0; r < reps; ++r) {
+    const cudaError_t e = cudaGraphLaunch(g.exec, o->stream);
+    if (e != cudaSuccess) return e;
+  }
+  *replayed = true;
+  return cudaSuccess;
 }
 
 // steps per graph of an rktvd integration of n steps (0: no graph)
@@ -622,7 +631,8 @@ static int rk_integrate(hrw_ode* o, double* du, double* t, double tout, double d
   double* other = o->w2;
   int64_t s0 = 0;
   if (const int64_t G = rk_graph_steps(o, n)) {
-    const bool ok = run_graph(o, du, dt, 0, G, n / G, [&]() {
+    bool ok = false;
+    HRW_CUDA(run_graph(o, du, dt, 0, G, n / G, &ok, [&]() {
       double* c = du;
       double* w = o->w2;
       for (int64_t s = 0; s < G; ++s) {
@@ -631,7 +641,7 @@ static int rk_integrate(hrw_ode* o, double* du, double* t, double tout, double d
         if (o->order == 1) std::swap(c, w);
       }
       return cudaSuccess;
-    });
+    }));
     if (ok) s0 = n / G * G;
   }
   for (int64_t s = s0; s < n; ++s) {
@@ -684,13 +694,14 @@ static int ms_integrate(hrw_ode* o, double* du, double* t, double tout, double d
   if (o->use_graphs && n >= kMsPeriod) {
     const int64_t m0 = o->level;
     const int64_t G = n < 3 * kMsPeriod ? kMsPeriod : 3 * kMsPeriod;
-    const bool ok = run_graph(o, o->ring_u[0], dt, m0 % kMsPeriod, G, n / G, [&]() {
+    bool ok = false;
+    HRW_CUDA(run_graph(o, o->ring_u[0], dt, m0 % kMsPeriod, G, n / G, &ok, [&]() {
       for (int64_t s = 0; s < G; ++s) {
         const cudaError_t e = ms_step(m0 + s);
         if (e != cudaSuccess) return e;
       }
       return cudaSuccess;
-    });
+    }));
     if (ok) {
       s0 = n / G * G;
       for (int64_t s = 0; s < s0; ++s) tt = tt + dt;
@@ -768,13 +779,14 @@ static int rk_integrate_f32c(hrw_ode* o, double* du, double* t, double tout, dou
   int64_t G = rk_graph_steps(o, n);
   G &= ~int64_t(1);  // the compensated form always ping-pongs its (hi, lo) slots
   if (G) {
-    const bool ok = run_graph(o, o->fhi[0], dt, 0, G, n / G, [&]() {
+    bool ok = false;
+    HRW_CUDA(run_graph(o, o->fhi[0], dt, 0, G, n / G, &ok, [&]() {
       for (int64_t s = 0; s < G; ++s) {
         const cudaError_t e = rk_step_f32c(o, (int)(s & 1), (int)(1 - (s & 1)), dt);
         if (e != cudaSuccess) return e;
       }
       return cudaSuccess;
-    });
+    }));
     if (ok) s0 = n / G * G;
   }
   for (int64_t s = s0; s < n; ++s) {
@@ -912,14 +924,24 @@ static int rk3_integrate_host(hrw_ode* o, double* uh, double* t, double tout, do
   return HRW_OK;
 }
 
+static int integrate_on(hrw_ode* o, int mem, void* u, double* t, double tout, double dt, int itask);
+
 extern "C" int hrw_integrate(hrw_ode* o, int mem, void* u, double* t, double tout, double dt, int itask) {
   if (!o) return fail(HRW_EINVAL, "Invalid input 'ode': null handle.");
   if (!u || !t) return fail(HRW_EINVAL, "Invalid input: null pointer.");
+  if (mem != HRW_MEM_HOST && mem != HRW_MEM_DEVICE) return fail(HRW_EINVAL, "Invalid input 'mem'.");
   if (o->istate < 1) return fail(HRW_ESTATE, "ode is in an error state.");  // (:126,228)
   if (is_done(*t, tout, dt)) return HRW_OK;                                  // (:127,229)
   if (!(dt != 0.0) || !std::isfinite(dt) || !std::isfinite(*t) || !std::isfinite(tout))
     return fail(HRW_EINVAL, "Invalid input 'dt': must be finite and nonzero.");
   if (itask != 1 && itask != 2) itask = 1;
+  const int rc = integrate_on(o, mem, u, t, tout, dt, itask);
+  // a CUDA failure part-way leaves u (and the mstvd history) undefined: later calls refuse
+  if (rc == HRW_ECUDA || rc == HRW_ENOMEM) o->istate = -1;
+  return rc;
+}
+
+static int integrate_on(hrw_ode* o, int mem, void* u, double* t, double tout, double dt, int itask) {
   const size_t bytes = sizeof(double) * (size_t)o->neq;
   double* du = (double*)u;
   if (mem == HRW_MEM_HOST && host_pipeline_ok(o, u)) {

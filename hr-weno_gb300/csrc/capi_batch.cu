@@ -295,6 +295,7 @@ int hrw_batch_integrate(hrw_batch* b, int mem, double* u, double* t, double tout
                         int itask) {
   if (!b) return batch_fail(HRW_EINVAL, "Invalid input 'batch': null handle.");
   if (!u || !t || !dt) return batch_fail(HRW_EINVAL, "Invalid input: null pointer.");
+  if (mem != HRW_MEM_HOST && mem != HRW_MEM_DEVICE) return batch_fail(HRW_EINVAL, "Invalid input 'mem'.");
   std::vector<double> tnew(b->nprob);
   for (int i = 0; i < b->nprob; ++i) {
     const double h = dt[i];
@@ -336,6 +337,7 @@ int hrw_batch_integrate(hrw_batch* b, int mem, double* u, double* t, double tout
 int hrw_batch_advance(hrw_batch* b, int mem, double* u, double* t, const double* dt, int64_t nsteps) {
   if (!b) return batch_fail(HRW_EINVAL, "Invalid input 'batch': null handle.");
   if (!u || !t || !dt) return batch_fail(HRW_EINVAL, "Invalid input: null pointer.");
+  if (mem != HRW_MEM_HOST && mem != HRW_MEM_DEVICE) return batch_fail(HRW_EINVAL, "Invalid input 'mem'.");
   if (nsteps < 0) return batch_fail(HRW_EINVAL, "Invalid input 'nsteps': must be >= 0.");
   for (int i = 0; i < b->nprob; ++i) {
     if (!(dt[i] != 0.0) || !std::isfinite(dt[i]) || !std::isfinite(t[i]))
@@ -369,6 +371,7 @@ int hrw_batch_advance(hrw_batch* b, int mem, double* u, double* t, const double*
 int hrw_batch_tune(hrw_batch* b, int mem, const double* u, const double* dt, int probe_steps,
                    const char* cache_path) {
   if (!b || !u || !dt) return batch_fail(HRW_EINVAL, "Invalid input: null pointer.");
+  if (mem != HRW_MEM_HOST && mem != HRW_MEM_DEVICE) return batch_fail(HRW_EINVAL, "Invalid input 'mem'.");
   if (probe_steps < 1) probe_steps = 1;
   std::vector<std::pair<std::string, int>> cache;
   if (cache_path) {

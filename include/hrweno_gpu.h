@@ -51,6 +51,8 @@ enum {
  *           difference form (compensated neighbour differences, flux differences relative
  *           to each cell's own flux, two-sum accumulation of u); t stays FP64. */
 enum { HRW_F64 = 0, HRW_F32 = 1, HRW_F32C = 2 };
+/* Memory space of the arrays a call receives: host arrays are copied in and out (page-locked
+ * ones asynchronously); device arrays are used in place.  Other values return HRW_EINVAL. */
 enum { HRW_MEM_HOST = 0, HRW_MEM_DEVICE = 1 };
 
 /* ---- problem descriptor: the right-hand side L(u) -------------------------------- */
@@ -131,7 +133,9 @@ int hrw_rktvd_create(const hrw_problem* p, int neq, int order, int dtype, hrw_od
 int hrw_mstvd_create(const hrw_problem* p, int neq, int dtype, hrw_ode** out);
 /* ode%integrate(u, t, tout, dt[, itask]): u (neq elements of the ode's dtype) is updated
  * in place, *t advances like the reference (it stops at the first step with t > tout).
- * itask: 1 normal integration until tout, 2 single step. */
+ * itask: 1 normal integration until tout, 2 single step.  A CUDA failure part-way leaves u
+ * undefined and puts the handle in the error state (istate = -1; later calls return
+ * HRW_ESTATE), as the reference's integrate refuses to continue after an error. */
 int hrw_integrate(hrw_ode* ode, int mem, void* u, double* t, double tout, double dt, int itask);
 /* fevals, istate (1 first call, 2 later calls, -1 error) and steps taken so far. */
 int hrw_ode_info(const hrw_ode* ode, int* fevals, int* istate, int64_t* nsteps);

@@ -300,6 +300,26 @@ def test_integrate_already_done_is_noop(hw):
     assert t == 1.0 and np.array_equal(u, u0) and g.fevals == 0 and g.istate == 1
 
 
+def test_invalid_memory_space_is_rejected(hw):
+    """A memory-space flag other than HRW_MEM_HOST / HRW_MEM_DEVICE returns HRW_EINVAL before any
+    copy or launch; u, t and the handle are untouched and the handle stays usable."""
+    import ctypes as C
+    from hrweno import _abi as A
+    prob, u0 = config1(hw, "fast")
+    g = hw.rktvd(prob, 500, 3)
+    u = u0.copy()
+    t = C.c_double(0.0)
+    assert A.lib().hrw_integrate(g._h, 7, u.ctypes.data, C.byref(t), 1.0, 1e-2, 1) == A.HRW_EINVAL
+    assert A.lib().hrw_last_error().decode() == "Invalid input 'mem'."
+    assert t.value == 0.0 and np.array_equal(u, u0) and g.istate == 1 and g.nsteps == 0
+    w = hw.weno(500)
+    vl, vr = np.zeros(500), np.zeros(500)
+    assert A.lib().hrw_weno_reconstruct(w._h, A.HRW_F64, -1, u.ctypes.data, vl.ctypes.data,
+                                        vr.ctypes.data) == A.HRW_EINVAL
+    assert not vl.any() and not vr.any()
+    assert g.integrate(u, 0.0, 1.0, 1e-2) > 1.0 and g.istate == 2
+
+
 def stretched_edges(nc, kind, seed=0):
     if kind == "cubic":  # test/test_hrweno.f90:123-128 stretches edges as (i/nc)^3
         return -1.0 + 2.0 * (np.arange(nc + 1) / nc) ** 3
