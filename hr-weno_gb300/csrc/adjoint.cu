@@ -859,6 +859,8 @@ int hrw_adjoint_forward(hrw_adjoint* h, int mem, const double* u0, const double*
   if (!h) return adj_fail(HRW_EINVAL, "Invalid input 'adjoint': null handle.");
   if (!u0) return adj_fail(HRW_EINVAL, "Invalid input: null pointer.");
   if (mem != HRW_MEM_HOST && mem != HRW_MEM_DEVICE) return adj_fail(HRW_EINVAL, "Invalid input 'mem'.");
+  if (nsteps < 0) return adj_fail(HRW_EINVAL, "Invalid input 'nsteps': must be >= 0.");
+  if (!(dt != 0.0) || !std::isfinite(dt)) return adj_fail(HRW_EINVAL, "Invalid input 'dt'.");
   const AdjLine& L = h->line;
   const size_t bytes = sizeof(double) * (size_t)L.n;
   const cudaMemcpyKind in = mem == HRW_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;

@@ -387,7 +387,15 @@ int hrw_batch_tune(hrw_batch* b, int mem, const double* u, const double* dt, int
                             b->main));
   if (b->dtype == HRW_F32C)
     HRW_BCUDA(launch_split_f64(b->u, b->fmem, b->fmem + b->total, b->total, b->main));
-  cudaEvent_t e0, e1;
+  struct Events {  // destroyed on every return, early ones included
+    cudaEvent_t e[2] = {};
+    ~Events() {
+      for (cudaEvent_t x : e)
+        if (x) cudaEventDestroy(x);
+    }
+  } ev;
+  cudaEvent_t& e0 = ev.e[0];
+  cudaEvent_t& e1 = ev.e[1];
   HRW_BCUDA(cudaEventCreate(&e0));
   HRW_BCUDA(cudaEventCreate(&e1));
   bool wrote = false;
@@ -426,8 +434,6 @@ int hrw_batch_tune(hrw_batch* b, int mem, const double* u, const double* dt, int
     cache.emplace_back(key, best_s);
     wrote = true;
   }
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
   b->tuned = true;
   if (wrote && cache_path) {
     std::ofstream outf(cache_path);
