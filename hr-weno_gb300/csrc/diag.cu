@@ -6,6 +6,7 @@
 
 #include "../../include/hrweno_diag.h"
 #include "../../include/hrweno_gpu.h"
+#include "hrw_internal.h"
 
 namespace {
 
@@ -26,28 +27,33 @@ __global__ void fma_chains(T* out, int iters, T a, T b) {
 template <typename T>
 int rate(int iters, double* result) {
   int dev = 0, sms = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess) return HRW_ECUDA;
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return hrw::set_error(HRW_ECUDA, cudaGetErrorString(e));
   const int blocks = sms * 8, threads = 256;
   T* buf = nullptr;
-  if (cudaMalloc(&buf, sizeof(T) * (size_t)blocks * threads) != cudaSuccess) return HRW_ENOMEM;
-  cudaEvent_t e0, e1;
-  cudaEventCreate(&e0);
-  cudaEventCreate(&e1);
+  if ((e = cudaMalloc(&buf, sizeof(T) * (size_t)blocks * threads)) != cudaSuccess)
+    return hrw::set_error(HRW_ENOMEM, cudaGetErrorString(e));
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  e = cudaEventCreate(&e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&e1);
   float best = 1e30f;
-  for (int rep = 0; rep < 3; ++rep) {
-    cudaEventRecord(e0);
-    fma_chains<T><<<blocks, threads>>>(buf, iters, T(0.999999), T(1e-7));
-    cudaEventRecord(e1);
-    cudaEventSynchronize(e1);
+  for (int rep = 0; rep < 3 && e == cudaSuccess; ++rep) {
+    e = cudaEventRecord(e0);
+    if (e == cudaSuccess) {
+      fma_chains<T><<<blocks, threads>>>(buf, iters, T(0.999999), T(1e-7));
+      e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(e1);
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
     float ms = 0;
-    cudaEventElapsedTime(&ms, e0, e1);
-    if (ms < best) best = ms;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+    if (e == cudaSuccess && ms < best) best = ms;
   }
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
   cudaFree(buf);
-  if (cudaGetLastError() != cudaSuccess) return HRW_ECUDA;
+  if (e != cudaSuccess) return hrw::set_error(HRW_ECUDA, cudaGetErrorString(e));
   *result = (double)blocks * threads * iters * 16 * 8 / (best * 1e-3);
   return HRW_OK;
 }
