@@ -14,7 +14,7 @@ import ctypes as C
 import numpy as np
 
 from . import _abi as A
-from ._arrays import describe
+from ._arrays import describe, same_space
 from .problems import Problem
 
 
@@ -61,8 +61,7 @@ class adjoint:  # noqa: N801
         if grad is None:
             grad = u0.new_empty(u0.shape) if hasattr(u0, "new_empty") else np.empty_like(u0)
         m2, p2, _ = describe(grad, self.size, True)
-        if not m0 == m1 == m2:
-            raise ValueError("u0, target and grad must share one memory space")
+        same_space(m0, m1, m2)
         J = np.empty(self.nseg)
         A.check(A.lib().hrw_adjoint_gradient(self._h, m0, p0, p1, float(dt), int(nsteps),
                                              J.ctypes.data_as(C.POINTER(C.c_double)), p2))
@@ -71,12 +70,16 @@ class adjoint:  # noqa: N801
     def forward(self, u0, target, dt: float, nsteps: int, uT=None):
         """(J, uT) of the forward solve alone (J is None when target is None)."""
         m0, p0, _ = describe(u0, self.size, False)
+        mems = [m0]
         p1 = None
         if target is not None:
-            _, p1, _ = describe(target, self.size, False)
+            m1, p1, _ = describe(target, self.size, False)
+            mems.append(m1)
         pT = None
         if uT is not None:
-            _, pT, _ = describe(uT, self.size, True)
+            mT, pT, _ = describe(uT, self.size, True)
+            mems.append(mT)
+        same_space(*mems)
         J = np.empty(self.nseg)
         A.check(A.lib().hrw_adjoint_forward(self._h, m0, p0, p1, float(dt), int(nsteps),
                                             J.ctypes.data_as(C.POINTER(C.c_double)), pT))
@@ -85,10 +88,11 @@ class adjoint:  # noqa: N801
     def vjp(self, u0, lambda_T, dt: float, nsteps: int, grad=None):
         """d <lambda_T, u(T)> / du0."""
         m0, p0, _ = describe(u0, self.size, False)
-        _, p1, _ = describe(lambda_T, self.size, False)
+        m1, p1, _ = describe(lambda_T, self.size, False)
         if grad is None:
             grad = u0.new_empty(u0.shape) if hasattr(u0, "new_empty") else np.empty_like(u0)
-        _, p2, _ = describe(grad, self.size, True)
+        m2, p2, _ = describe(grad, self.size, True)
+        same_space(m0, m1, m2)
         A.check(A.lib().hrw_adjoint_vjp(self._h, m0, p0, p1, float(dt), int(nsteps), p2))
         return grad
 

@@ -6,7 +6,7 @@ import ctypes as C
 import numpy as np
 
 from . import _abi as A
-from ._arrays import describe
+from ._arrays import describe, same_space
 
 
 class weno:  # noqa: N801 - the reference's type name
@@ -36,11 +36,12 @@ class weno:  # noqa: N801 - the reference's type name
 
     def reconstruct(self, v, vl, vr) -> None:
         """vl(i) = v^+_{i-1/2}, vr(i) = v^-_{i+1/2} (src/hrweno_weno.f90:129-219)."""
-        m0, p0, d0 = describe(v, self.ncells, False)
-        m1, p1, d1 = describe(vl, self.ncells, True)
-        m2, p2, d2 = describe(vr, self.ncells, True)
-        if not (m0 == m1 == m2 and d0 == d1 == d2):
-            raise ValueError("v, vl and vr must share memory space and dtype")
+        m0, p0, d0 = describe(v, self.ncells, False, f64_only=False)
+        m1, p1, d1 = describe(vl, self.ncells, True, f64_only=False)
+        m2, p2, d2 = describe(vr, self.ncells, True, f64_only=False)
+        same_space(m0, m1, m2)
+        if not d0 == d1 == d2:
+            raise ValueError("v, vl and vr must share one element type")
         A.check(A.lib().hrw_weno_reconstruct(self._h, d0, m0, p0, p1, p2))
 
     @property
