@@ -63,6 +63,15 @@ class batch:  # noqa: N801
         """Length of the packed state."""
         return int(self.offsets[-1])
 
+    def _check_times(self, t, dt) -> None:
+        """t (updated in place: a float64 numpy array) and dt hold one value per problem."""
+        if t is not None and not (isinstance(t, np.ndarray) and t.dtype == np.float64
+                                  and t.ndim == 1 and t.size == self.nprob and t.flags.c_contiguous
+                                  and t.flags.writeable):
+            raise ValueError(f"t must be a writable contiguous float64 numpy array of {self.nprob} times")
+        if np.size(dt) != self.nprob:
+            raise ValueError(f"dt must hold {self.nprob} step sizes, one per problem")
+
     def pack(self, lines) -> np.ndarray:
         u = np.zeros(self.size)
         for k, v in enumerate(lines):
@@ -76,7 +85,7 @@ class batch:  # noqa: N801
     def integrate(self, u, t: np.ndarray, tout: float, dt: np.ndarray, itask: int = 1) -> None:
         """integrate(u_i, t[i], tout, dt[i], itask) for every problem; u and t in place."""
         mem, p, _ = describe(u, self.size, True)
-        assert t.dtype == np.float64 and t.size == self.nprob and t.flags.c_contiguous
+        self._check_times(t, dt)
         dt = np.ascontiguousarray(dt, dtype=np.float64)
         dp = C.POINTER(C.c_double)
         A.check(A.lib().hrw_batch_integrate(self._h, mem, p, t.ctypes.data_as(dp), float(tout),
@@ -85,7 +94,7 @@ class batch:  # noqa: N801
     def advance(self, u, t: np.ndarray, dt: np.ndarray, nsteps: int) -> None:
         """Exactly nsteps steps of every problem (nsteps integrate calls with itask=2)."""
         mem, p, _ = describe(u, self.size, True)
-        assert t.dtype == np.float64 and t.size == self.nprob and t.flags.c_contiguous
+        self._check_times(t, dt)
         dt = np.ascontiguousarray(dt, dtype=np.float64)
         dp = C.POINTER(C.c_double)
         A.check(A.lib().hrw_batch_advance(self._h, mem, p, t.ctypes.data_as(dp),
@@ -94,6 +103,7 @@ class batch:  # noqa: N801
     def tune(self, u, dt: np.ndarray, probe_steps: int = 5, cache_path: str | None = None):
         """Autotune the (group, cells-per-thread) shape of each size class; returns shapes."""
         mem, p, _ = describe(u, self.size, False)
+        self._check_times(None, dt)
         dt = np.ascontiguousarray(dt, dtype=np.float64)
         A.check(A.lib().hrw_batch_tune(self._h, mem, p, dt.ctypes.data_as(C.POINTER(C.c_double)),
                                        int(probe_steps),

@@ -60,3 +60,21 @@ def test_integrate_rejects_float32_before_the_library(hw):
     a._h, a.size, a.nseg = None, 8, 1
     with pytest.raises(TypeError, match="float64"):
         a.forward(np.zeros(8, dtype=np.float32), None, 0.1, 1)
+
+
+def test_batch_times_are_checked(hw):
+    """t is updated in place and dt read per problem: both must hold one value per problem."""
+    b = object.__new__(hw.batch)
+    b._h, b.offsets, b.nprob = None, np.array([0, 64, 128]), 2
+    u = np.zeros(128)
+    for t, dt in (([0.0, 0.0], np.ones(2)),            # t not an array
+                  (np.zeros(3), np.ones(2)),           # t too long
+                  (np.zeros(2, dtype=np.float32), np.ones(2)),
+                  (np.zeros(4)[::2], np.ones(2)),      # t not contiguous
+                  (np.zeros(2), np.ones(1))):          # dt too short
+        with pytest.raises(ValueError):
+            b.advance(u, t, dt, 1)
+        with pytest.raises(ValueError):
+            b.integrate(u, t, 1.0, dt)
+    with pytest.raises(ValueError, match="dt must hold 2"):
+        b.tune(u, np.ones(3))
