@@ -74,12 +74,17 @@ class Problem:
             p.xmax[d] = float(self.xmax[d])
             w = self.width[d]
             if w is not None:
-                w = np.ascontiguousarray(w, dtype=np.float64)
+                w = np.ascontiguousarray(w, dtype=np.float64).reshape(-1)
+                if w.size != p.ncells[d]:  # the library reads ncells widths
+                    raise A.HrwError(A.HRW_EINVAL, "Invalid input 'width': size(width) /= ncells.")
                 self._keep.append(w)
                 p.width[d] = w.ctypes.data_as(C.POINTER(C.c_double))
             xe = self.xedges[d] if self.xedges is not None else None
             if xe is not None:
-                xe = np.ascontiguousarray(xe, dtype=np.float64)
+                xe = np.ascontiguousarray(xe, dtype=np.float64).reshape(-1)
+                if xe.size != p.ncells[d] + 1:  # the library reads ncells + 1 edges
+                    raise A.HrwError(A.HRW_EINVAL,
+                                     "Invalid input 'xedges': size(xedges) /= ncells + 1.")
                 self._keep.append(xe)
                 p.xedges[d] = xe.ctypes.data_as(C.POINTER(C.c_double))
         if self.rates is not None:

@@ -78,3 +78,14 @@ def test_batch_times_are_checked(hw):
             b.integrate(u, t, 1.0, dt)
     with pytest.raises(ValueError, match="dt must hold 2"):
         b.tune(u, np.ones(3))
+
+
+def test_problem_grid_arrays_are_checked(hw):
+    """The library reads ncells widths and ncells + 1 edges from the descriptor's host arrays."""
+    from hrweno import HrwError
+    hw.burgers_1d(10, width=np.full(10, 0.1)).to_c()
+    with pytest.raises(HrwError, match="size\\(width\\) /= ncells"):
+        hw.burgers_1d(10, width=np.full(9, 0.1)).to_c()
+    hw.Problem(ncells=(10, 1), xedges=(np.linspace(0, 1, 11), None)).to_c()
+    with pytest.raises(HrwError, match="size\\(xedges\\) /= ncells \\+ 1"):
+        hw.Problem(ncells=(10, 1), xedges=(np.linspace(0, 1, 10), None)).to_c()
