@@ -43,7 +43,10 @@ def weno_solve(u0: torch.Tensor, problem: Problem, dt: float, nsteps: int,
         raise TypeError("weno_solve needs a CUDA float64 tensor")
     nseg = 1 if u0.dim() == 1 else int(u0.shape[0])
     key = (id(problem), nseg, checkpoint_every, u0.device.index)
-    if key not in _cache:
-        _cache[key] = (problem, adjoint(problem, nseg=nseg, checkpoint_every=checkpoint_every))
-    adj = _cache[key][1]
+    # the descriptor's bytes: a problem edited since its handle was made gets a new handle
+    # (the problems the adjoint takes hold no host arrays, so the bytes are its whole content)
+    snap = bytes(problem.to_c())
+    if key not in _cache or _cache[key][1] != snap:
+        _cache[key] = (problem, snap, adjoint(problem, nseg=nseg, checkpoint_every=checkpoint_every))
+    adj = _cache[key][2]
     return _WenoSolve.apply(u0, adj, float(dt), int(nsteps))

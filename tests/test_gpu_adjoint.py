@@ -146,3 +146,18 @@ def test_torch_autograd_op(hw):
     (hw.weno_solve(u0b, prob, dt, steps) * w).sum().backward()
     g1 = hw.adjoint(prob).vjp(u0b.detach()[1].contiguous(), w.contiguous(), dt, steps)
     assert torch.equal(u0b.grad[1], g1)
+
+
+def test_torch_op_follows_an_edited_problem(hw):
+    """weno_solve keeps one adjoint handle per problem; editing the problem between calls gives
+    the edited problem's solve, not the cached handle's."""
+    import torch
+    n, steps = 256, 20
+    prob = problem(hw, n, 3, "burgers", "copy")
+    dt = 0.4 * (10.0 / n) / 2.0
+    u0 = torch.from_numpy(line(n, 9)).cuda()
+    a = hw.weno_solve(u0, prob, dt, steps)
+    prob.alpha = (2.0, 2.0)
+    b = hw.weno_solve(u0, prob, dt, steps)
+    _, ref = hw.adjoint(prob).forward(u0, None, dt, steps, uT=torch.empty_like(u0))
+    assert torch.equal(b, ref) and not torch.equal(a, b)
