@@ -94,6 +94,7 @@ class SnapshotWriter:
         for k in range(depth):
             self._free.put(k)
         self._work: queue.Queue = queue.Queue()
+        self._error: BaseException | None = None  # the worker's failure, raised in the caller
         self._copy = torch.cuda.Stream()
         self._thread = threading.Thread(target=self._run, daemon=True)
         self._thread.start()
@@ -102,7 +103,9 @@ class SnapshotWriter:
         """Queue the state u (CUDA float64 tensor) at time t; the copy is ordered after the work
         already queued on `stream` (default: the current stream)."""
         import torch
+        self._raise()
         k = self._free.get()  # waits only when `depth` snapshots are still being written
+        self._raise()
         prod = stream or torch.cuda.current_stream()
         with torch.cuda.stream(prod):
             self._dev[k].copy_(u)  # ordered before any later work on the producing stream
@@ -121,11 +124,20 @@ class SnapshotWriter:
             if item is None:
                 return
             t, k, done = item
-            done.synchronize()
-            self._fh.write(u_record(t, self._slots[k].numpy()) + "\n")
-            self._free.put(k)
+            try:
+                done.synchronize()
+                if self._error is None:
+                    self._fh.write(u_record(t, self._slots[k].numpy()) + "\n")
+            except BaseException as e:  # noqa: BLE001 - handed to the caller
+                self._error = e
+            self._free.put(k)  # a waiting snapshot() wakes up and raises
+
+    def _raise(self) -> None:
+        if self._error is not None:
+            raise RuntimeError("snapshot writer failed") from self._error
 
     def close(self) -> None:
         self._work.put(None)
         self._thread.join()
         self._fh.close()
+        self._raise()

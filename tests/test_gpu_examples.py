@@ -42,3 +42,20 @@ def test_example2_runs(hw, tmp_path):
     assert np.all(np.isfinite(u)) and u.max() < 1.1 and u.min() > -0.1
     dx = 10.0 / 250
     assert abs(u.sum() * dx * dx - 4.0) < 1e-9
+
+
+def test_snapshot_writer_reports_a_failed_write(tmp_path):
+    """A record the worker thread cannot write (here: its file was closed under it) is raised
+    in the caller's next snapshot() or close(), instead of leaving snapshot() waiting forever
+    for a slot."""
+    import torch
+    from hrweno.output import SnapshotWriter
+    x = np.linspace(0.0, 1.0, 16)
+    out = SnapshotWriter(tmp_path, [(x, np.full(16, 1.0 / 16))], depth=2)
+    out._fh.close()
+    u = torch.zeros(16, dtype=torch.float64, device="cuda")
+    with pytest.raises(RuntimeError, match="snapshot writer failed"):
+        for k in range(8):
+            out.snapshot(0.1 * k, u)
+    out._work.put(None)  # stop the worker; close() would raise the same error again
+    out._thread.join()
