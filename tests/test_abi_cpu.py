@@ -111,3 +111,29 @@ def test_f32c_rejects_burgers_linear(hw):
                       coef_a=(0.5, 0.0), xmin=(-1.0, 0.0), xmax=(1.0, 1.0))
     with pytest.raises(HrwError, match=r"HRW_F32C supports BURGERS and LINEAR"):
         hw.rktvd(prob, 100, 3, dtype="f32c")
+
+
+def test_last_error_is_per_thread(hw):
+    """hrw_last_error() holds the message of the last failing call on the calling thread: an
+    error on one thread neither shows on nor overwrites another's (validation fails before
+    any CUDA call, so this runs without a GPU)."""
+    import threading
+    from hrweno import _abi as A
+    L = A.lib()
+    h = C.c_void_p()
+    assert L.hrw_weno_create(0, 3, 1e-6, None, C.byref(h)) == A.HRW_EINVAL
+    mine = L.hrw_last_error().decode()
+    seen = {}
+
+    def other():
+        seen["before"] = L.hrw_last_error().decode()
+        hh = C.c_void_p()
+        seen["rc"] = L.hrw_weno_create(10, 4, 1e-6, None, C.byref(hh))
+        seen["after"] = L.hrw_last_error().decode()
+
+    t = threading.Thread(target=other)
+    t.start()
+    t.join()
+    assert seen == {"before": "", "rc": A.HRW_EINVAL,
+                    "after": "Invalid input 'k'. Valid range: 1 <= k <= 3."}
+    assert L.hrw_last_error().decode() == mine == "Invalid input 'ncells'. Valid range: ncells > 0."
