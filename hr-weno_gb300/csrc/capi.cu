@@ -975,6 +975,7 @@ static int integrate_on(hrw_ode* o, int mem, void* u, double* t, double tout, do
 
 extern "C" int hrw_rhs(const hrw_problem* p, int dtype, double t, const void* v, void* vdot, void* stream) {
   (void)t;
+  if (!v || !vdot) return fail(HRW_EINVAL, "Invalid input: null pointer.");
   if (dtype != HRW_F64 && dtype != HRW_F32C)
     return fail(HRW_EINVAL, "Invalid input 'dtype': hrw_rhs supports HRW_F64 and HRW_F32C.");
   int neq = p && p->kind == HRW_PROBLEM_FV2D ? p->ncells[0] * p->ncells[1] : (p ? p->ncells[0] : 0);

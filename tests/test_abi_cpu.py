@@ -137,3 +137,11 @@ def test_last_error_is_per_thread(hw):
     assert seen == {"before": "", "rc": A.HRW_EINVAL,
                     "after": "Invalid input 'k'. Valid range: 1 <= k <= 3."}
     assert L.hrw_last_error().decode() == mine == "Invalid input 'ncells'. Valid range: ncells > 0."
+
+
+def test_rhs_rejects_null_arrays(hw):
+    """hrw_rhs takes device arrays; a null one returns HRW_EINVAL before any CUDA call."""
+    from hrweno import _abi as A
+    cp = hw.burgers_1d(16).to_c()
+    rc = A.lib().hrw_rhs(C.byref(cp), A.HRW_F64, 0.0, None, None, None)
+    assert rc == A.HRW_EINVAL and A.lib().hrw_last_error().decode() == "Invalid input: null pointer."
