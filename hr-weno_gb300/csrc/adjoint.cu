@@ -683,6 +683,8 @@ int hrw_adjoint_create(const hrw_problem* p, int nseg, int checkpoint_every, hrw
     return adj_fail(HRW_EINVAL, "hrw_adjoint: the global Lax-Friedrichs flux with fixed alpha only.");
   if (p->width[0] || p->xedges[0]) return adj_fail(HRW_EINVAL, "hrw_adjoint: uniform grids only.");
   if (p->ncells[0] <= 0) return adj_fail(HRW_EINVAL, "Invalid input 'ncells'. Valid range: ncells > 0.");
+  if (!(p->xmax[0] > p->xmin[0]))
+    return adj_fail(HRW_EINVAL, "Invalid input 'xmin', 'xmax'. Valid range: xmax > xmin.");
   if (p->k < 1 || p->k > 3) return adj_fail(HRW_EINVAL, "Invalid input 'k'. Valid range: 1 <= k <= 3.");
   if (!(p->eps > 2.220446049250313e-16))
     return adj_fail(HRW_EINVAL, "Invalid input 'eps'. Valid range: eps > epsilon.");

@@ -145,3 +145,19 @@ def test_rhs_rejects_null_arrays(hw):
     cp = hw.burgers_1d(16).to_c()
     rc = A.lib().hrw_rhs(C.byref(cp), A.HRW_F64, 0.0, None, None, None)
     assert rc == A.HRW_EINVAL and A.lib().hrw_last_error().decode() == "Invalid input: null pointer."
+
+
+def test_adjoint_and_batch_validation_messages(hw):
+    """The adjoint and batch constructors validate before any CUDA call."""
+    from hrweno import HrwError
+    p = hw.burgers_1d(16, xmin=1.0, xmax=1.0)
+    with pytest.raises(HrwError, match=r"Valid range: xmax > xmin"):
+        hw.adjoint(p)
+    with pytest.raises(HrwError, match=r"Valid range: xmax > xmin. \(problem 1\)"):
+        hw.batch([hw.burgers_1d(16), p])
+    with pytest.raises(HrwError, match=r"global Lax-Friedrichs"):
+        hw.adjoint(hw.burgers_1d(16, flux="godunov"))
+    with pytest.raises(HrwError, match=r"with nseg > 1, ncells must be a multiple of 8"):
+        hw.adjoint(hw.burgers_1d(12), nseg=2)
+    with pytest.raises(HrwError, match=r"batches hold uniform grids"):
+        hw.batch([hw.burgers_1d(10, width=np.full(10, 0.1))])
