@@ -161,3 +161,28 @@ def test_adjoint_and_batch_validation_messages(hw):
         hw.adjoint(hw.burgers_1d(12), nseg=2)
     with pytest.raises(HrwError, match=r"batches hold uniform grids"):
         hw.batch([hw.burgers_1d(10, width=np.full(10, 0.1))])
+
+
+def test_headers_compile_strictly_and_example_links(hw, tmp_path):
+    """The public headers are plain C99/C11 and C++17 under -pedantic -Wall -Wextra -Werror, and
+    the C caller (tests/c/abi_example.c) links against the library.  A C++ program calls
+    hrw_problem_init, which touches no CUDA state, so this runs without a GPU."""
+    import shutil
+    import subprocess
+    from hrweno import _abi
+    cc, cxx = shutil.which("gcc") or shutil.which("cc"), shutil.which("g++") or shutil.which("c++")
+    if cc is None or cxx is None:
+        pytest.skip("no C/C++ compiler")
+    lib = Path(_abi.LIB_PATH)
+    link = ["-L", str(lib.parent), "-l" + lib.stem[3:], "-Wl,-rpath," + str(lib.parent)]
+    strict = ["-pedantic", "-Wall", "-Wextra", "-Werror", "-I", str(ROOT / "include")]
+    for std in ("c99", "c11"):
+        subprocess.run([cc, "-std=" + std, *strict, str(ROOT / "tests" / "c" / "abi_example.c"),
+                        "-o", str(tmp_path / ("abi_" + std)), *link, "-lm"], check=True)
+    src = tmp_path / "headers.cpp"
+    src.write_text('#include "hrweno_gpu.h"\n#include "hrweno_diag.h"\n'
+                   "int main() {\n  hrw_problem p;\n  hrw_problem_init(&p);\n"
+                   "  return p.kind == HRW_PROBLEM_FV1D && p.k == 3 && p.xedges[0] == nullptr ? 0 : 1;\n}\n")
+    exe = tmp_path / "headers"
+    subprocess.run([cxx, "-std=c++17", *strict, str(src), "-o", str(exe), *link], check=True)
+    assert subprocess.run([str(exe)]).returncode == 0
