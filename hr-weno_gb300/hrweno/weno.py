@@ -29,7 +29,10 @@ class weno:  # noqa: N801 - the reference's type name
                                   xe.ctypes.data_as(C.POINTER(C.c_double)) if xe is not None else None,
                                   C.byref(h)))
         self._h = h
-        self.ncells, self.k, self.eps = int(ncells), int(k), float(eps)
+        # k <= 0 and eps <= 0 select the defaults, as in hrw_weno_create
+        self.ncells = int(ncells)
+        self.k = int(k) if int(k) > 0 else 3
+        self.eps = float(eps) if float(eps) > 0.0 else 1e-6
         self.uniform_grid = xedges is None
         if numerics != "fast":
             A.check(L.hrw_weno_set_numerics(h, A.HRW_NUMERICS_STRICT))

@@ -15,17 +15,20 @@ C = {
 }
 
 
-def reconstruct_np(v, k, eps):
-    """weno%reconstruct (src/hrweno_weno.f90:163-215): (vl, vr) of every cell."""
+def reconstruct_np(v, k, eps, cn=None):
+    """weno%reconstruct (src/hrweno_weno.f90:163-215): (vl, vr) of every cell.  cn: per-cell
+    coefficients [nc, k+1, k] of a non-uniform grid (cell i's c(j, r) at cn[i-1, r+1, j]),
+    used as the reference uses cnu(:, :, i) (:170,177-181); None: the uniform tables."""
     nc = v.size
     ext = np.concatenate([np.full(k - 1, v[0]), v, np.full(k - 1, v[-1])])  # vext, ghosts replicate
     at = lambda o: ext[k - 1 + o: k - 1 + o + nc]  # noqa: E731  vext(i + o) for every cell i
+    coef = (lambda j, col: C[k][j, col]) if cn is None else (lambda j, col: cn[:, col, j])  # noqa: E731
     vrr = np.zeros((k, nc))
     vlr = np.zeros((k, nc))
     for r in range(k):
         for j in range(k):
-            vrr[r] += C[k][j, r + 1] * at(j - r)
-            vlr[r] += C[k][j, r] * at(j - r)
+            vrr[r] += coef(j, r + 1) * at(j - r)
+            vlr[r] += coef(j, r) * at(j - r)
     if k == 1:
         beta = np.zeros((1, nc))
     elif k == 2:
@@ -186,3 +189,88 @@ def test_rktvd3_and_mstvd_match_numpy(hw, orc):
     uo = u0.copy()
     o.integrate(uo, 0.0, 13.5 * dt, dt)
     assert np.max(np.abs(uo - u)) <= 1e-12 * np.max(np.abs(u))
+
+
+# ---- non-uniform grids ------------------------------------------------------------------------
+def cnu_moments(xe, k):
+    """c(j, r) of every cell of the grid with edges xe(0:nc), found without Shu's eq. 2.20: the
+    polynomial p of degree k-1 whose averages over cells i-r .. i-r+k-1 are the given values is
+    solved for from the averages of the monomials ((x - x_{i+1/2}) / h)^q, and c(j, r) is the
+    weight of cell i-r+j in p(x_{i+1/2}).  Edges beyond the line continue the end cells' widths
+    (src/hrweno_weno.f90:245-255).  Returns [nc, k+1, k] (cell i's c(j, r) at [i-1, r+1, j])."""
+    nc, ng = xe.size - 1, k + 1
+    ext = np.concatenate([xe[0] - (xe[1] - xe[0]) * np.arange(ng, 0, -1), xe,
+                          xe[-1] + (xe[-1] - xe[-2]) * np.arange(1, ng + 1)])
+    edge = lambda e: ext[e + ng]  # noqa: E731  x_{e+1/2}; cell m spans [edge(m-1), edge(m)]
+    out = np.empty((nc, k + 1, k))
+    q = np.arange(k)
+    for i in range(1, nc + 1):
+        x0 = edge(i)
+        for r in range(-1, k):
+            cells = i - r + np.arange(k)
+            h = edge(cells[-1]) - edge(cells[0] - 1)
+            sl = (np.array([edge(m - 1) for m in cells]) - x0) / h
+            sr = (np.array([edge(m) for m in cells]) - x0) / h
+            # M[a, q]: average of s^q over cell a of the stencil
+            M = (sr[:, None] ** (q + 1) - sl[:, None] ** (q + 1)) / ((q + 1) * (sr - sl)[:, None])
+            out[i - 1, r + 1] = np.linalg.solve(M.T, np.eye(k)[0])  # p(x0) = a_0 = e0 . M^-1 v
+    return out
+
+
+def grids(nc, seed):
+    rng = np.random.default_rng(seed)
+    yield "cubic", -1.0 + 2.0 * (np.arange(nc + 1) / nc) ** 3  # test/test_hrweno.f90:123-128
+    yield "random", np.concatenate([[0.0], np.cumsum(rng.uniform(0.5, 1.5, nc))])
+    yield "geometric", np.concatenate([[0.0], np.cumsum(1.1 ** np.arange(nc))])
+
+
+@pytest.mark.parametrize("k", [1, 2, 3])
+@pytest.mark.parametrize("nc", [1, 2, 5, 40])
+def test_cnu_matches_moment_solve(orc, k, nc):
+    """weno_calc_cnu (src/hrweno_weno.f90:221-297) against coefficients found by a linear solve
+    instead of Shu's closed form, ghost edges included."""
+    for name, xe in grids(nc, nc + k):
+        ref = orc.calc_cnu(nc, k, xe)
+        got = cnu_moments(xe, k)
+        assert np.max(np.abs(got - ref)) <= 1e-11 * max(1.0, np.max(np.abs(ref))), (name, k, nc)
+
+
+@pytest.mark.parametrize("k", [1, 2, 3])
+@pytest.mark.parametrize("nc", [1, 3, 40, 301])
+def test_nonuniform_reconstruct_matches_numpy(orc, k, nc):
+    for name, xe in grids(nc, 7 * nc + k):
+        cn = cnu_moments(xe, k)
+        for v in lines(nc, nc + k):
+            vl, vr = orc.reconstruct(v, k, 1e-6, xe)
+            nl, nr = reconstruct_np(v, k, 1e-6, cn)
+            scale = max(np.max(np.abs(v)), 1e-300)
+            assert np.max(np.abs(vl - nl)) <= 1e-11 * scale, (name, k, nc)
+            assert np.max(np.abs(vr - nr)) <= 1e-11 * scale, (name, k, nc)
+
+
+def test_nonuniform_left_states_use_cell_i_coefficients(orc):
+    """On a non-uniform grid the reference forms vl(i) with cell i's coefficients c(:, r-1, i)
+    (src/hrweno_weno.f90:170,181); the set that reproduces polynomials exactly at x_{i-1/2} is
+    cell i-1's.  The oracle keeps the reference's choice (the GPU path matches the oracle bit for
+    bit), so vl is exact for polynomials of degree k-1 only where the two sets coincide: on
+    grids with a constant ratio of neighbouring widths (uniform, geometric and logarithmic
+    grids: the stencils of cells i and i-1 are scaled copies of each other).  vr is exact on
+    every grid.  Cell averages of p(x) = 1 + 2x - 0.3x^2, k = 3, cells away from the ends."""
+    nc, k = 40, 3
+    P = lambda x: x + x ** 2 - 0.1 * x ** 3  # noqa: E731  a primitive of p
+    p = lambda x: 1 + 2 * x - 0.3 * x ** 2  # noqa: E731
+    inner = slice(4, nc - 4)
+    for name, xe in [("uniform", np.linspace(0.0, 4.0, nc + 1))] + list(grids(nc, 3)):
+        v = (P(xe[1:]) - P(xe[:-1])) / np.diff(xe)
+        vl, vr = orc.reconstruct(v, k, 1e-6, xe)
+        assert np.max(np.abs(vr[inner] - p(xe[1:][inner]))) <= 1e-10 * np.max(np.abs(v)), name
+        cn = cnu_moments(xe, k)
+        shifted = np.concatenate([cn[:1], cn[:-1]])  # cell i-1's coefficients for cell i
+        left = np.stack([sum(shifted[:, r, j] * np.concatenate([v[:1]] * 2 + [v] + [v[-1:]] * 2)[2 - r + j: 2 - r + j + nc]
+                             for j in range(k)) for r in range(k)])
+        assert np.max(np.abs(left[:, inner] - p(xe[:-1][inner]))) <= 1e-10 * np.max(np.abs(v)), name
+        err = np.max(np.abs(vl[inner] - p(xe[:-1][inner])))
+        if name in ("uniform", "geometric"):
+            assert err <= 1e-10 * np.max(np.abs(v)), (name, err)
+        else:
+            assert err > 1e-6, (name, err)
