@@ -41,7 +41,7 @@ class Problem:
     rates: object = None
     numerics: str = "fast"
     xedges: tuple = (None, None)
-    _keep: list = field(default_factory=list, repr=False)
+    _keep: list = field(default_factory=list, repr=False, compare=False)  # arrays to_c() points at
 
     @property
     def neq(self) -> int:

@@ -274,3 +274,46 @@ def test_nonuniform_left_states_use_cell_i_coefficients(orc):
             assert err <= 1e-10 * np.max(np.abs(v)), (name, err)
         else:
             assert err > 1e-6, (name, err)
+
+
+def rktvd_np(u, t, tout, dt, order, L, itask=1):
+    """rktvd_integrate (src/hrweno_tvdode.f90:122-178): the stage formulas as written, t = t + dt
+    per step and the stopping test is_done (:282); returns (u, t, fevals)."""
+    done = lambda tt: (tt - tout) * np.copysign(1.0, dt) > 0  # noqa: E731
+    if done(t):
+        return u, t, 0
+    fe = 0
+    while True:
+        if order == 1:
+            u = u + dt * L(u)
+        elif order == 2:
+            ui = u + dt * L(u)
+            u = (u + ui + dt * L(ui)) / 2
+        else:
+            u = rk3_step(u, dt, L)
+        t = t + dt
+        fe += order
+        if done(t) or itask == 2:
+            return u, t, fe
+
+
+@pytest.mark.parametrize("order", [1, 2, 3])
+@pytest.mark.parametrize("itask", [1, 2])
+@pytest.mark.parametrize("sign", [1.0, -1.0])
+def test_rktvd_orders_times_and_fevals_match_numpy(hw, orc, order, itask, sign):
+    """Every rktvd order, one step (itask 2) or a run to tout (itask 1), forward and backward in
+    time: the oracle's u, t and fevals against the numpy restatement of the time loop."""
+    nc = 120
+    prob = hw.burgers_1d(nc, -5.0, 5.0, k=3, eps=1e-6, flux="godunov", alpha=1.0, bc="zero_inflow",
+                         numerics="strict")
+    x = -5.0 + 10.0 / nc * (np.arange(nc) + 0.5)
+    u0 = 0.2 + np.exp(-x * x)
+    L = lambda u: rhs_burgers_np(u, -5.0, 5.0, 3, 1e-6, "godunov", 1.0, "zero_inflow")  # noqa: E731
+    dt, t0 = sign * 2e-3, 0.1
+    tout = t0 + sign * 0.0137  # not a multiple of dt: the last step passes tout
+    un, tn, fen = rktvd_np(u0.copy(), t0, tout, dt, order, L, itask)
+    o = orc.ODE(prob, nc, 0, order)
+    uo = u0.copy()
+    to = o.integrate(uo, t0, tout, dt, itask)
+    assert to == tn and o.info()[0] == fen
+    assert np.max(np.abs(uo - un)) <= 1e-12 * np.max(np.abs(un))
