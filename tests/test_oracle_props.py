@@ -132,3 +132,17 @@ def test_flux_burgers_linear_consistency_and_upwinding(orc):
     vm, vp = 0.4, 0.9
     assert orc.numflux(A.HRW_FLUX_GODUNOV, A.HRW_FN_BURGERS_LINEAR, vm, vp, x, 0.0, a=a, b=b) == f(vm)
     assert orc.numflux(A.HRW_FLUX_GODUNOV, A.HRW_FN_BURGERS_LINEAR, vp, vm, x, 0.0, a=a, b=b) == f(vp)
+
+
+def test_godunov_takes_the_endpoint_extremum(orc):
+    """godunov (src/hrweno_fluxes.f90:67-74) takes min(f(vm), f(vp)) when vm <= vp and the max
+    otherwise: the endpoints only, where Shu's eq. 2.70 takes the extremum over [vm, vp].  The
+    two agree unless f has a critical point between the states; for Burgers that is a
+    rarefaction across u = 0, where the reference gives min(vm^2, vp^2)/2 instead of f(0) = 0.
+    The oracle and the GPU fluxes keep the reference's rule."""
+    from hrweno import _abi as A
+    g = lambda vm, vp: orc.numflux(A.HRW_FLUX_GODUNOV, A.HRW_FN_BURGERS, vm, vp, 0.0, 0.0)  # noqa: E731
+    assert g(-1.0, 2.0) == 0.5          # rarefaction through the sonic point: eq. 2.70 gives 0
+    assert g(2.0, -1.0) == 2.0          # shock: the max over [vp, vm] is at an endpoint
+    assert g(0.5, 2.0) == 0.125         # f' > 0 on [vm, vp]: the upwind state
+    assert g(-2.0, -0.5) == 0.125       # f' < 0: the downwind end is upwind
