@@ -978,8 +978,13 @@ extern "C" int hrw_rhs(const hrw_problem* p, int dtype, double t, const void* v,
   if (!v || !vdot) return fail(HRW_EINVAL, "Invalid input: null pointer.");
   if (dtype != HRW_F64 && dtype != HRW_F32C)
     return fail(HRW_EINVAL, "Invalid input 'dtype': hrw_rhs supports HRW_F64 and HRW_F32C.");
-  int neq = p && p->kind == HRW_PROBLEM_FV2D ? p->ncells[0] * p->ncells[1] : (p ? p->ncells[0] : 0);
-  if (p && p->kind == HRW_PROBLEM_LINEAR_ODE) neq = p->ncells[0];
+  // cells in 64 bits: the arrays hold at most 2^31 - 1 elements (neq is an int in the ABI)
+  const int64_t cells = !p ? 0
+                        : p->kind == HRW_PROBLEM_FV2D ? (int64_t)p->ncells[0] * p->ncells[1]
+                                                      : (int64_t)p->ncells[0];
+  if (p && p->ncells[0] > 0 && p->ncells[1] > 0 && cells > INT32_MAX)
+    return fail(HRW_EINVAL, "Invalid input 'ncells': more than 2^31 - 1 cells.");
+  const int neq = (int)cells;
   hrw_ode* o = nullptr;
   int rc = ode_create(p, neq, 1, 0, dtype, &o);
   if (rc != HRW_OK) return rc;

@@ -186,3 +186,13 @@ def test_headers_compile_strictly_and_example_links(hw, tmp_path):
     exe = tmp_path / "headers"
     subprocess.run([cxx, "-std=c++17", *strict, str(src), "-o", str(exe), *link], check=True)
     assert subprocess.run([str(exe)]).returncode == 0
+
+
+def test_rhs_rejects_grids_beyond_the_int_range(hw):
+    """A 2D grid of more than 2^31 - 1 cells is refused with a message (its cell count is formed
+    in 64 bits, before any CUDA call), not wrapped around to a negative int."""
+    from hrweno import _abi as A
+    cp = hw.pbe_2d(50000, 50000).to_c()
+    rc = A.lib().hrw_rhs(C.byref(cp), A.HRW_F64, 0.0, C.c_void_p(16), C.c_void_p(16), None)
+    assert rc == A.HRW_EINVAL
+    assert A.lib().hrw_last_error().decode() == "Invalid input 'ncells': more than 2^31 - 1 cells."
