@@ -146,3 +146,54 @@ def test_godunov_takes_the_endpoint_extremum(orc):
     assert g(2.0, -1.0) == 2.0          # shock: the max over [vp, vm] is at an endpoint
     assert g(0.5, 2.0) == 0.125         # f' > 0 on [vm, vp]: the upwind state
     assert g(-2.0, -0.5) == 0.125       # f' < 0: the downwind end is upwind
+
+
+@pytest.mark.parametrize("k", [1, 2, 3])
+def test_reconstruct_symmetries(orc, k):
+    """Invariances of weno%reconstruct on a uniform grid that follow from its formulas
+    (src/hrweno_weno.f90:163-215), to rounding:
+      mirror     reversing the line swaps the roles of vl and vr (c and d are symmetric);
+      shift      v + s reconstructs to vl + s, vr + s (beta sees differences only);
+      scale      s v with eps s^2 reconstructs to s vl, s vr (beta scales with s^2)."""
+    rng = np.random.default_rng(k)
+    x = np.linspace(-1.0, 1.0, 257)
+    for v in (np.sin(3 * x) + (x > 0.2), rng.standard_normal(257), np.exp(-30 * x * x)):
+        vl, vr = orc.reconstruct(v, k, 1e-6)
+        ml, mr = orc.reconstruct(v[::-1].copy(), k, 1e-6)
+        scale = np.max(np.abs(v))
+        assert np.max(np.abs(ml[::-1] - vr)) <= 1e-14 * scale
+        assert np.max(np.abs(mr[::-1] - vl)) <= 1e-14 * scale
+        sl, sr = orc.reconstruct(v + 3.0, k, 1e-6)
+        assert np.max(np.abs(sl - (vl + 3.0))) <= 1e-13 * (scale + 3.0)
+        assert np.max(np.abs(sr - (vr + 3.0))) <= 1e-13 * (scale + 3.0)
+        for s in (1e-3, 7.0):
+            ql, qr = orc.reconstruct(s * v, k, 1e-6 * s * s)
+            assert np.max(np.abs(ql - s * vl)) <= 1e-14 * s * scale
+            assert np.max(np.abs(qr - s * vr)) <= 1e-14 * s * scale
+
+
+def test_numerical_fluxes_are_monotone(orc):
+    """The fluxes are monotone (src/hrweno_fluxes.f90:22-76): h(vm, vp) does not decrease in vm
+    nor increase in vp.  Lax-Friedrichs (alpha = max|f'| over the states) and Godunov for linear
+    fluxes of either sign are monotone everywhere.  The reference's endpoint Godunov rule is
+    monotone for Burgers on states of one sign only: across the sonic point u = 0,
+    min(f(vm), f(vp)) grows as vm falls below -vp's magnitude (the true Godunov flux is 0 there)."""
+    from hrweno import _abi as A
+
+    def table(kind, fn, a, alpha, vs):
+        return np.array([[orc.numflux(kind, fn, vm, vp, 0.0, 0.0, alpha=alpha, a=a, b=0.0)
+                          for vp in vs] for vm in vs])
+
+    def monotone(h):
+        return bool(np.all(np.diff(h, axis=0) >= -1e-15) and np.all(np.diff(h, axis=1) <= 1e-15))
+
+    vs = np.linspace(-2.0, 2.0, 41)
+    for fn, a, alpha in [(A.HRW_FN_BURGERS, 1.0, 2.0), (A.HRW_FN_LINEAR, 0.7, 0.7),
+                         (A.HRW_FN_LINEAR, -1.3, 1.3)]:
+        assert monotone(table(A.HRW_FLUX_LAX_FRIEDRICHS, fn, a, alpha, vs)), (fn, a)
+    for a in (0.7, -1.3):
+        assert monotone(table(A.HRW_FLUX_GODUNOV, A.HRW_FN_LINEAR, a, 0.0, vs)), a
+    burgers = lambda vs: table(A.HRW_FLUX_GODUNOV, A.HRW_FN_BURGERS, 1.0, 0.0, vs)  # noqa: E731
+    assert monotone(burgers(np.linspace(0.0, 2.0, 21)))
+    assert monotone(burgers(np.linspace(-2.0, 0.0, 21)))
+    assert not monotone(burgers(vs))
