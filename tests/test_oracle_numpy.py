@@ -15,10 +15,11 @@ C = {
 }
 
 
-def reconstruct_np(v, k, eps, cn=None):
+def reconstruct_np(v, k, eps, cn=None, weights=None):
     """weno%reconstruct (src/hrweno_weno.f90:163-215): (vl, vr) of every cell.  cn: per-cell
     coefficients [nc, k+1, k] of a non-uniform grid (cell i's c(j, r) at cn[i-1, r+1, j]),
-    used as the reference uses cnu(:, :, i) (:170,177-181); None: the uniform tables."""
+    used as the reference uses cnu(:, :, i) (:170,177-181); None: the uniform tables.
+    weights: optional map applied to the normalised weights (w, w~) before the sums."""
     nc = v.size
     ext = np.concatenate([np.full(k - 1, v[0]), v, np.full(k - 1, v[-1])])  # vext, ghosts replicate
     at = lambda o: ext[k - 1 + o: k - 1 + o + nc]  # noqa: E731  vext(i + o) for every cell i
@@ -42,6 +43,9 @@ def reconstruct_np(v, k, eps, cn=None):
     s = (eps + beta) ** 2
     alfa = D[k][:, None] / s
     alfat = D[k][::-1, None] / s
+    if weights is not None:
+        w, wt = weights(alfa / alfa.sum(0), alfat / alfat.sum(0))
+        return (wt * vlr).sum(0), (w * vrr).sum(0)
     return (alfat * vlr).sum(0) / alfat.sum(0), (alfa * vrr).sum(0) / alfa.sum(0)
 
 
@@ -317,3 +321,49 @@ def test_rktvd_orders_times_and_fevals_match_numpy(hw, orc, order, itask, sign):
     to = o.integrate(uo, t0, tout, dt, itask)
     assert to == tn and o.info()[0] == fen
     assert np.max(np.abs(uo - un)) <= 1e-12 * np.max(np.abs(un))
+
+
+def test_weights_need_more_than_fp32_precision():
+    """How precisely must the nonlinear weights be computed to keep the 1e-12 agreement?  The
+    large 1D configuration's problem (seeded 8-Gaussian u0, WENO5, Lax-Friedrichs, copy
+    boundaries, RK3 at CFL 0.4) on 2^12 cells for 600 steps, with every weight perturbed by a
+    random relative error of at most rel and renormalised: at rel = 2^-44 (float-pair
+    arithmetic) the solution stays at the rounding floor, at rel = 2^-24 (FP32 weights) it
+    leaves 1e-12 as the shocks form.  Weights in plain FP32 are therefore no route to a faster
+    FP64 stage."""
+    nc, steps = 1 << 12, 600
+    x = -5.0 + 10.0 / nc * (np.arange(nc) + 0.5)
+    rng0 = np.random.default_rng(1)
+    u0 = np.zeros(nc)
+    for _ in range(8):
+        a, c, w = rng0.uniform(0.2, 1.0), rng0.uniform(-4.0, 4.0), rng0.uniform(0.05, 0.5)
+        u0 += a * np.exp(-((x - c) / w) ** 2)
+    alpha = float(np.max(np.abs(u0)))
+    dx = 10.0 / nc
+    dt = 0.4 * dx / alpha
+    f = lambda u: u * u / 2  # noqa: E731
+
+    def rhs(v, weights):
+        vl, vr = reconstruct_np(v, 3, 1e-6, weights=weights)
+        F = np.zeros(nc + 1)
+        F[1:nc] = (f(vr[:-1]) + f(vl[1:]) - alpha * (vl[1:] - vr[:-1])) / 2
+        F[0], F[nc] = F[1], F[nc - 1]
+        return -(F[1:] - F[:-1]) / dx
+
+    def run(rel):
+        rng = np.random.default_rng(0)
+
+        def perturb(w, wt):
+            w = w * (1.0 + rel * rng.uniform(-1.0, 1.0, w.shape))
+            wt = wt * (1.0 + rel * rng.uniform(-1.0, 1.0, wt.shape))
+            return w / w.sum(0), wt / wt.sum(0)
+
+        u = u0.copy()
+        for _ in range(steps):
+            u = rk3_step(u, dt, lambda v: rhs(v, perturb if rel else None))  # noqa: B023
+        return u
+
+    exact = run(0.0)
+    err = {rel: np.max(np.abs(run(rel) - exact)) / np.max(np.abs(exact)) for rel in (2.0 ** -44, 2.0 ** -24)}
+    assert err[2.0 ** -44] <= 1e-13, err
+    assert err[2.0 ** -24] > 1e-11, err
