@@ -367,3 +367,27 @@ def test_weights_need_more_than_fp32_precision():
     err = {rel: np.max(np.abs(run(rel) - exact)) / np.max(np.abs(exact)) for rel in (2.0 ** -44, 2.0 ** -24)}
     assert err[2.0 ** -44] <= 1e-13, err
     assert err[2.0 ** -24] > 1e-11, err
+
+
+def test_reconstruct_matches_numpy_on_generated_lines(orc):
+    """Generated cases: line lengths 1..300, every k, eps from 1e-12 to 1e-2, values spread over
+    twelve decades and of either sign, uniform and non-uniform grids."""
+    hyp = pytest.importorskip("hypothesis")
+    st = pytest.importorskip("hypothesis.strategies")
+
+    @hyp.settings(max_examples=150, deadline=None, derandomize=True)
+    @hyp.given(nc=st.integers(1, 300), k=st.integers(1, 3), log_eps=st.floats(-12.0, -2.0),
+               log_scale=st.floats(-6.0, 6.0), seed=st.integers(0, 2 ** 31 - 1),
+               nonuniform=st.booleans())
+    def check(nc, k, log_eps, log_scale, seed, nonuniform):
+        rng = np.random.default_rng(seed)
+        eps = 10.0 ** log_eps
+        v = 10.0 ** log_scale * rng.standard_normal(nc) * np.where(rng.random(nc) < 0.1, 100.0, 1.0)
+        xe = np.concatenate([[0.0], np.cumsum(rng.uniform(0.5, 1.5, nc))]) if nonuniform else None
+        vl, vr = orc.reconstruct(v, k, eps, xe)
+        nl, nr = reconstruct_np(v, k, eps, cnu_moments(xe, k) if nonuniform else None)
+        scale = np.max(np.abs(v))
+        tol = (1e-11 if nonuniform else 1e-13) * scale
+        assert np.max(np.abs(vl - nl)) <= tol and np.max(np.abs(vr - nr)) <= tol
+
+    check()
