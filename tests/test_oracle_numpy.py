@@ -391,3 +391,68 @@ def test_reconstruct_matches_numpy_on_generated_lines(orc):
         assert np.max(np.abs(vl - nl)) <= tol and np.max(np.abs(vr - nr)) <= tol
 
     check()
+
+
+def rhs1d_np(v, k, eps, flux, fn, a, b, alpha, bc, edges, width, cn=None):
+    """example1's right-hand side generalised as the problem descriptor describes it
+    (example/example1_burgers_1d_fv.f90:72-109): fluxes at the interior edges x_{i+1/2} with
+    f = u^2/2, (a + b x) u or their sum, the boundary rule, and -dF / width.  Returns (vdot, F)."""
+    nc = v.size
+    vl, vr = reconstruct_np(v, k, eps, cn)
+
+    def f(u, x):
+        if fn == "burgers":
+            return u * u / 2
+        if fn == "linear":
+            return (a + b * x) * u
+        return u * u / 2 + (a + b * x) * u
+
+    F = np.zeros(nc + 1)
+    xi = edges[1:nc]
+    F[1:nc] = numflux_np(flux, lambda u: f(u, xi), vr[:-1], vl[1:], alpha)
+    if bc == "copy":
+        F[0], F[nc] = F[1], F[nc - 1]
+    elif bc == "zero_inflow":
+        F[nc] = f(vr[-1], edges[nc])
+    return -(F[1:] - F[:-1]) / width, F
+
+
+def test_rhs_matches_numpy_on_generated_problems(hw, orc):
+    """Generated 1D problems: every flux function (with x-dependent velocity), numerical flux and
+    boundary rule, on uniform grids, uniform grids with given widths, and non-uniform edges."""
+    hyp = pytest.importorskip("hypothesis")
+    st = pytest.importorskip("hypothesis.strategies")
+
+    @hyp.settings(max_examples=200, deadline=None, derandomize=True)
+    @hyp.given(nc=st.integers(2, 200), k=st.integers(1, 3),
+               fn=st.sampled_from(["burgers", "linear", "burgers_linear"]),
+               flux=st.sampled_from(["lax_friedrichs", "godunov"]),
+               bc=st.sampled_from(["copy", "zero", "zero_inflow"]),
+               grid=st.sampled_from(["uniform", "width", "xedges"]), seed=st.integers(0, 2 ** 31 - 1))
+    def check(nc, k, fn, flux, bc, grid, seed):
+        rng = np.random.default_rng(seed)
+        a, b, alpha = rng.uniform(-1.0, 1.0), rng.uniform(-0.5, 0.5), 1.7
+        xmin, xmax = -2.0, 3.0
+        v = rng.standard_normal(nc) * np.where(rng.random(nc) < 0.2, 3.0, 0.3)
+        rx = (xmax - xmin) / nc
+        edges = xmin + rx * np.arange(nc + 1)
+        width = np.full(nc, rx)
+        kw = {}
+        cn = None
+        if grid == "width":
+            width = rng.uniform(0.5, 1.5, nc) * rx
+            kw["width"] = (width, None)
+        elif grid == "xedges":
+            edges = xmin + np.concatenate([[0.0], np.cumsum(rng.uniform(0.5, 1.5, nc))]) * rx
+            width = np.diff(edges)
+            kw["xedges"] = (edges, None)
+            cn = orc.calc_cnu(nc, k, edges)
+        prob = hw.Problem(kind="fv1d", ncells=(nc, 1), k=k, eps=1e-6, flux=flux, fn=(fn, fn),
+                          coef_a=(a, 0.0), coef_b=(b, 0.0), alpha=(alpha, alpha), bc=(bc, bc),
+                          xmin=(xmin, 0.0), xmax=(xmax, 1.0), numerics="strict", **kw)
+        ref = orc.rhs(prob, v)
+        got, F = rhs1d_np(v, k, 1e-6, flux, fn, a, b, alpha, bc, edges, width, cn)
+        scale = max(np.max(np.abs(F)) / np.min(width), 1e-300)
+        assert np.max(np.abs(got - ref)) <= 1e-13 * scale, (nc, k, fn, flux, bc, grid)
+
+    check()
