@@ -456,3 +456,44 @@ def test_rhs_matches_numpy_on_generated_problems(hw, orc):
         assert np.max(np.abs(got - ref)) <= 1e-13 * scale, (nc, k, fn, flux, bc, grid)
 
     check()
+
+
+def test_2d_rhs_matches_numpy_on_generated_problems(hw, orc):
+    """Generated 2D problems (example2's dimension-by-dimension right-hand side,
+    example/example2_pbe_2d_fv.f90:96-127): per direction its own flux function, velocity
+    a + b x_d at the interfaces and boundary rule; rectangular grids of 2..40 cells a side."""
+    hyp = pytest.importorskip("hypothesis")
+    st = pytest.importorskip("hypothesis.strategies")
+    fns = st.sampled_from(["burgers", "linear", "burgers_linear"])
+    bcs = st.sampled_from(["copy", "zero", "zero_inflow"])
+
+    @hyp.settings(max_examples=100, deadline=None, derandomize=True)
+    @hyp.given(n1=st.integers(2, 40), n2=st.integers(2, 40), k=st.integers(1, 3), fn1=fns, fn2=fns,
+               bc1=bcs, bc2=bcs, flux=st.sampled_from(["lax_friedrichs", "godunov"]),
+               seed=st.integers(0, 2 ** 31 - 1))
+    def check(n1, n2, k, fn1, fn2, bc1, bc2, flux, seed):
+        rng = np.random.default_rng(seed)
+        a, b = rng.uniform(-1.0, 1.0, 2), rng.uniform(-0.5, 0.5, 2)
+        alpha = (1.3, 0.9)
+        xmin, xmax = (0.0, -1.0), (2.0, 1.5)
+        v = rng.standard_normal(n1 * n2) * 0.5 + 1.0
+        prob = hw.Problem(kind="fv2d", ncells=(n1, n2), k=k, eps=1e-6, flux=flux, fn=(fn1, fn2),
+                          coef_a=tuple(a), coef_b=tuple(b), alpha=alpha, bc=(bc1, bc2),
+                          xmin=xmin, xmax=xmax, numerics="strict")
+        ref = orc.rhs(prob, v)
+        u = v.reshape(n2, n1)  # u((j-1) n1 + i): rows are x1 lines
+        got = np.zeros_like(u)
+        scale = 0.0
+        for d, (n, fn, bc, lines_) in enumerate([(n1, fn1, bc1, u), (n2, fn2, bc2, u.T)]):
+            rx = (xmax[d] - xmin[d]) / n
+            edges = xmin[d] + rx * np.arange(n + 1)
+            part = np.empty_like(lines_)
+            for r in range(lines_.shape[0]):
+                part[r], F = rhs1d_np(lines_[r].copy(), k, 1e-6, flux, fn, a[d], b[d], alpha[d], bc,
+                                      edges, np.full(n, rx))
+                scale = max(scale, np.max(np.abs(F)) / rx)
+            got += part if d == 0 else part.T
+        assert np.max(np.abs(got.reshape(-1) - ref)) <= 1e-13 * max(scale, 1e-300), \
+            (n1, n2, k, fn1, fn2, bc1, bc2, flux)
+
+    check()
