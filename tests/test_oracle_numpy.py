@@ -497,3 +497,66 @@ def test_2d_rhs_matches_numpy_on_generated_problems(hw, orc):
             (n1, n2, k, fn1, fn2, bc1, bc2, flux)
 
     check()
+
+
+def mstvd_np(state, u, t, tout, dt, L):
+    """mstvd_integrate (src/hrweno_tvdode.f90:203-271): on the first call four RK3 start steps
+    record u and L(u) (run even past tout), then equation 4.26 until is_done, shifting the
+    history.  state carries the history and fevals between calls; returns (u, t)."""
+    done = lambda tt: (tt - tout) * np.copysign(1.0, dt) > 0  # noqa: E731
+    if done(t):
+        return u, t
+    if not state:
+        state.update(hu=[], hl=[], fe=0)
+        for _ in range(4):
+            state["hu"].append(u.copy())
+            state["hl"].append(L(u))
+            u = rk3_step(u, dt, L)
+            t = t + dt
+        state["fe"] = 12
+    while not done(t):
+        ud = L(u)
+        ui = (25 * u + 50 * dt * ud + 7 * state["hu"][0] + 10 * dt * state["hl"][0]) / 32
+        t = t + dt
+        state["fe"] += 1
+        state["hu"] = state["hu"][1:] + [u.copy()]
+        state["hl"] = state["hl"][1:] + [ud]
+        u = ui
+    return u, t
+
+
+def test_time_loops_match_numpy_on_generated_calls(hw, orc):
+    """Generated call sequences of the integrators on the linear test ODE u_i' = a_i u_i
+    (test/test_tvdode.f90:107-111): start time, two output times, dt of either sign and size,
+    itask, rktvd orders 1-3 and mstvd across two integrate calls.  The oracle's u, t and fevals
+    against the numpy restatement of the reference's time loops."""
+    hyp = pytest.importorskip("hypothesis")
+    st = pytest.importorskip("hypothesis.strategies")
+
+    @hyp.settings(max_examples=150, deadline=None, derandomize=True)
+    @hyp.given(t0=st.floats(-2.0, 2.0), d1=st.floats(-0.4, 0.4), d2=st.floats(-0.4, 0.4),
+               h=st.floats(1e-3, 0.05), sign=st.sampled_from([1.0, -1.0]),
+               method=st.sampled_from(["rk1", "rk2", "rk3", "ms"]), itask=st.sampled_from([1, 2]))
+    def check(t0, d1, d2, h, sign, method, itask):
+        rates = np.linspace(-1.0, 3.0, 10)
+        prob = hw.linear_ode(rates, numerics="strict")
+        L = lambda u: rates * u  # noqa: E731
+        dt = sign * h
+        ms = method == "ms"
+        order = 3 if ms else int(method[-1])
+        o = orc.ODE(prob, rates.size, 1 if ms else 0, order)
+        uo, un = np.full(10, 0.1), np.full(10, 0.1)
+        to = tn = t0
+        fe, state = 0, {}
+        for tout in (t0 + d1, t0 + d1 + d2):
+            to = o.integrate(uo, to, tout, dt, 1 if ms else itask)
+            if ms:
+                un, tn = mstvd_np(state, un, tn, tout, dt, L)
+                fe = state.get("fe", 0)
+            else:
+                un, tn, f = rktvd_np(un, tn, tout, dt, order, L, itask)
+                fe += f
+            assert to == tn and o.info()[0] == fe, (method, to, tn, o.info(), fe)
+            assert np.max(np.abs(uo - un)) <= 1e-13 * np.max(np.abs(un))
+
+    check()
