@@ -229,3 +229,32 @@ def test_tangent_linear_oracle_matches_central_differences(orc, bc):
     h = 1e-5
     fd = (8 * (J(u0 + h * d) - J(u0 - h * d)) - (J(u0 + 2 * h * d) - J(u0 - 2 * h * d))) / (12 * h)
     assert abs(fd - dJ) <= 1e-9 * abs(dJ), (fd, dJ)
+
+
+def test_results_do_not_depend_on_the_thread_count(orc):
+    """The oracle splits the reference's `do concurrent` cell loop (src/hrweno_weno.f90:174) and
+    its elementwise stage combines over OpenMP threads; each element's arithmetic is unchanged,
+    so 1 and several threads give the same bits (reconstruction, rktvd, mstvd, the 2D
+    right-hand side)."""
+    import os
+    before = orc.set_threads(0)
+    many = max(2, min(8, os.cpu_count() or 2))
+    try:
+        runs = []
+        for threads in (1, many):
+            assert orc.set_threads(threads) == threads
+            rng = np.random.default_rng(5)
+            v = rng.standard_normal(3001)
+            out = list(orc.reconstruct(v, 3, 1e-6))
+            prob = burgers_1d(3001, -5.0, 5.0, k=3, eps=1e-6, flux="godunov", alpha=1.0,
+                              bc="zero_inflow", numerics="strict")
+            for method in (0, 1):
+                u = config1_u0(3001)
+                orc.ODE(prob, 3001, method, 3).integrate(u, 0.0, 0.035, 1e-3)
+                out.append(u)
+            out.append(orc.rhs(pbe_2d(96, 80, k=3, numerics="strict"), np.abs(rng.standard_normal(96 * 80))))
+            runs.append(out)
+        for a, b in zip(*runs):
+            assert np.array_equal(a, b)
+    finally:
+        orc.set_threads(before)
