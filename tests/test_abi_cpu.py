@@ -196,3 +196,13 @@ def test_rhs_rejects_grids_beyond_the_int_range(hw):
     rc = A.lib().hrw_rhs(C.byref(cp), A.HRW_F64, 0.0, C.c_void_p(16), C.c_void_p(16), None)
     assert rc == A.HRW_EINVAL
     assert A.lib().hrw_last_error().decode() == "Invalid input 'ncells': more than 2^31 - 1 cells."
+
+
+def test_constants_agree_with_the_header():
+    """Every enum constant of include/hrweno_gpu.h has the same value in the Python package."""
+    import hrweno
+    txt = re.sub(r"/\*.*?\*/", "", (ROOT / "include" / "hrweno_gpu.h").read_text(), flags=re.S)
+    consts = {n: int(v) for n, v in re.findall(r"\b(HRW_[A-Z0-9_]+)\s*=\s*(\d+)", txt)}
+    assert len(consts) >= 20
+    for name, value in consts.items():
+        assert getattr(hrweno, name) == value, name
