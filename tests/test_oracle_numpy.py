@@ -560,3 +560,50 @@ def test_time_loops_match_numpy_on_generated_calls(hw, orc):
             assert np.max(np.abs(uo - un)) <= 1e-13 * np.max(np.abs(un))
 
     check()
+
+
+def reconstruct_product_form_np(v, k, eps):
+    """The FAST kernels' algebra for k = 2, 3, restated in numpy with true divisions: candidates
+    scaled to integer stencils, the k = 3 indicators from per-centre terms D, eps + 13/12 D^2 and
+    H (E0(j) = D(j+1) + H(j+1), E1(j) = H(j), E2(j) = D(j-1) - H(j-1)), and the weights in product
+    form w_r = d_r P_r / sum d_q P_q with P_r the product of the other (eps + beta)^2."""
+    nc = v.size
+    ext = np.concatenate([np.full(k - 1, v[0]), v, np.full(k - 1, v[-1])])
+    at = lambda o: ext[k - 1 + o: k - 1 + o + nc]  # noqa: E731
+    if k == 2:
+        V0, V1 = at(0) + at(1), 3 * at(0) - at(-1)
+        W0, W1 = 3 * at(0) - at(1), at(-1) + at(0)
+        s0 = (eps + (at(1) - at(0)) ** 2) ** 2
+        s1 = (eps + (at(0) - at(-1)) ** 2) ** 2
+        den, dent = 2 * s1 + s0, s1 + 2 * s0
+        return (s1 * W0 + 2 * s0 * W1) / (2 * dent), (2 * s1 * V0 + s0 * V1) / (2 * den)
+    D = lambda o: at(o - 1) - 2 * at(o) + at(o + 1)  # noqa: E731
+    H = lambda o: 0.5 * (at(o - 1) - at(o + 1))  # noqa: E731
+    A = lambda o: eps + 13 / 12 * D(o) ** 2  # noqa: E731
+    e0 = (D(1) + H(1)) ** 2 + A(1)
+    e1 = H(0) ** 2 + A(0)
+    e2 = (D(-1) - H(-1)) ** 2 + A(-1)
+    s0, s1, s2 = e0 ** 2, e1 ** 2, e2 ** 2
+    P0, P1, P2 = s1 * s2, s0 * s2, s0 * s1
+    V0 = 2 * at(0) + 5 * at(1) - at(2)
+    V1 = -at(-1) + 5 * at(0) + 2 * at(1)
+    V2 = 2 * at(-2) - 7 * at(-1) + 11 * at(0)
+    W0 = 11 * at(0) - 7 * at(1) + 2 * at(2)
+    W1 = 2 * at(-1) + 5 * at(0) - at(1)
+    W2 = -at(-2) + 5 * at(-1) + 2 * at(0)
+    den, dent = 3 * P0 + 6 * P1 + P2, P0 + 6 * P1 + 3 * P2
+    return ((3 * P2 * W2 + 6 * P1 * W1 + P0 * W0) / (6 * dent),
+            (3 * P0 * V0 + 6 * P1 * V1 + P2 * V2) / (6 * den))
+
+
+@pytest.mark.parametrize("k", [2, 3])
+@pytest.mark.parametrize("nc", [1, 2, 5, 64, 1001])
+def test_product_form_algebra_matches_the_oracle(orc, k, nc):
+    """The FAST kernels compute the reference's reconstruction in a rearranged but equal form;
+    restated in exact-division numpy, that form agrees with the oracle to rounding level on
+    smooth, discontinuous and rough lines (the kernels' own rounding is checked on the GPU)."""
+    for v in lines(nc, 11 * nc + k):
+        vl, vr = orc.reconstruct(v, k, 1e-6)
+        fl, fr = reconstruct_product_form_np(v, k, 1e-6)
+        scale = max(np.max(np.abs(v)), 1e-300)
+        assert np.max(np.abs(fl - vl)) <= 1e-13 * scale and np.max(np.abs(fr - vr)) <= 1e-13 * scale
