@@ -607,3 +607,90 @@ def test_product_form_algebra_matches_the_oracle(orc, k, nc):
         fl, fr = reconstruct_product_form_np(v, k, 1e-6)
         scale = max(np.max(np.abs(v)), 1e-300)
         assert np.max(np.abs(fl - vl)) <= 1e-13 * scale and np.max(np.abs(fr - vr)) <= 1e-13 * scale
+
+
+def offsets_np(v, k, eps):
+    """(rl, rr) = (vl - v, vr - v) of every cell from the neighbour differences d_m = v_{m+1} - v_m,
+    as the compensated FP32 kernels form them (candidates and indicators as linear and quadratic
+    forms in the differences, product-form weights), here in float64 with true divisions."""
+    nc = v.size
+    if k == 1:
+        return np.zeros(nc), np.zeros(nc)
+    ext = np.concatenate([np.full(2, v[0]), v, np.full(2, v[-1])])
+    dd = np.diff(ext)  # dd[q] = d_{q-2}
+    at = lambda o: dd[2 + o: 2 + o + nc]  # noqa: E731  d_{j+o}, j = 0 .. nc-1
+    dmm, dm, d0, d1 = at(-2), at(-1), at(0), at(1)
+    if k == 2:
+        s0, s1 = (eps + d0 ** 2) ** 2, (eps + dm ** 2) ** 2
+        return (-0.5 * (s1 * d0 + 2 * s0 * dm) / (s1 + 2 * s0),
+                0.5 * (2 * s1 * d0 + s0 * dm) / (2 * s1 + s0))
+    e0 = eps + 13 / 12 * (d1 - d0) ** 2 + 0.25 * (d1 - 3 * d0) ** 2
+    e1 = eps + 13 / 12 * (d0 - dm) ** 2 + 0.25 * (dm + d0) ** 2
+    e2 = eps + 13 / 12 * (dm - dmm) ** 2 + 0.25 * (3 * dm - dmm) ** 2
+    s0, s1, s2 = e0 ** 2, e1 ** 2, e2 ** 2
+    P0, P1, P2 = s1 * s2, s0 * s2, s0 * s1
+    R0, R1, R2 = 4 * d0 - d1, 2 * d0 + dm, 5 * dm - 2 * dmm
+    L0, L1, L2 = 2 * d1 - 5 * d0, -(2 * dm + d0), dmm - 4 * dm
+    rr = (3 * P0 * R0 + 6 * P1 * R1 + P2 * R2) / (6 * (3 * P0 + 6 * P1 + P2))
+    rl = (P0 * L0 + 6 * P1 * L1 + 3 * P2 * L2) / (6 * (P0 + 6 * P1 + 3 * P2))
+    return rl, rr
+
+
+def rhs_difference_form_np(v, k, eps, flux, fn, a, b, alpha, bc, xmin, xmax):
+    """example1's right-hand side in the compensated kernels' difference form: per cell j,
+    F_{j+1/2} - F_{j-1/2} = G_R - G_L (+ (g_R - g_L) v_j for f = g(x) u), G = F - f_base(v_j)
+    evaluated from the offsets, so the O(1) part cancels exactly; boundary cells in full."""
+    nc = v.size
+    rx = (xmax - xmin) / nc
+    rl, rr = offsets_np(v, k, eps)
+    d = np.append(np.diff(v), 0.0)  # d_j = v_{j+1} - v_j (0 past the end: ghosts replicate)
+    lin = fn == "linear"
+    g = (a + b * (xmin + rx * np.arange(nc + 1))) if lin else np.zeros(nc + 1)
+
+    def G(vj, am, bp, gg):  # F(vj + am, vj + bp) - f_base(vj)
+        if flux == "lax_friedrichs":
+            if lin:
+                return 0.5 * ((gg + alpha) * am + (gg - alpha) * bp)
+            return 0.25 * (am * (2 * vj + am + 2 * alpha) + bp * (2 * vj + bp - 2 * alpha))
+        fa, fb = (gg * am, gg * bp) if lin else (0.5 * am * (2 * vj + am), 0.5 * bp * (2 * vj + bp))
+        return np.where(am <= bp, np.minimum(fa, fb), np.maximum(fa, fb))
+
+    rr_m = np.concatenate([[rr[0]], rr[:-1]])
+    d_m = np.concatenate([[0.0], d[:-1]])
+    rl_p = np.append(rl[1:], rl[-1])
+    GL = G(v, rr_m - d_m, rl, g[:-1])
+    GR = G(v, rr, d + rl_p, g[1:])
+    dF = GR - GL + ((g[1:] - g[:-1]) * v if lin else 0.0)
+    for j in {0, nc - 1}:  # boundary cells, fluxes in full
+        fb = (lambda e, vv: g[e] * vv) if lin else (lambda e, vv: 0.5 * vv * vv)  # noqa: E731
+        FL, FR = fb(j, v[j]) + GL[j], fb(j + 1, v[j]) + GR[j]
+        if bc == "copy":
+            dF[j] = 0.0
+            continue
+        if j == 0:
+            FL = 0.0
+        if j == nc - 1:
+            FR = 0.0 if bc == "zero" else fb(nc, v[j] + rr[j])
+        dF[j] = FR - FL
+    return -dF / rx
+
+
+@pytest.mark.parametrize("k", [1, 2, 3])
+@pytest.mark.parametrize("fn", ["burgers", "linear"])
+@pytest.mark.parametrize("flux", ["lax_friedrichs", "godunov"])
+@pytest.mark.parametrize("bc", ["copy", "zero", "zero_inflow"])
+def test_difference_form_matches_the_oracle(hw, orc, k, fn, flux, bc):
+    """The compensated FP32 kernels' difference form of the right-hand side (offsets from the
+    neighbour differences, G-form flux differences, boundary cells in full) is the reference's
+    right-hand side rearranged: restated in float64 it agrees with the oracle to rounding level
+    (the kernels' FP32 rounding is checked against FP64 on the GPU)."""
+    a, b, alpha = (0.6, 0.3, 1.6) if fn == "linear" else (0.0, 0.0, 1.3)
+    for nc in (2, 3, 9, 400):
+        for v in lines(nc, 5 * nc + k):
+            prob = hw.Problem(kind="fv1d", ncells=(nc, 1), k=k, eps=1e-6, flux=flux, fn=(fn, fn),
+                              coef_a=(a, 0.0), coef_b=(b, 0.0), alpha=(alpha, alpha), bc=(bc, bc),
+                              xmin=(-1.0, 0.0), xmax=(2.0, 1.0), numerics="strict")
+            ref = orc.rhs(prob, v)
+            got = rhs_difference_form_np(v, k, 1e-6, flux, fn, a, b, alpha, bc, -1.0, 2.0)
+            scale = (1.0 + np.max(np.abs(v))) ** 2 * nc / 3.0
+            assert np.max(np.abs(got - ref)) <= 1e-13 * scale, (nc, k, fn, flux, bc)
