@@ -24,8 +24,8 @@ def reconstruct_np(v, k, eps, cn=None, weights=None):
     ext = np.concatenate([np.full(k - 1, v[0]), v, np.full(k - 1, v[-1])])  # vext, ghosts replicate
     at = lambda o: ext[k - 1 + o: k - 1 + o + nc]  # noqa: E731  vext(i + o) for every cell i
     coef = (lambda j, col: C[k][j, col]) if cn is None else (lambda j, col: cn[:, col, j])  # noqa: E731
-    vrr = np.zeros((k, nc))
-    vlr = np.zeros((k, nc))
+    vrr = np.zeros((k, nc), dtype=np.result_type(v, float))  # complex lines: complex-step tests
+    vlr = np.zeros_like(vrr)
     for r in range(k):
         for j in range(k):
             vrr[r] += coef(j, r + 1) * at(j - r)
@@ -694,3 +694,110 @@ def test_difference_form_matches_the_oracle(hw, orc, k, fn, flux, bc):
             got = rhs_difference_form_np(v, k, 1e-6, flux, fn, a, b, alpha, bc, -1.0, 2.0)
             scale = (1.0 + np.max(np.abs(v))) ** 2 * nc / 3.0
             assert np.max(np.abs(got - ref)) <= 1e-13 * scale, (nc, k, fn, flux, bc)
+
+
+def _beta_forms(k):
+    """Smoothness indicators as sums of weighted squares of linear forms in v(i-2 .. i+2):
+    beta_r = sum (c, coefficients) over its terms (src/hrweno_weno.f90:189-202)."""
+    if k == 1:
+        return [[]]
+    if k == 2:
+        return [[(1.0, {1: 1.0, 0: -1.0})], [(1.0, {0: 1.0, -1: -1.0})]]
+    return [[(13 / 12, {0: 1.0, 1: -2.0, 2: 1.0}), (1 / 4, {0: 3.0, 1: -4.0, 2: 1.0})],
+            [(13 / 12, {-1: 1.0, 0: -2.0, 1: 1.0}), (1 / 4, {-1: 1.0, 1: -1.0})],
+            [(13 / 12, {-2: 1.0, -1: -2.0, 0: 1.0}), (1 / 4, {-2: 1.0, -1: -4.0, 0: 3.0})]]
+
+
+def weno_vjp_np(v, k, eps, ar, al):
+    """d(sum ar vr + al vl)/dv through the WENO map, by the identities the adjoint kernels use:
+    the candidates are linear, d vr/d beta_s = -2 w_s (q_s - vr)/(eps + beta_s) (and likewise for
+    vl with the mirrored weights), the indicators are quadratic forms; ghost cells replicate the
+    end values, so their sensitivities land on v(1) and v(nc)."""
+    nc = v.size
+    ext = np.concatenate([np.full(k - 1, v[0]), v, np.full(k - 1, v[-1])])
+    at = lambda o: ext[k - 1 + o: k - 1 + o + nc]  # noqa: E731
+    q = [sum(C[k][j, r + 1] * at(j - r) for j in range(k)) for r in range(k)]
+    p = [sum(C[k][j, r] * at(j - r) for j in range(k)) for r in range(k)]
+    forms = _beta_forms(k)
+    beta = [sum(c * sum(w * at(o) for o, w in lin.items()) ** 2 for c, lin in forms[r]) if forms[r]
+            else np.zeros(nc) for r in range(k)]
+    alfa = [D[k][r] / (eps + beta[r]) ** 2 for r in range(k)]
+    alft = [D[k][k - 1 - r] / (eps + beta[r]) ** 2 for r in range(k)]
+    w = [a / sum(alfa) for a in alfa]
+    wt = [a / sum(alft) for a in alft]
+    vr = sum(w[r] * q[r] for r in range(k))
+    vl = sum(wt[r] * p[r] for r in range(k))
+    gext = np.zeros(nc + 2 * (k - 1))
+
+    def push(o, coef):  # add coef (per cell) at offset o of every cell
+        gext[k - 1 + o: k - 1 + o + nc] += coef
+
+    for r in range(k):
+        for j in range(k):
+            push(j - r, ar * w[r] * C[k][j, r + 1] + al * wt[r] * C[k][j, r])
+        g_beta = (ar * -2 * w[r] * (q[r] - vr) + al * -2 * wt[r] * (p[r] - vl)) / (eps + beta[r])
+        for c, lin in forms[r]:
+            val = sum(wt_ * at(o) for o, wt_ in lin.items())
+            for o, wt_ in lin.items():
+                push(o, g_beta * 2 * c * val * wt_)
+    grad = gext[k - 1: k - 1 + nc].copy()
+    grad[0] += gext[:k - 1].sum()
+    grad[-1] += gext[k - 1 + nc:].sum()
+    return grad
+
+
+def lf_burgers_rhs_vjp_np(v, k, eps, alpha, bc, dx, mu):
+    """J(v)^T mu of example1's right-hand side with the fixed-alpha Lax-Friedrichs flux: flux
+    adjoints phi_e = (mu_e - mu_{e-1})/dx with the boundary rules transposed, then the states'
+    adjoints ar, al and the reverse WENO map."""
+    nc = v.size
+    vl, vr = reconstruct_np(v, k, eps)
+    m = np.concatenate([[0.0], mu, [0.0]])
+    phi = (m[1:] - m[:-1]) / dx  # phi[e], e = 0 .. nc: faces
+    if bc == "copy" and nc >= 2:
+        phi[1] += phi[0]
+        phi[nc - 1] += phi[nc]
+    ar, al = np.zeros(nc), np.zeros(nc)
+    ar[:-1] += phi[1:nc] * (vr[:-1] + alpha) / 2  # dF/dvm, f' = u
+    al[1:] += phi[1:nc] * (vl[1:] - alpha) / 2    # dF/dvp
+    if bc == "zero_inflow":
+        ar[-1] += phi[nc] * vr[-1]                # F_nc = f(vr(nc))
+    return weno_vjp_np(v, k, eps, ar, al)
+
+
+@pytest.mark.parametrize("k", [2, 3])
+@pytest.mark.parametrize("bc", ["copy", "zero", "zero_inflow"])
+def test_rk3_step_adjoint_identities(hw, k, bc):
+    """The transposed RK3 step of the adjoint kernels (A3: l2 = 2/3 (l' + dt J(u2)^T l'), A2:
+    l1 = 1/4 (l2 + dt J(u1)^T l2), A1: l = acc + l1 + dt J(u)^T l1 with acc = l'/3 + 3/4 l2) with
+    the flux and WENO transposes above: <l, d> equals <l', J_step d> computed by complex-step
+    differentiation of the numpy forward step, to rounding level."""
+    nc, eps, alpha = 40, 1e-6, 1.5
+    dx = 10.0 / nc
+    dt = 0.4 * dx / alpha
+    x = -5.0 + dx * (np.arange(nc) + 0.5)
+    u = 0.3 + np.exp(-x ** 2) + 0.05 * np.sin(3 * x)
+    rng = np.random.default_rng(k)
+    d, lam = rng.standard_normal(nc), rng.standard_normal(nc)
+
+    def L(v):
+        vl, vr = reconstruct_np(v, k, eps)
+        f = lambda z: z * z / 2  # noqa: E731
+        F = np.zeros(nc + 1, dtype=np.result_type(v, float))
+        F[1:nc] = (f(vr[:-1]) + f(vl[1:]) - alpha * (vl[1:] - vr[:-1])) / 2
+        if bc == "copy":
+            F[0], F[nc] = F[1], F[nc - 1]
+        elif bc == "zero_inflow":
+            F[nc] = f(vr[-1])
+        return -(F[1:] - F[:-1]) / dx
+
+    h = 1e-30
+    jd = np.imag(rk3_step(u + 1j * h * d, dt, L)) / h  # J_step d, exact to rounding
+    u1 = u + dt * L(u)
+    u2 = (3 * u + u1 + dt * L(u1)) / 4
+    JT = lambda v, mu: lf_burgers_rhs_vjp_np(v, k, eps, alpha, bc, dx, mu)  # noqa: E731
+    l2 = 2 / 3 * (lam + dt * JT(u2, lam))
+    acc = lam / 3 + 3 / 4 * l2
+    l1 = 1 / 4 * (l2 + dt * JT(u1, l2))
+    lu = acc + l1 + dt * JT(u, l1)
+    assert abs(lu @ d - lam @ jd) <= 1e-12 * abs(lam @ jd)
