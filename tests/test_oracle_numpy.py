@@ -1,7 +1,13 @@
 """A second, independent restatement of the reference's formulas -- vectorised numpy, written
 from src/hrweno_weno.f90, src/hrweno_fluxes.f90, src/hrweno_tvdode.f90 and the two example
-drivers -- against the C++ oracle on random inputs (CPU only).  The oracle is pinned to the reference's known-answer tests; this
-checks it everywhere else, to rounding level (numpy sums in its own order)."""
+drivers -- against the C++ oracle on random and generated inputs (CPU only).  The oracle is
+pinned to the reference's known-answer tests; this checks it everywhere else, to rounding level
+(numpy sums in its own order).
+
+The same restatement also carries the rearranged algebra the GPU kernels use (the FAST product
+form, the compensated FP32 difference form, the adjoint's transposes), so that each
+rearrangement is shown equal to the reference's formulas independently of the kernels' own
+rounding, which the GPU tests check."""
 import numpy as np
 import pytest
 
