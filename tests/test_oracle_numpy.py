@@ -807,3 +807,28 @@ def test_rk3_step_adjoint_identities(hw, k, bc):
     l1 = 1 / 4 * (l2 + dt * JT(u1, l2))
     lu = acc + l1 + dt * JT(u, l1)
     assert abs(lu @ d - lam @ jd) <= 1e-12 * abs(lam @ jd)
+
+
+def test_increment_form_stages_match_the_reference_formulas():
+    """The compensated kernels store stage values as increments relative to u and add the last
+    one to (hi, lo): E1 d1 = dt L(u); RK3B d2 = (d1 + dt L(u + d1))/4; RK3C u' = u + 2/3 (d2 +
+    dt L(u + d2)); RK2B u' = u + (d1 + dt L(u + d1))/2; multistep u' = u + (7 (u4 - u) +
+    50 dt L(u) + 10 dt L4)/32.  These equal the reference's formulas
+    (src/hrweno_tvdode.f90:139-167,257) to rounding level."""
+    nc, dt = 300, 4e-3
+    L = lambda u: rhs_burgers_np(u, -5.0, 5.0, 3, 1e-6, "lax_friedrichs", 1.0, "copy")  # noqa: E731
+    rng = np.random.default_rng(2)
+    x = -5.0 + 10.0 / nc * (np.arange(nc) + 0.5)
+    u = np.exp(-x * x) + 0.1 * rng.standard_normal(nc)
+    u4 = u + 0.01 * rng.standard_normal(nc)
+    L4 = L(u4)
+    tol = lambda ref: 1e-14 * np.max(np.abs(ref))  # noqa: E731
+    d1 = dt * L(u)
+    d2 = (d1 + dt * L(u + d1)) / 4
+    ref = rk3_step(u, dt, L)
+    assert np.max(np.abs(u + 2 / 3 * (d2 + dt * L(u + d2)) - ref)) <= tol(ref)
+    ui = u + dt * L(u)
+    ref2 = (u + ui + dt * L(ui)) / 2
+    assert np.max(np.abs(u + (d1 + dt * L(u + d1)) / 2 - ref2)) <= tol(ref2)
+    refm = (25 * u + 50 * dt * L(u) + 7 * u4 + 10 * dt * L4) / 32
+    assert np.max(np.abs(u + (7 * (u4 - u) + 50 * dt * L(u) + 10 * dt * L4) / 32 - refm)) <= tol(refm)
