@@ -1,6 +1,6 @@
 """bench.py's JSON contract through its CPU arm (--impl reference runs the oracle on the host
 cores, no GPU): one line with the required keys, the reference arm's own fields, and no output
-from ranks other than 0."""
+from ranks other than 0; and the parser behind the line's `clocks` key."""
 import json
 import os
 import subprocess
@@ -46,3 +46,22 @@ def test_reference_arm_other_ranks_are_silent():
 def test_warmup_below_three_is_refused():
     r = run(["--impl", "reference", "--steps", "1", "--warmup", "2", "--cells", "4096"])
     assert r.returncode != 0 and "warmup" in r.stderr
+
+
+def test_clock_summary_parses_the_sampler_output():
+    """The `clocks` key of the bench line: median SM clock under load, the maximum, and the
+    throttle reasons seen Active, from nvidia-smi's csv rows (no GPU needed: the rows are given)."""
+    sys.path.insert(0, str(ROOT))
+    import bench
+    s = bench.ClockSampler(0)
+    s.out = "\n".join([
+        "0, 1965, 2070, 812.35, 0x0000000000000000, Not Active, Not Active, Not Active, Not Active",
+        "0, 1980, 2070, 1011.20, 0x0000000000000004, Not Active, Not Active, Not Active, Active",
+        "0, 2070, 2070, 900.00, 0x0000000000000000, Not Active, Not Active, Not Active, Not Active",
+        "0, [N/A], 2070, 0, 0x0, Not Active, Not Active, Not Active, Not Active",  # unreadable
+        "garbage",
+    ])
+    assert s.summary() == {"sm_mhz": 1980.0, "sm_max_mhz": 2070.0, "samples": 3,
+                           "reasons": ["sw_power_cap"]}
+    s.out = ""
+    assert s.summary() is None
