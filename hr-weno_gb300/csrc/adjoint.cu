@@ -551,7 +551,8 @@ int misfit_blocks_per_seg(const AdjLine& A) { return (int)((A.seg + kMisfitChunk
 template <int K, int C, bool TAPE>
 cudaError_t fwd_stage_kt(const AdjLine& A, const StageArgs& a, int st, double* wt, cudaStream_t s) {
   const int64_t warps = (A.n + 32 * C - 1) / (32 * C);
-  const int blocks = (int)((warps + 7) / 8 < 152 * 32 ? (warps + 7) / 8 : 152 * 32);
+  const int64_t cap = (int64_t)device_sms() * 32;
+  const int blocks = (int)((warps + 7) / 8 < cap ? (warps + 7) / 8 : cap);
   if (st == ST_EULER) adj_fwd_kernel<K, ST_EULER, C, TAPE><<<blocks, 256, 0, s>>>(A, a, wt);
   else if (st == ST_RK3B) adj_fwd_kernel<K, ST_RK3B, C, TAPE><<<blocks, 256, 0, s>>>(A, a, wt);
   else adj_fwd_kernel<K, ST_RK3C, C, TAPE><<<blocks, 256, 0, s>>>(A, a, wt);

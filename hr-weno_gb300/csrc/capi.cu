@@ -156,6 +156,8 @@ struct hrw_ode {
   // stream beside `stream`, and their events
   cudaStream_t pipe[2] = {}, copy = nullptr;
   cudaEvent_t ev_start = nullptr, ev_in[16] = {}, ev_s3[16] = {}, ev_join[3] = {};
+  // 2D problems: the word a stage block sets when its bounded wait for its tile copies ran out
+  unsigned int* tflag = nullptr;
 };
 
 extern "C" {
@@ -388,6 +390,11 @@ static int ode_create(const hrw_problem* p, int neq, int order, int method, int 
     b.ld = p->ncells[0];
     b.upwind = nd == 2 && p->flux == HRW_FLUX_GODUNOV && positive_velocity(b.L) &&
                positive_velocity(b.L2);
+    if (nd == 2) {
+      if ((e = cudaMalloc(&o->tflag, sizeof(unsigned int))) != cudaSuccess) return cleanup(e);
+      if ((e = cudaMemset(o->tflag, 0, sizeof(unsigned int))) != cudaSuccess) return cleanup(e);
+      b.timeout_flag = o->tflag;
+    }
   }
   if ((e = cudaMalloc(&o->u, bytes)) != cudaSuccess) return cleanup(e);
   if (dtype == HRW_F32C) {
@@ -410,6 +417,7 @@ static int ode_create(const hrw_problem* p, int neq, int order, int method, int 
     F32CArgs& f = o->fbase;
     f.eps = (float)p->eps;
     f.ld = p->ncells[0];
+    f.timeout_flag = o->tflag;
     for (int d = 0; d < nd; ++d) {
       const LineArgs& L = d == 0 ? b.L : b.L2;
       LineF& F = d == 0 ? f.L : f.L2;
@@ -494,6 +502,7 @@ int hrw_ode_destroy(hrw_ode* o) {
   for (double* p : o->ring_l)
     if (p) cudaFree(p);
   if (o->fmem) cudaFree(o->fmem);
+  if (o->tflag) cudaFree(o->tflag);
   if (o->graph.exec) cudaGraphExecDestroy(o->graph.exec);
   for (cudaStream_t st : {o->pipe[0], o->pipe[1], o->copy})
     if (st) cudaStreamDestroy(st);
@@ -848,7 +857,7 @@ static_assert(kPipeChunks <= (int)(sizeof(hrw_ode::ev_in) / sizeof(cudaEvent_t))
 
 static bool host_pipeline_ok(const hrw_ode* o, const void* u) {
   if (o->dtype != HRW_F64 || o->prob.kind != HRW_PROBLEM_FV1D || o->method != 0 || o->order != 3 ||
-      o->line[0].xe || (int64_t)o->neq < 2 * 152 * kPipeTile)
+      o->line[0].xe || (int64_t)o->neq < 2 * (int64_t)device_sms() * kPipeTile)
     return false;
   cudaPointerAttributes at{};
   if (cudaPointerGetAttributes(&at, u) != cudaSuccess) {
@@ -924,6 +933,20 @@ static int rk3_integrate_host(hrw_ode* o, double* uh, double* t, double tout, do
   return HRW_OK;
 }
 
+// Whether a 2D stage block of this handle gave up waiting for its tile copies since the last
+// check; clears the handle's flag.  Waits for the handle's stream.
+static cudaError_t take_timeout(hrw_ode* o, bool* timed_out) {
+  *timed_out = false;
+  if (!o->tflag) return cudaSuccess;
+  unsigned int v = 0;
+  cudaError_t e = cudaMemcpyAsync(&v, o->tflag, sizeof(v), cudaMemcpyDeviceToHost, o->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(o->stream);
+  if (e == cudaSuccess && v) e = cudaMemsetAsync(o->tflag, 0, sizeof(v), o->stream);
+  if (e == cudaSuccess && v) e = cudaStreamSynchronize(o->stream);
+  *timed_out = v != 0;
+  return e;
+}
+
 static int integrate_on(hrw_ode* o, int mem, void* u, double* t, double tout, double dt, int itask);
 
 extern "C" int hrw_integrate(hrw_ode* o, int mem, void* u, double* t, double tout, double dt, int itask) {
@@ -964,7 +987,7 @@ static int integrate_on(hrw_ode* o, int mem, void* u, double* t, double tout, do
   HRW_CUDA(cudaStreamSynchronize(o->stream));
   if (o->prob.kind == HRW_PROBLEM_FV2D) {
     bool timed_out = false;
-    HRW_CUDA(o->dtype == HRW_F32C ? stage2d_f32c_timed_out(&timed_out) : stage2d_timed_out(&timed_out));
+    HRW_CUDA(take_timeout(o, &timed_out));
     if (timed_out) {
       o->istate = -1;
       return fail(HRW_ETIMEOUT, "hrw_integrate: a 2D stage block's bounded wait for its tile copies ran out.");
@@ -1001,8 +1024,7 @@ extern "C" int hrw_rhs(const hrw_problem* p, int dtype, double t, const void* v,
   }
   if (e == cudaSuccess) e = cudaStreamSynchronize(o->stream);
   bool timed_out = false;
-  if (e == cudaSuccess && p->kind == HRW_PROBLEM_FV2D)
-    e = dtype == HRW_F32C ? stage2d_f32c_timed_out(&timed_out) : stage2d_timed_out(&timed_out);
+  if (e == cudaSuccess && p->kind == HRW_PROBLEM_FV2D) e = take_timeout(o, &timed_out);
   hrw_ode_destroy(o);
   if (e != cudaSuccess) return fail(HRW_ECUDA, std::string("hrw_rhs: ") + cudaGetErrorString(e));
   if (timed_out) return fail(HRW_ETIMEOUT, "hrw_rhs: a 2D stage block's bounded wait for its tile copies ran out.");

@@ -1,11 +1,13 @@
-// diag.cu - FMA throughput of the device (hrweno_diag.h): the denominator of the FP64-pipe
-// roofline that bounds the FP64 stage kernels on GB300.
+// diag.cu - diagnostics (hrweno_diag.h): the FMA throughput of the device (the denominator of
+// the FP64-pipe roofline that bounds the FP64 stage kernels on GB300), the test hook for the 2D
+// kernels' bounded tile wait, and the FAST reciprocal next to IEEE division.
 #include <string>
 
 #include <cuda_runtime.h>
 
 #include "../../include/hrweno_diag.h"
 #include "../../include/hrweno_gpu.h"
+#include "hrw_device.cuh"
 #include "hrw_internal.h"
 
 namespace {
@@ -58,11 +60,37 @@ int rate(int iters, double* result) {
   return HRW_OK;
 }
 
+__global__ void rcp_kernel(const double* __restrict__ x, double* __restrict__ fast,
+                           double* __restrict__ exact, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    fast[i] = hrw::rcp_fast(x[i]);
+    exact[i] = __ddiv_rn(1.0, x[i]);
+  }
+}
+
 }  // namespace
 
 extern "C" int hrw_diag_fma_rates(double* dfma, double* ffma) {
   int rc = HRW_OK;
   if (dfma && (rc = rate<double>(256, dfma)) != HRW_OK) return rc;
   if (ffma && (rc = rate<float>(4096, ffma)) != HRW_OK) return rc;
+  return HRW_OK;
+}
+
+extern "C" int hrw_diag_set_tile_wait_limit(int polls) {
+  cudaError_t e = hrw::stage2d_set_tile_wait_limit(polls);
+  if (e == cudaSuccess) e = hrw::stage2d_f32c_set_tile_wait_limit(polls);
+  if (e != cudaSuccess) return hrw::set_error(HRW_ECUDA, cudaGetErrorString(e));
+  return HRW_OK;
+}
+
+extern "C" int hrw_diag_rcp(const double* x, double* fast, double* exact, int n) {
+  if (!x || !fast || !exact || n < 0) return hrw::set_error(HRW_EINVAL, "Invalid input: null pointer.");
+  if (n == 0) return HRW_OK;
+  rcp_kernel<<<(n + 255) / 256, 256>>>(x, fast, exact, n);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) return hrw::set_error(HRW_ECUDA, cudaGetErrorString(e));
   return HRW_OK;
 }

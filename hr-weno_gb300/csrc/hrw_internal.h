@@ -50,8 +50,14 @@ struct StageArgs {
   const double* cnu;  // non-uniform 1D line: weno coefficients cnu(0:k-1,-1:k-1,1:nc)
   // uniform 1D line (stage1d_kernel): update only cells cell0 .. cell0 + ncell - 1 (ncell = 0:
   // the whole line); cell0 and ncell are multiples of the launch's tile (1024 cells for lines
-  // of at least 2 x 152 x 1024 cells), so that ranges launched side by side write disjoint cells
+  // of at least 2 x SMs x 1024 cells), so that ranges launched side by side write disjoint cells
   int64_t cell0, ncell;
+  // set by the launcher: grids of at most this many blocks are one wave (4 blocks per SM of the
+  // current device) and release their programmatic dependents at once
+  int wave_blocks;
+  // 2D stages: the handle's word that a block sets when its bounded wait for its tile copies
+  // runs out (zero-initialised device memory; checked and cleared by the host after the call)
+  unsigned int* timeout_flag;
 };
 
 // ---- compensated FP32 form (hrw_f32c.cuh, stage1d_f32c.cu) ---------------------------------
@@ -99,18 +105,22 @@ struct F32CArgs {
   float c2_hi, c2_lo;
   float lscale2;
   int64_t ld;
+  unsigned int* timeout_flag;  // 2D stages: as StageArgs::timeout_flag
 };
 
 cudaError_t launch_stage1d_f32c(const F32CArgs& a, int k, int stage, cudaStream_t s);
 cudaError_t launch_stage2d_f32c(const F32CArgs& a, int k, int stage, cudaStream_t s);
-// whether a 2D compensated stage block gave up waiting for its TMA tile copies since the last
-// call (the flag is cleared); synchronises with the device
-cudaError_t stage2d_f32c_timed_out(bool* timed_out);
-// the same for the FP64 2D stage
-cudaError_t stage2d_timed_out(bool* timed_out);
+// Poll limit of the 2D stage kernels' first wait for their TMA tile copies (both the FP64 and
+// the compensated kernels; the wait that drains the copies after a timeout keeps its own
+// bound).  polls < 0 restores the default, 2^20.
+cudaError_t stage2d_set_tile_wait_limit(int polls);
+cudaError_t stage2d_f32c_set_tile_wait_limit(int polls);
 cudaError_t launch_split_f64(const double* u, float* hi, float* lo, int64_t n, cudaStream_t s);
 cudaError_t launch_merge_f64(const float* hi, const float* lo, double* u, int64_t n, cudaStream_t s);
 cudaError_t launch_widen_f32(const float* x, double* y, int64_t n, cudaStream_t s);
+
+// Multiprocessor count of the current device (cached per device; 152 on GB300).
+int device_sms();
 
 // FAST flux form: the kernels evaluate F / fscale, fscale folded into rws.
 double fast_flux_scale(int flux, int fn);

@@ -4,6 +4,8 @@
 //  * weno_calc_cnu on the device (src/hrweno_weno.f90:221-297): Shu eq. 2.20 coefficients of a
 //    non-uniform grid, one thread per (cell, r, j), in the reference's operation order;
 //  * reconstruction with per-cell coefficients (src/hrweno_weno.f90:170,177-181).
+#include <atomic>
+
 #include <cuda_runtime.h>
 
 #include "../../include/hrweno_gpu.h"
@@ -11,6 +13,24 @@
 #include "hrw_internal.h"
 
 namespace hrw {
+
+int device_sms() {
+  constexpr int kMaxDevices = 64;
+  static std::atomic<int> cache[kMaxDevices];  // 0: not looked up yet
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+    cudaGetLastError();
+    return 152;
+  }
+  int n = cache[dev].load(std::memory_order_relaxed);
+  if (n > 0) return n;
+  if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) {
+    cudaGetLastError();
+    return 152;
+  }
+  cache[dev].store(n, std::memory_order_relaxed);
+  return n;
+}
 
 // ---------------------------------------------------------------------------------------------
 template <int ST, bool STRICT>
@@ -59,7 +79,7 @@ static cudaError_t launch_linear_st(const double* rates, const StageArgs& a, int
                                     cudaStream_t s) {
   const int nt = 256;
   int64_t nb = (n + nt - 1) / nt;
-  if (nb > 152 * 16) nb = 152 * 16;
+  if (nb > (int64_t)device_sms() * 16) nb = (int64_t)device_sms() * 16;
   switch (stage) {
     case ST_RHS: stage_linear_kernel<ST_RHS, STRICT><<<(unsigned)nb, nt, 0, s>>>(rates, a, n); break;
     case ST_EULER: stage_linear_kernel<ST_EULER, STRICT><<<(unsigned)nb, nt, 0, s>>>(rates, a, n); break;

@@ -4,8 +4,10 @@
 // The two RK stage arrays of an rktvd(order 3) handle normally come from cudaMalloc when the
 // handle is created.  Here they live in one file-scope device array of fixed size, so a call
 // performs no allocation at all: it validates the problem on the host, looks up the array's
-// device address once per device, and launches the same three fused stage kernels, in the
-// same order, as hrw_integrate does for one RK3 step.
+// device address (on every call made outside stream capture, so that a device reset, which
+// reloads the module, cannot leave a stale address behind; a captured call uses the address
+// the last uncaptured call on that device found), and launches the same three fused stage
+// kernels, in the same order, as hrw_integrate does for one RK3 step.
 #include <cmath>
 #include <mutex>
 
@@ -27,19 +29,27 @@ static __device__ __align__(256) double g_stage_scratch[2 * kMaxCells];
 std::mutex g_mu;
 double* g_addr[kMaxDevices] = {};
 
-// Device address of g_stage_scratch on the current device, looked up once per device.
-int scratch_address(double** out) {
+// Device address of g_stage_scratch on the current device.  Looked up again on every call
+// whose stream is not capturing (cheap once the module is loaded); a capturing call reuses the
+// address of the last uncaptured call on the device and fails if there was none.
+int scratch_address(cudaStream_t s, double** out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return hrw::set_error(HRW_ECUDA, cudaGetErrorString(e));
   if (dev < 0 || dev >= kMaxDevices) return hrw::set_error(HRW_EINVAL, "device ordinal too large");
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  e = cudaStreamIsCapturing(s, &cs);
+  if (e != cudaSuccess) return hrw::set_error(HRW_ECUDA, cudaGetErrorString(e));
   std::lock_guard<std::mutex> lock(g_mu);
-  if (!g_addr[dev]) {
+  if (cs == cudaStreamCaptureStatusNone) {
     void* p = nullptr;
     e = cudaGetSymbolAddress(&p, g_stage_scratch);
     if (e != cudaSuccess || !p)
       return hrw::set_error(HRW_ECUDA, "hrw_rktvd3_steps_noalloc: cudaGetSymbolAddress failed");
     g_addr[dev] = static_cast<double*>(p);
+  } else if (!g_addr[dev]) {
+    return hrw::set_error(HRW_ECUDA,
+                          "hrw_rktvd3_steps_noalloc: the first call on a device must not be captured");
   }
   *out = g_addr[dev];
   return HRW_OK;
@@ -77,8 +87,11 @@ extern "C" int hrw_rktvd3_steps_noalloc(const hrw_problem* p, double* u, double 
   if (!(dt != 0.0) || !std::isfinite(dt))
     return set_error(HRW_EINVAL, "Invalid input 'dt': must be finite and nonzero.");
 
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  // an error left by earlier, unrelated work is not this call's: clear it before launching
+  cudaGetLastError();
   double* scratch = nullptr;
-  int rc = scratch_address(&scratch);
+  int rc = scratch_address(s, &scratch);
   if (rc != HRW_OK) return rc;
   double* u1 = scratch;
   double* u2 = scratch + kMaxCells;
@@ -100,7 +113,6 @@ extern "C" int hrw_rktvd3_steps_noalloc(const hrw_problem* p, double* u, double 
   L.rws0 = fast_flux_scale(p->flux, p->fn[0]) / L.rx;
   b.ld = nc;
   const bool strict = p->numerics == HRW_NUMERICS_STRICT;
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
 
   for (int n = 0; n < nsteps; ++n) {  // rktvd order 3 (src/hrweno_tvdode.f90:161-169)
     StageArgs a = b;

@@ -78,7 +78,7 @@ __global__ void __launch_bounds__(NT) stage1d_kernel(StageArgs a) {
   // a grid of at most one wave (every block resident from the start) lets the next stage's
   // grid launch at once, its blocks queueing behind this one's; larger grids trigger it as
   // their blocks exit, so that waiting blocks take no slots from their later waves
-  if (gridDim.x <= 152 * 4) asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  if ((int)gridDim.x <= a.wave_blocks) asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 
   for (int q = tid; q < T + 2 * H; q += NT) {
     int64_t g = s - H + q;
@@ -160,7 +160,9 @@ static cudaError_t launch_shape(const StageArgs& a, cudaStream_t s) {
   attr[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  const cudaError_t e = cudaLaunchKernelEx(&cfg, stage1d_kernel<K, ST, STRICT, NT, C>, a);
+  StageArgs b = a;
+  b.wave_blocks = device_sms() * 4;
+  const cudaError_t e = cudaLaunchKernelEx(&cfg, stage1d_kernel<K, ST, STRICT, NT, C>, b);
   if (e != cudaSuccess) return e;
   return cudaGetLastError();
 }
@@ -170,9 +172,9 @@ static cudaError_t launch_shape(const StageArgs& a, cudaStream_t s) {
 // spread over many SMs (each SM retires only about 2 FP64 instructions per clock).
 template <int K, int ST, bool STRICT>
 static cudaError_t launch_k(const StageArgs& a, cudaStream_t s) {
-  const int64_t nc = a.L.nc;
-  if (nc >= 2 * 152 * 1024) return launch_shape<K, ST, STRICT, 128, 8>(a, s);
-  if (nc >= 2 * 152 * 256) return launch_shape<K, ST, STRICT, 64, 4>(a, s);
+  const int64_t nc = a.L.nc, sms = device_sms();
+  if (nc >= 2 * sms * 1024) return launch_shape<K, ST, STRICT, 128, 8>(a, s);
+  if (nc >= 2 * sms * 256) return launch_shape<K, ST, STRICT, 64, 4>(a, s);
   return launch_shape<K, ST, STRICT, 32, 2>(a, s);
 }
 

@@ -48,7 +48,7 @@ template <int K, int ST>
 static cudaError_t launch_k(const F32CArgs& a, cudaStream_t s) {
   // long lines: 8 cells per thread; 256-thread blocks for k = 3, 128 for k = 2 (measured on the
   // 2^24-cell line: 0.229 vs 0.231 ms per RK3 step for k = 3, 0.184 vs 0.172 ms for k = 2)
-  if (a.L.nc >= 2 * 152 * 2048)
+  if (a.L.nc >= 2 * (int64_t)device_sms() * 2048)
     return K == 2 ? launch_shape<K, ST, 128, 8>(a, s) : launch_shape<K, ST, 256, 8>(a, s);
   return launch_shape<K, ST, 32, 4>(a, s);
 }
@@ -100,20 +100,20 @@ __global__ void widen_f32_kernel(const float* __restrict__ x, double* __restrict
 cudaError_t launch_widen_f32(const float* x, double* y, int64_t n, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
   const int64_t nb = (n + 255) / 256;
-  widen_f32_kernel<<<(unsigned)(nb < 152 * 16 ? nb : 152 * 16), 256, 0, s>>>(x, y, n);
+  widen_f32_kernel<<<(unsigned)(nb < device_sms() * 16 ? nb : device_sms() * 16), 256, 0, s>>>(x, y, n);
   return cudaGetLastError();
 }
 
 cudaError_t launch_split_f64(const double* u, float* hi, float* lo, int64_t n, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
   const int64_t nb = (n + 255) / 256;
-  split_f64_kernel<<<(unsigned)(nb < 152 * 16 ? nb : 152 * 16), 256, 0, s>>>(u, hi, lo, n);
+  split_f64_kernel<<<(unsigned)(nb < device_sms() * 16 ? nb : device_sms() * 16), 256, 0, s>>>(u, hi, lo, n);
   return cudaGetLastError();
 }
 cudaError_t launch_merge_f64(const float* hi, const float* lo, double* u, int64_t n, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
   const int64_t nb = (n + 255) / 256;
-  merge_f64_kernel<<<(unsigned)(nb < 152 * 16 ? nb : 152 * 16), 256, 0, s>>>(hi, lo, u, n);
+  merge_f64_kernel<<<(unsigned)(nb < device_sms() * 16 ? nb : device_sms() * 16), 256, 0, s>>>(hi, lo, u, n);
   return cudaGetLastError();
 }
 

@@ -37,8 +37,10 @@ constexpr int TX = 32, TY = 32, C = 8, NT = 128;
 static_assert(TX * TY == NT * C, "one segment of C cells per thread and direction");
 static_assert(TX == 32 && TY / C == NT / 32 && TX / C == NT / 32, "warp-per-segment mapping");
 
-__device__ unsigned int g_tma_timeout;  // set when a block's bounded mbarrier wait ran out
-constexpr int BX = 40, BY = 38;         // TMA box of the tile plus halo: x from bx - 4, y from by - 3
+// poll limit of the first wait for the tile copies (stage2d_set_tile_wait_limit)
+constexpr int kTileWaitPolls = 1 << 20;
+__device__ int g_tile_wait_limit = kTileWaitPolls;
+constexpr int BX = 40, BY = 38;  // TMA box of the tile plus halo: x from bx - 4, y from by - 3
 
 // TMA: the tile plus halo of the stage input comes in as one 40 x 38 box of doubles at
 // (bx - 4, by - 3) (x on a 16-byte boundary), completing on a block mbarrier; the block then
@@ -73,10 +75,12 @@ __global__ void __launch_bounds__(NT) stage2d_kernel(const __grid_constant__ CUt
       mbar_expect_tx(&bar, BY * BX * 8);
       tma_load_2d(tbox, &Mv, (int)bx - 4, (int)by - 3, &bar);
     }
-    const bool ok = mbar_wait(&bar, 0, 1 << 20);  // bounded, as stage2d_f32c.cu
+    // bounded wait; on a timeout every thread of the block learns of it, the block waits
+    // (with the default bound) for its copy to land and leaves, and the host sees the flag
+    const bool ok = mbar_wait(&bar, 0, g_tile_wait_limit);
     if (__syncthreads_or(!ok)) {
-      if (tid == 0) atomicExch(&g_tma_timeout, 1u);
-      mbar_wait(&bar, 0, 1 << 20);
+      if (tid == 0) atomicExch(a.timeout_flag, 1u);
+      mbar_wait(&bar, 0, kTileWaitPolls);
       return;
     }
     const int ibx = (int)bx, iby = (int)by, in1 = (int)n1, in2 = (int)n2;
@@ -256,17 +260,14 @@ cudaError_t launch_kk(const StageArgs& a, int k, int stage, cudaStream_t s) {
 
 }  // namespace
 
-cudaError_t stage2d_timed_out(bool* timed_out) {
-  unsigned int v = 0, zero = 0;
-  cudaError_t e = cudaMemcpyFromSymbol(&v, g_tma_timeout, sizeof(v));
-  if (e == cudaSuccess && v) e = cudaMemcpyToSymbol(g_tma_timeout, &zero, sizeof(zero));
-  *timed_out = v != 0;
-  return e;
+cudaError_t stage2d_set_tile_wait_limit(int polls) {
+  const int v = polls < 0 ? kTileWaitPolls : polls;
+  return cudaMemcpyToSymbol(g_tile_wait_limit, &v, sizeof(v));
 }
 
 cudaError_t launch_stage2d(const StageArgs& a, int k, int stage, bool strict, cudaStream_t s) {
   if (a.L.nc <= 0 || a.L2.nc <= 0) return cudaSuccess;
-  if (a.L2.nc > 65535LL * TY) return cudaErrorInvalidValue;
+  if (a.L2.nc > 65535LL * TY || !a.timeout_flag) return cudaErrorInvalidValue;
   const bool upw = a.upwind;
   if (strict) return upw ? launch_kk<true, true>(a, k, stage, s) : launch_kk<true, false>(a, k, stage, s);
   return upw ? launch_kk<false, true>(a, k, stage, s) : launch_kk<false, false>(a, k, stage, s);

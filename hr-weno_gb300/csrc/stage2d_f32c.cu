@@ -46,7 +46,9 @@ struct TileMaps {
   CUtensorMap h4, l4, L4;
 };
 
-__device__ unsigned int g_tma_timeout;  // set when a block's bounded mbarrier wait ran out
+// poll limit of the first wait for the tile copies (stage2d_f32c_set_tile_wait_limit)
+constexpr int kTileWaitPolls = 1 << 20;
+__device__ int g_tile_wait_limit = kTileWaitPolls;
 
 // WENO offsets of the C cells of a segment from its differences d[0 .. C+2K-2]; for k = 3 the
 // 13/12 (second difference)^2 terms are computed once per window position (as the 1D pass)
@@ -134,10 +136,10 @@ __global__ void __launch_bounds__(NT) stage2d_f32c_kernel(const __grid_constant_
     }
     // bounded wait; on a timeout every thread of the block learns of it, the block waits
     // (bounded again) for its copies to land and leaves, and the host sees the flag
-    const bool ok = mbar_wait(&bar, 0, 1 << 20);
+    const bool ok = mbar_wait(&bar, 0, g_tile_wait_limit);
     if (__syncthreads_or(!ok)) {
-      if (tid == 0) atomicExch(&g_tma_timeout, 1u);
-      mbar_wait(&bar, 0, 1 << 20);
+      if (tid == 0) atomicExch(a.timeout_flag, 1u);
+      mbar_wait(&bar, 0, kTileWaitPolls);
       return;
     }
     for (int q = tid; q < (TY + 2 * H) * RW; q += NT) {
@@ -251,10 +253,10 @@ __global__ void __launch_bounds__(NT) stage2d_f32c_kernel(const __grid_constant_
 
   // ---- x2 flux differences, dt L and the stage update ------------------------------------------
   if constexpr (TMA && MS) {  // the history tiles (bounded wait, as for the boxes)
-    const bool ok = mbar_wait(&bar, 1, 1 << 20);
+    const bool ok = mbar_wait(&bar, 1, kTileWaitPolls);
     if (__syncthreads_or(!ok)) {
-      if (tid == 0) atomicExch(&g_tma_timeout, 1u);
-      mbar_wait(&bar, 1, 1 << 20);
+      if (tid == 0) atomicExch(a.timeout_flag, 1u);
+      mbar_wait(&bar, 1, kTileWaitPolls);
       return;
     }
   }
@@ -404,20 +406,15 @@ bool tile_map_2d(const void* p, int elem_bytes, int n1, int n2, int box_x, int b
 
 cudaError_t launch_stage2d_f32c(const F32CArgs& a, int k, int stage, cudaStream_t s) {
   if (a.L.nc <= 0 || a.L2.nc <= 0) return cudaSuccess;
-  if (a.L2.nc > 65535LL * TY) return cudaErrorInvalidValue;
+  if (a.L2.nc > 65535LL * TY || !a.timeout_flag) return cudaErrorInvalidValue;
   if (k == 1) return launch_st<1>(a, stage, s);
   if (k == 2) return launch_st<2>(a, stage, s);
   return launch_st<3>(a, stage, s);
 }
 
-// Whether a block of a 2D compensated stage gave up waiting for its tile copies since the
-// last call (and clear the flag).  Synchronises with the device.
-cudaError_t stage2d_f32c_timed_out(bool* timed_out) {
-  unsigned int v = 0, zero = 0;
-  cudaError_t e = cudaMemcpyFromSymbol(&v, g_tma_timeout, sizeof(v));
-  if (e == cudaSuccess && v) e = cudaMemcpyToSymbol(g_tma_timeout, &zero, sizeof(zero));
-  *timed_out = v != 0;
-  return e;
+cudaError_t stage2d_f32c_set_tile_wait_limit(int polls) {
+  const int v = polls < 0 ? kTileWaitPolls : polls;
+  return cudaMemcpyToSymbol(g_tile_wait_limit, &v, sizeof(v));
 }
 
 }  // namespace hrw

@@ -1,9 +1,10 @@
 /*
  * hrweno_diag.h - diagnostics of the GB300 library (no counterpart in the reference).
  *
- * The stage kernels of the FP64 path are bound by the FP64 pipe, not by HBM; this call
+ * The stage kernels of the FP64 path are bound by the FP64 pipe, not by HBM; one call
  * measures that pipe on the current device so that a benchmark can report the kernel's
- * fraction of it next to its HBM roofline fraction.
+ * fraction of it next to its HBM roofline fraction.  The others expose internals to the tests:
+ * the 2D kernels' bounded wait, and the FAST path's reciprocal.
  */
 #ifndef HRWENO_DIAG_H
 #define HRWENO_DIAG_H
@@ -14,6 +15,18 @@ extern "C" {
 /* DFMA instructions retired per second by the whole device (independent FMA chains on every
  * SM), and FFMA likewise; either pointer may be NULL. */
 int hrw_diag_fma_rates(double* dfma_per_second, double* ffma_per_second);
+
+/* Poll limit of the 2D stage kernels' first wait for their TMA tile copies, on the current
+ * device (FP64 and compensated FP32 kernels).  A block whose wait runs out flags its handle,
+ * waits for its copies with the default bound and leaves; hrw_integrate / hrw_rhs then return
+ * HRW_ETIMEOUT.  A small limit (0: no poll at all) lets a test drive that path to expiry
+ * without any copy going missing.  polls < 0 restores the default (2^20 polls). */
+int hrw_diag_set_tile_wait_limit(int polls);
+
+/* Reciprocals by the FAST path's rcp_fast (an rcp.approx.f64 seed and one cubic
+ * Newton-Raphson step) and by IEEE division (__ddiv_rn(1, x)), for n device doubles x:
+ * fast[i], exact[i].  Device pointers; synchronous. */
+int hrw_diag_rcp(const double* x, double* fast, double* exact, int n);
 
 #ifdef __cplusplus
 }

@@ -230,11 +230,14 @@ int hrw_adjoint_destroy(hrw_adjoint* a);
  * stream), and returns without waiting for the GPU.  The two RK stage arrays live in one
  * fixed buffer inside the library (2 * HRW_NOALLOC_MAX_CELLS doubles, 16 MiB, held by every
  * GPU that loads the library until the process exits); larger lines are rejected with
- * HRW_EINVAL.  The first call on a device looks up that buffer's device address, so make
- * that first call before any stream capture.  All calls share the buffer: calls whose work
- * overlaps on the GPU (other streams, other threads) race and give wrong results; calls on
- * one stream are ordered and safe.  Same kernels and operation order as hrw_integrate, so
- * the results are bit-identical to an rktvd(order 3) handle's. */
+ * HRW_EINVAL.  A call looks up that buffer's device address when its stream is not being
+ * captured; a captured call reuses the address found by the last uncaptured call on the
+ * device, so make the first call on a device (and the first after a device reset) outside any
+ * stream capture.  All calls share the buffer: calls whose work overlaps on the GPU (other
+ * streams, other threads) race and give wrong results; calls on one stream are ordered and
+ * safe.  On HRW_ECUDA some steps may have been queued: the contents of u are then undefined.
+ * Same kernels and operation order as hrw_integrate, so the results are bit-identical to an
+ * rktvd(order 3) handle's. */
 #define HRW_NOALLOC_MAX_CELLS (1 << 20)
 int hrw_rktvd3_steps_noalloc(const hrw_problem* p, double* u, double dt, int nsteps, void* stream);
 

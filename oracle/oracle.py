@@ -16,25 +16,45 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 SRC = HERE / "hrweno_oracle.cpp"
 LIB = HERE / "_build" / "libhrweno_oracle.so"
+# Two builds of the same source:
+#  parity   -O2, no fused multiply-add: the reference's operation order, the parity checker
+#  baseline -O3 with the compiler's default contraction (as a gfortran -O3 build of the
+#           reference would be): the fastest build of the restatement, used only to time the
+#           CPU baseline; its results agree with the parity build to rounding
+BUILDS = {
+    "parity": (LIB, ["-O2", "-ffp-contract=off"]),
+    "baseline": (HERE / "_build" / "libhrweno_oracle_o3.so", ["-O3"]),
+}
+COMMON = ["-fopenmp", "-fPIC", "-shared", "-std=c++17"]
 
 _lib = None
+_variant = "parity"
 
 
-def build(force: bool = False) -> Path:
-    """Compile the oracle with g++ (no fused multiply-add)."""
-    LIB.parent.mkdir(exist_ok=True)
+def build(force: bool = False, variant: str = "parity") -> Path:
+    """Compile one build of the oracle with g++."""
+    out, flags = BUILDS[variant]
+    out.parent.mkdir(exist_ok=True)
     hdr = HERE.parent / "include" / "hrweno_gpu.h"
-    if force or not LIB.exists() or LIB.stat().st_mtime < max(SRC.stat().st_mtime, hdr.stat().st_mtime):
-        subprocess.run(["g++", "-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared",
-                        "-std=c++17", "-o", str(LIB), str(SRC)], check=True)
-    return LIB
+    if force or not out.exists() or out.stat().st_mtime < max(SRC.stat().st_mtime, hdr.stat().st_mtime):
+        subprocess.run(["g++", *flags, *COMMON, "-o", str(out), str(SRC)], check=True)
+    return out
+
+
+def select_build(variant: str) -> None:
+    """Use the 'parity' (default) or the 'baseline' build for the calls that follow."""
+    global _lib, _variant
+    if variant not in BUILDS:
+        raise ValueError(variant)
+    if variant != _variant:
+        _variant = variant
+        _lib = None
 
 
 def lib() -> C.CDLL:
     global _lib
     if _lib is None:
-        build()
-        L = C.CDLL(str(LIB))
+        L = C.CDLL(str(build(variant=_variant)))
         dp = C.POINTER(C.c_double)
         L.orc_last_error.restype = C.c_char_p
         L.orc_weno_reconstruct.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, dp, dp, dp, dp]

@@ -66,15 +66,16 @@ def _header_problem_fields():
 
 
 def test_problem_layouts_agree():
-    """struct hrw_problem, its ctypes mirror and the Fortran bind(c) type in INTEGRATION.md list
-    the same fields in the same order (a missing field shifts every later one)."""
+    """struct hrw_problem, its ctypes mirror and the Fortran bind(c) type of the binding module
+    (hr-weno_gb300/fortran/hrweno_gpu.f90) list the same fields in the same order (a missing
+    field shifts every later one)."""
     import re
     import ctypes as C
     from hrweno import _abi
     hdr = _header_problem_fields()
     cty = [(name, getattr(t, "_length_", 1)) for name, t in _abi.HrwProblem._fields_]
     assert hdr == cty, (hdr, cty)
-    text = (ROOT / "INTEGRATION.md").read_text()
+    text = (ROOT / "hr-weno_gb300" / "fortran" / "hrweno_gpu.f90").read_text()
     block = text[text.index("type, bind(c) :: hrw_problem"):]
     block = block[:block.index("end type")]
     fort = []
@@ -206,3 +207,20 @@ def test_constants_agree_with_the_header():
     assert len(consts) >= 20
     for name, value in consts.items():
         assert getattr(hrweno, name) == value, name
+
+
+def test_fortran_binding_names_exist():
+    """Every C entry point the Fortran module binds (bind(c, name=...)) is declared in the
+    header and exported by the library; the module keeps the reference's type names."""
+    import re
+    text = (ROOT / "hr-weno_gb300" / "fortran" / "hrweno_gpu.f90").read_text()
+    hdr = (ROOT / "include" / "hrweno_gpu.h").read_text()
+    names = re.findall(r'bind\(c,\s*name="(\w+)"\)', text)
+    assert len(names) >= 10
+    for n in names:
+        assert re.search(rf"\b{n}\s*\(", hdr), n
+    for t in ("weno", "rktvd", "mstvd"):
+        assert re.search(rf"^\s*type(, extends\(\w+\))? :: {t}\s*$", text, flags=re.M), t
+        assert re.search(rf"^\s*interface {t}\s*$", text, flags=re.M), t
+    for m in ("reconstruct", "integrate"):
+        assert re.search(rf"procedure :: {m} =>", text), m
