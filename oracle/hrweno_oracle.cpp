@@ -310,21 +310,38 @@ struct Problem {
     const Line<T>& L2 = line[1];
     const int n1 = L1.nc, n2 = L2.nc;
     std::vector<T> F1((size_t)(n1 + 1) * n2), F2((size_t)(n2 + 1) * n1);
-    for (int j = 1; j <= n2; ++j)  // x1 sweep over contiguous rows (:97-103)
-      line_fluxes<T>(p, 0, L1, eps, t, v + (size_t)(j - 1) * n1, vl.data(), vr.data(),
-                     F1.data() + (size_t)(j - 1) * (n1 + 1));
-    for (int i = 1; i <= n1; ++i) {  // x2 sweep over strided columns (:106-112)
-      for (int j = 1; j <= n2; ++j) col[j - 1] = v[(size_t)(j - 1) * n1 + (i - 1)];
-      line_fluxes<T>(p, 1, L2, eps, t, col.data(), vl.data(), vr.data(),
-                     F2.data() + (size_t)(i - 1) * (n2 + 1));
-    }
-    for (int j = 1; j <= n2; ++j)  // (:123-127)
-      for (int i = 1; i <= n1; ++i) {
-        const T* f1 = F1.data() + (size_t)(j - 1) * (n1 + 1);
-        const T* f2 = F2.data() + (size_t)(i - 1) * (n2 + 1);
-        vdot[(size_t)(j - 1) * n1 + (i - 1)] =
-            -((f1[i] - f1[i - 1]) / L1.w(i)) - (f2[j] - f2[j - 1]) / L2.w(j);
+    // the rows, then the columns, split over threads (the example's own commented-out OpenMP
+    // loop, example2...f90:95-114): each line's arithmetic, and so every bit, is unchanged
+#ifdef _OPENMP
+#pragma omp parallel
+#endif
+    {
+      std::vector<T> tvl(vl.size()), tvr(vr.size()), tcol(col.size());
+#ifdef _OPENMP
+#pragma omp for schedule(static)
+#endif
+      for (int j = 1; j <= n2; ++j)  // x1 sweep over contiguous rows (:97-103)
+        line_fluxes<T>(p, 0, L1, eps, t, v + (size_t)(j - 1) * n1, tvl.data(), tvr.data(),
+                       F1.data() + (size_t)(j - 1) * (n1 + 1));
+#ifdef _OPENMP
+#pragma omp for schedule(static)
+#endif
+      for (int i = 1; i <= n1; ++i) {  // x2 sweep over strided columns (:106-112)
+        for (int j = 1; j <= n2; ++j) tcol[j - 1] = v[(size_t)(j - 1) * n1 + (i - 1)];
+        line_fluxes<T>(p, 1, L2, eps, t, tcol.data(), tvl.data(), tvr.data(),
+                       F2.data() + (size_t)(i - 1) * (n2 + 1));
       }
+#ifdef _OPENMP
+#pragma omp for schedule(static)
+#endif
+      for (int j = 1; j <= n2; ++j)  // (:123-127)
+        for (int i = 1; i <= n1; ++i) {
+          const T* f1 = F1.data() + (size_t)(j - 1) * (n1 + 1);
+          const T* f2 = F2.data() + (size_t)(i - 1) * (n2 + 1);
+          vdot[(size_t)(j - 1) * n1 + (i - 1)] =
+              -((f1[i] - f1[i - 1]) / L1.w(i)) - (f2[j] - f2[j - 1]) / L2.w(j);
+        }
+    }
   }
 };
 
