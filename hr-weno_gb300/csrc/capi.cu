@@ -46,6 +46,9 @@ inline bool is_done(double t, double tout, double dt) {
 }
 
 constexpr int64_t kMaxSteps = int64_t(1) << 40;
+// MIXED numerics take the MIXED kernel on lines of at least this many cells (shorter lines are
+// launch-bound, and the FAST kernel's shared-memory tile serves them better)
+constexpr int kMixedMinCells = 1 << 16;
 
 struct DevLine {
   double* width = nullptr;  // device copy of the user's widths (STRICT)
@@ -90,8 +93,11 @@ int validate_problem(const hrw_problem* p, int neq) {
     return fail(HRW_EINVAL, "Invalid input 'eps'. Valid range: eps > epsilon.");
   if (p->flux != HRW_FLUX_LAX_FRIEDRICHS && p->flux != HRW_FLUX_GODUNOV)
     return fail(HRW_EINVAL, "Invalid input 'flux'.");
-  if (p->numerics != HRW_NUMERICS_FAST && p->numerics != HRW_NUMERICS_STRICT)
+  if (p->numerics != HRW_NUMERICS_FAST && p->numerics != HRW_NUMERICS_STRICT &&
+      p->numerics != HRW_NUMERICS_MIXED)
     return fail(HRW_EINVAL, "Invalid input 'numerics'.");
+  if (p->numerics == HRW_NUMERICS_MIXED && !(p->eps >= 1e-8))
+    return fail(HRW_EINVAL, "Invalid input 'eps': HRW_NUMERICS_MIXED needs eps >= 1e-8.");
   if (cells != neq) return fail(HRW_EINVAL, "Invalid input 'neq': neq /= product of ncells.");
   return HRW_OK;
 }
@@ -158,6 +164,11 @@ struct hrw_ode {
   cudaEvent_t ev_start = nullptr, ev_in[16] = {}, ev_s3[16] = {}, ev_join[3] = {};
   // 2D problems: the word a stage block sets when its bounded wait for its tile copies ran out
   unsigned int* tflag = nullptr;
+  // MIXED numerics on a line the MIXED kernel covers: its arguments and the word holding the
+  // high word of max|u| at the start of each integrate call
+  bool mixed = false;
+  MixedArgs mbase{};
+  unsigned int* mscale = nullptr;
 };
 
 extern "C" {
@@ -447,6 +458,15 @@ static int ode_create(const hrw_problem* p, int neq, int order, int method, int 
   }
   if ((e = cudaMalloc(&o->w1, bytes)) != cudaSuccess) return cleanup(e);
   if ((e = cudaMalloc(&o->w2, bytes)) != cudaSuccess) return cleanup(e);
+  // MIXED numerics: lines of at least kMixedMinCells cells that the MIXED kernel covers take it
+  // (shorter lines, and everything else, run the FAST kernels)
+  if (p->numerics == HRW_NUMERICS_MIXED && p->kind == HRW_PROBLEM_FV1D && method == 0 &&
+      !p->xedges[0] && !p->width[0] && neq >= kMixedMinCells && mixed_supported(b.L, p->k)) {
+    if ((e = cudaMalloc(&o->mscale, sizeof(unsigned int))) != cudaSuccess) return cleanup(e);
+    o->mixed = true;
+    o->mbase.L = b.L;
+    o->mbase.eps = p->eps;
+  }
   if (method == 1) {
     for (int q = 0; q < 5; ++q)
       if ((e = cudaMalloc(&o->ring_u[q], bytes)) != cudaSuccess) return cleanup(e);
@@ -503,6 +523,7 @@ int hrw_ode_destroy(hrw_ode* o) {
     if (p) cudaFree(p);
   if (o->fmem) cudaFree(o->fmem);
   if (o->tflag) cudaFree(o->tflag);
+  if (o->mscale) cudaFree(o->mscale);
   if (o->graph.exec) cudaGraphExecDestroy(o->graph.exec);
   for (cudaStream_t st : {o->pipe[0], o->pipe[1], o->copy})
     if (st) cudaStreamDestroy(st);
@@ -566,6 +587,38 @@ static cudaError_t rk_step(hrw_ode* o, double* u, double* out1, double dt) {
   return run_stage(o, ST_RK3C, o->w2, u, u, nullptr, nullptr, nullptr, dt);
 }
 
+// One rktvd step of the MIXED kernel from `cur` into `other` (the state ping-pongs between
+// them: a stage's stencil reads u, so the last stage cannot write u in place).  Order 3:
+//   d1 -> other (float pairs), d2 -> w2 (float pairs), u' -> other (over d1).
+static cudaError_t rk_step_mixed(hrw_ode* o, const double* cur, double* other, double dt) {
+  MixedArgs a = o->mbase;
+  mixed_fill(a, o->prob.eps, dt);
+  a.u = cur;
+  a.scale = o->mscale;
+  const int k = o->prob.k;
+  cudaError_t e;
+  float2* d1 = reinterpret_cast<float2*>(o->order == 2 ? o->w2 : other);
+  float2* d2 = reinterpret_cast<float2*>(o->w2);
+  if (o->order == 1) {
+    a.uout = other;
+    return launch_stage1d_mixed(a, k, MX_RK1, o->stream);
+  }
+  a.dout = d1;
+  if ((e = launch_stage1d_mixed(a, k, MX_E1, o->stream)) != cudaSuccess) return e;
+  a.dout = nullptr;
+  a.dv = d1;
+  if (o->order == 2) {
+    a.uout = other;
+    return launch_stage1d_mixed(a, k, MX_RK2B, o->stream);
+  }
+  a.dout = d2;
+  if ((e = launch_stage1d_mixed(a, k, MX_RK3B, o->stream)) != cudaSuccess) return e;
+  a.dout = nullptr;
+  a.dv = d2;
+  a.uout = other;
+  return launch_stage1d_mixed(a, k, MX_RK3C, o->stream);
+}
+
 // Captured graphs hold up to kGraphMax consecutive steps (rktvd; an even count for order 1,
 // which ping-pongs between two arrays) or a multiple of kMsPeriod steps (mstvd rotates a
 // 5-slot and a 4-slot ring, so its launch pattern repeats every 20 steps).  A driver loop that
@@ -623,8 +676,37 @@ static cudaError_t run_graph(hrw_ode* o, const void* ptr, double dt, int64_t pha
 static int64_t rk_graph_steps(const hrw_ode* o, int64_t n) {
   if (!o->use_graphs || n < 4) return 0;
   int64_t G = n < kGraphMax ? n : kGraphMax;
-  if (o->order == 1) G &= ~int64_t(1);
+  if (o->order == 1 || o->mixed) G &= ~int64_t(1);  // the state ping-pongs between two arrays
   return G;
+}
+
+// rktvd_integrate of the MIXED kernel: n steps from du (the state alternates between du and w1)
+static int rk_integrate_mixed(hrw_ode* o, double* du, int64_t n, double dt) {
+  HRW_CUDA(launch_mixed_scale(du, o->neq, o->mscale, o->stream));
+  double* cur = du;
+  double* other = o->w1;
+  int64_t s0 = 0;
+  if (const int64_t G = rk_graph_steps(o, n)) {
+    bool ok = false;
+    HRW_CUDA(run_graph(o, du, dt, 1, G, n / G, &ok, [&]() {
+      double* c = du;
+      double* w = o->w1;
+      for (int64_t s = 0; s < G; ++s) {
+        const cudaError_t e = rk_step_mixed(o, c, w, dt);
+        if (e != cudaSuccess) return e;
+        std::swap(c, w);
+      }
+      return cudaSuccess;
+    }));
+    if (ok) s0 = n / G * G;
+  }
+  for (int64_t s = s0; s < n; ++s) {
+    HRW_CUDA(rk_step_mixed(o, cur, other, dt));
+    std::swap(cur, other);
+  }
+  if (cur != du)
+    HRW_CUDA(cudaMemcpyAsync(du, cur, sizeof(double) * (size_t)o->neq, cudaMemcpyDeviceToDevice, o->stream));
+  return HRW_OK;
 }
 
 // rktvd_integrate (src/hrweno_tvdode.f90:97-178) on device array du.
@@ -636,6 +718,17 @@ static int rk_integrate(hrw_ode* o, double* du, double* t, double tout, double d
     tt = tt + dt;
     if (++n > kMaxSteps) return fail(HRW_EINVAL, "Invalid input 'dt': too many steps to reach tout.");
   } while (!(is_done(tt, tout, dt) || itask == 2));
+  // the MIXED kernel moves 16-byte vectors: a device array that is not 16-byte aligned (a view
+  // at an odd offset) runs the FAST kernels
+  if (o->mixed && ((uintptr_t)du & 15) == 0) {
+    const int rc = rk_integrate_mixed(o, du, n, dt);
+    if (rc != HRW_OK) return rc;
+    *t = tt;
+    o->fevals += (int)(o->order * n);
+    o->nsteps += n;
+    if (o->istate == 1) o->istate = 2;
+    return HRW_OK;
+  }
   double* cur = du;
   double* other = o->w2;
   int64_t s0 = 0;
@@ -856,7 +949,7 @@ constexpr int64_t kPipeTile = 1024;
 static_assert(kPipeChunks <= (int)(sizeof(hrw_ode::ev_in) / sizeof(cudaEvent_t)), "one event per chunk");
 
 static bool host_pipeline_ok(const hrw_ode* o, const void* u) {
-  if (o->dtype != HRW_F64 || o->prob.kind != HRW_PROBLEM_FV1D || o->method != 0 || o->order != 3 ||
+  if (o->mixed || o->dtype != HRW_F64 || o->prob.kind != HRW_PROBLEM_FV1D || o->method != 0 || o->order != 3 ||
       o->line[0].xe || (int64_t)o->neq < 2 * (int64_t)device_sms() * kPipeTile)
     return false;
   cudaPointerAttributes at{};

@@ -94,3 +94,16 @@ extern "C" int hrw_diag_rcp(const double* x, double* fast, double* exact, int n)
   if (e != cudaSuccess) return hrw::set_error(HRW_ECUDA, cudaGetErrorString(e));
   return HRW_OK;
 }
+
+extern "C" int hrw_diag_mixed_soft(int enable) {
+  const cudaError_t e = hrw::mixed_set_soft(enable);
+  if (e != cudaSuccess) return hrw::set_error(HRW_ECUDA, cudaGetErrorString(e));
+  return HRW_OK;
+}
+
+extern "C" int hrw_diag_mixed_hard_warps(unsigned long long* count, int reset) {
+  if (!count) return hrw::set_error(HRW_EINVAL, "Invalid input: null pointer.");
+  const cudaError_t e = hrw::mixed_hard_warps(count, reset != 0);
+  if (e != cudaSuccess) return hrw::set_error(HRW_ECUDA, cudaGetErrorString(e));
+  return HRW_OK;
+}

@@ -108,6 +108,43 @@ struct F32CArgs {
   unsigned int* timeout_flag;  // 2D stages: as StageArgs::timeout_flag
 };
 
+// ---- MIXED numerics (hrw_mixed.cuh, stage1d_mixed.cu) --------------------------------------
+enum MixedStage : int {
+  MX_E1 = 0,    // dout = d1 = dt L(u)
+  MX_RK1 = 1,   // uout = u + dt L(u)
+  MX_RK2B = 2,  // uout = u + (d1 + dt L(u + d1)) / 2
+  MX_RK3B = 3,  // dout = d2 = (d1 + dt L(u + d1)) / 4
+  MX_RK3C = 4   // uout = u + 2/3 (d2 + dt L(u + d2))
+};
+
+struct MixedArgs {
+  const double* u;       // u^n (FP64)
+  const float2* dv;      // stage increment of the stencil input (u + dv), float pairs; or null
+  float2* dout;          // increment output (MX_E1, MX_RK3B)
+  double* uout;          // new state (MX_RK1, MX_RK2B, MX_RK3C); never u itself
+  const unsigned* scale; // high word of max|u| over the line (launch_mixed_scale)
+  double eps, dt;        // the FP64 path's scalars
+  LineArgs L;            // the line as the FAST kernels see it
+  // the FP32 path's scalars (mixed_fill)
+  float epsf, inv_eps, alpha_f;
+  float c_h, c_l;        // dt / (4 dx) as a pair: dt L = -c (4 dF)
+  float g_h, g_l;        // linear flux: the velocity g = a as a pair
+  float two3_h, two3_l;  // 2/3 as a pair
+};
+
+// Whether the MIXED kernel covers a line: k = 2 or 3, Lax-Friedrichs, uniform grid, Burgers or
+// linear advection at constant speed.  Other lines run the FAST kernels.
+bool mixed_supported(const LineArgs& L, int k);
+// The FP32 scalars of a from its line, eps and dt.
+void mixed_fill(MixedArgs& a, double eps, double dt);
+cudaError_t launch_stage1d_mixed(const MixedArgs& a, int k, int stage, cudaStream_t s);
+// *word = high word of max |u_i| (reset first; asynchronous on s).
+cudaError_t launch_mixed_scale(const double* u, int64_t n, unsigned* word, cudaStream_t s);
+// Test hooks: every warp through the FP64 path (enable = 0), and the count of warps away from
+// the line ends that took it (optionally reset).
+cudaError_t mixed_set_soft(int enable);
+cudaError_t mixed_hard_warps(unsigned long long* count, bool reset);
+
 cudaError_t launch_stage1d_f32c(const F32CArgs& a, int k, int stage, cudaStream_t s);
 cudaError_t launch_stage2d_f32c(const F32CArgs& a, int k, int stage, cudaStream_t s);
 // Poll limit of the 2D stage kernels' first wait for their TMA tile copies (both the FP64 and

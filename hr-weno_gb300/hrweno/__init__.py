@@ -10,7 +10,7 @@ from ._abi import (HRW_BC_COPY, HRW_BC_ZERO, HRW_BC_ZERO_INFLOW, HRW_EINVAL, HRW
                    HRW_ECUDA, HRW_ESTATE, HRW_ETIMEOUT, HRW_F32, HRW_F32C, HRW_F64,
                    HRW_FLUX_GODUNOV, HRW_FLUX_LAX_FRIEDRICHS, HRW_FN_BURGERS, HRW_FN_BURGERS_LINEAR,
                    HRW_FN_LINEAR, HRW_MEM_DEVICE, HRW_MEM_HOST, HRW_NUMERICS_FAST,
-                   HRW_NUMERICS_STRICT, HRW_OK, HRW_PROBLEM_FV1D, HRW_PROBLEM_FV2D,
+                   HRW_NUMERICS_MIXED, HRW_NUMERICS_STRICT, HRW_OK, HRW_PROBLEM_FV1D, HRW_PROBLEM_FV2D,
                    HRW_PROBLEM_LINEAR_ODE, HrwError, lib)
 from .adjoint import adjoint  # noqa: F401
 from .batch import batch  # noqa: F401

@@ -18,7 +18,7 @@ HRW_PROBLEM_FV1D, HRW_PROBLEM_FV2D, HRW_PROBLEM_LINEAR_ODE = 1, 2, 3
 HRW_FLUX_LAX_FRIEDRICHS, HRW_FLUX_GODUNOV = 0, 1
 HRW_FN_BURGERS, HRW_FN_LINEAR, HRW_FN_BURGERS_LINEAR = 0, 1, 2
 HRW_BC_COPY, HRW_BC_ZERO, HRW_BC_ZERO_INFLOW = 0, 1, 2
-HRW_NUMERICS_FAST, HRW_NUMERICS_STRICT = 0, 1
+HRW_NUMERICS_FAST, HRW_NUMERICS_STRICT, HRW_NUMERICS_MIXED = 0, 1, 2
 
 
 class HrwProblem(C.Structure):

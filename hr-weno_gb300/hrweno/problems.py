@@ -18,7 +18,8 @@ _FLUX = {"lax_friedrichs": A.HRW_FLUX_LAX_FRIEDRICHS, "godunov": A.HRW_FLUX_GODU
 # flux functions f(u, x): "burgers" u^2/2, "linear" (a + b x) u, "burgers_linear" u^2/2 + (a + b x) u
 _FN = {"burgers": A.HRW_FN_BURGERS, "linear": A.HRW_FN_LINEAR, "burgers_linear": A.HRW_FN_BURGERS_LINEAR}
 _BC = {"copy": A.HRW_BC_COPY, "zero": A.HRW_BC_ZERO, "zero_inflow": A.HRW_BC_ZERO_INFLOW}
-_NUM = {"fast": A.HRW_NUMERICS_FAST, "strict": A.HRW_NUMERICS_STRICT}
+_NUM = {"fast": A.HRW_NUMERICS_FAST, "strict": A.HRW_NUMERICS_STRICT,
+        "mixed": A.HRW_NUMERICS_MIXED}
 
 
 @dataclass

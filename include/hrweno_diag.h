@@ -4,7 +4,8 @@
  * The stage kernels of the FP64 path are bound by the FP64 pipe, not by HBM; one call
  * measures that pipe on the current device so that a benchmark can report the kernel's
  * fraction of it next to its HBM roofline fraction.  The others expose internals to the tests:
- * the 2D kernels' bounded wait, and the FAST path's reciprocal.
+ * the 2D kernels' bounded wait, the FAST path's reciprocal, and the MIXED kernel's choice
+ * between its FP32 and FP64 paths.
  */
 #ifndef HRWENO_DIAG_H
 #define HRWENO_DIAG_H
@@ -27,6 +28,14 @@ int hrw_diag_set_tile_wait_limit(int polls);
  * Newton-Raphson step) and by IEEE division (__ddiv_rn(1, x)), for n device doubles x:
  * fast[i], exact[i].  Device pointers; synchronous. */
 int hrw_diag_rcp(const double* x, double* fast, double* exact, int n);
+
+/* MIXED numerics: enable = 0 sends every warp of the MIXED stage kernel through its FP64 path
+ * (the FAST arithmetic), 1 restores the default; the setting holds for the current device.
+ * Tests use it to check the FP64 path on its own. */
+int hrw_diag_mixed_soft(int enable);
+/* Warps of the MIXED stage kernel, away from the line ends, that took the FP64 path since the
+ * last reset (*count; reset != 0 clears the counter), on the current device. */
+int hrw_diag_mixed_hard_warps(unsigned long long* count, int reset);
 
 #ifdef __cplusplus
 }

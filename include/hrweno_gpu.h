@@ -74,8 +74,18 @@ enum { HRW_BC_COPY = 0, HRW_BC_ZERO = 1, HRW_BC_ZERO_INFLOW = 2 };
 /* FAST: the FP64 method with the fewest FP64 instructions (product-form WENO weights, one
  * reciprocal per cell, fused multiply-adds); agrees with the reference to rounding level.
  * STRICT: the reference's operation order with no fused multiply-add and true divisions;
- * bit-identical to a non-fused CPU build of the reference's formulas. */
-enum { HRW_NUMERICS_FAST = 0, HRW_NUMERICS_STRICT = 1 };
+ * bit-identical to a non-fused CPU build of the reference's formulas.
+ * MIXED: the FP64 state and stage combines with the right-hand side evaluated in difference
+ * form on the FP32 pipe: FP64 neighbour differences split into float pairs, the linear-weight
+ * part of the reconstruction in float-pair precision, the WENO weights' deviations from the
+ * linear weights in FP32, stage increments stored as float pairs.  A warp whose data would let
+ * the FP32 parts move dt L by more than 2^-54 max|u| per stage (steep or under-resolved
+ * data, the line ends, max|u| outside [2^-40, 2^60]) runs the FAST arithmetic instead; so does
+ * everything the MIXED kernel does not cover.  Covered: rktvd integrators of FV1D lines of at
+ * least 65536 uniform cells, k = 2 or 3, Lax-Friedrichs flux, Burgers or linear advection at
+ * constant speed (b = 0); eps >= 1e-8.  Agrees with the reference to the same 1e-12 (normwise
+ * relative) bar as FAST. */
+enum { HRW_NUMERICS_FAST = 0, HRW_NUMERICS_STRICT = 1, HRW_NUMERICS_MIXED = 2 };
 
 typedef struct hrw_problem {
   int32_t kind;       /* HRW_PROBLEM_* */

@@ -1,0 +1,66 @@
+"""The MIXED kernel's difference-form algebra (hr-weno_gb300/csrc/hrw_mixed.cuh,
+stage1d_mixed.cu), checked on the CPU through a numpy model of its FP32 path
+(tests/mixed_model.py) against the oracle evaluated in binary128 (the REAL128 build of the
+reference's formulas, src/hrweno_kinds.F90:13-14).
+
+On cells where the kernel's rounding-error bound admits the FP32 path, dt L agrees with the
+exact right-hand side to within that bound, and the bound is within the per-stage budget of
+2^-54 max|u|; every variant the kernel covers (k = 2, 3; Burgers, linear advection; the first
+stage and a stage with a float-pair increment) is checked.
+"""
+import numpy as np
+import pytest
+
+from mixed_model import mixed_dtl, split
+
+
+def large_line(n, k, fn):
+    from hrweno import Problem, workloads
+    prob, u0, dt = workloads.large_burgers(n, k=k, numerics="strict")
+    if fn == "linear":
+        prob = Problem(kind="fv1d", ncells=(n, 1), k=k, flux="lax_friedrichs", fn=("linear", "linear"),
+                       coef_a=(0.7, 0.0), coef_b=(0.0, 0.0), alpha=(1.0, 1.0), bc=("copy", "copy"),
+                       xmin=(-5.0, 0.0), xmax=(5.0, 1.0), numerics="strict")
+        dt = 0.4 * (10.0 / n)
+    return prob, u0, dt
+
+
+@pytest.mark.parametrize("stage", ["first", "increment"])
+@pytest.mark.parametrize("fn", ["burgers", "linear"])
+@pytest.mark.parametrize("k", [3, 2])
+def test_fp32_path_within_its_bound(orc, k, fn, stage):
+    n = 1 << 19
+    prob, u0, dt = large_line(n, k, fn)
+    g = 0.7 if fn == "linear" else 0.0
+    dx = 10.0 / n
+    dv = None
+    v = u0
+    if stage == "increment":
+        # the stage input u + d1 with d1 a float-pair increment whose sum with u is exact in FP64
+        d1 = (orc.rhs(prob, u0, prec=128) * dt).astype(np.float32)
+        v = u0 + d1.astype(np.float64)
+        dh, dl = split(v - u0)
+        exact = dh.astype(np.float64) + dl.astype(np.float64) == v - u0
+        v = np.where(exact, v, u0)
+        dh, dl = split(v - u0)
+        dv = (dh, dl)
+    ref = orc.rhs(prob, v, prec=128) * dt
+    cells, dtl, bound = mixed_dtl(u0, k, 1e-6, prob.alpha[0], dt, dx, fn=fn, g=g, dv=dv)
+    err = np.abs(dtl - ref[cells])
+    lim = 2.0 ** (np.floor(np.log2(np.max(np.abs(u0)))) - 54)
+    soft = bound <= lim
+    assert soft.mean() > 0.4  # much of a resolved line takes the FP32 path (more as n grows)
+    # the bound holds wherever the FP32 path is taken (1e-30: values flushed below float range)
+    assert np.all(err[soft] <= bound[soft] + 1e-30), float(np.max(err[soft] - bound[soft]))
+    assert float(err[soft].max()) <= lim
+    # and the FP32 path is far more accurate than the bound needs on this resolved line
+    assert float(err[soft].max()) <= lim / 4
+
+
+def test_split_is_the_fp64_value_to_48_bits():
+    rng = np.random.default_rng(3)
+    d = rng.standard_normal(100000) * np.exp2(rng.uniform(-70, 60, 100000))
+    h, lo = split(d)
+    recon = h.astype(np.float64) + lo.astype(np.float64)
+    assert np.all(np.abs(recon - d) <= 2.0 ** -48 * np.abs(d))
+    assert np.all(h == d.astype(np.float32))
