@@ -56,6 +56,27 @@ __device__ __forceinline__ F2 split(double d) {
   return r;
 }
 
+// The same split with h = d truncated to 24 significant bits, by integer operations alone
+// (the FP64-to-FP32 conversion of split() shares the narrow FP64 unit's issue slots):
+// h takes d's sign, exponent and top 23 stored mantissa bits; l = fl32 of the 29 bits below
+// them.  d = h + l to 2^-47 |d|; |d| < 2^-126 gives (0, 0); |d| < 2^-74 gives l = 0.  Valid for
+// |d| < 2^127 (callers keep |d| far below).
+__device__ __forceinline__ F2 split_t(double d) {
+  const unsigned hi = (unsigned)__double2hiint(d), lo = (unsigned)__double2loint(d);
+  const int E = (int)((hi >> 20) & 0x7FFu);
+  // bits 30..23 of the funnel shift are E's low 8 bits; for 897 <= E <= 1150 the float's
+  // exponent field E - 896 equals them with the top bit flipped
+  const unsigned f = __funnelshift_l(lo, hi, 3);
+  F2 r;
+  r.h = __uint_as_float(((f ^ 0x40000000u) & 0x7FFFFFFFu) | (hi & 0x80000000u));
+  const float scale = __int_as_float((E - 948) << 23);  // 2^(E - 1075), normal for E >= 949
+  float l = __uint2float_rn(lo & 0x1FFFFFFFu) * scale;
+  l = __uint_as_float(__float_as_uint(l) | (hi & 0x80000000u));
+  r.l = E >= 949 ? l : 0.f;
+  if (E < 897) r.h = 0.f;
+  return r;
+}
+
 // The double of a normal float (or zero) by integer operations (cvt.f64.f32 runs on the
 // narrow FP64 unit).  Subnormal floats give zero.
 __device__ __forceinline__ double widen(float f) {

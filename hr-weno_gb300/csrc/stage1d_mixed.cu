@@ -122,7 +122,7 @@ __device__ __noinline__ void fp64_pass(const MixedArgs& a, int64_t j0) {
 // The kernel.
 // ------------------------------------------------------------------------------------------------
 template <int K, int ST, bool LIN>
-__global__ void __launch_bounds__(NT) stage1d_mixed_kernel(MixedArgs a) {
+__global__ void __launch_bounds__(NT, 2) stage1d_mixed_kernel(MixedArgs a) {
   constexpr int ND = C + 2 * K - 1;  // window of differences d_{j0-K} .. d_{j0+C+K-2}
   constexpr int NH = 2 * K - 1;      // the warp's edge differences: K on the left, K-1 on the right
   const int lane = threadIdx.x & 31;
@@ -183,7 +183,7 @@ __global__ void __launch_bounds__(NT) stage1d_mixed_kernel(MixedArgs a) {
 #pragma unroll
     for (int c = 0; c < C; ++c) {
       const double hi = c + 1 < C ? u[c + 1] : un;
-      mx::F2 p = mx::split(hi - u[c]);
+      mx::F2 p = mx::split_t(hi - u[c]);
       if constexpr (reads_inc<ST>()) {
         const mx::F2 n = c + 1 < C ? dv[c + 1] : dvn;
         p = mx::add(p, {n.h - dv[c].h, n.l - dv[c].l});
@@ -195,7 +195,7 @@ __global__ void __launch_bounds__(NT) stage1d_mixed_kernel(MixedArgs a) {
     mx::F2 h = {0.f, 0.f};
     if (lane < NH) {
       const int64_t q = lane < K ? w0 - K + lane : w0 + WC + (lane - K);
-      h = mx::split(a.u[q + 1] - a.u[q]);
+      h = mx::split_t(a.u[q + 1] - a.u[q]);
       if constexpr (reads_inc<ST>()) {
         const mx::F2 x = ld2(a.dv, q), y = ld2(a.dv, q + 1);
         h = mx::add(h, {y.h - x.h, y.l - x.l});
@@ -278,7 +278,7 @@ __global__ void __launch_bounds__(NT) stage1d_mixed_kernel(MixedArgs a) {
       const float T = (Y[c + 1] - Y[c]) + Tn;
       // 4 dF = 2 V S + Q + 2 alpha T: Burgers V = v_j (Q = aR^2 + bR^2 - aL^2 - bL^2), linear V = g
       if constexpr (!LIN) {
-        const mx::F2 v = mx::split(u[c]);
+        const mx::F2 v = mx::split_t(u[c]);
         Vh = v.h;
         Vl = v.l;
         if constexpr (reads_inc<ST>()) Vl += dv[c].h + dv[c].l;
@@ -309,7 +309,8 @@ __global__ void __launch_bounds__(NT) stage1d_mixed_kernel(MixedArgs a) {
     const float eNL = fmaf(0x1p-18f * Mdd, dev, 0x1p-12f * Mdd * Mdd * (Md + Mdd) * a.inv_eps);
     const float eST = fmaf(0x1p-21f, Mdd, fmaf(0x1p-46f, Md, eNL));
     const float Vb = LIN ? fabsf(a.g_h) : Vmax * 1.001f;
-    float e4 = fmaf(2.f * Vb, eST, 2.f * a.alpha_f * eST);
+    // (the 2^-92 (V + alpha) floor covers differences below 2^-74, whose low words are dropped)
+    float e4 = fmaf(2.f * Vb, eST, fmaf(2.f * a.alpha_f, eST, 0x1p-92f * (Vb + a.alpha_f)));
     if constexpr (!LIN) e4 = fmaf(0x1p-20f * Md, 2.f * errmax, e4);
     const bool ok = a.c_h * e4 <= bound_lim;  // false for NaN and infinities
     soft = !__any_sync(FULL, !ok);

@@ -28,9 +28,16 @@ def fma(a, b, c):
 
 
 def split(d):
-    """FP64 d -> (h, l): h = fl32(d), l = fl32(d - h)"""
-    h = d.astype(f32)
-    lo = (d - h.astype(np.float64)).astype(f32)
+    """FP64 d -> (h, l) as the kernel's split_t: h = d truncated to 24 significant bits,
+    l = fl32(d - h); |d| < 2^-126 gives (0, 0) and |d| < 2^-74 gives l = 0"""
+    d = np.asarray(d, np.float64)
+    bits = d.view(np.uint64) & ~np.uint64(0x1FFFFFFF)
+    ht = bits.view(np.float64)
+    h = ht.astype(f32)
+    lo = (d - ht).astype(f32)
+    E = ((d.view(np.uint64) >> np.uint64(52)) & np.uint64(0x7FF)).astype(np.int64)
+    lo = np.where(E >= 949, lo, f32(0))
+    h = np.where(E >= 897, h, f32(0))
     return h, lo
 
 
@@ -167,7 +174,7 @@ def mixed_dtl(u, k, eps, alpha, dt, dx, fn="burgers", g=0.0, dv=None):
             * (Md.astype(np.float64) + Mdd) * inv_eps)
     eST = 2.0 ** -21 * Mdd + 2.0 ** -46 * Md + eNL
     Vb = np.abs(Vh.astype(np.float64)) * 1.001
-    e4 = 2.0 * Vb * eST + 2.0 * float(f32(alpha)) * eST
+    e4 = 2.0 * Vb * eST + 2.0 * float(f32(alpha)) * eST + 2.0 ** -92 * (Vb + float(f32(alpha)))
     if fn == "burgers":
         errmax = np.maximum(np.abs(aR), np.abs(bR)) + np.maximum(np.abs(aL), np.abs(bL))
         e4 = e4 + 2.0 ** -20 * Md * 2.0 * errmax
