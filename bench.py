@@ -9,11 +9,19 @@ boundaries, rktvd order 3, CFL 0.4.  One step is one RK3 time step over the whol
 (three fused stage kernels); the metric is cell-updates per second, one cell-update being
 one cell advanced one full RK3 step.
 
+The headline line (printed last) is the MIXED numerics mode: the FP64 state and stage combines
+with the right-hand side evaluated in difference form on the FP32 pipe, parity-tested against
+the oracle at the same 1e-12 bar as the plain FAST FP64 path.  Every other form of the metric
+is printed first, one short JSON line each ("form": name; values in cell-updates/s unless a
+key says otherwise; hbm_frac from the algorithmic bytes per cell-update of the form):
+the plain FP64 path and the compensated FP32 form of the same line, the line with WENO3, the
+2D grids, the batched lines, the adjoint and the reference's own 500-cell driver loop.
+
 `value` times K steps on device-resident data with CUDA events on the library's stream.
 `e2e` times K calls of the reference-facing integrate(u, t, tout, dt, itask=2) with u in
 pinned host memory: each call copies u to the device, takes one step and copies u back.
-`--impl reference` times the CPU restatement of the reference (oracle/, all host threads,
-bit-identical results for any thread count) on the same workload.
+`--impl reference` times the CPU restatement of the reference (oracle/, its -O3 build, all
+host threads) on the same workload.
 
 Under torchrun (N > 1) every rank integrates its own replica of the line (replicas only:
 the single-line path has no exchange step here); value = all ranks' cell-updates / the
@@ -44,17 +52,19 @@ NC = 1 << 24
 # stage 2 reads u, u1, writes u2 (24 B); stage 3 reads u, u2, writes u (24 B)
 BYTES_PER_CELL_UPDATE = 64
 LAUNCHES_PER_STEP = 3
-# compensated FP32: stage 1 reads hi, lo and writes d1 (12 B); stage 2 reads hi, lo, d1 and
-# writes d2 (16 B); stage 3 reads hi, lo, d2 and writes hi, lo (20 B)
-F32C_BYTES_PER_CELL_UPDATE = 48
+# compensated FP32, algorithmic bytes of a state u = hi + lo and one float per increment:
+# 40 B per RK3 cell-update (the lo word of u read and written in the last stage beside the
+# 32 B of a plain FP32 RK3 step).  The kernel moves 48 B: stage 1 reads hi, lo and writes d1
+# (12 B); stage 2 reads hi, lo, d1 and writes d2 (16 B); stage 3 reads hi, lo, d2 and writes
+# hi, lo (20 B).
+F32C_BYTES_PER_CELL_UPDATE = 40
+F32C_MOVED_BYTES_PER_CELL_UPDATE = 48
 L2_BYTES = 126 * 1024 * 1024
 
-# DRAM bytes per cell and stage launch of the FP64 stage kernel, measured by ncu
-# (dram__bytes_read.sum + dram__bytes_write.sum over the three RK3 stage launches of one
-# step of the 2^24-cell line, divided by cells x 3); profiles/stage1d_fp64_weno5_rk3.md.
-NCU_DRAM_BYTES_PER_CELL_LAUNCH = 943.8e6 / (3 * (1 << 24))
-# FP64 pipe utilisation of the same capture (sm__inst_executed_pipe_fp64, % of peak active)
-NCU_FP64_PIPE_PCT = 86.0
+# DRAM bytes per cell and stage launch of the MIXED stage kernel, measured by ncu on the
+# 2^24-cell line (dram__bytes_read.sum + dram__bytes_write.sum of the three RK3 stage launches
+# of one step, divided by cells x 3); profiles/stage1d_mixed_weno5_rk3.md.  None until captured.
+NCU_DRAM_BYTES_PER_CELL_LAUNCH = None
 
 
 def peaks() -> dict:
@@ -164,6 +174,7 @@ class Dist:
 def cpu_rate(u0: np.ndarray, prob, dt: float, steps: int, threads: int):
     """cell-updates/s of the oracle over `steps` RK3 steps of the full line."""
     from oracle import oracle
+    oracle.select_build("baseline")
     used = oracle.set_threads(threads)
     ode = oracle.ODE(prob, u0.size, 0, 3)
     u = u0.copy()
@@ -197,7 +208,8 @@ def run_reference(args) -> None:
     el = time.perf_counter() - t0
     v = n * args.steps / el
     sample = (f"{args.steps} RK3 steps, each one step over {n} cells"
-              + (" (a strided sub-line of the 2^24-cell line)" if n != NC else " (the full line)"))
+              + (" (a strided sub-line of the 2^24-cell line)" if n != NC else " (the full line)")
+              + ", oracle restatement -O3")
     line = {
         "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True,
@@ -216,64 +228,22 @@ def config_dict() -> dict:
     name = "2^24" if NC == 1 << 24 else str(NC)
     return {"workload": f"burgers1d_{name}_weno5_lf_rk3", "cells": NC, "k": 3, "eps": 1e-6,
             "flux": "lax_friedrichs", "alpha": "max|u0|", "bc": "copy", "cfl": 0.4,
-            "integrator": "rktvd order 3", "numerics": "fast",
-            "l2": (f"inputs larger than L2: u, u1, u2 are {mib} MiB each ({3 * mib} MiB working set)"
+            "integrator": "rktvd order 3",
+            "numerics": "mixed: FP64 state; RHS in float-pair difference form on the FP32 pipe",
+            "l2": (f"inputs larger than L2: u, d1, d2 are {mib} MiB each ({3 * mib} MiB working set)"
                    if 3 * NC * 8 > 126 << 20 else
-                   f"L2-resident: u, u1, u2 are {NC * 8 >> 10} KiB each (a reduced line, not the benchmark workload)")}
+                   f"L2-resident: u, d1, d2 are {NC * 8 >> 10} KiB each (a reduced line, not the benchmark workload)")}
 
 
 # ------------------------------------------------------------------------------------------
 # GPU arm
 # ------------------------------------------------------------------------------------------
-def run_k2(args, dist: Dist) -> dict | None:
-    """The same 2^24-cell line with WENO3 (k = 2): FP64 and compensated FP32, and the FP32
-    form's error against FP64 after the same steps."""
+def time_line(prob, u0, dt, dtype, args, dist, stream, clk=None):
+    """(seconds for K RK3 steps after W untimed ones, the state, the handle) on device memory"""
     import torch
 
     import hrweno
-    from hrweno import workloads
-
-    dev = dist.local if dist.world > 1 else 0
-    torch.cuda.set_device(dev)
-    prob, u0, dt = workloads.large_burgers(NC, k=2)
-    stream = torch.cuda.Stream()
-    res = {}
-    for dtype in ("f64", "f32c"):
-        ode = hrweno.rktvd(prob, NC, 3, dtype=dtype)
-        ode.set_stream(stream.cuda_stream)
-        u = torch.from_numpy(u0).cuda()
-        t = ode.integrate(u, 0.0, (args.warmup - 0.5) * dt, dt)
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        dist.barrier()
-        e0.record(stream)
-        t = ode.integrate(u, t, t + (args.steps - 0.5) * dt, dt)
-        e1.record(stream)
-        torch.cuda.synchronize()
-        el = dist.max(e0.elapsed_time(e1) * 1e-3)
-        res[dtype] = (dist.world * NC * args.steps / el, 1e3 * el / args.steps, u)
-    a, b = res["f64"][2], res["f32c"][2]
-    return {"k": 2, "value": res["f64"][0], "unit": UNIT, "ms_per_step": res["f64"][1],
-            "f32c": {"value": res["f32c"][0], "ms_per_step": res["f32c"][1],
-                     "speedup_vs_f64": res["f32c"][0] / res["f64"][0],
-                     "rel_l1_vs_f64": float((a - b).abs().sum() / a.abs().sum()),
-                     "rel_linf_vs_f64": float((a - b).abs().max() / a.abs().max()),
-                     "steps_compared": args.warmup + args.steps}}
-
-
-def run_ours(args, dist: Dist) -> dict | None:
-    import torch
-
-    import hrweno
-    from hrweno import workloads
-
-    dev = dist.local if dist.world > 1 else 0
-    torch.cuda.set_device(dev)
-    prob, u0, dt = workloads.large_burgers(NC, k=3)
-    stream = torch.cuda.Stream()
-
-    # ---- device-resident K steps ---------------------------------------------------------
-    ode = hrweno.rktvd(prob, NC, 3)
+    ode = hrweno.rktvd(prob, u0.size, 3, dtype=dtype)
     ode.set_stream(stream.cuda_stream)
     u = torch.from_numpy(u0).cuda()
     t = ode.integrate(u, 0.0, (args.warmup - 0.5) * dt, dt)
@@ -282,44 +252,75 @@ def run_ours(args, dist: Dist) -> dict | None:
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     dist.barrier()
     torch.cuda.synchronize()
-    with ClockSampler(dev) as clk:
-        e0.record(stream)
-        t = ode.integrate(u, t, t + (args.steps - 0.5) * dt, dt)
-        e1.record(stream)
-        torch.cuda.synchronize()
+    if clk is not None:
+        clk.__enter__()
+    e0.record(stream)
+    t = ode.integrate(u, t, t + (args.steps - 0.5) * dt, dt)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    if clk is not None:
+        clk.__exit__(None, None, None)
     dist.barrier()
-    steps_done = ode.nsteps - n0
-    assert steps_done == args.steps, (steps_done, args.steps)
-    el = dist.max(e0.elapsed_time(e1) * 1e-3)
-    value = dist.world * NC * args.steps / el
+    assert ode.nsteps - n0 == args.steps, (ode.nsteps - n0, args.steps)
     assert bool(torch.isfinite(u).all())
+    return dist.max(e0.elapsed_time(e1) * 1e-3), u, ode
 
-    # ---- compensated FP32 form on the same line: same steps, error against FP64 ----------
-    forms = {}
-    if "f32c" in args.forms:
-        ode32 = hrweno.rktvd(prob, NC, 3, dtype="f32c")
-        ode32.set_stream(stream.cuda_stream)
-        u32 = torch.from_numpy(u0).cuda()
-        t32 = ode32.integrate(u32, 0.0, (args.warmup - 0.5) * dt, dt)
-        torch.cuda.synchronize()
-        dist.barrier()
-        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        f0.record(stream)
-        t32 = ode32.integrate(u32, t32, t32 + (args.steps - 0.5) * dt, dt)
-        f1.record(stream)
-        torch.cuda.synchronize()
-        el32 = dist.max(f0.elapsed_time(f1) * 1e-3)
-        diff = (u32 - u).abs()
-        v32 = dist.world * NC * args.steps / el32
-        forms["f32c"] = {
-            "value": v32, "unit": UNIT, "ms_per_step": 1e3 * el32 / args.steps,
-            "speedup_vs_f64": v32 / value, "bytes_per_cell_update": F32C_BYTES_PER_CELL_UPDATE,
-            "hbm_frac": F32C_BYTES_PER_CELL_UPDATE * v32 / dist.world / 1e9 / peaks()["hbm_gbs"],
-            "rel_l1_vs_f64": float(diff.sum() / u.abs().sum()),
-            "rel_linf_vs_f64": float(diff.max() / u.abs().max()),
-            "steps_compared": args.warmup + args.steps,
-        }
-        del ode32, u32, diff
+
+def hbm(bytes_per_cell_update: float, value: float, dist) -> float:
+    return bytes_per_cell_update * value / dist.world / 1e9 / peaks()["hbm_gbs"]
+
+
+def run_line_forms(args, dist: Dist, k: int, u_ref=None) -> list:
+    """Short lines for the plain FP64 (FAST), MIXED (k = 2 only; k = 3 is the headline) and
+    compensated FP32 forms of the 2^24-cell line with WENO(2k-1)."""
+    import torch
+
+    from hrweno import workloads
+
+    stream = torch.cuda.Stream()
+    out = []
+    res = {}
+    for num, dtype in (("fast", "f64"), ("mixed", "f64"), ("fast", "f32c")):
+        if k == 3 and num == "mixed":
+            continue
+        prob, u0, dt = workloads.large_burgers(NC, k=k, numerics=num)
+        el, u, _ = time_line(prob, u0, dt, dtype, args, dist, stream)
+        v = dist.world * NC * args.steps / el
+        res[(num, dtype)] = u
+        name = f"1d_k{k}_{'f32c' if dtype == 'f32c' else num}"
+        line = {"form": name, "value": v, "ms": 1e3 * el / args.steps}
+        if dtype == "f32c":
+            line["hbm_frac"] = hbm(F32C_BYTES_PER_CELL_UPDATE, v, dist)
+            line["moved_B"] = F32C_MOVED_BYTES_PER_CELL_UPDATE
+        else:
+            line["hbm_frac"] = hbm(BYTES_PER_CELL_UPDATE, v, dist)
+        out.append(line)
+    base = u_ref if u_ref is not None else res[("mixed", "f64")]
+    for line, key in zip(out, [kk for kk in (("fast", "f64"), ("mixed", "f64"), ("fast", "f32c"))
+                               if kk in res]):
+        if key != ("mixed", "f64") or u_ref is not None:
+            d = (res[key] - base).abs()
+            line["l1_vs_mixed"] = float(d.sum() / base.abs().sum())
+    return out
+
+
+def run_ours(args, dist: Dist):
+    """(headline line, form lines): the MIXED form of the 2^24-cell WENO5 line."""
+    import torch
+
+    import hrweno
+    from hrweno import workloads
+
+    dev = dist.local if dist.world > 1 else 0
+    torch.cuda.set_device(dev)
+    prob, u0, dt = workloads.large_burgers(NC, k=3, numerics="mixed")
+    stream = torch.cuda.Stream()
+
+    # ---- device-resident K steps ---------------------------------------------------------
+    clk = ClockSampler(dev)
+    el, u, ode = time_line(prob, u0, dt, "f64", args, dist, stream, clk=clk)
+    value = dist.world * NC * args.steps / el
+    forms = run_line_forms(args, dist, 3, u_ref=u) if "line" in args.forms else []
 
     # ---- e2e: reference-facing call on pinned host memory, one step per call -------------
     ode2 = hrweno.rktvd(prob, NC, 3)
@@ -340,38 +341,28 @@ def run_ours(args, dist: Dist) -> dict | None:
            "h2d_bytes_per_step": 8 * NC, "d2h_bytes_per_step": 8 * NC}
 
     if dist.rank != 0:
-        return None
+        return None, forms
 
     pk = peaks()
-    launch_s = el / (args.steps * LAUNCHES_PER_STEP)
+    launches = args.steps * LAUNCHES_PER_STEP
+    launch_s = el / launches
     bytes_per_launch = BYTES_PER_CELL_UPDATE * NC / LAUNCHES_PER_STEP
     achieved = bytes_per_launch / launch_s / 1e9
     traffic = (None if NCU_DRAM_BYTES_PER_CELL_LAUNCH is None
                else NCU_DRAM_BYTES_PER_CELL_LAUNCH * NC)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
                 "frac": achieved / pk["hbm_gbs"], "traffic": traffic,
-                "peak_src": f"{pk['src']} (MEASURED_PEAKS.json hbm_gbs)" if pk["src"] == "measured"
+                "peak_src": "measured (MEASURED_PEAKS.json hbm_gbs)" if pk["src"] == "measured"
                 else "fallback 6.8 TB/s"}
-    # the FP64 pipe bounds this kernel on GB300 (FP64 is 1/64 of the FP32 rate)
-    dfma = ffma = None
-    try:
-        import ctypes as C
-        d, f = C.c_double(), C.c_double()
-        L = hrweno.lib()
-        L.hrw_diag_fma_rates.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_double)]
-        if L.hrw_diag_fma_rates(C.byref(d), C.byref(f)) == 0:
-            dfma, ffma = d.value, f.value
-    except Exception:  # diagnostics only
-        pass
 
-    # ---- CPU baseline: the oracle, 1 core, bounded sample ----------------------------------
+    # ---- CPU baseline: the oracle's -O3 build, 1 core, bounded sample ---------------------
     cpu = None
     if not args.no_cpu:
         steps = 3
         v, el_cpu, used = cpu_rate(u0, prob, dt, steps, 1)
         cpu = {"value": v, "unit": UNIT, "cores": used, "kind": "port",
-               "sample": f"{steps} RK3 steps of the full 2^24-cell line ({el_cpu:.1f} s), "
-                         f"oracle restatement, -O2, 1 thread; host has {os.cpu_count()} cores"}
+               "sample": f"{steps} RK3 steps of the full 2^24-cell line ({el_cpu:.1f} s), oracle "
+                         f"restatement -O3, 1 thread; host has {os.cpu_count()} cores"}
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world,
@@ -380,15 +371,12 @@ def run_ours(args, dist: Dist) -> dict | None:
         "data": "synthetic: seeded 8-Gaussian u0 (numpy default_rng(1))",
         "config": config_dict(),
         "roofline": roofline,
-        "fp64_pipe": {"bound": "fp64", "ncu_pct_of_peak": NCU_FP64_PIPE_PCT,
-                      "dfma_per_s_measured": dfma, "ffma_per_s_measured": ffma},
         "cpu_baseline": cpu,
         "e2e": e2e,
-        "forms": forms,
-        "gpu_launches": steps_done * LAUNCHES_PER_STEP,
+        "gpu_launches": launches + 1,  # 3 stage kernels per step and one max|u| reduction
         "clocks": clk.summary(),
     }
-    return line
+    return line, forms
 
 
 # ------------------------------------------------------------------------------------------
@@ -443,7 +431,7 @@ def run_pbe2d(args, dist: Dist) -> dict | None:
     value = dist.world * cells * args.steps / el
     # compensated FP32 on the same grid and steps, error against the FP64 result
     forms = {}
-    if "f32c" in args.forms:
+    if "line" in args.forms or "pbe2d" in args.forms:
         ode32 = hrweno.mstvd(prob, cells, dtype="f32c")
         ode32.set_stream(stream.cuda_stream)
         u32 = torch.from_numpy(n0).cuda()
@@ -456,9 +444,12 @@ def run_pbe2d(args, dist: Dist) -> dict | None:
         el32 = dist.max(e0.elapsed_time(e1) * 1e-3)
         diff = (u32 - u).abs()
         v32 = dist.world * cells * args.steps / el32
+        # algorithmic bytes 28 B per multistep cell-update (the lo word of u read and written
+        # beside the 20 B of plain FP32); the kernel moves 32 B (L(u^{n-4}) is a plain float)
         forms["f32c"] = {"value": v32, "unit": UNIT, "ms_per_step": 1e3 * el32 / args.steps,
-                         "speedup_vs_f64": v32 / value, "bytes_per_cell_update": 32,
-                         "hbm_frac": 32 * v32 / dist.world / 1e9 / peaks()["hbm_gbs"],
+                         "speedup_vs_f64": v32 / value, "bytes_per_cell_update": 28,
+                         "moved_bytes_per_cell_update": 32,
+                         "hbm_frac": 28 * v32 / dist.world / 1e9 / peaks()["hbm_gbs"],
                          "rel_l1_vs_f64": float(diff.sum() / u.abs().sum()),
                          "rel_linf_vs_f64": float(diff.max() / u.abs().max())}
         del ode32, u32, diff
@@ -493,6 +484,7 @@ def run_pbe2d(args, dist: Dist) -> dict | None:
     cpu = None
     if not args.no_cpu:
         from oracle import oracle
+        oracle.select_build("baseline")
         m = 1024  # bounded sample: the 1024^2 grid, 3 multistep steps after the start
         p1, v1, dt1 = workloads.pbe_config(m, m)
         used = oracle.set_threads(1)
@@ -799,6 +791,7 @@ def run_config1(args, dist: Dist) -> dict | None:
     cpu = None
     if not args.no_cpu:
         from oracle import oracle
+        oracle.select_build("baseline")
         used = oracle.set_threads(1)
         o = oracle.ODE(prob, 500, 0, 3)
         u = u0.copy()
@@ -829,6 +822,40 @@ def run_config1(args, dist: Dist) -> dict | None:
     return line
 
 
+def form_lines(name: str, d: dict) -> list:
+    """Short JSON lines of a workload's result dict (its own line and its nested forms)."""
+    out = []
+    if name.startswith("pbe2d"):
+        out.append({"form": f"{name}_fast", "value": d["value"], "ms": d["ms_per_step"],
+                    "hbm_frac": d["roofline"]["frac"] if "roofline" in d else None})
+        f = d["forms"].get("f32c")
+        if f:
+            out.append({"form": f"{name}_f32c", "value": f["value"], "ms": f["ms_per_step"],
+                        "hbm_frac": f["hbm_frac"], "moved_B": f["moved_bytes_per_cell_update"],
+                        "l1_vs_fast": f["rel_l1_vs_f64"]})
+    elif name == "batched":
+        out.append({"form": "batched_4096_fast", "value": d["value"], "ms": d["ms_per_step"],
+                    "cells": d["config"]["cells"],
+                    "x_plain_per_problem": d["plain_per_problem"]["speedup_batched"]})
+        f = d["forms"]["f32c"]
+        out.append({"form": "batched_4096_f32c", "value": f["value"], "ms": f["ms_per_step"],
+                    "x_fast_batched": f["speedup_vs_f64_batched"], "l1_vs_fast": f["rel_l1_vs_f64"]})
+    elif name == "adjoint":
+        a = d["adjoint"]
+        out.append({"form": "adjoint_2^20_2000steps", "grad_ms": a["gradient_ms"],
+                    "fwd_ms": a["forward_ms"], "cost_vs_fwd": a["cost_vs_forward"],
+                    "fd_dirs": a["fd_directions"], "fd_max_rel": max(a["fd_max_rel_err_smooth"] or 0,
+                                                                     a["fd_max_rel_err_rough"] or 0),
+                    "batch256x4096_cost_vs_fwd": a["batch"]["cost_vs_forward"]})
+    elif name == "config1":
+        ms = d["driver_loop_ms"]
+        out.append({"form": "config1_500x1201", "ms_graphs": ms["device_graphs"],
+                    "ms_host_arrays": ms["host_graphs"],
+                    "ms_cpu_1core": (500 * 1201 / d["cpu_baseline"]["value"] * 1e3
+                                     if d.get("cpu_baseline") else None)})
+    return out
+
+
 def main() -> None:
     global NC
     ap = argparse.ArgumentParser()
@@ -839,11 +866,11 @@ def main() -> None:
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
-    ap.add_argument("--forms", default="f32c,k2,pbe2d,batched,adjoint,config1",
-                    help="comma-separated forms reported beside the workload's own line "
-                         "(f32c: the compensated FP32 form of the same workload; k2: the line "
+    ap.add_argument("--forms", default="line,k2,pbe2d,batched,adjoint,config1",
+                    help="comma-separated forms printed before the headline line (line: the "
+                         "plain FP64 and compensated FP32 forms of the same line; k2: the line "
                          "with WENO3; pbe2d: the 4096^2 and 1024^2 grids; the others: their "
-                         "workloads, run after the default burgers1d line)")
+                         "workloads)")
     ap.add_argument("--no-forms", action="store_true", help="same as --forms ''")
     ap.add_argument("--workload", default="burgers1d", choices=["burgers1d", "pbe2d", "batched", "adjoint", "config1"],
                     help="burgers1d (default): the 2^24-cell line; pbe2d: the 2D PBE grid")
@@ -874,46 +901,46 @@ def main() -> None:
                 "config1": run_config1}
         if args.workload != "burgers1d":
             line = runs[args.workload](args, dist)
-        else:
-            line = run_ours(args, dist)
-            # the other forms of the metric, each on its own workload, summarised
-            sub = argparse.Namespace(**vars(args))
-            sub.steps, sub.no_cpu = min(args.steps, 100), True
-            forms = {}
-            if "k2" in args.forms:
-                k2 = run_k2(sub, dist)
-                if k2 is not None:
-                    forms["weno3_k2"] = k2
-            if "pbe2d" in args.forms:
-                pb = run_pbe2d(sub, dist)
+            if line is not None and dist.rank == 0:
+                print(json.dumps(line), flush=True)
+            return
+        line, forms = run_ours(args, dist)
+        # the other forms of the metric, each on its own workload, one short line each
+        sub = argparse.Namespace(**vars(args))
+        sub.steps, sub.no_cpu = min(args.steps, 100), True
+        if "k2" in args.forms:
+            forms += run_line_forms(sub, dist, 2)
+        if "pbe2d" in args.forms:
+            for n in (PBE_N, 1024):
+                sp = argparse.Namespace(**vars(sub))
+                sp.pbe_n = n
+                pb = run_pbe2d(sp, dist)
                 if pb is not None:
-                    forms["pbe2d_4096"] = {k: pb[k] for k in ("value", "ms_per_step", "roofline", "forms")}
-                sub1024 = argparse.Namespace(**vars(sub))
-                sub1024.pbe_n = 1024
-                p1 = run_pbe2d(sub1024, dist)
-                if p1 is not None:
-                    forms["pbe2d_1024"] = {k: p1[k] for k in ("value", "ms_per_step", "forms")}
-                    forms["pbe2d_1024"]["l2"] = p1["config"]["l2"]
-            if "batched" in args.forms:
-                sub.steps = min(args.steps, 20)
-                bt = run_batched(sub, dist)
-                if bt is not None:
-                    forms["batched_4096_lines"] = {k: bt[k] for k in ("value", "ms_per_step", "config",
-                                                                     "plain_per_problem", "forms")}
-            if "adjoint" in args.forms:
-                sub.steps, sub.fd_directions = 1, 2
-                ad = run_adjoint(sub, dist)
-                if ad is not None:
-                    forms["adjoint_2^20"] = ad["adjoint"]
-            if "config1" in args.forms:
-                sub.steps = 3
-                c1 = run_config1(sub, dist)
-                if c1 is not None:
-                    forms["config1_500"] = {k: c1[k] for k in ("value", "driver_loop_ms")}
+                    forms += form_lines(f"pbe2d_{n}", pb)
+        if "batched" in args.forms:
+            sb = argparse.Namespace(**vars(sub))
+            sb.steps = min(args.steps, 20)
+            bt = run_batched(sb, dist)
+            if bt is not None:
+                forms += form_lines("batched", bt)
+        if "adjoint" in args.forms:
+            sa = argparse.Namespace(**vars(sub))
+            sa.steps, sa.fd_directions = 1, 2
+            ad = run_adjoint(sa, dist)
+            if ad is not None:
+                forms += form_lines("adjoint", ad)
+        if "config1" in args.forms:
+            sc = argparse.Namespace(**vars(sub))
+            sc.steps, sc.no_cpu = 3, args.no_cpu
+            c1 = run_config1(sc, dist)
+            if c1 is not None:
+                forms += form_lines("config1", c1)
+        if dist.rank == 0:
+            for f in forms:
+                print(json.dumps(f, separators=(",", ":")), flush=True)
             if line is not None:
-                line["forms"].update(forms)
-        if line is not None and dist.rank == 0:
-            print(json.dumps(line), flush=True)
+                line["forms"] = [f["form"] for f in forms]
+                print(json.dumps(line), flush=True)
     finally:
         dist.close()
 

@@ -15,7 +15,7 @@
 //   MX_RK3C  uout = u + 2/3 (d2 + dt L(u + d2))                   (rktvd :167)
 // uout is never the array u itself: other warps read u as their stencil while a stage runs.
 //
-// Layout: a warp owns 256 consecutive cells, 8 per lane, and keeps each lane's stencil window
+// Layout: a warp owns 128 consecutive cells, 4 per lane, and keeps each lane's stencil window
 // in registers (no shared memory).  The neighbour differences of the lane's own cells come from
 // its own loads; the window's edges come from the neighbouring lanes by shuffles, and five
 // lanes compute the warp's edge differences.  A warp whose cells touch a line end, or whose
@@ -35,9 +35,13 @@ namespace hrw {
 
 namespace {
 
-constexpr int C = 8;            // cells per lane
+// 4 cells per lane, 256-thread blocks, 3 blocks (24 warps) per SM at <= 80 registers: on the
+// 2^24-cell line 0.50 ms per RK3 step (k = 3), against 0.57 ms for 8 cells per lane at 2 blocks
+// per SM and 0.77 ms at one (the kernel is bound by instruction issue, so resident warps count)
+constexpr int C = 4;            // cells per lane
 constexpr int WC = 32 * C;      // cells per warp
 constexpr int NT = 256;         // threads per block
+constexpr int MINB = 3;         // resident blocks per SM
 constexpr unsigned FULL = 0xffffffffu;
 
 __device__ int g_mixed_soft = 1;                 // 0: every warp takes the FP64 path (tests)
@@ -122,7 +126,7 @@ __device__ __noinline__ void fp64_pass(const MixedArgs& a, int64_t j0) {
 // The kernel.
 // ------------------------------------------------------------------------------------------------
 template <int K, int ST, bool LIN>
-__global__ void __launch_bounds__(NT, 2) stage1d_mixed_kernel(MixedArgs a) {
+__global__ void __launch_bounds__(NT, MINB) stage1d_mixed_kernel(MixedArgs a) {
   constexpr int ND = C + 2 * K - 1;  // window of differences d_{j0-K} .. d_{j0+C+K-2}
   constexpr int NH = 2 * K - 1;      // the warp's edge differences: K on the left, K-1 on the right
   const int lane = threadIdx.x & 31;

@@ -69,7 +69,7 @@ def test_mixed_vs_oracle(hw, orc, k, fn, order):
     got = ug.cpu().numpy()
     assert tg == to and ode.nsteps == steps and ode.fevals == o.info()[0]
     e, p = nrel(got, uo), prel(got, uo)
-    warps = (n // 256) * steps * order
+    warps = (n // 128) * steps * order
     print(f"mixed k={k} {fn} order {order}: normwise {e:.3e}, pointwise {p:.3e}, "
           f"FP64-path warps {hw_ / warps:.3f}")
     assert e <= TOL
@@ -84,7 +84,7 @@ def test_mixed_takes_the_fp32_path_on_a_resolved_line(hw):
     ug = torch.from_numpy(u0).cuda()
     hard_warps()
     hw.rktvd(prob, n, 3).integrate(ug, 0.0, 0.5 * dt, dt)
-    frac = hard_warps() / (3 * (n // 256))
+    frac = hard_warps() / (3 * (n // 128))
     print(f"2^22 cells: FP64-path warps {frac:.4f}")
     assert frac < 0.05
 
