@@ -185,6 +185,22 @@ __device__ __forceinline__ Rec rec3(const float* d, const float* D, const float*
   return r;
 }
 
+// The linear-weight parts of rr and rl alone (FP32): k = 3 (24 d0 - 3 d1 + 11 dm - 2 dmm) / 60 and
+// (2 d1 - 11 d0 - 24 dm + 3 dmm) / 60 with d as in rec3; k = 2 d0/3 + dm/6 and -(d0/6 + dm/3) with
+// d as in rec2.  rec3 and rec2 add the nonlinear parts to these.
+template <int K>
+__device__ __forceinline__ void lin(const float* d, float& rr, float& rl) {
+  if constexpr (K == 3) {
+    const float dmm = d[0], dm = d[1], d0 = d[2], d1 = d[3];
+    rr = fmaf(24.f, d0, fmaf(-3.f, d1, fmaf(11.f, dm, -2.f * dmm))) * (1.f / 60.f);
+    rl = fmaf(2.f, d1, fmaf(-11.f, d0, fmaf(-24.f, dm, 3.f * dmm))) * (1.f / 60.f);
+  } else {
+    const float dm = d[0], d0 = d[1];
+    rr = fmaf(1.f / 3.f, d0, (1.f / 6.f) * dm);
+    rl = -fmaf(1.f / 6.f, d0, (1.f / 3.f) * dm);
+  }
+}
+
 // k = 2.  d[0..1] = d_{j-1}, d_j; D[0] = Dd_{j-1} = d_j - d_{j-1}.  Candidates minus v_j:
 // vrr0 - v = d0/2, vrr1 - v = dm/2, vlr0 - v = -d0/2, vlr1 - v = -dm/2 (src/hrweno_weno.f90:
 // 16-18); beta0 = d0^2, beta1 = dm^2 (:189-191); d = (2, 1)/3, d~ = (1, 2)/3.  With

@@ -42,6 +42,7 @@ constexpr int C = 4;            // cells per lane
 constexpr int WC = 32 * C;      // cells per warp
 constexpr int NT = 256;         // threads per block
 constexpr int MINB = 3;         // resident blocks per SM
+constexpr int ND_MAX = C + 4;   // differences of a lane's window for k <= 3
 constexpr unsigned FULL = 0xffffffffu;
 
 __device__ int g_mixed_soft = 1;                 // 0: every warp takes the FP64 path (tests)
@@ -123,6 +124,119 @@ __device__ __noinline__ void fp64_pass(const MixedArgs& a, int64_t j0) {
 }
 
 // ------------------------------------------------------------------------------------------------
+// The FP32 path of a lane's C cells: reconstructions in difference form, the interface sums, the
+// flux differences and dt L as float pairs (out).  NL = false: linear weights only (the caller has
+// shown that the weight deviations cannot move dt L by more than the budget); NL = true: the full
+// WENO weights.  Returns the NL pass's bound on the rounding error of dt L (mx_bound), 0 for the
+// linear pass.
+// ------------------------------------------------------------------------------------------------
+template <int K, int ST, bool LIN, bool NL>
+__device__ __forceinline__ float soft_cells(const MixedArgs& a, const double* u, const mx::F2* dv,
+                                            const mx::F2* dd, const float* d, const float* D,
+                                            float Md, float Mdd, mx::F2* out) {
+  // reconstructions of cells j0-1 .. j0+C (window position m = K-1 .. K+C; cell m uses
+  // d[m-K+1 .. m+K-2] and D[m-K+1 .. m-1])
+  float rr[C + 2], rl[C + 2], rrn[C + 2], rln[C + 2];
+  float dev = 0.f;
+  if constexpr (NL) {
+    float tA[ND_MAX];
+    if constexpr (K == 3) {
+#pragma unroll
+      for (int q = 0; q < C + 2 * K - 2; ++q) tA[q] = fmaf((13.f / 12.f) * D[q], D[q], a.epsf);
+    }
+#pragma unroll
+    for (int i = 0; i < C + 2; ++i) {
+      const int m = K - 1 + i;
+      mx::Rec R;
+      if constexpr (K == 3) R = mx::rec3(&d[m - 2], &D[m - 2], &tA[m - 2]);
+      else R = mx::rec2(&d[m - 1], &D[m - 1], a.epsf);
+      rr[i] = R.rr, rl[i] = R.rl, rrn[i] = R.rrn, rln[i] = R.rln;
+      dev = fmaxf(dev, R.dev);
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < C + 2; ++i) {
+      const int m = K - 1 + i;
+      mx::lin<K>(&d[m - K + 1], rr[i], rl[i]);
+      rrn[i] = rln[i] = 0.f;
+    }
+  }
+  // interface sums of the linear-weight states at interface i + 1/2 (window position m):
+  //   k = 3: X = -Dd_{i-2} + 6 Dd_{i-1} + 6 Dd_i - Dd_{i+1},  Y = Dd_{i+1} - 3 Dd_i + 3 Dd_{i-1} - Dd_{i-2}
+  //          vr_lin(i) + vl_lin(i+1) - 2 v_i = d_i - X/30,  vr_lin(i) - vl_lin(i+1) = -Y/30
+  //   k = 2: X = Dd_{i-1} + Dd_i, Y = Dd_i - Dd_{i-1}: d_i - X/6 and Y/6
+  // (X[] and Y[] below hold X/30 and the second expression, resp. X/6 and Y/6)
+  float X[C + 1], Y[C + 1];
+#pragma unroll
+  for (int i = 0; i < C + 1; ++i) {
+    const int m = K - 1 + i;
+    if constexpr (K == 3) {
+      X[i] = fmaf(6.f, D[m - 1] + D[m], -(D[m - 2] + D[m + 1])) * (1.f / 30.f);
+      Y[i] = -fmaf(-3.f, D[m] - D[m - 1], D[m + 1] - D[m - 2]) * (1.f / 30.f);
+    } else {
+      X[i] = (D[m - 1] + D[m]) * (1.f / 6.f);
+      Y[i] = (D[m] - D[m - 1]) * (1.f / 6.f);
+    }
+  }
+  float Vh = 0.f, Vl = 0.f, Vmax = 0.f;
+  if constexpr (LIN) Vh = a.g_h, Vl = a.g_l;
+  float errmax = 0.f;
+#pragma unroll
+  for (int c = 0; c < C; ++c) {
+    const int m = K + c;  // d[m] = d_j, d[m-1] = d_{j-1}
+    // offsets of the interface states from v_j (FP32)
+    const float aR = rr[c + 1], bR = d[m] + rl[c + 2];
+    const float aL = rr[c] - d[m - 1], bL = rl[c + 1];
+    // S = (aR + bR) - (aL + bL), T = (aR - bR) - (aL - bL): linear parts in pairs, the
+    // nonlinear parts (FP32) added to the low word
+    float sh, se;
+    mx::two_sum(dd[m].h, dd[m - 1].h, sh, se);
+    float sl = (se + (dd[m].l + dd[m - 1].l)) - (X[c + 1] - X[c]);
+    float T = Y[c + 1] - Y[c];
+    if constexpr (NL) {
+      sl += (rrn[c + 1] + rln[c + 2]) - (rrn[c] + rln[c + 1]);
+      T += (rrn[c + 1] - rln[c + 2]) - (rrn[c] - rln[c + 1]);
+    }
+    // 4 dF = 2 V S + Q + 2 alpha T: Burgers V = v_j (Q = aR^2 + bR^2 - aL^2 - bL^2), linear V = g
+    if constexpr (!LIN) {
+      const mx::F2 v = mx::split_t(u[c]);
+      Vh = v.h;
+      Vl = v.l;
+      if constexpr (reads_inc<ST>()) Vl += dv[c].h + dv[c].l;
+      Vmax = fmaxf(Vmax, fabsf(Vh));
+    }
+    const float p = 2.f * Vh * sh;
+    float pl = fmaf(2.f * Vh, sh, -p);
+    pl = fmaf(2.f * Vh, sl, pl);
+    pl = fmaf(2.f * Vl, sh, pl);
+    float q = 2.f * a.alpha_f * T;
+    if constexpr (!LIN) q += fmaf(aR, aR, bR * bR) - fmaf(aL, aL, bL * bL);
+    // dt L = -c (4 dF), c = dt / (4 dx) as a pair
+    const mx::F2 F = mx::renorm(p, pl + q);
+    const float th = a.c_h * F.h;
+    float tl = fmaf(a.c_h, F.h, -th);
+    tl = fmaf(a.c_h, F.l, fmaf(a.c_l, F.h, tl));
+    out[c] = mx::renorm(-th, -tl);
+    if constexpr (NL && !LIN)
+      errmax = fmaxf(errmax, fmaxf(fabsf(aR), fabsf(bR)) + fmaxf(fabsf(aL), fabsf(bL)));
+  }
+  if constexpr (!NL) return 0.f;
+  // mx_bound: |error of 4 dF| <= 2|V| eS + 2 alpha eT + eQ with
+  //   eS, eT <= 2^-21 Mdd (the interface sums) + 2^-46 Md (the difference pairs) + eNL
+  //   eNL = 2^-18 Mdd dev + 2^-12 Mdd^2 (Md + Mdd) / eps: the four reconstructions' weight
+  //         deviations, rounded (a few ulps of dev) and moved by the rounding of the indicator
+  //         differences (at most 2^-18 Mdd (Md + Mdd) each; |dw / dbeta| <= 2 / eps)
+  //   eQ <= 2^-20 Md (|aR| + |bR| + |aL| + |bL|)
+  // (the 2^-92 (V + alpha) floor covers differences below 2^-74, whose low words are dropped)
+  const float eNL = fmaf(0x1p-18f * Mdd, dev, 0x1p-12f * Mdd * Mdd * (Md + Mdd) * a.inv_eps);
+  const float eST = fmaf(0x1p-21f, Mdd, fmaf(0x1p-46f, Md, eNL));
+  const float Vb = LIN ? fabsf(a.g_h) : Vmax * 1.001f;
+  float e4 = fmaf(2.f * Vb, eST, fmaf(2.f * a.alpha_f, eST, 0x1p-92f * (Vb + a.alpha_f)));
+  if constexpr (!LIN) e4 = fmaf(0x1p-20f * Md, 2.f * errmax, e4);
+  return a.c_h * e4;  // NaN for NaN and infinite inputs: the caller's test fails
+}
+
+// ------------------------------------------------------------------------------------------------
 // The kernel.
 // ------------------------------------------------------------------------------------------------
 template <int K, int ST, bool LIN>
@@ -175,7 +289,6 @@ __global__ void __launch_bounds__(NT, MINB) stage1d_mixed_kernel(MixedArgs a) {
 
   // ---- float-pair differences of the stage values, v = u (+ dv) ----------------------------------
   mx::F2 dd[ND];
-  float Vmax = 0.f;
   if (soft) {
     double un = __shfl_down_sync(FULL, u[0], 1);
     mx::F2 dvn = {0.f, 0.f};
@@ -222,7 +335,7 @@ __global__ void __launch_bounds__(NT, MINB) stage1d_mixed_kernel(MixedArgs a) {
   // ---- the soft path: reconstruction, fluxes, dt L in difference form ------------------------------
   mx::F2 out[C];
   if (soft) {
-    float d[ND], D[ND - 1], tA[ND - 1];
+    float d[ND], D[ND - 1];
     float Md = 0.f, Mdd = 0.f;
 #pragma unroll
     for (int q = 0; q < ND; ++q) {
@@ -233,90 +346,35 @@ __global__ void __launch_bounds__(NT, MINB) stage1d_mixed_kernel(MixedArgs a) {
     for (int q = 0; q < ND - 1; ++q) {
       D[q] = (dd[q + 1].h - dd[q].h) + (dd[q + 1].l - dd[q].l);
       Mdd = fmaxf(Mdd, fabsf(D[q]));
-      if constexpr (K == 3) tA[q] = fmaf((13.f / 12.f) * D[q], D[q], a.epsf);
     }
-    // reconstructions of cells j0-1 .. j0+C (window position m = K-1 .. K+C; cell m uses
-    // d[m-K+1 .. m+K-2] and D[m-K+1 .. m-1])
-    mx::Rec R[C + 2];
-    float dev = 0.f;
+    // The weight deviations w_r - d_r are at most 2.01 |Dbeta| / eps while the indicator
+    // differences |Dbeta| <= Db = 4 Mdd (Md + 2.5 Mdd) stay below eps / 100, and their share of
+    // rr or rl at most 1.34 |Dbeta| Mdd / eps.  Where dropping them moves dt L by less than the
+    // budget in every lane of the warp (mx_bound with the dropped parts as an error term), the
+    // warp takes the linear-weight pass, which skips the weights altogether.
+    float Vb = LIN ? fabsf(a.g_h) : 0.f;
+    if constexpr (!LIN) {
 #pragma unroll
-    for (int i = 0; i < C + 2; ++i) {
-      const int m = K - 1 + i;
-      if constexpr (K == 3) R[i] = mx::rec3(&d[m - 2], &D[m - 2], &tA[m - 2]);
-      else R[i] = mx::rec2(&d[m - 1], &D[m - 1], a.epsf);
-      dev = fmaxf(dev, R[i].dev);
-    }
-    // interface sums of the linear-weight states at interface i + 1/2 (window position m):
-    //   k = 3: X = -Dd_{i-2} + 6 Dd_{i-1} + 6 Dd_i - Dd_{i+1},  Y = Dd_{i+1} - 3 Dd_i + 3 Dd_{i-1} - Dd_{i-2}
-    //          vr_lin(i) + vl_lin(i+1) - 2 v_i = d_i - X/30,  vr_lin(i) - vl_lin(i+1) = -Y/30
-    //   k = 2: X = Dd_{i-1} + Dd_i, Y = Dd_i - Dd_{i-1}: d_i - X/6 and Y/6
-    // (X[] and Y[] below hold X/30 and the second expression, resp. X/6 and Y/6)
-    float X[C + 1], Y[C + 1];
-#pragma unroll
-    for (int i = 0; i < C + 1; ++i) {
-      const int m = K - 1 + i;
-      if constexpr (K == 3) {
-        X[i] = fmaf(6.f, D[m - 1] + D[m], -(D[m - 2] + D[m + 1])) * (1.f / 30.f);
-        Y[i] = -fmaf(-3.f, D[m] - D[m - 1], D[m + 1] - D[m - 2]) * (1.f / 30.f);
-      } else {
-        X[i] = (D[m - 1] + D[m]) * (1.f / 6.f);
-        Y[i] = (D[m] - D[m - 1]) * (1.f / 6.f);
+      for (int c = 0; c < C; ++c) {
+        float x = fabsf((float)u[c]);
+        if constexpr (reads_inc<ST>()) x += fabsf(dv[c].h);
+        Vb = fmaxf(Vb, x);
       }
+      Vb *= 1.001f;
     }
-    float Vh = 0.f, Vl = 0.f;
-    if constexpr (LIN) Vh = a.g_h, Vl = a.g_l;
-    float errmax = 0.f;
-#pragma unroll
-    for (int c = 0; c < C; ++c) {
-      const int m = K + c;  // d[m] = d_j, d[m-1] = d_{j-1}
-      // offsets of the interface states from v_j (FP32)
-      const float aR = R[c + 1].rr, bR = d[m] + R[c + 2].rl;
-      const float aL = R[c].rr - d[m - 1], bL = R[c + 1].rl;
-      // S = (aR + bR) - (aL + bL), T = (aR - bR) - (aL - bL): linear parts in pairs, the
-      // nonlinear parts (FP32) added to the low word
-      const float Sn = (R[c + 1].rrn + R[c + 2].rln) - (R[c].rrn + R[c + 1].rln);
-      const float Tn = (R[c + 1].rrn - R[c + 2].rln) - (R[c].rrn - R[c + 1].rln);
-      float sh, se;
-      mx::two_sum(dd[m].h, dd[m - 1].h, sh, se);
-      const float sl = ((se + (dd[m].l + dd[m - 1].l)) - (X[c + 1] - X[c])) + Sn;
-      const float T = (Y[c + 1] - Y[c]) + Tn;
-      // 4 dF = 2 V S + Q + 2 alpha T: Burgers V = v_j (Q = aR^2 + bR^2 - aL^2 - bL^2), linear V = g
-      if constexpr (!LIN) {
-        const mx::F2 v = mx::split_t(u[c]);
-        Vh = v.h;
-        Vl = v.l;
-        if constexpr (reads_inc<ST>()) Vl += dv[c].h + dv[c].l;
-        Vmax = fmaxf(Vmax, fabsf(Vh));
-      }
-      const float p = 2.f * Vh * sh;
-      float pl = fmaf(2.f * Vh, sh, -p);
-      pl = fmaf(2.f * Vh, sl, pl);
-      pl = fmaf(2.f * Vl, sh, pl);
-      float q = 2.f * a.alpha_f * T;
-      if constexpr (!LIN) q += fmaf(aR, aR, bR * bR) - fmaf(aL, aL, bL * bL);
-      // dt L = -c (4 dF), c = dt / (4 dx) as a pair
-      const mx::F2 F = mx::renorm(p, pl + q);
-      const float th = a.c_h * F.h;
-      float tl = fmaf(a.c_h, F.h, -th);
-      tl = fmaf(a.c_h, F.l, fmaf(a.c_l, F.h, tl));
-      out[c] = mx::renorm(-th, -tl);
-      // rounding-error bound of this cell's 4 dF (FP32 parts): the single-precision interface
-      // sums X, Y (2^-21 max|Dd|), the weight deviations (mx_bound), the quadratic terms
-      if constexpr (!LIN) errmax = fmaxf(errmax, fmaxf(fabsf(aR), fabsf(bR)) + fmaxf(fabsf(aL), fabsf(bL)));
+    const float Db = 4.f * Mdd * fmaf(2.5f, Mdd, Md);
+    const float eSkip = 6.f * Db * Mdd * a.inv_eps;  // the four reconstructions' dropped parts
+    const float eL = fmaf(0x1p-21f, Mdd, fmaf(0x1p-46f, Md, eSkip));
+    float e4 = fmaf(2.f * Vb, eL, fmaf(2.f * a.alpha_f, eL, 0x1p-92f * (Vb + a.alpha_f)));
+    if constexpr (!LIN) e4 = fmaf(Md, fmaf(0x1p-17f, Md, 8.f * eSkip), e4);  // quadratic terms
+    const bool lin_ok = Db * a.inv_eps <= 0.01f && a.c_h * e4 <= bound_lim;
+    bool ok;
+    if (__all_sync(FULL, lin_ok)) {
+      soft_cells<K, ST, LIN, false>(a, u, dv, dd, d, D, Md, Mdd, out);
+      ok = true;
+    } else {
+      ok = soft_cells<K, ST, LIN, true>(a, u, dv, dd, d, D, Md, Mdd, out) <= bound_lim;
     }
-    // mx_bound: |error of 4 dF| <= 2|V| eS + 2 alpha eT + eQ with
-    //   eS, eT <= 2^-21 Mdd (the interface sums) + 2^-46 Md (the difference pairs) + eNL
-    //   eNL = 2^-18 Mdd dev + 2^-12 Mdd^2 (Md + Mdd) / eps: the four reconstructions' weight
-    //         deviations, rounded (a few ulps of dev) and moved by the rounding of the indicator
-    //         differences (at most 2^-18 Mdd (Md + Mdd) each; |dw / dbeta| <= 2 / eps)
-    //   eQ <= 2^-20 Md (|aR| + |bR| + |aL| + |bL|)
-    const float eNL = fmaf(0x1p-18f * Mdd, dev, 0x1p-12f * Mdd * Mdd * (Md + Mdd) * a.inv_eps);
-    const float eST = fmaf(0x1p-21f, Mdd, fmaf(0x1p-46f, Md, eNL));
-    const float Vb = LIN ? fabsf(a.g_h) : Vmax * 1.001f;
-    // (the 2^-92 (V + alpha) floor covers differences below 2^-74, whose low words are dropped)
-    float e4 = fmaf(2.f * Vb, eST, fmaf(2.f * a.alpha_f, eST, 0x1p-92f * (Vb + a.alpha_f)));
-    if constexpr (!LIN) e4 = fmaf(0x1p-20f * Md, 2.f * errmax, e4);
-    const bool ok = a.c_h * e4 <= bound_lim;  // false for NaN and infinities
     soft = !__any_sync(FULL, !ok);
   }
 

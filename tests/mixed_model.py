@@ -89,11 +89,26 @@ def rec2(d, D, eps):
     return rr, rl, rrn, rln, dev
 
 
-def mixed_dtl(u, k, eps, alpha, dt, dx, fn="burgers", g=0.0, dv=None):
+def lin(k, d):
+    """the kernel's mx::lin: linear-weight parts of rr and rl"""
+    if k == 3:
+        dmm, dm, d0, d1 = d
+        rr = r(fma(24.0, d0, fma(-3.0, d1, fma(11.0, dm, r(-2.0 * dmm)))) * f32(1.0 / 60.0))
+        rl = r(fma(2.0, d1, fma(-11.0, d0, fma(-24.0, dm, r(3.0 * dmm)))) * f32(1.0 / 60.0))
+    else:
+        dm, d0 = d
+        rr = fma(1.0 / 3.0, d0, r(f32(1.0 / 6.0) * dm))
+        rl = -fma(1.0 / 6.0, d0, r(f32(1.0 / 3.0) * dm))
+    return rr, rl
+
+
+def mixed_dtl(u, k, eps, alpha, dt, dx, fn="burgers", g=0.0, dv=None, nl=True):
     """dt L(v) of the FP32 path for the interior cells j = 4 .. n-5 of v = u (+ dv, a float-pair
     increment given as (h, l) arrays), and the kernel's bound on its rounding error, as
     (cells, dtL (float64 value of the pair), bound).  The bound is per cell here; the kernel
-    takes the largest over each lane's window, which is no smaller."""
+    takes the largest over each lane's window, which is no smaller.  nl = False: the
+    linear-weight pass (weights dropped); its bound includes the dropped parts and is inf where
+    the kernel would not take that pass (indicator differences above eps / 100)."""
     u = np.asarray(u, np.float64)
     n = u.size
     d64 = u[1:] - u[:-1]              # d_q = u_{q+1} - u_q, q = 0 .. n-2
@@ -113,6 +128,11 @@ def mixed_dtl(u, k, eps, alpha, dt, dx, fn="burgers", g=0.0, dv=None):
     cells = np.arange(4, n - 4)
     # reconstructions of cells j-1, j, j+1 for every interior j: index arrays on cell c
     def rec(c):
+        if not nl:
+            dd = (dh[c - 2], dh[c - 1], dh[c], dh[c + 1]) if k == 3 else (dh[c - 1], dh[c])
+            rr, rl = lin(k, dd)
+            z = np.zeros_like(rr)
+            return rr, rl, z, z, z
         if k == 3:
             dd = (dh[c - 2], dh[c - 1], dh[c], dh[c + 1])
             DD = (D[c - 2], D[c - 1], D[c])
@@ -170,6 +190,20 @@ def mixed_dtl(u, k, eps, alpha, dt, dx, fn="burgers", g=0.0, dv=None):
     Mdd = np.maximum.reduce([np.abs(D[np.clip(lo + t, 0, D.size - 1)]) for t in range(5)])
     dev = np.maximum.reduce([Rm[4], R0[4], Rp[4]])
     inv_eps = f32(1.0 / eps)
+    if not nl:  # the linear-weight pass's bound, from the window maxima alone
+        Md64, Mdd64 = Md.astype(np.float64), Mdd.astype(np.float64)
+        Vb = (np.abs(u[j]) + (np.abs(dv[0][j]) if dv is not None else 0.0)) * 1.001
+        if fn != "burgers":
+            Vb = np.full(j.size, abs(float(f32(g))))
+        Db = 4.0 * Mdd64 * (Md64 + 2.5 * Mdd64)
+        eSkip = 6.0 * Db * Mdd64 * float(inv_eps)
+        eL = 2.0 ** -21 * Mdd64 + 2.0 ** -46 * Md64 + eSkip
+        a_f = float(f32(alpha))
+        e4 = 2.0 * Vb * eL + 2.0 * a_f * eL + 2.0 ** -92 * (Vb + a_f)
+        if fn == "burgers":
+            e4 = e4 + Md64 * (2.0 ** -17 * Md64 + 8.0 * eSkip)
+        bound = float(f32(dt / (4.0 * dx))) * e4
+        return cells, dtl, np.where(Db * float(inv_eps) <= 0.01, bound, np.inf)
     eNL = r(2.0 ** -18 * Mdd.astype(np.float64) * dev + 2.0 ** -12 * Mdd.astype(np.float64) ** 2
             * (Md.astype(np.float64) + Mdd) * inv_eps)
     eST = 2.0 ** -21 * Mdd + 2.0 ** -46 * Md + eNL

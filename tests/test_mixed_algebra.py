@@ -6,7 +6,8 @@ reference's formulas, src/hrweno_kinds.F90:13-14).
 On cells where the kernel's rounding-error bound admits the FP32 path, dt L agrees with the
 exact right-hand side to within that bound, and the bound is within the per-stage budget of
 2^-54 max|u|; every variant the kernel covers (k = 2, 3; Burgers, linear advection; the first
-stage and a stage with a float-pair increment) is checked.
+stage and a stage with a float-pair increment; the full weights and the linear-weight pass that
+warps take where the weights' deviations cannot matter) is checked.
 """
 import numpy as np
 import pytest
@@ -25,10 +26,11 @@ def large_line(n, k, fn):
     return prob, u0, dt
 
 
+@pytest.mark.parametrize("nl", [True, False], ids=["weights", "linear_pass"])
 @pytest.mark.parametrize("stage", ["first", "increment"])
 @pytest.mark.parametrize("fn", ["burgers", "linear"])
 @pytest.mark.parametrize("k", [3, 2])
-def test_fp32_path_within_its_bound(orc, k, fn, stage):
+def test_fp32_path_within_its_bound(orc, k, fn, stage, nl):
     n = 1 << 19
     prob, u0, dt = large_line(n, k, fn)
     g = 0.7 if fn == "linear" else 0.0
@@ -45,7 +47,7 @@ def test_fp32_path_within_its_bound(orc, k, fn, stage):
         dh, dl = split(v - u0)
         dv = (dh, dl)
     ref = orc.rhs(prob, v, prec=128) * dt
-    cells, dtl, bound = mixed_dtl(u0, k, 1e-6, prob.alpha[0], dt, dx, fn=fn, g=g, dv=dv)
+    cells, dtl, bound = mixed_dtl(u0, k, 1e-6, prob.alpha[0], dt, dx, fn=fn, g=g, dv=dv, nl=nl)
     err = np.abs(dtl - ref[cells])
     lim = 2.0 ** (np.floor(np.log2(np.max(np.abs(u0)))) - 54)
     soft = bound <= lim
