@@ -16,7 +16,7 @@
 //  * stage values are stored as float-pair increments from u; the last stage adds its
 //    increment to u in FP64.
 //
-// Where the FP32 parts could move a result by more than 2^-54 max|u| per stage (steep or
+// Where the FP32 parts could move a result by more than 2^-53 max|u| per stage (steep or
 // under-resolved data, the line ends, values outside [2^-40, 2^60]) the whole warp runs the
 // FAST FP64 arithmetic instead; each warp's decision rests on a bound of its own rounding
 // errors, evaluated from the data (mx_bound below).

@@ -19,7 +19,7 @@
 // in registers (no shared memory).  The neighbour differences of the lane's own cells come from
 // its own loads; the window's edges come from the neighbouring lanes by shuffles, and five
 // lanes compute the warp's edge differences.  A warp whose cells touch a line end, or whose
-// rounding-error bound (mx_bound) exceeds 2^-54 of its largest |u|, runs the FAST FP64
+// rounding-error bound (mx_bound) exceeds 2^-53 of the line's largest |u|, runs the FAST FP64
 // arithmetic of stage1d.cu on its cells instead, with the same stage formulas.
 #include <cmath>
 
@@ -226,13 +226,15 @@ __device__ __forceinline__ float soft_cells(const MixedArgs& a, const double* u,
   //   eNL = 2^-18 Mdd dev + 2^-12 Mdd^2 (Md + Mdd) / eps: the four reconstructions' weight
   //         deviations, rounded (a few ulps of dev) and moved by the rounding of the indicator
   //         differences (at most 2^-18 Mdd (Md + Mdd) each; |dw / dbeta| <= 2 / eps)
-  //   eQ <= 2^-20 Md (|aR| + |bR| + |aL| + |bL|)
+  //   eQ <= 2^-21 Md (|aR| + |bR| + |aL| + |bL|): each offset is within 2^-22.2 Md of its
+  //         value (d rounded to FP32, the rounding of the linear stencils), its square and the sum
+  //         add a few roundings of Md^2
   // (the 2^-92 (V + alpha) floor covers differences below 2^-74, whose low words are dropped)
   const float eNL = fmaf(0x1p-18f * Mdd, dev, 0x1p-12f * Mdd * Mdd * (Md + Mdd) * a.inv_eps);
   const float eST = fmaf(0x1p-21f, Mdd, fmaf(0x1p-46f, Md, eNL));
   const float Vb = LIN ? fabsf(a.g_h) : Vmax * 1.001f;
   float e4 = fmaf(2.f * Vb, eST, fmaf(2.f * a.alpha_f, eST, 0x1p-92f * (Vb + a.alpha_f)));
-  if constexpr (!LIN) e4 = fmaf(0x1p-20f * Md, 2.f * errmax, e4);
+  if constexpr (!LIN) e4 = fmaf(0x1p-21f * Md, 2.f * errmax, e4);
   return a.c_h * e4;  // NaN for NaN and infinite inputs: the caller's test fails
 }
 
@@ -278,13 +280,14 @@ __global__ void __launch_bounds__(NT, MINB) stage1d_mixed_kernel(MixedArgs a) {
   bool soft = inside && g_mixed_soft != 0;
 
   // ---- the scale: the line's largest |u| at the start of the integrate call (its high word,
-  // *a.scale), as a power of two below it; 2^-54 of it is the per-stage error budget of dt L.
+  // *a.scale), as a power of two below it; 2^-53 of it (half an FP64 ulp of the largest values)
+  // is the per-stage error budget of dt L.
   // Soft range: 2^-40 <= max|u| < 2^60.
   float bound_lim = 0.f;
   if (soft) {
     const int E = (int)(*a.scale >> 20) - 1023;  // 2^E <= max|u|
     soft = E >= -40 && E < 60;
-    bound_lim = __int_as_float((E - 54 + 127) << 23);
+    bound_lim = __int_as_float((E - 53 + 127) << 23);
   }
 
   // ---- float-pair differences of the stage values, v = u (+ dv) ----------------------------------
@@ -339,7 +342,7 @@ __global__ void __launch_bounds__(NT, MINB) stage1d_mixed_kernel(MixedArgs a) {
     float Md = 0.f, Mdd = 0.f;
 #pragma unroll
     for (int q = 0; q < ND; ++q) {
-      d[q] = dd[q].h;
+      d[q] = dd[q].h + dd[q].l;  // d to FP32 precision (the pair rounded to nearest)
       Md = fmaxf(Md, fabsf(d[q]));
     }
 #pragma unroll
@@ -366,7 +369,8 @@ __global__ void __launch_bounds__(NT, MINB) stage1d_mixed_kernel(MixedArgs a) {
     const float eSkip = 6.f * Db * Mdd * a.inv_eps;  // the four reconstructions' dropped parts
     const float eL = fmaf(0x1p-21f, Mdd, fmaf(0x1p-46f, Md, eSkip));
     float e4 = fmaf(2.f * Vb, eL, fmaf(2.f * a.alpha_f, eL, 0x1p-92f * (Vb + a.alpha_f)));
-    if constexpr (!LIN) e4 = fmaf(Md, fmaf(0x1p-17f, Md, 8.f * eSkip), e4);  // quadratic terms
+    // quadratic terms: eQ with |aR| + |bR| + |aL| + |bL| <= 4 Md, and the dropped parts' effect
+    if constexpr (!LIN) e4 = fmaf(Md, fmaf(0x1p-18f, Md, 8.f * eSkip), e4);
     const bool lin_ok = Db * a.inv_eps <= 0.01f && a.c_h * e4 <= bound_lim;
     bool ok;
     if (__all_sync(FULL, lin_ok)) {

@@ -79,7 +79,7 @@ enum { HRW_BC_COPY = 0, HRW_BC_ZERO = 1, HRW_BC_ZERO_INFLOW = 2 };
  * form on the FP32 pipe: FP64 neighbour differences split into float pairs, the linear-weight
  * part of the reconstruction in float-pair precision, the WENO weights' deviations from the
  * linear weights in FP32, stage increments stored as float pairs.  A warp whose data would let
- * the FP32 parts move dt L by more than 2^-54 max|u| per stage (steep or under-resolved
+ * the FP32 parts move dt L by more than 2^-53 max|u| per stage (steep or under-resolved
  * data, the line ends, max|u| outside [2^-40, 2^60]) runs the FAST arithmetic instead; so does
  * everything the MIXED kernel does not cover.  Covered: rktvd integrators of FV1D lines of at
  * least 65536 uniform cells, k = 2 or 3, Lax-Friedrichs flux, Burgers or linear advection at

@@ -124,21 +124,22 @@ def mixed_dtl(u, k, eps, alpha, dt, dx, fn="burgers", g=0.0, dv=None, nl=True):
         dl = r(lo - r(h2 - s))
         dh = h2
     D = r(r(dh[1:] - dh[:-1]) + r(dl[1:] - dl[:-1]))  # D_q = Dd_q, q = 0 .. n-3
+    df = r(dh + dl)                   # d to FP32 precision (the kernel's d[])
     epsf = f32(eps)
     cells = np.arange(4, n - 4)
     # reconstructions of cells j-1, j, j+1 for every interior j: index arrays on cell c
     def rec(c):
         if not nl:
-            dd = (dh[c - 2], dh[c - 1], dh[c], dh[c + 1]) if k == 3 else (dh[c - 1], dh[c])
+            dd = (df[c - 2], df[c - 1], df[c], df[c + 1]) if k == 3 else (df[c - 1], df[c])
             rr, rl = lin(k, dd)
             z = np.zeros_like(rr)
             return rr, rl, z, z, z
         if k == 3:
-            dd = (dh[c - 2], dh[c - 1], dh[c], dh[c + 1])
+            dd = (df[c - 2], df[c - 1], df[c], df[c + 1])
             DD = (D[c - 2], D[c - 1], D[c])
             tA = tuple(fma(r(f32(13.0 / 12.0) * x), x, epsf) for x in DD)
             return rec3(dd, DD, tA, epsf)
-        return rec2((dh[c - 1], dh[c]), (D[c - 1],), epsf)
+        return rec2((df[c - 1], df[c]), (D[c - 1],), epsf)
     Rm, R0, Rp = rec(cells - 1), rec(cells), rec(cells + 1)
 
     def XY(i):
@@ -152,8 +153,8 @@ def mixed_dtl(u, k, eps, alpha, dt, dx, fn="burgers", g=0.0, dv=None, nl=True):
     Xj, Yj = XY(cells)
     Xm, Ym = XY(cells - 1)
     j = cells
-    aR, bR = R0[0], r(dh[j] + Rp[1])
-    aL, bL = r(Rm[0] - dh[j - 1]), R0[1]
+    aR, bR = R0[0], r(df[j] + Rp[1])
+    aL, bL = r(Rm[0] - df[j - 1]), R0[1]
     Sn = r(r(R0[2] + Rp[3]) - r(Rm[2] + R0[3]))
     Tn = r(r(R0[2] - Rp[3]) - r(Rm[2] - R0[3]))
     sh = r(dh[j] + dh[j - 1])
@@ -186,7 +187,7 @@ def mixed_dtl(u, k, eps, alpha, dt, dx, fn="burgers", g=0.0, dv=None, nl=True):
     dtl = -(th.astype(np.float64) + tl.astype(np.float64))
     # the kernel's bound (per cell, over the cell's window)
     lo, hi = j - 3, j + 3
-    Md = np.maximum.reduce([np.abs(dh[lo + t]) for t in range(6)])
+    Md = np.maximum.reduce([np.abs(df[lo + t]) for t in range(6)])
     Mdd = np.maximum.reduce([np.abs(D[np.clip(lo + t, 0, D.size - 1)]) for t in range(5)])
     dev = np.maximum.reduce([Rm[4], R0[4], Rp[4]])
     inv_eps = f32(1.0 / eps)
@@ -201,7 +202,7 @@ def mixed_dtl(u, k, eps, alpha, dt, dx, fn="burgers", g=0.0, dv=None, nl=True):
         a_f = float(f32(alpha))
         e4 = 2.0 * Vb * eL + 2.0 * a_f * eL + 2.0 ** -92 * (Vb + a_f)
         if fn == "burgers":
-            e4 = e4 + Md64 * (2.0 ** -17 * Md64 + 8.0 * eSkip)
+            e4 = e4 + Md64 * (2.0 ** -18 * Md64 + 8.0 * eSkip)
         bound = float(f32(dt / (4.0 * dx))) * e4
         return cells, dtl, np.where(Db * float(inv_eps) <= 0.01, bound, np.inf)
     eNL = r(2.0 ** -18 * Mdd.astype(np.float64) * dev + 2.0 ** -12 * Mdd.astype(np.float64) ** 2
@@ -211,5 +212,5 @@ def mixed_dtl(u, k, eps, alpha, dt, dx, fn="burgers", g=0.0, dv=None, nl=True):
     e4 = 2.0 * Vb * eST + 2.0 * float(f32(alpha)) * eST + 2.0 ** -92 * (Vb + float(f32(alpha)))
     if fn == "burgers":
         errmax = np.maximum(np.abs(aR), np.abs(bR)) + np.maximum(np.abs(aL), np.abs(bL))
-        e4 = e4 + 2.0 ** -20 * Md * 2.0 * errmax
+        e4 = e4 + 2.0 ** -21 * Md * 2.0 * errmax
     return cells, dtl, float(ch) * e4
