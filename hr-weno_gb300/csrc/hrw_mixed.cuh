@@ -87,6 +87,21 @@ __device__ __forceinline__ double widen(float f) {
   return __hiloint2double((int)hi, (int)lo);
 }
 
+// The double nearest (within 2^-52 |h + l|) to a normalised pair h + l (|l| <= ulp(h) / 2) by
+// integer operations: the FP64 pattern of h, plus l counted in units of h's FP64 ulp
+// 2^(e_h - 52) (at most 2^28 of them).  Below a power of two the ulp halves, so a negative step
+// from a power of two counts double.  |h| < 2^-70: l is dropped.
+__device__ __forceinline__ double pack(F2 p) {
+  const unsigned hb = (unsigned)__float_as_int(p.h);
+  const int eb = (int)((hb >> 23) & 0xFFu);  // biased exponent of h
+  const float scale = __int_as_float(min(max(52 - (eb - 127) + 127, 1), 254) << 23);
+  int k = __float2int_rn(p.l * scale);       // l / 2^(e_h - 52)
+  k = eb >= 57 ? k : 0;
+  if (hb & 0x80000000u) k = -k;               // the pattern counts magnitudes
+  if ((hb & 0x7FFFFFu) == 0 && k < 0) k *= 2;
+  return __longlong_as_double(__double_as_longlong(widen(p.h)) + (long long)k);
+}
+
 // ---- float-pair arithmetic -------------------------------------------------------------------
 
 // error-free sum: s + e == a + b

@@ -355,15 +355,18 @@ __global__ void __launch_bounds__(NT, MINB) stage1d_mixed_kernel(MixedArgs a) {
     // rr or rl at most 1.34 |Dbeta| Mdd / eps.  Where dropping them moves dt L by less than the
     // budget in every lane of the warp (mx_bound with the dropped parts as an error term), the
     // warp takes the linear-weight pass, which skips the weights altogether.
+    // |V| <= 2^(E+1) + |dv| with E the exponent of the lane's largest |u| (from high words:
+    // an FP64-to-FP32 conversion would take the narrow FP64 unit)
     float Vb = LIN ? fabsf(a.g_h) : 0.f;
     if constexpr (!LIN) {
+      unsigned m = 0;
+      float x = 0.f;
 #pragma unroll
       for (int c = 0; c < C; ++c) {
-        float x = fabsf((float)u[c]);
-        if constexpr (reads_inc<ST>()) x += fabsf(dv[c].h);
-        Vb = fmaxf(Vb, x);
+        m = max(m, (unsigned)__double2hiint(u[c]) & 0x7FFFFFFFu);
+        if constexpr (reads_inc<ST>()) x = fmaxf(x, fabsf(dv[c].h));
       }
-      Vb *= 1.001f;
+      Vb = __int_as_float(max((int)(m >> 20) - 1023 + 1, -126) + 127 << 23) + 1.001f * x;
     }
     const float Db = 4.f * Mdd * fmaf(2.5f, Mdd, Md);
     const float eSkip = 6.f * Db * Mdd * a.inv_eps;  // the four reconstructions' dropped parts
@@ -414,7 +417,7 @@ __global__ void __launch_bounds__(NT, MINB) stage1d_mixed_kernel(MixedArgs a) {
         } else if constexpr (ST == MX_RK3C) {
           inc = mx::mul(mx::add(dv[c + s], inc), {a.two3_h, a.two3_l});
         }
-        r[s] = (u[c + s] + mx::widen(inc.h)) + mx::widen(inc.l);
+        r[s] = u[c + s] + mx::pack(inc);  // one FP64 addition
       }
       *reinterpret_cast<double2*>(a.uout + j0 + c) = make_double2(r[0], r[1]);
     }

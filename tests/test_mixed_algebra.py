@@ -70,3 +70,37 @@ def test_split_is_the_fp64_value_to_47_bits():
     assert np.all(np.abs(recon - d) <= 2.0 ** -47 * np.abs(d))
     assert np.all(np.abs(h.astype(np.float64)) <= np.abs(d))  # truncation toward zero
     assert np.all(np.abs(d - h.astype(np.float64)) < 2.0 ** -23 * np.abs(d))
+
+
+def pack_model(h, lo):
+    """numpy restatement of the kernel's mx::pack (float pair -> double by integer operations)"""
+    h = np.asarray(h, np.float32)
+    lo = np.asarray(lo, np.float32)
+    hb = h.view(np.uint32).astype(np.int64)
+    eb = (hb >> 23) & 0xFF
+    se = np.clip(52 - (eb - 127) + 127, 1, 254)
+    scale = ((se << 23).astype(np.uint32)).view(np.float32)
+    k = np.rint((lo * scale).astype(np.float64)).astype(np.int64)
+    k = np.where(eb >= 57, k, 0)
+    k = np.where(hb & 0x80000000, -k, k)
+    k = np.where(((hb & 0x7FFFFF) == 0) & (k < 0), 2 * k, k)
+    return (h.astype(np.float64).view(np.int64) + k).view(np.float64)
+
+
+def test_pack_is_the_pair_to_2e_52():
+    """The last MIXED stage adds a float-pair increment to u with one FP64 addition, after
+    packing the pair into the double nearest it (within 2^-52 of its value): random normalised
+    pairs, powers of two with negative low words (the step into the lower binade), both signs."""
+    rng = np.random.default_rng(11)
+    n = 200000
+    h = (rng.standard_normal(n) * np.exp2(rng.uniform(-60, 60, n))).astype(np.float32)
+    h[: n // 4] = np.exp2(rng.integers(-60, 60, n // 4)).astype(np.float32) * rng.choice([-1, 1], n // 4)
+    ulp = np.spacing(np.abs(h)).astype(np.float64)
+    lo = (rng.uniform(-0.5, 0.5, n) * ulp).astype(np.float32)
+    # keep the pairs normalised (fl32(h + l) == h)
+    keep = (h + lo) == h
+    h, lo = h[keep], lo[keep]
+    exact = h.astype(np.longdouble) + lo.astype(np.longdouble)
+    got = pack_model(h, lo).astype(np.longdouble)
+    err = np.abs(got - exact) / np.abs(exact)
+    assert float(err.max()) <= 2.0 ** -52, float(err.max())
