@@ -35,15 +35,18 @@ namespace hrw {
 
 namespace {
 
-// 4 cells per lane, 256-thread blocks, 3 blocks (24 warps) per SM at <= 80 registers: on the
-// 2^24-cell line 0.50 ms per RK3 step (k = 3), against 0.57 ms for 8 cells per lane at 2 blocks
-// per SM and 0.77 ms at one (the kernel is bound by instruction issue, so resident warps count)
+// 4 cells per lane, 256-thread blocks, 4 blocks (32 warps) per SM at <= 64 registers: on the
+// 2^24-cell line 0.349 ms per RK3 step (k = 3), against 0.376 ms at 3 blocks per SM and
+// 0.425 / 0.451 ms for 8 cells per lane at 3 / 2 blocks (the kernel is bound by instruction
+// issue and latency, so resident warps count)
 constexpr int C = 4;            // cells per lane
 constexpr int WC = 32 * C;      // cells per warp
 constexpr int NT = 256;         // threads per block
-constexpr int MINB = 3;         // resident blocks per SM
+constexpr int MINB = 4;         // resident blocks per SM
 constexpr int ND_MAX = C + 4;   // differences of a lane's window for k <= 3
 constexpr unsigned FULL = 0xffffffffu;
+static_assert(C % 2 == 0 && C >= 3, "pairs of cells per vector access; the window's edges (up to 3 "
+              "differences) come from one neighbouring lane");
 
 __device__ int g_mixed_soft = 1;                 // 0: every warp takes the FP64 path (tests)
 __device__ unsigned long long g_mixed_hard = 0;  // warps that took the FP64 path
