@@ -63,8 +63,8 @@ L2_BYTES = 126 * 1024 * 1024
 
 # DRAM bytes per cell and stage launch of the MIXED stage kernel, measured by ncu on the
 # 2^24-cell line (dram__bytes_read.sum + dram__bytes_write.sum of the three RK3 stage launches
-# of one step, divided by cells x 3); profiles/stage1d_mixed_weno5_rk3.md.  None until captured.
-NCU_DRAM_BYTES_PER_CELL_LAUNCH = None
+# of one step, divided by cells x 3); profiles/stage1d_mixed_weno5_rk3.md.
+NCU_DRAM_BYTES_PER_CELL_LAUNCH = 969.9e6 / (3 * (1 << 24))
 
 
 def peaks() -> dict:
