@@ -59,6 +59,8 @@ LAUNCHES_PER_STEP = 3
 # hi, lo (20 B).
 F32C_BYTES_PER_CELL_UPDATE = 40
 F32C_MOVED_BYTES_PER_CELL_UPDATE = 48
+# REAL32 (a REAL32 build of the reference, FP32 state): 32 B per RK3 cell-update, half of FP64's
+F32_BYTES_PER_CELL_UPDATE = 32
 L2_BYTES = 126 * 1024 * 1024
 
 # DRAM bytes per cell and stage launch of the MIXED stage kernel, measured by ncu on the
@@ -270,9 +272,12 @@ def hbm(bytes_per_cell_update: float, value: float, dist) -> float:
     return bytes_per_cell_update * value / dist.world / 1e9 / peaks()["hbm_gbs"]
 
 
+LINE_FORMS = (("fast", "f64"), ("mixed", "f64"), ("fast", "f32c"), ("strict", "f32"))
+
+
 def run_line_forms(args, dist: Dist, k: int, u_ref=None) -> list:
-    """Short lines for the plain FP64 (FAST), MIXED (k = 2 only; k = 3 is the headline) and
-    compensated FP32 forms of the 2^24-cell line with WENO(2k-1)."""
+    """Short lines for the plain FP64 (FAST), MIXED (k = 2 only; k = 3 is the headline),
+    compensated FP32 and REAL32 forms of the 2^24-cell line with WENO(2k-1)."""
     import torch
 
     from hrweno import workloads
@@ -280,24 +285,27 @@ def run_line_forms(args, dist: Dist, k: int, u_ref=None) -> list:
     stream = torch.cuda.Stream()
     out = []
     res = {}
-    for num, dtype in (("fast", "f64"), ("mixed", "f64"), ("fast", "f32c")):
+    for num, dtype in LINE_FORMS:
         if k == 3 and num == "mixed":
             continue
         prob, u0, dt = workloads.large_burgers(NC, k=k, numerics=num)
+        if dtype == "f32":
+            u0 = u0.astype(np.float32)
         el, u, _ = time_line(prob, u0, dt, dtype, args, dist, stream)
         v = dist.world * NC * args.steps / el
         res[(num, dtype)] = u
-        name = f"1d_k{k}_{'f32c' if dtype == 'f32c' else num}"
+        name = f"1d_k{k}_{dtype if dtype != 'f64' else num}"
         line = {"form": name, "value": v, "ms": 1e3 * el / args.steps}
         if dtype == "f32c":
             line["hbm_frac"] = hbm(F32C_BYTES_PER_CELL_UPDATE, v, dist)
             line["moved_B"] = F32C_MOVED_BYTES_PER_CELL_UPDATE
+        elif dtype == "f32":
+            line["hbm_frac"] = hbm(F32_BYTES_PER_CELL_UPDATE, v, dist)
         else:
             line["hbm_frac"] = hbm(BYTES_PER_CELL_UPDATE, v, dist)
         out.append(line)
     base = u_ref if u_ref is not None else res[("mixed", "f64")]
-    for line, key in zip(out, [kk for kk in (("fast", "f64"), ("mixed", "f64"), ("fast", "f32c"))
-                               if kk in res]):
+    for line, key in zip(out, [kk for kk in LINE_FORMS if kk in res]):
         if key != ("mixed", "f64") or u_ref is not None:
             d = (res[key] - base).abs()
             line["l1_vs_mixed"] = float(d.sum() / base.abs().sum())

@@ -6,10 +6,10 @@
 //   mstvd_init/integrate src/hrweno_tvdode.f90:180-271
 //   is_done              src/hrweno_tvdode.f90:273-284
 //
-// The time t stays on the host in FP64 and is advanced by the same `t = t + dt` sequence as
-// the reference, so the step count of every integrate call is known before the first launch;
-// the kernels themselves do not depend on t (every flux of the problem descriptor is
-// autonomous).
+// The time t stays on the host in the handle's real type (FP64, or FP32 for the REAL32 handles
+// of HRW_F32) and is advanced by the same `t = t + dt` sequence as the reference, so the step
+// count of every integrate call is known before the first launch; the kernels themselves do not
+// depend on t (every flux of the problem descriptor is autonomous).
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -40,10 +40,15 @@ int fail(int code, const std::string& msg) {
                   std::string(#call ": ") + cudaGetErrorString(e_));                      \
   } while (0)
 
-// is_done (src/hrweno_tvdode.f90:282)
-inline bool is_done(double t, double tout, double dt) {
-  return (t - tout) * std::copysign(1.0, dt) > 0.0;
+// is_done (src/hrweno_tvdode.f90:282), in the handle's real type
+template <class R>
+inline bool is_done(R t, R tout, R dt) {
+  return (t - tout) * std::copysign(R(1), dt) > R(0);
 }
+
+// epsilon(1.0_rk) of the eps check (src/hrweno_weno.f90:92) for rk = real64 and real32
+constexpr double kEps64 = 2.220446049250313e-16;
+constexpr float kEps32 = 1.1920928955078125e-07f;
 
 constexpr int64_t kMaxSteps = int64_t(1) << 40;
 // MIXED numerics take the MIXED kernel on lines of at least this many cells (shorter lines are
@@ -89,7 +94,7 @@ int validate_problem(const hrw_problem* p, int neq) {
     cells *= p->ncells[d];
   }
   if (p->k < 1 || p->k > 3) return fail(HRW_EINVAL, "Invalid input 'k'. Valid range: 1 <= k <= 3.");
-  if (!(p->eps > 2.220446049250313e-16))
+  if (!(p->eps > kEps64))
     return fail(HRW_EINVAL, "Invalid input 'eps'. Valid range: eps > epsilon.");
   if (p->flux != HRW_FLUX_LAX_FRIEDRICHS && p->flux != HRW_FLUX_GODUNOV)
     return fail(HRW_EINVAL, "Invalid input 'flux'.");
@@ -99,6 +104,59 @@ int validate_problem(const hrw_problem* p, int neq) {
   if (p->numerics == HRW_NUMERICS_MIXED && !(p->eps >= 1e-8))
     return fail(HRW_EINVAL, "Invalid input 'eps': HRW_NUMERICS_MIXED needs eps >= 1e-8.");
   if (cells != neq) return fail(HRW_EINVAL, "Invalid input 'neq': neq /= product of ncells.");
+  return HRW_OK;
+}
+
+// The checks of a REAL32 build on top of validate_problem: its epsilon is FP32's, and the
+// grid's values must stay valid once rounded to FP32 (the values that build would hold).
+int validate_problem_f32(const hrw_problem* p) {
+  if (!((float)p->eps > kEps32)) return fail(HRW_EINVAL, "Invalid input 'eps'. Valid range: eps > epsilon.");
+  if (p->kind == HRW_PROBLEM_LINEAR_ODE) return HRW_OK;
+  for (int d = 0; d < (p->kind == HRW_PROBLEM_FV2D ? 2 : 1); ++d) {
+    if (!((float)p->xmax[d] > (float)p->xmin[d]))
+      return fail(HRW_EINVAL, "Invalid input 'xmin', 'xmax': xmax > xmin must hold in REAL32.");
+    if (p->xedges[d])
+      for (int i = 0; i < p->ncells[d]; ++i)
+        if (!((float)p->xedges[d][i + 1] > (float)p->xedges[d][i]))
+          return fail(HRW_EINVAL, "Invalid input 'xedges': edges must increase in REAL32.");
+    if (p->width[d])
+      for (int i = 0; i < p->ncells[d]; ++i)
+        if (!((float)p->width[d][i] > 0.0f))
+          return fail(HRW_EINVAL, "Invalid input 'width': widths must be > 0 in REAL32.");
+  }
+  return HRW_OK;
+}
+
+// The number of steps n of an integrate call from t and the time it ends at (*tend), by the
+// reference's sequence t = t + dt (src/hrweno_tvdode.f90:137-143,170-171) in real type R: one
+// step for itask = 2, else until is_done.  A step that leaves t unchanged would never reach
+// tout and is refused.
+template <class R>
+int count_steps(R t, R tout, R dt, int itask, int64_t* n, R* tend) {
+  int64_t k = 0;
+  do {
+    const R t1 = t + dt;
+    if (t1 == t) return fail(HRW_EINVAL, "Invalid input 'dt': t + dt == t, so tout is never reached.");
+    t = t1;
+    if (++k > kMaxSteps) return fail(HRW_EINVAL, "Invalid input 'dt': too many steps to reach tout.");
+  } while (!(is_done(t, tout, dt) || itask == 2));
+  *n = k;
+  *tend = t;
+  return HRW_OK;
+}
+
+// The number of mstvd steps from t (src/hrweno_tvdode.f90:252-268: is_done is tested before
+// each step, so n may be 0), with the same refusal of steps that leave t unchanged.
+template <class R>
+int count_ms_steps(R t, R tout, R dt, int64_t* n) {
+  int64_t k = 0;
+  while (!is_done(t, tout, dt)) {
+    const R t1 = t + dt;
+    if (t1 == t) return fail(HRW_EINVAL, "Invalid input 'dt': t + dt == t, so tout is never reached.");
+    t = t1;
+    if (++k > kMaxSteps) return fail(HRW_EINVAL, "Invalid input 'dt': too many steps to reach tout.");
+  }
+  *n = k;
   return HRW_OK;
 }
 
@@ -120,6 +178,10 @@ struct hrw_weno {
   double* cnu = nullptr;  // device cnu(0:k-1,-1:k-1,1:nc)
   double* buf = nullptr;  // device v, vl, vr for host-memory calls (3 nc)
   cudaStream_t stream = nullptr;
+  // REAL32 calls on a non-uniform grid: the edges, and cnu computed from them in FP32 at the
+  // first such call
+  std::vector<double> xedges;
+  float* cnu32 = nullptr;
 };
 
 struct hrw_ode {
@@ -169,7 +231,159 @@ struct hrw_ode {
   bool mixed = false;
   MixedArgs mbase{};
   unsigned int* mscale = nullptr;
+  // REAL32 (HRW_F32): the problem in FP32 as a REAL32 build holds it, the state and stage
+  // buffers in FP32 (rktvd: su, sw1, sw2; mstvd also the rings), every allocation in sallocs
+  StageArgs32 sbase{};
+  float* su = nullptr;
+  float* sw1 = nullptr;
+  float* sw2 = nullptr;
+  float* sring_u[5] = {};
+  float* sring_l[4] = {};
+  float* srates = nullptr;
+  std::vector<void*> sallocs;
 };
+
+// weno%reconstruct of a REAL32 build: float arrays, FP32 eps, FP32 tables or FP32 cnu, in the
+// reference's operation order.
+static int weno_reconstruct_f32(hrw_weno* w, int mem, const void* v, void* vl, void* vr) {
+  if (!((float)w->eps > kEps32)) return fail(HRW_EINVAL, "Invalid input 'eps'. Valid range: eps > epsilon.");
+  if (!w->uniform && !w->cnu32) {
+    const int nc = w->nc;
+    std::vector<float> xe(nc + 1);
+    for (int i = 0; i <= nc; ++i) xe[i] = (float)w->xedges[i];
+    for (int i = 0; i < nc; ++i)
+      if (!(xe[i + 1] > xe[i])) return fail(HRW_EINVAL, "Invalid input 'xedges': edges must increase in REAL32.");
+    float* dx = nullptr;
+    float* cnu = nullptr;
+    cudaError_t e = cudaMalloc(&cnu, sizeof(float) * (size_t)w->k * (w->k + 1) * nc);
+    if (e == cudaSuccess) e = cudaMalloc(&dx, sizeof(float) * ((size_t)nc + 1));
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dx, xe.data(), sizeof(float) * ((size_t)nc + 1), cudaMemcpyHostToDevice, w->stream);
+    if (e == cudaSuccess) e = launch_calc_cnu(dx, cnu, nc, w->k, w->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(w->stream);
+    if (dx) cudaFree(dx);
+    if (e != cudaSuccess) {
+      if (cnu) cudaFree(cnu);
+      return fail(e == cudaErrorMemoryAllocation ? HRW_ENOMEM : HRW_ECUDA,
+                  std::string("hrw_weno_reconstruct: ") + cudaGetErrorString(e));
+    }
+    w->cnu32 = cnu;
+  }
+  const size_t bytes = sizeof(float) * (size_t)w->nc;
+  const float* dv = (const float*)v;
+  float* dl = (float*)vl;
+  float* dr = (float*)vr;
+  if (mem == HRW_MEM_HOST) {  // the 3 nc doubles of buf hold 3 nc floats
+    float* b = (float*)w->buf;
+    dv = b;
+    dl = b + w->nc;
+    dr = b + 2 * (size_t)w->nc;
+    HRW_CUDA(cudaMemcpyAsync((void*)dv, v, bytes, cudaMemcpyHostToDevice, w->stream));
+  }
+  if (w->uniform) {
+    StageArgs32 a{};
+    a.v = dv;
+    a.out = dl;
+    a.lout = dr;
+    a.eps = (float)w->eps;
+    a.L.nc = w->nc;
+    a.L.rx = 1.0f;
+    HRW_CUDA(launch_stage1d(a, w->k, ST_RECON, w->stream));
+  } else {
+    HRW_CUDA(launch_recon_nonuniform(dv, w->cnu32, dl, dr, w->nc, w->k, (float)w->eps, w->stream));
+  }
+  if (mem == HRW_MEM_HOST) {
+    HRW_CUDA(cudaMemcpyAsync(vl, dl, bytes, cudaMemcpyDeviceToHost, w->stream));
+    HRW_CUDA(cudaMemcpyAsync(vr, dr, bytes, cudaMemcpyDeviceToHost, w->stream));
+  }
+  HRW_CUDA(cudaStreamSynchronize(w->stream));
+  return HRW_OK;
+}
+
+// The REAL32 problem on the device: lines, widths, edges and cnu in FP32 as a REAL32 build
+// computes them (grid1%linear: dx = (xmax - xmin)/nc in FP32, src/hrweno_grids.f90:72; widths
+// edges(i) - edges(i-1); cnu by weno_calc_cnu in FP32), and the state and stage buffers.
+static cudaError_t setup_f32(hrw_ode* o, const hrw_problem* p) {
+  auto alloc = [&](size_t n, float** out) {
+    const cudaError_t e = cudaMalloc(out, sizeof(float) * (n ? n : 1));
+    if (e == cudaSuccess) o->sallocs.push_back(*out);
+    return e;
+  };
+  auto upload = [&](const std::vector<float>& h, float** out) {
+    cudaError_t e = alloc(h.size(), out);
+    if (e == cudaSuccess) e = cudaMemcpy(*out, h.data(), sizeof(float) * h.size(), cudaMemcpyHostToDevice);
+    return e;
+  };
+  cudaError_t e;
+  StageArgs32& b = o->sbase;
+  b.eps = (float)p->eps;
+  const size_t n = (size_t)o->neq;
+  if (p->kind == HRW_PROBLEM_LINEAR_ODE) {
+    std::vector<float> r(n);
+    for (size_t i = 0; i < n; ++i) r[i] = (float)p->rates[i];
+    if ((e = upload(r, &o->srates)) != cudaSuccess) return e;
+  } else {
+    const int nd = p->kind == HRW_PROBLEM_FV2D ? 2 : 1;
+    for (int d = 0; d < nd; ++d) {
+      LineArgsT<float>& L = d == 0 ? b.L : b.L2;
+      L.nc = p->ncells[d];
+      L.fn = p->fn[d];
+      L.bc = p->bc[d];
+      L.flux = p->flux;
+      L.a = (float)p->coef_a[d];
+      L.b = (float)p->coef_b[d];
+      L.alpha = (float)p->alpha[d];
+      L.xmin = (float)p->xmin[d];
+      const float span = (float)p->xmax[d] - (float)p->xmin[d];
+      L.rx = span / (float)L.nc;
+      if (p->width[d]) {
+        std::vector<float> w(L.nc);
+        for (int i = 0; i < L.nc; ++i) w[i] = (float)p->width[d][i];
+        float* dw = nullptr;
+        if ((e = upload(w, &dw)) != cudaSuccess) return e;
+        L.width = dw;
+      }
+      if (p->xedges[d]) {
+        std::vector<float> xe(L.nc + 1), w(L.nc);
+        for (int i = 0; i <= L.nc; ++i) xe[i] = (float)p->xedges[d][i];
+        for (int i = 0; i < L.nc; ++i) w[i] = xe[i + 1] - xe[i];
+        float *dxe = nullptr, *dw = nullptr, *cnu = nullptr;
+        if ((e = upload(xe, &dxe)) != cudaSuccess) return e;
+        if ((e = upload(w, &dw)) != cudaSuccess) return e;
+        if ((e = alloc((size_t)p->k * (p->k + 1) * L.nc, &cnu)) != cudaSuccess) return e;
+        if ((e = launch_calc_cnu(dxe, cnu, L.nc, p->k, o->own)) != cudaSuccess) return e;
+        if ((e = cudaStreamSynchronize(o->own)) != cudaSuccess) return e;
+        L.xe = dxe;
+        L.width = dw;
+        b.cnu = cnu;
+      }
+    }
+    b.ld = p->ncells[0];
+    if (nd == 2) {
+      // upwind when g > 0 at every interface in FP32: the FP32 evaluation of g at the line ends
+      // differs from the FP64 one by a few FP32 rounding errors, far inside a 1e-5 margin
+      LineArgs g1{}, g2{};
+      for (int d = 0; d < 2; ++d) {
+        const LineArgsT<float>& F = d == 0 ? b.L : b.L2;
+        LineArgs& G = d == 0 ? g1 : g2;
+        G.nc = F.nc, G.fn = F.fn, G.a = F.a, G.b = F.b, G.xmin = F.xmin, G.rx = F.rx;
+      }
+      b.upwind = p->flux == HRW_FLUX_GODUNOV && positive_velocity(g1, 1e-5) && positive_velocity(g2, 1e-5);
+      if ((e = cudaMalloc(&o->tflag, sizeof(unsigned int))) != cudaSuccess) return e;
+      if ((e = cudaMemset(o->tflag, 0, sizeof(unsigned int))) != cudaSuccess) return e;
+      b.timeout_flag = o->tflag;
+    }
+  }
+  if ((e = alloc(n, &o->su)) != cudaSuccess) return e;
+  if ((e = alloc(n, &o->sw1)) != cudaSuccess) return e;
+  if ((e = alloc(n, &o->sw2)) != cudaSuccess) return e;
+  if (o->method == 1) {
+    for (float*& q : o->sring_u)
+      if ((e = alloc(n, &q)) != cudaSuccess) return e;
+    for (float*& q : o->sring_l)
+      if ((e = alloc(n, &q)) != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
 
 extern "C" {
 
@@ -200,7 +414,7 @@ int hrw_weno_create(int ncells, int k, double eps, const double* xedges, hrw_wen
   if (k > 0 && k > 3) return fail(HRW_EINVAL, "Invalid input 'k'. Valid range: 1 <= k <= 3.");
   if (k == 0 || k < 0) k = 3;
   if (eps <= 0.0 && eps == eps) eps = 1e-6;
-  if (!(eps > 2.220446049250313e-16))
+  if (!(eps > kEps64))
     return fail(HRW_EINVAL, "Invalid input 'eps'. Valid range: eps > epsilon.");
   hrw_weno* w = new hrw_weno;
   w->nc = ncells;
@@ -210,6 +424,7 @@ int hrw_weno_create(int ncells, int k, double eps, const double* xedges, hrw_wen
   if (e == cudaSuccess) e = cudaMalloc(&w->buf, sizeof(double) * 3 * (size_t)ncells);
   if (e == cudaSuccess && xedges) {
     w->uniform = false;
+    w->xedges.assign(xedges, xedges + (size_t)ncells + 1);
     double* dx = nullptr;
     e = cudaMalloc(&w->cnu, sizeof(double) * (size_t)k * (k + 1) * ncells);
     if (e == cudaSuccess) e = cudaMalloc(&dx, sizeof(double) * ((size_t)ncells + 1));
@@ -239,8 +454,10 @@ int hrw_weno_set_numerics(hrw_weno* w, int numerics) {
 int hrw_weno_reconstruct(hrw_weno* w, int dtype, int mem, const void* v, void* vl, void* vr) {
   if (!w) return fail(HRW_EINVAL, "Invalid input 'w': null handle.");
   if (!v || !vl || !vr) return fail(HRW_EINVAL, "Invalid input: null array.");
-  if (dtype != HRW_F64) return fail(HRW_EINVAL, "Invalid input 'dtype': reconstruct supports HRW_F64.");
+  if (dtype != HRW_F64 && dtype != HRW_F32)
+    return fail(HRW_EINVAL, "Invalid input 'dtype': reconstruct supports HRW_F64 and HRW_F32.");
   if (mem != HRW_MEM_HOST && mem != HRW_MEM_DEVICE) return fail(HRW_EINVAL, "Invalid input 'mem'.");
+  if (dtype == HRW_F32) return weno_reconstruct_f32(w, mem, v, vl, vr);
   const size_t bytes = sizeof(double) * (size_t)w->nc;
   const double* dv = (const double*)v;
   double* dl = (double*)vl;
@@ -283,6 +500,7 @@ int hrw_weno_cnu(const hrw_weno* w, double* cnu_host) {
 int hrw_weno_destroy(hrw_weno* w) {
   if (!w) return HRW_OK;
   if (w->cnu) cudaFree(w->cnu);
+  if (w->cnu32) cudaFree(w->cnu32);
   if (w->buf) cudaFree(w->buf);
   if (w->stream) cudaStreamDestroy(w->stream);
   delete w;
@@ -297,13 +515,10 @@ static int ode_create(const hrw_problem* p, int neq, int order, int method, int 
   if (neq <= 0) return fail(HRW_EINVAL, "Invalid input 'neq'. Valid range: neq >= 1.");
   if (method == 0 && (order < 1 || order > 3))
     return fail(HRW_EINVAL, "Invalid input 'order' in 'rktvd'. Valid range: 1 <= k <= 3.");
-  if (dtype != HRW_F64 && dtype != HRW_F32C) {
-    if (dtype == HRW_F32)
-      return fail(HRW_EINVAL, "Invalid input 'dtype': HRW_F32 integrators are not built; use HRW_F32C.");
-    return fail(HRW_EINVAL, "Invalid input 'dtype'.");
-  }
+  if (dtype != HRW_F64 && dtype != HRW_F32C && dtype != HRW_F32) return fail(HRW_EINVAL, "Invalid input 'dtype'.");
   int rc = validate_problem(p, neq);
   if (rc != HRW_OK) return rc;
+  if (dtype == HRW_F32 && (rc = validate_problem_f32(p)) != HRW_OK) return rc;
   if (dtype == HRW_F32C) {
     if (p->xedges[0] || p->xedges[1])
       return fail(HRW_EINVAL, "Invalid input 'xedges': non-uniform lines are supported for HRW_F64.");
@@ -332,6 +547,12 @@ static int ode_create(const hrw_problem* p, int neq, int order, int method, int 
   cudaError_t e = cudaStreamCreateWithFlags(&o->own, cudaStreamDefault);
   if (e != cudaSuccess) return cleanup(e);
   o->stream = o->own;
+  if (dtype == HRW_F32) {
+    if ((e = setup_f32(o, p)) != cudaSuccess) return cleanup(e);
+    o->istate = 1;
+    *out = o;
+    return HRW_OK;
+  }
   const size_t bytes = sizeof(double) * (size_t)neq;
   StageArgs& b = o->base;
   b.eps = p->eps;
@@ -522,6 +743,7 @@ int hrw_ode_destroy(hrw_ode* o) {
   for (double* p : o->ring_l)
     if (p) cudaFree(p);
   if (o->fmem) cudaFree(o->fmem);
+  for (void* q : o->sallocs) cudaFree(q);
   if (o->tflag) cudaFree(o->tflag);
   if (o->mscale) cudaFree(o->mscale);
   if (o->graph.exec) cudaGraphExecDestroy(o->graph.exec);
@@ -712,12 +934,9 @@ static int rk_integrate_mixed(hrw_ode* o, double* du, int64_t n, double dt) {
 // rktvd_integrate (src/hrweno_tvdode.f90:97-178) on device array du.
 static int rk_integrate(hrw_ode* o, double* du, double* t, double tout, double dt, int itask) {
   // replay the reference's time sequence (:137-143) to count the steps
-  double tt = *t;
-  int64_t n = 0;
-  do {
-    tt = tt + dt;
-    if (++n > kMaxSteps) return fail(HRW_EINVAL, "Invalid input 'dt': too many steps to reach tout.");
-  } while (!(is_done(tt, tout, dt) || itask == 2));
+  double tt;
+  int64_t n;
+  if (const int rc = count_steps(*t, tout, dt, itask, &n, &tt)) return rc;
   // the MIXED kernel moves 16-byte vectors: a device array that is not 16-byte aligned (a view
   // at an odd offset) runs the FAST kernels
   if (o->mixed && ((uintptr_t)du & 15) == 0) {
@@ -783,9 +1002,8 @@ static int ms_integrate(hrw_ode* o, double* du, double* t, double tout, double d
   } else {
     HRW_CUDA(cudaMemcpyAsync(o->ring_u[o->level % 5], du, bytes, cudaMemcpyDeviceToDevice, o->stream));
   }
-  int64_t n = 0;
-  for (double t2 = tt; !is_done(t2, tout, dt); t2 = t2 + dt)
-    if (++n > kMaxSteps) return fail(HRW_EINVAL, "Invalid input 'dt': too many steps to reach tout.");
+  int64_t n;
+  if (const int rc = count_ms_steps(tt, tout, dt, &n)) return rc;
   auto ms_step = [&](int64_t m) {  // (:252-268)
     double* um = o->ring_u[m % 5];
     double* un = o->ring_u[(m + 1) % 5];  // holds u^{m-4}, overwritten in place
@@ -869,12 +1087,9 @@ static cudaError_t rk_step_f32c(hrw_ode* o, int from, int to, double dt) {
 }
 
 static int rk_integrate_f32c(hrw_ode* o, double* du, double* t, double tout, double dt, int itask) {
-  double tt = *t;
-  int64_t n = 0;
-  do {
-    tt = tt + dt;
-    if (++n > kMaxSteps) return fail(HRW_EINVAL, "Invalid input 'dt': too many steps to reach tout.");
-  } while (!(is_done(tt, tout, dt) || itask == 2));
+  double tt;
+  int64_t n;
+  if (const int rc = count_steps(*t, tout, dt, itask, &n, &tt)) return rc;
   int slot = 0;
   HRW_CUDA(launch_split_f64(du, o->fhi[0], o->flo[0], o->neq, o->stream));
   int64_t s0 = 0;
@@ -920,9 +1135,8 @@ static int ms_integrate_f32c(hrw_ode* o, double* du, double* t, double tout, dou
   } else {
     HRW_CUDA(launch_split_f64(du, o->fhi[o->level % 5], o->flo[o->level % 5], o->neq, o->stream));
   }
-  int64_t n = 0;
-  for (double t2 = tt; !is_done(t2, tout, dt); t2 = t2 + dt)
-    if (++n > kMaxSteps) return fail(HRW_EINVAL, "Invalid input 'dt': too many steps to reach tout.");
+  int64_t n;
+  if (const int rc = count_ms_steps(tt, tout, dt, &n)) return rc;
   for (int64_t s = 0; s < n; ++s) {  // (:252-268)
     const int64_t m = o->level;
     const int cur = (int)(m % 5), nxt = (int)((m + 1) % 5);  // nxt holds u^{m-4}
@@ -932,6 +1146,133 @@ static int ms_integrate_f32c(hrw_ode* o, double* du, double* t, double tout, dou
     o->level = m + 1;
   }
   HRW_CUDA(launch_merge_f64(o->fhi[o->level % 5], o->flo[o->level % 5], du, o->neq, o->stream));
+  *t = tt;
+  o->fevals += (int)n;
+  o->nsteps += n;
+  return HRW_OK;
+}
+
+// ---- REAL32 (HRW_F32) ---------------------------------------------------------------------------
+// The time loops of a REAL32 build: t, tout and dt in FP32, the state and every stage in FP32
+// in the reference's operation order.
+static cudaError_t run_stage32(hrw_ode* o, int stage, const float* v, const float* u, float* out,
+                               float* lout, const float* uo4, const float* lo4, float dt) {
+  StageArgs32 a = o->sbase;
+  a.v = v;
+  a.u = u;
+  a.out = out;
+  a.lout = lout;
+  a.uo4 = uo4;
+  a.lo4 = lo4;
+  a.dt = dt;
+  const int k = o->prob.k;
+  switch (o->prob.kind) {
+    case HRW_PROBLEM_LINEAR_ODE: return launch_stage_linear(o->srates, a, o->neq, stage, o->stream);
+    case HRW_PROBLEM_FV1D:
+      return a.cnu ? launch_stage1d_nu(a, k, stage, o->stream) : launch_stage1d(a, k, stage, o->stream);
+    default: return launch_stage2d(a, k, stage, o->stream);
+  }
+}
+
+// one rktvd step (src/hrweno_tvdode.f90:136-171) from u, in place for orders 2 and 3
+static cudaError_t rk_step32(hrw_ode* o, float* u, float* out1, float dt) {
+  cudaError_t e;
+  if (o->order == 1) return run_stage32(o, ST_EULER, u, u, out1, nullptr, nullptr, nullptr, dt);
+  if ((e = run_stage32(o, ST_EULER, u, u, o->sw1, nullptr, nullptr, nullptr, dt)) != cudaSuccess) return e;
+  if (o->order == 2) return run_stage32(o, ST_RK2B, o->sw1, u, u, nullptr, nullptr, nullptr, dt);
+  if ((e = run_stage32(o, ST_RK3B, o->sw1, u, o->sw2, nullptr, nullptr, nullptr, dt)) != cudaSuccess) return e;
+  return run_stage32(o, ST_RK3C, o->sw2, u, u, nullptr, nullptr, nullptr, dt);
+}
+
+static int rk_integrate32(hrw_ode* o, float* du, float* t, float tout, float dt, int itask) {
+  float tt;
+  int64_t n;
+  if (const int rc = count_steps(*t, tout, dt, itask, &n, &tt)) return rc;
+  float* cur = du;
+  float* other = o->sw2;
+  int64_t s0 = 0;
+  if (const int64_t G = rk_graph_steps(o, n)) {
+    bool ok = false;
+    HRW_CUDA(run_graph(o, du, dt, 0, G, n / G, &ok, [&]() {
+      float* c = du;
+      float* w = o->sw2;
+      for (int64_t s = 0; s < G; ++s) {
+        const cudaError_t e = rk_step32(o, c, w, dt);
+        if (e != cudaSuccess) return e;
+        if (o->order == 1) std::swap(c, w);
+      }
+      return cudaSuccess;
+    }));
+    if (ok) s0 = n / G * G;
+  }
+  for (int64_t s = s0; s < n; ++s) {
+    HRW_CUDA(rk_step32(o, cur, other, dt));
+    if (o->order == 1) std::swap(cur, other);
+  }
+  if (cur != du)
+    HRW_CUDA(cudaMemcpyAsync(du, cur, sizeof(float) * (size_t)o->neq, cudaMemcpyDeviceToDevice, o->stream));
+  *t = tt;
+  o->fevals += (int)(o->order * n);
+  o->nsteps += n;
+  if (o->istate == 1) o->istate = 2;  // (:176)
+  return HRW_OK;
+}
+
+// mstvd_integrate (src/hrweno_tvdode.f90:203-271): u^m in sring_u[m % 5], L(u^m) in sring_l[m % 4]
+static int ms_integrate32(hrw_ode* o, float* du, float* t, float tout, float dt) {
+  const size_t bytes = sizeof(float) * (size_t)o->neq;
+  float tt = *t;
+  if (o->istate == 1) {  // RK3 start (:236-249)
+    o->level = 0;
+    HRW_CUDA(cudaMemcpyAsync(o->sring_u[0], du, bytes, cudaMemcpyDeviceToDevice, o->stream));
+    for (int m = 0; m < 4; ++m) {
+      float* um = o->sring_u[m % 5];
+      float* un = o->sring_u[(m + 1) % 5];
+      HRW_CUDA(run_stage32(o, ST_RHS, um, um, o->sring_l[m % 4], nullptr, nullptr, nullptr, dt));
+      HRW_CUDA(run_stage32(o, ST_EULER, um, um, o->sw1, nullptr, nullptr, nullptr, dt));
+      HRW_CUDA(run_stage32(o, ST_RK3B, o->sw1, um, o->sw2, nullptr, nullptr, nullptr, dt));
+      HRW_CUDA(run_stage32(o, ST_RK3C, o->sw2, um, un, nullptr, nullptr, nullptr, dt));
+      tt = tt + dt;  // ode_start%integrate(u, t, t + 2*dt, dt, itask=2): one step
+    }
+    o->level = 4;
+    o->fevals = 12;  // (:246)
+    o->nsteps += 4;
+    o->istate = 2;
+  } else {
+    HRW_CUDA(cudaMemcpyAsync(o->sring_u[o->level % 5], du, bytes, cudaMemcpyDeviceToDevice, o->stream));
+  }
+  int64_t n;
+  if (const int rc = count_ms_steps(tt, tout, dt, &n)) return rc;
+  auto ms_step = [&](int64_t m) {  // (:252-268)
+    float* um = o->sring_u[m % 5];
+    float* un = o->sring_u[(m + 1) % 5];  // holds u^{m-4}, overwritten in place
+    float* lm = o->sring_l[m % 4];        // holds L(u^{m-4}), overwritten in place
+    return run_stage32(o, ST_MS, um, um, un, lm, un, lm, dt);
+  };
+  int64_t s0 = 0;
+  if (o->use_graphs && n >= kMsPeriod) {
+    const int64_t m0 = o->level;
+    const int64_t G = n < 3 * kMsPeriod ? kMsPeriod : 3 * kMsPeriod;
+    bool ok = false;
+    HRW_CUDA(run_graph(o, o->sring_u[0], dt, m0 % kMsPeriod, G, n / G, &ok, [&]() {
+      for (int64_t s = 0; s < G; ++s) {
+        const cudaError_t e = ms_step(m0 + s);
+        if (e != cudaSuccess) return e;
+      }
+      return cudaSuccess;
+    }));
+    if (ok) {
+      s0 = n / G * G;
+      for (int64_t s = 0; s < s0; ++s) tt = tt + dt;
+      o->level = m0 + s0;
+    }
+  }
+  for (int64_t s = s0; s < n; ++s) {
+    HRW_CUDA(ms_step(o->level));
+    tt = tt + dt;
+    o->level = o->level + 1;
+  }
+  HRW_CUDA(cudaMemcpyAsync(du, o->sring_u[o->level % 5], bytes, cudaMemcpyDeviceToDevice, o->stream));
   *t = tt;
   o->fevals += (int)n;
   o->nsteps += n;
@@ -961,12 +1302,9 @@ static bool host_pipeline_ok(const hrw_ode* o, const void* u) {
 }
 
 static int rk3_integrate_host(hrw_ode* o, double* uh, double* t, double tout, double dt, int itask) {
-  double tt = *t;
-  int64_t n = 0;
-  do {  // the reference's time sequence (src/hrweno_tvdode.f90:137-143)
-    tt = tt + dt;
-    if (++n > kMaxSteps) return fail(HRW_EINVAL, "Invalid input 'dt': too many steps to reach tout.");
-  } while (!(is_done(tt, tout, dt) || itask == 2));
+  double tt;
+  int64_t n;
+  if (const int rc = count_steps(*t, tout, dt, itask, &n, &tt)) return rc;
   if (!o->copy) {
     for (cudaStream_t* st : {&o->pipe[0], &o->pipe[1], &o->copy})
       HRW_CUDA(cudaStreamCreateWithFlags(st, cudaStreamNonBlocking));
@@ -1047,14 +1385,38 @@ extern "C" int hrw_integrate(hrw_ode* o, int mem, void* u, double* t, double tou
   if (!u || !t) return fail(HRW_EINVAL, "Invalid input: null pointer.");
   if (mem != HRW_MEM_HOST && mem != HRW_MEM_DEVICE) return fail(HRW_EINVAL, "Invalid input 'mem'.");
   if (o->istate < 1) return fail(HRW_ESTATE, "ode is in an error state.");  // (:126,228)
-  if (is_done(*t, tout, dt)) return HRW_OK;                                  // (:127,229)
-  if (!(dt != 0.0) || !std::isfinite(dt) || !std::isfinite(*t) || !std::isfinite(tout))
-    return fail(HRW_EINVAL, "Invalid input 'dt': must be finite and nonzero.");
+  if (o->dtype == HRW_F32) {  // a REAL32 build holds t, tout and dt in FP32
+    const float tf = (float)*t, toutf = (float)tout, dtf = (float)dt;
+    if (is_done(tf, toutf, dtf)) return HRW_OK;  // (:127,229)
+    if (!(dtf != 0.0f) || !std::isfinite(dtf) || !std::isfinite(tf) || !std::isfinite(toutf))
+      return fail(HRW_EINVAL, "Invalid input 'dt': must be finite and nonzero.");
+  } else {
+    if (is_done(*t, tout, dt)) return HRW_OK;  // (:127,229)
+    if (!(dt != 0.0) || !std::isfinite(dt) || !std::isfinite(*t) || !std::isfinite(tout))
+      return fail(HRW_EINVAL, "Invalid input 'dt': must be finite and nonzero.");
+  }
   if (itask != 1 && itask != 2) itask = 1;
   const int rc = integrate_on(o, mem, u, t, tout, dt, itask);
   // a CUDA failure part-way leaves u (and the mstvd history) undefined: later calls refuse
   if (rc == HRW_ECUDA || rc == HRW_ENOMEM) o->istate = -1;
   return rc;
+}
+
+static int integrate_on32(hrw_ode* o, int mem, void* u, double* t, double tout, double dt, int itask) {
+  const size_t bytes = sizeof(float) * (size_t)o->neq;
+  float* du = (float*)u;
+  if (mem == HRW_MEM_HOST) {
+    du = o->su;
+    HRW_CUDA(cudaMemcpyAsync(du, u, bytes, cudaMemcpyHostToDevice, o->stream));
+  }
+  float tf = (float)*t;
+  const int rc = o->method == 0 ? rk_integrate32(o, du, &tf, (float)tout, (float)dt, itask)
+                                : ms_integrate32(o, du, &tf, (float)tout, (float)dt);
+  if (rc != HRW_OK) return rc;
+  *t = tf;
+  if (mem == HRW_MEM_HOST) HRW_CUDA(cudaMemcpyAsync(u, du, bytes, cudaMemcpyDeviceToHost, o->stream));
+  HRW_CUDA(cudaStreamSynchronize(o->stream));
+  return HRW_OK;
 }
 
 static int integrate_on(hrw_ode* o, int mem, void* u, double* t, double tout, double dt, int itask) {
@@ -1066,17 +1428,20 @@ static int integrate_on(hrw_ode* o, int mem, void* u, double* t, double tout, do
     HRW_CUDA(cudaStreamSynchronize(o->stream));
     return HRW_OK;
   }
-  if (mem == HRW_MEM_HOST) {
+  if (mem == HRW_MEM_HOST && o->dtype != HRW_F32) {
     du = o->u;
     HRW_CUDA(cudaMemcpyAsync(du, u, bytes, cudaMemcpyHostToDevice, o->stream));
   }
   int rc;
-  if (o->dtype == HRW_F32C)
+  if (o->dtype == HRW_F32)
+    rc = integrate_on32(o, mem, u, t, tout, dt, itask);
+  else if (o->dtype == HRW_F32C)
     rc = o->method == 0 ? rk_integrate_f32c(o, du, t, tout, dt, itask) : ms_integrate_f32c(o, du, t, tout, dt);
   else
     rc = o->method == 0 ? rk_integrate(o, du, t, tout, dt, itask) : ms_integrate(o, du, t, tout, dt);
   if (rc != HRW_OK) return rc;
-  if (mem == HRW_MEM_HOST) HRW_CUDA(cudaMemcpyAsync(u, du, bytes, cudaMemcpyDeviceToHost, o->stream));
+  if (mem == HRW_MEM_HOST && o->dtype != HRW_F32)
+    HRW_CUDA(cudaMemcpyAsync(u, du, bytes, cudaMemcpyDeviceToHost, o->stream));
   HRW_CUDA(cudaStreamSynchronize(o->stream));
   if (o->prob.kind == HRW_PROBLEM_FV2D) {
     bool timed_out = false;
@@ -1092,8 +1457,7 @@ static int integrate_on(hrw_ode* o, int mem, void* u, double* t, double tout, do
 extern "C" int hrw_rhs(const hrw_problem* p, int dtype, double t, const void* v, void* vdot, void* stream) {
   (void)t;
   if (!v || !vdot) return fail(HRW_EINVAL, "Invalid input: null pointer.");
-  if (dtype != HRW_F64 && dtype != HRW_F32C)
-    return fail(HRW_EINVAL, "Invalid input 'dtype': hrw_rhs supports HRW_F64 and HRW_F32C.");
+  if (dtype != HRW_F64 && dtype != HRW_F32C && dtype != HRW_F32) return fail(HRW_EINVAL, "Invalid input 'dtype'.");
   // cells in 64 bits: the arrays hold at most 2^31 - 1 elements (neq is an int in the ABI)
   const int64_t cells = !p ? 0
                         : p->kind == HRW_PROBLEM_FV2D ? (int64_t)p->ncells[0] * p->ncells[1]
@@ -1106,7 +1470,9 @@ extern "C" int hrw_rhs(const hrw_problem* p, int dtype, double t, const void* v,
   if (rc != HRW_OK) return rc;
   if (stream) o->stream = (cudaStream_t)stream;
   cudaError_t e;
-  if (dtype == HRW_F32C) {
+  if (dtype == HRW_F32) {
+    e = run_stage32(o, ST_RHS, (const float*)v, (const float*)v, (float*)vdot, nullptr, nullptr, nullptr, 0.0f);
+  } else if (dtype == HRW_F32C) {
     e = launch_split_f64((const double*)v, o->fhi[0], o->flo[0], neq, o->stream);
     if (e == cudaSuccess)
       e = run_f32c(o, FC_RHS, 0, nullptr, o->fd1, -1, nullptr, nullptr, nullptr, nullptr, 1.0);

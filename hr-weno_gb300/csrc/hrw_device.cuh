@@ -36,83 +36,98 @@ __device__ __forceinline__ double rcp_fast(double x) {
 __device__ __forceinline__ int hiword(double x) { return __double2hiint(x); }
 
 // ------------------------------------------------------------------------------------------
-// Reference tables (src/hrweno_weno.f90:11-21), used by the STRICT path and the guard path.
-// c(j, r) at [j + k*(r+1)].
+// One IEEE operation, round to nearest, never fused: the reference-order (STRICT and REAL32)
+// arithmetic in either precision.
 // ------------------------------------------------------------------------------------------
-template <int K> struct Tab;
-template <> struct Tab<1> {
-  __device__ static double d(int) { return 1.0; }
-  __device__ static double c(int, int) { return 1.0; }
+__device__ __forceinline__ double rn_add(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double rn_sub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double rn_mul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double rn_div(double a, double b) { return __ddiv_rn(a, b); }
+__device__ __forceinline__ float rn_add(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float rn_sub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float rn_mul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float rn_div(float a, float b) { return __fdiv_rn(a, b); }
+
+// ------------------------------------------------------------------------------------------
+// Reference tables (src/hrweno_weno.f90:11-21) in the real type T: each entry is the quotient
+// of two small integers rounded once to T, as the Fortran constant expressions (3._rk/10 ...)
+// give.  c(j, r) at [j + k*(r+1)].
+// ------------------------------------------------------------------------------------------
+template <int K, class T = double> struct Tab;
+template <class T> struct Tab<1, T> {
+  __device__ static T d(int) { return T(1); }
+  __device__ static T c(int, int) { return T(1); }
 };
-template <> struct Tab<2> {
-  __device__ static double d(int r) { return r == 0 ? 2.0 / 3 : 1.0 / 3; }
-  __device__ static double c(int j, int r) {
-    const double t[6] = {3.0 / 2, -1.0 / 2, 1.0 / 2, 1.0 / 2, -1.0 / 2, 3.0 / 2};
+template <class T> struct Tab<2, T> {
+  __device__ static T d(int r) { return r == 0 ? T(2) / T(3) : T(1) / T(3); }
+  __device__ static T c(int j, int r) {
+    const T t[6] = {T(3) / T(2), T(-1) / T(2), T(1) / T(2), T(1) / T(2), T(-1) / T(2), T(3) / T(2)};
     return t[j + 2 * (r + 1)];
   }
 };
-template <> struct Tab<3> {
-  __device__ static double d(int r) { return r == 0 ? 3.0 / 10 : (r == 1 ? 6.0 / 10 : 1.0 / 10); }
-  __device__ static double c(int j, int r) {
-    const double t[12] = {11.0 / 6, -7.0 / 6, 1.0 / 3,  1.0 / 3,  5.0 / 6,  -1.0 / 6,
-                          -1.0 / 6, 5.0 / 6,  1.0 / 3,  1.0 / 3,  -7.0 / 6, 11.0 / 6};
+template <class T> struct Tab<3, T> {
+  __device__ static T d(int r) { return r == 0 ? T(3) / T(10) : (r == 1 ? T(6) / T(10) : T(1) / T(10)); }
+  __device__ static T c(int j, int r) {
+    const T t[12] = {T(11) / T(6), T(-7) / T(6), T(1) / T(3),  T(1) / T(3),  T(5) / T(6),  T(-1) / T(6),
+                     T(-1) / T(6), T(5) / T(6),  T(1) / T(3),  T(1) / T(3),  T(-7) / T(6), T(11) / T(6)};
     return t[j + 3 * (r + 1)];
   }
 };
 
 // ------------------------------------------------------------------------------------------
-// STRICT reconstruction of one cell, reference order (src/hrweno_weno.f90:175-214).
-// p points at v(i); p[-(K-1)] .. p[K-1] must be valid (ghosts already substituted).
+// Reference-order reconstruction of one cell (src/hrweno_weno.f90:175-214), in double (STRICT)
+// or float (REAL32).  p points at v(i); p[-(K-1)] .. p[K-1] must be valid (ghosts already
+// substituted).
 // ------------------------------------------------------------------------------------------
-template <int K>
-__device__ __forceinline__ void recon_strict(const double* p, double eps, double& vl, double& vr) {
-  double vrr[K], vlr[K], beta[K];
+template <int K, class T>
+__device__ __forceinline__ void recon_strict(const T* p, T eps, T& vl, T& vr) {
+  T vrr[K], vlr[K], beta[K];
 #pragma unroll
   for (int r = 0; r < K; ++r) {
-    double sr = 0.0, sl = 0.0;
+    T sr = T(0), sl = T(0);
 #pragma unroll
     for (int j = 0; j < K; ++j) {
-      sr = __dadd_rn(sr, __dmul_rn(Tab<K>::c(j, r), p[j - r]));
-      sl = __dadd_rn(sl, __dmul_rn(Tab<K>::c(j, r - 1), p[j - r]));
+      sr = rn_add(sr, rn_mul(Tab<K, T>::c(j, r), p[j - r]));
+      sl = rn_add(sl, rn_mul(Tab<K, T>::c(j, r - 1), p[j - r]));
     }
     vrr[r] = sr;
     vlr[r] = sl;
   }
   if constexpr (K == 1) {
-    beta[0] = 0.0;
+    beta[0] = T(0);
   } else if constexpr (K == 2) {  // (src/hrweno_weno.f90:189-191)
-    double a = __dsub_rn(p[1], p[0]), b = __dsub_rn(p[0], p[-1]);
-    beta[0] = __dmul_rn(a, a);
-    beta[1] = __dmul_rn(b, b);
+    T a = rn_sub(p[1], p[0]), b = rn_sub(p[0], p[-1]);
+    beta[0] = rn_mul(a, a);
+    beta[1] = rn_mul(b, b);
   } else {  // (src/hrweno_weno.f90:194-202)
-    const double c13 = 13.0 / 12, c14 = 1.0 / 4;
-    double a, b;
-    a = __dadd_rn(__dsub_rn(p[0], __dmul_rn(2.0, p[1])), p[2]);
-    b = __dadd_rn(__dsub_rn(__dmul_rn(3.0, p[0]), __dmul_rn(4.0, p[1])), p[2]);
-    beta[0] = __dadd_rn(__dmul_rn(c13, __dmul_rn(a, a)), __dmul_rn(c14, __dmul_rn(b, b)));
-    a = __dadd_rn(__dsub_rn(p[-1], __dmul_rn(2.0, p[0])), p[1]);
-    b = __dsub_rn(p[-1], p[1]);
-    beta[1] = __dadd_rn(__dmul_rn(c13, __dmul_rn(a, a)), __dmul_rn(c14, __dmul_rn(b, b)));
-    a = __dadd_rn(__dsub_rn(p[-2], __dmul_rn(2.0, p[-1])), p[0]);
-    b = __dadd_rn(__dsub_rn(p[-2], __dmul_rn(4.0, p[-1])), __dmul_rn(3.0, p[0]));
-    beta[2] = __dadd_rn(__dmul_rn(c13, __dmul_rn(a, a)), __dmul_rn(c14, __dmul_rn(b, b)));
+    const T c13 = T(13) / T(12), c14 = T(1) / T(4);
+    T a, b;
+    a = rn_add(rn_sub(p[0], rn_mul(T(2), p[1])), p[2]);
+    b = rn_add(rn_sub(rn_mul(T(3), p[0]), rn_mul(T(4), p[1])), p[2]);
+    beta[0] = rn_add(rn_mul(c13, rn_mul(a, a)), rn_mul(c14, rn_mul(b, b)));
+    a = rn_add(rn_sub(p[-1], rn_mul(T(2), p[0])), p[1]);
+    b = rn_sub(p[-1], p[1]);
+    beta[1] = rn_add(rn_mul(c13, rn_mul(a, a)), rn_mul(c14, rn_mul(b, b)));
+    a = rn_add(rn_sub(p[-2], rn_mul(T(2), p[-1])), p[0]);
+    b = rn_add(rn_sub(p[-2], rn_mul(T(4), p[-1])), rn_mul(T(3), p[0]));
+    beta[2] = rn_add(rn_mul(c13, rn_mul(a, a)), rn_mul(c14, rn_mul(b, b)));
   }
-  double alfa[K], alfat[K];  // (src/hrweno_weno.f90:207-210)
-  double sa = 0.0, sat = 0.0;
+  T alfa[K], alfat[K];  // (src/hrweno_weno.f90:207-210)
+  T sa = T(0), sat = T(0);
 #pragma unroll
   for (int r = 0; r < K; ++r) {
-    double e = __dadd_rn(eps, beta[r]);
-    double e2 = __dmul_rn(e, e);
-    alfa[r] = __ddiv_rn(Tab<K>::d(r), e2);
-    alfat[r] = __ddiv_rn(Tab<K>::d(K - 1 - r), e2);
+    T e = rn_add(eps, beta[r]);
+    T e2 = rn_mul(e, e);
+    alfa[r] = rn_div(Tab<K, T>::d(r), e2);
+    alfat[r] = rn_div(Tab<K, T>::d(K - 1 - r), e2);
   }
 #pragma unroll
-  for (int r = 0; r < K; ++r) { sa = __dadd_rn(sa, alfa[r]); sat = __dadd_rn(sat, alfat[r]); }
-  double ar = 0.0, al = 0.0;  // (src/hrweno_weno.f90:213-214)
+  for (int r = 0; r < K; ++r) { sa = rn_add(sa, alfa[r]); sat = rn_add(sat, alfat[r]); }
+  T ar = T(0), al = T(0);  // (src/hrweno_weno.f90:213-214)
 #pragma unroll
   for (int r = 0; r < K; ++r) {
-    ar = __dadd_rn(ar, __dmul_rn(__ddiv_rn(alfa[r], sa), vrr[r]));
-    al = __dadd_rn(al, __dmul_rn(__ddiv_rn(alfat[r], sat), vlr[r]));
+    ar = rn_add(ar, rn_mul(rn_div(alfa[r], sa), vrr[r]));
+    al = rn_add(al, rn_mul(rn_div(alfat[r], sat), vlr[r]));
   }
   vr = ar;
   vl = al;
@@ -304,11 +319,10 @@ __device__ __forceinline__ void recon_fast_one(const double* p, double eps, doub
   vr = r[0];
 }
 
-// STRICT single cell with a stride: gathers p[o * stride] and runs the reference order.
-template <int K>
-__device__ __forceinline__ void recon_strict_strided(const double* p, int stride, double eps,
-                                                     double& vl, double& vr) {
-  double w[2 * K - 1];
+// Reference-order single cell with a stride: gathers p[o * stride].
+template <int K, class T>
+__device__ __forceinline__ void recon_strict_strided(const T* p, int stride, T eps, T& vl, T& vr) {
+  T w[2 * K - 1];
 #pragma unroll
   for (int q = 0; q < 2 * K - 1; ++q) w[q] = p[(q - (K - 1)) * stride];
   recon_strict<K>(w + (K - 1), eps, vl, vr);
@@ -320,18 +334,17 @@ __device__ __forceinline__ void recon_strict_strided(const double* p, int stride
 // c0[-(K-1)] .. c0[K-1] valid.  FAST: product-form weights as the uniform kernels; STRICT:
 // reference order.
 // ------------------------------------------------------------------------------------------
-template <int K, bool STRICT>
-__device__ __forceinline__ void recon_nu(const double* c0, const double* ci, double eps, double& vl,
-                                         double& vr) {
-  double vrr[K], vlr[K], beta[K];
+template <int K, bool STRICT, class T>
+__device__ __forceinline__ void recon_nu(const T* c0, const T* ci, T eps, T& vl, T& vr) {
+  T vrr[K], vlr[K], beta[K];
 #pragma unroll
   for (int r = 0; r < K; ++r) {
-    double sr = 0.0, sl = 0.0;
+    T sr = T(0), sl = T(0);
 #pragma unroll
     for (int j = 0; j < K; ++j) {
       if constexpr (STRICT) {
-        sr = __dadd_rn(sr, __dmul_rn(ci[j + K * (r + 1)], c0[j - r]));
-        sl = __dadd_rn(sl, __dmul_rn(ci[j + K * r], c0[j - r]));
+        sr = rn_add(sr, rn_mul(ci[j + K * (r + 1)], c0[j - r]));
+        sl = rn_add(sl, rn_mul(ci[j + K * r], c0[j - r]));
       } else {
         sr = fma(ci[j + K * (r + 1)], c0[j - r], sr);
         sl = fma(ci[j + K * r], c0[j - r], sl);
@@ -341,42 +354,41 @@ __device__ __forceinline__ void recon_nu(const double* c0, const double* ci, dou
     vlr[r] = sl;
   }
   if constexpr (STRICT) {
-    // reuse the uniform strict path for beta and weights by re-deriving from the same p
-    // (beta does not depend on the grid, src/hrweno_weno.f90:183-204)
+    // beta and the weights do not depend on the grid (src/hrweno_weno.f90:183-214)
     if constexpr (K == 1) {
-      beta[0] = 0.0;
+      beta[0] = T(0);
     } else if constexpr (K == 2) {
-      double a = __dsub_rn(c0[1], c0[0]), b = __dsub_rn(c0[0], c0[-1]);
-      beta[0] = __dmul_rn(a, a);
-      beta[1] = __dmul_rn(b, b);
+      T a = rn_sub(c0[1], c0[0]), b = rn_sub(c0[0], c0[-1]);
+      beta[0] = rn_mul(a, a);
+      beta[1] = rn_mul(b, b);
     } else {
-      const double c13 = 13.0 / 12, c14 = 1.0 / 4;
-      double a, b;
-      a = __dadd_rn(__dsub_rn(c0[0], __dmul_rn(2.0, c0[1])), c0[2]);
-      b = __dadd_rn(__dsub_rn(__dmul_rn(3.0, c0[0]), __dmul_rn(4.0, c0[1])), c0[2]);
-      beta[0] = __dadd_rn(__dmul_rn(c13, __dmul_rn(a, a)), __dmul_rn(c14, __dmul_rn(b, b)));
-      a = __dadd_rn(__dsub_rn(c0[-1], __dmul_rn(2.0, c0[0])), c0[1]);
-      b = __dsub_rn(c0[-1], c0[1]);
-      beta[1] = __dadd_rn(__dmul_rn(c13, __dmul_rn(a, a)), __dmul_rn(c14, __dmul_rn(b, b)));
-      a = __dadd_rn(__dsub_rn(c0[-2], __dmul_rn(2.0, c0[-1])), c0[0]);
-      b = __dadd_rn(__dsub_rn(c0[-2], __dmul_rn(4.0, c0[-1])), __dmul_rn(3.0, c0[0]));
-      beta[2] = __dadd_rn(__dmul_rn(c13, __dmul_rn(a, a)), __dmul_rn(c14, __dmul_rn(b, b)));
+      const T c13 = T(13) / T(12), c14 = T(1) / T(4);
+      T a, b;
+      a = rn_add(rn_sub(c0[0], rn_mul(T(2), c0[1])), c0[2]);
+      b = rn_add(rn_sub(rn_mul(T(3), c0[0]), rn_mul(T(4), c0[1])), c0[2]);
+      beta[0] = rn_add(rn_mul(c13, rn_mul(a, a)), rn_mul(c14, rn_mul(b, b)));
+      a = rn_add(rn_sub(c0[-1], rn_mul(T(2), c0[0])), c0[1]);
+      b = rn_sub(c0[-1], c0[1]);
+      beta[1] = rn_add(rn_mul(c13, rn_mul(a, a)), rn_mul(c14, rn_mul(b, b)));
+      a = rn_add(rn_sub(c0[-2], rn_mul(T(2), c0[-1])), c0[0]);
+      b = rn_add(rn_sub(c0[-2], rn_mul(T(4), c0[-1])), rn_mul(T(3), c0[0]));
+      beta[2] = rn_add(rn_mul(c13, rn_mul(a, a)), rn_mul(c14, rn_mul(b, b)));
     }
-    double alfa[K], alfat[K], sa = 0.0, sat = 0.0;
+    T alfa[K], alfat[K], sa = T(0), sat = T(0);
 #pragma unroll
     for (int r = 0; r < K; ++r) {
-      const double e = __dadd_rn(eps, beta[r]);
-      const double e2 = __dmul_rn(e, e);
-      alfa[r] = __ddiv_rn(Tab<K>::d(r), e2);
-      alfat[r] = __ddiv_rn(Tab<K>::d(K - 1 - r), e2);
+      const T e = rn_add(eps, beta[r]);
+      const T e2 = rn_mul(e, e);
+      alfa[r] = rn_div(Tab<K, T>::d(r), e2);
+      alfat[r] = rn_div(Tab<K, T>::d(K - 1 - r), e2);
     }
 #pragma unroll
-    for (int r = 0; r < K; ++r) { sa = __dadd_rn(sa, alfa[r]); sat = __dadd_rn(sat, alfat[r]); }
-    double ar = 0.0, al = 0.0;
+    for (int r = 0; r < K; ++r) { sa = rn_add(sa, alfa[r]); sat = rn_add(sat, alfat[r]); }
+    T ar = T(0), al = T(0);
 #pragma unroll
     for (int r = 0; r < K; ++r) {
-      ar = __dadd_rn(ar, __dmul_rn(__ddiv_rn(alfa[r], sa), vrr[r]));
-      al = __dadd_rn(al, __dmul_rn(__ddiv_rn(alfat[r], sat), vlr[r]));
+      ar = rn_add(ar, rn_mul(rn_div(alfa[r], sa), vrr[r]));
+      al = rn_add(al, rn_mul(rn_div(alfat[r], sat), vlr[r]));
     }
     vr = ar;
     vl = al;

@@ -17,37 +17,42 @@ enum StageKind : int {
   ST_RECON = 6   // out = vl, lout = vr                    (weno%reconstruct)
 };
 
-// One dimension of the problem as the kernels see it.
-struct LineArgs {
+// One dimension of the problem as the kernels see it.  T is the real type of the problem: double
+// for HRW_F64 handles, float for HRW_F32 handles (the REAL32 build of the reference; those run
+// the reference-order arithmetic only, so the FAST-only fields stay unset).
+template <class T>
+struct LineArgsT {
   int nc;
   int fn;        // HRW_FN_*
   int bc;        // HRW_BC_*
   int flux;      // HRW_FLUX_*
-  double a, b;   // LINEAR: g(x) = a + b x
-  double alpha;  // Lax-Friedrichs alpha
-  double xmin, rx;
+  T a, b;        // LINEAR: g(x) = a + b x
+  T alpha;       // Lax-Friedrichs alpha
+  T xmin, rx;
   // STRICT: divide by width (width[] or rx); FAST: multiply by rws (rws[] or rws0), which
   // already carries the flux scaling of the FAST flux form.
-  const double* width;
-  const double* rws;
-  double rws0;
-  const double* xe;  // non-uniform line: edges(0:nc) (x of interface e = xe[e]); null: uniform
+  const T* width;
+  const T* rws;
+  T rws0;
+  const T* xe;  // non-uniform line: edges(0:nc) (x of interface e = xe[e]); null: uniform
 };
+using LineArgs = LineArgsT<double>;
 
-struct StageArgs {
-  const double* v;    // stencil input
-  const double* u;    // u^n for RK2B / RK3B / RK3C
-  double* out;
-  double* lout;       // ST_MS: L(v); ST_RECON: vr
-  const double* uo4;  // ST_MS: u^{n-4}
-  const double* lo4;  // ST_MS: L(u^{n-4})
-  double eps, dt;
-  LineArgs L;
+template <class T>
+struct StageArgsT {
+  const T* v;    // stencil input
+  const T* u;    // u^n for RK2B / RK3B / RK3C
+  T* out;
+  T* lout;       // ST_MS: L(v); ST_RECON: vr
+  const T* uo4;  // ST_MS: u^{n-4}
+  const T* lo4;  // ST_MS: L(u^{n-4})
+  T eps, dt;
+  LineArgsT<T> L;
   // 2D only
-  LineArgs L2;
-  int64_t ld;         // row stride (nc1) of the 2D layout
-  int upwind;         // Godunov flux of g(x) u with g > 0 everywhere: F = g vm (2D kernel)
-  const double* cnu;  // non-uniform 1D line: weno coefficients cnu(0:k-1,-1:k-1,1:nc)
+  LineArgsT<T> L2;
+  int64_t ld;    // row stride (nc1) of the 2D layout
+  int upwind;    // Godunov flux of g(x) u with g > 0 everywhere: F = g vm (2D kernel)
+  const T* cnu;  // non-uniform 1D line: weno coefficients cnu(0:k-1,-1:k-1,1:nc)
   // uniform 1D line (stage1d_kernel): update only cells cell0 .. cell0 + ncell - 1 (ncell = 0:
   // the whole line); cell0 and ncell are multiples of the launch's tile (1024 cells for lines
   // of at least 2 x SMs x 1024 cells), so that ranges launched side by side write disjoint cells
@@ -59,6 +64,8 @@ struct StageArgs {
   // runs out (zero-initialised device memory; checked and cleared by the host after the call)
   unsigned int* timeout_flag;
 };
+using StageArgs = StageArgsT<double>;
+using StageArgs32 = StageArgsT<float>;
 
 // ---- compensated FP32 form (hrw_f32c.cuh, stage1d_f32c.cu) ---------------------------------
 enum F32CStage : int {
@@ -163,8 +170,9 @@ int device_sms();
 double fast_flux_scale(int flux, int fn);
 // Record msg as the calling thread's last error (hrw_last_error) and return code.
 int set_error(int code, const char* msg);
-// True when the line's flux is g(x) u with g > 0 at every interface (upwind Godunov).
-bool positive_velocity(const LineArgs& L);
+// True when the line's flux is g(x) u with g > 0 at every interface (upwind Godunov), with g
+// at the line ends above rel_margin (|a| + |b x|).
+bool positive_velocity(const LineArgs& L, double rel_margin = 1e-12);
 
 // 1D fused stage over nc cells; k in 1..3; strict selects the reference-order numerics.
 cudaError_t launch_stage1d(const StageArgs& a, int k, int stage, bool strict, cudaStream_t s);
@@ -180,5 +188,16 @@ cudaError_t launch_calc_cnu(const double* xedges, double* cnu, int nc, int k, cu
 // Reconstruction with per-cell coefficients (non-uniform grid).
 cudaError_t launch_recon_nonuniform(const double* v, const double* cnu, double* vl, double* vr,
                                     int nc, int k, double eps, bool strict, cudaStream_t s);
+
+// REAL32 (HRW_F32): the same kernels instantiated on float, always in the reference's operation
+// order (what a REAL32 build of the reference computes, src/hrweno_kinds.F90:9-10).
+cudaError_t launch_stage1d(const StageArgs32& a, int k, int stage, cudaStream_t s);
+cudaError_t launch_stage2d(const StageArgs32& a, int k, int stage, cudaStream_t s);
+cudaError_t launch_stage1d_nu(const StageArgs32& a, int k, int stage, cudaStream_t s);
+cudaError_t launch_stage_linear(const float* rates, const StageArgs32& a, int64_t n, int stage,
+                                cudaStream_t s);
+cudaError_t launch_calc_cnu(const float* xedges, float* cnu, int nc, int k, cudaStream_t s);
+cudaError_t launch_recon_nonuniform(const float* v, const float* cnu, float* vl, float* vr, int nc,
+                                    int k, float eps, cudaStream_t s);
 
 }  // namespace hrw

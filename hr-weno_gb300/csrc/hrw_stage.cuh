@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 
 #include "../../include/hrweno_gpu.h"
+#include "hrw_device.cuh"
 #include "hrw_internal.h"
 
 namespace hrw {
@@ -52,32 +53,37 @@ __device__ __forceinline__ double phys_fast(const LineArgs& L, double v, int64_t
   return s * (g_fast(L, e) * v);
 }
 
-// STRICT: reference order (src/hrweno_fluxes.f90:43,67-74; example1...f90:111-122).
-__device__ __forceinline__ double g_strict(const LineArgs& L, int64_t e) {
-  const double x = L.xe ? L.xe[e] : __dadd_rn(L.xmin, __dmul_rn(L.rx, (double)e));
-  return __dadd_rn(L.a, __dmul_rn(L.b, x));
+// Reference order (src/hrweno_fluxes.f90:43,67-74; example1...f90:111-122), in double (STRICT)
+// or float (REAL32).
+template <class T>
+__device__ __forceinline__ T g_strict(const LineArgsT<T>& L, int64_t e) {
+  const T x = L.xe ? L.xe[e] : rn_add(L.xmin, rn_mul(L.rx, (T)e));
+  return rn_add(L.a, rn_mul(L.b, x));
 }
-__device__ __forceinline__ double phys_strict(const LineArgs& L, double v, int64_t e) {
-  if (L.fn == HRW_FN_BURGERS) return __ddiv_rn(__dmul_rn(v, v), 2.0);
+template <class T>
+__device__ __forceinline__ T phys_strict(const LineArgsT<T>& L, T v, int64_t e) {
+  if (L.fn == HRW_FN_BURGERS) return rn_div(rn_mul(v, v), T(2));
   if (L.fn == HRW_FN_BURGERS_LINEAR)  // (u*u)/2 + (a + b*x)*u
-    return __dadd_rn(__ddiv_rn(__dmul_rn(v, v), 2.0), __dmul_rn(g_strict(L, e), v));
-  return __dmul_rn(g_strict(L, e), v);
+    return rn_add(rn_div(rn_mul(v, v), T(2)), rn_mul(g_strict(L, e), v));
+  return rn_mul(g_strict(L, e), v);
 }
-__device__ __forceinline__ double flux_strict(const LineArgs& L, double vm, double vp, int64_t e) {
-  const double fm = phys_strict(L, vm, e), fp = phys_strict(L, vp, e);
+template <class T>
+__device__ __forceinline__ T flux_strict(const LineArgsT<T>& L, T vm, T vp, int64_t e) {
+  const T fm = phys_strict(L, vm, e), fp = phys_strict(L, vp, e);
   if (L.flux == HRW_FLUX_LAX_FRIEDRICHS)
-    return __ddiv_rn(__dsub_rn(__dadd_rn(fm, fp), __dmul_rn(L.alpha, __dsub_rn(vp, vm))), 2.0);
+    return rn_div(rn_sub(rn_add(fm, fp), rn_mul(L.alpha, rn_sub(vp, vm))), T(2));
   if (vm <= vp) return fm < fp ? fm : fp;
   return fm > fp ? fm : fp;
 }
 
-template <bool STRICT>
-__device__ __forceinline__ double numflux(const LineArgs& L, double vm, double vp, int64_t e) {
+// FAST exists for double only; a float line always takes the reference order
+template <bool STRICT, class T>
+__device__ __forceinline__ T numflux(const LineArgsT<T>& L, T vm, T vp, int64_t e) {
   if constexpr (STRICT) return flux_strict(L, vm, vp, e);
   else return flux_fast(L, vm, vp, e);
 }
-template <bool STRICT>
-__device__ __forceinline__ double physflux(const LineArgs& L, double v, int64_t e) {
+template <bool STRICT, class T>
+__device__ __forceinline__ T physflux(const LineArgsT<T>& L, T v, int64_t e) {
   if constexpr (STRICT) return phys_strict(L, v, e);
   else return phys_fast(L, v, e);
 }
@@ -86,9 +92,9 @@ __device__ __forceinline__ double physflux(const LineArgs& L, double v, int64_t 
 // vm <= vp, rounding is monotone so fl(g vm) <= fl(g vp) and min() picks fl(g vm); for
 // vm > vp max() picks it too: the result is bit-identical to numflux<STRICT>() and needs
 // only the left state.
-template <bool STRICT>
-__device__ __forceinline__ double upwind_flux(const LineArgs& L, double vm, int64_t e) {
-  if constexpr (STRICT) return __dmul_rn(g_strict(L, e), vm);
+template <bool STRICT, class T>
+__device__ __forceinline__ T upwind_flux(const LineArgsT<T>& L, T vm, int64_t e) {
+  if constexpr (STRICT) return rn_mul(g_strict(L, e), vm);
   else return g_fast(L, e) * vm;
 }
 
@@ -96,18 +102,17 @@ __device__ __forceinline__ double upwind_flux(const LineArgs& L, double vm, int6
 //   COPY        F_{1/2} = F_{3/2}, F_{nc+1/2} = F_{nc-1/2}  (example1...f90:103-104)
 //   ZERO        F_{1/2} = F_{nc+1/2} = 0                    (example2...f90:117-120)
 //   ZERO_INFLOW F_{1/2} = 0, F_{nc+1/2} = f(vr(nc))
-template <bool STRICT>
-__device__ __forceinline__ double flux_diff(const LineArgs& L, int64_t j, double FL, double FR,
-                                            double vr_j) {
+template <bool STRICT, class T>
+__device__ __forceinline__ T flux_diff(const LineArgsT<T>& L, int64_t j, T FL, T FR, T vr_j) {
   if (j == 0 || j == L.nc - 1) {
     if (L.bc == HRW_BC_COPY) {
-      FL = FR = 0.0;
+      FL = FR = T(0);
     } else {
-      if (j == 0) FL = 0.0;
-      if (j == L.nc - 1) FR = L.bc == HRW_BC_ZERO ? 0.0 : physflux<STRICT>(L, vr_j, j + 1);
+      if (j == 0) FL = T(0);
+      if (j == L.nc - 1) FR = L.bc == HRW_BC_ZERO ? T(0) : physflux<STRICT>(L, vr_j, j + 1);
     }
   }
-  if constexpr (STRICT) return __dsub_rn(FR, FL);
+  if constexpr (STRICT) return rn_sub(FR, FL);
   else return FR - FL;
 }
 
@@ -116,24 +121,23 @@ __device__ __forceinline__ double flux_diff(const LineArgs& L, int64_t j, double
 // STRICT: udot is the exact right-hand side value, reference order.
 // FAST:   q = sum over dimensions of rws * dF (= -udot), or for 1D dF and rws separately.
 // --------------------------------------------------------------------------------------------
-template <int ST>
-__device__ __forceinline__ void combine_strict(const StageArgs& a, int64_t j, double v, double udot) {
-  const double dt = a.dt;
+template <int ST, class T>
+__device__ __forceinline__ void combine_strict(const StageArgsT<T>& a, int64_t j, T v, T udot) {
+  const T dt = a.dt;
   if constexpr (ST == ST_RHS) {
     a.out[j] = udot;
   } else if constexpr (ST == ST_EULER) {  // ui = u + dt*udot  (:139,150,163)
-    a.out[j] = __dadd_rn(v, __dmul_rn(dt, udot));
+    a.out[j] = rn_add(v, rn_mul(dt, udot));
   } else if constexpr (ST == ST_RK2B) {  // u = (u + ui + dt*udot)/2  (:152)
-    a.out[j] = __ddiv_rn(__dadd_rn(__dadd_rn(a.u[j], v), __dmul_rn(dt, udot)), 2.0);
+    a.out[j] = rn_div(rn_add(rn_add(a.u[j], v), rn_mul(dt, udot)), T(2));
   } else if constexpr (ST == ST_RK3B) {  // ui = (3*u + ui + dt*udot)/4  (:165)
-    a.out[j] = __ddiv_rn(__dadd_rn(__dadd_rn(__dmul_rn(3.0, a.u[j]), v), __dmul_rn(dt, udot)), 4.0);
+    a.out[j] = rn_div(rn_add(rn_add(rn_mul(T(3), a.u[j]), v), rn_mul(dt, udot)), T(4));
   } else if constexpr (ST == ST_RK3C) {  // u = (u + 2*ui + 2*dt*udot)/3  (:167)
-    a.out[j] = __ddiv_rn(
-        __dadd_rn(__dadd_rn(a.u[j], __dmul_rn(2.0, v)), __dmul_rn(__dmul_rn(2.0, dt), udot)), 3.0);
+    a.out[j] = rn_div(rn_add(rn_add(a.u[j], rn_mul(T(2), v)), rn_mul(rn_mul(T(2), dt), udot)), T(3));
   } else if constexpr (ST == ST_MS) {  // (25u + 50dt udot + 7 uold4 + 10dt udotold4)/32  (:257)
-    const double t1 = __dadd_rn(__dmul_rn(25.0, v), __dmul_rn(__dmul_rn(50.0, dt), udot));
-    const double t2 = __dadd_rn(t1, __dmul_rn(7.0, a.uo4[j]));
-    a.out[j] = __ddiv_rn(__dadd_rn(t2, __dmul_rn(__dmul_rn(10.0, dt), a.lo4[j])), 32.0);
+    const T t1 = rn_add(rn_mul(T(25), v), rn_mul(rn_mul(T(50), dt), udot));
+    const T t2 = rn_add(t1, rn_mul(T(7), a.uo4[j]));
+    a.out[j] = rn_div(rn_add(t2, rn_mul(rn_mul(T(10), dt), a.lo4[j])), T(32));
     a.lout[j] = udot;
   }
 }

@@ -21,6 +21,8 @@
 // Upwind specialisation (UPW): for the Godunov flux of f = g(x) u with g > 0 on the whole
 // domain in both directions, F = g vm exactly (hrw_stage.cuh: upwind_flux), so only the left
 // state vr of every interface is reconstructed.
+#include <type_traits>
+
 #include <cuda_runtime.h>
 
 #include "../../include/hrweno_gpu.h"
@@ -42,27 +44,29 @@ constexpr int kTileWaitPolls = 1 << 20;
 __device__ int g_tile_wait_limit = kTileWaitPolls;
 constexpr int BX = 40, BY = 38;  // TMA box of the tile plus halo: x from bx - 4, y from by - 3
 
-// TMA: the tile plus halo of the stage input comes in as one 40 x 38 box of doubles at
-// (bx - 4, by - 3) (x on a 16-byte boundary), completing on a block mbarrier; the block then
-// builds its padded tile from shared memory, replicating edge cells into the ghosts (the box
+// TMA: the tile plus halo of the stage input comes in as one 40 x 38 box at (bx - 4, by - 3)
+// (x on a 16-byte boundary for doubles and floats alike), completing on a block mbarrier; the
+// block then builds its padded tile from shared memory, replicating edge cells into the ghosts (the box
 // reads zeros outside the grid).  Otherwise every thread gathers the tile from global memory.
 // Both give the same tile, so the same bits.
-template <int K, int ST, bool STRICT, bool UPW, bool TMA>
-__global__ void __launch_bounds__(NT) stage2d_kernel(const __grid_constant__ CUtensorMap Mv, StageArgs a) {
+// R = double (HRW_F64, FAST or STRICT) or float (HRW_F32, reference order only).
+template <class R, int K, int ST, bool STRICT, bool UPW, bool TMA>
+__global__ void __launch_bounds__(NT) stage2d_kernel(const __grid_constant__ CUtensorMap Mv, StageArgsT<R> a) {
+  static_assert(STRICT || std::is_same<R, double>::value, "float grids take the reference order");
   constexpr int H = K;
   constexpr int RW = TX + 2 * H;      // loaded row width
   constexpr int SW = RW + 1;          // odd row stride: the x1 pass reads 32 rows per warp
   constexpr int SQ = TX + 1;          // odd stride of the parked x1 divergence
   constexpr int NSX = TX / C, NSY = TY / C;
-  __shared__ double sv[(TY + 2 * H) * SW];
-  __shared__ double sq[TY * SQ];
-  __shared__ double sLx[TY * (NSX + 1)], sRx[TY * (NSX + 1)];  // [row][segment edge]
-  __shared__ double sLy[(NSY + 1) * TX], sRy[(NSY + 1) * TX];  // [segment edge][column]
-  __shared__ alignas(128) double tbox[TMA ? BY * BX : 1];
+  __shared__ R sv[(TY + 2 * H) * SW];
+  __shared__ R sq[TY * SQ];
+  __shared__ R sLx[TY * (NSX + 1)], sRx[TY * (NSX + 1)];  // [row][segment edge]
+  __shared__ R sLy[(NSY + 1) * TX], sRy[(NSY + 1) * TX];  // [segment edge][column]
+  __shared__ alignas(128) R tbox[TMA ? BY * BX : 1];
   __shared__ alignas(8) uint64_t bar;
 
-  const LineArgs& L1 = a.L;
-  const LineArgs& L2 = a.L2;
+  const LineArgsT<R>& L1 = a.L;
+  const LineArgsT<R>& L2 = a.L2;
   const int64_t n1 = L1.nc, n2 = L2.nc, ld = a.ld;
   const int64_t bx = (int64_t)blockIdx.x * TX, by = (int64_t)blockIdx.y * TY;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -72,7 +76,7 @@ __global__ void __launch_bounds__(NT) stage2d_kernel(const __grid_constant__ CUt
     if (tid == 0) mbar_init(&bar);
     __syncthreads();
     if (tid == 0) {
-      mbar_expect_tx(&bar, BY * BX * 8);
+      mbar_expect_tx(&bar, BY * BX * (uint32_t)sizeof(R));
       tma_load_2d(tbox, &Mv, (int)bx - 4, (int)by - 3, &bar);
     }
     // bounded wait; on a timeout every thread of the block learns of it, the block waits
@@ -104,14 +108,14 @@ __global__ void __launch_bounds__(NT) stage2d_kernel(const __grid_constant__ CUt
 
   // ---- x1 reconstruction: row r = lane, segment sg = warp ------------------------------------
   const int r = lane, sg = warp;
-  double vl[C], vr[C];
+  R vl[C], vr[C];
   {
-    const double* row = &sv[(r + H) * SW + sg * C];  // row[q] = v(bx + sg*C - H + q)
+    const R* row = &sv[(r + H) * SW + sg * C];  // row[q] = v(bx + sg*C - H + q)
     if constexpr (STRICT) {
 #pragma unroll
       for (int c = 0; c < C; ++c) recon_strict<K>(row + H + c, a.eps, vl[c], vr[c]);
     } else {
-      double w[C + 2 * K];
+      R w[C + 2 * K];
 #pragma unroll
       for (int q = 0; q < C + 2 * K; ++q) w[q] = row[q];
       recon_fast<K, C, !UPW>(w, a.eps, vl, vr);
@@ -122,8 +126,8 @@ __global__ void __launch_bounds__(NT) stage2d_kernel(const __grid_constant__ CUt
   // tile-edge cells: warp 0 the left column (vr of x1 = bx-1), warp 1 the right column (vl of
   // x1 = bx+TX); warp 2 the row above (vr of x2 = by-1), warp 3 the row below (vl of by+TY)
   {
-    double el, er;
-    const double* p;
+    R el, er;
+    const R* p;
     int stride;
     if (warp < 2) {
       p = &sv[(lane + H) * SW + (warp == 0 ? H - 1 : H + TX)];
@@ -147,7 +151,7 @@ __global__ void __launch_bounds__(NT) stage2d_kernel(const __grid_constant__ CUt
   // ---- x1 fluxes of the segment; park the x1 divergence --------------------------------------
   {
     const int64_t j0 = bx + sg * C;
-    double F[C + 1];
+    R F[C + 1];
     if constexpr (UPW) {
       F[0] = upwind_flux<STRICT>(L1, sRx[r * (NSX + 1) + sg], j0);
 #pragma unroll
@@ -161,10 +165,10 @@ __global__ void __launch_bounds__(NT) stage2d_kernel(const __grid_constant__ CUt
 #pragma unroll
     for (int c = 0; c < C; ++c) {
       const int64_t gx = j0 + c;
-      double t = 0.0;
+      R t = R(0);
       if (gx < n1) {
-        const double dF = flux_diff<STRICT>(L1, gx, F[c], F[c + 1], vr[c]);
-        if constexpr (STRICT) t = __ddiv_rn(dF, L1.width ? L1.width[gx] : L1.rx);
+        const R dF = flux_diff<STRICT>(L1, gx, F[c], F[c + 1], vr[c]);
+        if constexpr (STRICT) t = rn_div(dF, L1.width ? L1.width[gx] : L1.rx);
         else t = (L1.rws ? L1.rws[gx] : L1.rws0) * dF;
       }
       sq[r * SQ + sg * C + c] = t;
@@ -174,12 +178,12 @@ __global__ void __launch_bounds__(NT) stage2d_kernel(const __grid_constant__ CUt
   // ---- x2 reconstruction: column = lane, segment sy = warp -----------------------------------
   const int col = lane, sy = warp;
   {
-    const double* cp = &sv[(sy * C) * SW + H + col];  // cp[q*SW] = v(x2 = by + sy*C - H + q)
+    const R* cp = &sv[(sy * C) * SW + H + col];  // cp[q*SW] = v(x2 = by + sy*C - H + q)
     if constexpr (STRICT) {
 #pragma unroll
       for (int c = 0; c < C; ++c) recon_strict_strided<K>(cp + (H + c) * SW, SW, a.eps, vl[c], vr[c]);
     } else {
-      double w[C + 2 * K];
+      R w[C + 2 * K];
 #pragma unroll
       for (int q = 0; q < C + 2 * K; ++q) w[q] = cp[q * SW];
       recon_fast<K, C, !UPW>(w, a.eps, vl, vr);
@@ -193,7 +197,7 @@ __global__ void __launch_bounds__(NT) stage2d_kernel(const __grid_constant__ CUt
   {
     const int64_t gx = bx + col;
     const int64_t j0 = by + sy * C;
-    double F[C + 1];
+    R F[C + 1];
     if constexpr (UPW) {
       F[0] = upwind_flux<STRICT>(L2, sRy[sy * TX + col], j0);
 #pragma unroll
@@ -209,15 +213,15 @@ __global__ void __launch_bounds__(NT) stage2d_kernel(const __grid_constant__ CUt
       for (int c = 0; c < C; ++c) {
         const int64_t gy = j0 + c;
         if (gy >= n2) break;
-        const double dF = flux_diff<STRICT>(L2, gy, F[c], F[c + 1], vr[c]);
+        const R dF = flux_diff<STRICT>(L2, gy, F[c], F[c + 1], vr[c]);
         const int ly = sy * C + c;
-        const double v = sv[(ly + H) * SW + H + col];
-        const double t1 = sq[ly * SQ + col];
+        const R v = sv[(ly + H) * SW + H + col];
+        const R t1 = sq[ly * SQ + col];
         const int64_t j = gy * ld + gx;
         if constexpr (STRICT) {
           // vdot = -((f1(i)-f1(i-1))/dx1) - (f2(j)-f2(j-1))/dx2   (example2...f90:123-127)
-          const double t2 = __ddiv_rn(dF, L2.width ? L2.width[gy] : L2.rx);
-          combine_strict<ST>(a, j, v, __dsub_rn(-t1, t2));
+          const R t2 = rn_div(dF, L2.width ? L2.width[gy] : L2.rx);
+          combine_strict<ST>(a, j, v, rn_sub(-t1, t2));
         } else {
           const double q = fma(L2.rws ? L2.rws[gy] : L2.rws0, dF, t1);
           combine_fast<ST>(a, j, v, q, 1.0);
@@ -227,35 +231,35 @@ __global__ void __launch_bounds__(NT) stage2d_kernel(const __grid_constant__ CUt
   }
 }
 
-template <int K, int ST, bool STRICT, bool UPW>
-cudaError_t launch_k(const StageArgs& a, cudaStream_t s) {
+template <class R, int K, int ST, bool STRICT, bool UPW>
+cudaError_t launch_k(const StageArgsT<R>& a, cudaStream_t s) {
   const dim3 grid((unsigned)((a.L.nc + TX - 1) / TX), (unsigned)((a.L2.nc + TY - 1) / TY));
   CUtensorMap mv{};
-  if (a.ld == a.L.nc && tile_map_2d(a.v, 8, (int)a.L.nc, (int)a.L2.nc, BX, BY, &mv))
-    stage2d_kernel<K, ST, STRICT, UPW, true><<<grid, NT, 0, s>>>(mv, a);
+  if (a.ld == a.L.nc && tile_map_2d(a.v, (int)sizeof(R), (int)a.L.nc, (int)a.L2.nc, BX, BY, &mv))
+    stage2d_kernel<R, K, ST, STRICT, UPW, true><<<grid, NT, 0, s>>>(mv, a);
   else
-    stage2d_kernel<K, ST, STRICT, UPW, false><<<grid, NT, 0, s>>>(mv, a);
+    stage2d_kernel<R, K, ST, STRICT, UPW, false><<<grid, NT, 0, s>>>(mv, a);
   return cudaGetLastError();
 }
 
-template <int K, bool STRICT, bool UPW>
-cudaError_t launch_st(const StageArgs& a, int stage, cudaStream_t s) {
+template <class R, int K, bool STRICT, bool UPW>
+cudaError_t launch_st(const StageArgsT<R>& a, int stage, cudaStream_t s) {
   switch (stage) {
-    case ST_RHS: return launch_k<K, ST_RHS, STRICT, UPW>(a, s);
-    case ST_EULER: return launch_k<K, ST_EULER, STRICT, UPW>(a, s);
-    case ST_RK2B: return launch_k<K, ST_RK2B, STRICT, UPW>(a, s);
-    case ST_RK3B: return launch_k<K, ST_RK3B, STRICT, UPW>(a, s);
-    case ST_RK3C: return launch_k<K, ST_RK3C, STRICT, UPW>(a, s);
-    case ST_MS: return launch_k<K, ST_MS, STRICT, UPW>(a, s);
+    case ST_RHS: return launch_k<R, K, ST_RHS, STRICT, UPW>(a, s);
+    case ST_EULER: return launch_k<R, K, ST_EULER, STRICT, UPW>(a, s);
+    case ST_RK2B: return launch_k<R, K, ST_RK2B, STRICT, UPW>(a, s);
+    case ST_RK3B: return launch_k<R, K, ST_RK3B, STRICT, UPW>(a, s);
+    case ST_RK3C: return launch_k<R, K, ST_RK3C, STRICT, UPW>(a, s);
+    case ST_MS: return launch_k<R, K, ST_MS, STRICT, UPW>(a, s);
   }
   return cudaErrorInvalidValue;
 }
 
-template <bool STRICT, bool UPW>
-cudaError_t launch_kk(const StageArgs& a, int k, int stage, cudaStream_t s) {
-  if (k == 1) return launch_st<1, STRICT, UPW>(a, stage, s);
-  if (k == 2) return launch_st<2, STRICT, UPW>(a, stage, s);
-  return launch_st<3, STRICT, UPW>(a, stage, s);
+template <class R, bool STRICT, bool UPW>
+cudaError_t launch_kk(const StageArgsT<R>& a, int k, int stage, cudaStream_t s) {
+  if (k == 1) return launch_st<R, 1, STRICT, UPW>(a, stage, s);
+  if (k == 2) return launch_st<R, 2, STRICT, UPW>(a, stage, s);
+  return launch_st<R, 3, STRICT, UPW>(a, stage, s);
 }
 
 }  // namespace
@@ -269,8 +273,15 @@ cudaError_t launch_stage2d(const StageArgs& a, int k, int stage, bool strict, cu
   if (a.L.nc <= 0 || a.L2.nc <= 0) return cudaSuccess;
   if (a.L2.nc > 65535LL * TY || !a.timeout_flag) return cudaErrorInvalidValue;
   const bool upw = a.upwind;
-  if (strict) return upw ? launch_kk<true, true>(a, k, stage, s) : launch_kk<true, false>(a, k, stage, s);
-  return upw ? launch_kk<false, true>(a, k, stage, s) : launch_kk<false, false>(a, k, stage, s);
+  using D = double;
+  if (strict) return upw ? launch_kk<D, true, true>(a, k, stage, s) : launch_kk<D, true, false>(a, k, stage, s);
+  return upw ? launch_kk<D, false, true>(a, k, stage, s) : launch_kk<D, false, false>(a, k, stage, s);
+}
+
+cudaError_t launch_stage2d(const StageArgs32& a, int k, int stage, cudaStream_t s) {
+  if (a.L.nc <= 0 || a.L2.nc <= 0) return cudaSuccess;
+  if (a.L2.nc > 65535LL * TY || !a.timeout_flag) return cudaErrorInvalidValue;
+  return a.upwind ? launch_kk<float, true, true>(a, k, stage, s) : launch_kk<float, true, false>(a, k, stage, s);
 }
 
 }  // namespace hrw

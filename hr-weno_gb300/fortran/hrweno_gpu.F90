@@ -19,14 +19,26 @@
 !> Each object holds a C handle that owns device memory; %destroy() frees it.  There is no
 !> final procedure: Fortran finalizes a constructor's function result once `ode = rktvd(...)`
 !> has copied it, which would free the handle just copied.
+!>
+!> The real kind rk of the arrays, eps and the times follows the reference's hrweno_kinds
+!> (src/hrweno_kinds.F90:8-17): REAL64 by default, REAL32 when preprocessed with -DREAL32, which
+!> selects the library's REAL32 handles (HRW_F32: everything held and computed in FP32, in the
+!> reference's operation order).  The adjoint, which the reference does not have, is REAL64.
 module hrweno_gpu
   use, intrinsic :: iso_c_binding
   implicit none
   private
-  public :: hrw_problem, hrw_problem_init, weno, rktvd, mstvd, adjoint, hrw_error_text
+  public :: hrw_problem, hrw_problem_init, weno, rktvd, mstvd, adjoint, hrw_error_text, rk
   public :: HRW_NUMERICS_FAST, HRW_NUMERICS_STRICT, HRW_NUMERICS_MIXED
 
-  integer(c_int), parameter :: HRW_F64 = 0, HRW_MEM_HOST = 0
+#ifdef REAL32
+  integer, parameter :: rk = c_float
+  integer(c_int), parameter :: HRW_RK = 1      ! HRW_F32
+#else
+  integer, parameter :: rk = c_double
+  integer(c_int), parameter :: HRW_RK = 0      ! HRW_F64
+#endif
+  integer(c_int), parameter :: HRW_MEM_HOST = 0
   integer(c_int32_t), parameter :: HRW_NUMERICS_FAST = 0, HRW_NUMERICS_STRICT = 1, &
                                    HRW_NUMERICS_MIXED = 2
 
@@ -188,29 +200,31 @@ contains
   function weno_new(ncells, k, eps, xedges) result(self)
     integer, intent(in) :: ncells
     integer, intent(in), optional :: k
-    real(c_double), intent(in), optional :: eps
-    real(c_double), intent(in), optional, target, contiguous :: xedges(0:)  ! xedges(0:ncells)
+    real(rk), intent(in), optional :: eps
+    real(rk), intent(in), optional :: xedges(0:)  ! xedges(0:ncells)
     type(weno) :: self
     integer(c_int) :: kk
     real(c_double) :: ee
+    real(c_double), allocatable, target :: xe64(:)
     type(c_ptr) :: xe
     kk = 0                                 ! 0 / 0.0: the reference's defaults (3, 1e-6)
     if (present(k)) kk = k
     ee = 0
-    if (present(eps)) ee = eps
+    if (present(eps)) ee = eps             ! a REAL32 value is exact in FP64
     xe = c_null_ptr
     if (present(xedges)) then              ! the reference's size check (src/hrweno_weno.f90:100-109)
       if (size(xedges) /= ncells + 1) error stop "Invalid input 'xedges': size(xedges) /= ncells + 1."
-      xe = c_loc(xedges)
+      xe64 = real(xedges, c_double)        ! the library copies the edges at creation
+      xe = c_loc(xe64)
     end if
     call check(c_weno_create(ncells, kk, ee, xe, self%h))
   end function
 
   subroutine weno_reconstruct(self, v, vl, vr)
     class(weno), intent(in) :: self
-    real(c_double), intent(in), target, contiguous :: v(:)
-    real(c_double), intent(out), target, contiguous :: vl(:), vr(:)
-    call check(c_weno_reconstruct(self%h, HRW_F64, HRW_MEM_HOST, c_loc(v), c_loc(vl), c_loc(vr)))
+    real(rk), intent(in), target, contiguous :: v(:)
+    real(rk), intent(out), target, contiguous :: vl(:), vr(:)
+    call check(c_weno_reconstruct(self%h, HRW_RK, HRW_MEM_HOST, c_loc(v), c_loc(vl), c_loc(vr)))
   end subroutine
 
   subroutine weno_destroy(self)
@@ -223,26 +237,30 @@ contains
     type(hrw_problem), intent(in) :: p
     integer, intent(in) :: neq, order      ! order 1..3, required as in src/hrweno_tvdode.f90:75
     type(rktvd) :: self
-    call check(c_rktvd_create(p, neq, order, HRW_F64, self%h))
+    call check(c_rktvd_create(p, neq, order, HRW_RK, self%h))
   end function
 
   function mstvd_new(p, neq) result(self)
     type(hrw_problem), intent(in) :: p
     integer, intent(in) :: neq
     type(mstvd) :: self
-    call check(c_mstvd_create(p, neq, HRW_F64, self%h))
+    call check(c_mstvd_create(p, neq, HRW_RK, self%h))
   end function
 
   subroutine ode_integrate(self, u, t, tout, dt, itask)
     class(rktvd), intent(inout) :: self
-    real(c_double), intent(inout), target, contiguous :: u(:)
-    real(c_double), intent(inout) :: t
-    real(c_double), intent(in) :: tout, dt
+    real(rk), intent(inout), target, contiguous :: u(:)
+    real(rk), intent(inout) :: t
+    real(rk), intent(in) :: tout, dt
     integer, intent(in), optional :: itask
     integer(c_int) :: it
+    real(c_double) :: tt
     it = 1
     if (present(itask)) it = itask
-    call check(c_integrate(self%h, HRW_MEM_HOST, c_loc(u), t, tout, dt, it))
+    tt = t                                 ! the library returns an FP32 time exactly for HRW_F32
+    call check(c_integrate(self%h, HRW_MEM_HOST, c_loc(u), tt, real(tout, c_double), &
+                           real(dt, c_double), it))
+    t = real(tt, rk)
   end subroutine
 
   integer function ode_fevals(self)

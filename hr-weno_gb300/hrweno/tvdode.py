@@ -11,18 +11,27 @@ from . import _abi as A
 from ._arrays import describe
 from .problems import Problem
 
-# "f64": the FP64 method; "f32c": compensated FP32 bulk precision (user arrays stay float64)
+# "f64": the FP64 method; "f32": a REAL32 build of the reference (float32 arrays, FP32 time);
+# "f32c": compensated FP32 bulk precision (user arrays stay float64)
 _DT = {"f64": A.HRW_F64, "f32": A.HRW_F32, "f32c": A.HRW_F32C}
 
 
 class _tvdode:
-    def __init__(self, h, problem: Problem, neq: int):
+    dtype = "f64"
+
+    def __init__(self, h, problem: Problem, neq: int, dtype: str):
         self._h = h
         self.problem = problem
         self.neq = neq
+        self.dtype = dtype
 
     def integrate(self, u, t: float, tout: float, dt: float, itask: int = 1) -> float:
-        mem, p, _ = describe(u, self.neq, True)
+        """For dtype "f32" u is float32 and t, tout, dt are rounded to FP32 (the returned t is
+        the FP32 time, exactly)."""
+        real32 = self.dtype == "f32"
+        mem, p, d = describe(u, self.neq, True, f64_only=not real32)
+        if real32 and d != A.HRW_F32:
+            raise TypeError("a REAL32 (dtype 'f32') integrator takes float32 arrays")
         tt = C.c_double(t)
         A.check(A.lib().hrw_integrate(self._h, mem, p, C.byref(tt), float(tout), float(dt),
                                       int(itask)))
@@ -68,7 +77,7 @@ class rktvd(_tvdode):  # noqa: N801
         self._cp = problem.to_c()
         A.check(A.lib().hrw_rktvd_create(C.byref(self._cp), int(neq), int(order), _DT[dtype],
                                          C.byref(h)))
-        super().__init__(h, problem, int(neq))
+        super().__init__(h, problem, int(neq), dtype)
         self.order = int(order)
 
 
@@ -79,5 +88,5 @@ class mstvd(_tvdode):  # noqa: N801
         h = C.c_void_p()
         self._cp = problem.to_c()
         A.check(A.lib().hrw_mstvd_create(C.byref(self._cp), int(neq), _DT[dtype], C.byref(h)))
-        super().__init__(h, problem, int(neq))
+        super().__init__(h, problem, int(neq), dtype)
         self.order = 3

@@ -45,7 +45,12 @@ enum {
 
 /* ---- element type and memory space of user arrays -------------------------------- */
 /* HRW_F64:  the FP64 method itself; user arrays are doubles.
- * HRW_F32:  reserved for the REAL32 build of the reference (src/hrweno_kinds.F90:9-10).
+ * HRW_F32:  what a REAL32 build of the reference computes (rk = real32, src/hrweno_kinds.F90:9-10):
+ *           user arrays are floats; eps, the grid, cnu, the state, every stage and the time
+ *           t, tout, dt are held in FP32 and computed in the reference's operation order (the
+ *           numerics field is ignored), so results are bit-identical to an FP32 CPU build of
+ *           the reference's formulas.  Integrators, reconstruct and hrw_rhs; all problem kinds.
+ *           The *t of hrw_integrate is rounded to FP32 on entry and returned exactly.
  * HRW_F32C: compensated FP32 bulk precision (FV1D and FV2D): user arrays stay doubles; inside,
  *           the state is a float pair hi + lo and the right-hand side is evaluated in FP32 in
  *           difference form (compensated neighbour differences, flux differences relative
@@ -127,7 +132,8 @@ typedef struct hrw_weno hrw_weno;
 int hrw_weno_create(int ncells, int k, double eps, const double* xedges, hrw_weno** out);
 /* Select HRW_NUMERICS_FAST (default) or HRW_NUMERICS_STRICT for later reconstructions. */
 int hrw_weno_set_numerics(hrw_weno* w, int numerics);
-/* w%reconstruct(v, vl, vr): arrays of ncells elements of `dtype` in memory space `mem`. */
+/* w%reconstruct(v, vl, vr): arrays of ncells elements of `dtype` (HRW_F64, or HRW_F32 for the
+ * REAL32 reconstruction, which needs eps > epsilon(1.0_real32)) in memory space `mem`. */
 int hrw_weno_reconstruct(hrw_weno* w, int dtype, int mem, const void* v, void* vl, void* vr);
 /* Copy the non-uniform coefficients cnu(0:k-1,-1:k-1,1:nc), Fortran order, to the host. */
 int hrw_weno_cnu(const hrw_weno* w, double* cnu_host);
@@ -136,13 +142,16 @@ int hrw_weno_destroy(hrw_weno* w);
 /* ---- TVD ODE integrators (rktvd / mstvd types) ------------------------------------ */
 typedef struct hrw_ode hrw_ode;
 
-/* rktvd(fu, neq, order): order 1..3; dtype HRW_F64 (the method itself) or HRW_F32C
- * (compensated FP32 bulk precision, FV1D and FV2D problems; the user array stays FP64). */
+/* rktvd(fu, neq, order): order 1..3; dtype HRW_F64 (the method itself), HRW_F32 (a REAL32
+ * build) or HRW_F32C (compensated FP32 bulk precision, FV1D and FV2D problems; the user array
+ * stays FP64). */
 int hrw_rktvd_create(const hrw_problem* p, int neq, int order, int dtype, hrw_ode** out);
 /* mstvd(fu, neq): 5-step, 3rd-order TVD multistep with an RK3 start. */
 int hrw_mstvd_create(const hrw_problem* p, int neq, int dtype, hrw_ode** out);
 /* ode%integrate(u, t, tout, dt[, itask]): u (neq elements of the ode's dtype) is updated
- * in place, *t advances like the reference (it stops at the first step with t > tout).
+ * in place, *t advances like the reference (it stops at the first step with t > tout).  A dt
+ * too small to change t (t + dt == t in the handle's precision) returns HRW_EINVAL, where the
+ * reference would never return.
  * itask: 1 normal integration until tout, 2 single step.  A CUDA failure part-way leaves u
  * undefined and puts the handle in the error state (istate = -1; later calls return
  * HRW_ESTATE), as the reference's integrate refuses to continue after an error. */
@@ -161,8 +170,8 @@ int hrw_ode_destroy(hrw_ode* ode);
 
 /* ---- right-hand side alone (fu of the reference's driver) -------------------------- */
 /* vdot = L(v) at time t for problem p, both arrays device pointers of doubles
- * (LINEAR_ODE: neq = ncells[0]); dtype HRW_F64, or HRW_F32C to evaluate L in the
- * compensated FP32 form (FV1D and FV2D problems). */
+ * (LINEAR_ODE: neq = ncells[0]); dtype HRW_F64, HRW_F32C to evaluate L in the compensated
+ * FP32 form (FV1D and FV2D problems), or HRW_F32 with float arrays (a REAL32 build). */
 int hrw_rhs(const hrw_problem* p, int dtype, double t, const void* v, void* vdot, void* stream);
 
 /* ---- batches of independent 1D problems ------------------------------------------- */

@@ -348,13 +348,21 @@ struct Problem {
 // ---------------------------------------------------------------------------------------
 // TVD ODE integrators (src/hrweno_tvdode.f90).
 // ---------------------------------------------------------------------------------------
-// is_done (src/hrweno_tvdode.f90:273-284); time stays FP64 in every precision
-static bool is_done(double t, double tout, double dt) {
-  return (t - tout) * std::copysign(1.0, dt) > 0.0;
+// The time type of each build: a REAL32 build holds t, tout and dt in real32 like everything
+// else (src/hrweno_kinds.F90:9-10, src/hrweno_tvdode.f90:97-135); the REAL64 build and the
+// REAL128 yardstick (used for the precision of the state only) keep them in FP64.
+template <class T> struct TimeOf { using type = double; };
+template <> struct TimeOf<float> { using type = float; };
+
+// is_done (src/hrweno_tvdode.f90:273-284)
+template <class R>
+static bool is_done(R t, R tout, R dt) {
+  return (t - tout) * std::copysign(R(1), dt) > R(0);
 }
 
 template <class T>
 struct ODE {
+  using Time = typename TimeOf<T>::type;
   Problem<T> prob;
   int neq, order, method;  // method 0 rktvd, 1 mstvd
   int fevals = 0, istate = 0;
@@ -374,7 +382,7 @@ struct ODE {
   }
 
   // one step of rktvd (src/hrweno_tvdode.f90:136-171)
-  void rk_step(T* u, double& t, double dt, int& fe) {
+  void rk_step(T* u, Time& t, Time dt, int& fe) {
     const int n = neq;
     const T dtt = (T)dt;
     if (order == 1) {  // (:137-143)
@@ -407,7 +415,7 @@ struct ODE {
   }
 
   // rktvd_integrate (src/hrweno_tvdode.f90:97-178)
-  void rk_integrate(T* u, double& t, double tout, double dt, int itask) {
+  void rk_integrate(T* u, Time& t, Time tout, Time dt, int itask) {
     if (istate < 1) return;  // (:126)
     if (is_done(t, tout, dt)) return;  // (:127)
     for (;;) {
@@ -418,7 +426,7 @@ struct ODE {
   }
 
   // mstvd_integrate (src/hrweno_tvdode.f90:203-271)
-  void ms_integrate(T* u, double& t, double tout, double dt) {
+  void ms_integrate(T* u, Time& t, Time tout, Time dt) {
     const int n = neq;
     if (istate < 1) return;  // (:228)
     if (is_done(t, tout, dt)) return;  // (:229)
@@ -509,11 +517,14 @@ static int reconstruct_T(int nc, int k, double eps, const double* xedges, const 
 
 template <class T>
 static int integrate_T(Handle* h, double* u, double* t, double tout, double dt, int itask) {
+  using Time = typename ODE<T>::Time;
   ODE<T>* o = (ODE<T>*)h->ode;
   std::vector<T> tu(o->neq);
   to_T(u, tu.data(), o->neq);
-  if (o->method == 0) o->rk_integrate(tu.data(), *t, tout, dt, itask);
-  else o->ms_integrate(tu.data(), *t, tout, dt);
+  Time tt = (Time)*t;
+  if (o->method == 0) o->rk_integrate(tu.data(), tt, (Time)tout, (Time)dt, itask);
+  else o->ms_integrate(tu.data(), tt, (Time)tout, (Time)dt);
+  *t = (double)tt;
   to_D(tu.data(), u, o->neq);
   return 0;
 }

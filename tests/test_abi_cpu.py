@@ -67,7 +67,7 @@ def _header_problem_fields():
 
 def test_problem_layouts_agree():
     """struct hrw_problem, its ctypes mirror and the Fortran bind(c) type of the binding module
-    (hr-weno_gb300/fortran/hrweno_gpu.f90) list the same fields in the same order (a missing
+    (hr-weno_gb300/fortran/hrweno_gpu.F90) list the same fields in the same order (a missing
     field shifts every later one)."""
     import re
     import ctypes as C
@@ -75,7 +75,7 @@ def test_problem_layouts_agree():
     hdr = _header_problem_fields()
     cty = [(name, getattr(t, "_length_", 1)) for name, t in _abi.HrwProblem._fields_]
     assert hdr == cty, (hdr, cty)
-    text = (ROOT / "hr-weno_gb300" / "fortran" / "hrweno_gpu.f90").read_text()
+    text = (ROOT / "hr-weno_gb300" / "fortran" / "hrweno_gpu.F90").read_text()
     block = text[text.index("type, bind(c) :: hrw_problem"):]
     block = block[:block.index("end type")]
     fort = []
@@ -112,6 +112,31 @@ def test_f32c_rejects_burgers_linear(hw):
                       coef_a=(0.5, 0.0), xmin=(-1.0, 0.0), xmax=(1.0, 1.0))
     with pytest.raises(HrwError, match=r"HRW_F32C supports BURGERS and LINEAR"):
         hw.rktvd(prob, 100, 3, dtype="f32c")
+
+
+def test_real32_validation_before_any_cuda_call(hw):
+    """A REAL32 handle (dtype "f32") applies the reference's checks to the FP32 values a REAL32
+    build holds: eps > epsilon(1.0_real32) (src/hrweno_weno.f90:92) and a grid that stays valid
+    once rounded to FP32.  Validation runs before any CUDA call, so this needs no GPU."""
+    from hrweno import HrwError
+    ok = hw.burgers_1d(100, eps=1e-6)
+    tiny_eps = hw.burgers_1d(100, eps=1e-8)  # valid in REAL64
+    with pytest.raises(HrwError, match=r"Invalid input 'eps'. Valid range: eps > epsilon."):
+        hw.rktvd(tiny_eps, 100, 3, dtype="f32")
+    with pytest.raises(HrwError, match=r"Invalid input 'eps'. Valid range: eps > epsilon."):
+        hw.mstvd(tiny_eps, 100, dtype="f32")
+    # edges 1e-9 apart around 1 are distinct doubles but one FP32 value
+    xe = 1.0 + 1e-9 * np.arange(11)
+    collapsed = hw.Problem(kind="fv1d", ncells=(10, 1), xedges=(xe, None))
+    with pytest.raises(HrwError, match=r"edges must increase in REAL32"):
+        hw.rktvd(collapsed, 10, 3, dtype="f32")
+    narrow = hw.Problem(kind="fv1d", ncells=(10, 1), xmin=(1.0, 0.0), xmax=(1.0 + 1e-9, 1.0))
+    with pytest.raises(HrwError, match=r"xmax > xmin must hold in REAL32"):
+        hw.rktvd(narrow, 10, 3, dtype="f32")
+    thin = hw.burgers_1d(10, width=np.full(10, 1e-50))
+    with pytest.raises(HrwError, match=r"widths must be > 0 in REAL32"):
+        hw.rktvd(thin, 10, 3, dtype="f32")
+    assert ok.eps == 1e-6
 
 
 def test_last_error_is_per_thread(hw):
@@ -213,7 +238,7 @@ def test_fortran_binding_names_exist():
     """Every C entry point the Fortran module binds (bind(c, name=...)) is declared in the
     header and exported by the library; the module keeps the reference's type names."""
     import re
-    text = (ROOT / "hr-weno_gb300" / "fortran" / "hrweno_gpu.f90").read_text()
+    text = (ROOT / "hr-weno_gb300" / "fortran" / "hrweno_gpu.F90").read_text()
     hdr = (ROOT / "include" / "hrweno_gpu.h").read_text()
     names = re.findall(r'bind\(c,\s*name="(\w+)"\)', text)
     assert len(names) >= 10

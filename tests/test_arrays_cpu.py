@@ -52,6 +52,9 @@ def test_integrate_rejects_float32_before_the_library(hw):
     ode._h, ode.neq = None, 8
     with pytest.raises(TypeError, match="float64"):
         ode.integrate(np.zeros(8, dtype=np.float32), 0.0, 1.0, 0.1)
+    ode.dtype = "f32"  # a REAL32 integrator takes float32 only
+    with pytest.raises(TypeError, match="float32"):
+        ode.integrate(np.zeros(8), 0.0, 1.0, 0.1)
     b = object.__new__(hw.batch)
     b._h, b.offsets, b.nprob = None, np.array([0, 8]), 1
     with pytest.raises(TypeError, match="float64"):

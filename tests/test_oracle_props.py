@@ -258,3 +258,23 @@ def test_results_do_not_depend_on_the_thread_count(orc):
             assert np.array_equal(a, b)
     finally:
         orc.set_threads(before)
+
+
+def test_real32_oracle_keeps_time_in_fp32(orc):
+    """The oracle's float instantiation is a REAL32 build: t, tout and dt are FP32 and t
+    advances by FP32 additions (src/hrweno_kinds.F90:9-10, src/hrweno_tvdode.f90:170-171), so
+    the step count and the final t follow FP32 arithmetic, not FP64."""
+    from hrweno import linear_ode
+    prob = linear_ode(np.full(4, -1.0))
+    for dt, tout in ((0.1, 1.0), (0.01, 12.0), (1e-3, 0.5)):
+        o = orc.ODE(prob, 4, 0, 3, prec=32)
+        u = np.ones(4)
+        t = o.integrate(u, 0.0, tout, dt)
+        t32, n = np.float32(0.0), 0
+        while not (t32 - np.float32(tout)) > 0:
+            t32 = np.float32(t32 + np.float32(dt))
+            n += 1
+        assert t == float(t32) and o.info()[2] == n
+        o64 = orc.ODE(prob, 4, 0, 3, prec=64)
+        t64 = o64.integrate(np.ones(4), 0.0, tout, dt)
+        assert t64 != t  # FP64 time takes other values
