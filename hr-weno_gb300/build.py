@@ -37,6 +37,11 @@ ORACLE_FLAGS = ["-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared", "-st
 ORACLE_BASELINE_LIB = ROOT / "oracle" / "_build" / "libhrweno_oracle_o3.so"
 ORACLE_BASELINE_FLAGS = ["-O3", "-fopenmp", "-fPIC", "-shared", "-std=c++17"]
 NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
+# sources whose kernel instantiations are split over several objects, each compiled with
+# -DHRW_PART=i, so that the longest translation units build in parallel
+PARTS = {"stage2d.cu": 9}
+# the slowest units first, so that they do not start last
+SLOW_FIRST = ["stage2d.cu", "batch.cu", "stage1d_f32c.cu", "stage2d_f32c.cu", "stage1d.cu"]
 
 
 def _run(cmd: list[str]) -> None:
@@ -55,15 +60,19 @@ def _stale(out: Path, deps: list[Path]) -> bool:
 def build_lib(force: bool = False) -> Path:
     BUILD.mkdir(exist_ok=True)
     LIBDIR.mkdir(parents=True, exist_ok=True)
-    sources = sorted(CSRC.glob("*.cu"))
+    sources = sorted(CSRC.glob("*.cu"),
+                     key=lambda p: (SLOW_FIRST.index(p.name) if p.name in SLOW_FIRST else len(SLOW_FIRST), p.name))
     headers = sorted(CSRC.glob("*.cuh")) + sorted(CSRC.glob("*.h")) + [ROOT / "include" / "hrweno_gpu.h"]
     jobs = []
     objs = []
     for src in sources:
-        obj = BUILD / (src.stem + ".o")
-        objs.append(obj)
-        if force or _stale(obj, [src] + headers):
-            jobs.append([NVCC, *ARCH, *NVFLAGS, "-c", str(src), "-o", str(obj)])
+        n = PARTS.get(src.name, 0)
+        for part in range(n) if n else [None]:
+            obj = BUILD / (src.stem + (f".p{part}" if part is not None else "") + ".o")
+            objs.append(obj)
+            if force or _stale(obj, [src] + headers):
+                extra = [f"-DHRW_PART={part}"] if part is not None else []
+                jobs.append([NVCC, *ARCH, *NVFLAGS, *extra, "-c", str(src), "-o", str(obj)])
     if jobs:
         with ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:
             list(ex.map(_run, jobs))

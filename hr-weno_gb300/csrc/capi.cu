@@ -84,8 +84,6 @@ int validate_problem(const hrw_problem* p, int neq) {
     if (p->bc[d] < HRW_BC_COPY || p->bc[d] > HRW_BC_ZERO_INFLOW)
       return fail(HRW_EINVAL, "Invalid input 'bc'.");
     if (p->xedges[d]) {
-      if (p->kind != HRW_PROBLEM_FV1D)
-        return fail(HRW_EINVAL, "Invalid input 'xedges': non-uniform lines are supported for FV1D.");
       if (p->width[d]) return fail(HRW_EINVAL, "Invalid input: give either 'xedges' or 'width'.");
       for (int i = 0; i < p->ncells[d]; ++i)
         if (!(p->xedges[d][i + 1] > p->xedges[d][i]))
@@ -354,7 +352,7 @@ static cudaError_t setup_f32(hrw_ode* o, const hrw_problem* p) {
         if ((e = cudaStreamSynchronize(o->own)) != cudaSuccess) return e;
         L.xe = dxe;
         L.width = dw;
-        b.cnu = cnu;
+        (d == 0 ? b.cnu : b.cnu2) = cnu;
       }
     }
     b.ld = p->ncells[0];
@@ -521,7 +519,7 @@ static int ode_create(const hrw_problem* p, int neq, int order, int method, int 
   if (dtype == HRW_F32 && (rc = validate_problem_f32(p)) != HRW_OK) return rc;
   if (dtype == HRW_F32C) {
     if (p->xedges[0] || p->xedges[1])
-      return fail(HRW_EINVAL, "Invalid input 'xedges': non-uniform lines are supported for HRW_F64.");
+      return fail(HRW_EINVAL, "Invalid input 'xedges': non-uniform lines are supported for HRW_F64 and HRW_F32.");
     if (p->kind != HRW_PROBLEM_FV1D && p->kind != HRW_PROBLEM_FV2D)
       return fail(HRW_EINVAL, "Invalid input 'dtype': HRW_F32C supports FV1D and FV2D problems.");
     if (!(p->eps > 1.1920928955078125e-07))  // epsilon(1.0_real32), src/hrweno_weno.f90:92
@@ -616,7 +614,7 @@ static int ode_create(const hrw_problem* p, int neq, int order, int method, int 
         L.width = D.width;
         L.rws = D.rws;
         L.xe = D.xe;
-        b.cnu = D.cnu;
+        (d == 0 ? b.cnu : b.cnu2) = D.cnu;
       }
     }
     b.ld = p->ncells[0];

@@ -52,7 +52,8 @@ struct StageArgsT {
   LineArgsT<T> L2;
   int64_t ld;    // row stride (nc1) of the 2D layout
   int upwind;    // Godunov flux of g(x) u with g > 0 everywhere: F = g vm (2D kernel)
-  const T* cnu;  // non-uniform 1D line: weno coefficients cnu(0:k-1,-1:k-1,1:nc)
+  const T* cnu;   // non-uniform line (1D, or x1 of 2D): weno coefficients cnu(0:k-1,-1:k-1,1:nc)
+  const T* cnu2;  // 2D: the x2 line's coefficients when it is non-uniform
   // uniform 1D line (stage1d_kernel): update only cells cell0 .. cell0 + ncell - 1 (ncell = 0:
   // the whole line); cell0 and ncell are multiples of the launch's tile (1024 cells for lines
   // of at least 2 x SMs x 1024 cells), so that ranges launched side by side write disjoint cells
@@ -61,8 +62,10 @@ struct StageArgsT {
   // current device) and release their programmatic dependents at once
   int wave_blocks;
   // 2D stages: the handle's word that a block sets when its bounded wait for its tile copies
-  // runs out (zero-initialised device memory; checked and cleared by the host after the call)
+  // runs out (zero-initialised device memory; checked and cleared by the host after the call),
+  // and the poll limit of that wait (set by the launcher)
   unsigned int* timeout_flag;
+  int tile_wait_polls;
 };
 using StageArgs = StageArgsT<double>;
 using StageArgs32 = StageArgsT<float>;

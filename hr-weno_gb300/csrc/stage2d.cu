@@ -21,6 +21,13 @@
 // Upwind specialisation (UPW): for the Godunov flux of f = g(x) u with g > 0 on the whole
 // domain in both directions, F = g vm exactly (hrw_stage.cuh: upwind_flux), so only the left
 // state vr of every interface is reconstructed.
+//
+// Non-uniform lines (NU): a line with xedges reconstructs every cell with its own coefficients
+// cnu (src/hrweno_weno.f90:170,177-181; "any smooth grid can be used",
+// example/example2_pbe_2d_fv.f90:36-39), divides by its cells' widths and evaluates the flux
+// function at its true interface coordinates; a uniform line of the same problem keeps the
+// tables.
+#include <atomic>
 #include <type_traits>
 
 #include <cuda_runtime.h>
@@ -39,10 +46,27 @@ constexpr int TX = 32, TY = 32, C = 8, NT = 128;
 static_assert(TX * TY == NT * C, "one segment of C cells per thread and direction");
 static_assert(TX == 32 && TY / C == NT / 32 && TX / C == NT / 32, "warp-per-segment mapping");
 
-// poll limit of the first wait for the tile copies (stage2d_set_tile_wait_limit)
+// default poll limit of the first wait for the tile copies (stage2d_set_tile_wait_limit
+// changes it per device; the launch passes it in the arguments), and the limit of the wait that
+// drains the copies after a timeout
 constexpr int kTileWaitPolls = 1 << 20;
-__device__ int g_tile_wait_limit = kTileWaitPolls;
 constexpr int BX = 40, BY = 38;  // TMA box of the tile plus halo: x from bx - 4, y from by - 3
+
+// Reconstruction of C consecutive cells g0 .. g0 + C - 1 of a non-uniform line of n cells, with
+// p[q * stride] = v(g0 - K + q) and cell g's coefficients at cnu + K(K+1) g (cells past the
+// line's end, whose results are not used, read the last cell's).
+template <class R, int K, bool STRICT>
+__device__ __forceinline__ void recon_nu_seg(const R* p, int stride, const R* cnu, int64_t g0,
+                                             int64_t n, R eps, R* vl, R* vr) {
+#pragma unroll
+  for (int c = 0; c < C; ++c) {
+    R w[2 * K - 1];  // v(g0 + c - (K-1)) .. v(g0 + c + (K-1))
+#pragma unroll
+    for (int q = 0; q < 2 * K - 1; ++q) w[q] = p[(c + 1 + q) * stride];
+    const int64_t g = g0 + c < n ? g0 + c : n - 1;
+    recon_nu<K, STRICT>(w + (K - 1), cnu + (int64_t)K * (K + 1) * g, eps, vl[c], vr[c]);
+  }
+}
 
 // TMA: the tile plus halo of the stage input comes in as one 40 x 38 box at (bx - 4, by - 3)
 // (x on a 16-byte boundary for doubles and floats alike), completing on a block mbarrier; the
@@ -50,7 +74,7 @@ constexpr int BX = 40, BY = 38;  // TMA box of the tile plus halo: x from bx - 4
 // reads zeros outside the grid).  Otherwise every thread gathers the tile from global memory.
 // Both give the same tile, so the same bits.
 // R = double (HRW_F64, FAST or STRICT) or float (HRW_F32, reference order only).
-template <class R, int K, int ST, bool STRICT, bool UPW, bool TMA>
+template <class R, int K, int ST, bool STRICT, bool UPW, bool TMA, bool NU>
 __global__ void __launch_bounds__(NT) stage2d_kernel(const __grid_constant__ CUtensorMap Mv, StageArgsT<R> a) {
   static_assert(STRICT || std::is_same<R, double>::value, "float grids take the reference order");
   constexpr int H = K;
@@ -81,7 +105,7 @@ __global__ void __launch_bounds__(NT) stage2d_kernel(const __grid_constant__ CUt
     }
     // bounded wait; on a timeout every thread of the block learns of it, the block waits
     // (with the default bound) for its copy to land and leaves, and the host sees the flag
-    const bool ok = mbar_wait(&bar, 0, g_tile_wait_limit);
+    const bool ok = mbar_wait(&bar, 0, a.tile_wait_polls);
     if (__syncthreads_or(!ok)) {
       if (tid == 0) atomicExch(a.timeout_flag, 1u);
       mbar_wait(&bar, 0, kTileWaitPolls);
@@ -111,14 +135,22 @@ __global__ void __launch_bounds__(NT) stage2d_kernel(const __grid_constant__ CUt
   R vl[C], vr[C];
   {
     const R* row = &sv[(r + H) * SW + sg * C];  // row[q] = v(bx + sg*C - H + q)
-    if constexpr (STRICT) {
+    auto uniform = [&]() {
+      if constexpr (STRICT) {
 #pragma unroll
-      for (int c = 0; c < C; ++c) recon_strict<K>(row + H + c, a.eps, vl[c], vr[c]);
+        for (int c = 0; c < C; ++c) recon_strict<K>(row + H + c, a.eps, vl[c], vr[c]);
+      } else {
+        R w[C + 2 * K];
+#pragma unroll
+        for (int q = 0; q < C + 2 * K; ++q) w[q] = row[q];
+        recon_fast<K, C, !UPW>(w, a.eps, vl, vr);
+      }
+    };
+    if constexpr (NU) {
+      if (a.cnu) recon_nu_seg<R, K, STRICT>(row, 1, a.cnu, bx + sg * C, n1, a.eps, vl, vr);
+      else uniform();
     } else {
-      R w[C + 2 * K];
-#pragma unroll
-      for (int q = 0; q < C + 2 * K; ++q) w[q] = row[q];
-      recon_fast<K, C, !UPW>(w, a.eps, vl, vr);
+      uniform();
     }
     if constexpr (!UPW) sLx[r * (NSX + 1) + sg] = vl[0];
     sRx[r * (NSX + 1) + sg + 1] = vr[C - 1];
@@ -137,9 +169,25 @@ __global__ void __launch_bounds__(NT) stage2d_kernel(const __grid_constant__ CUt
       stride = SW;
     }
     const bool need = !UPW || warp == 0 || warp == 2;
-    if (need) {
+    bool done = false;
+    if constexpr (NU) {
+      const R* ci = warp < 2 ? a.cnu : a.cnu2;
+      if (need && ci) {
+        const int64_t n = warp < 2 ? n1 : n2;
+        int64_t g = warp == 0 ? bx - 1 : (warp == 1 ? bx + TX : (warp == 2 ? by - 1 : by + TY));
+        g = g < 0 ? 0 : (g >= n ? n - 1 : g);
+        R w[2 * K - 1];
+#pragma unroll
+        for (int q = 0; q < 2 * K - 1; ++q) w[q] = p[(q - (K - 1)) * stride];
+        recon_nu<K, STRICT>(w + (K - 1), ci + (int64_t)K * (K + 1) * g, a.eps, el, er);
+        done = true;
+      }
+    }
+    if (need && !done) {
       if constexpr (STRICT) recon_strict_strided<K>(p, stride, a.eps, el, er);
       else recon_fast_one<K>(p, a.eps, el, er, stride);
+    }
+    if (need) {
       if (warp == 0) sRx[lane * (NSX + 1)] = er;
       else if (warp == 1) sLx[lane * (NSX + 1) + NSX] = el;
       else if (warp == 2) sRy[lane] = er;
@@ -179,14 +227,22 @@ __global__ void __launch_bounds__(NT) stage2d_kernel(const __grid_constant__ CUt
   const int col = lane, sy = warp;
   {
     const R* cp = &sv[(sy * C) * SW + H + col];  // cp[q*SW] = v(x2 = by + sy*C - H + q)
-    if constexpr (STRICT) {
+    auto uniform = [&]() {
+      if constexpr (STRICT) {
 #pragma unroll
-      for (int c = 0; c < C; ++c) recon_strict_strided<K>(cp + (H + c) * SW, SW, a.eps, vl[c], vr[c]);
+        for (int c = 0; c < C; ++c) recon_strict_strided<K>(cp + (H + c) * SW, SW, a.eps, vl[c], vr[c]);
+      } else {
+        R w[C + 2 * K];
+#pragma unroll
+        for (int q = 0; q < C + 2 * K; ++q) w[q] = cp[q * SW];
+        recon_fast<K, C, !UPW>(w, a.eps, vl, vr);
+      }
+    };
+    if constexpr (NU) {
+      if (a.cnu2) recon_nu_seg<R, K, STRICT>(cp, SW, a.cnu2, by + sy * C, n2, a.eps, vl, vr);
+      else uniform();
     } else {
-      R w[C + 2 * K];
-#pragma unroll
-      for (int q = 0; q < C + 2 * K; ++q) w[q] = cp[q * SW];
-      recon_fast<K, C, !UPW>(w, a.eps, vl, vr);
+      uniform();
     }
     if constexpr (!UPW) sLy[sy * TX + col] = vl[0];
     sRy[(sy + 1) * TX + col] = vr[C - 1];
@@ -235,10 +291,12 @@ template <class R, int K, int ST, bool STRICT, bool UPW>
 cudaError_t launch_k(const StageArgsT<R>& a, cudaStream_t s) {
   const dim3 grid((unsigned)((a.L.nc + TX - 1) / TX), (unsigned)((a.L2.nc + TY - 1) / TY));
   CUtensorMap mv{};
-  if (a.ld == a.L.nc && tile_map_2d(a.v, (int)sizeof(R), (int)a.L.nc, (int)a.L2.nc, BX, BY, &mv))
-    stage2d_kernel<R, K, ST, STRICT, UPW, true><<<grid, NT, 0, s>>>(mv, a);
+  if (a.cnu || a.cnu2)  // non-uniform lines: the general flux path (upwind is only a shortcut)
+    stage2d_kernel<R, K, ST, STRICT, false, false, true><<<grid, NT, 0, s>>>(mv, a);
+  else if (a.ld == a.L.nc && tile_map_2d(a.v, (int)sizeof(R), (int)a.L.nc, (int)a.L2.nc, BX, BY, &mv))
+    stage2d_kernel<R, K, ST, STRICT, UPW, true, false><<<grid, NT, 0, s>>>(mv, a);
   else
-    stage2d_kernel<R, K, ST, STRICT, UPW, false><<<grid, NT, 0, s>>>(mv, a);
+    stage2d_kernel<R, K, ST, STRICT, UPW, false, false><<<grid, NT, 0, s>>>(mv, a);
   return cudaGetLastError();
 }
 
@@ -255,33 +313,104 @@ cudaError_t launch_st(const StageArgsT<R>& a, int stage, cudaStream_t s) {
   return cudaErrorInvalidValue;
 }
 
-template <class R, bool STRICT, bool UPW>
-cudaError_t launch_kk(const StageArgsT<R>& a, int k, int stage, cudaStream_t s) {
-  if (k == 1) return launch_st<R, 1, STRICT, UPW>(a, stage, s);
-  if (k == 2) return launch_st<R, 2, STRICT, UPW>(a, stage, s);
-  return launch_st<R, 3, STRICT, UPW>(a, stage, s);
-}
+}  // namespace
 
+// Every stage kind of one (real type, numerics, k).  The nine combinations compile as separate
+// objects, HRW_PART = 0 .. 8 in the order below (the build compiles this file once per part,
+// in parallel); part 0 also holds the dispatch.  Built without HRW_PART, the file holds all.
+template <class R, bool STRICT, int K>
+cudaError_t stage2d_launch(const StageArgsT<R>& a, int stage, cudaStream_t s) {
+  return a.upwind ? launch_st<R, K, STRICT, true>(a, stage, s) : launch_st<R, K, STRICT, false>(a, stage, s);
+}
+extern template cudaError_t stage2d_launch<double, false, 1>(const StageArgsT<double>&, int, cudaStream_t);
+extern template cudaError_t stage2d_launch<double, false, 2>(const StageArgsT<double>&, int, cudaStream_t);
+extern template cudaError_t stage2d_launch<double, false, 3>(const StageArgsT<double>&, int, cudaStream_t);
+extern template cudaError_t stage2d_launch<double, true, 1>(const StageArgsT<double>&, int, cudaStream_t);
+extern template cudaError_t stage2d_launch<double, true, 2>(const StageArgsT<double>&, int, cudaStream_t);
+extern template cudaError_t stage2d_launch<double, true, 3>(const StageArgsT<double>&, int, cudaStream_t);
+extern template cudaError_t stage2d_launch<float, true, 1>(const StageArgsT<float>&, int, cudaStream_t);
+extern template cudaError_t stage2d_launch<float, true, 2>(const StageArgsT<float>&, int, cudaStream_t);
+extern template cudaError_t stage2d_launch<float, true, 3>(const StageArgsT<float>&, int, cudaStream_t);
+#if !defined(HRW_PART) || HRW_PART == 0
+template cudaError_t stage2d_launch<double, false, 1>(const StageArgsT<double>&, int, cudaStream_t);
+#endif
+#if !defined(HRW_PART) || HRW_PART == 1
+template cudaError_t stage2d_launch<double, false, 2>(const StageArgsT<double>&, int, cudaStream_t);
+#endif
+#if !defined(HRW_PART) || HRW_PART == 2
+template cudaError_t stage2d_launch<double, false, 3>(const StageArgsT<double>&, int, cudaStream_t);
+#endif
+#if !defined(HRW_PART) || HRW_PART == 3
+template cudaError_t stage2d_launch<double, true, 1>(const StageArgsT<double>&, int, cudaStream_t);
+#endif
+#if !defined(HRW_PART) || HRW_PART == 4
+template cudaError_t stage2d_launch<double, true, 2>(const StageArgsT<double>&, int, cudaStream_t);
+#endif
+#if !defined(HRW_PART) || HRW_PART == 5
+template cudaError_t stage2d_launch<double, true, 3>(const StageArgsT<double>&, int, cudaStream_t);
+#endif
+#if !defined(HRW_PART) || HRW_PART == 6
+template cudaError_t stage2d_launch<float, true, 1>(const StageArgsT<float>&, int, cudaStream_t);
+#endif
+#if !defined(HRW_PART) || HRW_PART == 7
+template cudaError_t stage2d_launch<float, true, 2>(const StageArgsT<float>&, int, cudaStream_t);
+#endif
+#if !defined(HRW_PART) || HRW_PART == 8
+template cudaError_t stage2d_launch<float, true, 3>(const StageArgsT<float>&, int, cudaStream_t);
+#endif
+
+#if !defined(HRW_PART) || HRW_PART == 0
+namespace {
+// poll limit of the first wait for the tile copies, per device (stage2d_set_tile_wait_limit);
+// stored + 1, so that 0 reads as the default
+constexpr int kMaxDevices = 64;
+std::atomic<int> g_tile_wait[kMaxDevices];
+
+int tile_wait_polls() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+    cudaGetLastError();
+    return kTileWaitPolls;
+  }
+  const int v = g_tile_wait[dev].load(std::memory_order_relaxed);
+  return v > 0 ? v - 1 : kTileWaitPolls;
+}
 }  // namespace
 
 cudaError_t stage2d_set_tile_wait_limit(int polls) {
-  const int v = polls < 0 ? kTileWaitPolls : polls;
-  return cudaMemcpyToSymbol(g_tile_wait_limit, &v, sizeof(v));
+  int dev = 0;
+  const cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+  g_tile_wait[dev].store(polls < 0 ? 0 : polls + 1, std::memory_order_relaxed);
+  return cudaSuccess;
+}
+
+template <class R>
+static cudaError_t dispatch(StageArgsT<R> a, int k, int stage, bool strict, cudaStream_t s) {
+  if (a.L.nc <= 0 || a.L2.nc <= 0) return cudaSuccess;
+  if (a.L2.nc > 65535LL * TY || !a.timeout_flag) return cudaErrorInvalidValue;
+  a.tile_wait_polls = tile_wait_polls();
+  if constexpr (std::is_same<R, float>::value) {
+    (void)strict;
+    return k == 1 ? stage2d_launch<R, true, 1>(a, stage, s)
+                  : (k == 2 ? stage2d_launch<R, true, 2>(a, stage, s) : stage2d_launch<R, true, 3>(a, stage, s));
+  } else if (strict) {
+    return k == 1 ? stage2d_launch<R, true, 1>(a, stage, s)
+                  : (k == 2 ? stage2d_launch<R, true, 2>(a, stage, s) : stage2d_launch<R, true, 3>(a, stage, s));
+  } else {
+    return k == 1 ? stage2d_launch<R, false, 1>(a, stage, s)
+                  : (k == 2 ? stage2d_launch<R, false, 2>(a, stage, s) : stage2d_launch<R, false, 3>(a, stage, s));
+  }
 }
 
 cudaError_t launch_stage2d(const StageArgs& a, int k, int stage, bool strict, cudaStream_t s) {
-  if (a.L.nc <= 0 || a.L2.nc <= 0) return cudaSuccess;
-  if (a.L2.nc > 65535LL * TY || !a.timeout_flag) return cudaErrorInvalidValue;
-  const bool upw = a.upwind;
-  using D = double;
-  if (strict) return upw ? launch_kk<D, true, true>(a, k, stage, s) : launch_kk<D, true, false>(a, k, stage, s);
-  return upw ? launch_kk<D, false, true>(a, k, stage, s) : launch_kk<D, false, false>(a, k, stage, s);
+  return dispatch(a, k, stage, strict, s);
 }
 
 cudaError_t launch_stage2d(const StageArgs32& a, int k, int stage, cudaStream_t s) {
-  if (a.L.nc <= 0 || a.L2.nc <= 0) return cudaSuccess;
-  if (a.L2.nc > 65535LL * TY || !a.timeout_flag) return cudaErrorInvalidValue;
-  return a.upwind ? launch_kk<float, true, true>(a, k, stage, s) : launch_kk<float, true, false>(a, k, stage, s);
+  return dispatch(a, k, stage, true, s);
 }
+#endif
 
 }  // namespace hrw

@@ -108,10 +108,12 @@ typedef struct hrw_problem {
   const double* width[2]; /* optional host array(nc) of cell widths; NULL: (xmax-xmin)/nc */
   const double* rates;    /* LINEAR_ODE: host array(neq) of rates a_i */
   int32_t numerics;       /* HRW_NUMERICS_* */
-  /* optional host array(nc+1) of cell edges of a non-uniform line (FV1D, HRW_F64): the WENO
-   * coefficients become cnu(xedges) as weno(ncells, k, eps, xedges) builds them
-   * (src/hrweno_weno.f90:100-104,221-297), the widths edges(i) - edges(i-1) and the flux's x the
-   * edges themselves; xmin/xmax and width[] are then ignored.  NULL: uniform grid. */
+  /* optional host array(nc+1) of cell edges of a non-uniform line, per dimension (FV1D and
+   * FV2D; HRW_F64 and HRW_F32 handles, not HRW_F32C, the batches, the adjoint or the
+   * allocation-free steps): the WENO coefficients become cnu(xedges) as weno(ncells, k, eps,
+   * xedges) builds them (src/hrweno_weno.f90:100-104,221-297), the widths edges(i) - edges(i-1)
+   * and the flux's x the edges themselves; xmin/xmax are then unused and width[] must be NULL.
+   * NULL: uniform grid. */
   const double* xedges[2];
 } hrw_problem;
 

@@ -94,6 +94,62 @@ def test_rhs_2d_widths(hw, orc):
             assert nrel(got, ref) <= TOL
 
 
+def stretched_edges(n, x0, x1, ratio):
+    """n + 1 edges on [x0, x1] with widths in geometric progression (a smooth stretched grid)."""
+    w = ratio ** np.arange(n, dtype=np.float64)
+    return x0 + (x1 - x0) * np.concatenate([[0.0], np.cumsum(w) / w.sum()])
+
+
+def nonuniform_pbe(hw, n1, n2, k, name, which, numerics):
+    kw = PROBLEMS[name]
+    prob = hw.pbe_2d(n1, n2, g1=kw["g1"], g2=kw["g2"], k=k, flux=kw["flux"], bc=kw["bc"],
+                     numerics=numerics)
+    prob.xedges = (stretched_edges(n1, 0.0, 1.0, 1.02) if which in ("x1", "both") else None,
+                   stretched_edges(n2, 0.0, 1.0, 0.97) if which in ("x2", "both") else None)
+    return prob
+
+
+@pytest.mark.parametrize("shape", [(1, 1), (5, 7), (33, 31), (64, 40), (100, 37)])
+@pytest.mark.parametrize("k", [1, 2, 3])
+@pytest.mark.parametrize("which", ["x1", "x2", "both"])
+@pytest.mark.parametrize("name", ["pbe_upwind", "pbe_mixed", "pbe_lf"])
+def test_rhs_2d_nonuniform(hw, orc, shape, k, which, name):
+    """Non-uniform lines in 2D ("any smooth grid can be used", example2...f90:36-39): each
+    line's cells reconstruct with their own cnu, divide by their widths and evaluate g at
+    the true edges; a uniform line of the same problem keeps the tables."""
+    n1, n2 = shape
+    rng = np.random.default_rng(n1 * 7 + n2 + k)
+    v = rng.uniform(0.0, 1.0, n1 * n2)
+    for numerics in ("strict", "fast"):
+        prob = nonuniform_pbe(hw, n1, n2, k, name, which, numerics)
+        ref = orc.rhs(prob, v)
+        got = device_rhs(prob, v)
+        if numerics == "strict":
+            assert np.array_equal(got, ref), (name, shape, k, which)
+        else:
+            assert nrel(got, ref) <= TOL, (name, shape, k, which, nrel(got, ref))
+
+
+@pytest.mark.parametrize("numerics", ["strict", "fast"])
+def test_mstvd_2d_nonuniform(hw, orc, numerics):
+    from hrweno import workloads
+    n1, n2 = 96, 80
+    _, n0, dt = workloads.pbe_config(n1, n2, cfl=0.25)
+    prob = nonuniform_pbe(hw, n1, n2, 3, "pbe_upwind", "both", numerics)
+    g, o = hw.mstvd(prob, n1 * n2), orc.ODE(prob, n1 * n2, 1)
+    ug, uo = n0.copy(), n0.copy()
+    tg = to = 0.0
+    for tout in (20 * dt, 61.5 * dt):
+        tg = g.integrate(ug, tg, tout, dt)
+        to = o.integrate(uo, to, tout, dt)
+        assert tg == to and g.nsteps == o.info()[2]
+        assert np.isfinite(uo).all()
+        if numerics == "strict":
+            assert np.array_equal(ug, uo)
+        else:
+            assert nrel(ug, uo) <= TOL
+
+
 @pytest.mark.parametrize("numerics", ["strict", "fast"])
 @pytest.mark.parametrize("bc", ["zero_inflow", "zero"])
 def test_mstvd_2d_pbe(hw, orc, numerics, bc):

@@ -140,6 +140,17 @@ def test_rhs_2d_pbe_f32(hw, orc, k, n1, n2, flux):
     assert np.array_equal(gpu_rhs32(prob, v).astype(np.float64), ref)
 
 
+@pytest.mark.parametrize("k", [1, 2, 3])
+@pytest.mark.parametrize("n1,n2", [(5, 3), (64, 48), (100, 37)])
+def test_rhs_2d_nonuniform_f32(hw, orc, k, n1, n2):
+    prob, n0, _ = workloads.pbe_config(n1, n2, k=k)
+    w1 = 1.02 ** np.arange(n1)
+    prob.xedges = (np.concatenate([[0.0], np.cumsum(w1) / w1.sum()]), None)
+    v = f32(n0 + 0.01 * np.random.default_rng(5).standard_normal(n0.size))
+    ref = orc.rhs(prob, v.astype(np.float64), prec=32)
+    assert np.array_equal(gpu_rhs32(prob, v).astype(np.float64), ref)
+
+
 def run_both(hw, orc, prob, n, u0, method, order, t0, tout, dt, itask=1, mem="device", graphs=True):
     import torch
     mk = (lambda: hw.rktvd(prob, n, order, dtype="f32")) if method == 0 else \

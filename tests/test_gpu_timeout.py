@@ -13,7 +13,7 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-N1 = N2 = 64  # rows of 64 doubles / floats: 16-byte row pitch, so both kernels take the TMA loader
+N1 = N2 = 64  # rows of 64 doubles / floats: 16-byte row pitch, so every 2D kernel takes the TMA loader
 
 
 def diag():
@@ -41,7 +41,7 @@ def pulse():
     return np.exp(-((X - 0.3) ** 2 + (Y - 0.3) ** 2) / 0.01).reshape(-1)
 
 
-@pytest.mark.parametrize("dtype", ["f64", "f32c"])
+@pytest.mark.parametrize("dtype", ["f64", "f32c", "f32"])
 @pytest.mark.parametrize("method", ["rktvd", "mstvd"])
 def test_integrate_times_out_and_refuses(hw, orc, short_wait, dtype, method):
     import torch
@@ -49,7 +49,8 @@ def test_integrate_times_out_and_refuses(hw, orc, short_wait, dtype, method):
     prob = hw.pbe_2d(N1, N2)
     dt = 0.3 / (1.5 * N1 + 0.5 * N2)
     ode = hw.rktvd(prob, N1 * N2, 3, dtype=dtype) if method == "rktvd" else hw.mstvd(prob, N1 * N2, dtype=dtype)
-    ug = torch.from_numpy(pulse()).cuda()
+    u0 = pulse().astype(np.float32) if dtype == "f32" else pulse()
+    ug = torch.from_numpy(u0).cuda()
     with pytest.raises(hw.HrwError) as e:
         ode.integrate(ug, 0.0, 2.5 * dt, dt)
     assert e.value.code == A.HRW_ETIMEOUT
@@ -60,15 +61,15 @@ def test_integrate_times_out_and_refuses(hw, orc, short_wait, dtype, method):
     assert e2.value.code == A.HRW_ESTATE
 
 
-@pytest.mark.parametrize("dtype", ["f64", "f32c"])
+@pytest.mark.parametrize("dtype", ["f64", "f32c", "f32"])
 def test_rhs_times_out(hw, short_wait, dtype):
     import torch
     from hrweno import _abi as A
     prob = hw.pbe_2d(N1, N2)
-    v = torch.from_numpy(pulse()).cuda()
+    v = torch.from_numpy(pulse().astype(np.float32) if dtype == "f32" else pulse()).cuda()
     out = torch.empty_like(v)
     cp = prob.to_c()
-    code = A.HRW_F64 if dtype == "f64" else A.HRW_F32C
+    code = {"f64": A.HRW_F64, "f32c": A.HRW_F32C, "f32": A.HRW_F32}[dtype]
     rc = A.lib().hrw_rhs(C.byref(cp), code, 0.0, v.data_ptr(), out.data_ptr(), None)
     assert rc == A.HRW_ETIMEOUT
     assert "bounded wait" in A.lib().hrw_last_error().decode()
