@@ -218,6 +218,8 @@ struct hrw_ode {
     int64_t steps = 0;
   } graph;
   bool use_graphs = true;
+  // short uniform 1D lines: all steps of an integrate call in one cluster launch
+  bool use_cluster = true;
   // host lines with the copies overlapped (rk3_integrate_host): two compute streams and a copy
   // stream beside `stream`, and their events
   cudaStream_t pipe[2] = {}, copy = nullptr;
@@ -717,6 +719,12 @@ int hrw_ode_set_graphs(hrw_ode* o, int enable) {
   return HRW_OK;
 }
 
+int hrw_ode_set_cluster(hrw_ode* o, int enable) {
+  if (!o) return fail(HRW_EINVAL, "Invalid input 'ode': null handle.");
+  o->use_cluster = enable != 0;
+  return HRW_OK;
+}
+
 int hrw_ode_info(const hrw_ode* o, int* fevals, int* istate, int64_t* nsteps) {
   if (!o) return fail(HRW_EINVAL, "Invalid input 'ode': null handle.");
   if (fevals) *fevals = o->fevals;
@@ -945,6 +953,24 @@ static int rk_integrate(hrw_ode* o, double* du, double* t, double tout, double d
     o->nsteps += n;
     if (o->istate == 1) o->istate = 2;
     return HRW_OK;
+  }
+  if (o->use_cluster && o->prob.kind == HRW_PROBLEM_FV1D && cluster_line_ok(o->base)) {
+    StageArgs a = o->base;
+    a.dt = dt;
+    const cudaError_t e = launch_rk_cluster(a, o->prob.k, o->order, o->prob.numerics == HRW_NUMERICS_STRICT,
+                                            du, n, o->stream);
+    if (e == cudaSuccess) {
+      *t = tt;
+      o->fevals += (int)(o->order * n);
+      o->nsteps += n;
+      if (o->istate == 1) o->istate = 2;
+      return HRW_OK;
+    }
+    // a device that cannot schedule the cluster: the stage-by-stage launches from now on
+    if (e != cudaErrorInvalidClusterSize && e != cudaErrorNotSupported && e != cudaErrorLaunchOutOfResources)
+      return fail(HRW_ECUDA, std::string("launch_rk_cluster: ") + cudaGetErrorString(e));
+    cudaGetLastError();
+    o->use_cluster = false;
   }
   double* cur = du;
   double* other = o->w2;

@@ -183,6 +183,12 @@ cudaError_t launch_stage1d(const StageArgs& a, int k, int stage, bool strict, cu
 cudaError_t launch_stage2d(const StageArgs& a, int k, int stage, bool strict, cudaStream_t s);
 // 1D fused stage on a non-uniform line (a.cnu, a.L.xe, a.L.width / a.L.rws set).
 cudaError_t launch_stage1d_nu(const StageArgs& a, int k, int stage, bool strict, cudaStream_t s);
+// Every step of an rktvd integrate call of a short uniform FV1D line (6 .. 4096 cells) in one
+// launch of one thread-block cluster holding the line in shared memory (stage1d_cluster.cu);
+// the same bits as the stage-by-stage launches.  cluster_line_ok: whether a line qualifies.
+bool cluster_line_ok(const StageArgs& a);
+cudaError_t launch_rk_cluster(const StageArgs& a, int k, int order, bool strict, double* u,
+                              int64_t nsteps, cudaStream_t s);
 // Linear ODE u' = a u stage (test problem of the reference's integrator tests).
 cudaError_t launch_stage_linear(const double* rates, const StageArgs& a, int64_t n, int stage,
                                 bool strict, cudaStream_t s);

@@ -79,12 +79,13 @@ def lib() -> C.CDLL:
         L.hrw_ode_info.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int64)]
         L.hrw_ode_set_stream.argtypes = [vp, vp]
         L.hrw_ode_set_graphs.argtypes = [vp, i]
+        L.hrw_ode_set_cluster.argtypes = [vp, i]
         L.hrw_ode_destroy.argtypes = [vp]
         L.hrw_rhs.argtypes = [C.POINTER(HrwProblem), i, d, vp, vp, vp]
         for name in ("hrw_weno_create", "hrw_weno_set_numerics", "hrw_weno_reconstruct",
                      "hrw_weno_cnu", "hrw_weno_destroy", "hrw_rktvd_create", "hrw_mstvd_create",
                      "hrw_integrate", "hrw_ode_info", "hrw_ode_set_stream", "hrw_ode_destroy",
-                     "hrw_ode_set_graphs",
+                     "hrw_ode_set_graphs", "hrw_ode_set_cluster",
                      "hrw_rhs"):
             getattr(L, name).restype = C.c_int
         _lib = L

@@ -45,6 +45,11 @@ class _tvdode:
         """Replay captured CUDA graphs for long integrations (default) or launch each stage."""
         A.check(A.lib().hrw_ode_set_graphs(self._h, int(bool(enable))))
 
+    def set_cluster(self, enable: bool) -> None:
+        """Run every step of an integrate call of a short uniform 1D line (6 to 4096 cells) in one
+        thread-block cluster launch (default), or launch stage by stage.  Same results."""
+        A.check(A.lib().hrw_ode_set_cluster(self._h, int(bool(enable))))
+
     def _info(self):
         fe, st, ns = C.c_int(), C.c_int(), C.c_int64()
         A.check(A.lib().hrw_ode_info(self._h, C.byref(fe), C.byref(st), C.byref(ns)))

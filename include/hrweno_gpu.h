@@ -166,6 +166,12 @@ int hrw_ode_info(const hrw_ode* ode, int* fevals, int* istate, int64_t* nsteps);
  * and replays on every later call; enable = 0 launches every stage directly.  Both give the
  * same results bit for bit.  Default: enabled. */
 int hrw_ode_set_graphs(hrw_ode* ode, int enable);
+/* rktvd integrate calls on a uniform FV1D line of 6 to 4096 cells (FP64, FAST or STRICT) run all
+ * their steps in one launch of one thread-block cluster of up to 16 CTAs that keeps the line in
+ * distributed shared memory, one cluster barrier per stage, instead of a launch per stage: such
+ * lines are bound by launch latency.  The same results bit for bit.  enable = 0 launches stage by
+ * stage (with graphs as set above).  Default: enabled. */
+int hrw_ode_set_cluster(hrw_ode* ode, int enable);
 /* Run this handle's kernels on `stream` (a cudaStream_t); NULL restores its own stream. */
 int hrw_ode_set_stream(hrw_ode* ode, void* stream);
 int hrw_ode_destroy(hrw_ode* ode);
