@@ -1,7 +1,7 @@
 // batch.cu - many independent 1D problems of uneven size in one persistent launch.
 //
 // Each problem is one reference solve: its own rktvd(fu, neq, order) object integrated with its
-// own dt (src/hrweno_tvdode.f90:69-178), whose fu is the example1 right-hand side
+// own dt (src/hrweno_tvdode.f90:69-178), or its own mstvd(fu, neq) (:180-271), whose fu is the example1 right-hand side
 // (example/example1_burgers_1d_fv.f90:72-109) with its own flux, k and alpha.  Here all of them
 // advance together:
 //
@@ -134,6 +134,65 @@ __device__ void run_problem(const BatchArgs& B, const BatchProblem& P, int lt, i
   }
 }
 
+// mstvd (src/hrweno_tvdode.f90:203-271) of one problem: the packed state u is copied into its
+// ring slot, the RK3 start (:236-249) runs on the problem's first call, then P.nsteps
+// multistep steps (:252-268), each reading u^m, u^{m-4}, L(u^{m-4}) and writing u^{m+1} and
+// L(u^m) over the two oldest entries; the newest state is copied back to u.
+template <int K, bool STRICT, int G, int C>
+__device__ void run_problem_ms(const BatchArgs& B, const BatchProblem& P, int lt, int gid) {
+  LineArgs L{};
+  L.nc = P.nc;
+  L.fn = P.fn;
+  L.bc = P.bc;
+  L.flux = P.flux;
+  L.a = P.a;
+  L.b = P.b;
+  L.alpha = P.alpha;
+  L.xmin = P.xmin;
+  L.rx = P.rx;
+  L.rws0 = P.rws0;
+  double* u = B.u + P.off;
+  double* u1 = B.u1 + P.off;
+  double* u2 = B.u2 + P.off;
+  double* R[5];
+  double* Lr[4];
+#pragma unroll
+  for (int q = 0; q < 5; ++q) R[q] = B.ring_u[q] + P.off;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) Lr[q] = B.ring_l[q] + P.off;
+  StageArgs a{};
+  a.eps = P.eps;
+  a.dt = P.dt;
+  int64_t level = P.level;
+  double* cur = R[P.start ? 0 : level % 5];
+  for (int64_t j = lt; j < L.nc; j += G) cur[j] = u[j];
+  group_sync<G>(gid);
+  if (P.start) {  // u^m and L(u^m), m = 0..3, by RK3 steps (the start's rhs calls)
+    for (int m = 0; m < 4; ++m) {
+      double* um = R[m % 5];
+      a.v = um, a.u = um, a.out = Lr[m % 4];
+      stage_sweep<K, ST_RHS, STRICT, G, C>(a, L, lt, gid);
+      a.v = um, a.u = um, a.out = u1;
+      stage_sweep<K, ST_EULER, STRICT, G, C>(a, L, lt, gid);
+      a.v = u1, a.u = um, a.out = u2;
+      stage_sweep<K, ST_RK3B, STRICT, G, C>(a, L, lt, gid);
+      a.v = u2, a.u = um, a.out = R[(m + 1) % 5];
+      stage_sweep<K, ST_RK3C, STRICT, G, C>(a, L, lt, gid);
+    }
+    level = 4;
+  }
+  for (int64_t n = 0; n < P.nsteps; ++n, ++level) {
+    double* um = R[level % 5];
+    double* un = R[(level + 1) % 5];  // holds u^{m-4}, overwritten with u^{m+1}
+    double* lm = Lr[level % 4];       // holds L(u^{m-4}), overwritten with L(u^m)
+    a.v = um, a.u = um, a.out = un, a.lout = lm, a.uo4 = un, a.lo4 = lm;
+    stage_sweep<K, ST_MS, STRICT, G, C>(a, L, lt, gid);
+  }
+  cur = R[level % 5];
+  for (int64_t j = lt; j < L.nc; j += G) u[j] = cur[j];
+  group_sync<G>(gid);
+}
+
 template <bool STRICT, int G, int C>
 __global__ void __launch_bounds__(NT, 1) batch_kernel(BatchArgs B) {
   static_assert(NT % G == 0 && G % 32 == 0 && NT / G <= 15, "groups of whole warps");
@@ -147,10 +206,16 @@ __global__ void __launch_bounds__(NT, 1) batch_kernel(BatchArgs B) {
     group_sync<G>(gid);  // every lane has read s_pid before lane 0 claims again
     if (pid >= B.nprob) break;
     const BatchProblem P = B.probs[B.order_idx[pid]];
-    if (P.nsteps <= 0) continue;
-    if (P.k == 3) run_problem<3, STRICT, G, C>(B, P, lt, gid);
-    else if (P.k == 2) run_problem<2, STRICT, G, C>(B, P, lt, gid);
-    else run_problem<1, STRICT, G, C>(B, P, lt, gid);
+    if (P.nsteps <= 0 && !P.start) continue;
+    if (B.method == 1) {
+      if (P.k == 3) run_problem_ms<3, STRICT, G, C>(B, P, lt, gid);
+      else if (P.k == 2) run_problem_ms<2, STRICT, G, C>(B, P, lt, gid);
+      else run_problem_ms<1, STRICT, G, C>(B, P, lt, gid);
+    } else {
+      if (P.k == 3) run_problem<3, STRICT, G, C>(B, P, lt, gid);
+      else if (P.k == 2) run_problem<2, STRICT, G, C>(B, P, lt, gid);
+      else run_problem<1, STRICT, G, C>(B, P, lt, gid);
+    }
   }
 }
 

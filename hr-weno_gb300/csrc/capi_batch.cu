@@ -3,7 +3,9 @@
 //
 // Every problem follows the reference's integrate contract on its own: its step count comes
 // from replaying `t = t + dt` until is_done (src/hrweno_tvdode.f90:137-143,273-284) with its
-// own t and dt, so a batched solve takes exactly the steps of a loop of single solves.
+// own t and dt, so a batched solve takes exactly the steps of a loop of single solves.  An
+// mstvd batch (hrw_batch_create_mstvd) keeps each problem's multistep history between calls and
+// runs its RK3 start on its first call that takes a step (src/hrweno_tvdode.f90:203-271).
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -44,6 +46,10 @@ int cls_of(int64_t nc) {
 
 struct hrw_batch {
   int nprob = 0, order = 3, dtype = HRW_F64;
+  int method = 0;  // 0 rktvd, 1 mstvd
+  double* ring = nullptr;     // mstvd: 5 packed states u^m and 4 packed L(u^m)
+  std::vector<char> started;  // mstvd: the problem's RK3 start has run
+  std::vector<int64_t> level; // mstvd: m of the problem's current state
   bool strict = false;
   std::vector<BatchProblem> probs;
   std::vector<int64_t> off;  // nprob + 1
@@ -111,6 +117,11 @@ int launch_all(hrw_batch* b, double* u, const int* shapes) {
       A.u1 = b->u1;
       A.u2 = b->u2;
       A.order = b->order;
+      A.method = b->method;
+      if (b->ring) {
+        for (int q = 0; q < 5; ++q) A.ring_u[q] = b->ring + (size_t)q * b->total;
+        for (int q = 0; q < 4; ++q) A.ring_l[q] = b->ring + (size_t)(5 + q) * b->total;
+      }
       const bool f32 = b->dtype == HRW_F32C;
       if (f32) {
         float* q = b->fmem;
@@ -160,18 +171,27 @@ std::string tune_key(const hrw_batch* b, int c) {
   }
   std::ostringstream s;
   s << b->dev_name << "|class" << c << "|n" << b->members[c].size() << "|cells" << cells << "|k" << mix
-    << "|order" << b->order << "|" << (b->strict ? "strict" : "fast")
+    << "|order" << b->order << "|" << (b->strict ? "strict" : "fast") << (b->method ? "|ms" : "")
     << (b->dtype == HRW_F32C ? "|f32c" : "|f64");
   std::string k = s.str();
   std::replace(k.begin(), k.end(), ' ', '_');
   return k;
 }
 
+// After a call: problem i's steps (the mstvd start counts its 4), its level and start flag.
+void note_steps(hrw_batch* b, int i) {
+  const BatchProblem& q = b->probs[i];
+  b->steps_done[i] += q.nsteps + (q.start ? 4 : 0);
+  if (b->method == 1 && (q.start || q.nsteps > 0)) {
+    b->level[i] = (q.start ? 4 : b->level[i]) + q.nsteps;
+    b->started[i] = 1;
+  }
+}
+
 }  // namespace
 
-extern "C" {
-
-int hrw_batch_create(const hrw_problem* probs, int nprob, int order, int dtype, hrw_batch** out) {
+static int batch_create(const hrw_problem* probs, int nprob, int order, int dtype, int method,
+                        hrw_batch** out) {
   if (!out) return batch_fail(HRW_EINVAL, "Invalid input 'out': null pointer.");
   *out = nullptr;
   if (!probs || nprob <= 0) return batch_fail(HRW_EINVAL, "Invalid input 'nprob': must be >= 1.");
@@ -179,10 +199,13 @@ int hrw_batch_create(const hrw_problem* probs, int nprob, int order, int dtype, 
     return batch_fail(HRW_EINVAL, "Invalid input 'order' in 'rktvd'. Valid range: 1 <= k <= 3.");
   if (dtype != HRW_F64 && dtype != HRW_F32C)
     return batch_fail(HRW_EINVAL, "Invalid input 'dtype': batches support HRW_F64 and HRW_F32C.");
+  if (method == 1 && dtype != HRW_F64)
+    return batch_fail(HRW_EINVAL, "Invalid input 'dtype': mstvd batches support HRW_F64.");
   hrw_batch* b = new hrw_batch;
   b->nprob = nprob;
   b->order = order;
   b->dtype = dtype;
+  b->method = method;
   if (dtype == HRW_F32C)
     for (int c = 0; c < kClasses; ++c) b->shape[c] = kDefaultShapeF32[c];
   b->strict = probs[0].numerics == HRW_NUMERICS_STRICT;
@@ -230,6 +253,8 @@ int hrw_batch_create(const hrw_problem* probs, int nprob, int order, int dtype, 
   b->off[nprob] = off;
   b->total = off;
   b->steps_done.assign(nprob, 0);
+  b->started.assign(nprob, 0);
+  b->level.assign(nprob, 0);
   auto cleanup = [&](cudaError_t e) {
     hrw_batch_destroy(b);
     return batch_fail(e == cudaErrorMemoryAllocation ? HRW_ENOMEM : HRW_ECUDA,
@@ -260,8 +285,19 @@ int hrw_batch_create(const hrw_problem* probs, int nprob, int order, int dtype, 
     if ((e = cudaMalloc(&b->u1, bytes)) != cudaSuccess) return cleanup(e);
     if ((e = cudaMalloc(&b->u2, bytes)) != cudaSuccess) return cleanup(e);
   }
+  if (method == 1 && (e = cudaMalloc(&b->ring, bytes * 9)) != cudaSuccess) return cleanup(e);
   *out = b;
   return HRW_OK;
+}
+
+extern "C" {
+
+int hrw_batch_create(const hrw_problem* probs, int nprob, int order, int dtype, hrw_batch** out) {
+  return batch_create(probs, nprob, order, dtype, 0, out);
+}
+
+int hrw_batch_create_mstvd(const hrw_problem* probs, int nprob, int dtype, hrw_batch** out) {
+  return batch_create(probs, nprob, 3, dtype, 1, out);
 }
 
 int hrw_batch_layout(const hrw_batch* b, int64_t* offsets) {
@@ -304,15 +340,34 @@ int hrw_batch_integrate(hrw_batch* b, int mem, double* u, double* t, double tout
                                         std::to_string(i) + ").");
     double tt = t[i];
     int64_t n = 0;
+    BatchProblem& q = b->probs[i];
+    q.start = 0;
+    q.level = b->level[i];
     if (!is_done(tt, tout, h)) {
-      do {  // (src/hrweno_tvdode.f90:137-143)
-        tt = tt + h;
-        if (++n > (int64_t(1) << 40))
-          return batch_fail(HRW_EINVAL, "Invalid input 'dt': too many steps to reach tout.");
-      } while (!(is_done(tt, tout, h) || itask == 2));
+      if (b->method == 1) {  // mstvd_integrate: the RK3 start once, then until is_done (:236-268)
+        if (!b->started[i]) {
+          q.start = 1;
+          for (int m = 0; m < 4; ++m) tt = tt + h;
+        }
+        while (!is_done(tt, tout, h)) {
+          const double t1 = tt + h;
+          if (t1 == tt) return batch_fail(HRW_EINVAL, "Invalid input 'dt': t + dt == t, so tout is never reached.");
+          tt = t1;
+          if (++n > (int64_t(1) << 40))
+            return batch_fail(HRW_EINVAL, "Invalid input 'dt': too many steps to reach tout.");
+        }
+      } else {
+        do {  // (src/hrweno_tvdode.f90:137-143)
+          const double t1 = tt + h;
+          if (t1 == tt) return batch_fail(HRW_EINVAL, "Invalid input 'dt': t + dt == t, so tout is never reached.");
+          tt = t1;
+          if (++n > (int64_t(1) << 40))
+            return batch_fail(HRW_EINVAL, "Invalid input 'dt': too many steps to reach tout.");
+        } while (!(is_done(tt, tout, h) || itask == 2));
+      }
     }
-    b->probs[i].dt = h;
-    b->probs[i].nsteps = n;
+    q.dt = h;
+    q.nsteps = n;
     tnew[i] = tt;
   }
   double* du = u;
@@ -327,7 +382,7 @@ int hrw_batch_integrate(hrw_batch* b, int mem, double* u, double* t, double tout
   HRW_BCUDA(cudaStreamSynchronize(b->main));
   for (int i = 0; i < b->nprob; ++i) {
     t[i] = tnew[i];
-    b->steps_done[i] += b->probs[i].nsteps;
+    note_steps(b, i);
   }
   return HRW_OK;
 }
@@ -343,8 +398,11 @@ int hrw_batch_advance(hrw_batch* b, int mem, double* u, double* t, const double*
     if (!(dt[i] != 0.0) || !std::isfinite(dt[i]) || !std::isfinite(t[i]))
       return batch_fail(HRW_EINVAL, "Invalid input 'dt': must be finite and nonzero (problem " +
                                         std::to_string(i) + ").");
-    b->probs[i].dt = dt[i];
-    b->probs[i].nsteps = nsteps;
+    BatchProblem& q = b->probs[i];
+    q.dt = dt[i];
+    q.nsteps = nsteps;
+    q.start = b->method == 1 && !b->started[i];
+    q.level = b->level[i];
   }
   double* du = u;
   const size_t bytes = sizeof(double) * (size_t)b->total;
@@ -357,8 +415,9 @@ int hrw_batch_advance(hrw_batch* b, int mem, double* u, double* t, const double*
   if (mem == HRW_MEM_HOST) HRW_BCUDA(cudaMemcpyAsync(u, du, bytes, cudaMemcpyDeviceToHost, b->main));
   HRW_BCUDA(cudaStreamSynchronize(b->main));
   for (int i = 0; i < b->nprob; ++i) {
-    for (int64_t n = 0; n < nsteps; ++n) t[i] = t[i] + dt[i];
-    b->steps_done[i] += nsteps;
+    const int64_t n = nsteps + (b->probs[i].start ? 4 : 0);
+    for (int64_t s = 0; s < n; ++s) t[i] = t[i] + dt[i];
+    note_steps(b, i);
   }
   return HRW_OK;
 }
@@ -413,6 +472,7 @@ int hrw_batch_tune(hrw_batch* b, int mem, const double* u, const double* dt, int
       b->probs[i].nsteps = 0;
     }
     for (int p : b->members[c]) b->probs[p].nsteps = probe_steps;
+    for (int i = 0; i < b->nprob; ++i) b->probs[i].start = 0;
     float best = 1e30f;
     const bool f32 = b->dtype == HRW_F32C;
     int best_s = f32 ? kDefaultShapeF32[c] : kDefaultShape[c];
@@ -422,7 +482,11 @@ int hrw_batch_tune(hrw_batch* b, int mem, const double* u, const double* dt, int
       float ms = 0.f;
       for (int rep = 0; rep < 2; ++rep) {  // first run warms up
         HRW_BCUDA(cudaEventRecord(e0, b->main));
+        // an mstvd batch probes RK3 steps of the same stage code, leaving its history as it is
+        const int method = b->method;
+        b->method = 0;
         int rc = launch_all(b, b->u, shapes);
+        b->method = method;
         if (rc != HRW_OK) return rc;
         HRW_BCUDA(cudaEventRecord(e1, b->main));
         HRW_BCUDA(cudaEventSynchronize(e1));
@@ -451,6 +515,7 @@ int hrw_batch_destroy(hrw_batch* b) {
   if (b->u1) cudaFree(b->u1);
   if (b->u2) cudaFree(b->u2);
   if (b->fmem) cudaFree(b->fmem);
+  if (b->ring) cudaFree(b->ring);
   for (int c = 0; c < kClasses; ++c) {
     if (b->side[c]) cudaStreamDestroy(b->side[c]);
     if (b->join[c]) cudaEventDestroy(b->join[c]);

@@ -13,7 +13,11 @@ struct BatchProblem {
   int nc, k, fn, flux, bc;
   double a, b, alpha, xmin, rx, rws0, eps;
   double dt;
-  int64_t nsteps;
+  int64_t nsteps;  // rktvd: steps; mstvd: multistep steps after the start
+  // mstvd: run the RK3 start first (the problem's first call), and the level m of the state
+  // u^m when the call begins (after the start: 4)
+  int start;
+  int64_t level;
 };
 
 struct BatchArgs {
@@ -25,6 +29,10 @@ struct BatchArgs {
   double* u1;            // packed stage arrays
   double* u2;
   int order;             // rktvd order 1..3
+  // mstvd batches (method 1): u^m in ring_u[m % 5], L(u^m) in ring_l[m % 4], packed
+  int method;
+  double* ring_u[5];
+  double* ring_l[4];
   // compensated FP32 batches: state slots (hi, lo) x 2 and the stage increments, packed
   float* fhi[2];
   float* flo[2];

@@ -23,6 +23,7 @@ def _setup(L):
     vp, i, d = C.c_void_p, C.c_int, C.c_double
     dp = C.POINTER(C.c_double)
     L.hrw_batch_create.argtypes = [C.POINTER(A.HrwProblem), i, i, i, C.POINTER(vp)]
+    L.hrw_batch_create_mstvd.argtypes = [C.POINTER(A.HrwProblem), i, i, C.POINTER(vp)]
     L.hrw_batch_layout.argtypes = [vp, C.POINTER(C.c_int64)]
     L.hrw_batch_integrate.argtypes = [vp, i, vp, dp, d, dp, i]
     L.hrw_batch_tune.argtypes = [vp, i, vp, dp, i, C.c_char_p]
@@ -30,7 +31,7 @@ def _setup(L):
     L.hrw_batch_info.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_int64)]
     L.hrw_batch_set_stream.argtypes = [vp, vp]
     L.hrw_batch_destroy.argtypes = [vp]
-    for n in ("hrw_batch_create", "hrw_batch_layout", "hrw_batch_integrate", "hrw_batch_tune",
+    for n in ("hrw_batch_create", "hrw_batch_create_mstvd", "hrw_batch_layout", "hrw_batch_integrate", "hrw_batch_tune",
               "hrw_batch_advance",
               "hrw_batch_info", "hrw_batch_set_stream", "hrw_batch_destroy"):
         getattr(L, n).restype = C.c_int
@@ -38,9 +39,13 @@ def _setup(L):
 
 
 class batch:  # noqa: N801
-    """batch(problems, order=3): problems are FV1D Problem descriptors on uniform grids."""
+    """batch(problems, order=3): problems are FV1D Problem descriptors on uniform grids.
 
-    def __init__(self, problems: list[Problem], order: int = 3, dtype: str = "f64"):
+    method="mstvd" makes every problem an mstvd(fu_i, neq_i) solve (src/hrweno_tvdode.f90:180-271):
+    each keeps its multistep history between calls, and its first call runs the RK3 start."""
+
+    def __init__(self, problems: list[Problem], order: int = 3, dtype: str = "f64",
+                 method: str = "rktvd"):
         L = A.lib()
         _setup(L)
         arr = (A.HrwProblem * len(problems))()
@@ -49,8 +54,15 @@ class batch:  # noqa: N801
             arr[k] = p.to_c()
             self._keep.append(p)
         h = C.c_void_p()
-        A.check(L.hrw_batch_create(arr, len(problems), int(order), _DT[dtype], C.byref(h)))
+        if method == "mstvd":
+            A.check(L.hrw_batch_create_mstvd(arr, len(problems), _DT[dtype], C.byref(h)))
+            order = 3
+        elif method == "rktvd":
+            A.check(L.hrw_batch_create(arr, len(problems), int(order), _DT[dtype], C.byref(h)))
+        else:
+            raise ValueError("method must be 'rktvd' or 'mstvd'")
         self._h = h
+        self.method = method
         self.nprob = len(problems)
         self.order = int(order)
         off = np.empty(self.nprob + 1, dtype=np.int64)

@@ -192,6 +192,13 @@ int hrw_rhs(const hrw_problem* p, int dtype, double t, const void* v, void* vdot
  * persistent launch per size class, the classes running concurrently. */
 typedef struct hrw_batch hrw_batch;
 int hrw_batch_create(const hrw_problem* problems, int nprob, int order, int dtype, hrw_batch** out);
+/* A batch of mstvd(fu_i, neq_i) solves (src/hrweno_tvdode.f90:180-271), HRW_F64: each problem keeps
+ * its 5-step history between calls and runs the RK3 start (4 steps; the 4 extra rhs calls of the
+ * reference) on its first call that takes a step.  hrw_batch_integrate follows mstvd_integrate
+ * (itask is ignored, as the reference's mstvd has none); hrw_batch_advance runs the start on a
+ * problem's first call and then nsteps multistep steps; hrw_batch_tune probes RK3 steps of the
+ * same stage code and leaves the histories as they are. */
+int hrw_batch_create_mstvd(const hrw_problem* problems, int nprob, int dtype, hrw_batch** out);
 /* offsets[0 .. nprob] of the packed layout */
 int hrw_batch_layout(const hrw_batch* b, int64_t* offsets);
 /* Per problem i: integrate(u_i, t[i], tout, dt[i], itask) with the reference's stopping rule

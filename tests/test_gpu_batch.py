@@ -155,3 +155,59 @@ def test_batch_f32c_vs_single_f32c(hw, order):
         v = lines[i].copy()
         hw.rktvd(p, p.ncells[0], order, dtype="f32c").integrate(v, 0.0, (steps - 0.5) * dts[i], dts[i])
         assert np.array_equal(got[i], v), i
+
+
+# ---- mstvd batches ---------------------------------------------------------------------------
+@pytest.mark.parametrize("numerics", ["strict", "fast"])
+def test_mstvd_batch_matches_single_solves(hw, orc, numerics):
+    """A batch of mstvd solves (src/hrweno_tvdode.f90:180-271) of uneven lines, over several
+    integrate calls: each problem bit-identical to its own single-problem mstvd handle (FAST)
+    and to the oracle (STRICT), with the same t and step count; the history carries across
+    calls, and a problem whose first call takes no step starts later."""
+    import torch
+    from hrweno import workloads
+    probs, lines, dts = workloads.batched_config(24, seed=3, nmin=40, nmax=3000, numerics=numerics,
+                                                 cfl=0.2)
+    b = hw.batch(probs, dtype="f64", method="mstvd")
+    u = torch.from_numpy(b.pack(lines)).cuda()
+    t = np.zeros(len(probs))
+    t[5] = 1.0  # problem 5 is past the first tout: it takes no step on the first call
+    singles = [hw.mstvd(p, int(p.ncells[0])) for p in probs]
+    us = [torch.from_numpy(v.copy()).cuda() for v in lines]
+    ts = [float(x) for x in t]
+    orcs = [orc.ODE(p, int(p.ncells[0]), 1) for p in probs]
+    uo = [v.copy() for v in lines]
+    to = [float(x) for x in t]
+    for tout in (0.05, 0.2, 1.5):
+        b.integrate(u, t, tout, dts)
+        got = b.unpack(u)
+        for i, p in enumerate(probs):
+            ts[i] = singles[i].integrate(us[i], ts[i], tout, dts[i])
+            assert t[i] == ts[i], i
+            assert np.array_equal(got[i], us[i].cpu().numpy()), (i, tout)
+            if numerics == "strict":
+                to[i] = orcs[i].integrate(uo[i], to[i], tout, dts[i])
+                assert to[i] == t[i] and np.array_equal(got[i], uo[i]), (i, tout)
+        assert list(b.steps_done) == [s.nsteps for s in singles]
+
+
+def test_mstvd_batch_advance_and_tune(hw, orc):
+    """advance: the start on the first call (4 steps), then exactly nsteps multistep steps; the
+    autotuner leaves the histories as they are."""
+    import torch
+    from hrweno import workloads
+    probs, lines, dts = workloads.batched_config(16, seed=4, nmin=64, nmax=5000, numerics="strict",
+                                                 cfl=0.2)
+    b = hw.batch(probs, method="mstvd")
+    u = torch.from_numpy(b.pack(lines)).cuda()
+    t = np.zeros(len(probs))
+    b.advance(u, t, dts, 10)
+    b.tune(u, dts, probe_steps=2)
+    b.advance(u, t, dts, 7)
+    got = b.unpack(u)
+    for i, p in enumerate(probs):
+        o = orc.ODE(p, int(p.ncells[0]), 1)
+        uo = lines[i].copy()
+        tt = o.integrate(uo, 0.0, (4 + 17 - 0.5) * dts[i], dts[i])
+        assert tt == t[i] and np.array_equal(got[i], uo), i
+    assert list(b.steps_done) == [21] * len(probs)
