@@ -673,6 +673,19 @@ static int ode_create(const hrw_problem* p, int neq, int order, int method, int 
         q += (size_t)(L.nc + 63) / 64 * 64;
       }
     }
+    if (nd == 2 && p->flux == HRW_FLUX_GODUNOV) {
+      // upwind when g > 0 at every interface in FP32: the kernels evaluate g(x_e) from the float
+      // a, b, rx, xmin, which differs from this FP64 evaluation of the same floats by a few FP32
+      // roundings, far inside a 1e-5 margin
+      bool up = true;
+      for (int d = 0; d < 2; ++d) {
+        const LineF& F = d == 0 ? f.L : f.L2;
+        LineArgs G{};
+        G.nc = F.nc, G.fn = F.fn, G.a = F.a, G.b = F.b, G.xmin = F.xmin, G.rx = F.rx;
+        up = up && positive_velocity(G, 1e-5);
+      }
+      f.upwind = up;
+    }
     o->istate = 1;
     *out = o;
     return HRW_OK;

@@ -3,6 +3,8 @@
 // kernels' bounded tile wait, and the FAST reciprocal next to IEEE division.
 #include <string>
 
+#include <atomic>
+
 #include <cuda_runtime.h>
 
 #include "../../include/hrweno_diag.h"
@@ -105,5 +107,10 @@ extern "C" int hrw_diag_mixed_hard_warps(unsigned long long* count, int reset) {
   if (!count) return hrw::set_error(HRW_EINVAL, "Invalid input: null pointer.");
   const cudaError_t e = hrw::mixed_hard_warps(count, reset != 0);
   if (e != cudaSuccess) return hrw::set_error(HRW_ECUDA, cudaGetErrorString(e));
+  return HRW_OK;
+}
+
+extern "C" int hrw_diag_upwind(int enable) {
+  hrw::g_upwind_enabled.store(enable != 0 ? 1 : 0, std::memory_order_relaxed);
   return HRW_OK;
 }

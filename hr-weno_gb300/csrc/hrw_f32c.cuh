@@ -122,7 +122,9 @@ __device__ __forceinline__ void recon_diff(const float* d, float eps, float& rl,
 
 // K = 3 reconstruction of one cell with the 13/12 (second difference)^2 terms of its three
 // indicators precomputed (neighbouring cells share them): t0, t1, t2 for beta0, beta1, beta2.
-// Same weights and candidates as recon_diff<3>.
+// Same weights and candidates as recon_diff<3>.  WL = false computes rr only (rl untouched),
+// with the same operations for rr: an upwind flux needs the left state of each interface alone.
+template <bool WL = true>
 __device__ __forceinline__ void recon_diff3_shared(const float* d, float t0, float t1, float t2,
                                                    float eps, float& rl, float& rr) {
   const float dmm = d[0], dm = d[1], d0 = d[2], d1 = d[3];
@@ -136,16 +138,20 @@ __device__ __forceinline__ void recon_diff3_shared(const float* d, float t0, flo
   if (fmaxf(s0, fmaxf(s1, s2)) < 1e18f) {
     const float P0 = s1 * s2, P1 = s0 * s2, P2 = s0 * s1;
     const float den = fmaf(3.f, P0, fmaf(6.f, P1, P2));
-    const float dent = fmaf(3.f, P2, fmaf(6.f, P1, P0));
     const float num = fmaf(3.f * P0, R0, fmaf(6.f * P1, R1, P2 * R2));
-    const float numt = fmaf(P0, L0, fmaf(6.f * P1, L1, 3.f * P2 * L2));
     rr = (num * rcpf(den)) * (1.f / 6.f);
-    rl = (numt * rcpf(dent)) * (1.f / 6.f);
+    if constexpr (WL) {
+      const float dent = fmaf(3.f, P2, fmaf(6.f, P1, P0));
+      const float numt = fmaf(P0, L0, fmaf(6.f * P1, L1, 3.f * P2 * L2));
+      rl = (numt * rcpf(dent)) * (1.f / 6.f);
+    }
   } else {
     const float a0 = 0.3f / s0, a1 = 0.6f / s1, a2 = 0.1f / s2;
-    const float u0 = 0.1f / s0, u1 = 0.6f / s1, u2 = 0.3f / s2;
     rr = (a0 * R0 + a1 * R1 + a2 * R2) / (6.f * (a0 + a1 + a2));
-    rl = (u0 * L0 + u1 * L1 + u2 * L2) / (6.f * (u0 + u1 + u2));
+    if constexpr (WL) {
+      const float u0 = 0.1f / s0, u1 = 0.6f / s1, u2 = 0.3f / s2;
+      rl = (u0 * L0 + u1 * L1 + u2 * L2) / (6.f * (u0 + u1 + u2));
+    }
   }
 }
 
@@ -249,6 +255,18 @@ __device__ __forceinline__ float flux_diff_interior(const LineF& L, int j, float
   const float GR = flux_g_t<FK>(L, v, rr_j, d_j + rl_p, gR);
   const float extra = lin ? L.gstep * v : 0.f;
   return __fadd_rn(GR - GL, extra);
+}
+
+// flux_diff_f32c of an interior cell when the flux is Godunov's of f = g(x) u with g > 0 at
+// every interface: F = g vm exactly (flux_g_t<3> picks g a for any finite right state, g > 0
+// and rounding being monotone), so G_L = g_L (rr_{j-1} - d_{j-1}) and G_R = g_R rr_j, the same
+// bits as flux_diff_interior with the right states.  The products are rounded on their own
+// (no contraction of G_R - G_L into a multiply-add), as there the min/max stands between them.
+__device__ __forceinline__ float flux_diff_upwind(const LineF& L, int j, float v, float rr_m,
+                                                  float d_m, float rr_j) {
+  const float GL = __fmul_rn(g_at(L, j), rr_m - d_m);
+  const float GR = __fmul_rn(g_at(L, j + 1), rr_j);
+  return __fadd_rn(GR - GL, L.gstep * v);
 }
 
 // Stage update of one cell in increment form.  h, l: the state u = h + l; dv: the stored

@@ -1,5 +1,6 @@
 // hrw_internal.h - host-side declarations shared by the C-ABI and the kernel launchers.
 #pragma once
+#include <atomic>
 #include <cstdint>
 
 #include <cuda_runtime.h>
@@ -116,6 +117,9 @@ struct F32CArgs {
   float lscale2;
   int64_t ld;
   unsigned int* timeout_flag;  // 2D stages: as StageArgs::timeout_flag
+  // 2D: Godunov's flux of linear fluxes g(x) u with g > 0 at every interface of both lines in
+  // FP32: only the left state of each interface is reconstructed (stage2d_f32c.cu)
+  int upwind;
 };
 
 // ---- MIXED numerics (hrw_mixed.cuh, stage1d_mixed.cu) --------------------------------------
@@ -176,6 +180,9 @@ int set_error(int code, const char* msg);
 // True when the line's flux is g(x) u with g > 0 at every interface (upwind Godunov), with g
 // at the line ends above rel_margin (|a| + |b x|).
 bool positive_velocity(const LineArgs& L, double rel_margin = 1e-12);
+// 0 turns the upwind specialisation of the 2D kernels off for handles created afterwards (a
+// test hook, hrw_diag_upwind: the general flux path gives the same bits)
+extern std::atomic<int> g_upwind_enabled;
 
 // 1D fused stage over nc cells; k in 1..3; strict selects the reference-order numerics.
 cudaError_t launch_stage1d(const StageArgs& a, int k, int stage, bool strict, cudaStream_t s);

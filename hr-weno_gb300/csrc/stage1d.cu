@@ -30,7 +30,10 @@ double fast_flux_scale(int flux, int fn) {
   return fn == HRW_FN_LINEAR ? 1.0 : 0.5;
 }
 
+std::atomic<int> g_upwind_enabled{1};
+
 bool positive_velocity(const LineArgs& L, double rel_margin) {
+  if (!g_upwind_enabled.load(std::memory_order_relaxed)) return false;
   if (L.fn != HRW_FN_LINEAR) return false;
   // g(x_e) = a + b*(xmin + rx*e) is monotone in e under any rounding of its three operations,
   // so its minimum over the interfaces e = 0..nc sits at an end; the margin stays far above

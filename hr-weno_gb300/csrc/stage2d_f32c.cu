@@ -51,8 +51,9 @@ constexpr int kTileWaitPolls = 1 << 20;
 __device__ int g_tile_wait_limit = kTileWaitPolls;
 
 // WENO offsets of the C cells of a segment from its differences d[0 .. C+2K-2]; for k = 3 the
-// 13/12 (second difference)^2 terms are computed once per window position (as the 1D pass)
-template <int K>
+// 13/12 (second difference)^2 terms are computed once per window position (as the 1D pass).
+// WL = false (upwind, k = 3): rr only.
+template <int K, bool WL = true>
 __device__ __forceinline__ void segment_recon(const float* d, float eps, float* rl, float* rr) {
   if constexpr (K == 3) {
     float t[C + 4];
@@ -62,7 +63,8 @@ __device__ __forceinline__ void segment_recon(const float* d, float eps, float* 
       t[m] = (13.f / 12.f) * D * D;
     }
 #pragma unroll
-    for (int c = 0; c < C; ++c) recon_diff3_shared(&d[c + 1], t[c + 4], t[c + 3], t[c + 2], eps, rl[c], rr[c]);
+    for (int c = 0; c < C; ++c)
+      recon_diff3_shared<WL>(&d[c + 1], t[c + 4], t[c + 3], t[c + 2], eps, rl[c], rr[c]);
   } else {
 #pragma unroll
     for (int c = 0; c < C; ++c) recon_diff<K>(&d[c + 1], eps, rl[c], rr[c]);
@@ -70,7 +72,7 @@ __device__ __forceinline__ void segment_recon(const float* d, float eps, float* 
 }
 
 // one cell's offsets from its 2K-2 differences (tile-edge cells), the same arithmetic
-template <int K>
+template <int K, bool WL = true>
 __device__ __forceinline__ void cell_recon(const float* de, float eps, float& el, float& er) {
   if constexpr (K == 3) {
     float te[3];
@@ -79,7 +81,7 @@ __device__ __forceinline__ void cell_recon(const float* de, float eps, float& el
       const float D = de[q + 1] - de[q];
       te[q] = (13.f / 12.f) * D * D;
     }
-    recon_diff3_shared(de, te[2], te[1], te[0], eps, el, er);
+    recon_diff3_shared<WL>(de, te[2], te[1], te[0], eps, el, er);
   } else {
     recon_diff<K>(de, eps, el, er);
   }
@@ -87,11 +89,16 @@ __device__ __forceinline__ void cell_recon(const float* de, float eps, float& el
 
 // flux difference of cell j of a segment: `interior` (no cell of the segment on the line's
 // ends) takes the path without the boundary rules when the numerical flux is known (FKI = 4
-// Lax-Friedrichs, 5 Godunov; the flux function is a uniform branch), with the same arithmetic
-template <int FKI>
+// Lax-Friedrichs, 5 Godunov; the flux function is a uniform branch), with the same arithmetic;
+// UPW (upwind Godunov of g u, g > 0): the interior takes flux_diff_upwind, and the line's end
+// cells the general path with any right states (rl = 0), which the upwind flux ignores
+template <int FKI, bool UPW = false>
 __device__ __forceinline__ float seg_flux(const LineF& L, bool interior, int j, float v, float rr_m,
                                           float d_m, float rl_j, float rr_j, float d_j, float rl_p) {
-  if constexpr (FKI >= 0) {
+  if constexpr (UPW) {
+    if (interior) return flux_diff_upwind(L, j, v, rr_m, d_m, rr_j);
+    return flux_diff_f32c_call(L, j, v, rr_m, d_m, 0.f, rr_j, d_j, 0.f);
+  } else if constexpr (FKI >= 0) {
     if (interior) return flux_diff_interior<FKI>(L, j, v, rr_m, d_m, rl_j, rr_j, d_j, rl_p);
     return flux_diff_f32c_call(L, j, v, rr_m, d_m, rl_j, rr_j, d_j, rl_p);
   } else {
@@ -99,9 +106,10 @@ __device__ __forceinline__ float seg_flux(const LineF& L, bool interior, int j, 
   }
 }
 
-template <int K, int ST, bool TMA, bool HAS_DV, int FKI>
+template <int K, int ST, bool TMA, bool HAS_DV, int FKI, bool UPW = false>
 __global__ void __launch_bounds__(NT) stage2d_f32c_kernel(const __grid_constant__ TileMaps M,
                                                           F32CArgs a) {
+  static_assert(!UPW || K == 3, "the upwind pass is written for k = 3");
   constexpr int H = K;
   constexpr int RW = TX + 2 * H, SW = RW + 1, SQ = TX + 1;
   constexpr int NSX = TX / C, NSY = TY / C;
@@ -142,14 +150,25 @@ __global__ void __launch_bounds__(NT) stage2d_f32c_kernel(const __grid_constant_
       mbar_wait(&bar, 0, kTileWaitPolls);
       return;
     }
-    for (int q = tid; q < (TY + 2 * H) * RW; q += NT) {
-      const int row = q / RW, col = q - row * RW;
-      int gy = by - H + row, gx = bx - H + col;
-      gy = gy < 0 ? 0 : (gy >= n2 ? n2 - 1 : gy);
-      gx = gx < 0 ? 0 : (gx >= n1 ? n1 - 1 : gx);
-      const int src = (gy - (by - 3)) * BX + (gx - (bx - 4));
-      sh[row * SW + col] = tb[0][src];
-      sm[row * SW + col] = HAS_DV ? tb[1][src] + tb[NB - 1][src] : tb[1][src];
+    if (bx >= H && bx + TX + H <= n1 && by >= H && by + TY + H <= n2) {
+      // no ghost cell in the tile: row by row, a warp per row and a lane per column
+      for (int row = warp; row < TY + 2 * H; row += NT / 32) {
+        const int src = (row + 3 - H) * BX + 4 - H;
+        for (int col = lane; col < RW; col += 32) {
+          sh[row * SW + col] = tb[0][src + col];
+          sm[row * SW + col] = HAS_DV ? tb[1][src + col] + tb[NB - 1][src + col] : tb[1][src + col];
+        }
+      }
+    } else {
+      for (int q = tid; q < (TY + 2 * H) * RW; q += NT) {
+        const int row = q / RW, col = q - row * RW;
+        int gy = by - H + row, gx = bx - H + col;
+        gy = gy < 0 ? 0 : (gy >= n2 ? n2 - 1 : gy);
+        gx = gx < 0 ? 0 : (gx >= n1 ? n1 - 1 : gx);
+        const int src = (gy - (by - 3)) * BX + (gx - (bx - 4));
+        sh[row * SW + col] = tb[0][src];
+        sm[row * SW + col] = HAS_DV ? tb[1][src] + tb[NB - 1][src] : tb[1][src];
+      }
     }
   } else {
     for (int q = tid; q < (TY + 2 * H) * RW; q += NT) {
@@ -185,8 +204,8 @@ __global__ void __launch_bounds__(NT) stage2d_f32c_kernel(const __grid_constant_
 #pragma unroll
     for (int q = 0; q < C + 2 * K - 1; ++q)
       d[q] = (sh[base + q + 1] - sh[base + q]) + (sm[base + q + 1] - sm[base + q]);
-    segment_recon<K>(d, a.eps, rl, rr);
-    sLx[r * (NSX + 1) + sg] = rl[0];
+    segment_recon<K, !UPW>(d, a.eps, rl, rr);
+    if constexpr (!UPW) sLx[r * (NSX + 1) + sg] = rl[0];
     sRx[r * (NSX + 1) + sg + 1] = rr[C - 1];
   }
   // tile-edge cells: warp 0 rr of x1 = bx-1, warp 1 rl of x1 = bx+TX, warp 2 rr of x2 = by-1,
@@ -201,17 +220,19 @@ __global__ void __launch_bounds__(NT) stage2d_f32c_kernel(const __grid_constant_
       p = (warp == 2 ? H - 1 : H + TY) * SW + H + lane;
       stride = SW;
     }
+    if (!UPW || warp == 0 || warp == 2) {  // upwind: the right-edge cells' rl are not needed
 #pragma unroll
-    for (int q = 0; q < 2 * K - 2; ++q) {
-      const int m0 = p + (q - (K - 1)) * stride, m1 = m0 + stride;
-      de[q] = (sh[m1] - sh[m0]) + (sm[m1] - sm[m0]);
+      for (int q = 0; q < 2 * K - 2; ++q) {
+        const int m0 = p + (q - (K - 1)) * stride, m1 = m0 + stride;
+        de[q] = (sh[m1] - sh[m0]) + (sm[m1] - sm[m0]);
+      }
+      float el, er;
+      cell_recon<K, !UPW>(de, a.eps, el, er);
+      if (warp == 0) sRx[lane * (NSX + 1)] = er;
+      else if (warp == 1) sLx[lane * (NSX + 1) + NSX] = el;
+      else if (warp == 2) sRy[lane] = er;
+      else sLy[NSY * TX + lane] = el;
     }
-    float el, er;
-    cell_recon<K>(de, a.eps, el, er);
-    if (warp == 0) sRx[lane * (NSX + 1)] = er;
-    else if (warp == 1) sLx[lane * (NSX + 1) + NSX] = el;
-    else if (warp == 2) sRy[lane] = er;
-    else sLy[NSY * TX + lane] = el;
   }
   __syncthreads();
 
@@ -227,9 +248,10 @@ __global__ void __launch_bounds__(NT) stage2d_f32c_kernel(const __grid_constant_
         const int lj = (r + H) * SW + H + sg * C + c;
         const float v = sh[lj] + sm[lj];
         const float rr_m = c == 0 ? sRx[r * (NSX + 1) + sg] : rr[c - 1];
-        const float rl_p = c == C - 1 ? sLx[r * (NSX + 1) + sg + 1] : rl[c + 1];
+        const float rl_j = UPW ? 0.f : rl[c];
+        const float rl_p = UPW ? 0.f : (c == C - 1 ? sLx[r * (NSX + 1) + sg + 1] : rl[c + 1]);
         const float dF =
-            seg_flux<FKI>(L1, interior, gx, v, rr_m, d[c + K - 1], rl[c], rr[c], d[c + K], rl_p);
+            seg_flux<FKI, UPW>(L1, interior, gx, v, rr_m, d[c + K - 1], rl_j, rr[c], d[c + K], rl_p);
         t = -dF;
       }
       sq[r * SQ + sg * C + c] = t;
@@ -245,8 +267,8 @@ __global__ void __launch_bounds__(NT) stage2d_f32c_kernel(const __grid_constant_
       const int m0 = base + q * SW, m1 = m0 + SW;
       d[q] = (sh[m1] - sh[m0]) + (sm[m1] - sm[m0]);
     }
-    segment_recon<K>(d, a.eps, rl, rr);
-    sLy[sy * TX + col] = rl[0];
+    segment_recon<K, !UPW>(d, a.eps, rl, rr);
+    if constexpr (!UPW) sLy[sy * TX + col] = rl[0];
     sRy[(sy + 1) * TX + col] = rr[C - 1];
   }
   __syncthreads();
@@ -272,9 +294,10 @@ __global__ void __launch_bounds__(NT) stage2d_f32c_kernel(const __grid_constant_
     const int lj = (ly + H) * SW + H + col;
     const float v = sh[lj] + sm[lj];
     const float rr_m = c == 0 ? sRy[sy * TX + col] : rr[c - 1];
-    const float rl_p = c == C - 1 ? sLy[(sy + 1) * TX + col] : rl[c + 1];
+    const float rl_j = UPW ? 0.f : rl[c];
+    const float rl_p = UPW ? 0.f : (c == C - 1 ? sLy[(sy + 1) * TX + col] : rl[c + 1]);
     const float dF2 =
-        seg_flux<FKI>(L2, interior, gy, v, rr_m, d[c + K - 1], rl[c], rr[c], d[c + K], rl_p);
+        seg_flux<FKI, UPW>(L2, interior, gy, v, rr_m, d[c + K - 1], rl_j, rr[c], d[c + K], rl_p);
     const float q1 = L1.rw ? sq[ly * SQ + col] * L1.rw[gx] : sq[ly * SQ + col];
     const float q2 = L2.rw ? -dF2 * L2.rw[gy] : -dF2;
     // dt L = c1 q1 + c2 q2 with the dt/dx float pairs; L = q1/dx1 + q2/dx2
@@ -303,6 +326,8 @@ cudaError_t launch_kt(const TileMaps& M, const F32CArgs& a, cudaStream_t s) {
   if constexpr (K == 3 && TMA) {
     if (a.L.flux == HRW_FLUX_LAX_FRIEDRICHS)
       stage2d_f32c_kernel<K, ST, TMA, HAS_DV, 4><<<grid, NT, 0, s>>>(M, a);
+    else if (a.upwind)
+      stage2d_f32c_kernel<K, ST, TMA, HAS_DV, 5, true><<<grid, NT, 0, s>>>(M, a);
     else
       stage2d_f32c_kernel<K, ST, TMA, HAS_DV, 5><<<grid, NT, 0, s>>>(M, a);
   } else {

@@ -4,8 +4,8 @@
  * The stage kernels of the FP64 path are bound by the FP64 pipe, not by HBM; one call
  * measures that pipe on the current device so that a benchmark can report the kernel's
  * fraction of it next to its HBM roofline fraction.  The others expose internals to the tests:
- * the 2D kernels' bounded wait, the FAST path's reciprocal, and the MIXED kernel's choice
- * between its FP32 and FP64 paths.
+ * the 2D kernels' bounded wait, the FAST path's reciprocal, the MIXED kernel's choice
+ * between its FP32 and FP64 paths, and the 2D kernels' upwind specialisation.
  */
 #ifndef HRWENO_DIAG_H
 #define HRWENO_DIAG_H
@@ -36,6 +36,11 @@ int hrw_diag_mixed_soft(int enable);
 /* Warps of the MIXED stage kernel, away from the line ends, that took the FP64 path since the
  * last reset (*count; reset != 0 clears the counter), on the current device. */
 int hrw_diag_mixed_hard_warps(unsigned long long* count, int reset);
+/* enable = 0: handles created afterwards do not take the upwind specialisation of the 2D
+ * kernels (Godunov's flux of g(x) u with g > 0 everywhere reconstructs only the left state of
+ * each interface); 1 restores it.  Process-wide.  Tests use it to check that both give the
+ * same bits. */
+int hrw_diag_upwind(int enable);
 
 #ifdef __cplusplus
 }

@@ -168,3 +168,36 @@ def test_f32c_pbe1024_vs_fp64_gpu(hw):
     hw.mstvd(prob, n * n, dtype="f32c").integrate(b, 0.0, 499.5 * dt, dt)
     l1 = float((a - b).abs().sum() / a.abs().sum())
     assert l1 <= 1e-6, l1
+
+
+# ---- the 2D upwind specialisation gives the general path's bits --------------------------------
+@pytest.mark.parametrize("n1,n2", [(64, 48), (128, 96), (100, 37)])
+@pytest.mark.parametrize("bc", ["zero_inflow", "zero", "copy"])
+def test_pbe_2d_upwind_same_bits(hw, n1, n2, bc):
+    """Godunov's flux of g(x) u with g > 0 everywhere: the upwind kernels reconstruct only the
+    left state of each interface (F = g vm exactly).  Handles created with the specialisation
+    off (hrw_diag_upwind(0)) take the general flux path: the compensated FP32 mstvd and
+    right-hand side, and the FP64 STRICT rktvd, give the same bits either way (n1 a multiple of
+    4: TMA tiles; 100: gathered).  (FP64 FAST's upwind pass takes one reciprocal per cell of its
+    own, so it agrees with the general pass to rounding only.)"""
+    import torch
+    from hrweno import _abi as A, workloads
+    L = A.lib()
+    L.hrw_diag_upwind.argtypes = [C.c_int]
+    prob, n0, dt = workloads.pbe_config(n1, n2, cfl=0.3, bc=bc)
+    sprob, _, _ = workloads.pbe_config(n1, n2, cfl=0.3, bc=bc, numerics="strict")
+    outs = []
+    try:
+        for enable in (1, 0):
+            assert L.hrw_diag_upwind(enable) == 0
+            res = []
+            for ode in (hw.mstvd(prob, n1 * n2, dtype="f32c"), hw.rktvd(sprob, n1 * n2, 3)):
+                u = torch.from_numpy(n0.copy()).cuda()
+                ode.integrate(u, 0.0, 30.5 * dt, dt)
+                res.append(u.cpu().numpy())
+            res.append(rhs_f32c(prob, n0))
+            outs.append(res)
+    finally:
+        L.hrw_diag_upwind(1)
+    for name, a, b in zip(("f32c mstvd", "f64 strict rktvd", "f32c rhs"), *outs):
+        assert np.array_equal(a, b), (name, float(np.max(np.abs(a - b))))
