@@ -35,9 +35,12 @@ constexpr int NT = kBatchThreads;
 
 
 // One warp-pass of stage ST over cells j0 .. j0 + C - 1 of this lane (all 32 lanes call it).
-template <int K, int ST, bool STRICT, int C>
+// NU: a non-uniform line (a.cnu, L.width, L.rws, L.xe): each cell reconstructs with its own
+// coefficients and divides by its own width, as stage1d_nu.cu.
+template <int K, int ST, bool STRICT, int C, bool NU>
 __device__ __forceinline__ void stage_pass(const StageArgs& a, const LineArgs& L, int64_t j0,
                                            int lane) {
+  constexpr int NCF = K * (K + 1);  // coefficients per cell
   const int64_t nc = L.nc;
   double w[C + 2 * K];  // w[q] = v(j0 - K + q), ghosts replicate v(1), v(nc)
 #pragma unroll
@@ -47,7 +50,13 @@ __device__ __forceinline__ void stage_pass(const StageArgs& a, const LineArgs& L
     w[q] = a.v[g];
   }
   double vl[C], vr[C];
-  if constexpr (STRICT) {
+  if constexpr (NU) {
+#pragma unroll
+    for (int c = 0; c < C; ++c) {
+      const int64_t jc = j0 + c < nc ? j0 + c : nc - 1;
+      recon_nu<K, STRICT>(&w[K + c], a.cnu + NCF * jc, a.eps, vl[c], vr[c]);
+    }
+  } else if constexpr (STRICT) {
 #pragma unroll
     for (int c = 0; c < C; ++c) recon_strict<K>(&w[K + c], a.eps, vl[c], vr[c]);
   } else {
@@ -60,8 +69,15 @@ __device__ __forceinline__ void stage_pass(const StageArgs& a, const LineArgs& L
 #pragma unroll
   for (int q = 0; q < 2 * K - 1; ++q) e[q] = lane == 31 ? w[C + 1 + q] : w[q];
   double el, er;
-  if constexpr (STRICT) recon_strict<K>(&e[K - 1], a.eps, el, er);
-  else recon_fast_one<K>(&e[K - 1], a.eps, el, er);
+  if constexpr (NU) {
+    int64_t je = lane == 31 ? j0 + C : j0 - 1;
+    je = je < 0 ? 0 : (je >= nc ? nc - 1 : je);
+    recon_nu<K, STRICT>(&e[K - 1], a.cnu + NCF * je, a.eps, el, er);
+  } else if constexpr (STRICT) {
+    recon_strict<K>(&e[K - 1], a.eps, el, er);
+  } else {
+    recon_fast_one<K>(&e[K - 1], a.eps, el, er);
+  }
   const double vr_up = __shfl_up_sync(FULL, vr[C - 1], 1);
   const double vl_dn = __shfl_down_sync(FULL, vl[0], 1);
   const double vr_m = lane == 0 ? er : vr_up;
@@ -76,25 +92,25 @@ __device__ __forceinline__ void stage_pass(const StageArgs& a, const LineArgs& L
     const int64_t j = j0 + c;
     if (j >= nc) break;
     const double dF = flux_diff<STRICT>(L, j, F[c], F[c + 1], vr[c]);
-    if constexpr (STRICT) combine_strict<ST>(a, j, w[K + c], __ddiv_rn(-dF, L.rx));
-    else combine_fast<ST>(a, j, w[K + c], dF, L.rws0);
+    if constexpr (STRICT) combine_strict<ST>(a, j, w[K + c], __ddiv_rn(-dF, NU ? L.width[j] : L.rx));
+    else combine_fast<ST>(a, j, w[K + c], dF, NU ? L.rws[j] : L.rws0);
   }
 }
 
-template <int K, int ST, bool STRICT, int G, int C>
+template <int K, int ST, bool STRICT, int G, int C, bool NU>
 __device__ __forceinline__ void stage_sweep(const StageArgs& a, const LineArgs& L, int lt, int gid) {
   const int lane = lt & 31;
   const int warp_in_group = lt >> 5;
   for (int64_t base = 0; base < L.nc; base += (int64_t)G * C) {
     const int64_t wbase = base + (int64_t)warp_in_group * 32 * C;
-    if (wbase < L.nc) stage_pass<K, ST, STRICT, C>(a, L, wbase + (int64_t)lane * C, lane);
+    if (wbase < L.nc) stage_pass<K, ST, STRICT, C, NU>(a, L, wbase + (int64_t)lane * C, lane);
   }
   group_sync<G>(gid);
 }
 
-// all steps of one problem
-template <int K, bool STRICT, int G, int C>
-__device__ void run_problem(const BatchArgs& B, const BatchProblem& P, int lt, int gid) {
+// the line of problem P as the stage code sees it (with its non-uniform arrays when NU)
+template <bool NU>
+__device__ __forceinline__ LineArgs problem_line(const BatchProblem& P) {
   LineArgs L{};
   L.nc = P.nc;
   L.fn = P.fn;
@@ -106,31 +122,44 @@ __device__ void run_problem(const BatchArgs& B, const BatchProblem& P, int lt, i
   L.xmin = P.xmin;
   L.rx = P.rx;
   L.rws0 = P.rws0;
+  if constexpr (NU) {
+    L.width = P.width;
+    L.rws = P.rws;
+    L.xe = P.xe;
+  }
+  return L;
+}
+
+// all steps of one problem
+template <int K, bool STRICT, int G, int C, bool NU>
+__device__ void run_problem(const BatchArgs& B, const BatchProblem& P, int lt, int gid) {
+  const LineArgs L = problem_line<NU>(P);
   double* u = B.u + P.off;
   double* u1 = B.u1 + P.off;
   double* u2 = B.u2 + P.off;
   StageArgs a{};
   a.eps = P.eps;
   a.dt = P.dt;
+  if constexpr (NU) a.cnu = P.cnu;
   for (int64_t n = 0; n < P.nsteps; ++n) {
     if (B.order == 1) {  // u' = u + dt L(u): out of place, then copied back by the next pass
       a.v = u, a.u = u, a.out = u1;
-      stage_sweep<K, ST_EULER, STRICT, G, C>(a, L, lt, gid);
+      stage_sweep<K, ST_EULER, STRICT, G, C, NU>(a, L, lt, gid);
       for (int64_t j = lt; j < L.nc; j += G) u[j] = u1[j];
       group_sync<G>(gid);
       continue;
     }
     a.v = u, a.u = u, a.out = u1;  // (src/hrweno_tvdode.f90:148-150 / 161-163)
-    stage_sweep<K, ST_EULER, STRICT, G, C>(a, L, lt, gid);
+    stage_sweep<K, ST_EULER, STRICT, G, C, NU>(a, L, lt, gid);
     if (B.order == 2) {  // (:151-152)
       a.v = u1, a.u = u, a.out = u;
-      stage_sweep<K, ST_RK2B, STRICT, G, C>(a, L, lt, gid);
+      stage_sweep<K, ST_RK2B, STRICT, G, C, NU>(a, L, lt, gid);
       continue;
     }
     a.v = u1, a.u = u, a.out = u2;  // (:164-165)
-    stage_sweep<K, ST_RK3B, STRICT, G, C>(a, L, lt, gid);
+    stage_sweep<K, ST_RK3B, STRICT, G, C, NU>(a, L, lt, gid);
     a.v = u2, a.u = u, a.out = u;  // (:166-167)
-    stage_sweep<K, ST_RK3C, STRICT, G, C>(a, L, lt, gid);
+    stage_sweep<K, ST_RK3C, STRICT, G, C, NU>(a, L, lt, gid);
   }
 }
 
@@ -138,19 +167,9 @@ __device__ void run_problem(const BatchArgs& B, const BatchProblem& P, int lt, i
 // ring slot, the RK3 start (:236-249) runs on the problem's first call, then P.nsteps
 // multistep steps (:252-268), each reading u^m, u^{m-4}, L(u^{m-4}) and writing u^{m+1} and
 // L(u^m) over the two oldest entries; the newest state is copied back to u.
-template <int K, bool STRICT, int G, int C>
+template <int K, bool STRICT, int G, int C, bool NU>
 __device__ void run_problem_ms(const BatchArgs& B, const BatchProblem& P, int lt, int gid) {
-  LineArgs L{};
-  L.nc = P.nc;
-  L.fn = P.fn;
-  L.bc = P.bc;
-  L.flux = P.flux;
-  L.a = P.a;
-  L.b = P.b;
-  L.alpha = P.alpha;
-  L.xmin = P.xmin;
-  L.rx = P.rx;
-  L.rws0 = P.rws0;
+  const LineArgs L = problem_line<NU>(P);
   double* u = B.u + P.off;
   double* u1 = B.u1 + P.off;
   double* u2 = B.u2 + P.off;
@@ -163,6 +182,7 @@ __device__ void run_problem_ms(const BatchArgs& B, const BatchProblem& P, int lt
   StageArgs a{};
   a.eps = P.eps;
   a.dt = P.dt;
+  if constexpr (NU) a.cnu = P.cnu;
   int64_t level = P.level;
   double* cur = R[P.start ? 0 : level % 5];
   for (int64_t j = lt; j < L.nc; j += G) cur[j] = u[j];
@@ -171,13 +191,13 @@ __device__ void run_problem_ms(const BatchArgs& B, const BatchProblem& P, int lt
     for (int m = 0; m < 4; ++m) {
       double* um = R[m % 5];
       a.v = um, a.u = um, a.out = Lr[m % 4];
-      stage_sweep<K, ST_RHS, STRICT, G, C>(a, L, lt, gid);
+      stage_sweep<K, ST_RHS, STRICT, G, C, NU>(a, L, lt, gid);
       a.v = um, a.u = um, a.out = u1;
-      stage_sweep<K, ST_EULER, STRICT, G, C>(a, L, lt, gid);
+      stage_sweep<K, ST_EULER, STRICT, G, C, NU>(a, L, lt, gid);
       a.v = u1, a.u = um, a.out = u2;
-      stage_sweep<K, ST_RK3B, STRICT, G, C>(a, L, lt, gid);
+      stage_sweep<K, ST_RK3B, STRICT, G, C, NU>(a, L, lt, gid);
       a.v = u2, a.u = um, a.out = R[(m + 1) % 5];
-      stage_sweep<K, ST_RK3C, STRICT, G, C>(a, L, lt, gid);
+      stage_sweep<K, ST_RK3C, STRICT, G, C, NU>(a, L, lt, gid);
     }
     level = 4;
   }
@@ -186,14 +206,16 @@ __device__ void run_problem_ms(const BatchArgs& B, const BatchProblem& P, int lt
     double* un = R[(level + 1) % 5];  // holds u^{m-4}, overwritten with u^{m+1}
     double* lm = Lr[level % 4];       // holds L(u^{m-4}), overwritten with L(u^m)
     a.v = um, a.u = um, a.out = un, a.lout = lm, a.uo4 = un, a.lo4 = lm;
-    stage_sweep<K, ST_MS, STRICT, G, C>(a, L, lt, gid);
+    stage_sweep<K, ST_MS, STRICT, G, C, NU>(a, L, lt, gid);
   }
   cur = R[level % 5];
   for (int64_t j = lt; j < L.nc; j += G) u[j] = cur[j];
   group_sync<G>(gid);
 }
 
-template <bool STRICT, int G, int C>
+// NU: a launch of the batch's non-uniform lines (the uniform ones run in the tuned launches of
+// their size classes), one shape for all of them
+template <bool STRICT, int G, int C, bool NU>
 __global__ void __launch_bounds__(NT, 1) batch_kernel(BatchArgs B) {
   static_assert(NT % G == 0 && G % 32 == 0 && NT / G <= 15, "groups of whole warps");
   constexpr int GPB = NT / G;
@@ -208,56 +230,111 @@ __global__ void __launch_bounds__(NT, 1) batch_kernel(BatchArgs B) {
     const BatchProblem P = B.probs[B.order_idx[pid]];
     if (P.nsteps <= 0 && !P.start) continue;
     if (B.method == 1) {
-      if (P.k == 3) run_problem_ms<3, STRICT, G, C>(B, P, lt, gid);
-      else if (P.k == 2) run_problem_ms<2, STRICT, G, C>(B, P, lt, gid);
-      else run_problem_ms<1, STRICT, G, C>(B, P, lt, gid);
+      if (P.k == 3) run_problem_ms<3, STRICT, G, C, NU>(B, P, lt, gid);
+      else if (P.k == 2) run_problem_ms<2, STRICT, G, C, NU>(B, P, lt, gid);
+      else run_problem_ms<1, STRICT, G, C, NU>(B, P, lt, gid);
     } else {
-      if (P.k == 3) run_problem<3, STRICT, G, C>(B, P, lt, gid);
-      else if (P.k == 2) run_problem<2, STRICT, G, C>(B, P, lt, gid);
-      else run_problem<1, STRICT, G, C>(B, P, lt, gid);
+      if (P.k == 3) run_problem<3, STRICT, G, C, NU>(B, P, lt, gid);
+      else if (P.k == 2) run_problem<2, STRICT, G, C, NU>(B, P, lt, gid);
+      else run_problem<1, STRICT, G, C, NU>(B, P, lt, gid);
     }
   }
 }
 
-template <bool STRICT, int G, int C>
+template <bool STRICT, int G, int C, bool NU = false>
 cudaError_t launch_shape(const BatchArgs& B, int blocks, cudaStream_t s) {
-  batch_kernel<STRICT, G, C><<<blocks, NT, 0, s>>>(B);
+  batch_kernel<STRICT, G, C, NU><<<blocks, NT, 0, s>>>(B);
   return cudaGetLastError();
 }
 
-template <bool STRICT, int G, int C>
+template <bool STRICT, int G, int C, bool NU = false>
 int occupancy() {
   int n = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_kernel<STRICT, G, C>, NT, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_kernel<STRICT, G, C, NU>, NT, 0);
   return n;
 }
 
 }  // namespace
 
+// The kernels of one numerics mode over every shape, and the non-uniform kernels.  The three
+// compile as separate objects, HRW_PART = 0 (FAST), 1 (STRICT), 2 (non-uniform lines), in
+// parallel; part 0 also holds the dispatch.  Built without HRW_PART, the file holds all.
+template <bool STRICT>
+int batch_occupancy(int shape) {
+  switch (shape) {
+    case 0: return occupancy<STRICT, 32, 2>();
+    case 1: return occupancy<STRICT, 32, 4>();
+    case 2: return occupancy<STRICT, 32, 8>();
+    case 3: return occupancy<STRICT, 128, 4>();
+    case 4: return occupancy<STRICT, 128, 8>();
+    default: return occupancy<STRICT, 256, 8>();
+  }
+}
+
+template <bool STRICT>
+cudaError_t batch_launch(const BatchArgs& B, int shape, int blocks, cudaStream_t s) {
+  switch (shape) {
+    case 0: return launch_shape<STRICT, 32, 2>(B, blocks, s);
+    case 1: return launch_shape<STRICT, 32, 4>(B, blocks, s);
+    case 2: return launch_shape<STRICT, 32, 8>(B, blocks, s);
+    case 3: return launch_shape<STRICT, 128, 4>(B, blocks, s);
+    case 4: return launch_shape<STRICT, 128, 8>(B, blocks, s);
+    case 5: return launch_shape<STRICT, 256, 8>(B, blocks, s);
+  }
+  return cudaErrorInvalidValue;
+}
+
+// the non-uniform lines: 128-thread groups, 4 cells per thread and pass
+template <bool STRICT>
+int batch_nu_occupancy() { return occupancy<STRICT, 128, 4, true>(); }
+template <bool STRICT>
+cudaError_t batch_nu_launch(const BatchArgs& B, int blocks, cudaStream_t s) {
+  return launch_shape<STRICT, 128, 4, true>(B, blocks, s);
+}
+
+extern template int batch_occupancy<false>(int);
+extern template int batch_occupancy<true>(int);
+extern template cudaError_t batch_launch<false>(const BatchArgs&, int, int, cudaStream_t);
+extern template cudaError_t batch_launch<true>(const BatchArgs&, int, int, cudaStream_t);
+extern template int batch_nu_occupancy<false>();
+extern template int batch_nu_occupancy<true>();
+extern template cudaError_t batch_nu_launch<false>(const BatchArgs&, int, cudaStream_t);
+extern template cudaError_t batch_nu_launch<true>(const BatchArgs&, int, cudaStream_t);
+#if !defined(HRW_PART) || HRW_PART == 0
+template int batch_occupancy<false>(int);
+template cudaError_t batch_launch<false>(const BatchArgs&, int, int, cudaStream_t);
+#endif
+#if !defined(HRW_PART) || HRW_PART == 1
+template int batch_occupancy<true>(int);
+template cudaError_t batch_launch<true>(const BatchArgs&, int, int, cudaStream_t);
+#endif
+#if !defined(HRW_PART) || HRW_PART == 2
+template int batch_nu_occupancy<false>();
+template int batch_nu_occupancy<true>();
+template cudaError_t batch_nu_launch<false>(const BatchArgs&, int, cudaStream_t);
+template cudaError_t batch_nu_launch<true>(const BatchArgs&, int, cudaStream_t);
+#endif
+
+#if !defined(HRW_PART) || HRW_PART == 0
 const BatchShape kBatchShapes[kNumBatchShapes] = {{32, 2}, {32, 4}, {32, 8}, {128, 4}, {128, 8}, {256, 8}};
 
 int batch_blocks_per_sm(int shape, bool strict) {
-  switch (shape) {
-    case 0: return strict ? occupancy<true, 32, 2>() : occupancy<false, 32, 2>();
-    case 1: return strict ? occupancy<true, 32, 4>() : occupancy<false, 32, 4>();
-    case 2: return strict ? occupancy<true, 32, 8>() : occupancy<false, 32, 8>();
-    case 3: return strict ? occupancy<true, 128, 4>() : occupancy<false, 128, 4>();
-    case 4: return strict ? occupancy<true, 128, 8>() : occupancy<false, 128, 8>();
-    default: return strict ? occupancy<true, 256, 8>() : occupancy<false, 256, 8>();
-  }
+  return strict ? batch_occupancy<true>(shape) : batch_occupancy<false>(shape);
 }
 
 cudaError_t launch_batch(const BatchArgs& B, int shape, bool strict, int blocks, cudaStream_t s) {
   if (B.nprob <= 0) return cudaSuccess;
-  switch (shape) {
-    case 0: return strict ? launch_shape<true, 32, 2>(B, blocks, s) : launch_shape<false, 32, 2>(B, blocks, s);
-    case 1: return strict ? launch_shape<true, 32, 4>(B, blocks, s) : launch_shape<false, 32, 4>(B, blocks, s);
-    case 2: return strict ? launch_shape<true, 32, 8>(B, blocks, s) : launch_shape<false, 32, 8>(B, blocks, s);
-    case 3: return strict ? launch_shape<true, 128, 4>(B, blocks, s) : launch_shape<false, 128, 4>(B, blocks, s);
-    case 4: return strict ? launch_shape<true, 128, 8>(B, blocks, s) : launch_shape<false, 128, 8>(B, blocks, s);
-    case 5: return strict ? launch_shape<true, 256, 8>(B, blocks, s) : launch_shape<false, 256, 8>(B, blocks, s);
-  }
-  return cudaErrorInvalidValue;
+  return strict ? batch_launch<true>(B, shape, blocks, s) : batch_launch<false>(B, shape, blocks, s);
 }
+
+int batch_nu_blocks_per_sm(bool strict) {
+  return strict ? batch_nu_occupancy<true>() : batch_nu_occupancy<false>();
+}
+
+cudaError_t launch_batch_nu(const BatchArgs& B, bool strict, int blocks, cudaStream_t s) {
+  if (B.nprob <= 0) return cudaSuccess;
+  return strict ? batch_nu_launch<true>(B, blocks, s) : batch_nu_launch<false>(B, blocks, s);
+}
+#endif
 
 }  // namespace hrw

@@ -48,13 +48,15 @@ struct hrw_batch {
   int nprob = 0, order = 3, dtype = HRW_F64;
   int method = 0;  // 0 rktvd, 1 mstvd
   double* ring = nullptr;     // mstvd: 5 packed states u^m and 4 packed L(u^m)
+  bool nu = false;            // some problem has a non-uniform line (xedges)
+  double* nu_mem = nullptr;   // their edges, widths, FAST scales and weno coefficients
   std::vector<char> started;  // mstvd: the problem's RK3 start has run
   std::vector<int64_t> level; // mstvd: m of the problem's current state
   bool strict = false;
   std::vector<BatchProblem> probs;
   std::vector<int64_t> off;  // nprob + 1
   int64_t total = 0;
-  std::vector<int> members[kClasses];
+  std::vector<int> members[kClasses + 1];  // + the non-uniform lines, launched on their own
   int shape[kClasses] = {kDefaultShape[0], kDefaultShape[1], kDefaultShape[2]};
   bool tuned = false;
   BatchProblem* d_probs = nullptr;
@@ -65,8 +67,8 @@ struct hrw_batch {
   double* u2 = nullptr;
   float* fmem = nullptr;  // HRW_F32C: hi/lo slots x 2, d1, d2 (packed like u)
   cudaStream_t own = nullptr, main = nullptr;
-  cudaStream_t side[kClasses] = {};
-  cudaEvent_t fork = nullptr, join[kClasses] = {};
+  cudaStream_t side[kClasses + 1] = {};
+  cudaEvent_t fork = nullptr, join[kClasses + 1] = {};
   int sms = 0;
   std::vector<int64_t> steps_done;  // per problem, all calls
   std::string dev_name;
@@ -85,11 +87,12 @@ int batch_fail(int code, const std::string& m) { return set_error(code, m.c_str(
   } while (0)
 
 // Launch every class of the batch for the step counts already in b->probs (uploaded) on the
-// state `u`: the classes run concurrently on their own streams, each one persistent launch.
+// state `u`: the classes run concurrently on their own streams, each one persistent launch; the
+// non-uniform lines (class kClasses) have one launch of their own.
 int launch_all(hrw_batch* b, double* u, const int* shapes) {
   std::vector<int> order;
-  std::vector<int> start(kClasses + 1, 0);
-  for (int c = 0; c < kClasses; ++c) {
+  std::vector<int> start(kClasses + 2, 0);
+  for (int c = 0; c <= kClasses; ++c) {
     std::vector<int> m = b->members[c];
     std::stable_sort(m.begin(), m.end(), [&](int x, int y) {
       return (double)b->probs[x].nc * b->probs[x].nsteps > (double)b->probs[y].nc * b->probs[y].nsteps;
@@ -97,14 +100,14 @@ int launch_all(hrw_batch* b, double* u, const int* shapes) {
     start[c] = (int)order.size();
     order.insert(order.end(), m.begin(), m.end());
   }
-  start[kClasses] = (int)order.size();
+  start[kClasses + 1] = (int)order.size();
   HRW_BCUDA(cudaMemcpyAsync(b->d_probs, b->probs.data(), sizeof(BatchProblem) * b->nprob,
                             cudaMemcpyHostToDevice, b->main));
   HRW_BCUDA(cudaMemcpyAsync(b->d_order, order.data(), sizeof(int) * order.size(), cudaMemcpyHostToDevice,
                             b->main));
-  HRW_BCUDA(cudaMemsetAsync(b->d_counter, 0, sizeof(int) * kClasses, b->main));
+  HRW_BCUDA(cudaMemsetAsync(b->d_counter, 0, sizeof(int) * (kClasses + 1), b->main));
   HRW_BCUDA(cudaEventRecord(b->fork, b->main));
-  for (int c = 0; c < kClasses; ++c) {
+  for (int c = 0; c <= kClasses; ++c) {
     const int n = start[c + 1] - start[c];
     HRW_BCUDA(cudaStreamWaitEvent(b->side[c], b->fork, 0));
     if (n > 0) {
@@ -132,13 +135,16 @@ int launch_all(hrw_batch* b, double* u, const int* shapes) {
         A.fd1 = q, q += b->total;
         A.fd2 = q;
       }
-      const int per_sm = std::max(1, f32 ? batch_f32_blocks_per_sm(shapes[c])
-                                         : batch_blocks_per_sm(shapes[c], b->strict));
-      const int group = f32 ? kBatchShapesF32[shapes[c]].group : kBatchShapes[shapes[c]].group;
+      const bool nu = c == kClasses;
+      const int per_sm = std::max(1, nu    ? batch_nu_blocks_per_sm(b->strict)
+                                     : f32 ? batch_f32_blocks_per_sm(shapes[c])
+                                           : batch_blocks_per_sm(shapes[c], b->strict));
+      const int group = nu ? kBatchNuGroup : f32 ? kBatchShapesF32[shapes[c]].group : kBatchShapes[shapes[c]].group;
       const int groups_per_block = 256 / group;
       int blocks = per_sm * b->sms;
       blocks = std::min<int64_t>(blocks, (n + groups_per_block - 1) / groups_per_block);
-      if (f32) HRW_BCUDA(launch_batch_f32c(A, shapes[c], std::max(blocks, 1), b->side[c]));
+      if (nu) HRW_BCUDA(launch_batch_nu(A, b->strict, std::max(blocks, 1), b->side[c]));
+      else if (f32) HRW_BCUDA(launch_batch_f32c(A, shapes[c], std::max(blocks, 1), b->side[c]));
       else HRW_BCUDA(launch_batch(A, shapes[c], b->strict, std::max(blocks, 1), b->side[c]));
     }
     HRW_BCUDA(cudaEventRecord(b->join[c], b->side[c]));
@@ -172,6 +178,7 @@ std::string tune_key(const hrw_batch* b, int c) {
   std::ostringstream s;
   s << b->dev_name << "|class" << c << "|n" << b->members[c].size() << "|cells" << cells << "|k" << mix
     << "|order" << b->order << "|" << (b->strict ? "strict" : "fast") << (b->method ? "|ms" : "")
+    << (b->nu ? "|nu" : "")
     << (b->dtype == HRW_F32C ? "|f32c" : "|f64");
   std::string k = s.str();
   std::replace(k.begin(), k.end(), ' ', '_');
@@ -220,7 +227,12 @@ static int batch_create(const hrw_problem* probs, int nprob, int order, int dtyp
     };
     if (p.kind != HRW_PROBLEM_FV1D) return bad("Invalid input 'kind': batches hold FV1D problems.");
     if (p.ncells[0] <= 0) return bad("Invalid input 'ncells'. Valid range: ncells > 0.");
-    if (p.width[0] || p.xedges[0]) return bad("Invalid input 'width': batches hold uniform grids.");
+    if (p.width[0]) return bad("Invalid input 'width': batches take non-uniform lines as xedges.");
+    if (p.xedges[0]) {
+      if (dtype != HRW_F64) return bad("Invalid input 'xedges': non-uniform lines are supported for HRW_F64.");
+      for (int q = 0; q < p.ncells[0]; ++q)
+        if (!(p.xedges[0][q + 1] > p.xedges[0][q])) return bad("Invalid input 'xedges': edges must increase.");
+    }
     if (p.k < 1 || p.k > 3) return bad("Invalid input 'k'. Valid range: 1 <= k <= 3.");
     if (!(p.eps > 2.220446049250313e-16)) return bad("Invalid input 'eps'. Valid range: eps > epsilon.");
     if (p.flux != HRW_FLUX_LAX_FRIEDRICHS && p.flux != HRW_FLUX_GODUNOV) return bad("Invalid input 'flux'.");
@@ -248,7 +260,7 @@ static int batch_create(const hrw_problem* probs, int nprob, int order, int dtyp
     b->probs.push_back(q);
     b->off[i] = off;
     off += (q.nc + 63) / 64 * 64;
-    b->members[cls_of(q.nc)].push_back(i);
+    b->members[p.xedges[0] ? kClasses : cls_of(q.nc)].push_back(i);
   }
   b->off[nprob] = off;
   b->total = off;
@@ -270,14 +282,14 @@ static int batch_create(const hrw_problem* probs, int nprob, int order, int dtyp
   const size_t bytes = sizeof(double) * (size_t)off;
   if ((e = cudaStreamCreateWithFlags(&b->own, cudaStreamDefault)) != cudaSuccess) return cleanup(e);
   b->main = b->own;
-  for (int c = 0; c < kClasses; ++c) {
+  for (int c = 0; c <= kClasses; ++c) {
     if ((e = cudaStreamCreateWithFlags(&b->side[c], cudaStreamNonBlocking)) != cudaSuccess) return cleanup(e);
     if ((e = cudaEventCreateWithFlags(&b->join[c], cudaEventDisableTiming)) != cudaSuccess) return cleanup(e);
   }
   if ((e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming)) != cudaSuccess) return cleanup(e);
   if ((e = cudaMalloc(&b->d_probs, sizeof(BatchProblem) * nprob)) != cudaSuccess) return cleanup(e);
   if ((e = cudaMalloc(&b->d_order, sizeof(int) * nprob)) != cudaSuccess) return cleanup(e);
-  if ((e = cudaMalloc(&b->d_counter, sizeof(int) * kClasses)) != cudaSuccess) return cleanup(e);
+  if ((e = cudaMalloc(&b->d_counter, sizeof(int) * (kClasses + 1))) != cudaSuccess) return cleanup(e);
   if ((e = cudaMalloc(&b->u, bytes)) != cudaSuccess) return cleanup(e);
   if (dtype == HRW_F32C) {
     if ((e = cudaMalloc(&b->fmem, sizeof(float) * (size_t)off * 6)) != cudaSuccess) return cleanup(e);
@@ -286,6 +298,39 @@ static int batch_create(const hrw_problem* probs, int nprob, int order, int dtyp
     if ((e = cudaMalloc(&b->u2, bytes)) != cudaSuccess) return cleanup(e);
   }
   if (method == 1 && (e = cudaMalloc(&b->ring, bytes * 9)) != cudaSuccess) return cleanup(e);
+  // non-uniform lines: per problem edges(0:nc), widths edges(i) - edges(i-1), FAST scales
+  // fs / width and cnu(0:k-1,-1:k-1,1:nc) by weno_calc_cnu on the device (src/hrweno_weno.f90:221-297)
+  size_t nu_len = 0;
+  for (int i = 0; i < nprob; ++i)
+    if (probs[i].xedges[0]) nu_len += (size_t)(probs[i].ncells[0] + 1) + 2 * (size_t)probs[i].ncells[0] +
+                                      (size_t)probs[i].k * (probs[i].k + 1) * probs[i].ncells[0];
+  if (nu_len) {
+    b->nu = true;
+    if ((e = cudaMalloc(&b->nu_mem, sizeof(double) * nu_len)) != cudaSuccess) return cleanup(e);
+    double* q = b->nu_mem;
+    for (int i = 0; i < nprob; ++i) {
+      const hrw_problem& p = probs[i];
+      if (!p.xedges[0]) continue;
+      BatchProblem& bp = b->probs[i];
+      const int nc = p.ncells[0];
+      const double fs = fast_flux_scale(p.flux, p.fn[0]);
+      std::vector<double> host((size_t)3 * nc + 1);
+      for (int j = 0; j <= nc; ++j) host[j] = p.xedges[0][j];
+      for (int j = 0; j < nc; ++j) {
+        host[nc + 1 + j] = p.xedges[0][j + 1] - p.xedges[0][j];
+        host[2 * nc + 1 + j] = fs / host[nc + 1 + j];
+      }
+      if ((e = cudaMemcpy(q, host.data(), sizeof(double) * host.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
+        return cleanup(e);
+      bp.xe = q;
+      bp.width = q + nc + 1;
+      bp.rws = q + 2 * nc + 1;
+      bp.cnu = q + 3 * nc + 1;
+      if ((e = launch_calc_cnu(bp.xe, q + 3 * nc + 1, nc, p.k, b->own)) != cudaSuccess) return cleanup(e);
+      q += host.size() + (size_t)p.k * (p.k + 1) * nc;
+    }
+    if ((e = cudaStreamSynchronize(b->own)) != cudaSuccess) return cleanup(e);
+  }
   *out = b;
   return HRW_OK;
 }
@@ -516,7 +561,8 @@ int hrw_batch_destroy(hrw_batch* b) {
   if (b->u2) cudaFree(b->u2);
   if (b->fmem) cudaFree(b->fmem);
   if (b->ring) cudaFree(b->ring);
-  for (int c = 0; c < kClasses; ++c) {
+  if (b->nu_mem) cudaFree(b->nu_mem);
+  for (int c = 0; c <= kClasses; ++c) {
     if (b->side[c]) cudaStreamDestroy(b->side[c]);
     if (b->join[c]) cudaEventDestroy(b->join[c]);
   }

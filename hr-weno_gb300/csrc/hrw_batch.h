@@ -18,6 +18,12 @@ struct BatchProblem {
   // u^m when the call begins (after the start: 4)
   int start;
   int64_t level;
+  // non-uniform line (xedges): its weno coefficients cnu, widths, FAST 1/width scales and edges
+  // (device arrays of the batch); null for a uniform line
+  const double* cnu;
+  const double* width;
+  const double* rws;
+  const double* xe;
 };
 
 struct BatchArgs {
@@ -50,6 +56,10 @@ extern const BatchShape kBatchShapes[kNumBatchShapes];
 
 int batch_blocks_per_sm(int shape, bool strict);
 cudaError_t launch_batch(const BatchArgs& B, int shape, bool strict, int blocks, cudaStream_t s);
+// the non-uniform lines of a batch: one launch of 128-thread groups, 4 cells per thread
+constexpr int kBatchNuGroup = 128;
+int batch_nu_blocks_per_sm(bool strict);
+cudaError_t launch_batch_nu(const BatchArgs& B, bool strict, int blocks, cudaStream_t s);
 
 // compensated FP32 batches: their own shapes (cells per thread a multiple of 4)
 constexpr int kNumBatchShapesF32 = 3;

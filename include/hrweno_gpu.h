@@ -109,7 +109,7 @@ typedef struct hrw_problem {
   const double* rates;    /* LINEAR_ODE: host array(neq) of rates a_i */
   int32_t numerics;       /* HRW_NUMERICS_* */
   /* optional host array(nc+1) of cell edges of a non-uniform line, per dimension (FV1D and
-   * FV2D; HRW_F64 and HRW_F32 handles, not HRW_F32C, the batches, the adjoint or the
+   * FV2D; HRW_F64 and HRW_F32 handles and HRW_F64 batches, not HRW_F32C, the adjoint or the
    * allocation-free steps): the WENO coefficients become cnu(xedges) as weno(ncells, k, eps,
    * xedges) builds them (src/hrweno_weno.f90:100-104,221-297), the widths edges(i) - edges(i-1)
    * and the flux's x the edges themselves; xmin/xmax are then unused and width[] must be NULL.
@@ -183,7 +183,8 @@ int hrw_ode_destroy(hrw_ode* ode);
 int hrw_rhs(const hrw_problem* p, int dtype, double t, const void* v, void* vdot, void* stream);
 
 /* ---- batches of independent 1D problems ------------------------------------------- */
-/* A batch holds nprob independent FV1D problems on uniform grids (each its own rktvd(fu,
+/* A batch holds nprob independent FV1D problems on uniform or (HRW_F64) non-uniform grids
+ * given as xedges (each its own rktvd(fu,
  * neq, order) of the reference, src/hrweno_tvdode.f90:69-178, with its own ncells, k, flux,
  * flux function, alpha and boundaries; all share `order`, the dtype (HRW_F64, or HRW_F32C:
  * the compensated FP32 form, states still packed as FP64) and one numerics mode).  Their states are packed in one array: problem i occupies cells

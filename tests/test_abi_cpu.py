@@ -185,7 +185,7 @@ def test_adjoint_and_batch_validation_messages(hw):
         hw.adjoint(hw.burgers_1d(16, flux="godunov"))
     with pytest.raises(HrwError, match=r"with nseg > 1, ncells must be a multiple of 8"):
         hw.adjoint(hw.burgers_1d(12), nseg=2)
-    with pytest.raises(HrwError, match=r"batches hold uniform grids"):
+    with pytest.raises(HrwError, match=r"batches take non-uniform lines as xedges"):
         hw.batch([hw.burgers_1d(10, width=np.full(10, 0.1))])
 
 

@@ -108,8 +108,11 @@ def test_batch_shapes_agree_and_tuner_caches(hw, tmp_path):
 def test_batch_validation(hw):
     from hrweno import HrwError
     ok = hw.burgers_1d(10)
-    with pytest.raises(HrwError, match="uniform grids"):
+    with pytest.raises(HrwError, match="non-uniform lines as xedges"):
         hw.batch([ok, hw.burgers_1d(10, width=np.full(10, 0.1))])
+    nu = hw.Problem(ncells=(10, 1), xedges=(np.linspace(0.0, 1.0, 11) ** 2, None))
+    with pytest.raises(HrwError, match="supported for HRW_F64"):
+        hw.batch([ok, nu], dtype="f32c")
     with pytest.raises(HrwError, match="one numerics mode"):
         hw.batch([ok, hw.burgers_1d(10, numerics="strict")])
     with pytest.raises(HrwError, match="FV1D"):
@@ -211,3 +214,62 @@ def test_mstvd_batch_advance_and_tune(hw, orc):
         tt = o.integrate(uo, 0.0, (4 + 17 - 0.5) * dts[i], dts[i])
         assert tt == t[i] and np.array_equal(got[i], uo), i
     assert list(b.steps_done) == [21] * len(probs)
+
+
+# ---- non-uniform lines in batches ----------------------------------------------------------------
+def nonuniform_mix(hw, n, numerics, seed):
+    """Uneven lines, every other one on a stretched grid (xedges), fluxes and k varied."""
+    rng = np.random.default_rng(seed)
+    probs, lines, dts = [], [], []
+    for i in range(n):
+        nc = int(rng.integers(20, 3000))
+        k = int(rng.integers(1, 4))
+        x = np.linspace(-1.0, 1.0, nc)
+        u = np.exp(-((x - rng.uniform(-0.5, 0.5)) / 0.2) ** 2)
+        if i % 3 == 0:
+            p = hw.burgers_1d(nc, -1.0, 1.0, k=k, alpha=1.0, flux="godunov", bc="copy", numerics=numerics)
+        else:
+            p = hw.Problem(kind="fv1d", ncells=(nc, 1), k=k, flux="godunov" if i % 2 else "lax_friedrichs",
+                           fn=("linear", "linear"), coef_a=(0.6, 0.0), coef_b=(0.3, 0.0), alpha=(0.9, 1.0),
+                           bc=("zero_inflow", "copy"), xmin=(-1.0, 0.0), xmax=(1.0, 1.0), numerics=numerics)
+        hmin = 2.0 / nc
+        if i % 2 == 0:
+            w = 1.001 ** np.arange(nc)
+            e = -1.0 + 2.0 * np.concatenate([[0.0], np.cumsum(w) / w.sum()])
+            p.xedges = (e, None)
+            hmin = float(np.min(np.diff(e)))
+        probs.append(p)
+        lines.append(u)
+        dts.append(0.2 * hmin)
+    return probs, lines, np.array(dts)
+
+
+@pytest.mark.parametrize("method", ["rktvd", "mstvd"])
+@pytest.mark.parametrize("numerics", ["strict", "fast"])
+def test_nonuniform_batch_matches_single_solves(hw, orc, method, numerics):
+    """A batch whose lines are partly non-uniform (xedges: per-cell cnu, widths and true edges):
+    every problem bit-identical to its own single-problem handle (FAST: the same recon_nu,
+    flux and combine code), and to the oracle (STRICT), over two calls."""
+    import torch
+    probs, lines, dts = nonuniform_mix(hw, 18, numerics, 11)
+    b = hw.batch(probs, method=method)
+    u = torch.from_numpy(b.pack(lines)).cuda()
+    t = np.zeros(len(probs))
+    mk = (lambda p: hw.rktvd(p, int(p.ncells[0]), 3)) if method == "rktvd" else \
+        (lambda p: hw.mstvd(p, int(p.ncells[0])))
+    singles = [mk(p) for p in probs]
+    us = [torch.from_numpy(v.copy()).cuda() for v in lines]
+    ts = [0.0] * len(probs)
+    orcs = [orc.ODE(p, int(p.ncells[0]), 0 if method == "rktvd" else 1, 3) for p in probs]
+    uo = [v.copy() for v in lines]
+    to = [0.0] * len(probs)
+    for tout in (0.02, 0.06):
+        b.integrate(u, t, tout, dts)
+        got = b.unpack(u)
+        for i, p in enumerate(probs):
+            ts[i] = singles[i].integrate(us[i], ts[i], tout, dts[i])
+            assert t[i] == ts[i]
+            assert np.array_equal(got[i], us[i].cpu().numpy()), (i, tout)
+            if numerics == "strict":
+                to[i] = orcs[i].integrate(uo[i], to[i], tout, dts[i])
+                assert to[i] == t[i] and np.array_equal(got[i], uo[i]), (i, tout)
