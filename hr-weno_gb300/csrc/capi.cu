@@ -922,8 +922,8 @@ static int64_t rk_graph_steps(const hrw_ode* o, int64_t n) {
 }
 
 // rktvd_integrate of the MIXED kernel: n steps from du (the state alternates between du and w1)
-static int rk_integrate_mixed(hrw_ode* o, double* du, int64_t n, double dt) {
-  HRW_CUDA(launch_mixed_scale(du, o->neq, o->mscale, o->stream));
+// n MIXED steps from du (after the scale), leaving the state in *where (du or w1)
+static int mixed_steps(hrw_ode* o, double* du, int64_t n, double dt, double** where) {
   double* cur = du;
   double* other = o->w1;
   int64_t s0 = 0;
@@ -945,6 +945,14 @@ static int rk_integrate_mixed(hrw_ode* o, double* du, int64_t n, double dt) {
     HRW_CUDA(rk_step_mixed(o, cur, other, dt));
     std::swap(cur, other);
   }
+  *where = cur;
+  return HRW_OK;
+}
+
+static int rk_integrate_mixed(hrw_ode* o, double* du, int64_t n, double dt) {
+  HRW_CUDA(launch_mixed_scale(du, o->neq, o->mscale, o->stream));
+  double* cur = du;
+  if (const int rc = mixed_steps(o, du, n, dt, &cur)) return rc;
   if (cur != du)
     HRW_CUDA(cudaMemcpyAsync(du, cur, sizeof(double) * (size_t)o->neq, cudaMemcpyDeviceToDevice, o->stream));
   return HRW_OK;
@@ -1401,6 +1409,97 @@ static int rk3_integrate_host(hrw_ode* o, double* uh, double* t, double tout, do
   return HRW_OK;
 }
 
+// MIXED rktvd(3) of a uniform line on a page-locked host array.  The line comes in whole (the
+// first stage of the call needs the line's largest |u|), the steps before the last run as on a
+// device array, and the last step's second and third stages run by chunks of whole 1024-cell
+// tiles: the second stage's chunks in order on one stream, the third stage of chunk i on
+// another once the second stage has passed chunk i + 1 (its halo), and each chunk's copy back
+// behind its third stage, so that the copy back overlaps both stages.  The third stage writes
+// u' over the first stage's increment, which the second stage has finished reading in chunk i
+// once it has passed chunk i + 1.  The arithmetic is that of rk_integrate_mixed.
+static bool host_pipeline_mixed_ok(const hrw_ode* o, const void* u) {
+  if (!o->mixed || o->order != 3 || (int64_t)o->neq < 2 * (int64_t)device_sms() * kMixedTile) return false;
+  cudaPointerAttributes at{};
+  if (cudaPointerGetAttributes(&at, u) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return at.type == cudaMemoryTypeHost;
+}
+
+static int rk3_integrate_host_mixed(hrw_ode* o, double* uh, double* t, double tout, double dt, int itask) {
+  double tt;
+  int64_t n;
+  if (const int rc = count_steps(*t, tout, dt, itask, &n, &tt)) return rc;
+  if (!o->copy) {
+    for (cudaStream_t* st : {&o->pipe[0], &o->pipe[1], &o->copy})
+      HRW_CUDA(cudaStreamCreateWithFlags(st, cudaStreamNonBlocking));
+    HRW_CUDA(cudaEventCreateWithFlags(&o->ev_start, cudaEventDisableTiming));
+    for (int i = 0; i < kPipeChunks; ++i) {
+      HRW_CUDA(cudaEventCreateWithFlags(&o->ev_in[i], cudaEventDisableTiming));
+      HRW_CUDA(cudaEventCreateWithFlags(&o->ev_s3[i], cudaEventDisableTiming));
+    }
+    for (cudaEvent_t& ev : o->ev_join) HRW_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  }
+  const int64_t nc = o->neq;
+  const size_t bytes = sizeof(double) * (size_t)nc;
+  double* du = o->u;
+  cudaStream_t ms = o->stream;
+  HRW_CUDA(cudaMemcpyAsync(du, uh, bytes, cudaMemcpyHostToDevice, ms));
+  HRW_CUDA(launch_mixed_scale(du, nc, o->mscale, ms));
+  double* cur = du;
+  if (const int rc = mixed_steps(o, du, n - 1, dt, &cur)) return rc;
+  double* other = cur == du ? o->w1 : du;
+  // the last step: the first stage whole
+  MixedArgs a = o->mbase;
+  mixed_fill(a, o->prob.eps, dt);
+  a.u = cur;
+  a.scale = o->mscale;
+  const int k = o->prob.k;
+  float2* d1 = reinterpret_cast<float2*>(other);
+  float2* d2 = reinterpret_cast<float2*>(o->w2);
+  a.dout = d1;
+  HRW_CUDA(launch_stage1d_mixed(a, k, MX_E1, ms));
+  HRW_CUDA(cudaEventRecord(o->ev_start, ms));
+  for (cudaStream_t st : {o->pipe[0], o->pipe[1], o->copy}) HRW_CUDA(cudaStreamWaitEvent(st, o->ev_start, 0));
+  const int64_t chunk = ((nc + kPipeChunks - 1) / kPipeChunks + kMixedTile - 1) / kMixedTile * kMixedTile;
+  const int nch = (int)((nc + chunk - 1) / chunk);
+  for (int i = 0; i < nch; ++i) {  // the second stage, chunk by chunk
+    MixedArgs b = a;
+    b.dv = d1;
+    b.dout = d2;
+    b.cell0 = i * chunk;
+    b.ncell = std::min(chunk, nc - b.cell0);
+    HRW_CUDA(launch_stage1d_mixed(b, k, MX_RK3B, o->pipe[0]));
+    HRW_CUDA(cudaEventRecord(o->ev_in[i], o->pipe[0]));
+  }
+  for (int i = 0; i < nch; ++i) {  // the third stage and the copy back, chunk by chunk
+    MixedArgs b = a;
+    b.dout = nullptr;
+    b.dv = d2;
+    b.uout = other;
+    b.cell0 = i * chunk;
+    b.ncell = std::min(chunk, nc - b.cell0);
+    HRW_CUDA(cudaStreamWaitEvent(o->pipe[1], o->ev_in[std::min(i + 1, nch - 1)], 0));
+    HRW_CUDA(launch_stage1d_mixed(b, k, MX_RK3C, o->pipe[1]));
+    HRW_CUDA(cudaEventRecord(o->ev_s3[i], o->pipe[1]));
+    HRW_CUDA(cudaStreamWaitEvent(o->copy, o->ev_s3[i], 0));
+    HRW_CUDA(cudaMemcpyAsync(uh + b.cell0, other + b.cell0, sizeof(double) * (size_t)b.ncell,
+                             cudaMemcpyDeviceToHost, o->copy));
+  }
+  for (int p = 0; p < 2; ++p) {
+    HRW_CUDA(cudaEventRecord(o->ev_join[p], o->pipe[p]));
+    HRW_CUDA(cudaStreamWaitEvent(ms, o->ev_join[p], 0));
+  }
+  HRW_CUDA(cudaEventRecord(o->ev_join[2], o->copy));
+  HRW_CUDA(cudaStreamWaitEvent(ms, o->ev_join[2], 0));  // later work on the handle's stream
+  *t = tt;
+  o->fevals += (int)(3 * n);
+  o->nsteps += n;
+  if (o->istate == 1) o->istate = 2;
+  return HRW_OK;
+}
+
 // Whether a 2D stage block of this handle gave up waiting for its tile copies since the last
 // check; clears the handle's flag.  Waits for the handle's stream.
 static cudaError_t take_timeout(hrw_ode* o, bool* timed_out) {
@@ -1461,6 +1560,12 @@ static int integrate_on(hrw_ode* o, int mem, void* u, double* t, double tout, do
   double* du = (double*)u;
   if (mem == HRW_MEM_HOST && host_pipeline_ok(o, u)) {
     const int rc = rk3_integrate_host(o, (double*)u, t, tout, dt, itask);
+    if (rc != HRW_OK) return rc;
+    HRW_CUDA(cudaStreamSynchronize(o->stream));
+    return HRW_OK;
+  }
+  if (mem == HRW_MEM_HOST && host_pipeline_mixed_ok(o, u)) {
+    const int rc = rk3_integrate_host_mixed(o, (double*)u, t, tout, dt, itask);
     if (rc != HRW_OK) return rc;
     HRW_CUDA(cudaStreamSynchronize(o->stream));
     return HRW_OK;

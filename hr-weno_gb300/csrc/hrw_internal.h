@@ -144,7 +144,11 @@ struct MixedArgs {
   float c_h, c_l;        // dt / (4 dx) as a pair: dt L = -c (4 dF)
   float g_h, g_l;        // linear flux: the velocity g = a as a pair
   float two3_h, two3_l;  // 2/3 as a pair
+  // update only cells cell0 .. cell0 + ncell - 1 (ncell = 0: the whole line); cell0 a multiple of
+  // the kernel's 1024-cell block tile (kMixedTile), so that ranges side by side write disjoint cells
+  int64_t cell0, ncell;
 };
+constexpr int64_t kMixedTile = 1024;
 
 // Whether the MIXED kernel covers a line: k = 2 or 3, Lax-Friedrichs, uniform grid, Burgers or
 // linear advection at constant speed.  Other lines run the FAST kernels.

@@ -249,7 +249,7 @@ __global__ void __launch_bounds__(NT, MINB) stage1d_mixed_kernel(MixedArgs a) {
   constexpr int ND = C + 2 * K - 1;  // window of differences d_{j0-K} .. d_{j0+C+K-2}
   constexpr int NH = 2 * K - 1;      // the warp's edge differences: K on the left, K-1 on the right
   const int lane = threadIdx.x & 31;
-  const int64_t w0 = ((int64_t)blockIdx.x * NT + (threadIdx.x & ~31)) / 32 * WC;
+  const int64_t w0 = a.cell0 + ((int64_t)blockIdx.x * NT + (threadIdx.x & ~31)) / 32 * WC;
   const int64_t nc = a.L.nc;
   asm volatile("griddepcontrol.wait;" ::: "memory");
   if (w0 >= nc) return;  // the whole warp is past the line
@@ -429,7 +429,9 @@ __global__ void __launch_bounds__(NT, MINB) stage1d_mixed_kernel(MixedArgs a) {
 
 template <int K, int ST>
 cudaError_t launch_st(const MixedArgs& a, cudaStream_t s) {
-  const int64_t warps = ((int64_t)a.L.nc + WC - 1) / WC;
+  static_assert(NT / 32 * WC == kMixedTile, "the block tile of cell ranges");
+  const int64_t span = a.ncell > 0 ? a.ncell : (int64_t)a.L.nc - a.cell0;
+  const int64_t warps = (span + WC - 1) / WC;
   const int64_t nblk = (warps + NT / 32 - 1) / (NT / 32);
   if (nblk <= 0) return cudaSuccess;
   cudaLaunchConfig_t cfg{};

@@ -127,6 +127,30 @@ def test_mixed_graphs_host_and_device_bits(hw, steps):
         assert np.array_equal(r, res[0])
 
 
+@pytest.mark.parametrize("n", [1 << 20, (1 << 20) + 777])
+@pytest.mark.parametrize("steps", [1, 2, 5])
+def test_mixed_host_pipeline_bits(hw, n, steps):
+    """Page-locked host lines of at least 2 x SMs x 1024 cells take the chunked pipeline (the
+    last step's second and third stages by chunks, each chunk copied back behind its third
+    stage): the same bits as the device-array call, for one and several steps, a ragged last
+    chunk, and single steps (itask = 2) in a row."""
+    import torch
+    prob, u0, dt = line(hw, n, 3, "burgers", "mixed")
+    ode = hw.rktvd(prob, n, 3)
+    ud = torch.from_numpy(u0.copy()).cuda()
+    td = ode.integrate(ud, 0.0, (steps - 0.5) * dt, dt)
+    oh = hw.rktvd(prob, n, 3)
+    uh = torch.from_numpy(u0.copy()).pin_memory()
+    th = oh.integrate(uh, 0.0, (steps - 0.5) * dt, dt)
+    assert th == td and np.array_equal(uh.numpy(), ud.cpu().numpy())
+    os_ = hw.rktvd(prob, n, 3)
+    us = torch.from_numpy(u0.copy()).pin_memory()
+    ts = 0.0
+    for _ in range(steps):
+        ts = os_.integrate(us, ts, 1e9, dt, itask=2)
+    assert ts == td and np.array_equal(us.numpy(), ud.cpu().numpy())
+
+
 def test_mixed_elsewhere_runs_fast(hw):
     """Where the MIXED kernel does not apply (a short line, Godunov, mstvd, one right-hand side)
     MIXED gives FAST's bits."""
