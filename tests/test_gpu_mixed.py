@@ -146,9 +146,29 @@ def test_mixed_host_pipeline_bits(hw, n, steps):
     os_ = hw.rktvd(prob, n, 3)
     us = torch.from_numpy(u0.copy()).pin_memory()
     ts = 0.0
-    for _ in range(steps):
+    for _ in range(steps):  # from the second call on, the pipelined step on the guessed scale
         ts = os_.integrate(us, ts, 1e9, dt, itask=2)
     assert ts == td and np.array_equal(us.numpy(), ud.cpu().numpy())
+
+
+def test_mixed_host_pipeline_guess_missed(hw):
+    """A driver that changes the host line between calls (here: scales it by 4 and by 1/3, which
+    moves the exponent of max|u|, and by 1.01, which keeps it): a call whose guess of the scale
+    misses takes the step again from the device copy of its input; every call gives the bits
+    of the device-array path on the same input."""
+    import torch
+    n = (1 << 20) + 2048
+    prob, u0, dt = line(hw, n, 3, "burgers", "mixed")
+    prob.alpha = (4.0 * float(np.max(np.abs(u0))), 1.0)
+    oh, od = hw.rktvd(prob, n, 3), hw.rktvd(prob, n, 3)
+    uh = torch.from_numpy(u0.copy()).pin_memory()
+    th = td = 0.0
+    for factor in (1.0, 1.0, 4.0, 1.01, 1.0 / 3.0, 1.0):
+        uh.mul_(factor)
+        ud = uh.clone().cuda()
+        th = oh.integrate(uh, th, 1e9, 0.25 * dt, itask=2)
+        td = od.integrate(ud, td, 1e9, 0.25 * dt, itask=2)
+        assert th == td and np.array_equal(uh.numpy(), ud.cpu().numpy()), factor
 
 
 def test_mixed_elsewhere_runs_fast(hw):
