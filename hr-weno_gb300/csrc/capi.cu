@@ -527,8 +527,8 @@ static int ode_create(const hrw_problem* p, int neq, int order, int method, int 
   if (rc != HRW_OK) return rc;
   if (dtype == HRW_F32 && (rc = validate_problem_f32(p)) != HRW_OK) return rc;
   if (dtype == HRW_F32C) {
-    if (p->xedges[0] || p->xedges[1])
-      return fail(HRW_EINVAL, "Invalid input 'xedges': non-uniform lines are supported for HRW_F64 and HRW_F32.");
+    if (p->kind == HRW_PROBLEM_FV2D && (p->xedges[0] || p->xedges[1]))
+      return fail(HRW_EINVAL, "Invalid input 'xedges': HRW_F32C takes non-uniform lines in FV1D problems.");
     if (p->kind != HRW_PROBLEM_FV1D && p->kind != HRW_PROBLEM_FV2D)
       return fail(HRW_EINVAL, "Invalid input 'dtype': HRW_F32C supports FV1D and FV2D problems.");
     if (!(p->eps > 1.1920928955078125e-07))  // epsilon(1.0_real32), src/hrweno_weno.f90:92
@@ -645,6 +645,8 @@ static int ode_create(const hrw_problem* p, int neq, int order, int method, int 
     size_t nw = 0;  // per-cell 1/width entries of the lines that have widths
     for (int d = 0; d < nd; ++d)
       if (p->width[d]) nw += (size_t)(p->ncells[d] + 63) / 64 * 64;
+    // a non-uniform line (FV1D): 1/width, the edges, b width and k (k + 1) coefficients per cell
+    if (p->xedges[0]) nw += ((size_t)p->ncells[0] + 64) / 64 * 64 * (3 + (size_t)p->k * (p->k + 1));
     const size_t nf = sn * (2 * slots + (method == 1 ? 4 : 0) + 2) + nw;
     if ((e = cudaMalloc(&o->fmem, sizeof(float) * nf)) != cudaSuccess) return cleanup(e);
     float* q = o->fmem;
@@ -678,6 +680,34 @@ static int ode_create(const hrw_problem* p, int neq, int order, int method, int 
         F.rw = q;
         if (d == 0) o->frw = q;
         q += (size_t)(L.nc + 63) / 64 * 64;
+      } else if (p->xedges[d]) {
+        // the FP64 coefficients of the line (computed above on the device) and its FP64 widths,
+        // rounded once to FP32; g at the edges from the rounded edges
+        const size_t nc = (size_t)L.nc, ncf = (size_t)p->k * (p->k + 1), seg = (nc + 64) / 64 * 64;
+        std::vector<double> c64(nc * ncf);
+        if ((e = cudaMemcpy(c64.data(), o->line[d].cnu, sizeof(double) * c64.size(), cudaMemcpyDeviceToHost)) !=
+            cudaSuccess)
+          return cleanup(e);
+        std::vector<float> rw(nc), xe(nc + 1), gst(nc), c32(c64.size());
+        for (size_t i = 0; i <= nc; ++i) xe[i] = (float)p->xedges[d][i];
+        for (size_t i = 0; i < nc; ++i) {
+          const double w = p->xedges[d][i + 1] - p->xedges[d][i];
+          rw[i] = (float)(1.0 / w);
+          gst[i] = (float)(L.b * w);
+        }
+        for (size_t i = 0; i < c64.size(); ++i) c32[i] = (float)c64[i];
+        float* dst[4] = {q, q + seg, q + 2 * seg, q + 3 * seg};
+        const std::vector<float>* src[4] = {&rw, &xe, &gst, &c32};
+        for (int m = 0; m < 4; ++m)
+          if ((e = cudaMemcpy(dst[m], src[m]->data(), sizeof(float) * src[m]->size(), cudaMemcpyHostToDevice)) !=
+              cudaSuccess)
+            return cleanup(e);
+        F.rw = dst[0];
+        F.xe = dst[1];
+        F.gst = dst[2];
+        F.cnu = dst[3];
+        if (d == 0) o->frw = q;
+        q += seg * (3 + ncf);
       }
     }
     if (nd == 2 && p->flux == HRW_FLUX_GODUNOV) {

@@ -156,6 +156,81 @@ __device__ __forceinline__ void recon_diff3_shared(const float* d, float t0, flo
 }
 
 // ---------------------------------------------------------------------------------------------
+// WENO offsets of one cell of a non-uniform line from its differences, with the cell's own
+// coefficients ci(q, r) at [q + K (r + 1)] (cnu of src/hrweno_weno.f90:170,177-181).  Each
+// candidate minus v_j is sum_q c(q, r) (v_{j-r+q} - v_j), the neighbour values relative to v_j
+// being sums of differences (S(m) below), so the rounding of the coefficients touches only the
+// small offsets.  The indicators and the weights are the uniform ones (:183-210, as the
+// reference computes them on any grid); d as recon_diff.
+// ---------------------------------------------------------------------------------------------
+template <int K>
+__device__ __forceinline__ void recon_diff_nu(const float* d, const float* ci, float eps, float& rl,
+                                              float& rr) {
+  if constexpr (K == 1) {
+    rl = 0.f;
+    rr = 0.f;
+  } else {
+    // S[m + K - 1] = v_{j+m} - v_j, m = -(K-1) .. K-1
+    float S[2 * K - 1];
+    S[K - 1] = 0.f;
+#pragma unroll
+    for (int m = 1; m < K; ++m) {
+      S[K - 1 + m] = S[K - 2 + m] + d[K - 2 + m];
+      S[K - 1 - m] = S[K - m] - d[K - 1 - m];
+    }
+    float R[K], Lc[K];
+#pragma unroll
+    for (int r = 0; r < K; ++r) {
+      float sr = 0.f, sl = 0.f;
+#pragma unroll
+      for (int q = 0; q < K; ++q) {
+        if (q == r) continue;  // the cell itself: v_j - v_j
+        const float x = S[K - 1 - r + q];
+        sr = fmaf(ci[q + K * (r + 1)], x, sr);
+        sl = fmaf(ci[q + K * r], x, sl);
+      }
+      R[r] = sr;
+      Lc[r] = sl;
+    }
+    if constexpr (K == 2) {
+      const float dm = d[0], d0 = d[1];
+      const float e0 = fmaf(d0, d0, eps), e1 = fmaf(dm, dm, eps);
+      const float s0 = e0 * e0, s1 = e1 * e1;
+      if (fmaxf(s0, s1) < 1e30f) {  // w0 = 2 s1 / (2 s1 + s0), mirrored w~0 = s1 / (s1 + 2 s0)
+        rr = fmaf(2.f * s1, R[0], s0 * R[1]) * rcpf(fmaf(2.f, s1, s0));
+        rl = fmaf(s1, Lc[0], 2.f * s0 * Lc[1]) * rcpf(fmaf(2.f, s0, s1));
+      } else {
+        const float a0 = (2.f / 3.f) / s0, a1 = (1.f / 3.f) / s1;
+        const float t0 = (1.f / 3.f) / s0, t1 = (2.f / 3.f) / s1;
+        rr = (a0 * R[0] + a1 * R[1]) / (a0 + a1);
+        rl = (t0 * Lc[0] + t1 * Lc[1]) / (t0 + t1);
+      }
+    } else {
+      const float dmm = d[0], dm = d[1], d0 = d[2], d1 = d[3];
+      const float c13 = 13.f / 12.f;
+      const float A0 = d1 - d0, A1 = d0 - dm, A2 = dm - dmm;
+      const float B0 = fmaf(-3.f, d0, d1), B1 = dm + d0, B2 = fmaf(3.f, dm, -dmm);
+      const float e0 = eps + fmaf(c13 * A0, A0, 0.25f * B0 * B0);
+      const float e1 = eps + fmaf(c13 * A1, A1, 0.25f * B1 * B1);
+      const float e2 = eps + fmaf(c13 * A2, A2, 0.25f * B2 * B2);
+      const float s0 = e0 * e0, s1 = e1 * e1, s2 = e2 * e2;
+      if (fmaxf(s0, fmaxf(s1, s2)) < 1e18f) {
+        const float P0 = s1 * s2, P1 = s0 * s2, P2 = s0 * s1;
+        const float den = fmaf(3.f, P0, fmaf(6.f, P1, P2));
+        const float dent = fmaf(3.f, P2, fmaf(6.f, P1, P0));
+        rr = fmaf(3.f * P0, R[0], fmaf(6.f * P1, R[1], P2 * R[2])) * rcpf(den);
+        rl = fmaf(P0, Lc[0], fmaf(6.f * P1, Lc[1], 3.f * P2 * Lc[2])) * rcpf(dent);
+      } else {
+        const float a0 = 0.3f / s0, a1 = 0.6f / s1, a2 = 0.1f / s2;
+        const float t0 = 0.1f / s0, t1 = 0.6f / s1, t2 = 0.3f / s2;
+        rr = (a0 * R[0] + a1 * R[1] + a2 * R[2]) / (a0 + a1 + a2);
+        rl = (t0 * Lc[0] + t1 * Lc[1] + t2 * Lc[2]) / (t0 + t1 + t2);
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
 // G = F(v + a, v + b) - f_base at interface e, for a cell of value v whose left-hand side
 // state at the interface is v + a and right-hand side state v + b.  f_base is f(v) for
 // Burgers and g(x_L) v for the linear flux, where x_L is the cell's left edge: the part of
@@ -206,17 +281,19 @@ __device__ __forceinline__ float g_at(const LineF& L, int64_t e) {
 //   left interface:  left state  v + (rr_{j-1} - d_{j-1}),  right state v + rl_j
 //   right interface: left state  v + rr_j,                  right state v + (d_j + rl_{j+1})
 // with the boundary fluxes of example1...f90:103-104 / example2...f90:117-120.
+// NU: a non-uniform line, g at the true edges and g_R - g_L = b width_j per cell
+template <bool NU = false>
 __device__ __forceinline__ float flux_diff_f32c(const LineF& L, int64_t j, float v, float rr_m,
                                                 float d_m, float rl_j, float rr_j, float d_j,
                                                 float rl_p) {
   const bool lin = L.fn != HRW_FN_BURGERS;
-  const float gL = lin ? g_at(L, j) : 0.f;
-  const float gR = lin ? g_at(L, j + 1) : 0.f;
+  const float gL = lin ? (NU ? fmaf(L.b, L.xe[j], L.a) : g_at(L, j)) : 0.f;
+  const float gR = lin ? (NU ? fmaf(L.b, L.xe[j + 1], L.a) : g_at(L, j + 1)) : 0.f;
   // G_R - G_L, with the base f(v) (Burgers) or g v (linear) of both interfaces removed; the
-  // linear flux adds back (g_R - g_L) v = b rx v
+  // linear flux adds back (g_R - g_L) v = b rx v (b width_j v on a non-uniform line)
   float GL = flux_g(L, v, rr_m - d_m, rl_j, gL);
   float GR = flux_g(L, v, rr_j, d_j + rl_p, gR);
-  float extra = lin ? L.gstep * v : 0.f;
+  float extra = lin ? (NU ? L.gst[j] : L.gstep) * v : 0.f;
   if (j == 0 || j == L.nc - 1) {
     // boundary fluxes in full (no cancellation there): F = fbase + G, each operation rounded
     // as written (no contraction), so that inlined and out-of-line copies give the same bits
@@ -349,8 +426,9 @@ __device__ __forceinline__ void store_cells(float* __restrict__ p, int j0, int n
 // FC_RK1 .. FC_RK3C; one copy of the pass then serves every stage of a step (the batched
 // kernel runs all stages of a problem in one launch, and per-stage copies would not fit the
 // instruction cache).  The per-stage arithmetic is the same as with ST fixed.
-template <int K, int ST, int C, int FK = -1>
+template <int K, int ST, int C, int FK = -1, bool NU = false>
 __device__ __forceinline__ void f32c_pass(const F32CArgs& a, int64_t j0l, int lane, int st_rt = ST) {
+  static_assert(!NU || FK < 0, "non-uniform lines take the general flux path");
   static_assert(ST != FC_MS || ST >= 0, "");
   const int st = ST >= 0 ? ST : st_rt;
   // the stage writes a.out (the first stages) or the state pair (the last stage)
@@ -399,7 +477,14 @@ __device__ __forceinline__ void f32c_pass(const F32CArgs& a, int64_t j0l, int la
 #pragma unroll
   for (int q = 0; q < C + 2 * K - 1; ++q) d[q] = (wh[q + 1] - wh[q]) + (wm[q + 1] - wm[q]);
   float rl[C], rr[C];
-  if constexpr (K == 3) {
+  constexpr int NCF = K * (K + 1);  // coefficients per cell of a non-uniform line
+  if constexpr (NU) {
+#pragma unroll
+    for (int c = 0; c < C; ++c) {
+      const int jc = j0 + c < nc ? j0 + c : nc - 1;
+      recon_diff_nu<K>(&d[c + 1], L.cnu + (int64_t)NCF * jc, a.eps, rl[c], rr[c]);
+    }
+  } else if constexpr (K == 3) {
     // 13/12 (d_m - d_{m-1})^2 once per window position.  Cell c reads d[c+1 .. c+4]
     // (d_{j-2} .. d_{j+1}): its beta0, beta1, beta2 take t[c+4], t[c+3], t[c+2]
     float t[C + 4];
@@ -421,7 +506,11 @@ __device__ __forceinline__ void f32c_pass(const F32CArgs& a, int64_t j0l, int la
 #pragma unroll
   for (int q = 0; q < 2 * K - 2; ++q) ed[q] = lane == 31 ? d[C + 1 + q] : d[q];
   float el, er;
-  if constexpr (K == 3) {
+  if constexpr (NU) {
+    int je = lane == 31 ? j0 + C : j0 - 1;
+    je = je < 0 ? 0 : (je >= nc ? nc - 1 : je);
+    recon_diff_nu<K>(ed, L.cnu + (int64_t)NCF * je, a.eps, el, er);
+  } else if constexpr (K == 3) {
     float te[3];
 #pragma unroll
     for (int q = 0; q < 3; ++q) {
@@ -459,7 +548,7 @@ __device__ __forceinline__ void f32c_pass(const F32CArgs& a, int64_t j0l, int la
       else
         dF = j < nc ? flux_diff_f32c(L, j, v, rr_m, d[c + K - 1], rl[c], rr[c], d[c + K], rl_p) : 0.f;
     } else {
-      dF = j < nc ? flux_diff_f32c(L, j, v, rr_m, d[c + K - 1], rl[c], rr[c], d[c + K], rl_p) : 0.f;
+      dF = j < nc ? flux_diff_f32c<NU>(L, j, v, rr_m, d[c + K - 1], rl[c], rr[c], d[c + K], rl_p) : 0.f;
     }
     const float qj = rw ? -dF * rw[j < nc ? j : nc - 1] : -dF;
     const float dtL = fmaf(a.c_hi, qj, a.c_lo * qj);  // dt L(v)_j

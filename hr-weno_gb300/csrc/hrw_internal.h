@@ -90,6 +90,11 @@ struct LineF {
   float xmin, rx;
   float gstep;        // g(x_{e+1}) - g(x_e) = b * rx
   const float* rw;    // per-cell 1 / width, or null (uniform grid)
+  // non-uniform line (1D): per-cell weno coefficients cnu(0:k-1,-1:k-1) rounded from FP64,
+  // the edges x_e, and per-cell g(x_{j+1}) - g(x_j) = b width_j (from FP64 widths); null: uniform
+  const float* cnu;
+  const float* xe;
+  const float* gst;
 };
 
 struct F32CArgs {

@@ -21,12 +21,12 @@
 
 namespace hrw {
 
-template <int K, int ST, int NT, int C, int FK>
+template <int K, int ST, int NT, int C, int FK, bool NU = false>
 __global__ void __launch_bounds__(NT) stage1d_f32c_kernel(F32CArgs a) {
   const int lane = threadIdx.x & 31;
   const int64_t gt = (int64_t)blockIdx.x * NT + threadIdx.x;
   if ((gt - lane) * C >= a.L.nc) return;  // whole warp past the line (uniform across the warp)
-  f32c_pass<K, ST, C, FK>(a, gt * C, lane);
+  f32c_pass<K, ST, C, FK, NU>(a, gt * C, lane);
 }
 
 template <int K, int ST, int NT, int C>
@@ -48,6 +48,11 @@ template <int K, int ST>
 static cudaError_t launch_k(const F32CArgs& a, cudaStream_t s) {
   // long lines: 8 cells per thread; 256-thread blocks for k = 3, 128 for k = 2 (measured on the
   // 2^24-cell line: 0.229 vs 0.231 ms per RK3 step for k = 3, 0.184 vs 0.172 ms for k = 2)
+  if (a.L.cnu) {  // a non-uniform line: per-cell coefficients, the general flux path
+    const int64_t nblk = ((int64_t)a.L.nc + 127) / 128;
+    stage1d_f32c_kernel<K, ST, 32, 4, -1, true><<<(unsigned)nblk, 32, 0, s>>>(a);
+    return cudaGetLastError();
+  }
   if (a.L.nc >= 2 * (int64_t)device_sms() * 2048)
     return K == 2 ? launch_shape<K, ST, 128, 8>(a, s) : launch_shape<K, ST, 256, 8>(a, s);
   return launch_shape<K, ST, 32, 4>(a, s);

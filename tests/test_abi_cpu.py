@@ -114,6 +114,17 @@ def test_f32c_rejects_burgers_linear(hw):
         hw.rktvd(prob, 100, 3, dtype="f32c")
 
 
+def test_f32c_nonuniform_lines_fv1d_only(hw):
+    """Compensated FP32 handles take xedges on FV1D lines; a 2D problem with a non-uniform line
+    is refused before any CUDA call."""
+    from hrweno import HrwError
+    nx = 16
+    xe = np.linspace(0.0, 1.0, nx + 1) ** 2
+    prob = hw.Problem(kind="fv2d", ncells=(nx, nx), k=3, xedges=(xe, None))
+    with pytest.raises(HrwError, match="HRW_F32C takes non-uniform lines in FV1D"):
+        hw.rktvd(prob, nx * nx, 3, dtype="f32c")
+
+
 def test_real32_validation_before_any_cuda_call(hw):
     """A REAL32 handle (dtype "f32") applies the reference's checks to the FP32 values a REAL32
     build holds: eps > epsilon(1.0_real32) (src/hrweno_weno.f90:92) and a grid that stays valid

@@ -58,6 +58,66 @@ def test_rhs_f32c_linear_and_widths(hw, orc, flux):
         assert np.max(np.abs(got - ref)) <= 2e-6 * np.max(np.abs(ref))
 
 
+def stretched(nc, kind, seed=0):
+    """Edges on [-1, 1]: cubic (i / nc)^3 stretching (test/test_hrweno.f90:123-128) or random
+    widths in a 1:3 range."""
+    if kind == "cubic":
+        return -1.0 + 2.0 * (np.arange(nc + 1) / nc) ** 3
+    rng = np.random.default_rng(seed)
+    return np.concatenate([[-1.0], -1.0 + np.cumsum(rng.uniform(0.5, 1.5, nc)) * (2.0 / nc)])
+
+
+@pytest.mark.parametrize("k", [1, 2, 3])
+@pytest.mark.parametrize("kind,nc", [(kd, n) for kd in ("cubic", "random") for n in (1, 2, 7, 300, 1000)]
+                         + [("random", 1 << 16)])
+def test_rhs_f32c_nonuniform(hw, orc, k, nc, kind):
+    """weno(ncells, k, eps, xedges) in the compensated form: per-cell coefficients rounded from
+    the FP64 ones, FP64 widths, g at the edges; against the FP64 oracle's stage.
+
+    The float pair holds the state to about 2^-48 of its size, so a cell's right-hand side is
+    resolved while its width is well above 2^-48 max|v| / 2e-6 (about 1e-9 here): the cubic
+    line stops at 1000 cells (smallest cell 2e-9); at 2^16 cells its first cells are 7e-15
+    wide, where the float pair (and even FP64, to about 1%) no longer resolves the
+    differences of v."""
+    xe = stretched(nc, kind, nc)
+    xc = 0.5 * (xe[1:] + xe[:-1])
+    v = 1.0 + 0.5 * np.sin(3.0 * xc) + 0.3 * np.exp(-40.0 * xc ** 2)
+    cases = [dict(flux="lax_friedrichs", fn="burgers", bc="copy", b=0.0),
+             dict(flux="godunov", fn="burgers", bc="zero", b=0.0),
+             dict(flux="godunov", fn="linear", bc="zero_inflow", b=0.4),
+             dict(flux="lax_friedrichs", fn="linear", bc="copy", b=-0.3)]
+    for c in cases:
+        prob = hw.Problem(kind="fv1d", ncells=(nc, 1), k=k, flux=c["flux"], fn=(c["fn"], c["fn"]),
+                          coef_a=(0.8, 0), coef_b=(c["b"], 0), alpha=(2.5, 2.5),
+                          bc=(c["bc"], c["bc"]), xedges=(xe, None))
+        ref = orc.rhs(prob, v)
+        got = rhs_f32c(prob, v)
+        scale = max(np.max(np.abs(ref)), 1e-30)
+        assert np.max(np.abs(got - ref)) <= 2e-6 * scale, (c, np.max(np.abs(got - ref)) / scale)
+
+
+@pytest.mark.parametrize("method", ["rktvd", "mstvd"])
+@pytest.mark.parametrize("kind", ["cubic", "random"])
+def test_f32c_nonuniform_integrate(hw, orc, method, kind):
+    nc = 2000
+    xe = stretched(nc, kind, 5)
+    xc = 0.5 * (xe[1:] + xe[:-1])
+    u0 = 0.5 + np.exp(-30 * xc ** 2)
+    prob = hw.Problem(kind="fv1d", ncells=(nc, 1), k=3, flux="godunov", fn=("burgers", "burgers"),
+                      alpha=(1.5, 1.5), bc=("copy", "copy"), xedges=(xe, None))
+    dt = 0.2 * np.min(np.diff(xe)) / 1.5
+    steps = 300 if kind == "random" else 40  # the cubic line's smallest cell is 2 / nc^3 wide
+    if method == "rktvd":
+        g, o = hw.rktvd(prob, nc, 3, dtype="f32c"), orc.ODE(prob, nc, 0, 3)
+    else:
+        g, o = hw.mstvd(prob, nc, dtype="f32c"), orc.ODE(prob, nc, 1)
+    u32, u64 = u0.copy(), u0.copy()
+    t32 = g.integrate(u32, 0.0, (steps - 0.5) * dt, dt)
+    t64 = o.integrate(u64, 0.0, (steps - 0.5) * dt, dt)
+    assert t32 == t64 and g.nsteps == o.info()[2]
+    assert rel_l1(u32, u64) <= 1e-6, rel_l1(u32, u64)
+
+
 @pytest.mark.parametrize("k", [2, 3])
 def test_f32c_large_burgers_vs_oracle(hw, orc, k):
     """2^16 cells, 8-Gaussian u0, LF, RK3 at CFL 0.4 for 1000 steps."""
