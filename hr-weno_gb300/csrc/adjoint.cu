@@ -24,6 +24,7 @@
 #include <algorithm>
 #include <cmath>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -64,6 +65,13 @@ struct AdjLine {
   int k, fn, bc;
   double a, b, alpha, xmin, rx, rdx, eps;
   double rws0;  // FAST flux scale / dx (stage kernels)
+  // a non-uniform line (xedges), the same for every segment, by local cell: the weno
+  // coefficients cnu (k (k + 1) per cell), 1 / width, the FAST flux scale / width, and the
+  // edges (seg + 1); null on a uniform line
+  const double* cnu;
+  const double* rdxv;
+  const double* rwsv;
+  const double* xe;
 };
 
 __device__ __forceinline__ LineArgs line_args(const AdjLine& A) {
@@ -78,6 +86,8 @@ __device__ __forceinline__ LineArgs line_args(const AdjLine& A) {
   L.xmin = A.xmin;
   L.rx = A.rx;
   L.rws0 = A.rws0;
+  L.xe = A.xe;
+  L.rws = A.rwsv;
   return L;
 }
 
@@ -163,6 +173,89 @@ template <> struct WenoTape<3> {
               fma(3.0, gB0 + gB2, fma(-2.0, gA1, gA0 + gA2))))));
     out[3] += fma(5.0, dq0, fma(2.0, dq1, fma(-7.0, dr0, fma(-2.0, gA0, fma(-4.0, gB0, gA1 - gB1 - dr1)))));
     out[4] += fma(2.0, dr0, gA0 + gB0 - dq0);
+  }
+};
+
+// --------------------------------------------------------------------------------------------
+// The same map on a non-uniform line: the candidates take the cell's own coefficients ci
+// (cnu(j, r) at [j + K (r + 1)], src/hrweno_weno.f90:177-181), the indicators and weights are
+// the uniform ones (:183-210).  Division form throughout; the reverse pushes the candidates'
+// adjoints back through ci and the indicators' through their quadratic forms.
+// --------------------------------------------------------------------------------------------
+template <int K> struct WenoTapeNu {
+  double vr, vl, q[K], r[K], w[K], u[K], ie[K], G[K][2];  // G: the indicators' A, B (K = 3), D (K = 2)
+  const double* ci;
+  __device__ void fwd(const double* p, double eps, const double* c) {
+    ci = c;
+#pragma unroll
+    for (int s = 0; s < K; ++s) {
+      double sq = 0.0, sr = 0.0;
+#pragma unroll
+      for (int j = 0; j < K; ++j) {
+        sq = fma(ci[j + K * (s + 1)], p[j - s], sq);
+        sr = fma(ci[j + K * s], p[j - s], sr);
+      }
+      q[s] = sq;
+      r[s] = sr;
+    }
+    double beta[K];
+    if constexpr (K == 1) {
+      beta[0] = 0.0;
+    } else if constexpr (K == 2) {
+      G[0][0] = p[1] - p[0], G[1][0] = p[0] - p[-1];
+      beta[0] = G[0][0] * G[0][0], beta[1] = G[1][0] * G[1][0];
+    } else {
+      const double vmm = p[-2], vm = p[-1], v0 = p[0], v1 = p[1], v2 = p[2];
+      G[0][0] = fma(-2.0, v1, v0 + v2), G[0][1] = fma(3.0, v0, fma(-4.0, v1, v2));
+      G[1][0] = fma(-2.0, v0, vm + v1), G[1][1] = vm - v1;
+      G[2][0] = fma(-2.0, vm, vmm + v0), G[2][1] = fma(3.0, v0, fma(-4.0, vm, vmm));
+#pragma unroll
+      for (int s = 0; s < 3; ++s) beta[s] = fma((13.0 / 12.0) * G[s][0], G[s][0], 0.25 * G[s][1] * G[s][1]);
+    }
+    double sa = 0.0, st = 0.0;
+#pragma unroll
+    for (int s = 0; s < K; ++s) {
+      ie[s] = 1.0 / (eps + beta[s]);
+      w[s] = Tab<K>::d(s) * ie[s] * ie[s];
+      u[s] = Tab<K>::d(K - 1 - s) * ie[s] * ie[s];
+      sa += w[s];
+      st += u[s];
+    }
+    vr = 0.0, vl = 0.0;
+#pragma unroll
+    for (int s = 0; s < K; ++s) {
+      w[s] /= sa;
+      u[s] /= st;
+      vr = fma(w[s], q[s], vr);
+      vl = fma(u[s], r[s], vl);
+    }
+  }
+  // out[0 .. 2K-2] += d(ar vr + al vl)/dp for p[-(K-1) .. K-1]
+  __device__ void rev(double ar, double al, double* out) const {
+#pragma unroll
+    for (int s = 0; s < K; ++s) {
+      const double dq = ar * w[s], dr = al * u[s];
+#pragma unroll
+      for (int j = 0; j < K; ++j) out[K - 1 + j - s] += fma(dq, ci[j + K * (s + 1)], dr * ci[j + K * s]);
+      if constexpr (K > 1) {
+        // d beta_s = -2 [ar w_s (q_s - vr) + al w~_s (r_s - vl)] / (eps + beta_s)
+        const double db = -2.0 * ie[s] * fma(dq, q[s] - vr, dr * (r[s] - vl));
+        if constexpr (K == 2) {  // beta_s = D_s^2: D0 = p1 - p0, D1 = p0 - p_{-1}
+          const double g = 2.0 * G[s][0] * db;
+          out[2 - s] += g;
+          out[1 - s] -= g;
+        } else {  // 13/12 A_s^2 + 1/4 B_s^2 with the gradients of WenoTape<3>::rev
+          const double gA = (13.0 / 6.0) * G[s][0] * db, gB = 0.5 * G[s][1] * db;
+          if (s == 0) {
+            out[2] += gA + 3.0 * gB, out[3] += -2.0 * gA - 4.0 * gB, out[4] += gA + gB;
+          } else if (s == 1) {
+            out[1] += gA + gB, out[2] += -2.0 * gA, out[3] += gA - gB;
+          } else {
+            out[0] += gA + gB, out[1] += -2.0 * gA - 4.0 * gB, out[2] += gA + 3.0 * gB;
+          }
+        }
+      }
+    }
   }
 };
 
@@ -371,6 +464,52 @@ __global__ void __launch_bounds__(256, TAPE ? HRW_ADJ_TAPE_MINB : HRW_ADJ_FWD_MI
   }
 }
 
+// --------------------------------------------------------------------------------------------
+// Forward stage on a non-uniform line (FAST FP64), segment-aware, one cell per thread: the
+// arithmetic of the single-line non-uniform stage (recon_nu, numflux, flux_diff, combine_fast
+// with the cell's own scale), so a one-segment line gives the same states as hrw_integrate.
+// --------------------------------------------------------------------------------------------
+template <int K>
+__device__ __forceinline__ void recon_cell_nu(const AdjLine& A, const double* __restrict__ v, int64_t j,
+                                              double& vl, double& vr) {
+  j = j < 0 ? 0 : (j >= A.n ? A.n - 1 : j);
+  const int64_t s0 = j / A.seg * A.seg, s1 = s0 + A.seg - 1;
+  double p[2 * K - 1];
+#pragma unroll
+  for (int q = 0; q < 2 * K - 1; ++q) {
+    int64_t g = j - (K - 1) + q;
+    g = g < s0 ? s0 : (g > s1 ? s1 : g);  // ghosts replicate the segment's end cells
+    p[q] = v[g];
+  }
+  recon_nu<K, false>(&p[K - 1], A.cnu + (int64_t)K * (K + 1) * (j - s0), A.eps, vl, vr);
+}
+
+template <int K, int ST, int NT>
+__global__ void __launch_bounds__(NT) adj_fwd_nu_kernel(AdjLine A, StageArgs a) {
+  __shared__ double sL[NT + 1], sR[NT + 1];  // vl of cell s+t at sL[t], vr at sR[t+1]
+  const LineArgs L = line_args(A);
+  const int64_t s = (int64_t)blockIdx.x * NT;
+  const int t = threadIdx.x;
+  const int64_t j = s + t;
+  double vl, vr;
+  recon_cell_nu<K>(A, a.v, j, vl, vr);
+  sL[t] = vl;
+  sR[t + 1] = vr;
+  if (t >= NT - 2) {  // cells s - 1 (vr) and s + NT (vl); across a segment end the boundary
+    double el, er;    // rules replace the interface, so their values are not used there
+    recon_cell_nu<K>(A, a.v, t == NT - 2 ? s - 1 : s + NT, el, er);
+    if (t == NT - 2) sR[0] = er;
+    else sL[NT] = el;
+  }
+  __syncthreads();
+  if (j >= A.n) return;
+  const int64_t li = j % A.seg;
+  const double FL = numflux<false>(L, sR[t], vl, li);
+  const double FR = numflux<false>(L, vr, sL[t + 1], li + 1);
+  const double dF = flux_diff<false>(L, li, FL, FR, vr);
+  combine_fast<ST>(a, j, a.v[j], dF, A.rwsv[li]);
+}
+
 // does cell with local index lc use the interface flux on its right / left?
 __device__ __forceinline__ bool uses_fr(int bc, int64_t lc, int64_t seg) {
   if (bc == HRW_BC_COPY) return lc > 0 && lc < seg - 1;
@@ -384,8 +523,8 @@ __device__ __forceinline__ bool uses_fl(int bc, int64_t lc, int64_t seg) {
 __device__ __forceinline__ double dflux(const AdjLine& A, double v, int64_t e) {
   // f'(v) at interface e (local index): Burgers u, linear g(x_e)
   if (A.fn == HRW_FN_BURGERS) return v;
-  if (A.fn == HRW_FN_BURGERS_LINEAR) return v + fma(A.b, fma(A.rx, (double)e, A.xmin), A.a);
-  return fma(A.b, fma(A.rx, (double)e, A.xmin), A.a);
+  const double g = fma(A.b, A.xe ? A.xe[e] : fma(A.rx, (double)e, A.xmin), A.a);
+  return A.fn == HRW_FN_BURGERS_LINEAR ? v + g : g;
 }
 
 enum AdjMode : int { ADJ_A3 = 0, ADJ_A2 = 1, ADJ_A1 = 2 };
@@ -395,7 +534,8 @@ enum AdjMode : int { ADJ_A3 = 0, ADJ_A2 = 1, ADJ_A1 = 2 };
 //   state: v (the stage input of the forward stage), mu: adjoint of that stage's L output
 //   (scaled as described in the mode), acc: the accumulated adjoint of u.
 // --------------------------------------------------------------------------------------------
-template <int K, int MODE, int NT, bool TAPE>
+// NU: a non-uniform line (recomputes its WENO maps with the cells' coefficients; no tape)
+template <int K, int MODE, int NT, bool TAPE, bool NU = false>
 __global__ void __launch_bounds__(NT) adj_vjp_kernel(AdjLine A, const double* __restrict__ v,
                                                      const double* __restrict__ wt,
                                                      const double* __restrict__ mu,
@@ -414,7 +554,7 @@ __global__ void __launch_bounds__(NT) adj_vjp_kernel(AdjLine A, const double* __
     if (i >= 0 && i < A.n) {
       const int64_t s0 = i / A.seg * A.seg, s1 = s0 + A.seg - 1, li = i - s0;
       double p[NS];
-      WenoTape<K> W;
+      std::conditional_t<NU, WenoTapeNu<K>, WenoTape<K>> W;
       double vl, vr;
       if constexpr (TAPE) {  // the forward pass recorded the cell's WENO map
         vr = wt[i];
@@ -426,24 +566,35 @@ __global__ void __launch_bounds__(NT) adj_vjp_kernel(AdjLine A, const double* __
           g = g < s0 ? s0 : (g > s1 ? s1 : g);
           p[q] = v[g];
         }
-        W.fwd(&p[K - 1], A.eps);
+        if constexpr (NU) W.fwd(&p[K - 1], A.eps, A.cnu + (int64_t)K * (K + 1) * li);
+        else W.fwd(&p[K - 1], A.eps);
         vl = W.vl, vr = W.vr;
       }
       const double mi = mu[i];
-      // flux adjoints of the cell's right and left interfaces
+      // flux adjoints of the cell's right and left interfaces; L_i = -(F_{i+1/2} - F_{i-1/2})
+      // / width_i, so a flux weighs each neighbour's adjoint by that cell's 1 / width
+      const double ri = NU ? A.rdxv[li] : idx;
       double ar = 0.0, al = 0.0;
       if (li < A.seg - 1) {
         const double mp = mu[i + 1];
-        const double phi = ((uses_fl(A.bc, li + 1, A.seg) ? mp : 0.0) -
-                            (uses_fr(A.bc, li, A.seg) ? mi : 0.0)) * hidx;  // phi / 2
+        double phi;  // phi / 2
+        if constexpr (NU)
+          phi = 0.5 * ((uses_fl(A.bc, li + 1, A.seg) ? mp * A.rdxv[li + 1] : 0.0) -
+                       (uses_fr(A.bc, li, A.seg) ? mi * ri : 0.0));
+        else
+          phi = ((uses_fl(A.bc, li + 1, A.seg) ? mp : 0.0) - (uses_fr(A.bc, li, A.seg) ? mi : 0.0)) * hidx;
         ar = phi * (dflux(A, vr, li + 1) + A.alpha);
       } else if (A.bc == HRW_BC_ZERO_INFLOW) {  // F_{nc+1/2} = f(vr(nc))
-        ar = -mi * idx * dflux(A, vr, li + 1);
+        ar = -mi * ri * dflux(A, vr, li + 1);
       }
       if (li > 0) {
         const double mm = mu[i - 1];
-        const double phi = ((uses_fl(A.bc, li, A.seg) ? mi : 0.0) -
-                            (uses_fr(A.bc, li - 1, A.seg) ? mm : 0.0)) * hidx;
+        double phi;
+        if constexpr (NU)
+          phi = 0.5 * ((uses_fl(A.bc, li, A.seg) ? mi * ri : 0.0) -
+                       (uses_fr(A.bc, li - 1, A.seg) ? mm * A.rdxv[li - 1] : 0.0));
+        else
+          phi = ((uses_fl(A.bc, li, A.seg) ? mi : 0.0) - (uses_fr(A.bc, li - 1, A.seg) ? mm : 0.0)) * hidx;
         al = phi * (dflux(A, vl, li) - A.alpha);
       }
       if constexpr (TAPE) rev_tape<K>(wt, A.n, i, ar, al, o);
@@ -561,33 +712,46 @@ cudaError_t fwd_stage_kt(const AdjLine& A, const StageArgs& a, int st, double* w
 
 // taped passes run fewer cells per thread (the tape's intermediates need the registers)
 template <int K>
+cudaError_t fwd_stage_nu(const AdjLine& A, const StageArgs& a, int st, cudaStream_t s) {
+  constexpr int NT = 128;
+  const unsigned blocks = (unsigned)((A.n + NT - 1) / NT);
+  if (st == ST_EULER) adj_fwd_nu_kernel<K, ST_EULER, NT><<<blocks, NT, 0, s>>>(A, a);
+  else if (st == ST_RK3B) adj_fwd_nu_kernel<K, ST_RK3B, NT><<<blocks, NT, 0, s>>>(A, a);
+  else adj_fwd_nu_kernel<K, ST_RK3C, NT><<<blocks, NT, 0, s>>>(A, a);
+  return cudaGetLastError();
+}
+
+template <int K>
 cudaError_t fwd_stage_k(const AdjLine& A, const StageArgs& a, int st, double* wt, cudaStream_t s) {
+  if (A.cnu) return fwd_stage_nu<K>(A, a, st, s);
   if (TapeN<K>::n > 0 && wt) return fwd_stage_kt<K, HRW_ADJ_TAPE_C, true>(A, a, st, wt, s);
   return fwd_stage_kt<K, HRW_ADJ_FWD_C, false>(A, a, st, nullptr, s);
 }
 
-template <int K, bool TAPE>
+template <int K, bool TAPE, bool NU = false>
 cudaError_t vjp_kt(const AdjLine& A, int mode, const double* v, const double* wt, const double* mu,
                    double* acc, double* out, double dt, cudaStream_t s) {
   constexpr int NT = HRW_ADJ_VJP_NT;
   const unsigned blocks = (unsigned)((A.n + NT - 1) / NT);
   if (mode == ADJ_A3)
-    adj_vjp_kernel<K, ADJ_A3, NT, TAPE><<<blocks, NT, 0, s>>>(A, v, wt, mu, acc, out, dt);
+    adj_vjp_kernel<K, ADJ_A3, NT, TAPE, NU><<<blocks, NT, 0, s>>>(A, v, wt, mu, acc, out, dt);
   else if (mode == ADJ_A2)
-    adj_vjp_kernel<K, ADJ_A2, NT, TAPE><<<blocks, NT, 0, s>>>(A, v, wt, mu, acc, out, dt);
+    adj_vjp_kernel<K, ADJ_A2, NT, TAPE, NU><<<blocks, NT, 0, s>>>(A, v, wt, mu, acc, out, dt);
   else
-    adj_vjp_kernel<K, ADJ_A1, NT, TAPE><<<blocks, NT, 0, s>>>(A, v, wt, mu, acc, out, dt);
+    adj_vjp_kernel<K, ADJ_A1, NT, TAPE, NU><<<blocks, NT, 0, s>>>(A, v, wt, mu, acc, out, dt);
   return cudaGetLastError();
 }
 
 template <int K>
 cudaError_t vjp_k(const AdjLine& A, int mode, const double* v, const double* wt, const double* mu,
                   double* acc, double* out, double dt, cudaStream_t s) {
+  if (A.cnu) return vjp_kt<K, false, true>(A, mode, v, nullptr, mu, acc, out, dt, s);
   if (TapeN<K>::n > 0 && wt) return vjp_kt<K, true>(A, mode, v, wt, mu, acc, out, dt, s);
   return vjp_kt<K, false>(A, mode, v, nullptr, mu, acc, out, dt, s);
 }
 
 cudaError_t fwd_stage(const AdjLine& A, const StageArgs& a, int st, double* wt, cudaStream_t s) {
+  if (A.k == 1 && A.cnu) return fwd_stage_nu<1>(A, a, st, s);
   if (A.k == 1) return fwd_stage_k<1>(A, a, st, nullptr, s);
   if (A.k == 2) return fwd_stage_k<2>(A, a, st, wt, s);
   return fwd_stage_k<3>(A, a, st, wt, s);
@@ -596,12 +760,18 @@ cudaError_t fwd_stage(const AdjLine& A, const StageArgs& a, int st, double* wt, 
 // v: the stage's input state; wt: the stage's WENO tape (null: recompute from v)
 cudaError_t vjp(const AdjLine& A, int mode, const double* v, const double* wt, const double* mu,
                 double* acc, double* out, double dt, cudaStream_t s) {
-  if (A.k == 1) return vjp_k<1>(A, mode, v, nullptr, mu, acc, out, dt, s);
+  if (A.k == 1) return A.cnu ? vjp_kt<1, false, true>(A, mode, v, nullptr, mu, acc, out, dt, s)
+                            : vjp_k<1>(A, mode, v, nullptr, mu, acc, out, dt, s);
   if (A.k == 2) return vjp_k<2>(A, mode, v, wt, mu, acc, out, dt, s);
   return vjp_k<3>(A, mode, v, wt, mu, acc, out, dt, s);
 }
 
-int tape_entries(int k) { return k == 3 ? TapeN<3>::n : (k == 2 ? TapeN<2>::n : 0); }
+// doubles per cell and stage of the WENO tape (none on a non-uniform line: its reverse pass
+// recomputes the maps)
+int tape_entries(const AdjLine& A) {
+  if (A.cnu) return 0;
+  return A.k == 3 ? TapeN<3>::n : (A.k == 2 ? TapeN<2>::n : 0);
+}
 
 }  // namespace
 }  // namespace hrw
@@ -616,6 +786,7 @@ struct hrw_adjoint {
   double *u = nullptr, *w1 = nullptr, *w2 = nullptr, *tgt = nullptr;
   double *lam = nullptr, *la = nullptr, *lb = nullptr, *acc = nullptr, *J = nullptr;
   double* part = nullptr;     // partial sums of J (nseg x misfit blocks per segment)
+  double* nu = nullptr;       // non-uniform line: cnu, 1 / width, scale / width, edges
   std::vector<double*> ckpt;  // checkpoints
   double* tape = nullptr;     // (E + 1) states + E u1 + E u2 of the segment being reversed
   int64_t tape_states = 0;    // capacity of the tape in states
@@ -659,7 +830,7 @@ cudaError_t misfit(hrw_adjoint* h, const double* u) {
 // (nullable): the WENO tape of the step's three stages, one after the other
 cudaError_t step(hrw_adjoint* h, const double* u, double* s1, double* s2, double* un, double dt,
                  double* wt = nullptr) {
-  const size_t plane = (size_t)tape_entries(h->line.k) * (size_t)h->line.n;
+  const size_t plane = (size_t)tape_entries(h->line) * (size_t)h->line.n;
   StageArgs a = base_args(h, dt);
   a.v = u, a.u = u, a.out = s1;
   cudaError_t e = fwd_stage(h->line, a, ST_EULER, wt, h->stream);
@@ -682,10 +853,15 @@ int hrw_adjoint_create(const hrw_problem* p, int nseg, int checkpoint_every, hrw
   if (p->kind != HRW_PROBLEM_FV1D) return adj_fail(HRW_EINVAL, "hrw_adjoint: FV1D problems only.");
   if (p->flux != HRW_FLUX_LAX_FRIEDRICHS)
     return adj_fail(HRW_EINVAL, "hrw_adjoint: the global Lax-Friedrichs flux with fixed alpha only.");
-  if (p->width[0] || p->xedges[0]) return adj_fail(HRW_EINVAL, "hrw_adjoint: uniform grids only.");
+  if (p->width[0]) return adj_fail(HRW_EINVAL, "hrw_adjoint: non-uniform lines are given as xedges.");
   if (p->ncells[0] <= 0) return adj_fail(HRW_EINVAL, "Invalid input 'ncells'. Valid range: ncells > 0.");
-  if (!(p->xmax[0] > p->xmin[0]))
+  if (p->xedges[0]) {
+    for (int i = 0; i < p->ncells[0]; ++i)
+      if (!(p->xedges[0][i + 1] > p->xedges[0][i]))
+        return adj_fail(HRW_EINVAL, "Invalid input 'xedges': edges must increase.");
+  } else if (!(p->xmax[0] > p->xmin[0])) {
     return adj_fail(HRW_EINVAL, "Invalid input 'xmin', 'xmax'. Valid range: xmax > xmin.");
+  }
   if (p->k < 1 || p->k > 3) return adj_fail(HRW_EINVAL, "Invalid input 'k'. Valid range: 1 <= k <= 3.");
   if (!(p->eps > 2.220446049250313e-16))
     return adj_fail(HRW_EINVAL, "Invalid input 'eps'. Valid range: eps > epsilon.");
@@ -721,6 +897,30 @@ int hrw_adjoint_create(const hrw_problem* p, int nseg, int checkpoint_every, hrw
     if (e == cudaSuccess) e = cudaMalloc(b, bytes);
   if (e == cudaSuccess) e = cudaMalloc(&h->J, sizeof(double) * nseg);
   if (e == cudaSuccess) e = cudaMalloc(&h->part, sizeof(double) * nseg * misfit_blocks_per_seg(L));
+  if (e == cudaSuccess && p->xedges[0]) {
+    // weno(ncells, k, eps, xedges): the coefficients on the device (as hrw_rktvd_create builds
+    // them), the widths edges(i) - edges(i-1) and the flux at the true edges
+    const size_t nc = (size_t)L.seg, ncf = (size_t)L.k * (L.k + 1);
+    std::vector<double> host(2 * nc + nc + 1);
+    const double fs = fast_flux_scale(HRW_FLUX_LAX_FRIEDRICHS, L.fn);
+    for (size_t i = 0; i < nc; ++i) {
+      const double w = p->xedges[0][i + 1] - p->xedges[0][i];
+      host[i] = 1.0 / w;
+      host[nc + i] = fs / w;
+    }
+    for (size_t i = 0; i <= nc; ++i) host[2 * nc + i] = p->xedges[0][i];
+    e = cudaMalloc(&h->nu, sizeof(double) * (nc * ncf + host.size()));
+    if (e == cudaSuccess)
+      e = cudaMemcpy(h->nu + nc * ncf, host.data(), sizeof(double) * host.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+      L.cnu = h->nu;
+      L.rdxv = h->nu + nc * ncf;
+      L.rwsv = L.rdxv + nc;
+      L.xe = L.rwsv + nc;
+      e = launch_calc_cnu(L.xe, h->nu, (int)nc, L.k, h->own);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->own);
+  }
   if (e != cudaSuccess) {
     hrw_adjoint_destroy(h);
     return adj_fail(e == cudaErrorMemoryAllocation ? HRW_ENOMEM : HRW_ECUDA,
@@ -745,7 +945,7 @@ static int adjoint_sweep(hrw_adjoint* h, int mem, const double* u0, const double
   // Memory budget: 80% of the free device memory plus the tapes this handle already holds.
   // A segment of E steps needs 3E + 1 states and, for the WENO tape, 3E stage planes of
   // tape_entries(k) doubles per cell.
-  const int nq = tape_entries(L.k);
+  const int nq = tape_entries(L);
   size_t fr = 0, tot = 0;
   HRW_ACUDA(cudaMemGetInfo(&fr, &tot));
   const double budget = 0.8 * ((double)fr + (double)bytes * (double)h->tape_states +
@@ -906,7 +1106,7 @@ int hrw_adjoint_tape_info(const hrw_adjoint* h, int64_t* state_bytes, int64_t* w
 int hrw_adjoint_destroy(hrw_adjoint* h) {
   if (!h) return HRW_OK;
   double* bufs[] = {h->u, h->w1, h->w2, h->tgt, h->lam, h->la, h->lb, h->acc, h->J, h->tape,
-                    h->wtape, h->part};
+                    h->wtape, h->part, h->nu};
   for (double* b : bufs)
     if (b) cudaFree(b);
   for (double* c : h->ckpt) cudaFree(c);

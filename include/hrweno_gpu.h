@@ -109,8 +109,8 @@ typedef struct hrw_problem {
   const double* rates;    /* LINEAR_ODE: host array(neq) of rates a_i */
   int32_t numerics;       /* HRW_NUMERICS_* */
   /* optional host array(nc+1) of cell edges of a non-uniform line, per dimension (FV1D and
-   * FV2D; HRW_F64 and HRW_F32 handles, HRW_F32C handles of FV1D problems and HRW_F64
-   * batches, not the adjoint or the allocation-free steps): the WENO coefficients become cnu(xedges) as weno(ncells, k, eps,
+   * FV2D; HRW_F64 and HRW_F32 handles, HRW_F32C handles of FV1D problems, HRW_F64 batches
+   * and the adjoint, not the allocation-free steps): the WENO coefficients become cnu(xedges) as weno(ncells, k, eps,
    * xedges) builds them (src/hrweno_weno.f90:100-104,221-297), the widths edges(i) - edges(i-1)
    * and the flux's x the edges themselves; xmin/xmax are then unused and width[] must be NULL.
    * NULL: uniform grid. */
@@ -233,7 +233,9 @@ int hrw_batch_destroy(hrw_batch* b);
  * k = 2) when they fit in 80% of the free device memory, so the reverse pass does not
  * recompute them.  checkpoint_every = 0 picks the first that fits that budget: the whole
  * trajectory with the WENO tape, sqrt(nsteps) segments with it, the whole trajectory's
- * states without it, sqrt(nsteps) segments without it. */
+ * states without it, sqrt(nsteps) segments without it.  A non-uniform line (p->xedges[0],
+ * the same edges for every problem of the state) keeps no WENO tape: the reverse pass
+ * recomputes each cell's map with its own coefficients; width[] is refused. */
 typedef struct hrw_adjoint hrw_adjoint;
 int hrw_adjoint_create(const hrw_problem* p, int nseg, int checkpoint_every, hrw_adjoint** out);
 /* grad = dJ/du0 (nseg * ncells doubles), J[nseg]; arrays in memory space `mem` (J on the host) */

@@ -60,6 +60,64 @@ def test_adjoint_vs_tangent_linear(hw, orc, case):
     assert adj.forward_steps == steps + (steps - steps % 7 if steps % 7 else steps - 7)
 
 
+def stretched_edges(n, seed):
+    """Edges on [-5, 5] with random widths in a 1:3 range."""
+    rng = np.random.default_rng(seed)
+    w = rng.uniform(0.5, 1.5, n)
+    return np.concatenate([[-5.0], -5.0 + np.cumsum(w) * (10.0 / w.sum())])
+
+
+NU_CASES = CASES + [dict(k=3, fn="burgers_linear", bc="copy"), dict(k=2, fn="burgers", bc="zero_inflow")]
+
+
+@pytest.mark.parametrize("case", range(len(NU_CASES)))
+def test_adjoint_nonuniform_vs_tangent_linear(hw, orc, case):
+    """weno(ncells, k, eps, xedges) in the adjoint: each cell's coefficients in the candidates
+    and their transposes, the cells' own widths in the flux adjoints, g at the true edges."""
+    n, steps = 400, 60
+    c = NU_CASES[case]
+    a, b = (0.7, 0.1) if c["fn"] != "burgers" else (1.0, 0.0)
+    xe = stretched_edges(n, case)
+    prob = hw.Problem(kind="fv1d", ncells=(n, 1), k=c["k"], eps=1e-6, flux="lax_friedrichs",
+                      fn=(c["fn"], c["fn"]), coef_a=(a, 0), coef_b=(b, 0), alpha=(1.5, 1.5),
+                      bc=(c["bc"], c["bc"]), xedges=(xe, None))
+    xc = 0.5 * (xe[1:] + xe[:-1])
+    u0 = np.interp(xc, np.linspace(-5, 5, n), line(n, case))
+    target = np.interp(xc, np.linspace(-5, 5, n), line(n, case + 100)) * 0.8
+    dt = 0.4 * np.min(np.diff(xe)) / 2.0
+    adj = hw.adjoint(prob, checkpoint_every=7)
+    J, g = adj.gradient(u0, target, dt, steps)
+    assert adj.tape_bytes[1] == 0  # the reverse recomputes the non-uniform maps
+    for s in range(3):
+        d = np.random.default_rng(s).standard_normal(n) if s else smooth_direction(n, s)
+        Jo, dJ = orc.tl_misfit(prob, u0, d, target, dt, steps)
+        assert abs(J[0] - Jo) <= 1e-12 * abs(Jo)
+        assert abs(g @ d - dJ) <= 1e-10 * max(abs(dJ), 1e-30), (case, s, g @ d, dJ)
+
+
+def test_adjoint_nonuniform_forward_and_batch(hw):
+    """The adjoint's forward map on a non-uniform line is hrw_integrate's (same bits), and a
+    batch of segments on the same edges matches one-segment solves."""
+    n, nseg, steps = 256, 3, 40
+    xe = stretched_edges(n, 11)
+    prob = hw.Problem(kind="fv1d", ncells=(n, 1), k=3, eps=1e-6, flux="lax_friedrichs",
+                      fn=("burgers", "burgers"), alpha=(1.5, 1.5), bc=("zero_inflow", "zero_inflow"),
+                      xedges=(xe, None))
+    dt = 0.4 * np.min(np.diff(xe)) / 1.5
+    u0 = np.concatenate([line(n, s) for s in range(nseg)])
+    tg = np.concatenate([line(n, 50 + s) * 0.9 for s in range(nseg)])
+    _, uT = hw.adjoint(prob).forward(u0[:n], None, dt, steps, uT=np.empty(n))
+    ui = u0[:n].copy()
+    hw.rktvd(prob, n, 3).integrate(ui, 0.0, (steps - 0.5) * dt, dt)
+    assert np.array_equal(uT, ui)
+    Jb, gb = hw.adjoint(prob, nseg=nseg, checkpoint_every=9).gradient(u0, tg, dt, steps)
+    for s in range(nseg):
+        sl = slice(s * n, (s + 1) * n)
+        J1, g1 = hw.adjoint(prob, checkpoint_every=9).gradient(u0[sl], tg[sl], dt, steps)
+        assert np.array_equal(gb[sl], g1)
+        assert abs(Jb[s] - J1[0]) <= 1e-13 * J1[0]
+
+
 def test_adjoint_checkpoint_interval_invariant(hw):
     n, steps = 300, 50
     prob = problem(hw, n, 3, "burgers", "copy")
@@ -138,7 +196,7 @@ def test_torch_autograd_op(hw):
     loss = 0.5 * ((uT - tg) ** 2).sum()
     loss.backward()
     J, g = hw.adjoint(prob, checkpoint_every=0).gradient(u0.detach(), tg, dt, steps)
-    assert abs(float(loss) - J[0]) <= 1e-13 * J[0]
+    assert abs(loss.item() - J[0]) <= 1e-13 * J[0]
     assert torch.equal(u0.grad, g)
     # batched lines with a weighted loss
     u0b = torch.from_numpy(np.stack([line(n, 7), line(n, 8)])).cuda().requires_grad_(True)
