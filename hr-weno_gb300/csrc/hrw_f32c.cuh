@@ -102,7 +102,10 @@ __device__ __forceinline__ void recon_diff(const float* d, float eps, float& rl,
     // candidates x6
     const float R0 = fmaf(4.f, d0, -d1), R1 = fmaf(2.f, d0, dm), R2 = fmaf(5.f, dm, -2.f * dmm);
     const float L0 = fmaf(2.f, d1, -5.f * d0), L1 = -fmaf(2.f, dm, d0), L2 = fmaf(-4.f, dm, dmm);
-    if (fmaxf(s0, fmaxf(s1, s2)) < 1e18f) {
+    // The product form's numerator is at most 30.4 max(s)^2.25 (|R_r| <= 3.04 sqrt(e_r), the
+    // indicators being positive definite forms in the same differences), finite in FP32 up to
+    // max(s) = 2.9e16; above 1e16 the division form.
+    if (fmaxf(s0, fmaxf(s1, s2)) < 1e16f) {
       // d = (3, 6, 1)/10: w_r ~ d_r P_r with P_0 = s1 s2, P_1 = s0 s2, P_2 = s0 s1
       const float P0 = s1 * s2, P1 = s0 * s2, P2 = s0 * s1;
       const float den = fmaf(3.f, P0, fmaf(6.f, P1, P2));
@@ -135,7 +138,7 @@ __device__ __forceinline__ void recon_diff3_shared(const float* d, float t0, flo
   const float s0 = e0 * e0, s1 = e1 * e1, s2 = e2 * e2;
   const float R0 = fmaf(4.f, d0, -d1), R1 = fmaf(2.f, d0, dm), R2 = fmaf(5.f, dm, -2.f * dmm);
   const float L0 = fmaf(2.f, d1, -5.f * d0), L1 = -fmaf(2.f, dm, d0), L2 = fmaf(-4.f, dm, dmm);
-  if (fmaxf(s0, fmaxf(s1, s2)) < 1e18f) {
+  if (fmaxf(s0, fmaxf(s1, s2)) < 1e16f) {  // the bound of recon_diff<3>
     const float P0 = s1 * s2, P1 = s0 * s2, P2 = s0 * s1;
     const float den = fmaf(3.f, P0, fmaf(6.f, P1, P2));
     const float num = fmaf(3.f * P0, R0, fmaf(6.f * P1, R1, P2 * R2));
@@ -196,7 +199,9 @@ __device__ __forceinline__ void recon_diff_nu(const float* d, const float* ci, f
       const float dm = d[0], d0 = d[1];
       const float e0 = fmaf(d0, d0, eps), e1 = fmaf(dm, dm, eps);
       const float s0 = e0 * e0, s1 = e1 * e1;
-      if (fmaxf(s0, s1) < 1e30f) {  // w0 = 2 s1 / (2 s1 + s0), mirrored w~0 = s1 / (s1 + 2 s0)
+      // w0 = 2 s1 / (2 s1 + s0), mirrored w~0 = s1 / (s1 + 2 s0); the candidates carry the
+      // coefficients' sums (a few units on graded lines), hence a lower bound than uniform k = 2
+      if (fmaxf(s0, s1) < 1e28f) {
         rr = fmaf(2.f * s1, R[0], s0 * R[1]) * rcpf(fmaf(2.f, s1, s0));
         rl = fmaf(s1, Lc[0], 2.f * s0 * Lc[1]) * rcpf(fmaf(2.f, s0, s1));
       } else {
@@ -214,7 +219,7 @@ __device__ __forceinline__ void recon_diff_nu(const float* d, const float* ci, f
       const float e1 = eps + fmaf(c13 * A1, A1, 0.25f * B1 * B1);
       const float e2 = eps + fmaf(c13 * A2, A2, 0.25f * B2 * B2);
       const float s0 = e0 * e0, s1 = e1 * e1, s2 = e2 * e2;
-      if (fmaxf(s0, fmaxf(s1, s2)) < 1e18f) {
+      if (fmaxf(s0, fmaxf(s1, s2)) < 1e14f) {  // as recon_diff<3>, with room for the coefficients
         const float P0 = s1 * s2, P1 = s0 * s2, P2 = s0 * s1;
         const float den = fmaf(3.f, P0, fmaf(6.f, P1, P2));
         const float dent = fmaf(3.f, P2, fmaf(6.f, P1, P0));

@@ -96,6 +96,46 @@ def test_rhs_f32c_nonuniform(hw, orc, k, nc, kind):
         assert np.max(np.abs(got - ref)) <= 2e-6 * scale, (c, np.max(np.abs(got - ref)) / scale)
 
 
+def jumpy(n, seed, amp=(3e3, 3e4)):
+    """A state of plateaus with jumps of |amp[0]| .. |amp[1]|: the WENO indicators' squares
+    then span 1e13 .. 1e20, across the bound between the weights' product and division forms."""
+    rng = np.random.default_rng(seed)
+    u = np.zeros(n)
+    for p in np.sort(rng.choice(np.arange(5, n - 5), size=max(n // 50, 2), replace=False)):
+        u[p:] += rng.choice([-1.0, 1.0]) * np.exp(rng.uniform(np.log(amp[0]), np.log(amp[1])))
+    return u - u.min() + 1.0 + 50.0 * np.sin(np.linspace(0.0, 6.0, n))
+
+
+@pytest.mark.parametrize("k", [2, 3])
+def test_rhs_f32c_large_jumps(hw, orc, k):
+    """Differences of 1e3 .. 3e4 between neighbours: the weights' product form stays finite
+    (the fast branch is taken only while the indicators' squares are below 1e16), so the
+    compensated right-hand side matches FP64 as on O(1) data.  Uniform and non-uniform lines
+    and a 2D grid."""
+    n = 1000
+    u = jumpy(n, k)
+    amax = float(np.max(np.abs(u)))
+    xe = stretched(n, "random", 3)
+    cases = [hw.burgers_1d(n, -5.0, 5.0, k=k, flux="lax_friedrichs", alpha=amax),
+             hw.burgers_1d(n, -5.0, 5.0, k=k, flux="godunov", bc="zero"),
+             hw.Problem(kind="fv1d", ncells=(n, 1), k=k, flux="lax_friedrichs", fn=("burgers", "burgers"),
+                        alpha=(amax, amax), xedges=(xe, None))]
+    for prob in cases:
+        ref = orc.rhs(prob, u)
+        got = rhs_f32c(prob, u)
+        assert np.isfinite(got).all()
+        assert np.max(np.abs(got - ref)) <= 2e-6 * np.max(np.abs(ref)), np.max(np.abs(got - ref)) / np.max(np.abs(ref))
+    from hrweno import workloads
+    n1 = n2 = 96
+    prob, _, _ = workloads.pbe_config(n1, n2)
+    v = np.stack([jumpy(n1, 10 + r) for r in range(n2)]).ravel()
+    v += np.repeat(jumpy(n2, 99), n1)
+    ref = orc.rhs(prob, v)
+    got = rhs_f32c(prob, v)
+    assert np.isfinite(got).all()
+    assert np.max(np.abs(got - ref)) <= 2e-6 * np.max(np.abs(ref))
+
+
 @pytest.mark.parametrize("method", ["rktvd", "mstvd"])
 @pytest.mark.parametrize("kind", ["cubic", "random"])
 def test_f32c_nonuniform_integrate(hw, orc, method, kind):
