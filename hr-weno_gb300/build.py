@@ -39,7 +39,7 @@ ORACLE_BASELINE_FLAGS = ["-O3", "-fopenmp", "-fPIC", "-shared", "-std=c++17"]
 NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 # sources whose kernel instantiations are split over several objects, each compiled with
 # -DHRW_PART=i, so that the longest translation units build in parallel
-PARTS = {"stage2d.cu": 9, "batch.cu": 3}
+PARTS = {"stage2d.cu": 9, "batch.cu": 3, "stage2d_f32c.cu": 2}
 # the slowest units first, so that they do not start last
 SLOW_FIRST = ["stage2d.cu", "batch.cu", "stage1d_f32c.cu", "stage2d_f32c.cu", "stage1d.cu"]
 

@@ -527,8 +527,6 @@ static int ode_create(const hrw_problem* p, int neq, int order, int method, int 
   if (rc != HRW_OK) return rc;
   if (dtype == HRW_F32 && (rc = validate_problem_f32(p)) != HRW_OK) return rc;
   if (dtype == HRW_F32C) {
-    if (p->kind == HRW_PROBLEM_FV2D && (p->xedges[0] || p->xedges[1]))
-      return fail(HRW_EINVAL, "Invalid input 'xedges': HRW_F32C takes non-uniform lines in FV1D problems.");
     if (p->kind != HRW_PROBLEM_FV1D && p->kind != HRW_PROBLEM_FV2D)
       return fail(HRW_EINVAL, "Invalid input 'dtype': HRW_F32C supports FV1D and FV2D problems.");
     if (!(p->eps > 1.1920928955078125e-07))  // epsilon(1.0_real32), src/hrweno_weno.f90:92
@@ -645,8 +643,9 @@ static int ode_create(const hrw_problem* p, int neq, int order, int method, int 
     size_t nw = 0;  // per-cell 1/width entries of the lines that have widths
     for (int d = 0; d < nd; ++d)
       if (p->width[d]) nw += (size_t)(p->ncells[d] + 63) / 64 * 64;
-    // a non-uniform line (FV1D): 1/width, the edges, b width and k (k + 1) coefficients per cell
-    if (p->xedges[0]) nw += ((size_t)p->ncells[0] + 64) / 64 * 64 * (3 + (size_t)p->k * (p->k + 1));
+    // a non-uniform line: 1/width, the edges, b width and k (k + 1) coefficients per cell
+    for (int d = 0; d < nd; ++d)
+      if (p->xedges[d]) nw += ((size_t)p->ncells[d] + 64) / 64 * 64 * (3 + (size_t)p->k * (p->k + 1));
     const size_t nf = sn * (2 * slots + (method == 1 ? 4 : 0) + 2) + nw;
     if ((e = cudaMalloc(&o->fmem, sizeof(float) * nf)) != cudaSuccess) return cleanup(e);
     float* q = o->fmem;
@@ -710,10 +709,10 @@ static int ode_create(const hrw_problem* p, int neq, int order, int method, int 
         q += seg * (3 + ncf);
       }
     }
-    if (nd == 2 && p->flux == HRW_FLUX_GODUNOV) {
+    if (nd == 2 && p->flux == HRW_FLUX_GODUNOV && !p->xedges[0] && !p->xedges[1]) {
       // upwind when g > 0 at every interface in FP32: the kernels evaluate g(x_e) from the float
       // a, b, rx, xmin, which differs from this FP64 evaluation of the same floats by a few FP32
-      // roundings, far inside a 1e-5 margin
+      // roundings, far inside a 1e-5 margin (non-uniform grids take the general flux path)
       bool up = true;
       for (int d = 0; d < 2; ++d) {
         const LineF& F = d == 0 ? f.L : f.L2;

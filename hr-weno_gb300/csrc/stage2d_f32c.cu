@@ -18,6 +18,10 @@
 // block then builds its padded compensated tile from shared memory, replicating edge cells
 // into the ghosts (the box reads zeros outside the grid).  Otherwise every thread gathers the
 // tile from global memory.  Both loaders feed the same arithmetic, so both give the same bits.
+//
+// Non-uniform grids (a line with xedges) take the gathering loader and the general flux path,
+// each cell of such a line reconstructing with its own coefficients (recon_diff_nu).  Their
+// kernels are compiled as part 1 of this file (HRW_PART = 1), the uniform ones as part 0.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_runtime.h>
@@ -32,6 +36,9 @@
 #include "hrw_tma.cuh"
 
 namespace hrw {
+
+// part 1 (non-uniform grids)
+cudaError_t launch_stage2d_f32c_nu(const F32CArgs& a, int k, int stage, cudaStream_t s);
 
 namespace {
 
@@ -52,9 +59,21 @@ __device__ int g_tile_wait_limit = kTileWaitPolls;
 
 // WENO offsets of the C cells of a segment from its differences d[0 .. C+2K-2]; for k = 3 the
 // 13/12 (second difference)^2 terms are computed once per window position (as the 1D pass).
-// WL = false (upwind, k = 3): rr only.
-template <int K, bool WL = true>
-__device__ __forceinline__ void segment_recon(const float* d, float eps, float* rl, float* rr) {
+// WL = false (upwind, k = 3): rr only.  NU: on a non-uniform line (L.cnu) each cell j0 + c
+// takes its own coefficients (recon_diff_nu); a uniform line of the same grid the tables.
+template <int K, bool WL = true, bool NU = false>
+__device__ __forceinline__ void segment_recon(const float* d, float eps, float* rl, float* rr,
+                                              const LineF& L, int j0) {
+  if constexpr (NU) {
+    if (L.cnu) {
+#pragma unroll
+      for (int c = 0; c < C; ++c) {
+        const int j = j0 + c < L.nc ? j0 + c : L.nc - 1;
+        recon_diff_nu<K>(&d[c + 1], L.cnu + (int64_t)K * (K + 1) * j, eps, rl[c], rr[c]);
+      }
+      return;
+    }
+  }
   if constexpr (K == 3) {
     float t[C + 4];
 #pragma unroll
@@ -71,9 +90,18 @@ __device__ __forceinline__ void segment_recon(const float* d, float eps, float* 
   }
 }
 
-// one cell's offsets from its 2K-2 differences (tile-edge cells), the same arithmetic
-template <int K, bool WL = true>
-__device__ __forceinline__ void cell_recon(const float* de, float eps, float& el, float& er) {
+// one cell's offsets from its 2K-2 differences (tile-edge cells), the same arithmetic; NU:
+// cell j of a non-uniform line with its coefficients
+template <int K, bool WL = true, bool NU = false>
+__device__ __forceinline__ void cell_recon(const float* de, float eps, float& el, float& er,
+                                           const LineF& L, int j) {
+  if constexpr (NU) {
+    if (L.cnu) {
+      j = j < 0 ? 0 : (j >= L.nc ? L.nc - 1 : j);
+      recon_diff_nu<K>(de, L.cnu + (int64_t)K * (K + 1) * j, eps, el, er);
+      return;
+    }
+  }
   if constexpr (K == 3) {
     float te[3];
 #pragma unroll
@@ -92,10 +120,15 @@ __device__ __forceinline__ void cell_recon(const float* de, float eps, float& el
 // Lax-Friedrichs, 5 Godunov; the flux function is a uniform branch), with the same arithmetic;
 // UPW (upwind Godunov of g u, g > 0): the interior takes flux_diff_upwind, and the line's end
 // cells the general path with any right states (rl = 0), which the upwind flux ignores
-template <int FKI, bool UPW = false>
+// NU: the general path, g at the true edges of a non-uniform line
+template <int FKI, bool UPW = false, bool NU = false>
 __device__ __forceinline__ float seg_flux(const LineF& L, bool interior, int j, float v, float rr_m,
                                           float d_m, float rl_j, float rr_j, float d_j, float rl_p) {
-  if constexpr (UPW) {
+  if constexpr (NU) {
+    static_assert(FKI < 0 && !UPW, "non-uniform grids take the general flux path");
+    if (L.cnu) return flux_diff_f32c<true>(L, j, v, rr_m, d_m, rl_j, rr_j, d_j, rl_p);
+    return flux_diff_f32c(L, j, v, rr_m, d_m, rl_j, rr_j, d_j, rl_p);
+  } else if constexpr (UPW) {
     if (interior) return flux_diff_upwind(L, j, v, rr_m, d_m, rr_j);
     return flux_diff_f32c_call(L, j, v, rr_m, d_m, 0.f, rr_j, d_j, 0.f);
   } else if constexpr (FKI >= 0) {
@@ -106,10 +139,11 @@ __device__ __forceinline__ float seg_flux(const LineF& L, bool interior, int j, 
   }
 }
 
-template <int K, int ST, bool TMA, bool HAS_DV, int FKI, bool UPW = false>
+template <int K, int ST, bool TMA, bool HAS_DV, int FKI, bool UPW = false, bool NU = false>
 __global__ void __launch_bounds__(NT) stage2d_f32c_kernel(const __grid_constant__ TileMaps M,
                                                           F32CArgs a) {
   static_assert(!UPW || K == 3, "the upwind pass is written for k = 3");
+  static_assert(!NU || (!TMA && FKI < 0 && !UPW), "non-uniform grids: gathered tiles, general flux");
   constexpr int H = K;
   constexpr int RW = TX + 2 * H, SW = RW + 1, SQ = TX + 1;
   constexpr int NSX = TX / C, NSY = TY / C;
@@ -204,7 +238,7 @@ __global__ void __launch_bounds__(NT) stage2d_f32c_kernel(const __grid_constant_
 #pragma unroll
     for (int q = 0; q < C + 2 * K - 1; ++q)
       d[q] = (sh[base + q + 1] - sh[base + q]) + (sm[base + q + 1] - sm[base + q]);
-    segment_recon<K, !UPW>(d, a.eps, rl, rr);
+    segment_recon<K, !UPW, NU>(d, a.eps, rl, rr, L1, bx + sg * C);
     if constexpr (!UPW) sLx[r * (NSX + 1) + sg] = rl[0];
     sRx[r * (NSX + 1) + sg + 1] = rr[C - 1];
   }
@@ -227,7 +261,8 @@ __global__ void __launch_bounds__(NT) stage2d_f32c_kernel(const __grid_constant_
         de[q] = (sh[m1] - sh[m0]) + (sm[m1] - sm[m0]);
       }
       float el, er;
-      cell_recon<K, !UPW>(de, a.eps, el, er);
+      const int je = warp == 0 ? bx - 1 : warp == 1 ? bx + TX : warp == 2 ? by - 1 : by + TY;
+      cell_recon<K, !UPW, NU>(de, a.eps, el, er, warp < 2 ? L1 : L2, je);
       if (warp == 0) sRx[lane * (NSX + 1)] = er;
       else if (warp == 1) sLx[lane * (NSX + 1) + NSX] = el;
       else if (warp == 2) sRy[lane] = er;
@@ -251,7 +286,7 @@ __global__ void __launch_bounds__(NT) stage2d_f32c_kernel(const __grid_constant_
         const float rl_j = UPW ? 0.f : rl[c];
         const float rl_p = UPW ? 0.f : (c == C - 1 ? sLx[r * (NSX + 1) + sg + 1] : rl[c + 1]);
         const float dF =
-            seg_flux<FKI, UPW>(L1, interior, gx, v, rr_m, d[c + K - 1], rl_j, rr[c], d[c + K], rl_p);
+            seg_flux<FKI, UPW, NU>(L1, interior, gx, v, rr_m, d[c + K - 1], rl_j, rr[c], d[c + K], rl_p);
         t = -dF;
       }
       sq[r * SQ + sg * C + c] = t;
@@ -267,7 +302,7 @@ __global__ void __launch_bounds__(NT) stage2d_f32c_kernel(const __grid_constant_
       const int m0 = base + q * SW, m1 = m0 + SW;
       d[q] = (sh[m1] - sh[m0]) + (sm[m1] - sm[m0]);
     }
-    segment_recon<K, !UPW>(d, a.eps, rl, rr);
+    segment_recon<K, !UPW, NU>(d, a.eps, rl, rr, L2, by + sy * C);
     if constexpr (!UPW) sLy[sy * TX + col] = rl[0];
     sRy[(sy + 1) * TX + col] = rr[C - 1];
   }
@@ -297,7 +332,7 @@ __global__ void __launch_bounds__(NT) stage2d_f32c_kernel(const __grid_constant_
     const float rl_j = UPW ? 0.f : rl[c];
     const float rl_p = UPW ? 0.f : (c == C - 1 ? sLy[(sy + 1) * TX + col] : rl[c + 1]);
     const float dF2 =
-        seg_flux<FKI, UPW>(L2, interior, gy, v, rr_m, d[c + K - 1], rl_j, rr[c], d[c + K], rl_p);
+        seg_flux<FKI, UPW, NU>(L2, interior, gy, v, rr_m, d[c + K - 1], rl_j, rr[c], d[c + K], rl_p);
     const float q1 = L1.rw ? sq[ly * SQ + col] * L1.rw[gx] : sq[ly * SQ + col];
     const float q2 = L2.rw ? -dF2 * L2.rw[gy] : -dF2;
     // dt L = c1 q1 + c2 q2 with the dt/dx float pairs; L = q1/dx1 + q2/dx2
@@ -320,6 +355,7 @@ __global__ void __launch_bounds__(NT) stage2d_f32c_kernel(const __grid_constant_
   }
 }
 
+#if !defined(HRW_PART) || HRW_PART == 0
 template <int K, int ST, bool TMA, bool HAS_DV>
 cudaError_t launch_kt(const TileMaps& M, const F32CArgs& a, cudaStream_t s) {
   const dim3 grid((unsigned)((a.L.nc + TX - 1) / TX), (unsigned)((a.L2.nc + TY - 1) / TY));
@@ -373,8 +409,47 @@ cudaError_t launch_st(const F32CArgs& a, int stage, cudaStream_t s) {
   }
   return cudaErrorInvalidValue;
 }
+#endif  // part 0
+
+#if !defined(HRW_PART) || HRW_PART == 1
+// Non-uniform grids: gathered tiles (each thread loads its share of the tile from global
+// memory) and the general flux path; the per-cell coefficients of a non-uniform line come
+// with its LineF.
+template <int K, int ST, bool HAS_DV>
+cudaError_t launch_nu_kt(const F32CArgs& a, cudaStream_t s) {
+  const dim3 grid((unsigned)((a.L.nc + TX - 1) / TX), (unsigned)((a.L2.nc + TY - 1) / TY));
+  const TileMaps M{};
+  stage2d_f32c_kernel<K, ST, false, HAS_DV, -1, false, true><<<grid, NT, 0, s>>>(M, a);
+  return cudaGetLastError();
+}
+
+template <int K>
+cudaError_t launch_nu_k(const F32CArgs& a, int stage, cudaStream_t s) {
+  const bool dv = a.dv != nullptr;
+  switch (stage) {
+    case FC_RHS: return dv ? launch_nu_kt<K, FC_RHS, true>(a, s) : launch_nu_kt<K, FC_RHS, false>(a, s);
+    case FC_E1: return dv ? launch_nu_kt<K, FC_E1, true>(a, s) : launch_nu_kt<K, FC_E1, false>(a, s);
+    case FC_RK1: return dv ? launch_nu_kt<K, FC_RK1, true>(a, s) : launch_nu_kt<K, FC_RK1, false>(a, s);
+    case FC_RK2B: return dv ? launch_nu_kt<K, FC_RK2B, true>(a, s) : launch_nu_kt<K, FC_RK2B, false>(a, s);
+    case FC_RK3B: return dv ? launch_nu_kt<K, FC_RK3B, true>(a, s) : launch_nu_kt<K, FC_RK3B, false>(a, s);
+    case FC_RK3C: return dv ? launch_nu_kt<K, FC_RK3C, true>(a, s) : launch_nu_kt<K, FC_RK3C, false>(a, s);
+    case FC_MS: return dv ? cudaErrorInvalidValue : launch_nu_kt<K, FC_MS, false>(a, s);
+  }
+  return cudaErrorInvalidValue;
+}
+#endif  // part 1
 
 }  // namespace
+
+#if !defined(HRW_PART) || HRW_PART == 1
+cudaError_t launch_stage2d_f32c_nu(const F32CArgs& a, int k, int stage, cudaStream_t s) {
+  if (k == 1) return launch_nu_k<1>(a, stage, s);
+  if (k == 2) return launch_nu_k<2>(a, stage, s);
+  return launch_nu_k<3>(a, stage, s);
+}
+#endif
+
+#if !defined(HRW_PART) || HRW_PART == 0
 
 // ---- TMA descriptors: cuTensorMapEncodeTiled (CUDA driver API), cached by array ---------------
 namespace {
@@ -432,6 +507,7 @@ bool tile_map_2d(const void* p, int elem_bytes, int n1, int n2, int box_x, int b
 cudaError_t launch_stage2d_f32c(const F32CArgs& a, int k, int stage, cudaStream_t s) {
   if (a.L.nc <= 0 || a.L2.nc <= 0) return cudaSuccess;
   if (a.L2.nc > 65535LL * TY || !a.timeout_flag) return cudaErrorInvalidValue;
+  if (a.L.cnu || a.L2.cnu) return launch_stage2d_f32c_nu(a, k, stage, s);
   if (k == 1) return launch_st<1>(a, stage, s);
   if (k == 2) return launch_st<2>(a, stage, s);
   return launch_st<3>(a, stage, s);
@@ -441,5 +517,7 @@ cudaError_t stage2d_f32c_set_tile_wait_limit(int polls) {
   const int v = polls < 0 ? kTileWaitPolls : polls;
   return cudaMemcpyToSymbol(g_tile_wait_limit, &v, sizeof(v));
 }
+
+#endif  // part 0
 
 }  // namespace hrw

@@ -109,8 +109,8 @@ typedef struct hrw_problem {
   const double* rates;    /* LINEAR_ODE: host array(neq) of rates a_i */
   int32_t numerics;       /* HRW_NUMERICS_* */
   /* optional host array(nc+1) of cell edges of a non-uniform line, per dimension (FV1D and
-   * FV2D; HRW_F64 and HRW_F32 handles, HRW_F32C handles of FV1D problems, HRW_F64 batches
-   * and the adjoint, not the allocation-free steps): the WENO coefficients become cnu(xedges) as weno(ncells, k, eps,
+   * FV2D; HRW_F64, HRW_F32 and HRW_F32C handles, HRW_F64 batches and the adjoint, not the
+   * allocation-free steps): the WENO coefficients become cnu(xedges) as weno(ncells, k, eps,
    * xedges) builds them (src/hrweno_weno.f90:100-104,221-297), the widths edges(i) - edges(i-1)
    * and the flux's x the edges themselves; xmin/xmax are then unused and width[] must be NULL.
    * NULL: uniform grid. */

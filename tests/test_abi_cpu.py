@@ -114,15 +114,15 @@ def test_f32c_rejects_burgers_linear(hw):
         hw.rktvd(prob, 100, 3, dtype="f32c")
 
 
-def test_f32c_nonuniform_lines_fv1d_only(hw):
-    """Compensated FP32 handles take xedges on FV1D lines; a 2D problem with a non-uniform line
-    is refused before any CUDA call."""
+def test_f32c_batches_refuse_nonuniform_lines(hw):
+    """Compensated FP32 handles take xedges (FV1D and FV2D); compensated batches refuse them,
+    before any CUDA call."""
     from hrweno import HrwError
     nx = 16
     xe = np.linspace(0.0, 1.0, nx + 1) ** 2
-    prob = hw.Problem(kind="fv2d", ncells=(nx, nx), k=3, xedges=(xe, None))
-    with pytest.raises(HrwError, match="HRW_F32C takes non-uniform lines in FV1D"):
-        hw.rktvd(prob, nx * nx, 3, dtype="f32c")
+    probs = [hw.Problem(kind="fv1d", ncells=(nx, 1), k=3), hw.Problem(kind="fv1d", ncells=(nx, 1), k=3, xedges=(xe, None))]
+    with pytest.raises(HrwError, match="non-uniform lines are supported for HRW_F64.*problem 1"):
+        hw.batch(probs, dtype="f32c")
 
 
 def test_real32_validation_before_any_cuda_call(hw):

@@ -96,6 +96,43 @@ def test_rhs_f32c_nonuniform(hw, orc, k, nc, kind):
         assert np.max(np.abs(got - ref)) <= 2e-6 * scale, (c, np.max(np.abs(got - ref)) / scale)
 
 
+@pytest.mark.parametrize("shape", [(1, 1), (5, 7), (33, 31), (64, 40), (100, 37)])
+@pytest.mark.parametrize("k", [1, 2, 3])
+@pytest.mark.parametrize("which", ["x1", "x2", "both"])
+@pytest.mark.parametrize("name", ["pbe_upwind", "pbe_mixed", "pbe_lf"])
+def test_rhs_f32c_2d_nonuniform(hw, orc, shape, k, which, name):
+    """Non-uniform lines in 2D in the compensated form: the cells of a line with edges
+    reconstruct with their own coefficients, divide by their widths and see g at the true
+    edges; a uniform line of the same grid keeps the tables (the FP64 cases of
+    test_gpu_2d.py against the FP64 oracle, within the compensated form's bound)."""
+    import test_gpu_2d as T2
+    n1, n2 = shape
+    v = np.random.default_rng(n1 * 7 + n2 + k).uniform(0.0, 1.0, n1 * n2)
+    prob = T2.nonuniform_pbe(hw, n1, n2, k, name, which, "fast")
+    ref = orc.rhs(prob, v)
+    got = rhs_f32c(prob, v)
+    assert np.max(np.abs(got - ref)) <= 2e-6 * max(np.max(np.abs(ref)), 1e-30), \
+        np.max(np.abs(got - ref)) / np.max(np.abs(ref))
+
+
+@pytest.mark.parametrize("method", ["rktvd", "mstvd"])
+def test_f32c_2d_nonuniform_integrate(hw, orc, method):
+    import test_gpu_2d as T2
+    from hrweno import workloads
+    n1, n2 = 96, 80
+    _, n0, dt = workloads.pbe_config(n1, n2, cfl=0.25)
+    prob = T2.nonuniform_pbe(hw, n1, n2, 3, "pbe_upwind", "both", "fast")
+    if method == "rktvd":
+        g, o = hw.rktvd(prob, n1 * n2, 3, dtype="f32c"), orc.ODE(prob, n1 * n2, 0, 3)
+    else:
+        g, o = hw.mstvd(prob, n1 * n2, dtype="f32c"), orc.ODE(prob, n1 * n2, 1)
+    u32, u64 = n0.copy(), n0.copy()
+    t32 = g.integrate(u32, 0.0, 61.5 * dt, dt)
+    t64 = o.integrate(u64, 0.0, 61.5 * dt, dt)
+    assert t32 == t64 and g.nsteps == o.info()[2]
+    assert rel_l1(u32, u64) <= 1e-6, rel_l1(u32, u64)
+
+
 def jumpy(n, seed, amp=(3e3, 3e4)):
     """A state of plateaus with jumps of |amp[0]| .. |amp[1]|: the WENO indicators' squares
     then span 1e13 .. 1e20, across the bound between the weights' product and division forms."""
