@@ -28,13 +28,13 @@ __device__ __forceinline__ void split_scalar(double x, float& hi, float& lo) {
   lo = __double2float_rn(x - (double)hi);
 }
 
-template <int K, int G, int C, int FK>
+template <int K, int G, int C, int FK, bool NU>
 __device__ __forceinline__ void f32c_sweep(const F32CArgs& a, int lt, int gid, int stage) {
   const int lane = lt & 31;
   const int warp_in_group = lt >> 5;
   for (int64_t base = 0; base < a.L.nc; base += (int64_t)G * C) {
     const int64_t wbase = base + (int64_t)warp_in_group * 32 * C;
-    if (wbase < a.L.nc) f32c_pass<K, -1, C, FK>(a, wbase + (int64_t)lane * C, lane, stage);
+    if (wbase < a.L.nc) f32c_pass<K, -1, C, FK, NU>(a, wbase + (int64_t)lane * C, lane, stage);
   }
   group_sync<G>(gid);
 }
@@ -42,8 +42,9 @@ __device__ __forceinline__ void f32c_sweep(const F32CArgs& a, int lt, int gid, i
 // all steps of one problem in the increment form of the compensated kernels (stage1d_f32c.cu):
 // the state ping-pongs between slots 0 and 1 and ends in slot 0
 // FK: the problem's flux kind as flux_g_t takes it (4 or 5 here: the numerical flux fixed, the
-// flux function chosen at run time), or -1 (resolved per call)
-template <int K, int G, int C, int FK>
+// flux function chosen at run time), or -1 (resolved per call).  NU: a non-uniform line (its
+// per-cell coefficients, widths and edges in P.fcnu, P.frw, P.fgst, P.fxe; FK = -1)
+template <int K, int G, int C, int FK, bool NU = false>
 __device__ void run_problem_f32c(const BatchArgs& B, const BatchProblem& P, int lt, int gid,
                                  F32CArgs& a) {
   // a: this group's arguments in shared memory (registers stay free for the warp pass);
@@ -71,6 +72,14 @@ __device__ void run_problem_f32c(const BatchArgs& B, const BatchProblem& P, int 
     split_scalar(P.dt / P.rx, a.c_hi, a.c_lo);
     split_scalar(P.dt, a.dt_hi, a.dt_lo);
     a.lscale = (float)(1.0 / P.rx);
+    if constexpr (NU) {  // as a single non-uniform line: dt L = dt (-dF / width)
+      a.L.cnu = P.fcnu;
+      a.L.rw = P.frw;
+      a.L.gst = P.fgst;
+      a.L.xe = P.fxe;
+      split_scalar(P.dt, a.c_hi, a.c_lo);
+      a.lscale = 1.0f;
+    }
   }
   // the step's stages in order, each one sweep through the single call site below (one copy of
   // the pass serves them all): order 1: RK1; 2: E1, RK2B; 3: E1, RK3B, RK3C
@@ -86,7 +95,7 @@ __device__ void run_problem_f32c(const BatchArgs& B, const BatchProblem& P, int 
         a.out = k == 0 ? d1 : d2;  // (the last stage writes the state pair instead)
       }
       group_sync<G>(gid);
-      f32c_sweep<K, G, C, FK>(a, lt, gid, st);
+      f32c_sweep<K, G, C, FK, NU>(a, lt, gid, st);
     }
     slot = 1 - slot;
   }
@@ -96,7 +105,7 @@ __device__ void run_problem_f32c(const BatchArgs& B, const BatchProblem& P, int 
   }
 }
 
-template <int G, int C>
+template <int G, int C, bool NU = false>
 __global__ void __launch_bounds__(NT, C == 4 ? 3 : 2) batch_f32c_kernel(BatchArgs B) {
   static_assert(NT % G == 0 && G % 32 == 0 && NT / G <= 15, "groups of whole warps");
   constexpr int GPB = NT / G;
@@ -114,7 +123,11 @@ __global__ void __launch_bounds__(NT, C == 4 ? 3 : 2) batch_f32c_kernel(BatchArg
     // one copy of the pass per (k, numerical flux); Burgers or linear is a uniform branch
     const bool god = P.flux != HRW_FLUX_LAX_FRIEDRICHS;
     F32CArgs& a = s_args[gid];
-    if (P.k == 3) {
+    if constexpr (NU) {  // one copy of the general pass per k
+      if (P.k == 3) run_problem_f32c<3, G, C, -1, true>(B, P, lt, gid, a);
+      else if (P.k == 2) run_problem_f32c<2, G, C, -1, true>(B, P, lt, gid, a);
+      else run_problem_f32c<1, G, C, -1, true>(B, P, lt, gid, a);
+    } else if (P.k == 3) {
       if (!god) run_problem_f32c<3, G, C, 4>(B, P, lt, gid, a);
       else run_problem_f32c<3, G, C, 5>(B, P, lt, gid, a);
     } else if (P.k == 2) {
@@ -143,6 +156,18 @@ int batch_f32_blocks_per_sm(int shape) {
     case 1: return occupancy_f32<128, 4>();
     default: return occupancy_f32<256, 4>();
   }
+}
+
+int batch_f32c_nu_blocks_per_sm() {
+  int n = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_f32c_kernel<kBatchNuGroup, 4, true>, NT, 0);
+  return n;
+}
+
+cudaError_t launch_batch_f32c_nu(const BatchArgs& B, int blocks, cudaStream_t s) {
+  if (B.nprob <= 0) return cudaSuccess;
+  batch_f32c_kernel<kBatchNuGroup, 4, true><<<blocks, NT, 0, s>>>(B);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_batch_f32c(const BatchArgs& B, int shape, int blocks, cudaStream_t s) {

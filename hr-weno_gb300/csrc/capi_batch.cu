@@ -50,6 +50,7 @@ struct hrw_batch {
   double* ring = nullptr;     // mstvd: 5 packed states u^m and 4 packed L(u^m)
   bool nu = false;            // some problem has a non-uniform line (xedges)
   double* nu_mem = nullptr;   // their edges, widths, FAST scales and weno coefficients
+  float* nu_fmem = nullptr;   // HRW_F32C: the same lines in FP32 (coefficients, 1/width, b width, edges)
   std::vector<char> started;  // mstvd: the problem's RK3 start has run
   std::vector<int64_t> level; // mstvd: m of the problem's current state
   bool strict = false;
@@ -136,14 +137,15 @@ int launch_all(hrw_batch* b, double* u, const int* shapes) {
         A.fd2 = q;
       }
       const bool nu = c == kClasses;
-      const int per_sm = std::max(1, nu    ? batch_nu_blocks_per_sm(b->strict)
+      const int per_sm = std::max(1, nu    ? (f32 ? batch_f32c_nu_blocks_per_sm() : batch_nu_blocks_per_sm(b->strict))
                                      : f32 ? batch_f32_blocks_per_sm(shapes[c])
                                            : batch_blocks_per_sm(shapes[c], b->strict));
       const int group = nu ? kBatchNuGroup : f32 ? kBatchShapesF32[shapes[c]].group : kBatchShapes[shapes[c]].group;
       const int groups_per_block = 256 / group;
       int blocks = per_sm * b->sms;
       blocks = std::min<int64_t>(blocks, (n + groups_per_block - 1) / groups_per_block);
-      if (nu) HRW_BCUDA(launch_batch_nu(A, b->strict, std::max(blocks, 1), b->side[c]));
+      if (nu && f32) HRW_BCUDA(launch_batch_f32c_nu(A, std::max(blocks, 1), b->side[c]));
+      else if (nu) HRW_BCUDA(launch_batch_nu(A, b->strict, std::max(blocks, 1), b->side[c]));
       else if (f32) HRW_BCUDA(launch_batch_f32c(A, shapes[c], std::max(blocks, 1), b->side[c]));
       else HRW_BCUDA(launch_batch(A, shapes[c], b->strict, std::max(blocks, 1), b->side[c]));
     }
@@ -229,7 +231,6 @@ static int batch_create(const hrw_problem* probs, int nprob, int order, int dtyp
     if (p.ncells[0] <= 0) return bad("Invalid input 'ncells'. Valid range: ncells > 0.");
     if (p.width[0]) return bad("Invalid input 'width': batches take non-uniform lines as xedges.");
     if (p.xedges[0]) {
-      if (dtype != HRW_F64) return bad("Invalid input 'xedges': non-uniform lines are supported for HRW_F64.");
       for (int q = 0; q < p.ncells[0]; ++q)
         if (!(p.xedges[0][q + 1] > p.xedges[0][q])) return bad("Invalid input 'xedges': edges must increase.");
     }
@@ -330,6 +331,39 @@ static int batch_create(const hrw_problem* probs, int nprob, int order, int dtyp
       q += host.size() + (size_t)p.k * (p.k + 1) * nc;
     }
     if ((e = cudaStreamSynchronize(b->own)) != cudaSuccess) return cleanup(e);
+    if (dtype == HRW_F32C) {
+      // the compensated pass's copy of each line, as a single-line handle builds it: the FP64
+      // coefficients rounded once, 1/width and b width from the FP64 widths, the edges rounded
+      size_t nf = 0;
+      for (int i = 0; i < nprob; ++i)
+        if (probs[i].xedges[0]) nf += (size_t)(probs[i].ncells[0] + 64) / 64 * 64 * (3 + (size_t)probs[i].k * (probs[i].k + 1));
+      if ((e = cudaMalloc(&b->nu_fmem, sizeof(float) * nf)) != cudaSuccess) return cleanup(e);
+      float* f = b->nu_fmem;
+      for (int i = 0; i < nprob; ++i) {
+        const hrw_problem& p = probs[i];
+        if (!p.xedges[0]) continue;
+        BatchProblem& bp = b->probs[i];
+        const size_t nc = (size_t)p.ncells[0], ncf = (size_t)p.k * (p.k + 1), seg = (nc + 64) / 64 * 64;
+        std::vector<double> c64(nc * ncf);
+        if ((e = cudaMemcpy(c64.data(), bp.cnu, sizeof(double) * c64.size(), cudaMemcpyDeviceToHost)) != cudaSuccess)
+          return cleanup(e);
+        std::vector<float> host(seg * (3 + ncf), 0.f);
+        for (size_t j = 0; j < nc; ++j) {
+          const double w = p.xedges[0][j + 1] - p.xedges[0][j];
+          host[j] = (float)(1.0 / w);
+          host[2 * seg + j] = (float)(p.coef_b[0] * w);
+        }
+        for (size_t j = 0; j <= nc; ++j) host[seg + j] = (float)p.xedges[0][j];
+        for (size_t j = 0; j < c64.size(); ++j) host[3 * seg + j] = (float)c64[j];
+        if ((e = cudaMemcpy(f, host.data(), sizeof(float) * host.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
+          return cleanup(e);
+        bp.frw = f;
+        bp.fxe = f + seg;
+        bp.fgst = f + 2 * seg;
+        bp.fcnu = f + 3 * seg;
+        f += host.size();
+      }
+    }
   }
   *out = b;
   return HRW_OK;
@@ -562,6 +596,7 @@ int hrw_batch_destroy(hrw_batch* b) {
   if (b->fmem) cudaFree(b->fmem);
   if (b->ring) cudaFree(b->ring);
   if (b->nu_mem) cudaFree(b->nu_mem);
+  if (b->nu_fmem) cudaFree(b->nu_fmem);
   for (int c = 0; c <= kClasses; ++c) {
     if (b->side[c]) cudaStreamDestroy(b->side[c]);
     if (b->join[c]) cudaEventDestroy(b->join[c]);

@@ -24,6 +24,12 @@ struct BatchProblem {
   const double* width;
   const double* rws;
   const double* xe;
+  // the same line for compensated FP32 batches: cnu rounded to FP32, 1/width and b width from
+  // the FP64 widths, the edges in FP32 (LineF's cnu, rw, gst, xe)
+  const float* fcnu;
+  const float* frw;
+  const float* fgst;
+  const float* fxe;
 };
 
 struct BatchArgs {
@@ -66,5 +72,8 @@ constexpr int kNumBatchShapesF32 = 3;
 extern const BatchShape kBatchShapesF32[kNumBatchShapesF32];
 int batch_f32_blocks_per_sm(int shape);
 cudaError_t launch_batch_f32c(const BatchArgs& B, int shape, int blocks, cudaStream_t s);
+// their non-uniform lines: one launch of 128-thread groups, 4 cells per thread
+int batch_f32c_nu_blocks_per_sm();
+cudaError_t launch_batch_f32c_nu(const BatchArgs& B, int blocks, cudaStream_t s);
 
 }  // namespace hrw

@@ -109,7 +109,7 @@ typedef struct hrw_problem {
   const double* rates;    /* LINEAR_ODE: host array(neq) of rates a_i */
   int32_t numerics;       /* HRW_NUMERICS_* */
   /* optional host array(nc+1) of cell edges of a non-uniform line, per dimension (FV1D and
-   * FV2D; HRW_F64, HRW_F32 and HRW_F32C handles, HRW_F64 batches and the adjoint, not the
+   * FV2D; HRW_F64, HRW_F32 and HRW_F32C handles, batches and the adjoint, not the
    * allocation-free steps): the WENO coefficients become cnu(xedges) as weno(ncells, k, eps,
    * xedges) builds them (src/hrweno_weno.f90:100-104,221-297), the widths edges(i) - edges(i-1)
    * and the flux's x the edges themselves; xmin/xmax are then unused and width[] must be NULL.
@@ -183,7 +183,7 @@ int hrw_ode_destroy(hrw_ode* ode);
 int hrw_rhs(const hrw_problem* p, int dtype, double t, const void* v, void* vdot, void* stream);
 
 /* ---- batches of independent 1D problems ------------------------------------------- */
-/* A batch holds nprob independent FV1D problems on uniform or (HRW_F64) non-uniform grids
+/* A batch holds nprob independent FV1D problems on uniform or non-uniform grids
  * given as xedges (each its own rktvd(fu,
  * neq, order) of the reference, src/hrweno_tvdode.f90:69-178, with its own ncells, k, flux,
  * flux function, alpha and boundaries; all share `order`, the dtype (HRW_F64, or HRW_F32C:

@@ -114,15 +114,17 @@ def test_f32c_rejects_burgers_linear(hw):
         hw.rktvd(prob, 100, 3, dtype="f32c")
 
 
-def test_f32c_batches_refuse_nonuniform_lines(hw):
-    """Compensated FP32 handles take xedges (FV1D and FV2D); compensated batches refuse them,
-    before any CUDA call."""
+def test_batch_edges_are_checked(hw):
+    """A batch's non-uniform lines (FP64 or compensated FP32) need increasing edges; the check
+    names the problem and runs before any CUDA call."""
     from hrweno import HrwError
     nx = 16
     xe = np.linspace(0.0, 1.0, nx + 1) ** 2
+    xe[5] = xe[4]
     probs = [hw.Problem(kind="fv1d", ncells=(nx, 1), k=3), hw.Problem(kind="fv1d", ncells=(nx, 1), k=3, xedges=(xe, None))]
-    with pytest.raises(HrwError, match="non-uniform lines are supported for HRW_F64.*problem 1"):
-        hw.batch(probs, dtype="f32c")
+    for dtype in ("f64", "f32c"):
+        with pytest.raises(HrwError, match="edges must increase.*problem 1"):
+            hw.batch(probs, dtype=dtype)
 
 
 def test_real32_validation_before_any_cuda_call(hw):

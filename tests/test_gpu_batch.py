@@ -110,9 +110,6 @@ def test_batch_validation(hw):
     ok = hw.burgers_1d(10)
     with pytest.raises(HrwError, match="non-uniform lines as xedges"):
         hw.batch([ok, hw.burgers_1d(10, width=np.full(10, 0.1))])
-    nu = hw.Problem(ncells=(10, 1), xedges=(np.linspace(0.0, 1.0, 11) ** 2, None))
-    with pytest.raises(HrwError, match="supported for HRW_F64"):
-        hw.batch([ok, nu], dtype="f32c")
     with pytest.raises(HrwError, match="one numerics mode"):
         hw.batch([ok, hw.burgers_1d(10, numerics="strict")])
     with pytest.raises(HrwError, match="FV1D"):
@@ -273,3 +270,29 @@ def test_nonuniform_batch_matches_single_solves(hw, orc, method, numerics):
             if numerics == "strict":
                 to[i] = orcs[i].integrate(uo[i], to[i], tout, dts[i])
                 assert to[i] == t[i] and np.array_equal(got[i], uo[i]), (i, tout)
+
+
+@pytest.mark.parametrize("order", [1, 2, 3])
+def test_nonuniform_batch_f32c_matches_single_solves(hw, orc, order):
+    """Compensated FP32 batches with non-uniform lines: every problem bit-identical to its own
+    compensated single-problem handle (the same warp pass with per-cell coefficients), over two
+    calls, and within the compensated form's bound of the FP64 oracle."""
+    import torch
+    probs, lines, dts = nonuniform_mix(hw, 18, "fast", 12)
+    b = hw.batch(probs, order=order, dtype="f32c")
+    u = torch.from_numpy(b.pack(lines)).cuda()
+    t = np.zeros(len(probs))
+    singles = [hw.rktvd(p, int(p.ncells[0]), order, dtype="f32c") for p in probs]
+    us = [torch.from_numpy(v.copy()).cuda() for v in lines]
+    ts = [0.0] * len(probs)
+    for tout in (0.02, 0.06):
+        b.integrate(u, t, tout, dts)
+        got = b.unpack(u)
+        for i in range(len(probs)):
+            ts[i] = singles[i].integrate(us[i], ts[i], tout, dts[i])
+            assert t[i] == ts[i]
+            assert np.array_equal(got[i], us[i].cpu().numpy()), (i, tout)
+    for i, p in enumerate(probs):
+        uo = lines[i].copy()
+        orc.ODE(p, int(p.ncells[0]), 0, order).integrate(uo, 0.0, 0.06, dts[i])
+        assert np.sum(np.abs(got[i] - uo)) <= 1e-6 * np.sum(np.abs(uo)), i
