@@ -44,18 +44,10 @@ __device__ __forceinline__ void f32c_sweep(const F32CArgs& a, int lt, int gid, i
 // FK: the problem's flux kind as flux_g_t takes it (4 or 5 here: the numerical flux fixed, the
 // flux function chosen at run time), or -1 (resolved per call).  NU: a non-uniform line (its
 // per-cell coefficients, widths and edges in P.fcnu, P.frw, P.fgst, P.fxe; FK = -1)
-template <int K, int G, int C, int FK, bool NU = false>
-__device__ void run_problem_f32c(const BatchArgs& B, const BatchProblem& P, int lt, int gid,
-                                 F32CArgs& a) {
-  // a: this group's arguments in shared memory (registers stay free for the warp pass);
-  // thread 0 of the group writes them between sweeps, each sweep ends with a group barrier
-  float* const h0 = B.fhi[0] + P.off;
-  float* const h1 = B.fhi[1] + P.off;
-  float* const l0 = B.flo[0] + P.off;
-  float* const l1 = B.flo[1] + P.off;
-  float* const d1 = B.fd1 + P.off;
-  float* const d2 = B.fd2 + P.off;
-  if (lt == 0) {
+// the problem's line and time-step constants, as a single-line handle sets them up
+template <bool NU>
+__device__ __forceinline__ void problem_args(const BatchProblem& P, F32CArgs& a) {
+  {
     a = F32CArgs{};
     a.eps = (float)P.eps;
     a.L.nc = P.nc;
@@ -81,6 +73,20 @@ __device__ void run_problem_f32c(const BatchArgs& B, const BatchProblem& P, int 
       a.lscale = 1.0f;
     }
   }
+}
+
+template <int K, int G, int C, int FK, bool NU = false>
+__device__ void run_problem_f32c(const BatchArgs& B, const BatchProblem& P, int lt, int gid,
+                                 F32CArgs& a) {
+  // a: this group's arguments in shared memory (registers stay free for the warp pass);
+  // thread 0 of the group writes them between sweeps, each sweep ends with a group barrier
+  float* const h0 = B.fhi[0] + P.off;
+  float* const h1 = B.fhi[1] + P.off;
+  float* const l0 = B.flo[0] + P.off;
+  float* const l1 = B.flo[1] + P.off;
+  float* const d1 = B.fd1 + P.off;
+  float* const d2 = B.fd2 + P.off;
+  if (lt == 0) problem_args<NU>(P, a);
   // the step's stages in order, each one sweep through the single call site below (one copy of
   // the pass serves them all): order 1: RK1; 2: E1, RK2B; 3: E1, RK3B, RK3C
   const int nst = B.order < 1 ? 1 : (B.order > 3 ? 3 : B.order);
@@ -105,6 +111,67 @@ __device__ void run_problem_f32c(const BatchArgs& B, const BatchProblem& P, int 
   }
 }
 
+// mstvd (src/hrweno_tvdode.f90:203-271) of one problem, as a single-line compensated mstvd
+// handle runs it: the packed FP64 state split into the ring slot of the current level (slot 0
+// on the first call, which then takes the four RK3 start steps, each after a right-hand side
+// into the L ring), the multistep steps from slot to slot, and the final slot merged back into
+// the packed state.  Ring slots u^m (hi, lo) in fring_h/fring_lo[m % 5], L(u^m) in
+// fring_L[m % 4]; the start's stage increments in fd1, fd2.
+template <int K, int G, int C, int FK, bool NU = false>
+__device__ void run_problem_f32c_ms(const BatchArgs& B, const BatchProblem& P, int lt, int gid,
+                                    F32CArgs& a) {
+  float* H[5];
+  float* Lo[5];
+  float* Lr[4];
+#pragma unroll
+  for (int q = 0; q < 5; ++q) H[q] = B.fring_h[q] + P.off, Lo[q] = B.fring_lo[q] + P.off;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) Lr[q] = B.fring_L[q] + P.off;
+  float* const d1 = B.fd1 + P.off;
+  float* const d2 = B.fd2 + P.off;
+  double* const u = B.u + P.off;
+  if (lt == 0) problem_args<NU>(P, a);
+  int64_t level = P.start ? 0 : P.level;
+  int cur = (int)(level % 5);
+  for (int64_t j = lt; j < P.nc; j += G) {
+    const double x = u[j];
+    const float h = __double2float_rn(x);
+    H[cur][j] = h;
+    Lo[cur][j] = __double2float_rn(x - (double)h);
+  }
+  group_sync<G>(gid);
+  if (P.start) {  // the RK3 start (:236-249): L(u^m) into the ring, then an RK3 step to u^{m+1}
+    for (int m = 0; m < 4; ++m) {
+      for (int k = 0; k < 4; ++k) {
+        const int st = k == 0 ? FC_RHS : k == 1 ? FC_E1 : k == 2 ? FC_RK3B : FC_RK3C;
+        if (lt == 0) {
+          a.hi = H[m], a.lo = Lo[m];
+          a.dv = k < 2 ? nullptr : (k == 2 ? d1 : d2);
+          a.out = k == 0 ? Lr[m] : (k == 1 ? d1 : d2);
+          a.hi_out = H[m + 1], a.lo_out = Lo[m + 1];
+        }
+        group_sync<G>(gid);
+        f32c_sweep<K, G, C, FK, NU>(a, lt, gid, st);
+      }
+    }
+    level = 4;
+  }
+  for (int64_t n = 0; n < P.nsteps; ++n, ++level) {  // (:252-268)
+    const int c0 = (int)(level % 5), c1 = (int)((level + 1) % 5);  // c1 holds u^{m-4}
+    float* const lm = Lr[level % 4];                                  // holds L(u^{m-4})
+    if (lt == 0) {
+      a.hi = H[c0], a.lo = Lo[c0], a.dv = nullptr;
+      a.hi_out = H[c1], a.lo_out = Lo[c1];
+      a.hi4 = H[c1], a.lo4 = Lo[c1], a.l4 = lm, a.lout = lm;
+    }
+    group_sync<G>(gid);
+    f32c_sweep<K, G, C, FK, NU>(a, lt, gid, FC_MS);
+  }
+  cur = (int)(level % 5);
+  for (int64_t j = lt; j < P.nc; j += G) u[j] = (double)H[cur][j] + (double)Lo[cur][j];
+  group_sync<G>(gid);
+}
+
 template <int G, int C, bool NU = false>
 __global__ void __launch_bounds__(NT, C == 4 ? 3 : 2) batch_f32c_kernel(BatchArgs B) {
   static_assert(NT % G == 0 && G % 32 == 0 && NT / G <= 15, "groups of whole warps");
@@ -119,23 +186,31 @@ __global__ void __launch_bounds__(NT, C == 4 ? 3 : 2) batch_f32c_kernel(BatchArg
     group_sync<G>(gid);
     if (pid >= B.nprob) break;
     const BatchProblem P = B.probs[B.order_idx[pid]];
-    if (P.nsteps <= 0) continue;
-    // one copy of the pass per (k, numerical flux); Burgers or linear is a uniform branch
+    if (P.nsteps <= 0 && !(B.method == 1 && P.start)) continue;
+    // one copy of the pass per (k, numerical flux); Burgers or linear is a uniform branch, and
+    // so is rktvd or mstvd
     const bool god = P.flux != HRW_FLUX_LAX_FRIEDRICHS;
+    const bool ms = B.method == 1;
     F32CArgs& a = s_args[gid];
+#define HRW_RUN(K_, FK_, NU_)                                              \
+  do {                                                                     \
+    if (ms) run_problem_f32c_ms<K_, G, C, FK_, NU_>(B, P, lt, gid, a);     \
+    else run_problem_f32c<K_, G, C, FK_, NU_>(B, P, lt, gid, a);           \
+  } while (0)
     if constexpr (NU) {  // one copy of the general pass per k
-      if (P.k == 3) run_problem_f32c<3, G, C, -1, true>(B, P, lt, gid, a);
-      else if (P.k == 2) run_problem_f32c<2, G, C, -1, true>(B, P, lt, gid, a);
-      else run_problem_f32c<1, G, C, -1, true>(B, P, lt, gid, a);
+      if (P.k == 3) HRW_RUN(3, -1, true);
+      else if (P.k == 2) HRW_RUN(2, -1, true);
+      else HRW_RUN(1, -1, true);
     } else if (P.k == 3) {
-      if (!god) run_problem_f32c<3, G, C, 4>(B, P, lt, gid, a);
-      else run_problem_f32c<3, G, C, 5>(B, P, lt, gid, a);
+      if (!god) HRW_RUN(3, 4, false);
+      else HRW_RUN(3, 5, false);
     } else if (P.k == 2) {
-      if (!god) run_problem_f32c<2, G, C, 4>(B, P, lt, gid, a);
-      else run_problem_f32c<2, G, C, 5>(B, P, lt, gid, a);
+      if (!god) HRW_RUN(2, 4, false);
+      else HRW_RUN(2, 5, false);
     } else {
-      run_problem_f32c<1, G, C, -1>(B, P, lt, gid, a);
+      HRW_RUN(1, -1, false);
     }
+#undef HRW_RUN
   }
 }
 

@@ -134,7 +134,12 @@ int launch_all(hrw_batch* b, double* u, const int* shapes) {
           A.flo[k] = q, q += b->total;
         }
         A.fd1 = q, q += b->total;
-        A.fd2 = q;
+        A.fd2 = q, q += b->total;
+        if (b->method == 1) {
+          for (int k = 0; k < 5; ++k) A.fring_h[k] = q, q += b->total;
+          for (int k = 0; k < 5; ++k) A.fring_lo[k] = q, q += b->total;
+          for (int k = 0; k < 4; ++k) A.fring_L[k] = q, q += b->total;
+        }
       }
       const bool nu = c == kClasses;
       const int per_sm = std::max(1, nu    ? (f32 ? batch_f32c_nu_blocks_per_sm() : batch_nu_blocks_per_sm(b->strict))
@@ -158,7 +163,9 @@ int launch_all(hrw_batch* b, double* u, const int* shapes) {
 // launch_all on the packed FP64 state du; compensated FP32 batches split it into their
 // (hi, lo) slot 0 first and merge the result back
 int run_all(hrw_batch* b, double* du) {
-  if (b->dtype == HRW_F32C) {
+  // (compensated mstvd: each problem splits its lines into its ring slot and merges them back
+  // in the kernel)
+  if (b->dtype == HRW_F32C && b->method == 0) {
     float* hi = b->fmem;
     float* lo = b->fmem + b->total;
     HRW_BCUDA(launch_split_f64(du, hi, lo, b->total, b->main));
@@ -208,8 +215,6 @@ static int batch_create(const hrw_problem* probs, int nprob, int order, int dtyp
     return batch_fail(HRW_EINVAL, "Invalid input 'order' in 'rktvd'. Valid range: 1 <= k <= 3.");
   if (dtype != HRW_F64 && dtype != HRW_F32C)
     return batch_fail(HRW_EINVAL, "Invalid input 'dtype': batches support HRW_F64 and HRW_F32C.");
-  if (method == 1 && dtype != HRW_F64)
-    return batch_fail(HRW_EINVAL, "Invalid input 'dtype': mstvd batches support HRW_F64.");
   hrw_batch* b = new hrw_batch;
   b->nprob = nprob;
   b->order = order;
@@ -293,7 +298,9 @@ static int batch_create(const hrw_problem* probs, int nprob, int order, int dtyp
   if ((e = cudaMalloc(&b->d_counter, sizeof(int) * (kClasses + 1))) != cudaSuccess) return cleanup(e);
   if ((e = cudaMalloc(&b->u, bytes)) != cudaSuccess) return cleanup(e);
   if (dtype == HRW_F32C) {
-    if ((e = cudaMalloc(&b->fmem, sizeof(float) * (size_t)off * 6)) != cudaSuccess) return cleanup(e);
+    // slots (hi, lo) x 2, d1, d2; mstvd adds the ring: u^m (hi, lo) x 5 and L(u^m) x 4
+    const size_t per_cell = method == 1 ? 6 + 14 : 6;
+    if ((e = cudaMalloc(&b->fmem, sizeof(float) * (size_t)off * per_cell)) != cudaSuccess) return cleanup(e);
   } else {
     if ((e = cudaMalloc(&b->u1, bytes)) != cudaSuccess) return cleanup(e);
     if ((e = cudaMalloc(&b->u2, bytes)) != cudaSuccess) return cleanup(e);

@@ -45,11 +45,15 @@ struct BatchArgs {
   int method;
   double* ring_u[5];
   double* ring_l[4];
-  // compensated FP32 batches: state slots (hi, lo) x 2 and the stage increments, packed
+  // compensated FP32 batches: state slots (hi, lo) x 2 and the stage increments, packed;
+  // mstvd: the ring of u^m (hi, lo) [m % 5] and L(u^m) [m % 4] instead of the two slots
   float* fhi[2];
   float* flo[2];
   float* fd1;
   float* fd2;
+  float* fring_h[5];
+  float* fring_lo[5];
+  float* fring_L[4];
 };
 
 struct BatchShape {

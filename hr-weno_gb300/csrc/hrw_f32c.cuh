@@ -296,8 +296,12 @@ __device__ __forceinline__ float flux_diff_f32c(const LineF& L, int64_t j, float
   const float gR = lin ? (NU ? fmaf(L.b, L.xe[j + 1], L.a) : g_at(L, j + 1)) : 0.f;
   // G_R - G_L, with the base f(v) (Burgers) or g v (linear) of both interfaces removed; the
   // linear flux adds back (g_R - g_L) v = b rx v (b width_j v on a non-uniform line)
-  float GL = flux_g(L, v, rr_m - d_m, rl_j, gL);
-  float GR = flux_g(L, v, rr_j, d_j + rl_p, gR);
+  // every operation between the offsets and G_R - G_L rounded as written (intrinsics): a
+  // compiler that contracted one into a neighbouring product would round differently where
+  // that product underflows, and the single-line, batched and 2D copies of this arithmetic
+  // (inlined into different code) would then disagree
+  float GL = flux_g(L, v, __fsub_rn(rr_m, d_m), rl_j, gL);
+  float GR = flux_g(L, v, rr_j, __fadd_rn(d_j, rl_p), gR);
   float extra = lin ? (NU ? L.gst[j] : L.gstep) * v : 0.f;
   if (j == 0 || j == L.nc - 1) {
     // boundary fluxes in full (no cancellation there): F = fbase + G, each operation rounded
@@ -312,7 +316,7 @@ __device__ __forceinline__ float flux_diff_f32c(const LineF& L, int64_t j, float
     if (j == L.nc - 1) FR = L.bc == HRW_BC_ZERO ? 0.f : __fadd_rn(fbR, phys_g(L, v, rr_j, gR));
     return __fsub_rn(FR, FL);
   }
-  return __fadd_rn(GR - GL, extra);  // never contracted with gstep * v: one rounding order
+  return __fadd_rn(__fsub_rn(GR, GL), extra);  // never contracted with gstep * v
 }
 
 // flux_diff_f32c out of line: the warp pass's path for the few threads whose cells touch a
@@ -333,10 +337,10 @@ __device__ __forceinline__ float flux_diff_interior(const LineF& L, int j, float
   const bool lin = FK >= 4 ? L.fn != HRW_FN_BURGERS : FK >= 2;
   const float gL = lin ? g_at(L, j) : 0.f;
   const float gR = lin ? g_at(L, j + 1) : 0.f;
-  const float GL = flux_g_t<FK>(L, v, rr_m - d_m, rl_j, gL);
-  const float GR = flux_g_t<FK>(L, v, rr_j, d_j + rl_p, gR);
+  const float GL = flux_g_t<FK>(L, v, __fsub_rn(rr_m, d_m), rl_j, gL);
+  const float GR = flux_g_t<FK>(L, v, rr_j, __fadd_rn(d_j, rl_p), gR);
   const float extra = lin ? L.gstep * v : 0.f;
-  return __fadd_rn(GR - GL, extra);
+  return __fadd_rn(__fsub_rn(GR, GL), extra);
 }
 
 // flux_diff_f32c of an interior cell when the flux is Godunov's of f = g(x) u with g > 0 at
@@ -346,9 +350,9 @@ __device__ __forceinline__ float flux_diff_interior(const LineF& L, int j, float
 // (no contraction of G_R - G_L into a multiply-add), as there the min/max stands between them.
 __device__ __forceinline__ float flux_diff_upwind(const LineF& L, int j, float v, float rr_m,
                                                   float d_m, float rr_j) {
-  const float GL = __fmul_rn(g_at(L, j), rr_m - d_m);
+  const float GL = __fmul_rn(g_at(L, j), __fsub_rn(rr_m, d_m));
   const float GR = __fmul_rn(g_at(L, j + 1), rr_j);
-  return __fadd_rn(GR - GL, L.gstep * v);
+  return __fadd_rn(__fsub_rn(GR, GL), L.gstep * v);
 }
 
 // Stage update of one cell in increment form.  h, l: the state u = h + l; dv: the stored
@@ -575,7 +579,8 @@ __device__ __forceinline__ void f32c_pass(const F32CArgs& a, int64_t j0l, int la
       }
     } else {
       float r;  // the same expressions as the fixed-stage branches above
-      if (st == FC_E1 || st == FC_RK1) r = dtL;
+      if (st == FC_RHS) r = lq[c];
+      else if (st == FC_E1 || st == FC_RK1 || st == FC_MS) r = dtL;  // FC_MS: completed below
       else if (st == FC_RK3B) r = 0.25f * (dv[c] + dtL);
       else if (st == FC_RK2B) r = 0.5f * (dv[c] + dtL);
       else r = (2.f / 3.f) * (dv[c] + dtL);  // FC_RK3C
@@ -591,7 +596,7 @@ __device__ __forceinline__ void f32c_pass(const F32CArgs& a, int64_t j0l, int la
   if (to_out) {
     store_cells<C>(a.out, j0, nc, o1);
   } else {
-    if constexpr (ST == FC_MS) {  // u' = u + (7 (u4 - u) + 50 dt L + 10 dt L4) / 32
+    if (ST == FC_MS || (ST < 0 && st == FC_MS)) {  // u' = u + (7 (u4 - u) + 50 dt L + 10 dt L4) / 32
       float h4[C], l4[C], L4[C];
       load_cells<C>(a.hi4, j0, nc, h4);
       load_cells<C>(a.lo4, j0, nc, l4);

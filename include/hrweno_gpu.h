@@ -193,7 +193,8 @@ int hrw_rhs(const hrw_problem* p, int dtype, double t, const void* v, void* vdot
  * persistent launch per size class, the classes running concurrently. */
 typedef struct hrw_batch hrw_batch;
 int hrw_batch_create(const hrw_problem* problems, int nprob, int order, int dtype, hrw_batch** out);
-/* A batch of mstvd(fu_i, neq_i) solves (src/hrweno_tvdode.f90:180-271), HRW_F64: each problem keeps
+/* A batch of mstvd(fu_i, neq_i) solves (src/hrweno_tvdode.f90:180-271), HRW_F64 or HRW_F32C (the
+ * compensated form of a single mstvd handle, its history in float pairs): each problem keeps
  * its 5-step history between calls and runs the RK3 start (4 steps; the 4 extra rhs calls of the
  * reference) on its first call that takes a step.  hrw_batch_integrate follows mstvd_integrate
  * (itask is ignored, as the reference's mstvd has none); hrw_batch_advance runs the start on a

@@ -296,3 +296,37 @@ def test_nonuniform_batch_f32c_matches_single_solves(hw, orc, order):
         uo = lines[i].copy()
         orc.ODE(p, int(p.ncells[0]), 0, order).integrate(uo, 0.0, 0.06, dts[i])
         assert np.sum(np.abs(got[i] - uo)) <= 1e-6 * np.sum(np.abs(uo)), i
+
+
+@pytest.mark.parametrize("mix", ["uniform", "nonuniform"])
+def test_mstvd_batch_f32c_matches_single_solves(hw, mix):
+    """Compensated FP32 mstvd batches: every problem bit-identical to its own compensated mstvd
+    handle over several integrate calls (the float-pair history carries across calls; problem 5
+    starts on the second call), uniform and non-uniform lines, and the autotuner between calls
+    leaves the histories as they are."""
+    import torch
+    from hrweno import workloads
+    if mix == "uniform":
+        probs, lines, dts = workloads.batched_config(24, seed=3, nmin=40, nmax=3000, cfl=0.2)
+        touts = (0.05, 0.2, 1.5)
+    else:
+        probs, lines, dts = nonuniform_mix(hw, 18, "fast", 13)
+        touts = (0.005, 0.01, 0.03)
+    b = hw.batch(probs, dtype="f32c", method="mstvd")
+    u = torch.from_numpy(b.pack(lines)).cuda()
+    t = np.zeros(len(probs))
+    t[5] = 1.0 if mix == "uniform" else 0.008
+    singles = [hw.mstvd(p, int(p.ncells[0]), dtype="f32c") for p in probs]
+    us = [torch.from_numpy(v.copy()).cuda() for v in lines]
+    ts = [float(x) for x in t]
+    for n, tout in enumerate(touts):
+        b.integrate(u, t, tout, dts)
+        got = b.unpack(u)
+        for i in range(len(probs)):
+            ts[i] = singles[i].integrate(us[i], ts[i], tout, dts[i])
+            assert t[i] == ts[i], i
+            assert np.isfinite(got[i]).all()
+            assert np.array_equal(got[i], us[i].cpu().numpy()), (i, tout)
+        if n == 0:
+            b.tune(u, dts, probe_steps=2)
+    assert list(b.steps_done) == [s.nsteps for s in singles]
