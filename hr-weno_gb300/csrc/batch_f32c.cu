@@ -28,13 +28,14 @@ __device__ __forceinline__ void split_scalar(double x, float& hi, float& lo) {
   lo = __double2float_rn(x - (double)hi);
 }
 
-template <int K, int G, int C, int FK, bool NU>
+// MS: an mstvd batch's sweep (the pass also takes the right-hand side and multistep stages)
+template <int K, int G, int C, int FK, bool NU, bool MS = false>
 __device__ __forceinline__ void f32c_sweep(const F32CArgs& a, int lt, int gid, int stage) {
   const int lane = lt & 31;
   const int warp_in_group = lt >> 5;
   for (int64_t base = 0; base < a.L.nc; base += (int64_t)G * C) {
     const int64_t wbase = base + (int64_t)warp_in_group * 32 * C;
-    if (wbase < a.L.nc) f32c_pass<K, -1, C, FK, NU>(a, wbase + (int64_t)lane * C, lane, stage);
+    if (wbase < a.L.nc) f32c_pass<K, -1, C, FK, NU, MS>(a, wbase + (int64_t)lane * C, lane, stage);
   }
   group_sync<G>(gid);
 }
@@ -151,7 +152,7 @@ __device__ void run_problem_f32c_ms(const BatchArgs& B, const BatchProblem& P, i
           a.hi_out = H[m + 1], a.lo_out = Lo[m + 1];
         }
         group_sync<G>(gid);
-        f32c_sweep<K, G, C, FK, NU>(a, lt, gid, st);
+        f32c_sweep<K, G, C, FK, NU, true>(a, lt, gid, st);
       }
     }
     level = 4;
@@ -165,14 +166,16 @@ __device__ void run_problem_f32c_ms(const BatchArgs& B, const BatchProblem& P, i
       a.hi4 = H[c1], a.lo4 = Lo[c1], a.l4 = lm, a.lout = lm;
     }
     group_sync<G>(gid);
-    f32c_sweep<K, G, C, FK, NU>(a, lt, gid, FC_MS);
+    f32c_sweep<K, G, C, FK, NU, true>(a, lt, gid, FC_MS);
   }
   cur = (int)(level % 5);
   for (int64_t j = lt; j < P.nc; j += G) u[j] = (double)H[cur][j] + (double)Lo[cur][j];
   group_sync<G>(gid);
 }
 
-template <int G, int C, bool NU = false>
+// MS: the kernel of mstvd batches (a kernel of its own, so that the rktvd batches' pass
+// carries no multistep code)
+template <int G, int C, bool NU = false, bool MS = false>
 __global__ void __launch_bounds__(NT, C == 4 ? 3 : 2) batch_f32c_kernel(BatchArgs B) {
   static_assert(NT % G == 0 && G % 32 == 0 && NT / G <= 15, "groups of whole warps");
   constexpr int GPB = NT / G;
@@ -186,16 +189,14 @@ __global__ void __launch_bounds__(NT, C == 4 ? 3 : 2) batch_f32c_kernel(BatchArg
     group_sync<G>(gid);
     if (pid >= B.nprob) break;
     const BatchProblem P = B.probs[B.order_idx[pid]];
-    if (P.nsteps <= 0 && !(B.method == 1 && P.start)) continue;
-    // one copy of the pass per (k, numerical flux); Burgers or linear is a uniform branch, and
-    // so is rktvd or mstvd
+    if (P.nsteps <= 0 && !(MS && P.start)) continue;
+    // one copy of the pass per (k, numerical flux); Burgers or linear is a uniform branch
     const bool god = P.flux != HRW_FLUX_LAX_FRIEDRICHS;
-    const bool ms = B.method == 1;
     F32CArgs& a = s_args[gid];
-#define HRW_RUN(K_, FK_, NU_)                                              \
-  do {                                                                     \
-    if (ms) run_problem_f32c_ms<K_, G, C, FK_, NU_>(B, P, lt, gid, a);     \
-    else run_problem_f32c<K_, G, C, FK_, NU_>(B, P, lt, gid, a);           \
+#define HRW_RUN(K_, FK_, NU_)                                                        \
+  do {                                                                               \
+    if constexpr (MS) run_problem_f32c_ms<K_, G, C, FK_, NU_>(B, P, lt, gid, a);     \
+    else run_problem_f32c<K_, G, C, FK_, NU_>(B, P, lt, gid, a);                     \
   } while (0)
     if constexpr (NU) {  // one copy of the general pass per k
       if (P.k == 3) HRW_RUN(3, -1, true);
@@ -214,46 +215,48 @@ __global__ void __launch_bounds__(NT, C == 4 ? 3 : 2) batch_f32c_kernel(BatchArg
   }
 }
 
-template <int G, int C>
-int occupancy_f32() {
+template <int G, int C, bool NU = false>
+int occupancy_f32(bool ms) {
   int n = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_f32c_kernel<G, C>, NT, 0);
+  if (ms) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_f32c_kernel<G, C, NU, true>, NT, 0);
+  else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_f32c_kernel<G, C, NU, false>, NT, 0);
   return n;
+}
+
+template <int G, int C, bool NU = false>
+cudaError_t launch_f32(const BatchArgs& B, int blocks, cudaStream_t s) {
+  if (B.method == 1) batch_f32c_kernel<G, C, NU, true><<<blocks, NT, 0, s>>>(B);
+  else batch_f32c_kernel<G, C, NU, false><<<blocks, NT, 0, s>>>(B);
+  return cudaGetLastError();
 }
 
 }  // namespace
 
 const BatchShape kBatchShapesF32[kNumBatchShapesF32] = {{64, 4}, {128, 4}, {256, 4}};
 
-int batch_f32_blocks_per_sm(int shape) {
+int batch_f32_blocks_per_sm(int shape, bool ms) {
   switch (shape) {
-    case 0: return occupancy_f32<64, 4>();
-    case 1: return occupancy_f32<128, 4>();
-    default: return occupancy_f32<256, 4>();
+    case 0: return occupancy_f32<64, 4>(ms);
+    case 1: return occupancy_f32<128, 4>(ms);
+    default: return occupancy_f32<256, 4>(ms);
   }
 }
 
-int batch_f32c_nu_blocks_per_sm() {
-  int n = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_f32c_kernel<kBatchNuGroup, 4, true>, NT, 0);
-  return n;
-}
+int batch_f32c_nu_blocks_per_sm(bool ms) { return occupancy_f32<kBatchNuGroup, 4, true>(ms); }
 
 cudaError_t launch_batch_f32c_nu(const BatchArgs& B, int blocks, cudaStream_t s) {
   if (B.nprob <= 0) return cudaSuccess;
-  batch_f32c_kernel<kBatchNuGroup, 4, true><<<blocks, NT, 0, s>>>(B);
-  return cudaGetLastError();
+  return launch_f32<kBatchNuGroup, 4, true>(B, blocks, s);
 }
 
 cudaError_t launch_batch_f32c(const BatchArgs& B, int shape, int blocks, cudaStream_t s) {
   if (B.nprob <= 0) return cudaSuccess;
   switch (shape) {
-    case 0: batch_f32c_kernel<64, 4><<<blocks, NT, 0, s>>>(B); break;
-    case 1: batch_f32c_kernel<128, 4><<<blocks, NT, 0, s>>>(B); break;
-    case 2: batch_f32c_kernel<256, 4><<<blocks, NT, 0, s>>>(B); break;
-    default: return cudaErrorInvalidValue;
+    case 0: return launch_f32<64, 4>(B, blocks, s);
+    case 1: return launch_f32<128, 4>(B, blocks, s);
+    case 2: return launch_f32<256, 4>(B, blocks, s);
   }
-  return cudaGetLastError();
+  return cudaErrorInvalidValue;
 }
 
 }  // namespace hrw

@@ -142,8 +142,9 @@ int launch_all(hrw_batch* b, double* u, const int* shapes) {
         }
       }
       const bool nu = c == kClasses;
-      const int per_sm = std::max(1, nu    ? (f32 ? batch_f32c_nu_blocks_per_sm() : batch_nu_blocks_per_sm(b->strict))
-                                     : f32 ? batch_f32_blocks_per_sm(shapes[c])
+      const bool ms = A.method == 1;
+      const int per_sm = std::max(1, nu    ? (f32 ? batch_f32c_nu_blocks_per_sm(ms) : batch_nu_blocks_per_sm(b->strict))
+                                     : f32 ? batch_f32_blocks_per_sm(shapes[c], ms)
                                            : batch_blocks_per_sm(shapes[c], b->strict));
       const int group = nu ? kBatchNuGroup : f32 ? kBatchShapesF32[shapes[c]].group : kBatchShapes[shapes[c]].group;
       const int groups_per_block = 256 / group;

@@ -74,10 +74,10 @@ cudaError_t launch_batch_nu(const BatchArgs& B, bool strict, int blocks, cudaStr
 // compensated FP32 batches: their own shapes (cells per thread a multiple of 4)
 constexpr int kNumBatchShapesF32 = 3;
 extern const BatchShape kBatchShapesF32[kNumBatchShapesF32];
-int batch_f32_blocks_per_sm(int shape);
+int batch_f32_blocks_per_sm(int shape, bool ms);  // ms: the mstvd batches' kernel
 cudaError_t launch_batch_f32c(const BatchArgs& B, int shape, int blocks, cudaStream_t s);
 // their non-uniform lines: one launch of 128-thread groups, 4 cells per thread
-int batch_f32c_nu_blocks_per_sm();
+int batch_f32c_nu_blocks_per_sm(bool ms);
 cudaError_t launch_batch_f32c_nu(const BatchArgs& B, int blocks, cudaStream_t s);
 
 }  // namespace hrw

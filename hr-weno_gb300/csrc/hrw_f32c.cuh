@@ -435,7 +435,9 @@ __device__ __forceinline__ void store_cells(float* __restrict__ p, int j0, int n
 // FC_RK1 .. FC_RK3C; one copy of the pass then serves every stage of a step (the batched
 // kernel runs all stages of a problem in one launch, and per-stage copies would not fit the
 // instruction cache).  The per-stage arithmetic is the same as with ST fixed.
-template <int K, int ST, int C, int FK = -1, bool NU = false>
+// MSR (run-time stage kind only): the run-time path also takes FC_RHS and FC_MS (an mstvd
+// batch); without it the code of those two stages stays out of the pass
+template <int K, int ST, int C, int FK = -1, bool NU = false, bool MSR = false>
 __device__ __forceinline__ void f32c_pass(const F32CArgs& a, int64_t j0l, int lane, int st_rt = ST) {
   static_assert(!NU || FK < 0, "non-uniform lines take the general flux path");
   static_assert(ST != FC_MS || ST >= 0, "");
@@ -579,8 +581,8 @@ __device__ __forceinline__ void f32c_pass(const F32CArgs& a, int64_t j0l, int la
       }
     } else {
       float r;  // the same expressions as the fixed-stage branches above
-      if (st == FC_RHS) r = lq[c];
-      else if (st == FC_E1 || st == FC_RK1 || st == FC_MS) r = dtL;  // FC_MS: completed below
+      if (MSR && st == FC_RHS) r = lq[c];
+      else if (st == FC_E1 || st == FC_RK1 || (MSR && st == FC_MS)) r = dtL;  // FC_MS: completed below
       else if (st == FC_RK3B) r = 0.25f * (dv[c] + dtL);
       else if (st == FC_RK2B) r = 0.5f * (dv[c] + dtL);
       else r = (2.f / 3.f) * (dv[c] + dtL);  // FC_RK3C
@@ -596,7 +598,7 @@ __device__ __forceinline__ void f32c_pass(const F32CArgs& a, int64_t j0l, int la
   if (to_out) {
     store_cells<C>(a.out, j0, nc, o1);
   } else {
-    if (ST == FC_MS || (ST < 0 && st == FC_MS)) {  // u' = u + (7 (u4 - u) + 50 dt L + 10 dt L4) / 32
+    if (ST == FC_MS || (MSR && ST < 0 && st == FC_MS)) {  // u' = u + (7 (u4 - u) + 50 dt L + 10 dt L4) / 32
       float h4[C], l4[C], L4[C];
       load_cells<C>(a.hi4, j0, nc, h4);
       load_cells<C>(a.lo4, j0, nc, l4);
