@@ -123,18 +123,25 @@ __device__ __forceinline__ void recon_diff(const float* d, float eps, float& rl,
   }
 }
 
-// K = 3 reconstruction of one cell with the 13/12 (second difference)^2 terms of its three
-// indicators precomputed (neighbouring cells share them): t0, t1, t2 for beta0, beta1, beta2.
-// Same weights and candidates as recon_diff<3>.  WL = false computes rr only (rl untouched),
+// eps + 13/12 D^2 for the second difference D = d_m - d_{m-1} at one window position
+__device__ __forceinline__ float shared_t(float dm1, float dm, float eps) {
+  const float D = dm - dm1;
+  return fmaf((13.f / 12.f) * D, D, eps);
+}
+
+// K = 3 reconstruction of one cell with eps + 13/12 (second difference)^2 of its three
+// indicators precomputed (neighbouring cells share them; shared_t below): t0, t1, t2 for
+// beta0, beta1, beta2.  Same weights and candidates as recon_diff<3>, eps added once per
+// window position instead of once per indicator.  WL = false computes rr only (rl untouched),
 // with the same operations for rr: an upwind flux needs the left state of each interface alone.
 template <bool WL = true>
 __device__ __forceinline__ void recon_diff3_shared(const float* d, float t0, float t1, float t2,
-                                                   float eps, float& rl, float& rr) {
+                                                   float& rl, float& rr) {
   const float dmm = d[0], dm = d[1], d0 = d[2], d1 = d[3];
   const float B0 = fmaf(-3.f, d0, d1), B1 = dm + d0, B2 = fmaf(3.f, dm, -dmm);
-  const float e0 = eps + fmaf(0.25f * B0, B0, t0);
-  const float e1 = eps + fmaf(0.25f * B1, B1, t1);
-  const float e2 = eps + fmaf(0.25f * B2, B2, t2);
+  const float e0 = fmaf(0.25f * B0, B0, t0);  // eps + beta0
+  const float e1 = fmaf(0.25f * B1, B1, t1);
+  const float e2 = fmaf(0.25f * B2, B2, t2);
   const float s0 = e0 * e0, s1 = e1 * e1, s2 = e2 * e2;
   const float R0 = fmaf(4.f, d0, -d1), R1 = fmaf(2.f, d0, dm), R2 = fmaf(5.f, dm, -2.f * dmm);
   const float L0 = fmaf(2.f, d1, -5.f * d0), L1 = -fmaf(2.f, dm, d0), L2 = fmaf(-4.f, dm, dmm);
@@ -496,17 +503,16 @@ __device__ __forceinline__ void f32c_pass(const F32CArgs& a, int64_t j0l, int la
       recon_diff_nu<K>(&d[c + 1], L.cnu + (int64_t)NCF * jc, a.eps, rl[c], rr[c]);
     }
   } else if constexpr (K == 3) {
-    // 13/12 (d_m - d_{m-1})^2 once per window position.  Cell c reads d[c+1 .. c+4]
+    // eps + 13/12 (d_m - d_{m-1})^2 once per window position.  Cell c reads d[c+1 .. c+4]
     // (d_{j-2} .. d_{j+1}): its beta0, beta1, beta2 take t[c+4], t[c+3], t[c+2]
     float t[C + 4];
 #pragma unroll
     for (int m = 2; m < C + 4; ++m) {
-      const float D = d[m] - d[m - 1];
-      t[m] = (13.f / 12.f) * D * D;
+      t[m] = shared_t(d[m - 1], d[m], a.eps);
     }
 #pragma unroll
     for (int c = 0; c < C; ++c)
-      recon_diff3_shared(&d[c + 1], t[c + 4], t[c + 3], t[c + 2], a.eps, rl[c], rr[c]);
+      recon_diff3_shared(&d[c + 1], t[c + 4], t[c + 3], t[c + 2], rl[c], rr[c]);
   } else {
 #pragma unroll
     for (int c = 0; c < C; ++c) recon_diff<K>(&d[c + 1], a.eps, rl[c], rr[c]);
@@ -524,11 +530,8 @@ __device__ __forceinline__ void f32c_pass(const F32CArgs& a, int64_t j0l, int la
   } else if constexpr (K == 3) {
     float te[3];
 #pragma unroll
-    for (int q = 0; q < 3; ++q) {
-      const float D = ed[q + 1] - ed[q];
-      te[q] = (13.f / 12.f) * D * D;
-    }
-    recon_diff3_shared(ed, te[2], te[1], te[0], a.eps, el, er);
+    for (int q = 0; q < 3; ++q) te[q] = shared_t(ed[q], ed[q + 1], a.eps);
+    recon_diff3_shared(ed, te[2], te[1], te[0], el, er);
   } else {
     recon_diff<K>(ed, a.eps, el, er);
   }

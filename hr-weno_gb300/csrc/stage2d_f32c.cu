@@ -58,7 +58,7 @@ constexpr int kTileWaitPolls = 1 << 20;
 __device__ int g_tile_wait_limit = kTileWaitPolls;
 
 // WENO offsets of the C cells of a segment from its differences d[0 .. C+2K-2]; for k = 3 the
-// 13/12 (second difference)^2 terms are computed once per window position (as the 1D pass).
+// eps + 13/12 (second difference)^2 terms are computed once per window position (as the 1D pass).
 // WL = false (upwind, k = 3): rr only.  NU: on a non-uniform line (L.cnu) each cell j0 + c
 // takes its own coefficients (recon_diff_nu); a uniform line of the same grid the tables.
 template <int K, bool WL = true, bool NU = false>
@@ -77,13 +77,10 @@ __device__ __forceinline__ void segment_recon(const float* d, float eps, float* 
   if constexpr (K == 3) {
     float t[C + 4];
 #pragma unroll
-    for (int m = 2; m < C + 4; ++m) {
-      const float D = d[m] - d[m - 1];
-      t[m] = (13.f / 12.f) * D * D;
-    }
+    for (int m = 2; m < C + 4; ++m) t[m] = shared_t(d[m - 1], d[m], eps);
 #pragma unroll
     for (int c = 0; c < C; ++c)
-      recon_diff3_shared<WL>(&d[c + 1], t[c + 4], t[c + 3], t[c + 2], eps, rl[c], rr[c]);
+      recon_diff3_shared<WL>(&d[c + 1], t[c + 4], t[c + 3], t[c + 2], rl[c], rr[c]);
   } else {
 #pragma unroll
     for (int c = 0; c < C; ++c) recon_diff<K>(&d[c + 1], eps, rl[c], rr[c]);
@@ -105,11 +102,8 @@ __device__ __forceinline__ void cell_recon(const float* de, float eps, float& el
   if constexpr (K == 3) {
     float te[3];
 #pragma unroll
-    for (int q = 0; q < 3; ++q) {
-      const float D = de[q + 1] - de[q];
-      te[q] = (13.f / 12.f) * D * D;
-    }
-    recon_diff3_shared<WL>(de, te[2], te[1], te[0], eps, el, er);
+    for (int q = 0; q < 3; ++q) te[q] = shared_t(de[q], de[q + 1], eps);
+    recon_diff3_shared<WL>(de, te[2], te[1], te[0], el, er);
   } else {
     recon_diff<K>(de, eps, el, er);
   }
