@@ -275,7 +275,7 @@ __device__ __forceinline__ void recon_fast(const double* w, double eps, double* 
         const double P0 = s1 * s2, P1 = s0 * s2, P2 = s0 * s1;
         const double Q1 = 6.0 * P1, T0 = 3.0 * P0, T2 = 3.0 * P2;
         // the sums as explicit fused multiply-adds: no rounding left to the compiler's choice
-        // of contraction, so that recon_fast3_side reproduces them exactly
+        // of contraction, so that every kernel that inlines this gets the same bits
         const double den = fma(3.0, P0, fma(6.0, P1, P2));   // d = (3, 6, 1)/10
         const double dent = fma(3.0, P2, fma(6.0, P1, P0));  // d mirrored = (1, 6, 3)/10
         const double num = fma(T0, V0, fma(Q1, V1, P2 * V2));
@@ -300,57 +300,6 @@ __device__ __forceinline__ void recon_fast(const double* w, double eps, double* 
       V1p = V1;
     }
   }
-}
-
-// One FAST k = 3 cell's vr (RIGHT) or vl alone, with recon_fast<3, 1>'s operations: the shared
-// indicators, both denominators and the common reciprocal R = 1 / ((6 den) dent), and only that
-// side's candidates and numerator.  Two threads (the cluster kernel's vr and vl warps, on
-// different sub-partitions) then give recon_fast's bits between them, each with about 11 FP64
-// instructions fewer.  w[0 .. 6]: recon_fast's window for C = 1 (cell at w[3]).
-template <bool RIGHT>
-__device__ __forceinline__ double recon_fast3_side(const double* w, double eps) {
-  double A[3], Dm[3], Hm[3];
-  const double c13 = 13.0 / 12;
-#pragma unroll
-  for (int m = 0; m < 3; ++m) {  // centre q = m + 2 (cells -1 .. 1)
-    const int q = m + 2;
-    const double D = fma(-2.0, w[q], w[q - 1] + w[q + 1]);
-    Dm[m] = D;
-    A[m] = fma(c13 * D, D, eps);
-    Hm[m] = 0.5 * (w[q - 1] - w[q + 1]);
-  }
-  constexpr int q = 3;
-  const double E0 = Dm[2] + Hm[2];
-  const double E1 = Hm[1];
-  const double E2 = Dm[0] - Hm[0];
-  const double e0 = fma(E0, E0, A[2]);
-  const double e1 = fma(E1, E1, A[1]);
-  const double e2 = fma(E2, E2, A[0]);
-  const double s0 = e0 * e0, s1 = e1 * e1, s2 = e2 * e2;
-  if (max(max(hiword(s0), hiword(s1)), hiword(s2)) < FastGuard<3>::hi_max) {
-    const double P0 = s1 * s2, P1 = s0 * s2, P2 = s0 * s1;
-    const double Q1 = 6.0 * P1;
-    const double den = fma(3.0, P0, fma(6.0, P1, P2));
-    const double dent = fma(3.0, P2, fma(6.0, P1, P0));
-    const double R = rcp_fast((6.0 * den) * dent);
-    if constexpr (RIGHT) {
-      const double T0 = 3.0 * P0;
-      const double V0 = fma(5.0, w[q + 1], fma(2.0, w[q], -w[q + 2]));
-      const double V1 = fma(5.0, w[q], fma(2.0, w[q + 1], -w[q - 1]));
-      const double V2 = fma(11.0, w[q], fma(-7.0, w[q - 1], 2.0 * w[q - 2]));
-      const double num = fma(T0, V0, fma(Q1, V1, P2 * V2));
-      return num * (dent * R);
-    } else {
-      const double T2 = 3.0 * P2;
-      const double W0 = fma(11.0, w[q], fma(-7.0, w[q + 1], 2.0 * w[q + 2]));
-      const double W1 = fma(5.0, w[3], fma(2.0, w[2], -w[4]));  // V0 of cell -1
-      const double W2 = fma(5.0, w[2], fma(2.0, w[3], -w[1]));  // V1 of cell -1
-      const double numt = fma(T2, W2, fma(Q1, W1, P0 * W0));
-      return numt * (den * R);
-    }
-  }
-  const double2 g = recon_guarded<3>(w[1], w[2], w[3], w[4], w[5], eps);
-  return RIGHT ? g.y : g.x;
 }
 
 // single cell, no neighbour sharing (block-edge cells).  Reads p[o * stride] for

@@ -41,37 +41,16 @@ namespace cg = cooperative_groups;
 
 constexpr int kMaxCluster = 16;
 
-// The split shape: k = 3 FAST with one cell warp per CTA.  Four warps, one per sub-partition's
-// FP64 unit, each take one side of the product form (recon_fast3_side: the same bits as
-// recon_fast): warp 0 the cells' vr, warp 1 the vr of cell s - 1, warp 2 the cells' vl, warp 3
-// the vl of cell s + NT.  A stage's critical warp then runs about 11 FP64 instructions fewer.
-// With more cell warps the extra warps would share sub-partitions.
-template <int K, bool STRICT, int NT>
-constexpr bool split_shape() { return K == 3 && !STRICT && NT == 32; }
-template <int K, bool STRICT, int NT>
-constexpr int cluster_threads() { return NT + 32 + (split_shape<K, STRICT, NT>() ? NT + 32 : 0); }
-
-// recon_fast3_side of the cell at p (p[-2] .. p[2] valid; the window's outer slots, which one
-// cell does not use, repeat the nearest value, as recon_fast_one)
-template <bool RIGHT>
-__device__ __forceinline__ double side_at(const double* p, double eps) {
-  double w[7];
-#pragma unroll
-  for (int q = 0; q < 7; ++q) w[q] = p[q < 1 ? -2 : (q > 5 ? 2 : q - 3)];
-  return recon_fast3_side<RIGHT>(w, eps);
-}
-
 // One stage of the CTA's own cells: out = stage(in), stencil input `in` (halo-extended, in[0]
 // is cell s - K), `u` the state u^n (own cells at u[K ..]).  Threads 0 .. NT-1 take one cell
-// each; lanes 0 and 1 of the warp after them reconstruct cells s - 1 and s + NT (in the split
-// shape the warp after that takes the cells' vl).  The last CTA of the line also fills its
-// ghost cells (positions K + owned .. NT + 2K - 1 replicate cell nc - 1) before the barrier,
-// since its neighbour reads some of them when the last CTA owns fewer than K cells.
+// each; lanes 0 and 1 of the warp after them reconstruct cells s - 1 and s + NT.  The last CTA
+// of the line also fills its ghost cells (positions K + owned .. NT + 2K - 1 replicate cell
+// nc - 1) before the barrier, since its neighbour reads some of them when the last CTA owns
+// fewer than K cells.
 template <int K, int ST, bool STRICT, int NT>
 __device__ __forceinline__ void cluster_stage(const StageArgs& a, const double* in, const double* u,
                                               double* out, double* sL, double* sR, int64_t s,
                                               int owned, bool last) {
-  constexpr bool SPLIT = split_shape<K, STRICT, NT>();
   const LineArgs& L = a.L;
   const int tid = threadIdx.x;
   double vl[1], vr[1];
@@ -79,26 +58,10 @@ __device__ __forceinline__ void cluster_stage(const StageArgs& a, const double* 
     double w[1 + 2 * K];
 #pragma unroll
     for (int q = 0; q < 1 + 2 * K; ++q) w[q] = in[tid + q];  // v(s + tid - K + q)
-    if constexpr (SPLIT) {
-      vr[0] = recon_fast3_side<true>(w, a.eps);
-    } else {
-      if constexpr (STRICT) recon_strict<K>(&w[K], a.eps, vl[0], vr[0]);
-      else recon_fast<K, 1>(w, a.eps, vl, vr);
-      sL[tid] = vl[0];
-    }
+    if constexpr (STRICT) recon_strict<K>(&w[K], a.eps, vl[0], vr[0]);
+    else recon_fast<K, 1>(w, a.eps, vl, vr);
+    sL[tid] = vl[0];
     sR[tid + 1] = vr[0];
-  } else if constexpr (SPLIT) {
-    if (tid == NT) {  // vr of cell s - 1
-      sR[0] = side_at<true>(in + K - 1, a.eps);
-    } else if (tid >= NT + 32 && tid < 2 * NT + 32) {  // the cells' vl
-      const int c = tid - NT - 32;
-      double w[1 + 2 * K];
-#pragma unroll
-      for (int q = 0; q < 1 + 2 * K; ++q) w[q] = in[c + q];
-      sL[c] = recon_fast3_side<false>(w, a.eps);
-    } else if (tid == 2 * NT + 32) {  // vl of cell s + NT
-      sL[NT] = side_at<false>(in + K + NT, a.eps);
-    }
   } else if (tid < NT + 2) {  // cells s - 1 (vr) and s + NT (vl)
     const int which = tid - NT;
     const double* p = in + (which == 0 ? K - 1 : K + NT);
@@ -109,9 +72,9 @@ __device__ __forceinline__ void cluster_stage(const StageArgs& a, const double* 
     else sL[NT] = el;
   }
   __syncthreads();
-  if (tid >= owned) return;  // also every thread of the edge (and vl) warps (owned <= NT)
+  if (tid >= owned) return;  // also every thread of the edge warp (owned <= NT)
   const int64_t j = s + tid;
-  const double FL = numflux<STRICT>(L, sR[tid], SPLIT ? sL[tid] : vl[0], j);
+  const double FL = numflux<STRICT>(L, sR[tid], vl[0], j);
   const double FR = numflux<STRICT>(L, vr[0], sL[tid + 1], j + 1);
   const double dF = flux_diff<STRICT>(L, j, FL, FR, vr[0]);
   // the combines index the CTA's buffers by the local cell (uniform line: no per-cell widths)
@@ -142,8 +105,7 @@ __device__ __forceinline__ void fill_halo(cg::cluster_group& cl, double* buf, in
 }
 
 template <int K, bool STRICT, int ORDER, int NT>
-__global__ void __launch_bounds__(cluster_threads<K, STRICT, NT>())
-    rk_cluster_kernel(StageArgs a, double* u_io, int64_t nsteps) {
+__global__ void __launch_bounds__(NT + 32) rk_cluster_kernel(StageArgs a, double* u_io, int64_t nsteps) {
   static_assert(NT >= 2 * K && NT % 32 == 0, "the halo lanes and whole cell warps");
   __shared__ double U[NT + 2 * K], A[NT + 2 * K], B[NT + 2 * K];
   __shared__ double sL[NT + 1], sR[NT + 1];
@@ -154,8 +116,7 @@ __global__ void __launch_bounds__(cluster_threads<K, STRICT, NT>())
   const int owned = (int)(nc - s < NT ? nc - s : NT);
   const int tid = threadIdx.x;
   // own cells; the last CTA also its ghosts (cell nc - 1 repeated)
-  constexpr int NB = cluster_threads<K, STRICT, NT>();
-  for (int q = tid; q < (last ? NT + K : NT); q += NB) U[K + q] = u_io[s + (q < owned ? q : owned - 1)];
+  for (int q = tid; q < (last ? NT + K : NT); q += NT + 32) U[K + q] = u_io[s + (q < owned ? q : owned - 1)];
   cl.sync();
   fill_halo<K, NT>(cl, U, rank, nrank);
   double* cur = U;  // order 1 alternates between U and A
@@ -184,7 +145,7 @@ __global__ void __launch_bounds__(cluster_threads<K, STRICT, NT>())
       fill_halo<K, NT>(cl, U, rank, nrank);
     }
   }
-  for (int q = tid; q < owned; q += NB) u_io[s + q] = cur[K + q];
+  for (int q = tid; q < owned; q += NT + 32) u_io[s + q] = cur[K + q];
   // no CTA leaves while a neighbour may still read its buffers
   cl.sync();
 }
@@ -199,7 +160,7 @@ cudaError_t launch_shape(const StageArgs& a, double* u, int64_t nsteps, cudaStre
   }
   cudaLaunchConfig_t cfg{};
   cfg.gridDim = dim3((unsigned)nrank);
-  cfg.blockDim = dim3(cluster_threads<K, STRICT, NT>());
+  cfg.blockDim = dim3(NT + 32);
   cfg.stream = s;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeClusterDimension;
