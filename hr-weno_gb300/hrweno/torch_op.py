@@ -2,11 +2,13 @@
 
 The forward pass runs the fused FP64 stage kernels; the backward pass is the hand-written
 discrete adjoint (hrw_adjoint_vjp), so d(loss)/du0 is the exact gradient of the discrete map
-for any loss of u(T).  Problems: FV1D, global Lax-Friedrichs at fixed alpha, rktvd order 3; a
-leading batch of equal-size lines is allowed (u0 of shape [nseg, ncells] or [ncells]).
+for any loss of u(T).  Problems: FV1D on uniform or non-uniform lines (xedges), global
+Lax-Friedrichs at fixed alpha, rktvd order 3; a leading batch of equal-size lines is allowed
+(u0 of shape [nseg, ncells] or [ncells]).
 """
 from __future__ import annotations
 
+import numpy as np
 import torch
 
 from .adjoint import adjoint
@@ -43,9 +45,10 @@ def weno_solve(u0: torch.Tensor, problem: Problem, dt: float, nsteps: int,
         raise TypeError("weno_solve needs a CUDA float64 tensor")
     nseg = 1 if u0.dim() == 1 else int(u0.shape[0])
     key = (id(problem), nseg, checkpoint_every, u0.device.index)
-    # the descriptor's bytes: a problem edited since its handle was made gets a new handle
-    # (the problems the adjoint takes hold no host arrays, so the bytes are its whole content)
-    snap = bytes(problem.to_c())
+    # the descriptor's bytes and the edges of a non-uniform line (the descriptor holds only
+    # their address): a problem edited since its handle was made gets a new handle
+    snap = bytes(problem.to_c()) + b"".join(
+        np.ascontiguousarray(e, dtype=np.float64).tobytes() for e in problem.xedges if e is not None)
     if key not in _cache or _cache[key][1] != snap:
         _cache[key] = (problem, snap, adjoint(problem, nseg=nseg, checkpoint_every=checkpoint_every))
     adj = _cache[key][2]

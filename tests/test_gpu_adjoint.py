@@ -206,6 +206,34 @@ def test_torch_autograd_op(hw):
     assert torch.equal(u0b.grad[1], g1)
 
 
+def test_torch_autograd_op_nonuniform(hw, orc):
+    """The autograd op on a non-uniform line: the forward is hrw_integrate's, the backward the
+    non-uniform adjoint; d(loss)/du0 . d matches the tangent-linear oracle."""
+    import torch
+    n, steps = 384, 50
+    xe = stretched_edges(n, 21)
+    prob = hw.Problem(kind="fv1d", ncells=(n, 1), k=3, eps=1e-6, flux="lax_friedrichs",
+                      fn=("burgers", "burgers"), alpha=(1.5, 1.5), bc=("copy", "copy"), xedges=(xe, None))
+    dt = 0.4 * np.min(np.diff(xe)) / 1.5
+    u0n, tgn = line(n, 9), line(n, 10) * 0.9
+    u0 = torch.from_numpy(u0n).cuda().requires_grad_(True)
+    tg = torch.from_numpy(tgn).cuda()
+    uT = hw.weno_solve(u0, prob, dt, steps)
+    ui = u0n.copy()
+    hw.rktvd(prob, n, 3).integrate(ui, 0.0, (steps - 0.5) * dt, dt)
+    assert np.array_equal(uT.detach().cpu().numpy(), ui)
+    (0.5 * ((uT - tg) ** 2).sum()).backward()
+    d = smooth_direction(n, 4)
+    _, dJ = orc.tl_misfit(prob, u0n, d, tgn, dt, steps)
+    assert abs(float(u0.grad.cpu().numpy() @ d) - dJ) <= 1e-10 * abs(dJ)
+    # edges edited in place (same array, same address): the op builds a new handle
+    xe[1:-1] = 0.5 * (xe[1:-1] + np.linspace(-5.0, 5.0, n + 1)[1:-1])
+    uT2 = hw.weno_solve(u0.detach(), prob, dt, steps)
+    ui = u0n.copy()
+    hw.rktvd(prob, n, 3).integrate(ui, 0.0, (steps - 0.5) * dt, dt)
+    assert np.array_equal(uT2.cpu().numpy(), ui)
+
+
 def test_torch_op_follows_an_edited_problem(hw):
     """weno_solve keeps one adjoint handle per problem; editing the problem between calls gives
     the edited problem's solve, not the cached handle's."""
