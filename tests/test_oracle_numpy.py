@@ -702,6 +702,107 @@ def test_difference_form_matches_the_oracle(hw, orc, k, fn, flux, bc):
             assert np.max(np.abs(got - ref)) <= 1e-13 * scale, (nc, k, fn, flux, bc)
 
 
+def offsets_nu_np(v, k, eps, cnu):
+    """(rl, rr) of every cell of a non-uniform line as the compensated kernels form them
+    (recon_diff_nu): a candidate minus v_j is sum_q c(q, r) (v_{j-r+q} - v_j) with the cell's
+    own coefficients cnu [nc, k+1, k] (cnu(q, r) at [j, r+1, q]); indicators and weights as on
+    a uniform line (float64, true divisions)."""
+    nc = v.size
+    if k == 1:
+        return np.zeros(nc), np.zeros(nc)
+    ext = np.concatenate([np.full(k - 1, v[0]), v, np.full(k - 1, v[-1])])
+    S = lambda m: ext[k - 1 + m: k - 1 + m + nc] - v  # noqa: E731  v_{j+m} - v_j
+    R, Lc = [], []
+    for r in range(k):
+        R.append(sum(cnu[:, r + 1, q] * S(q - r) for q in range(k) if q != r))
+        Lc.append(sum(cnu[:, r, q] * S(q - r) for q in range(k) if q != r))
+    d = lambda o: S(o + 1) - S(o)  # noqa: E731  d_{j+o} = v_{j+o+1} - v_{j+o}
+    if k == 2:
+        s0, s1 = (eps + d(0) ** 2) ** 2, (eps + d(-1) ** 2) ** 2
+        return ((s1 * Lc[0] + 2 * s0 * Lc[1]) / (s1 + 2 * s0),
+                (2 * s1 * R[0] + s0 * R[1]) / (2 * s1 + s0))
+    dmm, dm, d0, d1 = d(-2), d(-1), d(0), d(1)
+    e0 = eps + 13 / 12 * (d1 - d0) ** 2 + 0.25 * (d1 - 3 * d0) ** 2
+    e1 = eps + 13 / 12 * (d0 - dm) ** 2 + 0.25 * (dm + d0) ** 2
+    e2 = eps + 13 / 12 * (dm - dmm) ** 2 + 0.25 * (3 * dm - dmm) ** 2
+    s0, s1, s2 = e0 ** 2, e1 ** 2, e2 ** 2
+    P0, P1, P2 = s1 * s2, s0 * s2, s0 * s1
+    return ((P0 * Lc[0] + 6 * P1 * Lc[1] + 3 * P2 * Lc[2]) / (P0 + 6 * P1 + 3 * P2),
+            (3 * P0 * R[0] + 6 * P1 * R[1] + P2 * R[2]) / (3 * P0 + 6 * P1 + P2))
+
+
+def random_edges(nc, seed):
+    rng = np.random.default_rng(seed)
+    return np.concatenate([[-1.0], -1.0 + np.cumsum(rng.uniform(0.5, 1.5, nc)) * (3.0 / nc)])
+
+
+@pytest.mark.parametrize("k", [1, 2, 3])
+@pytest.mark.parametrize("nc", [1, 2, 5, 64, 1001])
+def test_nonuniform_offsets_match_the_oracle(orc, k, nc):
+    """The compensated kernels' non-uniform reconstruction (offsets from per-cell coefficients
+    and neighbour differences) is the reference's weno(ncells, k, eps, xedges) rearranged:
+    v + offsets agree with the oracle's vl, vr to rounding level."""
+    xe = random_edges(nc, nc + k)
+    cnu = orc.calc_cnu(nc, k, xe)
+    for v in lines(nc, 3 * nc + k):
+        vl, vr = orc.reconstruct(v, k, 1e-6, xedges=xe)
+        rl, rr = offsets_nu_np(v, k, 1e-6, cnu)
+        scale = max(np.max(np.abs(v)), 1e-300)
+        assert np.max(np.abs(v + rl - vl)) <= 1e-13 * scale and np.max(np.abs(v + rr - vr)) <= 1e-13 * scale
+
+
+@pytest.mark.parametrize("k", [1, 2, 3])
+@pytest.mark.parametrize("fn", ["burgers", "linear"])
+@pytest.mark.parametrize("flux", ["lax_friedrichs", "godunov"])
+@pytest.mark.parametrize("bc", ["copy", "zero", "zero_inflow"])
+def test_nonuniform_difference_form_matches_the_oracle(hw, orc, k, fn, flux, bc):
+    """The compensated kernels' difference form on a non-uniform line: g at the true edges, the
+    linear flux's (g_R - g_L) v as b width_j v, each cell divided by its own width; restated in
+    float64 it agrees with the oracle's right-hand side to rounding level."""
+    a, b, alpha = (0.6, 0.3, 1.6) if fn == "linear" else (0.0, 0.0, 1.3)
+    for nc in (2, 3, 9, 400):
+        xe = random_edges(nc, 7 * nc + k)
+        w = np.diff(xe)
+        cnu = orc.calc_cnu(nc, k, xe)
+        for v in lines(nc, 5 * nc + k):
+            prob = hw.Problem(kind="fv1d", ncells=(nc, 1), k=k, eps=1e-6, flux=flux, fn=(fn, fn),
+                              coef_a=(a, 0.0), coef_b=(b, 0.0), alpha=(alpha, alpha), bc=(bc, bc),
+                              xedges=(xe, None), numerics="strict")
+            ref = orc.rhs(prob, v)
+            rl, rr = offsets_nu_np(v, k, 1e-6, cnu)
+            d = np.append(np.diff(v), 0.0)
+            lin = fn == "linear"
+            g = (a + b * xe) if lin else np.zeros(nc + 1)
+
+            def G(vj, am, bp, gg):  # F(vj + am, vj + bp) - f_base(vj), as rhs_difference_form_np
+                if flux == "lax_friedrichs":
+                    if lin:
+                        return 0.5 * ((gg + alpha) * am + (gg - alpha) * bp)
+                    return 0.25 * (am * (2 * vj + am + 2 * alpha) + bp * (2 * vj + bp - 2 * alpha))
+                fa, fb = (gg * am, gg * bp) if lin else (0.5 * am * (2 * vj + am), 0.5 * bp * (2 * vj + bp))
+                return np.where(am <= bp, np.minimum(fa, fb), np.maximum(fa, fb))
+
+            rr_m = np.concatenate([[rr[0]], rr[:-1]])
+            d_m = np.concatenate([[0.0], d[:-1]])
+            rl_p = np.append(rl[1:], rl[-1])
+            GL, GR = G(v, rr_m - d_m, rl, g[:-1]), G(v, rr, d + rl_p, g[1:])
+            dF = GR - GL + (b * w * v if lin else 0.0)
+            for j in {0, nc - 1}:
+                fb = (lambda e, vv: g[e] * vv) if lin else (lambda e, vv: 0.5 * vv * vv)  # noqa: E731
+                FL, FR = fb(j, v[j]) + GL[j], fb(j + 1, v[j]) + GR[j]
+                if bc == "copy":
+                    dF[j] = 0.0
+                    continue
+                if j == 0:
+                    FL = 0.0
+                if j == nc - 1:
+                    FR = 0.0 if bc == "zero" else fb(nc, v[j] + rr[j])
+                dF[j] = FR - FL
+            got = -dF / w
+            scale = (1.0 + np.max(np.abs(v))) ** 2 / np.min(w)
+            assert np.max(np.abs(got - ref)) <= 1e-13 * scale, (nc, k, fn, flux, bc)
+
+
 def _beta_forms(k):
     """Smoothness indicators as sums of weighted squares of linear forms in v(i-2 .. i+2):
     beta_r = sum (c, coefficients) over its terms (src/hrweno_weno.f90:189-202)."""
