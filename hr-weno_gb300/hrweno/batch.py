@@ -39,7 +39,9 @@ def _setup(L):
 
 
 class batch:  # noqa: N801
-    """batch(problems, order=3): problems are FV1D Problem descriptors on uniform grids.
+    """batch(problems, order=3, dtype="f64", method="rktvd"): problems are FV1D Problem
+    descriptors on uniform grids or non-uniform ones (xedges); dtype "f64" or "f32c" (the
+    compensated FP32 form, states still packed as float64).
 
     method="mstvd" makes every problem an mstvd(fu_i, neq_i) solve (src/hrweno_tvdode.f90:180-271):
     each keeps its multistep history between calls, and its first call runs the RK3 start."""
