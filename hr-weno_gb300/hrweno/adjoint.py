@@ -39,7 +39,8 @@ def _setup(L):
 
 
 class adjoint:  # noqa: N801
-    """adjoint(problem, nseg=1, checkpoint_every=45): nseg packed problems of ncells each;
+    """adjoint(problem, nseg=1, checkpoint_every=45): nseg packed problems of ncells each, on a
+    uniform line or the problem's non-uniform one (xedges, the same edges in every segment);
     checkpoint_every=0 picks the segment length from the free device memory (the whole
     trajectory with the WENO tape when it fits, else sqrt(nsteps) segments)."""
 
