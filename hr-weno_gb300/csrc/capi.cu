@@ -645,7 +645,7 @@ static int ode_create(const hrw_problem* p, int neq, int order, int method, int 
       if (p->width[d]) nw += (size_t)(p->ncells[d] + 63) / 64 * 64;
     // a non-uniform line: 1/width, the edges, b width and k (k + 1) coefficients per cell
     for (int d = 0; d < nd; ++d)
-      if (p->xedges[d]) nw += ((size_t)p->ncells[d] + 64) / 64 * 64 * (3 + (size_t)p->k * (p->k + 1));
+      if (p->xedges[d]) nw += nu_line_f32_floats(p->ncells[d], p->k);
     const size_t nf = sn * (2 * slots + (method == 1 ? 4 : 0) + 2) + nw;
     if ((e = cudaMalloc(&o->fmem, sizeof(float) * nf)) != cudaSuccess) return cleanup(e);
     float* q = o->fmem;
@@ -682,31 +682,15 @@ static int ode_create(const hrw_problem* p, int neq, int order, int method, int 
       } else if (p->xedges[d]) {
         // the FP64 coefficients of the line (computed above on the device) and its FP64 widths,
         // rounded once to FP32; g at the edges from the rounded edges
-        const size_t nc = (size_t)L.nc, ncf = (size_t)p->k * (p->k + 1), seg = (nc + 64) / 64 * 64;
-        std::vector<double> c64(nc * ncf);
-        if ((e = cudaMemcpy(c64.data(), o->line[d].cnu, sizeof(double) * c64.size(), cudaMemcpyDeviceToHost)) !=
-            cudaSuccess)
+        NuLineF32 nl{};
+        if ((e = build_nu_line_f32(p->xedges[d], L.nc, p->k, L.b, o->line[d].cnu, q, &nl)) != cudaSuccess)
           return cleanup(e);
-        std::vector<float> rw(nc), xe(nc + 1), gst(nc), c32(c64.size());
-        for (size_t i = 0; i <= nc; ++i) xe[i] = (float)p->xedges[d][i];
-        for (size_t i = 0; i < nc; ++i) {
-          const double w = p->xedges[d][i + 1] - p->xedges[d][i];
-          rw[i] = (float)(1.0 / w);
-          gst[i] = (float)(L.b * w);
-        }
-        for (size_t i = 0; i < c64.size(); ++i) c32[i] = (float)c64[i];
-        float* dst[4] = {q, q + seg, q + 2 * seg, q + 3 * seg};
-        const std::vector<float>* src[4] = {&rw, &xe, &gst, &c32};
-        for (int m = 0; m < 4; ++m)
-          if ((e = cudaMemcpy(dst[m], src[m]->data(), sizeof(float) * src[m]->size(), cudaMemcpyHostToDevice)) !=
-              cudaSuccess)
-            return cleanup(e);
-        F.rw = dst[0];
-        F.xe = dst[1];
-        F.gst = dst[2];
-        F.cnu = dst[3];
-        if (d == 0) o->frw = q;
-        q += seg * (3 + ncf);
+        F.rw = nl.rw;
+        F.xe = nl.xe;
+        F.gst = nl.gst;
+        F.cnu = nl.cnu;
+        if (d == 0) o->frw = nl.rw;
+        q += nu_line_f32_floats(L.nc, p->k);
       }
     }
     if (nd == 2 && p->flux == HRW_FLUX_GODUNOV && !p->xedges[0] && !p->xedges[1]) {
@@ -1128,6 +1112,34 @@ static int ms_integrate(hrw_ode* o, double* du, double* t, double tout, double d
 }
 
 // ---- compensated FP32 form ---------------------------------------------------------------------
+namespace hrw {
+
+size_t nu_line_f32_floats(int nc, int k) {
+  return ((size_t)nc + 64) / 64 * 64 * (3 + (size_t)k * (k + 1));
+}
+
+cudaError_t build_nu_line_f32(const double* xedges, int nc, int k, double b, const double* cnu64,
+                              float* dst, NuLineF32* out) {
+  const size_t n = (size_t)nc, ncf = (size_t)k * (k + 1), seg = (n + 64) / 64 * 64;
+  std::vector<double> c64(n * ncf);
+  cudaError_t e = cudaMemcpy(c64.data(), cnu64, sizeof(double) * c64.size(), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return e;
+  std::vector<float> host(seg * (3 + ncf), 0.f);  // rw | xe | gst | cnu
+  for (size_t j = 0; j < n; ++j) {
+    const double w = xedges[j + 1] - xedges[j];
+    host[j] = (float)(1.0 / w);
+    host[2 * seg + j] = (float)(b * w);
+  }
+  for (size_t j = 0; j <= n; ++j) host[seg + j] = (float)xedges[j];
+  for (size_t j = 0; j < c64.size(); ++j) host[3 * seg + j] = (float)c64[j];
+  if ((e = cudaMemcpy(dst, host.data(), sizeof(float) * host.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
+    return e;
+  *out = NuLineF32{dst, dst + seg, dst + 2 * seg, dst + 3 * seg};
+  return cudaSuccess;
+}
+
+}  // namespace hrw
+
 static void split_pair(double x, float& hi, float& lo) {
   hi = (float)x;
   lo = (float)(x - (double)hi);

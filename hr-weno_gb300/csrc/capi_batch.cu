@@ -344,32 +344,21 @@ static int batch_create(const hrw_problem* probs, int nprob, int order, int dtyp
       // coefficients rounded once, 1/width and b width from the FP64 widths, the edges rounded
       size_t nf = 0;
       for (int i = 0; i < nprob; ++i)
-        if (probs[i].xedges[0]) nf += (size_t)(probs[i].ncells[0] + 64) / 64 * 64 * (3 + (size_t)probs[i].k * (probs[i].k + 1));
+        if (probs[i].xedges[0]) nf += nu_line_f32_floats(probs[i].ncells[0], probs[i].k);
       if ((e = cudaMalloc(&b->nu_fmem, sizeof(float) * nf)) != cudaSuccess) return cleanup(e);
       float* f = b->nu_fmem;
       for (int i = 0; i < nprob; ++i) {
         const hrw_problem& p = probs[i];
         if (!p.xedges[0]) continue;
         BatchProblem& bp = b->probs[i];
-        const size_t nc = (size_t)p.ncells[0], ncf = (size_t)p.k * (p.k + 1), seg = (nc + 64) / 64 * 64;
-        std::vector<double> c64(nc * ncf);
-        if ((e = cudaMemcpy(c64.data(), bp.cnu, sizeof(double) * c64.size(), cudaMemcpyDeviceToHost)) != cudaSuccess)
+        NuLineF32 nl{};
+        if ((e = build_nu_line_f32(p.xedges[0], p.ncells[0], p.k, p.coef_b[0], bp.cnu, f, &nl)) != cudaSuccess)
           return cleanup(e);
-        std::vector<float> host(seg * (3 + ncf), 0.f);
-        for (size_t j = 0; j < nc; ++j) {
-          const double w = p.xedges[0][j + 1] - p.xedges[0][j];
-          host[j] = (float)(1.0 / w);
-          host[2 * seg + j] = (float)(p.coef_b[0] * w);
-        }
-        for (size_t j = 0; j <= nc; ++j) host[seg + j] = (float)p.xedges[0][j];
-        for (size_t j = 0; j < c64.size(); ++j) host[3 * seg + j] = (float)c64[j];
-        if ((e = cudaMemcpy(f, host.data(), sizeof(float) * host.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
-          return cleanup(e);
-        bp.frw = f;
-        bp.fxe = f + seg;
-        bp.fgst = f + 2 * seg;
-        bp.fcnu = f + 3 * seg;
-        f += host.size();
+        bp.frw = nl.rw;
+        bp.fxe = nl.xe;
+        bp.fgst = nl.gst;
+        bp.fcnu = nl.cnu;
+        f += nu_line_f32_floats(p.ncells[0], p.k);
       }
     }
   }

@@ -191,6 +191,17 @@ int set_error(int code, const char* msg);
 bool positive_velocity(const LineArgs& L, double rel_margin = 1e-12);
 // 0 turns the upwind specialisation of the 2D kernels off for handles created afterwards (a
 // test hook, hrw_diag_upwind: the general flux path gives the same bits)
+// The compensated FP32 kernels' copy of a non-uniform line (LineF's rw, xe, gst, cnu): 1/width,
+// the edges and b width from the FP64 edges (host), and the FP64 weno coefficients (device,
+// k (k + 1) per cell) rounded once; one block of nu_line_f32_floats(nc, k) floats at dst, the
+// four arrays 256-byte aligned.
+struct NuLineF32 {
+  float *rw, *xe, *gst, *cnu;
+};
+size_t nu_line_f32_floats(int nc, int k);
+cudaError_t build_nu_line_f32(const double* xedges, int nc, int k, double b, const double* cnu64,
+                              float* dst, NuLineF32* out);
+
 extern std::atomic<int> g_upwind_enabled;
 
 // 1D fused stage over nc cells; k in 1..3; strict selects the reference-order numerics.
